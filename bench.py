@@ -1,0 +1,312 @@
+"""Benchmark: plain path tracing of the procedural displaced-icosphere scene.
+
+Workload (one "step"): the 1,310,720-triangle icosphere (level 8) displaced by
+5-octave value noise on a ground plane, 50 % Lambertian / 30 % GGX / 20 %
+dielectric material groups, seeded 512x256 HDR smooth-noise environment;
+the SAH BVH rebuilt on the GPU, then 1920x1080 at 16 spp, max depth 12.
+Metric: Msamples/s = 1920*1080*16 / step time.
+
+  value : device-resident inputs (mcrt_rebuild_bvh + mcrt_render, results kept on the GPU)
+  e2e   : through the C ABI with host buffers: mcrt_update_vertices (vertex upload +
+          rebuild) and mcrt_render returning the image to the host, copies inside the timer
+
+roofline : the closest-hit (extend) kernel against the bytes-per-ray memory roofline:
+           B_ray = 48 N_node + 64 N_tri + 48 bytes, N_node / N_tri = mean nodes visited and
+           triangles tested by the reference traversal of the reference BVH (oracle statistics
+           over a sample of the workload's own paths).
+cpu_baseline / --impl reference : the CPU oracle (a restatement of the reference's path:
+           its single-threaded SAH build and the path_trace.wgsl estimator on all host cores),
+           on a bounded row sample of the frame, extrapolated to one frame.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Under torchrun each rank renders an independent replica (the path does not
+shard: "replicas only"); value = all ranks' samples / max step time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W, H, SPP, DEPTH, LEVEL, SEED = 1920, 1080, 16, 12, 8, 1234
+WORKLOAD = "displaced_icosphere_l8_1.31Mtri_1920x1080_16spp_depth12_gpu_rebuild"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="mcrt", choices=["mcrt", "reference"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init(n):
+    rank, world, local = int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), \
+        int(os.environ.get("LOCAL_RANK", 0))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return rank, world, local
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def make_scene():
+    from mcrt_gb300 import scenes
+    return scenes.displaced_icosphere(seed=SEED, level=LEVEL, width=W, height=H)
+
+
+def camera(sc):
+    import mcrt_gb300 as M
+    c = sc["camera"]
+    return M.compute_camera(W, H, c["look_from"], c["look_at"], c["vfov"], c["aperture"])
+
+
+# ------------------------------------------------------------------ CPU oracle (baseline / reference arm)
+def cpu_frame_estimate(sc, cam, rows_total=32, threads=0, stats=False):
+    """Reference SAH build (single thread, as the reference runs it) + the path_trace.wgsl
+    estimator on `rows_total` image rows spread over the frame (all host cores); returns
+    the extrapolated seconds per frame and the sample description."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    t0 = time.perf_counter()
+    osc = O.OracleScene(materials=sc["materials"], vertices=sc["vertices"], triangles=sc["triangles"], env=sc["env"])
+    t_build = time.perf_counter() - t0
+    n_rects = 8
+    rows = max(1, rows_total // n_rects)
+    t_render, st = 0.0, dict(rays=0, nodes=0, prims=0)
+    for k in range(n_rects):
+        y0 = int((k + 0.5) * H / n_rects) - rows // 2
+        t1 = time.perf_counter()
+        r = osc.render(cam, W, H, SPP, 0, DEPTH, threads=threads, rect=(0, y0, W, rows), stats=stats)
+        t_render += time.perf_counter() - t1
+        if stats:
+            for key in st:
+                st[key] += r["stats"][key]
+    sampled_rows = rows * n_rects
+    t_frame = t_build + t_render * (H / sampled_rows)
+    sample = (f"reference SAH build of all {len(sc['triangles'])} triangles (1 thread, {t_build:.2f} s) + "
+              f"{sampled_rows} of {H} rows x {W} px x {SPP} spp (depth {DEPTH}, {t_render:.2f} s), "
+              f"render time scaled by {H / sampled_rows:.1f} to one frame")
+    return t_frame, sample, st, osc
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", 0))
+    if rank != 0:
+        return
+    sc = make_scene()
+    cam = camera(sc)
+    cores = os.cpu_count() or 1
+    times = []
+    sample = ""
+    for i in range(args.warmup + args.steps):
+        t_frame, sample, _, _ = cpu_frame_estimate(sc, cam, rows_total=16, threads=cores)
+        if i >= args.warmup:
+            times.append(t_frame)
+    t = sum(times) / len(times)
+    value = W * H * SPP / t / 1e6
+    print(json.dumps({
+        "impl": "reference", "metric": "Msamples/s", "value": round(value, 4), "unit": "Msamples/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1000, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": SPP, "max_depth": DEPTH,
+                   "triangles": int(len(sc["triangles"])), "seed": SEED},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Msamples/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 4), "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_mcrt(args):
+    import torch
+    import mcrt_gb300 as M
+    rank, world, local = dist_init(args.gpus)
+    torch.cuda.set_device(local)
+    stream = torch.cuda.Stream()          # a dedicated stream shared by torch events and the library
+    torch.cuda.set_stream(stream)
+    sc = make_scene()
+    cam = camera(sc)
+    ctx = M.Context(local, stream=stream.cuda_stream)
+    ctx.upload_scene(vertices=sc["vertices"], triangles=sc["triangles"], materials=sc["materials"], env=sc["env"])
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # > 129 MB L2
+
+    def step_device(i):
+        ctx.rebuild_bvh()
+        ctx.render(cam, W, H, SPP, first_frame=i * SPP, max_depth=DEPTH, outputs=())
+
+    def step_e2e(i):
+        ctx.update_vertices(sc["vertices"])
+        ctx.render(cam, W, H, SPP, first_frame=i * SPP, max_depth=DEPTH, outputs=("rgba",))
+
+    def timed(fn, n_warm, n_steps, sampler=None):
+        for i in range(n_warm):
+            fn(i)
+        torch.cuda.synchronize()
+        ms, extend = [], []
+        launches = 0
+        for i in range(n_steps):
+            flush.fill_(float(i))                         # evict the scene and path state from L2
+            barrier(world)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn(n_warm + i)
+            b.record(stream)
+            b.synchronize()
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+            t = ctx.timings()
+            extend.append((t["extend_ms"], t["extend_launches"], t["rays"]))
+            launches += t["render_launches"] + t["build_launches"]
+        return ms, extend, launches
+
+    with ClockSampler(local) as clk:
+        ms, ext, launches = timed(step_device, args.warmup, args.steps)
+    e2e_ms, _, _ = timed(step_e2e, args.warmup, args.steps)
+    step_ms = max_over_ranks(sum(ms) / len(ms), world)
+    e2e_step_ms = max_over_ranks(sum(e2e_ms) / len(e2e_ms), world)
+    samples = W * H * SPP * world
+    value = samples / (step_ms / 1000.0) / 1e6
+    e2e_value = samples / (e2e_step_ms / 1000.0) / 1e6
+    if rank != 0:
+        barrier(world)
+        return
+    # ---- roofline of the extend kernel (bytes per ray from oracle statistics of this workload)
+    peak, peak_kind = peaks()
+    cpu = None
+    st = None
+    if not args.no_cpu_baseline:
+        t_frame, sample, st, _ = cpu_frame_estimate(sc, cam, rows_total=16, threads=os.cpu_count() or 1, stats=True)
+        cpu = {"value": round(W * H * SPP / t_frame / 1e6, 4), "unit": "Msamples/s", "cores": os.cpu_count() or 1,
+               "kind": "port", "sample": sample}
+    ext_ms = sum(e[0] for e in ext)
+    ext_launches = sum(e[1] for e in ext)
+    rays = sum(e[2] for e in ext)
+    roof = None
+    if st and st["rays"]:
+        n_node, n_tri = st["nodes"] / st["rays"], st["prims"] / st["rays"]
+        b_ray = 48 * n_node + 64 * n_tri + 32 + 16
+        achieved = rays * b_ray / (ext_ms / 1000.0) / 1e9
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": peak_kind,
+                "kernel": "k_extend", "bytes_per_ray": round(b_ray, 1), "n_node": round(n_node, 2),
+                "n_tri": round(n_tri, 2), "mrays_per_s": round(rays / (ext_ms / 1000.0) / 1e6, 1),
+                "avg_launch_ms": round(ext_ms / max(ext_launches, 1), 4)}
+    clocks = clk.summary()
+    out = {
+        "metric": "Msamples/s", "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": SPP, "max_depth": DEPTH,
+                   "triangles": int(len(sc["triangles"])), "seed": SEED, "estimator": "reference (no NEE)",
+                   "parallelism": f"replicas{world}", "l2": "256 MB buffer written between timed steps"},
+        "e2e": {"value": round(e2e_value, 3), "unit": "Msamples/s",
+                "h2d_bytes_per_step": int(sc["vertices"].nbytes), "d2h_bytes_per_step": W * H * 16},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "extend_ms_per_step": round(ext_ms / len(ext), 3),
+    }
+    print(json.dumps(out))
+    barrier(world)
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_mcrt(a)

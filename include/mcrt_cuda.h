@@ -1,0 +1,281 @@
+/* mcrt_cuda.h — C ABI of libmcrt_cuda.so, the GB300-native path-tracing hot path.
+ *
+ * This ABI replaces the reference's wgpu "operator API" for the path tracer:
+ * the 14-binding compute bind-group layout (src/gpu_layout.rs:78-234, slot
+ * constants :28-54), the buffers built by build_scene_buffers
+ * (src/gpu_layout.rs:259-390), the compute entry point cs_main
+ * (src/shaders/path_trace.wgsl:626-662, created at src/gpu_layout.rs:484-502)
+ * driven once per sample by headless::run (src/headless.rs:268-290), and the
+ * denoiser cs_denoise (src/shaders/denoise.wgsl:52-120, dispatched at
+ * src/gpu.rs:1155-1169).
+ *
+ * Conventions
+ *  - Every call returns mcrt_status (0 = success, < 0 = error).  The message of
+ *    the last failing call is available from mcrt_last_error(ctx) (or with a
+ *    NULL ctx for calls that have no context) until the next call on the same
+ *    context from the same thread.  No C++ exception crosses the ABI.
+ *  - The caller owns every host pointer; the context owns all device memory.
+ *  - Calls are synchronous on return unless documented otherwise.  A context is
+ *    not thread-safe; separate contexts are independent.
+ *  - Device loops are bounded; a bound that runs out is reported as a status,
+ *    never as a hang.
+ *  - Plain-old-data structs below are byte-identical to the reference's
+ *    #[repr(C)] bytemuck types (sizes asserted in the implementation).
+ */
+#ifndef MCRT_CUDA_H
+#define MCRT_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCRT_ABI_VERSION 1
+
+typedef int32_t mcrt_status;
+enum {
+    MCRT_OK = 0,
+    MCRT_ERR_INVALID_ARG = -1,
+    MCRT_ERR_OOM = -2,
+    MCRT_ERR_CUDA = -3,
+    MCRT_ERR_TIMEOUT = -4,          /* a bounded device loop ran out */
+    MCRT_ERR_STACK_OVERFLOW = -5,   /* a traversal stack bound was reached */
+    MCRT_ERR_NO_SCENE = -6,
+    MCRT_ERR_PARSE = -7,            /* SceneError::Parse, scene.rs:603 */
+    MCRT_ERR_IO = -8,               /* SceneError::Io, scene.rs:601 */
+    MCRT_ERR_UNKNOWN_MATERIAL = -9, /* SceneError::UnknownMaterial, scene.rs:605 */
+    MCRT_ERR_MESH_LOAD = -10,       /* SceneError::MeshLoad, scene.rs:607 */
+    MCRT_ERR_TOO_MANY_MATERIALS = -11, /* SceneError::TooManyMaterials, scene.rs:609 */
+    MCRT_ERR_UNSUPPORTED = -12
+};
+
+/* ------------------------------------------------------------------ reference data types */
+
+/* GpuSphere, src/scene.rs:24-29 (32 bytes). */
+typedef struct { float center_r[4]; uint32_t mat_and_pad[4]; } mcrt_gpu_sphere;
+/* GpuBvhNode, src/bvh.rs:56-68 (48 bytes). Pre-order; left = i+1. */
+typedef struct {
+    float aabb_min[4];
+    float aabb_max[4];
+    uint32_t right_or_offset;
+    uint32_t prim_count;
+    uint32_t _pad[2];
+} mcrt_gpu_bvh_node;
+/* GpuVertex, src/mesh.rs:26-34 (48 bytes). */
+typedef struct { float position[4]; float normal[4]; float uv[4]; } mcrt_gpu_vertex;
+/* GpuTriangle, src/mesh.rs:41-46 (16 bytes). mat_idx bit 31 = backface cull (scene.rs:709-718). */
+typedef struct { uint32_t v[3]; uint32_t mat_idx; } mcrt_gpu_triangle;
+/* GpuMaterial, src/material.rs:37-44 (48 bytes). */
+typedef struct { uint32_t type_pad[4]; float albedo_fuzz[4]; float ior_pad[4]; } mcrt_gpu_material;
+/* GpuMaterialData, src/material.rs:56-63 (3088 bytes). */
+#define MCRT_MAX_MATERIALS 64
+typedef struct {
+    uint32_t mat_count;
+    uint32_t n_emissive;
+    uint32_t _pad[2];
+    mcrt_gpu_material materials[MCRT_MAX_MATERIALS];
+} mcrt_gpu_material_data;
+/* CameraUniform, src/camera.rs:37-53 (112 bytes). */
+typedef struct {
+    float origin[4];
+    float lower_left[4];
+    float horizontal[4];
+    float vertical[4];
+    float defocus_u[4];
+    float defocus_v[4];
+    uint32_t frame_count;
+    uint32_t _pad[3];
+} mcrt_camera_uniform;
+
+/* Material types: material.rs:70-75, plus GGX (an extension; the reference has
+ * only fuzzy metal).  GGX: albedo_fuzz.xyz = F0 (Schlick), albedo_fuzz.w = roughness
+ * (alpha = roughness^2), sampled by visible normals. */
+enum { MCRT_MAT_LAMBERTIAN = 0, MCRT_MAT_METAL = 1, MCRT_MAT_DIELECTRIC = 2,
+       MCRT_MAT_EMISSIVE = 3, MCRT_MAT_GGX = 4 };
+#define MCRT_BACKFACE_CULL_FLAG 0x80000000u
+
+/* ------------------------------------------------------------------ context */
+
+typedef struct mcrt_ctx mcrt_ctx;
+
+/* Create a context on CUDA device `device`.  stream: a cudaStream_t to issue
+ * all work on, or NULL for a private non-blocking stream.  (No reference
+ * counterpart: wgpu's Instance/Adapter/Device, headless.rs:135-148.) */
+mcrt_status mcrt_create(int device, void *stream, mcrt_ctx **out);
+void mcrt_destroy(mcrt_ctx *ctx);
+const char *mcrt_last_error(const mcrt_ctx *ctx);
+const char *mcrt_version(void);
+
+/* ------------------------------------------------------------------ scene upload */
+
+/* Scene buffers as the reference binds them (gpu_layout.rs:28-54):
+ *   binding 2 spheres, 5 sphere_bvh, 6 vertices, 7 triangles, 8 mesh_bvh,
+ *   4 materials, 11 env_map (RGBA32F), 12 emissive_spheres (derived here).
+ * If sphere_bvh / mesh_bvh are given they are the outputs of the reference's
+ * build_bvh / build_mesh_bvh (bvh.rs:239, mesh.rs:82) and spheres / triangles
+ * are the matching ordered arrays; *_order then maps each ordered slot to its
+ * original index (the id reported by hits; identity when NULL).
+ * If a BVH pointer is NULL the BVH is built on the GPU by the binned SAH
+ * builder (same algorithm as the reference: 8 bins, leaf <= 4, Ct=0/Ci=1). */
+typedef struct {
+    const mcrt_gpu_sphere *spheres; uint32_t n_spheres;
+    const mcrt_gpu_bvh_node *sphere_bvh; uint32_t n_sphere_nodes;
+    const uint32_t *sphere_order;
+    const mcrt_gpu_vertex *vertices; uint32_t n_vertices;
+    const mcrt_gpu_triangle *triangles; uint32_t n_triangles;
+    const mcrt_gpu_bvh_node *mesh_bvh; uint32_t n_mesh_nodes;
+    const uint32_t *triangle_order;
+    const mcrt_gpu_material_data *materials;
+    const float *env_rgba; uint32_t env_w; uint32_t env_h;
+    uint32_t flags; /* reserved, 0 */
+} mcrt_scene_desc;
+
+/* Upload (or replace) the scene.  Replaces gpu_layout::build_scene_buffers
+ * (gpu_layout.rs:259-390). */
+mcrt_status mcrt_upload_scene(mcrt_ctx *ctx, const mcrt_scene_desc *desc);
+
+/* Replace the vertex positions/normals/uvs of the current scene (same count and
+ * topology) and rebuild the mesh BVH on the GPU (a per-frame rebuild). */
+mcrt_status mcrt_update_vertices(mcrt_ctx *ctx, const mcrt_gpu_vertex *vertices, uint32_t n_vertices);
+
+/* Rebuild the mesh BVH of the current scene on the GPU from the device-resident
+ * vertices (the per-frame rebuild without a host upload). */
+mcrt_status mcrt_rebuild_bvh(mcrt_ctx *ctx);
+
+/* Copy the device-resident mesh BVH of the current scene (reference layout,
+ * pre-order) back to the host.  out_nodes: capacity 2*n_triangles;
+ * out_order: capacity n_triangles (original id per ordered slot).  */
+mcrt_status mcrt_get_mesh_bvh(mcrt_ctx *ctx, mcrt_gpu_bvh_node *out_nodes, uint32_t capacity,
+                              uint32_t *out_n_nodes, uint32_t *out_order);
+
+/* ------------------------------------------------------------------ closest hit (parity probe) */
+
+typedef struct { float org[3]; float tmin; float dir[3]; float tmax; } mcrt_ray;   /* 32 B */
+typedef struct { float t; uint32_t prim; float u; float v; } mcrt_hit;             /* 16 B */
+#define MCRT_HIT_MISS 0xFFFFFFFFu
+#define MCRT_HIT_SPHERE 0x80000000u   /* prim = MCRT_HIT_SPHERE | sphere id, else triangle id */
+
+enum {
+    MCRT_TRACE_REFERENCE_LAYOUT = 1u << 0,  /* traverse the 48-byte reference nodes in
+                                              the reference visit order (path_trace.wgsl:343-479) */
+    MCRT_TRACE_STATS = 1u << 1              /* reserved */
+};
+
+/* world_hit (path_trace.wgsl:471-479) for n host rays.  Tie rule: smallest t,
+ * then smallest original id; a sphere wins over a triangle at equal t.
+ * Requires ray.tmin > 0.  miss: prim = MCRT_HIT_MISS, t = -1. */
+mcrt_status mcrt_trace_closest(mcrt_ctx *ctx, const mcrt_ray *rays, uint32_t n, mcrt_hit *hits, uint32_t flags);
+
+/* ------------------------------------------------------------------ render */
+
+enum {
+    MCRT_RENDER_NEE = 1u << 0,        /* next-event estimation + MIS (else the reference estimator) */
+    MCRT_RENDER_GBUFFER = 1u << 1,    /* keep the primary-hit G-buffer (path_trace.wgsl:593-601) */
+    MCRT_RENDER_KEEP_ACCUM = 1u << 2  /* continue the device running mean / f64 sum of the previous call */
+};
+
+typedef struct {
+    uint32_t max_depth;     /* bounces; 0 -> 8 = the reference's MAX_BOUNCES (path_trace.wgsl:61) */
+    uint32_t flags;
+    uint32_t spp_per_pass;  /* samples traced concurrently; 0 -> automatic */
+    uint32_t reserved;
+} mcrt_render_opts;
+
+/* Render frames first_frame .. first_frame+spp-1 of a w x h image
+ * (headless.rs:249-290: one cs_main dispatch per frame, frame_count = index).
+ * cam->frame_count is ignored.  Outputs (all optional, host memory):
+ *   out_rgba  : the reference's accumulation texture after the last frame —
+ *               the f32 running mean (path_trace.wgsl:656-661) with alpha 1
+ *               (w*h*4 floats);
+ *   accum_rgb : f64 sample sums per pixel, ADDED to the caller's values (w*h*3);
+ *   out_gbuf  : primary-hit normal.xyz + depth of the last frame (w*h*4 floats).
+ * With all outputs NULL the results stay on the device (see mcrt_read_accum). */
+mcrt_status mcrt_render(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t w, uint32_t h,
+                        uint32_t spp, uint32_t first_frame, const mcrt_render_opts *opts,
+                        float *out_rgba, double *accum_rgb, float *out_gbuf);
+
+/* Copy the device accumulation of the last render to the host (any may be NULL). */
+mcrt_status mcrt_read_accum(mcrt_ctx *ctx, float *out_rgba, double *accum_rgb, float *out_gbuf);
+
+/* Per-kernel device time of the last render, from CUDA events on the context
+ * stream: [0] total, [1] trace (extend), [2] shade, [3] shadow rays, [4] resolve,
+ * [5] BVH build (ms); counters: [0] rays traced, [1] shadow rays, [2] kernel
+ * launches of the last render, [3] kernel launches of the last BVH build,
+ * [4] extend launches of the last render.  out_ms: 6 floats, out_counts: 5 uint64. */
+mcrt_status mcrt_last_timings(mcrt_ctx *ctx, float *out_ms, uint64_t *out_counts);
+
+/* ------------------------------------------------------------------ denoiser */
+
+/* DenoiseParams, gpu.rs:166-185 (std140, 16 bytes) followed by extensions.
+ * Defaults R=3, sigma_s=2, sigma_d=0.5, normal_pow=8.
+ * Extensions (0 = the reference's filter):
+ *   sigma_color  > 0: multiply by exp(-|c_p - c_q|^2 / (2 sigma_color^2));
+ *   sigma_normal > 0: the normal term is exp(-(1 - n_p.n_q)^2 / (2 sigma_normal^2))
+ *                     instead of max(0, n_p.n_q)^normal_pow. */
+typedef struct {
+    int32_t radius;
+    float sigma_s;
+    float sigma_d;
+    float normal_pow;
+    float sigma_color;
+    float sigma_normal;
+    uint32_t _pad[2];
+} mcrt_denoise_params;
+
+/* cs_denoise (denoise.wgsl:52-120) over host images (w*h*4 floats each). */
+mcrt_status mcrt_denoise(mcrt_ctx *ctx, const float *in_rgba, const float *gbuf, uint32_t w, uint32_t h,
+                         const mcrt_denoise_params *params, float *out_rgba);
+
+/* ------------------------------------------------------------------ host-side scene API
+ * (the reference's Scene/Material/Camera/YAML API, run on the CPU exactly as
+ * the reference runs it). */
+
+typedef struct mcrt_loaded_scene mcrt_loaded_scene;
+
+/* load_scene_from_yaml / load_scene_from_str (scene.rs:640-999). */
+mcrt_status mcrt_scene_load_yaml(const char *path, mcrt_loaded_scene **out);
+mcrt_status mcrt_scene_load_yaml_str(const char *text, const char *source, mcrt_loaded_scene **out);
+void mcrt_scene_free(mcrt_loaded_scene *scene);
+
+typedef struct {
+    const mcrt_gpu_sphere *spheres; uint32_t n_spheres;
+    const mcrt_gpu_vertex *vertices; uint32_t n_vertices;
+    const mcrt_gpu_triangle *triangles; uint32_t n_triangles;
+    const mcrt_gpu_sphere *emissive_spheres; uint32_t n_emissive_spheres;
+    const mcrt_gpu_material_data *materials;
+    int32_t has_camera;
+    float look_from[3]; float look_at[3]; float vfov; float aperture; float focus_dist;
+    const char *env_map_path;   /* NULL when absent */
+    uint32_t n_material_names;
+} mcrt_scene_view;
+mcrt_status mcrt_scene_view_get(const mcrt_loaded_scene *scene, mcrt_scene_view *out);
+const char *mcrt_scene_material_name(const mcrt_loaded_scene *scene, uint32_t index);
+
+/* compute_camera (camera.rs:76-127). */
+mcrt_status mcrt_compute_camera(uint32_t width, uint32_t height, const float look_from[3], const float look_at[3],
+                                float vfov_deg, float aperture, float focus_dist, mcrt_camera_uniform *out);
+
+/* load_env_map_data (texture.rs:209-220): RGBA32F, 1024 x 512.  path may be NULL.
+ * out must hold 1024*512*4 floats. */
+#define MCRT_ENV_MAP_WIDTH 1024
+#define MCRT_ENV_MAP_HEIGHT 512
+mcrt_status mcrt_load_env_map(const char *path, float *out);
+/* build_gradient_env_map (texture.rs:158-199). */
+mcrt_status mcrt_gradient_env_map(float *out);
+
+/* tonemap_to_u8 over an RGBA32F image (headless.rs:93-98, :350-368): RGBA8, alpha 255. */
+mcrt_status mcrt_tonemap_rgba8(const float *rgba, uint32_t n_pixels, uint8_t *out);
+/* RGBA8 PNG writer (the image crate's save, headless.rs:380-382). */
+mcrt_status mcrt_write_png(const char *path, const uint8_t *rgba, uint32_t w, uint32_t h);
+
+/* headless::run (headless.rs:112-386): parameters CLI > sidecar [render] > 512/512/64.
+ * width/height/spp = 0 means "not given".  opts may be NULL (reference estimator). */
+mcrt_status mcrt_headless_run(const char *scene_path, const char *output_path, uint32_t width, uint32_t height,
+                              uint32_t spp, const mcrt_render_opts *opts);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MCRT_CUDA_H */

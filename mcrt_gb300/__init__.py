@@ -1,0 +1,274 @@
+"""mcrt_gb300 — GB300-native path-tracing hot path of mcrt behind a C ABI.
+
+Python view of libmcrt_cuda.so (include/mcrt_cuda.h).  The CUDA library does
+all of the work; this module only marshals numpy arrays.  It mirrors the
+reference's interfaces for the path:
+
+* ``load_scene_yaml`` / ``load_scene_yaml_str`` — scene.rs load_scene_from_yaml /
+  load_scene_from_str (src/scene.rs:640-999);
+* ``compute_camera`` — camera.rs compute_camera (src/camera.rs:76-127);
+* ``load_env_map`` / ``gradient_env_map`` — texture.rs (src/texture.rs:158-220);
+* ``Context.upload_scene`` — gpu_layout::build_scene_buffers (src/gpu_layout.rs:259-390);
+* ``Context.render`` — the per-sample cs_main dispatches of headless::run
+  (src/headless.rs:249-290, src/shaders/path_trace.wgsl:626-662);
+* ``Context.denoise`` — cs_denoise (src/shaders/denoise.wgsl:52-120);
+* ``headless_run`` — headless::run (src/headless.rs:112-386).
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import c_float, c_uint32, c_uint64, c_void_p
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native as N
+from ._native import (CAMERA, HIT, MATERIAL, MATERIAL_DATA, NODE, RAY, SPHERE, TRIANGLE, VERTEX, MCRTError,
+                      check, lib, ptr)
+
+__all__ = ["Context", "Scene", "load_scene_yaml", "load_scene_yaml_str", "compute_camera", "load_env_map",
+           "gradient_env_map", "tonemap_rgba8", "write_png", "headless_run", "MCRTError", "SPHERE", "NODE",
+           "VERTEX", "TRIANGLE", "MATERIAL", "MATERIAL_DATA", "CAMERA", "RAY", "HIT", "make_rays", "materials"]
+
+
+def _arr(a, dtype):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a)
+    if a.dtype != dtype:
+        raise TypeError(f"expected dtype {dtype}, got {a.dtype}")
+    return a
+
+
+@dataclass
+class Scene:
+    """LoadedScene (src/scene.rs:311-351) as numpy record arrays."""
+    spheres: np.ndarray
+    vertices: np.ndarray
+    triangles: np.ndarray
+    materials: np.ndarray          # MATERIAL_DATA, shape ()
+    emissive_spheres: np.ndarray
+    camera: dict | None = None     # look_from, look_at, vfov, aperture, focus_dist
+    env_map_path: str | None = None
+    material_names: list = field(default_factory=list)
+
+
+def _scene_from_handle(h) -> Scene:
+    L = lib()
+    v = N.SceneView()
+    check(L.mcrt_scene_view_get(h, ctypes.byref(v)))
+
+    def grab(p, n, dt):
+        if n == 0:
+            return np.zeros(0, dt)
+        buf = (ctypes.c_uint8 * (n * dt.itemsize)).from_address(p)
+        return np.frombuffer(bytes(buf), dtype=dt).copy()
+
+    mats = np.frombuffer(bytes((ctypes.c_uint8 * MATERIAL_DATA.itemsize).from_address(v.materials)),
+                         dtype=MATERIAL_DATA)[0].copy()
+    cam = None
+    if v.has_camera:
+        cam = dict(look_from=list(v.look_from), look_at=list(v.look_at), vfov=v.vfov, aperture=v.aperture,
+                   focus_dist=v.focus_dist)
+    names = [L.mcrt_scene_material_name(h, i).decode() for i in range(v.n_material_names)]
+    return Scene(spheres=grab(v.spheres, v.n_spheres, SPHERE), vertices=grab(v.vertices, v.n_vertices, VERTEX),
+                 triangles=grab(v.triangles, v.n_triangles, TRIANGLE), materials=mats,
+                 emissive_spheres=grab(v.emissive_spheres, v.n_emissive_spheres, SPHERE), camera=cam,
+                 env_map_path=v.env_map_path.decode() if v.env_map_path else None, material_names=names)
+
+
+def load_scene_yaml(path: str) -> Scene:
+    h = c_void_p()
+    check(lib().mcrt_scene_load_yaml(path.encode(), ctypes.byref(h)))
+    try:
+        return _scene_from_handle(h)
+    finally:
+        lib().mcrt_scene_free(h)
+
+
+def load_scene_yaml_str(text: str, source: str = "<inline>") -> Scene:
+    h = c_void_p()
+    check(lib().mcrt_scene_load_yaml_str(text.encode(), source.encode(), ctypes.byref(h)))
+    try:
+        return _scene_from_handle(h)
+    finally:
+        lib().mcrt_scene_free(h)
+
+
+def compute_camera(width, height, look_from, look_at, vfov=60.0, aperture=0.0, focus_dist=None) -> np.ndarray:
+    lf = (c_float * 3)(*look_from)
+    la = (c_float * 3)(*look_at)
+    if focus_dist is None:
+        d = np.asarray(look_from, np.float32) - np.asarray(look_at, np.float32)
+        focus_dist = float(np.sqrt(np.float32(d[0] * d[0] + d[1] * d[1]) + np.float32(d[2] * d[2])))
+    out = np.zeros((), CAMERA)
+    check(lib().mcrt_compute_camera(width, height, lf, la, vfov, aperture, focus_dist, ptr(out)))
+    return out
+
+
+def load_env_map(path: str | None) -> np.ndarray:
+    out = np.zeros((N.ENV_H, N.ENV_W, 4), np.float32)
+    check(lib().mcrt_load_env_map(path.encode() if path else None, ptr(out)))
+    return out
+
+
+def gradient_env_map() -> np.ndarray:
+    out = np.zeros((N.ENV_H, N.ENV_W, 4), np.float32)
+    check(lib().mcrt_gradient_env_map(ptr(out)))
+    return out
+
+
+def tonemap_rgba8(rgba: np.ndarray) -> np.ndarray:
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    out = np.zeros(rgba.shape[:-1] + (4,), np.uint8)
+    check(lib().mcrt_tonemap_rgba8(ptr(rgba), rgba.size // 4, ptr(out)))
+    return out
+
+
+def write_png(path: str, rgba8: np.ndarray):
+    rgba8 = np.ascontiguousarray(rgba8, np.uint8)
+    h, w = rgba8.shape[:2]
+    check(lib().mcrt_write_png(path.encode(), ptr(rgba8), w, h))
+
+
+def headless_run(scene_path, output_path, width=None, height=None, spp=None, max_depth=0, nee=False):
+    o = N.RenderOpts(max_depth=max_depth, flags=N.RENDER_NEE if nee else 0)
+    check(lib().mcrt_headless_run(scene_path.encode(), output_path.encode(), width or 0, height or 0, spp or 0,
+                                  ctypes.byref(o)))
+
+
+def materials(entries) -> np.ndarray:
+    """Build a GpuMaterialData from (type, albedo_rgb, w, ior_or_strength[, texture_layer]) tuples."""
+    md = np.zeros((), MATERIAL_DATA)
+    md["mat_count"] = len(entries)
+    for i, e in enumerate(entries):
+        t, alb, w, x = e[:4]
+        md["materials"][i]["type_pad"][0] = t
+        md["materials"][i]["type_pad"][1] = e[4] if len(e) > 4 else 0
+        md["materials"][i]["albedo_fuzz"][:3] = alb
+        md["materials"][i]["albedo_fuzz"][3] = w
+        md["materials"][i]["ior_pad"][0] = x
+    return md
+
+
+def make_rays(org, dirs, tmin=1e-4, tmax=1e9) -> np.ndarray:
+    org = np.asarray(org, np.float32).reshape(-1, 3)
+    dirs = np.asarray(dirs, np.float32).reshape(-1, 3)
+    r = np.zeros(len(dirs), RAY)
+    r["org"] = org
+    r["dir"] = dirs
+    r["tmin"] = tmin
+    r["tmax"] = tmax
+    return r
+
+
+class Context:
+    """A CUDA context of the library: one device, one stream, one resident scene."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        self._h = c_void_p()
+        check(lib().mcrt_create(device, c_void_p(stream) if stream else None, ctypes.byref(self._h)))
+        self._keep = []
+
+    def close(self):
+        if self._h:
+            lib().mcrt_destroy(self._h)
+            self._h = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, s):
+        check(s, self._h)
+
+    def upload_scene(self, *, materials, spheres=None, vertices=None, triangles=None, env=None, sphere_bvh=None,
+                     sphere_order=None, mesh_bvh=None, triangle_order=None):
+        sph = _arr(spheres, SPHERE)
+        ver = _arr(vertices, VERTEX)
+        tri = _arr(triangles, TRIANGLE)
+        mats = _arr(materials, MATERIAL_DATA)
+        sbvh = _arr(sphere_bvh, NODE)
+        mbvh = _arr(mesh_bvh, NODE)
+        sord = _arr(sphere_order, np.uint32)
+        tord = _arr(triangle_order, np.uint32)
+        envp = None if env is None else np.ascontiguousarray(env, np.float32)
+        d = N.SceneDesc()
+        d.spheres, d.n_spheres = ptr(sph), 0 if sph is None else len(sph)
+        d.sphere_bvh, d.n_sphere_nodes = ptr(sbvh), 0 if sbvh is None else len(sbvh)
+        d.sphere_order = ptr(sord)
+        d.vertices, d.n_vertices = ptr(ver), 0 if ver is None else len(ver)
+        d.triangles, d.n_triangles = ptr(tri), 0 if tri is None else len(tri)
+        d.mesh_bvh, d.n_mesh_nodes = ptr(mbvh), 0 if mbvh is None else len(mbvh)
+        d.triangle_order = ptr(tord)
+        d.materials = ptr(mats)
+        if envp is not None:
+            d.env_rgba, d.env_h, d.env_w = ptr(envp), envp.shape[0], envp.shape[1]
+        self._check(lib().mcrt_upload_scene(self._h, ctypes.byref(d)))
+        self.n_triangles = d.n_triangles
+
+    def update_vertices(self, vertices):
+        ver = _arr(vertices, VERTEX)
+        self._check(lib().mcrt_update_vertices(self._h, ptr(ver), len(ver)))
+
+    def rebuild_bvh(self):
+        self._check(lib().mcrt_rebuild_bvh(self._h))
+
+    def mesh_bvh(self):
+        n = c_uint32()
+        self._check(lib().mcrt_get_mesh_bvh(self._h, None, 0, ctypes.byref(n), None))
+        nodes = np.zeros(n.value, NODE)
+        order = np.zeros(self.n_triangles, np.uint32)
+        self._check(lib().mcrt_get_mesh_bvh(self._h, ptr(nodes), n.value, ctypes.byref(n), ptr(order)))
+        return nodes, order
+
+    def trace_closest(self, rays, reference_layout=False) -> np.ndarray:
+        rays = _arr(rays, RAY)
+        hits = np.zeros(len(rays), HIT)
+        self._check(lib().mcrt_trace_closest(self._h, ptr(rays), len(rays), ptr(hits),
+                                             N.TRACE_REFERENCE_LAYOUT if reference_layout else 0))
+        return hits
+
+    def render(self, camera, width, height, spp, first_frame=0, max_depth=0, nee=False, spp_per_pass=0,
+               keep=False, outputs=("rgba", "sum", "gbuf")):
+        cam = _arr(camera, CAMERA)
+        o = N.RenderOpts(max_depth=max_depth, flags=(N.RENDER_NEE if nee else 0) |
+                         (N.RENDER_KEEP_ACCUM if keep else 0), spp_per_pass=spp_per_pass)
+        rgba = np.zeros((height, width, 4), np.float32) if "rgba" in outputs else None
+        acc = np.zeros((height, width, 3), np.float64) if "sum" in outputs else None
+        gb = np.zeros((height, width, 4), np.float32) if "gbuf" in outputs else None
+        self._check(lib().mcrt_render(self._h, ptr(cam), width, height, spp, first_frame, ctypes.byref(o),
+                                      ptr(rgba), ptr(acc), ptr(gb)))
+        return dict(rgba=rgba, sum=acc, gbuf=gb)
+
+    def timings(self):
+        ms = (c_float * 6)()
+        cnt = (c_uint64 * 5)()
+        self._check(lib().mcrt_last_timings(self._h, ms, cnt))
+        keys = ["total", "extend", "shade", "shadow", "resolve", "bvh_build"]
+        d = {f"{k}_ms": ms[i] for i, k in enumerate(keys)}
+        d["rays"] = cnt[0]
+        d["shadow_rays"] = cnt[1]
+        d["render_launches"] = cnt[2]
+        d["build_launches"] = cnt[3]
+        d["extend_launches"] = cnt[4]
+        return d
+
+    def denoise(self, rgba, gbuf, radius=3, sigma_s=2.0, sigma_d=0.5, normal_pow=8.0, sigma_color=0.0,
+                sigma_normal=0.0):
+        rgba = np.ascontiguousarray(rgba, np.float32)
+        gbuf = np.ascontiguousarray(gbuf, np.float32)
+        h, w = rgba.shape[:2]
+        p = N.DenoiseParams(radius=radius, sigma_s=sigma_s, sigma_d=sigma_d, normal_pow=normal_pow,
+                            sigma_color=sigma_color, sigma_normal=sigma_normal)
+        out = np.zeros_like(rgba)
+        self._check(lib().mcrt_denoise(self._h, ptr(rgba), ptr(gbuf), w, h, ctypes.byref(p), ptr(out)))
+        return out

@@ -1,0 +1,729 @@
+// api.cu — the extern "C" entry points of libmcrt_cuda.so (include/mcrt_cuda.h):
+// context, scene upload (with host-side validation of every index the kernels
+// will dereference), closest-hit probe, render driver, denoiser.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+
+static_assert(sizeof(mcrt_gpu_sphere) == 32, "GpuSphere is 32 bytes (scene.rs:24-29)");
+static_assert(sizeof(mcrt_gpu_bvh_node) == 48, "GpuBvhNode is 48 bytes (bvh.rs:56-68)");
+static_assert(sizeof(mcrt_gpu_vertex) == 48, "GpuVertex is 48 bytes (mesh.rs:26-34)");
+static_assert(sizeof(mcrt_gpu_triangle) == 16, "GpuTriangle is 16 bytes (mesh.rs:41-46)");
+static_assert(sizeof(mcrt_gpu_material) == 48, "GpuMaterial is 48 bytes (material.rs:37-44)");
+static_assert(sizeof(mcrt_gpu_material_data) == 3088, "GpuMaterialData is 3088 bytes (material.rs:56-63)");
+static_assert(sizeof(mcrt_camera_uniform) == 112, "CameraUniform is 112 bytes (camera.rs:37-53)");
+static_assert(sizeof(mcrt_ray) == 32 && sizeof(mcrt_hit) == 16, "ray/hit records");
+static_assert(sizeof(mcrt_denoise_params) == 32, "denoise params");
+static_assert(sizeof(mcrt::TriRec) == 48, "fast triangle record");
+
+namespace mcrt {
+void launch_light_cdf(const DeviceScene &S, float *d_cdf, float *d_total, cudaStream_t st);
+cudaError_t gpu_build_sphere_bvh(const mcrt_gpu_sphere *d_spheres, uint32_t n, mcrt_gpu_bvh_node *d_nodes,
+                                 uint32_t *d_order, uint32_t *n_nodes_out, BvhScratch **scratch, cudaStream_t st,
+                                 std::string *err);
+}  // namespace mcrt
+
+namespace {
+
+thread_local std::string g_error;   // errors of calls without a context
+
+}  // namespace
+
+namespace mcrt {
+void set_global_error(const std::string &msg) { g_error = msg; }
+static std::atomic<unsigned long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+unsigned long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+}  // namespace mcrt
+
+namespace {
+
+struct DBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes == 0) bytes = 16;
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e == cudaSuccess) cap = bytes;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <typename T> T *as() const { return static_cast<T *>(p); }
+};
+
+}  // namespace
+
+struct mcrt_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    // scene
+    bool has_scene = false;
+    DBuf spheres, sphere_ids, sphere_nodes, vertices, triangles, mesh_nodes, tri_order, trirecs, cnodes, materials,
+        env, lights, light_cdf, tmp, staging;
+    uint32_t n_spheres = 0, n_sphere_nodes = 0, n_vertices = 0, n_triangles = 0, n_mesh_nodes = 0, n_cnodes = 0,
+             n_lights = 0, env_w = 0, env_h = 0;
+    float light_total = 0.0f;
+    mcrt::BvhScratch *bvh_scratch = nullptr;
+    // render state
+    mcrt::PathBuffers pb;
+    DBuf pbmem;
+    DBuf mean, sum, gbuf;
+    uint32_t acc_w = 0, acc_h = 0;
+    bool acc_valid = false, gbuf_valid = false;
+    // probe / denoise buffers
+    DBuf io_a, io_b, io_c, counters;
+    // timing
+    std::vector<cudaEvent_t> ev_pool;
+    float last_ms[6] = {0, 0, 0, 0, 0, 0};
+    unsigned long long last_counts[2] = {0, 0};
+    unsigned long long last_render_launches = 0, last_build_launches = 0, last_extend_launches = 0;
+    float last_build_ms = 0.0f;
+};
+
+namespace {
+
+mcrt_status fail(mcrt_ctx *c, mcrt_status code, const std::string &msg) {
+    if (c) c->err = msg;
+    else g_error = msg;
+    return code;
+}
+mcrt_status cuda_fail(mcrt_ctx *c, cudaError_t e, const std::string &what) {
+    std::string m = what + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return fail(c, MCRT_ERR_OOM, m);
+    return fail(c, MCRT_ERR_CUDA, m);
+}
+#define CK(call, what)                                            \
+    do {                                                          \
+        cudaError_t e__ = (call);                                 \
+        if (e__ != cudaSuccess) return cuda_fail(ctx, e__, what); \
+    } while (0)
+
+mcrt::DeviceScene device_scene(const mcrt_ctx *c) {
+    mcrt::DeviceScene S{};
+    S.spheres = c->spheres.as<mcrt_gpu_sphere>();
+    S.n_spheres = c->n_spheres;
+    S.sphere_ids = c->sphere_ids.as<uint32_t>();
+    S.sphere_nodes = c->sphere_nodes.as<mcrt_gpu_bvh_node>();
+    S.n_sphere_nodes = c->n_sphere_nodes;
+    S.vertices = c->vertices.as<mcrt_gpu_vertex>();
+    S.n_vertices = c->n_vertices;
+    S.triangles = c->triangles.as<mcrt_gpu_triangle>();
+    S.n_triangles = c->n_triangles;
+    S.mesh_nodes = c->mesh_nodes.as<mcrt_gpu_bvh_node>();
+    S.n_mesh_nodes = c->n_mesh_nodes;
+    S.tri_ids = c->tri_order.as<uint32_t>();
+    S.tris = c->trirecs.as<mcrt::TriRec>();
+    S.cnodes = c->cnodes.as<float4>();
+    S.n_cnodes = c->n_cnodes;
+    S.materials = c->materials.as<mcrt_gpu_material_data>();
+    S.env = c->env.as<float4>();
+    S.env_w = c->env_w;
+    S.env_h = c->env_h;
+    S.lights = c->lights.as<uint32_t>();
+    S.n_lights = c->n_lights;
+    S.light_cdf = c->light_cdf.as<float>();
+    S.light_total = c->light_total;
+    return S;
+}
+
+// Host validation of a reference-layout BVH: pre-order children strictly after
+// the parent (so every traversal terminates) and every index in range.
+bool valid_bvh(const mcrt_gpu_bvh_node *nodes, uint32_t n_nodes, uint32_t n_prims, std::string *why) {
+    for (uint32_t i = 0; i < n_nodes; ++i) {
+        const mcrt_gpu_bvh_node &nd = nodes[i];
+        if (nd.prim_count == 0) {
+            if (i + 1 >= n_nodes || nd.right_or_offset <= i + 1 || nd.right_or_offset >= n_nodes) {
+                *why = "internal node " + std::to_string(i) + " has an out-of-order or out-of-range child";
+                return false;
+            }
+        } else if ((uint64_t)nd.right_or_offset + nd.prim_count > n_prims) {
+            *why = "leaf " + std::to_string(i) + " references primitives beyond the primitive count";
+            return false;
+        }
+    }
+    return true;
+}
+
+bool valid_permutation(const uint32_t *order, uint32_t n) {
+    std::vector<uint8_t> seen(n, 0);
+    for (uint32_t i = 0; i < n; ++i) {
+        if (order[i] >= n || seen[order[i]]) return false;
+        seen[order[i]] = 1;
+    }
+    return true;
+}
+
+__global__ void k_scatter_tris(const mcrt_gpu_triangle *ordered, const uint32_t *order, uint32_t n,
+                               mcrt_gpu_triangle *out) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) out[order[s]] = ordered[s];
+}
+__global__ void k_gather_spheres(const mcrt_gpu_sphere *orig, const uint32_t *order, uint32_t n,
+                                 mcrt_gpu_sphere *out) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) out[s] = orig[order[s]];
+}
+__global__ void k_iota(uint32_t *p, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = i;
+}
+
+cudaEvent_t ev(mcrt_ctx *ctx, size_t i) {
+    while (ctx->ev_pool.size() <= i) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        ctx->ev_pool.push_back(e);
+    }
+    return ctx->ev_pool[i];
+}
+
+// Derived device structures of the mesh: compact nodes and triangle records.
+mcrt_status finish_mesh(mcrt_ctx *ctx) {
+    cudaStream_t st = ctx->stream;
+    uint32_t nt = ctx->n_triangles, nn = ctx->n_mesh_nodes;
+    CK(ctx->trirecs.ensure((size_t)std::max(nt, 1u) * sizeof(mcrt::TriRec)), "allocate triangle records");
+    CK(ctx->cnodes.ensure((size_t)(nn / 2 + 1) * 64), "allocate compact nodes");
+    size_t tmp_words = 2 * (size_t)std::max(nn, 1u) + mcrt::scan_tmp_words(std::max(nn, 1u));
+    CK(ctx->tmp.ensure(tmp_words * 4), "allocate scan scratch");
+    float4 *cn = ctx->cnodes.as<float4>();
+    uint32_t ncn = 0;
+    CK(mcrt::gpu_make_compact(ctx->mesh_nodes.as<mcrt_gpu_bvh_node>(), nn, ctx->tri_order.as<uint32_t>(),
+                              ctx->vertices.as<mcrt_gpu_vertex>(), ctx->triangles.as<mcrt_gpu_triangle>(), nt, &cn,
+                              &ncn, ctx->trirecs.p, ctx->tmp.as<uint32_t>(), tmp_words, st),
+       "compact BVH");
+    ctx->n_cnodes = ncn;
+    return MCRT_OK;
+}
+
+// Light CDF over the light list (device), total weight read back.
+mcrt_status finish_lights(mcrt_ctx *ctx) {
+    ctx->light_total = 0.0f;
+    if (ctx->n_lights == 0) return MCRT_OK;
+    CK(ctx->light_cdf.ensure(((size_t)ctx->n_lights + 2) * sizeof(float)), "allocate light cdf");
+    mcrt::DeviceScene S = device_scene(ctx);
+    float *d_total = ctx->light_cdf.as<float>() + ctx->n_lights + 1;
+    mcrt::launch_light_cdf(S, ctx->light_cdf.as<float>(), d_total, ctx->stream);
+    float total = 0.0f;
+    CK(cudaMemcpyAsync(&total, d_total, 4, cudaMemcpyDeviceToHost, ctx->stream), "read light total");
+    CK(cudaStreamSynchronize(ctx->stream), "light cdf");
+    ctx->light_total = total;
+    if (!(total > 0.0f)) ctx->n_lights = 0;
+    return MCRT_OK;
+}
+
+mcrt_status build_mesh_bvh_gpu(mcrt_ctx *ctx) {
+    uint32_t nn = 0;
+    std::string err;
+    const unsigned long long l0 = mcrt::launch_count();
+    cudaEvent_t a = ev(ctx, 0), b = ev(ctx, 1);
+    cudaEventRecord(a, ctx->stream);
+    cudaError_t e = mcrt::gpu_build_mesh_bvh(ctx->vertices.as<mcrt_gpu_vertex>(),
+                                             ctx->triangles.as<mcrt_gpu_triangle>(), ctx->n_triangles,
+                                             ctx->mesh_nodes.as<mcrt_gpu_bvh_node>(), ctx->tri_order.as<uint32_t>(),
+                                             &nn, &ctx->bvh_scratch, ctx->stream, &err);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "mesh BVH build: " + err);
+    ctx->n_mesh_nodes = nn;
+    mcrt_status s = finish_mesh(ctx);
+    if (s != MCRT_OK) return s;
+    cudaEventRecord(b, ctx->stream);
+    CK(cudaEventSynchronize(b), "BVH build");
+    cudaEventElapsedTime(&ctx->last_build_ms, a, b);
+    ctx->last_build_launches = mcrt::launch_count() - l0;
+    return MCRT_OK;
+}
+
+}  // namespace
+
+// ====================================================================== ABI
+
+extern "C" {
+
+const char *mcrt_version(void) { return "mcrt_gb300 1 (sm_103a)"; }
+
+const char *mcrt_last_error(const mcrt_ctx *ctx) { return ctx ? ctx->err.c_str() : g_error.c_str(); }
+
+mcrt_status mcrt_create(int device, void *stream, mcrt_ctx **out) {
+    if (!out) return fail(nullptr, MCRT_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(nullptr, MCRT_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    if (device < 0 || device >= ndev) return fail(nullptr, MCRT_ERR_INVALID_ARG, "device index out of range");
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) return fail(nullptr, MCRT_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    mcrt_ctx *c = new mcrt_ctx();
+    c->device = device;
+    if (stream) {
+        c->stream = static_cast<cudaStream_t>(stream);
+    } else {
+        e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            delete c;
+            return fail(nullptr, MCRT_ERR_CUDA, "cudaStreamCreate failed");
+        }
+        c->own_stream = true;
+    }
+    *out = c;
+    return MCRT_OK;
+}
+
+void mcrt_destroy(mcrt_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    DBuf *bufs[] = {&ctx->spheres, &ctx->sphere_ids, &ctx->sphere_nodes, &ctx->vertices, &ctx->triangles,
+                    &ctx->mesh_nodes, &ctx->tri_order, &ctx->trirecs, &ctx->cnodes, &ctx->materials, &ctx->env,
+                    &ctx->lights, &ctx->light_cdf, &ctx->tmp, &ctx->staging, &ctx->pbmem, &ctx->mean,
+                    &ctx->sum, &ctx->gbuf, &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->counters};
+    for (DBuf *b : bufs) b->release();
+    mcrt::free_bvh_scratch(ctx->bvh_scratch);
+    for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+mcrt_status mcrt_upload_scene(mcrt_ctx *ctx, const mcrt_scene_desc *d) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!d) return fail(ctx, MCRT_ERR_INVALID_ARG, "desc is NULL");
+    if (!d->materials) return fail(ctx, MCRT_ERR_INVALID_ARG, "materials is NULL");
+    if (d->n_spheres && !d->spheres) return fail(ctx, MCRT_ERR_INVALID_ARG, "spheres is NULL");
+    if (d->n_triangles && (!d->triangles || !d->vertices))
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "triangles or vertices is NULL");
+    if (d->n_triangles >= (1u << 27) - 1) return fail(ctx, MCRT_ERR_INVALID_ARG, "too many triangles (max 2^27-2)");
+    if (d->n_spheres >= (1u << 30)) return fail(ctx, MCRT_ERR_INVALID_ARG, "too many spheres");
+    if ((d->env_w == 0) != (d->env_h == 0) || (d->env_w && !d->env_rgba))
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "inconsistent environment map");
+    if ((uint64_t)d->env_w * d->env_h > (1ull << 28)) return fail(ctx, MCRT_ERR_INVALID_ARG, "environment map too large");
+    for (uint32_t i = 0; i < d->n_triangles; ++i)
+        for (int k = 0; k < 3; ++k)
+            if (d->triangles[i].v[k] >= d->n_vertices)
+                return fail(ctx, MCRT_ERR_INVALID_ARG,
+                            "triangle " + std::to_string(i) + " references a vertex beyond n_vertices");
+    std::string why;
+    if (d->mesh_bvh) {
+        if (d->n_triangles == 0 || d->n_mesh_nodes == 0) return fail(ctx, MCRT_ERR_INVALID_ARG, "empty mesh BVH");
+        if (!valid_bvh(d->mesh_bvh, d->n_mesh_nodes, d->n_triangles, &why))
+            return fail(ctx, MCRT_ERR_INVALID_ARG, "mesh BVH: " + why);
+        if (d->triangle_order && !valid_permutation(d->triangle_order, d->n_triangles))
+            return fail(ctx, MCRT_ERR_INVALID_ARG, "triangle_order is not a permutation");
+    }
+    if (d->sphere_bvh) {
+        if (d->n_spheres == 0 || d->n_sphere_nodes == 0) return fail(ctx, MCRT_ERR_INVALID_ARG, "empty sphere BVH");
+        if (!valid_bvh(d->sphere_bvh, d->n_sphere_nodes, d->n_spheres, &why))
+            return fail(ctx, MCRT_ERR_INVALID_ARG, "sphere BVH: " + why);
+        if (d->sphere_order && !valid_permutation(d->sphere_order, d->n_spheres))
+            return fail(ctx, MCRT_ERR_INVALID_ARG, "sphere_order is not a permutation");
+    }
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+    ctx->has_scene = false;
+    ctx->acc_valid = false;
+    const uint32_t ns = d->n_spheres, nv = d->n_vertices, nt = d->n_triangles;
+
+    // ---- spheres, stored in BVH order, with their original ids
+    CK(ctx->spheres.ensure((size_t)ns * 32), "allocate spheres");
+    CK(ctx->sphere_ids.ensure((size_t)ns * 4), "allocate sphere ids");
+    CK(ctx->sphere_nodes.ensure((size_t)2 * ns * 48), "allocate sphere nodes");
+    ctx->n_spheres = ns;
+    ctx->n_sphere_nodes = 0;
+    if (ns) {
+        if (d->sphere_bvh) {
+            CK(cudaMemcpyAsync(ctx->spheres.p, d->spheres, (size_t)ns * 32, cudaMemcpyHostToDevice, st), "upload");
+            CK(cudaMemcpyAsync(ctx->sphere_nodes.p, d->sphere_bvh, (size_t)d->n_sphere_nodes * 48,
+                               cudaMemcpyHostToDevice, st), "upload");
+            if (d->sphere_order)
+                CK(cudaMemcpyAsync(ctx->sphere_ids.p, d->sphere_order, (size_t)ns * 4, cudaMemcpyHostToDevice, st),
+                   "upload");
+            else
+                k_iota<<<(ns + 255) / 256, 256, 0, st>>>(ctx->sphere_ids.as<uint32_t>(), ns); ::mcrt::note_launch();
+            ctx->n_sphere_nodes = d->n_sphere_nodes;
+        } else {
+            CK(ctx->staging.ensure((size_t)ns * 32), "allocate staging");
+            CK(cudaMemcpyAsync(ctx->staging.p, d->spheres, (size_t)ns * 32, cudaMemcpyHostToDevice, st), "upload");
+            uint32_t nn = 0;
+            std::string err;
+            cudaError_t e = mcrt::gpu_build_sphere_bvh(ctx->staging.as<mcrt_gpu_sphere>(), ns,
+                                                       ctx->sphere_nodes.as<mcrt_gpu_bvh_node>(),
+                                                       ctx->sphere_ids.as<uint32_t>(), &nn, &ctx->bvh_scratch, st,
+                                                       &err);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "sphere BVH build: " + err);
+            k_gather_spheres<<<(ns + 255) / 256, 256, 0, st>>>(ctx->staging.as<mcrt_gpu_sphere>(),
+                                                               ctx->sphere_ids.as<uint32_t>(), ns,
+                                                               ctx->spheres.as<mcrt_gpu_sphere>()); ::mcrt::note_launch();
+            ctx->n_sphere_nodes = nn;
+        }
+    }
+    // ---- vertices
+    CK(ctx->vertices.ensure((size_t)nv * 48), "allocate vertices");
+    if (nv) CK(cudaMemcpyAsync(ctx->vertices.p, d->vertices, (size_t)nv * 48, cudaMemcpyHostToDevice, st), "upload");
+    ctx->n_vertices = nv;
+    // ---- triangles (kept in original order on the device) and the mesh BVH
+    CK(ctx->triangles.ensure((size_t)nt * 16), "allocate triangles");
+    CK(ctx->tri_order.ensure((size_t)nt * 4), "allocate triangle order");
+    CK(ctx->mesh_nodes.ensure((size_t)2 * nt * 48), "allocate mesh nodes");
+    ctx->n_triangles = nt;
+    ctx->n_mesh_nodes = 0;
+    if (nt) {
+        if (d->mesh_bvh) {
+            CK(ctx->staging.ensure((size_t)nt * 16), "allocate staging");
+            CK(cudaMemcpyAsync(ctx->staging.p, d->triangles, (size_t)nt * 16, cudaMemcpyHostToDevice, st), "upload");
+            if (d->triangle_order)
+                CK(cudaMemcpyAsync(ctx->tri_order.p, d->triangle_order, (size_t)nt * 4, cudaMemcpyHostToDevice, st),
+                   "upload");
+            else
+                k_iota<<<(nt + 255) / 256, 256, 0, st>>>(ctx->tri_order.as<uint32_t>(), nt); ::mcrt::note_launch();
+            k_scatter_tris<<<(nt + 255) / 256, 256, 0, st>>>(ctx->staging.as<mcrt_gpu_triangle>(),
+                                                             ctx->tri_order.as<uint32_t>(), nt,
+                                                             ctx->triangles.as<mcrt_gpu_triangle>()); ::mcrt::note_launch();
+            CK(cudaMemcpyAsync(ctx->mesh_nodes.p, d->mesh_bvh, (size_t)d->n_mesh_nodes * 48, cudaMemcpyHostToDevice,
+                               st), "upload");
+            ctx->n_mesh_nodes = d->n_mesh_nodes;
+            mcrt_status s = finish_mesh(ctx);
+            if (s != MCRT_OK) return s;
+        } else {
+            CK(cudaMemcpyAsync(ctx->triangles.p, d->triangles, (size_t)nt * 16, cudaMemcpyHostToDevice, st), "upload");
+            mcrt_status s = build_mesh_bvh_gpu(ctx);
+            if (s != MCRT_OK) return s;
+        }
+    } else {
+        ctx->n_cnodes = 0;
+    }
+    // ---- materials, environment
+    CK(ctx->materials.ensure(sizeof(mcrt_gpu_material_data)), "allocate materials");
+    CK(cudaMemcpyAsync(ctx->materials.p, d->materials, sizeof(mcrt_gpu_material_data), cudaMemcpyHostToDevice, st),
+       "upload");
+    ctx->env_w = d->env_w;
+    ctx->env_h = d->env_h;
+    CK(ctx->env.ensure((size_t)d->env_w * d->env_h * 16), "allocate env map");
+    if (d->env_w)
+        CK(cudaMemcpyAsync(ctx->env.p, d->env_rgba, (size_t)d->env_w * d->env_h * 16, cudaMemcpyHostToDevice, st),
+           "upload");
+    // ---- lights: emissive triangles by original id, emissive spheres by ordered slot
+    std::vector<uint32_t> lights;
+    auto emissive = [&](uint32_t mat) {
+        const mcrt_gpu_material &m = d->materials->materials[std::min(mat & 0x7fffffffu, 63u)];
+        return m.type_pad[0] == MCRT_MAT_EMISSIVE;
+    };
+    for (uint32_t i = 0; i < nt; ++i) {
+        uint32_t id = (d->mesh_bvh && d->triangle_order) ? d->triangle_order[i] : i;
+        if (emissive(d->triangles[i].mat_idx)) lights.push_back(id);
+    }
+    std::sort(lights.begin(), lights.end());
+    if (ns) {
+        std::vector<mcrt_gpu_sphere> ordered(ns);
+        CK(cudaMemcpyAsync(ordered.data(), ctx->spheres.p, (size_t)ns * 32, cudaMemcpyDeviceToHost, st),
+           "read spheres");
+        CK(cudaStreamSynchronize(st), "sync");
+        for (uint32_t s = 0; s < ns; ++s)
+            if (emissive(ordered[s].mat_and_pad[0])) lights.push_back(s | MCRT_HIT_SPHERE);
+    }
+    ctx->n_lights = (uint32_t)lights.size();
+    CK(ctx->lights.ensure(lights.size() * 4), "allocate lights");
+    if (!lights.empty())
+        CK(cudaMemcpyAsync(ctx->lights.p, lights.data(), lights.size() * 4, cudaMemcpyHostToDevice, st), "upload");
+    mcrt_status s = finish_lights(ctx);
+    if (s != MCRT_OK) return s;
+    CK(cudaStreamSynchronize(st), "scene upload");
+    ctx->has_scene = true;
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_update_vertices(mcrt_ctx *ctx, const mcrt_gpu_vertex *vertices, uint32_t n_vertices) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!ctx->has_scene) return fail(ctx, MCRT_ERR_NO_SCENE, "no scene uploaded");
+    if (n_vertices != ctx->n_vertices || (n_vertices && !vertices))
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "vertex count differs from the uploaded scene");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    ctx->acc_valid = false;
+    if (n_vertices)
+        CK(cudaMemcpyAsync(ctx->vertices.p, vertices, (size_t)n_vertices * 48, cudaMemcpyHostToDevice, ctx->stream),
+           "upload vertices");
+    if (ctx->n_triangles) {
+        mcrt_status s = build_mesh_bvh_gpu(ctx);
+        if (s != MCRT_OK) return s;
+    }
+    return finish_lights(ctx);
+}
+
+mcrt_status mcrt_get_mesh_bvh(mcrt_ctx *ctx, mcrt_gpu_bvh_node *out_nodes, uint32_t capacity, uint32_t *out_n_nodes,
+                              uint32_t *out_order) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!ctx->has_scene) return fail(ctx, MCRT_ERR_NO_SCENE, "no scene uploaded");
+    if (out_n_nodes) *out_n_nodes = ctx->n_mesh_nodes;
+    if (out_nodes) {
+        if (capacity < ctx->n_mesh_nodes) return fail(ctx, MCRT_ERR_INVALID_ARG, "capacity too small");
+        CK(cudaMemcpyAsync(out_nodes, ctx->mesh_nodes.p, (size_t)ctx->n_mesh_nodes * 48, cudaMemcpyDeviceToHost,
+                           ctx->stream), "read nodes");
+    }
+    if (out_order && ctx->n_triangles)
+        CK(cudaMemcpyAsync(out_order, ctx->tri_order.p, (size_t)ctx->n_triangles * 4, cudaMemcpyDeviceToHost,
+                           ctx->stream), "read order");
+    CK(cudaStreamSynchronize(ctx->stream), "read BVH");
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_trace_closest(mcrt_ctx *ctx, const mcrt_ray *rays, uint32_t n, mcrt_hit *hits, uint32_t flags) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!ctx->has_scene) return fail(ctx, MCRT_ERR_NO_SCENE, "no scene uploaded");
+    if (n && (!rays || !hits)) return fail(ctx, MCRT_ERR_INVALID_ARG, "rays or hits is NULL");
+    for (uint32_t i = 0; i < n; ++i)
+        if (!(rays[i].tmin > 0.0f)) return fail(ctx, MCRT_ERR_INVALID_ARG, "ray.tmin must be > 0");
+    if (n == 0) return MCRT_OK;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+    CK(ctx->io_a.ensure((size_t)n * 32), "allocate rays");
+    CK(ctx->io_b.ensure((size_t)n * 16), "allocate hits");
+    CK(ctx->counters.ensure(64), "allocate counters");
+    CK(cudaMemcpyAsync(ctx->io_a.p, rays, (size_t)n * 32, cudaMemcpyHostToDevice, st), "upload rays");
+    CK(cudaMemsetAsync(ctx->counters.p, 0, 64, st), "clear");
+    mcrt::DeviceScene S = device_scene(ctx);
+    mcrt::launch_trace_closest(S, ctx->io_a.as<mcrt_ray>(), n, ctx->io_b.as<mcrt_hit>(),
+                               (flags & MCRT_TRACE_REFERENCE_LAYOUT) != 0, ctx->counters.as<uint32_t>(), st);
+    CK(cudaGetLastError(), "trace launch");
+    uint32_t overflow = 0;
+    CK(cudaMemcpyAsync(hits, ctx->io_b.p, (size_t)n * 16, cudaMemcpyDeviceToHost, st), "read hits");
+    CK(cudaMemcpyAsync(&overflow, ctx->counters.p, 4, cudaMemcpyDeviceToHost, st), "read flag");
+    CK(cudaStreamSynchronize(st), "trace");
+    if (overflow) return fail(ctx, MCRT_ERR_STACK_OVERFLOW, "traversal stack bound reached");
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_render(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t w, uint32_t h, uint32_t spp,
+                        uint32_t first_frame, const mcrt_render_opts *opts, float *out_rgba, double *accum_rgb,
+                        float *out_gbuf) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!ctx->has_scene) return fail(ctx, MCRT_ERR_NO_SCENE, "no scene uploaded");
+    if (!cam) return fail(ctx, MCRT_ERR_INVALID_ARG, "cam is NULL");
+    if (w == 0 || h == 0 || spp == 0) return fail(ctx, MCRT_ERR_INVALID_ARG, "width, height and spp must be > 0");
+    if ((uint64_t)w * h > (1ull << 26)) return fail(ctx, MCRT_ERR_INVALID_ARG, "image too large (max 2^26 pixels)");
+    mcrt_render_opts o{};
+    if (opts) o = *opts;
+    const uint32_t depth = o.max_depth ? o.max_depth : mcrt::kDefaultBounces;
+    if (depth > 1024) return fail(ctx, MCRT_ERR_INVALID_ARG, "max_depth too large");
+    const uint32_t npix = w * h;
+    const bool keep = (o.flags & MCRT_RENDER_KEEP_ACCUM) != 0;
+    if (keep && (!ctx->acc_valid || ctx->acc_w != w || ctx->acc_h != h))
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "KEEP_ACCUM needs a previous render of the same size");
+    // samples traced at once: enough paths in flight to fill the GPU, bounded memory
+    const uint64_t kTargetSlots = 1ull << 22, kMaxSlots = 1ull << 24;
+    uint32_t spp_pass = o.spp_per_pass;
+    if (spp_pass == 0) spp_pass = (uint32_t)std::max<uint64_t>(1, (kTargetSlots + npix - 1) / npix);
+    spp_pass = std::min(spp_pass, spp);
+    spp_pass = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(spp_pass, kMaxSlots / npix));
+    const uint32_t n_slots = npix * spp_pass;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+    // ---- buffers
+    if (ctx->pb.n_slots < n_slots) {
+        size_t per = 16 * 3 + 16 * 4 + 16 + 16 * 3;   // thr L aux, q_o q_d x2, hits, sh o d c
+        CK(ctx->pbmem.ensure((size_t)n_slots * per + 256), "allocate path state");
+        char *p = ctx->pbmem.as<char>();
+        auto take = [&](size_t bytes) { char *r = p; p += bytes; return r; };
+        ctx->pb.thr = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
+        ctx->pb.L = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
+        ctx->pb.aux = reinterpret_cast<uint4 *>(take((size_t)n_slots * 16));
+        for (int k = 0; k < 2; ++k) {
+            ctx->pb.q_o[k] = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
+            ctx->pb.q_d[k] = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
+        }
+        ctx->pb.hits = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
+        ctx->pb.sh_o = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
+        ctx->pb.sh_d = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
+        ctx->pb.sh_c = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
+        ctx->pb.n_slots = n_slots;
+    }
+    CK(ctx->counters.ensure(256), "allocate counters");
+    ctx->pb.counters = ctx->counters.as<uint32_t>();
+    ctx->pb.stats = reinterpret_cast<unsigned long long *>(ctx->counters.as<char>() + 128);
+    if (!keep || ctx->acc_w != w || ctx->acc_h != h) {
+        CK(ctx->mean.ensure((size_t)npix * 16), "allocate accumulation");
+        CK(ctx->sum.ensure((size_t)npix * 24), "allocate accumulation");
+        CK(ctx->gbuf.ensure((size_t)npix * 16), "allocate G-buffer");
+        ctx->acc_w = w;
+        ctx->acc_h = h;
+    }
+    CK(cudaMemsetAsync(ctx->counters.p, 0, 256, st), "clear counters");
+    mcrt::DeviceScene S = device_scene(ctx);
+    const bool want_gbuf = true;
+    // ---- passes
+    const unsigned long long launches0 = mcrt::launch_count();
+    unsigned long long extend_launches = 0;
+    size_t evi = 2;
+    std::vector<std::pair<size_t, int>> marks;   // (event index, category)
+    cudaEvent_t e_begin = ev(ctx, evi++);
+    cudaEventRecord(e_begin, st);
+    const bool nee = (o.flags & MCRT_RENDER_NEE) != 0 && ctx->n_lights > 0;
+    uint32_t done = 0;
+    bool first_pass = true;
+    while (done < spp) {
+        mcrt::RenderParams P{};
+        P.w = w; P.h = h; P.npix = npix;
+        P.spp_pass = std::min(spp_pass, spp - done);
+        P.frame0 = first_frame + done;
+        P.max_depth = depth;
+        P.flags = o.flags;
+        P.cam = *cam;
+        const bool last_pass = done + P.spp_pass >= spp;
+        P.gbuf_plane = (want_gbuf && last_pass) ? (int)P.spp_pass - 1 : -1;
+        mcrt::launch_raygen(S, P, ctx->pb, st);
+        int qi = 0;
+        for (uint32_t b = 0; b < depth; ++b) {
+            size_t a0 = evi++;
+            cudaEventRecord(ev(ctx, a0), st);
+            mcrt::launch_extend(S, P, ctx->pb, qi, st);
+            ++extend_launches;
+            size_t a1 = evi++;
+            cudaEventRecord(ev(ctx, a1), st);
+            mcrt::launch_shade(S, P, ctx->pb, qi, b, ctx->gbuf.as<float4>(), st);
+            size_t a2 = evi++;
+            cudaEventRecord(ev(ctx, a2), st);
+            marks.push_back({a0, 1});
+            marks.push_back({a1, 2});
+            if (nee) {
+                mcrt::launch_shadow(S, P, ctx->pb, st);
+                size_t a3 = evi++;
+                cudaEventRecord(ev(ctx, a3), st);
+                marks.push_back({a2, 3});
+            }
+            qi ^= 1;
+        }
+        size_t r0 = evi++;
+        cudaEventRecord(ev(ctx, r0), st);
+        mcrt::launch_resolve(P, ctx->pb, ctx->mean.as<float4>(), ctx->sum.as<double>(), keep || !first_pass, st);
+        size_t r1 = evi++;
+        cudaEventRecord(ev(ctx, r1), st);
+        marks.push_back({r0, 4});
+        (void)r1;
+        done += P.spp_pass;
+        first_pass = false;
+    }
+    cudaEvent_t e_end = ev(ctx, evi++);
+    cudaEventRecord(e_end, st);
+    CK(cudaGetLastError(), "render launch");
+    CK(cudaEventSynchronize(e_end), "render");
+    ctx->last_render_launches = mcrt::launch_count() - launches0;
+    ctx->last_extend_launches = extend_launches;
+    ctx->acc_valid = true;
+    ctx->gbuf_valid = want_gbuf;
+    // ---- timings
+    float ms[6] = {0, 0, 0, 0, 0, ctx->last_build_ms};
+    cudaEventElapsedTime(&ms[0], e_begin, e_end);
+    for (auto &m : marks) {
+        float t = 0.0f;
+        cudaEventElapsedTime(&t, ev(ctx, m.first), ev(ctx, m.first + 1));
+        ms[m.second] += t;
+    }
+    std::memcpy(ctx->last_ms, ms, sizeof(ms));
+    uint32_t ctr[4];
+    CK(cudaMemcpy(ctr, ctx->counters.p, 16, cudaMemcpyDeviceToHost), "read counters");
+    CK(cudaMemcpy(ctx->last_counts, ctx->pb.stats, 16, cudaMemcpyDeviceToHost), "read counters");
+    if (ctr[3]) return fail(ctx, MCRT_ERR_STACK_OVERFLOW, "traversal stack bound reached");
+    // ---- outputs
+    if (out_rgba)
+        CK(cudaMemcpyAsync(out_rgba, ctx->mean.p, (size_t)npix * 16, cudaMemcpyDeviceToHost, st), "read image");
+    if (accum_rgb) {
+        std::vector<double> tmp((size_t)npix * 3);
+        CK(cudaMemcpyAsync(tmp.data(), ctx->sum.p, (size_t)npix * 24, cudaMemcpyDeviceToHost, st), "read sums");
+        CK(cudaStreamSynchronize(st), "read sums");
+        for (size_t i = 0; i < tmp.size(); ++i) accum_rgb[i] += tmp[i];
+    }
+    if (out_gbuf)
+        CK(cudaMemcpyAsync(out_gbuf, ctx->gbuf.p, (size_t)npix * 16, cudaMemcpyDeviceToHost, st), "read G-buffer");
+    CK(cudaStreamSynchronize(st), "render outputs");
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_read_accum(mcrt_ctx *ctx, float *out_rgba, double *accum_rgb, float *out_gbuf) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!ctx->acc_valid) return fail(ctx, MCRT_ERR_INVALID_ARG, "no render to read");
+    size_t npix = (size_t)ctx->acc_w * ctx->acc_h;
+    cudaStream_t st = ctx->stream;
+    if (out_rgba) CK(cudaMemcpyAsync(out_rgba, ctx->mean.p, npix * 16, cudaMemcpyDeviceToHost, st), "read image");
+    if (accum_rgb) {
+        std::vector<double> tmp(npix * 3);
+        CK(cudaMemcpyAsync(tmp.data(), ctx->sum.p, npix * 24, cudaMemcpyDeviceToHost, st), "read sums");
+        CK(cudaStreamSynchronize(st), "read sums");
+        for (size_t i = 0; i < tmp.size(); ++i) accum_rgb[i] += tmp[i];
+    }
+    if (out_gbuf && ctx->gbuf_valid)
+        CK(cudaMemcpyAsync(out_gbuf, ctx->gbuf.p, npix * 16, cudaMemcpyDeviceToHost, st), "read G-buffer");
+    CK(cudaStreamSynchronize(st), "read accumulation");
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_last_timings(mcrt_ctx *ctx, float *out_ms, uint64_t *out_counts) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (out_ms) {
+        std::memcpy(out_ms, ctx->last_ms, sizeof(ctx->last_ms));
+        out_ms[5] = ctx->last_build_ms;
+    }
+    if (out_counts) {
+        out_counts[0] = ctx->last_counts[0];
+        out_counts[1] = ctx->last_counts[1];
+        out_counts[2] = ctx->last_render_launches;
+        out_counts[3] = ctx->last_build_launches;
+        out_counts[4] = ctx->last_extend_launches;
+    }
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_rebuild_bvh(mcrt_ctx *ctx) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!ctx->has_scene) return fail(ctx, MCRT_ERR_NO_SCENE, "no scene uploaded");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    ctx->acc_valid = false;
+    if (ctx->n_triangles) {
+        mcrt_status s = build_mesh_bvh_gpu(ctx);
+        if (s != MCRT_OK) return s;
+    }
+    return finish_lights(ctx);
+}
+
+mcrt_status mcrt_denoise(mcrt_ctx *ctx, const float *in_rgba, const float *gbuf, uint32_t w, uint32_t h,
+                         const mcrt_denoise_params *params, float *out_rgba) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!in_rgba || !gbuf || !out_rgba || !params) return fail(ctx, MCRT_ERR_INVALID_ARG, "NULL argument");
+    if (w == 0 || h == 0 || (uint64_t)w * h > (1ull << 28)) return fail(ctx, MCRT_ERR_INVALID_ARG, "bad image size");
+    if (params->radius < 0 || params->radius > 64) return fail(ctx, MCRT_ERR_INVALID_ARG, "radius must be in [0, 64]");
+    if (!(params->sigma_s > 0.0f) || !(params->sigma_d > 0.0f))
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "sigma_s and sigma_d must be > 0");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+    size_t bytes = (size_t)w * h * 16;
+    CK(ctx->io_a.ensure(bytes), "allocate");
+    CK(ctx->io_b.ensure(bytes), "allocate");
+    CK(ctx->io_c.ensure(bytes), "allocate");
+    CK(cudaMemcpyAsync(ctx->io_a.p, in_rgba, bytes, cudaMemcpyHostToDevice, st), "upload");
+    CK(cudaMemcpyAsync(ctx->io_b.p, gbuf, bytes, cudaMemcpyHostToDevice, st), "upload");
+    cudaEvent_t a = ev(ctx, 0), b = ev(ctx, 1);
+    cudaEventRecord(a, st);
+    mcrt::launch_denoise(ctx->io_a.as<float4>(), ctx->io_b.as<float4>(), w, h, *params, ctx->io_c.as<float4>(), st);
+    cudaEventRecord(b, st);
+    CK(cudaGetLastError(), "denoise launch");
+    CK(cudaMemcpyAsync(out_rgba, ctx->io_c.p, bytes, cudaMemcpyDeviceToHost, st), "read");
+    CK(cudaStreamSynchronize(st), "denoise");
+    float t = 0.0f;
+    cudaEventElapsedTime(&t, a, b);
+    ctx->last_ms[0] = t;
+    return MCRT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,77 @@
+// internal.h — declarations shared between the translation units of libmcrt_cuda.so.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <cuda_runtime.h>
+
+#include "mcrt_cuda.h"
+
+namespace mcrt {
+
+// Process-wide count of kernel launches issued by this library (every launch
+// site calls note_launch()); reported per call by mcrt_last_timings.
+void note_launch();
+unsigned long long launch_count();
+
+struct DeviceScene;
+
+// Path state for one render pass (structure of arrays, n_slots entries).
+struct PathBuffers {
+    uint32_t n_slots = 0;
+    float4 *thr = nullptr;       // throughput rgb | previous-bounce BSDF pdf (< 0: no MIS)
+    float4 *L = nullptr;         // radiance rgb | unused
+    uint4 *aux = nullptr;        // rng | pixel | frame | flags
+    float4 *q_o[2] = {nullptr, nullptr};   // ray queues: origin | slot bits
+    float4 *q_d[2] = {nullptr, nullptr};   // direction | unused
+    float4 *hits = nullptr;      // t | prim bits | u | v, in queue order
+    float4 *sh_o = nullptr;      // shadow queue: origin | slot bits
+    float4 *sh_d = nullptr;      // direction | t_max
+    float4 *sh_c = nullptr;      // contribution rgb | unused
+    uint32_t *counters = nullptr;  // [0],[1] ray queue sizes, [2] shadow queue size, [3] overflow flag, [4..] stats
+    unsigned long long *stats = nullptr;  // [0] rays traced, [1] shadow rays
+};
+
+struct RenderParams {
+    uint32_t w, h, npix;
+    uint32_t spp_pass;       // sample planes in this pass
+    uint32_t frame0;         // frame index of plane 0
+    uint32_t max_depth;
+    uint32_t flags;          // MCRT_RENDER_*
+    int32_t gbuf_plane;      // plane whose primary hit is stored in the G-buffer (-1: none)
+    mcrt_camera_uniform cam;
+};
+
+// Launchers (render.cu)
+void launch_trace_closest(const DeviceScene &S, const mcrt_ray *rays, uint32_t n, mcrt_hit *hits, bool ref_layout,
+                          uint32_t *overflow, cudaStream_t st);
+void launch_raygen(const DeviceScene &S, const RenderParams &P, PathBuffers &B, cudaStream_t st);
+void launch_extend(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, cudaStream_t st);
+void launch_shade(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, uint32_t bounce,
+                  float4 *gbuf, cudaStream_t st);
+void launch_shadow(const DeviceScene &S, const RenderParams &P, PathBuffers &B, cudaStream_t st);
+void launch_resolve(const RenderParams &P, const PathBuffers &B, float4 *mean, double *sum, bool keep,
+                    cudaStream_t st);
+
+// BVH (bvh_build.cu)
+struct BvhScratch;
+// Build the reference-layout mesh BVH on the GPU (bvh.rs / mesh.rs algorithm).
+cudaError_t gpu_build_mesh_bvh(const mcrt_gpu_vertex *d_verts, const mcrt_gpu_triangle *d_tris, uint32_t nt,
+                               mcrt_gpu_bvh_node *d_nodes, uint32_t *d_order, uint32_t *n_nodes_out,
+                               BvhScratch **scratch, cudaStream_t st, std::string *err);
+void free_bvh_scratch(BvhScratch *s);
+// Convert a reference-layout mesh BVH into the compact layout and the leaf-ordered triangle records.
+cudaError_t gpu_make_compact(const mcrt_gpu_bvh_node *d_nodes, uint32_t n_nodes, const uint32_t *d_order,
+                             const mcrt_gpu_vertex *d_verts, const mcrt_gpu_triangle *d_tris, uint32_t nt,
+                             float4 **d_cnodes, uint32_t *n_cnodes, void *d_trirecs, uint32_t *d_tmp,
+                             size_t tmp_words, cudaStream_t st);
+
+// Denoiser (denoise.cu)
+void launch_denoise(const float4 *in, const float4 *gbuf, uint32_t w, uint32_t h, const mcrt_denoise_params &p,
+                    float4 *out, cudaStream_t st);
+
+// scan utility (bvh_build.cu)
+size_t scan_tmp_words(uint32_t n);
+void exclusive_scan_u32(const uint32_t *d_in, uint32_t *d_out, uint32_t n, uint32_t *d_tmp, cudaStream_t st);
+
+}  // namespace mcrt

@@ -1,0 +1,647 @@
+// render.cu — wavefront path tracer kernels: ray generation, closest-hit
+// extension, shading (reference estimator or next-event estimation with MIS),
+// shadow rays and per-pixel resolve; plus the closest-hit parity probe.
+//
+// One render pass traces `spp_pass` sample planes of the image at once (slot =
+// plane * npix + pixel).  Each bounce is extend -> shade (-> shadow); shade
+// appends surviving paths to the next ray queue with warp-aggregated atomics
+// (one atomicAdd per warp), so later bounces run on compacted queues.  All
+// per-path state is indexed by slot and every path owns its radiance, so the
+// result is independent of queue order (deterministic, no float atomics).
+#include "common.cuh"
+#include "internal.h"
+#include "traverse.cuh"
+
+namespace mcrt {
+
+namespace {
+
+constexpr uint32_t kMatMetal = 1u, kMatDielectric = 2u, kMatEmissive = 3u, kMatGgx = 4u;
+constexpr uint32_t kFlagSpecular = 1u;   // aux.w: last bounce had no MIS-able pdf
+
+inline int grid_blocks_for(uint32_t n, int threads) { return (int)((n + threads - 1) / threads); }
+
+// ------------------------------------------------------------------ sampling (path_trace.wgsl:210-227)
+__device__ __forceinline__ f3 random_unit_sphere(uint32_t &rng) {
+    float cos_phi = 1.0f - 2.0f * rand_f32(rng);
+    float sin_phi = sqrtf(fmaxf(0.0f, 1.0f - cos_phi * cos_phi));
+    float theta = kTau * rand_f32(rng);
+    float s, c;
+    dm_sincos(theta, &s, &c);
+    return {sin_phi * c, sin_phi * s, cos_phi};
+}
+__device__ __forceinline__ f3 cosine_scatter(uint32_t &rng, f3 n) {
+    f3 sc = n + random_unit_sphere(rng);
+    if (dot(sc, sc) < 1e-6f) return n;
+    return normalize(sc);
+}
+
+// sample_env_map, path_trace.wgsl:233-242
+__device__ __forceinline__ f3 sample_env(const DeviceScene &S, f3 d) {
+    if (S.env_w == 0 || S.env_h == 0) return {0.0f, 0.0f, 0.0f};
+    float phi = dm_atan2(d.z, d.x);
+    float theta = dm_asin(fminf(fmaxf(d.y, -1.0f), 1.0f));
+    float u = phi / kTau + 0.5f;
+    float v = 0.5f - theta / kPi;
+    uint32_t ix = f2u_sat(u * (float)S.env_w) % S.env_w;
+    uint32_t iy = f2u_sat(v * (float)S.env_h) % S.env_h;
+    return xyz(__ldg(S.env + (size_t)iy * S.env_w + ix));
+}
+
+// path_trace.wgsl:485-500
+__device__ __forceinline__ f3 reflect_vec(f3 v, f3 n) { return v - (2.0f * dot(v, n)) * n; }
+__device__ __forceinline__ f3 refract_vec(f3 v, f3 n, float eta) {
+    float cos_theta = fminf(dot(-v, n), 1.0f);
+    f3 r_perp = eta * (v + cos_theta * n);
+    f3 r_para = (-sqrtf(fmaxf(0.0f, 1.0f - dot(r_perp, r_perp)))) * n;
+    return r_perp + r_para;
+}
+__device__ __forceinline__ float schlick(float cos_theta, float eta) {
+    float r0 = (1.0f - eta) / (1.0f + eta);
+    r0 = r0 * r0;
+    return r0 + (1.0f - r0) * dm_pow(1.0f - cos_theta, 5.0f);
+}
+
+// cs_main ray generation, path_trace.wgsl:636-652
+__device__ __forceinline__ void camera_ray(const mcrt_camera_uniform &cam, uint32_t x, uint32_t y, uint32_t w,
+                                           uint32_t h, uint32_t &rng, f3 *o_out, f3 *d_out) {
+    float u = ((float)x + rand_f32(rng)) / (float)w;
+    float v = 1.0f - ((float)y + rand_f32(rng)) / (float)h;
+    f3 focal = (ld3(cam.lower_left) + u * ld3(cam.horizontal)) + v * ld3(cam.vertical);
+    float r = sqrtf(rand_f32(rng));
+    float theta = kTau * rand_f32(rng);
+    float s, c;
+    dm_sincos(theta, &s, &c);
+    float lx = r * c, ly = r * s;
+    f3 lens = lx * ld3(cam.defocus_u) + ly * ld3(cam.defocus_v);
+    f3 o = ld3(cam.origin) + lens;
+    *o_out = o;
+    *d_out = normalize(focal - o);
+}
+
+struct SurfaceHit { float t; f3 p; f3 n; bool front; uint32_t mat; };
+
+__device__ __forceinline__ SurfaceHit surface(const DeviceScene &S, f3 o, f3 d, float4 h) {
+    SurfaceHit s;
+    s.t = h.x;
+    s.p = o + h.x * d;                                          // path_trace.wgsl:283, :455
+    uint32_t prim = __float_as_uint(h.y);
+    if (prim & MCRT_HIT_SPHERE) {                               // :282-287
+        uint32_t slot = __float_as_uint(h.z);
+        float4 cr = __ldg(reinterpret_cast<const float4 *>(S.spheres + slot));
+        f3 outn = (s.p - xyz(cr)) / cr.w;
+        s.front = dot(d, outn) < 0.0f;
+        s.n = s.front ? outn : -outn;
+        s.mat = S.spheres[slot].mat_and_pad[0];
+    } else {                                                    // :444-459
+        f3 n = tri_shading_normal(S, prim, h.z, h.w);
+        s.front = dot(d, n) < 0.0f;
+        s.n = s.front ? n : -n;
+        s.mat = S.triangles[prim].mat_idx & 0x7fffffffu;
+    }
+    return s;
+}
+
+// GGX conductor (extension): Trowbridge-Reitz distribution, Smith
+// height-correlated masking-shadowing, Schlick Fresnel with F0 = albedo;
+// sampled by visible normals (Heitz 2018, "Sampling the GGX Distribution of
+// Visible Normals", JCGT 7(4)).
+__device__ __forceinline__ void onb(f3 n, f3 *t, f3 *b) {
+    // Duff et al. 2017, "Building an Orthonormal Basis, Revisited"
+    float sign = n.z >= 0.0f ? 1.0f : -1.0f;
+    float a = -1.0f / (sign + n.z);
+    float bb = n.x * n.y * a;
+    *t = mk3(1.0f + sign * n.x * n.x * a, sign * bb, -sign * n.x);
+    *b = mk3(bb, sign + n.y * n.y * a, -n.y);
+}
+__device__ __forceinline__ float ggx_lambda(float alpha, float cos_t) {
+    float c2 = cos_t * cos_t;
+    float t2 = fmaxf(0.0f, 1.0f - c2) / fmaxf(c2, 1e-12f);
+    return 0.5f * (-1.0f + sqrtf(1.0f + alpha * alpha * t2));
+}
+__device__ __forceinline__ float ggx_d(float alpha, float cos_h) {
+    float a2 = alpha * alpha;
+    float c2 = cos_h * cos_h;
+    float den = c2 * (a2 - 1.0f) + 1.0f;
+    return a2 / (kPi * den * den);
+}
+// Sample wi for wo (both in the local frame, z = normal); returns the weight f*cos/pdf.
+__device__ __forceinline__ bool ggx_sample(f3 wo, float alpha, f3 f0, float r1, float r2, f3 *wi_out, f3 *weight,
+                                           float *pdf_out) {
+    // stretch
+    f3 vh = normalize(mk3(alpha * wo.x, alpha * wo.y, wo.z));
+    float lensq = vh.x * vh.x + vh.y * vh.y;
+    f3 t1 = lensq > 0.0f ? mk3(-vh.y, vh.x, 0.0f) / sqrtf(lensq) : mk3(1.0f, 0.0f, 0.0f);
+    f3 t2 = cross(vh, t1);
+    float r = sqrtf(r1);
+    float phi = 2.0f * kPi * r2;
+    float sp, cp;
+    dm_sincos(phi, &sp, &cp);
+    float p1 = r * cp;
+    float p2 = r * sp;
+    float s = 0.5f * (1.0f + vh.z);
+    p2 = (1.0f - s) * sqrtf(fmaxf(0.0f, 1.0f - p1 * p1)) + s * p2;
+    f3 nh = (p1 * t1 + p2 * t2) + sqrtf(fmaxf(0.0f, 1.0f - p1 * p1 - p2 * p2)) * vh;
+    f3 m = normalize(mk3(alpha * nh.x, alpha * nh.y, fmaxf(1e-6f, nh.z)));
+    float wo_m = dot(wo, m);
+    f3 wi = (2.0f * wo_m) * m - wo;
+    if (wi.z <= 0.0f) return false;
+    float l_o = ggx_lambda(alpha, wo.z), l_i = ggx_lambda(alpha, wi.z);
+    float g1 = 1.0f / (1.0f + l_o);
+    float g2 = 1.0f / ((1.0f + l_o) + l_i);
+    float fw = dm_pow(1.0f - fmaxf(0.0f, wo_m), 5.0f);
+    f3 F = f0 + fw * (mk3(1.0f, 1.0f, 1.0f) - f0);
+    *weight = (g2 / g1) * F;
+    // pdf(wi) = D_v(m) / (4 wo.m) = G1(wo) max(0, wo.m) D(m) / (wo.z 4 wo.m)
+    *pdf_out = g1 * ggx_d(alpha, m.z) / (4.0f * wo.z);
+    *wi_out = wi;
+    return true;
+}
+__device__ __forceinline__ f3 ggx_eval(f3 wo, f3 wi, float alpha, f3 f0, float *pdf_out) {
+    // returns f * cos(wi)
+    *pdf_out = 0.0f;
+    if (wo.z <= 0.0f || wi.z <= 0.0f) return mk3(0.0f, 0.0f, 0.0f);
+    f3 m = normalize(wo + wi);
+    float l_o = ggx_lambda(alpha, wo.z), l_i = ggx_lambda(alpha, wi.z);
+    float g1 = 1.0f / (1.0f + l_o);
+    float g2 = 1.0f / ((1.0f + l_o) + l_i);
+    float D = ggx_d(alpha, m.z);
+    float wo_m = dot(wo, m);
+    float fw = dm_pow(1.0f - fmaxf(0.0f, wo_m), 5.0f);
+    f3 F = f0 + fw * (mk3(1.0f, 1.0f, 1.0f) - f0);
+    *pdf_out = g1 * D / (4.0f * wo.z);
+    return (D * g2 / (4.0f * wo.z)) * F;
+}
+
+// ------------------------------------------------------------------ light sampling (NEE)
+// Lights are the emissive triangles (by original id) and emissive spheres (by
+// ordered slot | MCRT_HIT_SPHERE).  A light is chosen with probability
+// proportional to area * luminance(emission); the same weight function is
+// evaluated when a BSDF-sampled ray hits an emitter, for the MIS weight.
+__device__ __forceinline__ float luminance(f3 c) { return (0.2126f * c.x + 0.7152f * c.y) + 0.0722f * c.z; }
+
+__device__ __forceinline__ f3 emission_of(const DeviceScene &S, uint32_t mat) {
+    const mcrt_gpu_material &m = S.materials->materials[min(mat, kMaxMatIdx)];
+    if (m.type_pad[0] != kMatEmissive) return mk3(0.0f, 0.0f, 0.0f);
+    return m.ior_pad[0] * ld3(m.albedo_fuzz);
+}
+
+}  // namespace
+
+__device__ float light_weight(const DeviceScene &S, uint32_t code) {
+    if (code & MCRT_HIT_SPHERE) {
+        uint32_t slot = code & ~MCRT_HIT_SPHERE;
+        float r = S.spheres[slot].center_r[3];
+        return ((4.0f * kPi) * (r * r)) * luminance(emission_of(S, S.spheres[slot].mat_and_pad[0]));
+    }
+    mcrt_gpu_triangle tri = S.triangles[code];
+    f3 a = ld3(S.vertices[tri.v[0]].position), b = ld3(S.vertices[tri.v[1]].position),
+       c = ld3(S.vertices[tri.v[2]].position);
+    f3 ng = cross(b - a, c - a);
+    return (0.5f * sqrtf(dot(ng, ng))) * luminance(emission_of(S, tri.mat_idx & 0x7fffffffu));
+}
+
+namespace {
+
+__device__ __forceinline__ uint32_t pick_light(const DeviceScene &S, float u) {
+    uint32_t lo = 0, hi = S.n_lights;               // largest k with cdf[k] <= u
+    while (lo + 1 < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(S.light_cdf + mid) <= u) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+struct LightSample { f3 dir; float dist; float pdf; f3 Le; bool ok; };
+
+// Uniform point on an emissive triangle, or a direction in the cone subtended by
+// an emissive sphere.  pdf is per unit solid angle at x (including the choice of
+// the light).
+__device__ __forceinline__ LightSample sample_light(const DeviceScene &S, f3 x, uint32_t &rng) {
+    LightSample ls{};
+    ls.ok = false;
+    uint32_t li = pick_light(S, rand_f32(rng));
+    uint32_t code = __ldg(S.lights + li);
+    float prob = light_weight(S, code) / S.light_total;
+    float r1 = rand_f32(rng), r2 = rand_f32(rng);
+    if (!(prob > 0.0f)) return ls;
+    if (code & MCRT_HIT_SPHERE) {
+        uint32_t slot = code & ~MCRT_HIT_SPHERE;
+        float4 cr = __ldg(reinterpret_cast<const float4 *>(S.spheres + slot));
+        f3 wc = xyz(cr) - x;
+        float d2 = dot(wc, wc);
+        float r2s = cr.w * cr.w;
+        if (d2 <= r2s) return ls;
+        float dc = sqrtf(d2);
+        f3 w = wc / dc;
+        float cosmax = sqrtf(fmaxf(0.0f, 1.0f - r2s / d2));
+        if (!(cosmax < 1.0f)) return ls;
+        float cos_t = (1.0f - r1) + r1 * cosmax;
+        float sin_t = sqrtf(fmaxf(0.0f, 1.0f - cos_t * cos_t));
+        float sp, cp;
+        dm_sincos(kTau * r2, &sp, &cp);
+        f3 t, b;
+        onb(w, &t, &b);
+        f3 dir = normalize(((sin_t * cp) * t + (sin_t * sp) * b) + cos_t * w);
+        float proj = dot(wc, dir);
+        float disc = r2s - (d2 - proj * proj);
+        float dist = proj - sqrtf(fmaxf(0.0f, disc));
+        ls.dir = dir;
+        ls.dist = dist;
+        ls.pdf = prob / (kTau * (1.0f - cosmax));
+        ls.Le = emission_of(S, S.spheres[slot].mat_and_pad[0]);
+        ls.ok = dist > 0.0f;
+        return ls;
+    }
+    mcrt_gpu_triangle tri = S.triangles[code];
+    f3 a = ld3(S.vertices[tri.v[0]].position), bq = ld3(S.vertices[tri.v[1]].position),
+       cq = ld3(S.vertices[tri.v[2]].position);
+    float su = sqrtf(r1);
+    float b0 = 1.0f - su, b1 = r2 * su, b2 = (1.0f - b0) - b1;
+    f3 y = (b0 * a + b1 * bq) + b2 * cq;
+    f3 ng = cross(bq - a, cq - a);
+    float area2 = sqrtf(dot(ng, ng));
+    if (!(area2 > 0.0f)) return ls;
+    f3 wv = y - x;
+    float dist2 = dot(wv, wv);
+    float dist = sqrtf(dist2);
+    if (!(dist > 0.0f)) return ls;
+    f3 dir = wv / dist;
+    float cos_l = fabsf(dot(ng, dir)) / area2;
+    if (!(cos_l > 1e-7f)) return ls;
+    if (tri.mat_idx & MCRT_BACKFACE_CULL_FLAG) {        // invisible from behind (path_trace.wgsl:452)
+        f3 ns = tri_shading_normal(S, code, b1, b2);
+        if (!(dot(dir, ns) < 0.0f)) return ls;
+    }
+    ls.dir = dir;
+    ls.dist = dist;
+    ls.pdf = prob * dist2 / (cos_l * (0.5f * area2));
+    ls.Le = emission_of(S, tri.mat_idx & 0x7fffffffu);
+    ls.ok = true;
+    return ls;
+}
+
+// Solid-angle pdf (at the ray origin o) with which NEE would have produced the
+// emitter hit h along d.
+__device__ __forceinline__ float light_pdf_of_hit(const DeviceScene &S, float4 h, f3 o, f3 d) {
+    uint32_t prim = __float_as_uint(h.y);
+    if (prim & MCRT_HIT_SPHERE) {
+        uint32_t slot = __float_as_uint(h.z);
+        float prob = light_weight(S, slot | MCRT_HIT_SPHERE) / S.light_total;
+        float4 cr = __ldg(reinterpret_cast<const float4 *>(S.spheres + slot));
+        f3 wc = xyz(cr) - o;
+        float d2 = dot(wc, wc);
+        float r2s = cr.w * cr.w;
+        if (d2 <= r2s) return 0.0f;
+        float cosmax = sqrtf(fmaxf(0.0f, 1.0f - r2s / d2));
+        if (!(cosmax < 1.0f)) return 0.0f;
+        return prob / (kTau * (1.0f - cosmax));
+    }
+    float prob = light_weight(S, prim) / S.light_total;
+    mcrt_gpu_triangle tri = S.triangles[prim];
+    f3 a = ld3(S.vertices[tri.v[0]].position), bq = ld3(S.vertices[tri.v[1]].position),
+       cq = ld3(S.vertices[tri.v[2]].position);
+    f3 ng = cross(bq - a, cq - a);
+    float area2 = sqrtf(dot(ng, ng));
+    if (!(area2 > 0.0f)) return 0.0f;
+    float cos_l = fabsf(dot(ng, d)) / area2;
+    if (!(cos_l > 1e-7f)) return 0.0f;
+    float t = h.x;
+    return prob * (t * t) / (cos_l * (0.5f * area2));
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ kernels
+
+__global__ void k_trace_closest(DeviceScene S, const mcrt_ray *rays, uint32_t n, mcrt_hit *hits, int ref_layout,
+                                uint32_t *overflow) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    mcrt_ray ry = rays[i];
+    RayInv r = make_ray(mk3(ry.org[0], ry.org[1], ry.org[2]), mk3(ry.dir[0], ry.dir[1], ry.dir[2]));
+    uint32_t nn = 0;
+    Closest c = world_hit(S, r, ry.tmin, ry.tmax, ref_layout != 0, &nn, overflow);
+    mcrt_hit h;
+    h.t = c.t;
+    h.prim = c.prim;
+    h.u = c.u;
+    h.v = c.v;
+    hits[i] = h;
+}
+
+__global__ void k_raygen(DeviceScene S, RenderParams P, PathBuffers B) {
+    uint32_t n = P.npix * P.spp_pass;
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) { B.counters[0] = n; B.counters[1] = 0; B.counters[2] = 0; }
+    if (i >= n) return;
+    uint32_t k = i / P.npix;
+    uint32_t p = i - k * P.npix;
+    uint32_t x = p % P.w, y = p / P.w;
+    uint32_t frame = P.frame0 + k;
+    uint32_t rng = pcg_hash(pcg_hash(x + y * P.w) ^ (frame * 2654435761u));   // path_trace.wgsl:636-637
+    f3 o, d;
+    camera_ray(P.cam, x, y, P.w, P.h, rng, &o, &d);
+    B.thr[i] = make_float4(1.0f, 1.0f, 1.0f, -1.0f);
+    B.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    B.aux[i] = make_uint4(rng, p, frame, kFlagSpecular);
+    B.q_o[0][i] = make_float4(o.x, o.y, o.z, __uint_as_float(i));
+    B.q_d[0][i] = make_float4(d.x, d.y, d.z, 0.0f);
+}
+
+__global__ void __launch_bounds__(128) k_extend(DeviceScene S, PathBuffers B, int qi) {
+    const uint32_t n = B.counters[qi];
+    if (blockIdx.x == 0 && threadIdx.x == 0) { B.counters[qi ^ 1] = 0; B.counters[2] = 0; }
+    const float4 *qo = B.q_o[qi];
+    const float4 *qd = B.q_d[qi];
+    uint32_t traced = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 o4 = qo[i], d4 = qd[i];
+        RayInv r = make_ray(xyz(o4), xyz(d4));
+        uint32_t nn = 0;
+        Closest c = world_hit(S, r, kTMin, kTMax, false, &nn, B.counters + 3);
+        float u = (c.prim != MCRT_HIT_MISS && (c.prim & MCRT_HIT_SPHERE)) ? __uint_as_float(c.slot) : c.u;
+        B.hits[i] = make_float4(c.t, __uint_as_float(c.prim), u, c.v);
+        ++traced;
+    }
+    if (traced) atomicAdd(B.stats, (unsigned long long)traced);
+}
+
+__global__ void __launch_bounds__(256) k_shade(DeviceScene S, RenderParams P, PathBuffers B, int qi,
+                                                uint32_t bounce, float4 *gbuf) {
+    const uint32_t n = B.counters[qi];
+    const bool nee = (P.flags & MCRT_RENDER_NEE) != 0 && S.n_lights > 0;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        bool cont = false, shadow = false;
+        f3 no = {0, 0, 0}, nd = {0, 0, 0}, so = {0, 0, 0}, sd = {0, 0, 0}, sc = {0, 0, 0};
+        float smax = 0.0f;
+        uint32_t slot = 0;
+        if (i < n) {
+            float4 o4 = B.q_o[qi][i], d4 = B.q_d[qi][i];
+            float4 h = B.hits[i];
+            slot = __float_as_uint(o4.w);
+            f3 o = xyz(o4), d = xyz(d4);
+            float4 thr4 = B.thr[slot];
+            uint4 aux = B.aux[slot];
+            f3 thr = xyz(thr4);
+            uint32_t rng = aux.x;
+            const bool write_g = gbuf && bounce == 0 && (int)(slot / P.npix) == P.gbuf_plane;
+            if (h.x < 0.0f) {                                                   // miss, :592-597
+                if (write_g) gbuf[aux.y] = make_float4(0.0f, 0.0f, 0.0f, kTMax);
+                f3 e = thr * sample_env(S, d);
+                float4 L = B.L[slot];
+                if (nee) B.L[slot] = make_float4(L.x + e.x, L.y + e.y, L.z + e.z, 0.0f);
+                else B.L[slot] = make_float4(e.x, e.y, e.z, 0.0f);
+            } else {
+                SurfaceHit sh = surface(S, o, d, h);
+                if (write_g) gbuf[aux.y] = make_float4(sh.n.x, sh.n.y, sh.n.z, sh.t);   // :599-602
+                const mcrt_gpu_material &m = S.materials->materials[min(sh.mat, kMaxMatIdx)];
+                const uint32_t mtype = m.type_pad[0];
+                f3 albedo = ld3(m.albedo_fuzz);
+                if (mtype == kMatEmissive) {                                    // :608-610
+                    f3 e = m.ior_pad[0] * (thr * albedo);
+                    if (nee) {
+                        float wmis = 1.0f;
+                        if (!(aux.w & kFlagSpecular) && thr4.w > 0.0f) {
+                            float pl = light_pdf_of_hit(S, h, o, d);
+                            float pb = thr4.w;
+                            wmis = (pb * pb) / (pb * pb + pl * pl);
+                        }
+                        float4 L = B.L[slot];
+                        B.L[slot] = make_float4(L.x + wmis * e.x, L.y + wmis * e.y, L.z + wmis * e.z, 0.0f);
+                    } else {
+                        B.L[slot] = make_float4(e.x, e.y, e.z, 0.0f);
+                    }
+                } else {
+                    f3 dir = {0, 0, 0}, atten = {0, 0, 0};
+                    bool absorbed = false;
+                    float pdf = -1.0f;
+                    if (mtype == kMatMetal) {                                   // :530-541
+                        float fuzz = m.albedo_fuzz[3];
+                        f3 refl = reflect_vec(normalize(d), sh.n);
+                        f3 pert = refl + fuzz * random_unit_sphere(rng);
+                        dir = normalize(dot(pert, pert) >= 1e-6f ? pert : refl);
+                        atten = albedo;
+                        absorbed = dot(dir, sh.n) <= 0.0f;
+                    } else if (mtype == kMatDielectric) {                       // :543-564
+                        atten = mk3(1.0f, 1.0f, 1.0f);
+                        float ior = m.ior_pad[0];
+                        float eta = sh.front ? 1.0f / ior : ior;
+                        float cos_t = fminf(dot(-d, sh.n), 1.0f);
+                        float sin_t = sqrtf(fmaxf(0.0f, 1.0f - cos_t * cos_t));
+                        bool cannot = eta * sin_t > 1.0f;
+                        float scos = (!sh.front && !cannot)
+                                         ? sqrtf(fmaxf(0.0f, 1.0f - (eta * eta) * (1.0f - cos_t * cos_t)))
+                                         : cos_t;
+                        float refl = schlick(scos, eta);
+                        if (cannot || refl > rand_f32(rng)) dir = reflect_vec(d, sh.n);
+                        else dir = normalize(refract_vec(d, sh.n, eta));
+                    } else if (mtype == kMatGgx) {
+                        f3 t, b;
+                        onb(sh.n, &t, &b);
+                        f3 wo = mk3(-dot(d, t), -dot(d, b), -dot(d, sh.n));
+                        float rough = m.albedo_fuzz[3];
+                        float alpha = fmaxf(rough * rough, 1e-4f);
+                        float r1 = rand_f32(rng), r2 = rand_f32(rng);
+                        f3 wi, wgt;
+                        float gpdf;
+                        if (wo.z > 0.0f && ggx_sample(wo, alpha, albedo, r1, r2, &wi, &wgt, &gpdf)) {
+                            dir = normalize((wi.x * t + wi.y * b) + wi.z * sh.n);
+                            atten = wgt;
+                            pdf = gpdf;
+                            if (nee) {                                          // light sample at a GGX vertex
+                                LightSample ls = sample_light(S, sh.p, rng);
+                                if (ls.ok) {
+                                    f3 wl = mk3(dot(ls.dir, t), dot(ls.dir, b), dot(ls.dir, sh.n));
+                                    float bp;
+                                    f3 fc = ggx_eval(wo, wl, alpha, albedo, &bp);
+                                    if (wl.z > 0.0f && (fc.x > 0.0f || fc.y > 0.0f || fc.z > 0.0f)) {
+                                        float wmis = (ls.pdf * ls.pdf) / (ls.pdf * ls.pdf + bp * bp);
+                                        sc = (wmis / ls.pdf) * (thr * (fc * ls.Le));
+                                        so = sh.p; sd = ls.dir; smax = ls.dist * (1.0f - 1e-4f);
+                                        shadow = true;
+                                    }
+                                }
+                            }
+                        } else {
+                            absorbed = true;
+                        }
+                    } else {                                                    // :521-528
+                        if (nee) {
+                            LightSample ls = sample_light(S, sh.p, rng);
+                            float cs = dot(ls.dir, sh.n);
+                            if (ls.ok && cs > 0.0f) {
+                                float bp = cs / kPi;
+                                float wmis = (ls.pdf * ls.pdf) / (ls.pdf * ls.pdf + bp * bp);
+                                sc = (wmis * bp / ls.pdf) * (thr * (albedo * ls.Le));
+                                so = sh.p; sd = ls.dir; smax = ls.dist * (1.0f - 1e-4f);
+                                shadow = true;
+                            }
+                        }
+                        dir = cosine_scatter(rng, sh.n);
+                        atten = albedo;
+                        pdf = fmaxf(dot(dir, sh.n), 0.0f) / kPi;
+                    }
+                    if (!absorbed) {
+                        thr = thr * atten;
+                        if (bounce + 1 < P.max_depth) {
+                            cont = true;
+                            no = sh.p;
+                            nd = dir;
+                        }
+                        B.thr[slot] = make_float4(thr.x, thr.y, thr.z, pdf);
+                    }
+                    B.aux[slot] = make_uint4(rng, aux.y, aux.z, pdf > 0.0f ? 0u : kFlagSpecular);
+                }
+            }
+        }
+        // warp-aggregated append to the next ray queue
+        unsigned mask = __ballot_sync(0xffffffffu, cont);
+        if (mask) {
+            int leader = __ffs(mask) - 1;
+            uint32_t basepos = 0;
+            if ((int)lane == leader) basepos = atomicAdd(B.counters + (qi ^ 1), (uint32_t)__popc(mask));
+            basepos = __shfl_sync(0xffffffffu, basepos, leader);
+            if (cont) {
+                uint32_t pos = basepos + __popc(mask & ((1u << lane) - 1u));
+                B.q_o[qi ^ 1][pos] = make_float4(no.x, no.y, no.z, __uint_as_float(slot));
+                B.q_d[qi ^ 1][pos] = make_float4(nd.x, nd.y, nd.z, 0.0f);
+            }
+        }
+        unsigned smask = __ballot_sync(0xffffffffu, shadow);
+        if (smask) {
+            int leader = __ffs(smask) - 1;
+            uint32_t basepos = 0;
+            if ((int)lane == leader) basepos = atomicAdd(B.counters + 2, (uint32_t)__popc(smask));
+            basepos = __shfl_sync(0xffffffffu, basepos, leader);
+            if (shadow) {
+                uint32_t pos = basepos + __popc(smask & ((1u << lane) - 1u));
+                B.sh_o[pos] = make_float4(so.x, so.y, so.z, __uint_as_float(slot));
+                B.sh_d[pos] = make_float4(sd.x, sd.y, sd.z, smax);
+                B.sh_c[pos] = make_float4(sc.x, sc.y, sc.z, 0.0f);
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_shadow(DeviceScene S, PathBuffers B) {
+    const uint32_t n = B.counters[2];
+    uint32_t traced = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 o4 = B.sh_o[i], d4 = B.sh_d[i];
+        RayInv r = make_ray(xyz(o4), xyz(d4));
+        ++traced;
+        if (occluded(S, r, kTMin, d4.w, B.counters + 3)) continue;
+        uint32_t slot = __float_as_uint(o4.w);
+        float4 c = B.sh_c[i];
+        float4 L = B.L[slot];
+        B.L[slot] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
+    }
+    if (traced) atomicAdd(B.stats + 1, (unsigned long long)traced);
+}
+
+// Per pixel, in frame order: the reference's f32 running mean
+// (path_trace.wgsl:656-661, mix = a*(1-t) + b*t) and the f64 sum.
+__global__ void k_resolve(RenderParams P, PathBuffers B, float4 *mean, double *sum, int keep) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P.npix) return;
+    float4 m = keep ? mean[p] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    double s0 = keep ? sum[3 * (size_t)p] : 0.0, s1 = keep ? sum[3 * (size_t)p + 1] : 0.0,
+           s2 = keep ? sum[3 * (size_t)p + 2] : 0.0;
+    for (uint32_t k = 0; k < P.spp_pass; ++k) {
+        float4 s = B.L[(size_t)k * P.npix + p];
+        uint32_t frame = P.frame0 + k;
+        float w = 1.0f / (float)(min(frame, kMaxFrameCount) + 1u);
+        float omw = 1.0f - w;
+        m.x = m.x * omw + s.x * w;
+        m.y = m.y * omw + s.y * w;
+        m.z = m.z * omw + s.z * w;
+        s0 += (double)s.x; s1 += (double)s.y; s2 += (double)s.z;
+    }
+    m.w = 1.0f;
+    mean[p] = m;
+    sum[3 * (size_t)p] = s0; sum[3 * (size_t)p + 1] = s1; sum[3 * (size_t)p + 2] = s2;
+}
+
+// Light-selection CDF: one block; each thread sums a contiguous chunk of light
+// weights, a block scan gives chunk offsets, cdf[k] = prefix / total.
+__global__ void __launch_bounds__(1024) k_light_cdf(DeviceScene S, float *cdf, float *total_out) {
+    __shared__ float part[1024];
+    const uint32_t n = S.n_lights;
+    const uint32_t chunk = (n + 1023) / 1024;
+    const uint32_t b = threadIdx.x * chunk, e = min(b + chunk, n);
+    float local = 0.0f;
+    for (uint32_t k = b; k < e; ++k) local += light_weight(S, __ldg(S.lights + k));
+    part[threadIdx.x] = local;
+    __syncthreads();
+    if (threadIdx.x == 0) {            // sequential scan of 1024 partial sums: fixed order
+        float run = 0.0f;
+        for (int k = 0; k < 1024; ++k) { float v = part[k]; part[k] = run; run += v; }
+        *total_out = run;
+    }
+    __syncthreads();
+    const float total = *total_out;
+    float run = part[threadIdx.x];
+    for (uint32_t k = b; k < e; ++k) {
+        cdf[k] = total > 0.0f ? run / total : 0.0f;
+        run += light_weight(S, __ldg(S.lights + k));
+    }
+    if (threadIdx.x == 0) { cdf[0] = 0.0f; cdf[n] = 1.0f; }
+}
+
+void launch_light_cdf(const DeviceScene &S, float *d_cdf, float *d_total, cudaStream_t st) {
+    k_light_cdf<<<1, 1024, 0, st>>>(S, d_cdf, d_total); ::mcrt::note_launch();
+}
+
+// ------------------------------------------------------------------ launchers
+
+static int sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+void launch_trace_closest(const DeviceScene &S, const mcrt_ray *rays, uint32_t n, mcrt_hit *hits, bool ref_layout,
+                          uint32_t *overflow, cudaStream_t st) {
+    if (n == 0) return;
+    k_trace_closest<<<(n + 127) / 128, 128, 0, st>>>(S, rays, n, hits, ref_layout ? 1 : 0, overflow); ::mcrt::note_launch();
+}
+
+void launch_raygen(const DeviceScene &S, const RenderParams &P, PathBuffers &B, cudaStream_t st) {
+    uint32_t n = P.npix * P.spp_pass;
+    k_raygen<<<(n + 255) / 256, 256, 0, st>>>(S, P, B); ::mcrt::note_launch();
+}
+
+void launch_extend(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, cudaStream_t st) {
+    uint32_t nmax = P.npix * P.spp_pass;
+    int blocks = min(grid_blocks_for(nmax, 128), sm_count() * 16);
+    k_extend<<<blocks, 128, 0, st>>>(S, B, qi); ::mcrt::note_launch();
+}
+
+void launch_shade(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, uint32_t bounce,
+                  float4 *gbuf, cudaStream_t st) {
+    uint32_t nmax = P.npix * P.spp_pass;
+    int blocks = min(grid_blocks_for(nmax, 256), sm_count() * 8);
+    k_shade<<<blocks, 256, 0, st>>>(S, P, B, qi, bounce, gbuf); ::mcrt::note_launch();
+}
+
+void launch_shadow(const DeviceScene &S, const RenderParams &P, PathBuffers &B, cudaStream_t st) {
+    uint32_t nmax = P.npix * P.spp_pass;
+    int blocks = min(grid_blocks_for(nmax, 128), sm_count() * 16);
+    k_shadow<<<blocks, 128, 0, st>>>(S, B); ::mcrt::note_launch();
+}
+
+void launch_resolve(const RenderParams &P, const PathBuffers &B, float4 *mean, double *sum, bool keep,
+                    cudaStream_t st) {
+    k_resolve<<<(P.npix + 255) / 256, 256, 0, st>>>(P, B, mean, sum, keep ? 1 : 0); ::mcrt::note_launch();
+}
+
+}  // namespace mcrt

@@ -1,0 +1,741 @@
+/* oracle/oracle.cpp — CPU restatement of the mcrt path-tracing hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the CUDA library.  Only tests/,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline leg load it; the product
+ * never links or calls it.
+ *
+ * Every function cites the reference file:line it restates.  Compiled with
+ * -O2 -ffp-contract=off (no FMA contraction, no fast-math) so that the float
+ * arithmetic is the IEEE sequence written here, identical on x86-64 and
+ * aarch64.
+ *
+ * Deliberate, documented choices where the reference leaves freedom:
+ *  - WGSL builtins sin/cos/atan2/asin/pow/exp/normalize: see fmath.h.
+ *    normalize(v) = v * (1 / sqrt(dot(v, v))); dot(a,b) = (ax*bx + ay*by) + az*bz.
+ *  - mix(a, b, t) = a*(1-t) + b*t (the WGSL specification's formula).
+ *  - Tie rule for the closest hit: smallest t, then smallest original primitive
+ *    id; a sphere wins over a triangle at equal t (path_trace.wgsl:471-479
+ *    already gives spheres precedence).  To make ties reachable in any visit
+ *    order the node cull is `tenter <= t_max` instead of `<` (path_trace.wgsl:255).
+ *  - BVH build: the reference's sort_unstable_by on the centroid (bvh.rs:303,
+ *    mesh.rs:153) is made deterministic by breaking ties on the original id.
+ *    Binning is monotone in the centroid, so this changes only the order of
+ *    primitives inside a leaf, never the tree.
+ */
+#include "oracle.h"
+#include "fmath.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+constexpr float TAU = 6.283185307179586f;       /* path_trace.wgsl:36 */
+constexpr float PI_F = 3.141592653589793f;      /* path_trace.wgsl:37 */
+constexpr uint32_t MAX_MAT_IDX = 63u;           /* path_trace.wgsl:43 */
+constexpr uint32_t MAT_METAL = 1u, MAT_DIELECTRIC = 2u, MAT_EMISSIVE = 3u; /* material.rs:70-75 */
+constexpr uint32_t STACK_SIZE = 64u;            /* path_trace.wgsl:49 */
+constexpr float T_MIN = 1e-4f;                  /* path_trace.wgsl:52 */
+constexpr float T_MAX = 1e9f;                   /* path_trace.wgsl:55 */
+constexpr uint32_t MAX_FRAME_COUNT = 65535u;    /* path_trace.wgsl:58 */
+constexpr uint32_t BVH_LEAF_MAX = 4;            /* bvh.rs:32 */
+constexpr int SAH_BINS = 8;                     /* bvh.rs:38 */
+
+struct V3 { float x, y, z; };
+inline V3 v3(float x, float y, float z) { return {x, y, z}; }
+inline V3 ld3(const float *p) { return {p[0], p[1], p[2]}; }
+inline V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 operator*(V3 a, V3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+inline V3 operator*(float s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
+inline V3 operator/(V3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+inline V3 operator-(V3 a) { return {-a.x, -a.y, -a.z}; }
+inline float dot(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+inline V3 cross(V3 a, V3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline V3 normalize(V3 a) { float inv = 1.0f / sqrtf(dot(a, a)); return {a.x * inv, a.y * inv, a.z * inv}; }
+
+/* ------------------------------------------------------------------ RNG */
+/* path_trace.wgsl:64-66, :194-204 */
+inline uint32_t pcg_hash(uint32_t v) {
+    uint32_t s = v * 747796405u + 2891336453u;
+    uint32_t rot = s >> 28u;
+    s = ((s >> (rot + 4u)) ^ s) * 277803737u;
+    return (s >> 22u) ^ s;
+}
+inline float rand_f32(uint32_t &rng) {
+    rng = pcg_hash(rng);
+    return of_bits((rng >> 9u) | 0x3f800000u) - 1.0f;
+}
+
+/* path_trace.wgsl:210-227 */
+inline V3 random_unit_sphere(uint32_t &rng) {
+    float cos_phi = 1.0f - 2.0f * rand_f32(rng);
+    float sin_phi = sqrtf(fmaxf(0.0f, 1.0f - cos_phi * cos_phi));
+    float theta = TAU * rand_f32(rng);
+    float s, c;
+    of_sincos(theta, &s, &c);
+    return {sin_phi * c, sin_phi * s, cos_phi};
+}
+inline V3 cosine_scatter(uint32_t &rng, V3 n) {
+    V3 sc = n + random_unit_sphere(rng);
+    if (dot(sc, sc) < 1e-6f) return n;
+    return normalize(sc);
+}
+
+/* ------------------------------------------------------------------ env */
+/* path_trace.wgsl:233-242 */
+inline V3 sample_env(const orc_scene *sc, V3 dir) {
+    if (sc->env_w == 0 || sc->env_h == 0) return {0, 0, 0};
+    float phi = of_atan2(dir.z, dir.x);
+    float theta = of_asin(fminf(fmaxf(dir.y, -1.0f), 1.0f));
+    float u = phi / TAU + 0.5f;
+    float v = 0.5f - theta / PI_F;
+    uint32_t ix = of_f2u_sat(u * (float)sc->env_w) % sc->env_w;
+    uint32_t iy = of_f2u_sat(v * (float)sc->env_h) % sc->env_h;
+    const float *p = sc->env_rgba + 4ull * ((uint64_t)iy * sc->env_w + ix);
+    return {p[0], p[1], p[2]};
+}
+
+/* ------------------------------------------------------------------ intersection */
+struct Ray { V3 o, d; };
+
+/* 1/d with the reference traversal test's clamp (bvh.rs:808-812, mesh.rs:950-954):
+ * |d| < 1e-7 -> +-1e30.  WGSL's 1/0 = inf makes (min - o) * inf = 0 * inf = NaN
+ * for a ray lying in a slab plane, whose min/max is backend-defined; with the
+ * clamp such a ray counts as inside the slab and traversal equals brute force. */
+inline float inv_dir(float d) { return fabsf(d) < 1e-7f ? (d >= 0.0f ? 1e30f : -1e30f) : 1.0f / d; }
+
+/* path_trace.wgsl:248-256, with `tenter <= t_max` (tie reachability, see header) */
+inline bool ray_aabb_hit(const Ray &r, const orc_node &nd, float t_min, float t_max) {
+    V3 inv = {inv_dir(r.d.x), inv_dir(r.d.y), inv_dir(r.d.z)};
+    V3 t0 = (ld3(nd.aabb_min) - r.o) * inv;
+    V3 t1 = (ld3(nd.aabb_max) - r.o) * inv;
+    float tenter = fmaxf(fmaxf(fminf(t0.x, t1.x), fminf(t0.y, t1.y)), fminf(t0.z, t1.z));
+    float texit = fminf(fminf(fmaxf(t0.x, t1.x), fmaxf(t0.y, t1.y)), fmaxf(t0.z, t1.z));
+    return texit > fmaxf(tenter, t_min) && tenter <= t_max;
+}
+
+/* path_trace.wgsl:262-281: candidate root with t > t_min (near first, then far),
+ * independent of t_max; the caller applies t_max and the tie rule. */
+inline bool sphere_t(const Ray &r, const orc_sphere &s, float t_min, float *t_out) {
+    V3 c = ld3(s.center_r);
+    float radius = s.center_r[3];
+    V3 oc = r.o - c;
+    float a = dot(r.d, r.d);
+    float h = dot(oc, r.d);
+    float cc = dot(oc, oc) - radius * radius;
+    float disc = h * h - a * cc;
+    if (disc < 0.0f) return false;
+    float sq = sqrtf(disc);
+    float t = (-h - sq) / a;
+    if (t <= t_min) {
+        t = (-h + sq) / a;
+        if (t <= t_min) return false;
+    }
+    *t_out = t;
+    return true;
+}
+
+/* path_trace.wgsl:300-317 (t_max applied by the caller) */
+inline bool tri_uvt(const Ray &r, V3 v0, V3 v1, V3 v2, float t_min, float *t, float *uu, float *vv) {
+    V3 e1 = v1 - v0;
+    V3 e2 = v2 - v0;
+    V3 h = cross(r.d, e2);
+    float a = dot(e1, h);
+    if (fabsf(a) < 1e-8f) return false;
+    float f = 1.0f / a;
+    V3 s = r.o - v0;
+    float u = f * dot(s, h);
+    if (u < 0.0f || u > 1.0f) return false;
+    V3 q = cross(s, e1);
+    float v = f * dot(r.d, q);
+    if (v < 0.0f || u + v > 1.0f) return false;
+    float tt = f * dot(e2, q);
+    if (tt < t_min) return false;
+    *t = tt; *uu = u; *vv = v;
+    return true;
+}
+
+struct Closest {
+    float t;
+    uint32_t prim;   /* ORC_HIT_MISS, ORC_HIT_SPHERE|sphere_id, or triangle id */
+    uint32_t slot;   /* ordered slot of the primitive */
+    float u, v;
+};
+
+inline bool tie_better(float t, uint32_t id, const Closest &b) {
+    if (t < b.t) return true;
+    if (t == b.t && b.prim != ORC_HIT_MISS && !(b.prim & ORC_HIT_SPHERE) && id < b.prim) return true;
+    return false;
+}
+
+/* Interpolated shading normal of an ordered triangle at (u, v) (path_trace.wgsl:448-450). */
+inline V3 tri_normal(const orc_scene *sc, const orc_triangle &tri, float u, float v) {
+    const orc_vertex &va = sc->vertices[tri.v[0]];
+    const orc_vertex &vb = sc->vertices[tri.v[1]];
+    const orc_vertex &vc = sc->vertices[tri.v[2]];
+    float w = 1.0f - u - v;
+    return normalize((w * ld3(va.normal) + u * ld3(vb.normal)) + v * ld3(vc.normal));
+}
+
+/* sphere_bvh_hit, path_trace.wgsl:343-364, :393-413 */
+void sphere_bvh_hit(const orc_scene *sc, const Ray &r, float t_min, float t_max, Closest &best,
+                    uint32_t *nodes_visited, uint32_t *prims_tested) {
+    if (sc->n_sphere_nodes == 0) return;
+    uint32_t stack[STACK_SIZE];
+    uint32_t top = 0;
+    stack[top++] = 0;
+    best.t = t_max;
+    while (top > 0) {
+        uint32_t ni = stack[--top];
+        const orc_node &nd = sc->sphere_nodes[ni];
+        ++*nodes_visited;
+        if (!ray_aabb_hit(r, nd, t_min, best.t)) continue;
+        if (nd.prim_count > 0) {
+            for (uint32_t j = 0; j < nd.prim_count; ++j) {
+                uint32_t slot = nd.right_or_offset + j;
+                ++*prims_tested;
+                float t;
+                if (!sphere_t(r, sc->spheres[slot], t_min, &t)) continue;
+                if (!(t < t_max)) continue;
+                uint32_t id = sc->sphere_ids ? sc->sphere_ids[slot] : slot;
+                bool better = t < best.t ||
+                              (t == best.t && best.prim != ORC_HIT_MISS && (id | ORC_HIT_SPHERE) < best.prim);
+                if (better) { best.t = t; best.prim = id | ORC_HIT_SPHERE; best.slot = slot; best.u = 0; best.v = 0; }
+            }
+            continue;
+        }
+        if (top + 2u <= STACK_SIZE) {
+            stack[top++] = nd.right_or_offset;
+            stack[top++] = ni + 1u;
+        }
+    }
+}
+
+/* mesh_bvh_hit, path_trace.wgsl:368-387, :419-465 */
+void mesh_bvh_hit(const orc_scene *sc, const Ray &r, float t_min, Closest &best,
+                  uint32_t *nodes_visited, uint32_t *prims_tested) {
+    if (sc->n_mesh_nodes == 0) return;
+    uint32_t stack[STACK_SIZE];
+    uint32_t top = 0;
+    stack[top++] = 0;
+    while (top > 0) {
+        uint32_t ni = stack[--top];
+        const orc_node &nd = sc->mesh_nodes[ni];
+        ++*nodes_visited;
+        if (!ray_aabb_hit(r, nd, t_min, best.t)) continue;
+        if (nd.prim_count > 0) {
+            for (uint32_t j = 0; j < nd.prim_count; ++j) {
+                uint32_t slot = nd.right_or_offset + j;
+                ++*prims_tested;
+                const orc_triangle &tri = sc->triangles[slot];
+                float t, u, v;
+                if (!tri_uvt(r, ld3(sc->vertices[tri.v[0]].position), ld3(sc->vertices[tri.v[1]].position),
+                             ld3(sc->vertices[tri.v[2]].position), t_min, &t, &u, &v))
+                    continue;
+                uint32_t id = sc->triangle_ids ? sc->triangle_ids[slot] : slot;
+                if (!tie_better(t, id, best)) continue;
+                if ((tri.mat_idx >> 31u) != 0u) {              /* backface cull, :438-452 */
+                    V3 n = tri_normal(sc, tri, u, v);
+                    if (!(dot(r.d, n) < 0.0f)) continue;
+                }
+                best.t = t; best.prim = id; best.slot = slot; best.u = u; best.v = v;
+            }
+            continue;
+        }
+        if (top + 2u <= STACK_SIZE) {
+            stack[top++] = nd.right_or_offset;
+            stack[top++] = ni + 1u;
+        }
+    }
+}
+
+/* world_hit, path_trace.wgsl:471-479 */
+Closest world_hit(const orc_scene *sc, const Ray &r, float t_min, float t_max, uint32_t *nv, uint32_t *pt) {
+    Closest best{t_max, ORC_HIT_MISS, 0, 0, 0};
+    sphere_bvh_hit(sc, r, t_min, t_max, best, nv, pt);
+    mesh_bvh_hit(sc, r, t_min, best, nv, pt);
+    if (best.prim == ORC_HIT_MISS) best.t = -1.0f;
+    return best;
+}
+
+Closest brute_hit(const orc_scene *sc, const Ray &r, float t_min, float t_max) {
+    Closest best{t_max, ORC_HIT_MISS, 0, 0, 0};
+    for (uint32_t slot = 0; slot < sc->n_spheres; ++slot) {
+        float t;
+        if (!sphere_t(r, sc->spheres[slot], t_min, &t) || !(t < t_max)) continue;
+        uint32_t id = sc->sphere_ids ? sc->sphere_ids[slot] : slot;
+        bool better = t < best.t || (t == best.t && best.prim != ORC_HIT_MISS && (id | ORC_HIT_SPHERE) < best.prim);
+        if (better) { best.t = t; best.prim = id | ORC_HIT_SPHERE; best.slot = slot; best.u = best.v = 0; }
+    }
+    for (uint32_t slot = 0; slot < sc->n_triangles; ++slot) {
+        const orc_triangle &tri = sc->triangles[slot];
+        float t, u, v;
+        if (!tri_uvt(r, ld3(sc->vertices[tri.v[0]].position), ld3(sc->vertices[tri.v[1]].position),
+                     ld3(sc->vertices[tri.v[2]].position), t_min, &t, &u, &v))
+            continue;
+        uint32_t id = sc->triangle_ids ? sc->triangle_ids[slot] : slot;
+        if (!tie_better(t, id, best)) continue;
+        if ((tri.mat_idx >> 31u) != 0u) {
+            V3 n = tri_normal(sc, tri, u, v);
+            if (!(dot(r.d, n) < 0.0f)) continue;
+        }
+        best.t = t; best.prim = id; best.slot = slot; best.u = u; best.v = v;
+    }
+    if (best.prim == ORC_HIT_MISS) best.t = -1.0f;
+    return best;
+}
+
+/* ------------------------------------------------------------------ shading */
+struct HitRec { float t; V3 p; V3 n; bool front; uint32_t mat; };
+
+inline HitRec make_hitrec(const orc_scene *sc, const Ray &r, const Closest &c) {
+    HitRec h;
+    h.t = c.t;
+    h.p = r.o + c.t * r.d;                                       /* :283, :455 */
+    if (c.prim & ORC_HIT_SPHERE) {                               /* :282-287 */
+        const orc_sphere &s = sc->spheres[c.slot];
+        V3 outn = (h.p - ld3(s.center_r)) / s.center_r[3];
+        h.front = dot(r.d, outn) < 0.0f;
+        h.n = h.front ? outn : -outn;
+        h.mat = s.mat_and_pad[0];
+    } else {                                                     /* :444-459 */
+        const orc_triangle &tri = sc->triangles[c.slot];
+        V3 n = tri_normal(sc, tri, c.u, c.v);
+        h.front = dot(r.d, n) < 0.0f;
+        h.n = h.front ? n : -n;
+        h.mat = tri.mat_idx & 0x7fffffffu;
+    }
+    return h;
+}
+
+/* path_trace.wgsl:485-500 */
+inline V3 reflect_vec(V3 v, V3 n) { return v - (2.0f * dot(v, n)) * n; }
+inline V3 refract_vec(V3 v, V3 n, float eta) {
+    float cos_theta = fminf(dot(-v, n), 1.0f);
+    V3 r_perp = eta * (v + cos_theta * n);
+    V3 r_para = (-sqrtf(fmaxf(0.0f, 1.0f - dot(r_perp, r_perp)))) * n;
+    return r_perp + r_para;
+}
+inline float schlick(float cos_theta, float eta) {
+    float r0 = (1.0f - eta) / (1.0f + eta);
+    r0 = r0 * r0;
+    return r0 + (1.0f - r0) * of_pow(1.0f - cos_theta, 5.0f);
+}
+
+/* path_color, path_trace.wgsl:583-620 (+ G-buffer :592-602) */
+/* stats (optional): [0] rays traced, [1] nodes visited, [2] primitives tested */
+V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, float *gbuf, uint64_t *stats) {
+    V3 thr = {1.0f, 1.0f, 1.0f};
+    bool first = true;
+    for (uint32_t bounce = 0; bounce < max_depth; ++bounce) {
+        uint32_t nv = 0, pt = 0;
+        Closest c = world_hit(sc, ray, T_MIN, T_MAX, &nv, &pt);
+        if (stats) { stats[0] += 1; stats[1] += nv; stats[2] += pt; }
+        if (c.t < 0.0f) {
+            if (first && gbuf) { gbuf[0] = 0; gbuf[1] = 0; gbuf[2] = 0; gbuf[3] = T_MAX; }
+            return thr * sample_env(sc, ray.d);
+        }
+        HitRec h = make_hitrec(sc, ray, c);
+        if (first) {
+            if (gbuf) { gbuf[0] = h.n.x; gbuf[1] = h.n.y; gbuf[2] = h.n.z; gbuf[3] = h.t; }
+            first = false;
+        }
+        uint32_t mi = std::min(h.mat, MAX_MAT_IDX);
+        const orc_material &m = sc->materials->materials[mi];
+        V3 albedo = ld3(m.albedo_fuzz);
+        if (m.type_pad[0] == MAT_EMISSIVE)                                     /* :608-610 */
+            return m.ior_pad[0] * (thr * albedo);
+        V3 dir, atten;
+        bool absorbed = false;
+        if (m.type_pad[0] == MAT_METAL) {                                      /* :530-541 */
+            float fuzz = m.albedo_fuzz[3];
+            V3 refl = reflect_vec(normalize(ray.d), h.n);
+            V3 pert = refl + fuzz * random_unit_sphere(rng);
+            dir = normalize(dot(pert, pert) >= 1e-6f ? pert : refl);
+            atten = albedo;
+            absorbed = dot(dir, h.n) <= 0.0f;
+        } else if (m.type_pad[0] == MAT_DIELECTRIC) {                          /* :543-564 */
+            atten = {1.0f, 1.0f, 1.0f};
+            float ior = m.ior_pad[0];
+            float eta = h.front ? 1.0f / ior : ior;
+            float cos_t = fminf(dot(-ray.d, h.n), 1.0f);
+            float sin_t = sqrtf(fmaxf(0.0f, 1.0f - cos_t * cos_t));
+            bool cannot = eta * sin_t > 1.0f;
+            float scos = (!h.front && !cannot)
+                             ? sqrtf(fmaxf(0.0f, 1.0f - (eta * eta) * (1.0f - cos_t * cos_t)))
+                             : cos_t;
+            float refl = schlick(scos, eta);
+            if (cannot || refl > rand_f32(rng))
+                dir = reflect_vec(ray.d, h.n);
+            else
+                dir = normalize(refract_vec(ray.d, h.n, eta));
+        } else {                                                               /* :521-528 */
+            dir = cosine_scatter(rng, h.n);
+            atten = albedo;
+        }
+        if (absorbed) return {0.0f, 0.0f, 0.0f};
+        thr = thr * atten;
+        ray = {h.p, dir};
+    }
+    return {0.0f, 0.0f, 0.0f};
+}
+
+/* cs_main raygen, path_trace.wgsl:626-652 */
+inline Ray camera_ray(const orc_camera *cam, uint32_t x, uint32_t y, uint32_t w, uint32_t h, uint32_t &rng) {
+    float u = ((float)x + rand_f32(rng)) / (float)w;
+    float v = 1.0f - ((float)y + rand_f32(rng)) / (float)h;
+    V3 focal = (ld3(cam->lower_left) + u * ld3(cam->horizontal)) + v * ld3(cam->vertical);
+    float r = sqrtf(rand_f32(rng));
+    float theta = TAU * rand_f32(rng);
+    float s, c;
+    of_sincos(theta, &s, &c);
+    float lx = r * c, ly = r * s;
+    V3 lens = lx * ld3(cam->defocus_u) + ly * ld3(cam->defocus_v);
+    V3 o = ld3(cam->origin) + lens;
+    return {o, normalize(focal - o)};
+}
+
+/* ------------------------------------------------------------------ BVH build */
+struct Aabb { float mn[3], mx[3]; };
+inline Aabb aabb_empty() { return {{INFINITY, INFINITY, INFINITY}, {-INFINITY, -INFINITY, -INFINITY}}; }
+inline Aabb aabb_union(const Aabb &a, const Aabb &b) {
+    Aabb r;
+    for (int i = 0; i < 3; ++i) { r.mn[i] = fminf(a.mn[i], b.mn[i]); r.mx[i] = fmaxf(a.mx[i], b.mx[i]); }
+    return r;
+}
+inline float half_area(const Aabb &a) {                       /* bvh.rs:168-175 */
+    float d0 = a.mx[0] - a.mn[0], d1 = a.mx[1] - a.mn[1], d2 = a.mx[2] - a.mn[2];
+    return d0 * d1 + d1 * d2 + d0 * d2;
+}
+inline void centroid(const Aabb &a, float c[3]) {            /* bvh.rs:179-185 */
+    for (int i = 0; i < 3; ++i) c[i] = (a.mn[i] + a.mx[i]) * 0.5f;
+}
+inline Aabb padded(const Aabb &a) {                          /* bvh.rs:194-207 */
+    const float EPS = 1e-4f;
+    Aabb r;
+    for (int i = 0; i < 3; ++i) { r.mn[i] = fminf(a.mn[i], a.mx[i] - EPS); r.mx[i] = fmaxf(a.mx[i], a.mn[i] + EPS); }
+    return r;
+}
+
+struct Prim { Aabb b; float c[3]; uint32_t id; };
+
+/* find_best_split, bvh.rs:388-463 (identical in mesh.rs:206-275) */
+bool find_best_split(const Prim *p, size_t n, const Aabb &cb, const Aabb &nb, int *axis_out, size_t *split_out) {
+    float parent = fmaxf(half_area(nb), 1e-8f);
+    float best_cost = (float)n;
+    int best_axis = 0;
+    size_t best_split = 0;
+    bool found = false;
+    for (int axis = 0; axis < 3; ++axis) {
+        float len = cb.mx[axis] - cb.mn[axis];
+        if (len < 1e-8f) continue;
+        Aabb bb[SAH_BINS];
+        uint32_t bc[SAH_BINS];
+        for (int i = 0; i < SAH_BINS; ++i) { bb[i] = aabb_empty(); bc[i] = 0; }
+        for (size_t k = 0; k < n; ++k) {
+            float t = (p[k].c[axis] - cb.mn[axis]) / len;
+            uint32_t b = of_f2u_sat(t * (float)SAH_BINS);
+            if (b > SAH_BINS - 1) b = SAH_BINS - 1;
+            bb[b] = aabb_union(bb[b], p[k].b);
+            bc[b] += 1;
+        }
+        Aabb lb[SAH_BINS];
+        uint32_t lc[SAH_BINS];
+        lb[0] = bb[0]; lc[0] = bc[0];
+        for (int i = 1; i < SAH_BINS; ++i) { lb[i] = aabb_union(lb[i - 1], bb[i]); lc[i] = lc[i - 1] + bc[i]; }
+        Aabb rb = aabb_empty();
+        uint32_t rc = 0;
+        for (int s = SAH_BINS - 2; s >= 0; --s) {
+            rb = aabb_union(rb, bb[s + 1]);
+            rc += bc[s + 1];
+            uint32_t l = lc[s];
+            if (l == 0 || rc == 0) continue;
+            float cost = (half_area(lb[s]) * (float)l + half_area(rb) * (float)rc) / parent;
+            if (cost < best_cost) { best_cost = cost; best_axis = axis; best_split = l; found = true; }
+        }
+    }
+    if (found && best_split > 0 && best_split < n) { *axis_out = best_axis; *split_out = best_split; return true; }
+    return false;
+}
+
+/* build_recursive, bvh.rs:285-349 / mesh.rs:129-183; make_leaf bvh.rs:352-370 */
+uint32_t build_recursive(Prim *p, size_t n, std::vector<orc_node> &nodes, std::vector<uint32_t> &order) {
+    uint32_t idx = (uint32_t)nodes.size();
+    nodes.push_back(orc_node{});
+    Aabb b = aabb_empty();
+    for (size_t k = 0; k < n; ++k) b = aabb_union(b, p[k].b);
+    auto make_leaf = [&]() {
+        orc_node nd{};
+        for (int i = 0; i < 3; ++i) { nd.aabb_min[i] = b.mn[i]; nd.aabb_max[i] = b.mx[i]; }
+        nd.right_or_offset = (uint32_t)order.size();
+        nd.prim_count = (uint32_t)n;
+        for (size_t k = 0; k < n; ++k) order.push_back(p[k].id);
+        nodes[idx] = nd;
+    };
+    if (n <= BVH_LEAF_MAX) { make_leaf(); return idx; }
+    Aabb cb = aabb_empty();
+    for (size_t k = 0; k < n; ++k) {
+        Aabb pt;
+        for (int i = 0; i < 3; ++i) { pt.mn[i] = p[k].c[i]; pt.mx[i] = p[k].c[i]; }
+        cb = aabb_union(cb, pt);
+    }
+    int axis;
+    size_t split;
+    if (!find_best_split(p, n, cb, b, &axis, &split)) { make_leaf(); return idx; }
+    std::sort(p, p + n, [axis](const Prim &x, const Prim &y) {
+        if (x.c[axis] < y.c[axis]) return true;
+        if (y.c[axis] < x.c[axis]) return false;
+        return x.id < y.id;
+    });
+    build_recursive(p, split, nodes, order);
+    uint32_t right = (uint32_t)nodes.size();
+    build_recursive(p + split, n - split, nodes, order);
+    orc_node nd{};
+    for (int i = 0; i < 3; ++i) { nd.aabb_min[i] = b.mn[i]; nd.aabb_max[i] = b.mx[i]; }
+    nd.right_or_offset = right;
+    nd.prim_count = 0;
+    nodes[idx] = nd;
+    return idx;
+}
+
+int n_threads(int threads) {
+#ifdef _OPENMP
+    return threads > 0 ? threads : omp_get_max_threads();
+#else
+    (void)threads;
+    return 1;
+#endif
+}
+
+} // namespace
+
+extern "C" {
+
+uint32_t orc_pcg_hash(uint32_t v) { return pcg_hash(v); }
+
+uint32_t orc_build_sphere_bvh(const orc_sphere *spheres, uint32_t n, orc_node *out_nodes,
+                              orc_sphere *out_ordered, uint32_t *out_ids) {
+    if (n == 0) return 0;                                                   /* bvh.rs:240-245 */
+    std::vector<Prim> prims(n);
+    for (uint32_t i = 0; i < n; ++i) {                                     /* bvh.rs:247-260, :133-143 */
+        const float *c = spheres[i].center_r;
+        float r = c[3];
+        Prim &p = prims[i];
+        for (int k = 0; k < 3; ++k) { p.b.mn[k] = c[k] - r; p.b.mx[k] = c[k] + r; }
+        centroid(p.b, p.c);
+        p.id = i;
+    }
+    std::vector<orc_node> nodes;
+    nodes.reserve(2 * (size_t)n);
+    std::vector<uint32_t> order;
+    order.reserve(n);
+    build_recursive(prims.data(), n, nodes, order);
+    std::memcpy(out_nodes, nodes.data(), nodes.size() * sizeof(orc_node));
+    for (uint32_t i = 0; i < n; ++i) {
+        if (out_ordered) out_ordered[i] = spheres[order[i]];
+        if (out_ids) out_ids[i] = order[i];
+    }
+    return (uint32_t)nodes.size();
+}
+
+uint32_t orc_build_mesh_bvh(const orc_vertex *verts, uint32_t nv, const orc_triangle *tris, uint32_t nt,
+                            orc_node *out_nodes, orc_triangle *out_ordered, uint32_t *out_ids) {
+    (void)nv;
+    if (nt == 0) return 0;                                                  /* mesh.rs:83-89 */
+    std::vector<Prim> prims(nt);
+    for (uint32_t i = 0; i < nt; ++i) {                                    /* mesh.rs:99-111, :282-291 */
+        Aabb b = aabb_empty();
+        for (int k = 0; k < 3; ++k) {
+            const float *q = verts[tris[i].v[k]].position;
+            for (int a = 0; a < 3; ++a) { b.mn[a] = fminf(b.mn[a], q[a]); b.mx[a] = fmaxf(b.mx[a], q[a]); }
+        }
+        prims[i].b = padded(b);
+        centroid(prims[i].b, prims[i].c);
+        prims[i].id = i;
+    }
+    std::vector<orc_node> nodes;
+    nodes.reserve(2 * (size_t)nt);
+    std::vector<uint32_t> order;
+    order.reserve(nt);
+    build_recursive(prims.data(), nt, nodes, order);
+    std::memcpy(out_nodes, nodes.data(), nodes.size() * sizeof(orc_node));
+    for (uint32_t i = 0; i < nt; ++i) {
+        if (out_ordered) out_ordered[i] = tris[order[i]];
+        if (out_ids) out_ids[i] = order[i];
+    }
+    return (uint32_t)nodes.size();
+}
+
+void orc_trace(const orc_scene *sc, const orc_ray *rays, uint32_t n, orc_hit *hits, int mode,
+               uint32_t *stats, int threads) {
+#pragma omp parallel for schedule(dynamic, 256) num_threads(n_threads(threads))
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        Ray r{ld3(rays[i].org), ld3(rays[i].dir)};
+        uint32_t nv = 0, pt = 0;
+        Closest c = mode == 1 ? brute_hit(sc, r, rays[i].tmin, rays[i].tmax)
+                              : world_hit(sc, r, rays[i].tmin, rays[i].tmax, &nv, &pt);
+        hits[i].t = c.t;
+        hits[i].prim = c.prim;
+        hits[i].u = c.u;
+        hits[i].v = c.v;
+        if (stats) { stats[2 * i] = nv; stats[2 * i + 1] = pt; }
+    }
+}
+
+void orc_render_rect_stats(const orc_scene *sc, const orc_camera *cam, uint32_t w, uint32_t h,
+                           uint32_t x0, uint32_t y0, uint32_t cw, uint32_t ch, uint32_t spp, uint32_t first_frame,
+                           uint32_t max_depth, float *out_mean, double *out_sum, float *out_gbuf, int threads,
+                           uint64_t *out_stats) {
+    int64_t npx = (int64_t)cw * ch;
+    uint64_t tot[3] = {0, 0, 0};
+#pragma omp parallel num_threads(n_threads(threads))
+    {
+    uint64_t loc[3] = {0, 0, 0};
+    uint64_t *st = out_stats ? loc : nullptr;
+#pragma omp for schedule(dynamic, 16)
+    for (int64_t i = 0; i < npx; ++i) {
+        uint32_t x = x0 + (uint32_t)(i % cw), y = y0 + (uint32_t)(i / cw);
+        float mean[3] = {0, 0, 0};
+        if (out_mean) { mean[0] = out_mean[4 * i]; mean[1] = out_mean[4 * i + 1]; mean[2] = out_mean[4 * i + 2]; }
+        double sum[3] = {0, 0, 0};
+        float g[4] = {0, 0, 0, 0};
+        for (uint32_t k = 0; k < spp; ++k) {
+            uint32_t frame = first_frame + k;
+            uint32_t rng = pcg_hash(pcg_hash(x + y * w) ^ (frame * 2654435761u));   /* :636-637 */
+            Ray r = camera_ray(cam, x, y, w, h, rng);
+            V3 s = path_color(sc, r, rng, max_depth, g, st);
+            float wgt = 1.0f / (float)(std::min(frame, MAX_FRAME_COUNT) + 1u);      /* :657 */
+            float omw = 1.0f - wgt;
+            mean[0] = mean[0] * omw + s.x * wgt;                                     /* :659 mix */
+            mean[1] = mean[1] * omw + s.y * wgt;
+            mean[2] = mean[2] * omw + s.z * wgt;
+            sum[0] += (double)s.x; sum[1] += (double)s.y; sum[2] += (double)s.z;
+        }
+        if (out_mean) {
+            out_mean[4 * i] = mean[0]; out_mean[4 * i + 1] = mean[1]; out_mean[4 * i + 2] = mean[2];
+            out_mean[4 * i + 3] = 1.0f;
+        }
+        if (out_sum) { out_sum[3 * i] += sum[0]; out_sum[3 * i + 1] += sum[1]; out_sum[3 * i + 2] += sum[2]; }
+        if (out_gbuf) for (int c = 0; c < 4; ++c) out_gbuf[4 * i + c] = g[c];
+    }
+    if (out_stats) {
+#pragma omp critical
+        for (int k = 0; k < 3; ++k) tot[k] += loc[k];
+    }
+    }
+    if (out_stats) for (int k = 0; k < 3; ++k) out_stats[k] = tot[k];
+}
+
+void orc_render_rect(const orc_scene *sc, const orc_camera *cam, uint32_t w, uint32_t h, uint32_t x0, uint32_t y0,
+                     uint32_t cw, uint32_t ch, uint32_t spp, uint32_t first_frame, uint32_t max_depth,
+                     float *out_mean, double *out_sum, float *out_gbuf, int threads) {
+    orc_render_rect_stats(sc, cam, w, h, x0, y0, cw, ch, spp, first_frame, max_depth, out_mean, out_sum, out_gbuf,
+                          threads, nullptr);
+}
+
+void orc_render(const orc_scene *sc, const orc_camera *cam, uint32_t w, uint32_t h, uint32_t spp,
+                uint32_t first_frame, uint32_t max_depth, float *out_mean, double *out_sum, float *out_gbuf,
+                int threads) {
+    orc_render_rect(sc, cam, w, h, 0, 0, w, h, spp, first_frame, max_depth, out_mean, out_sum, out_gbuf, threads);
+}
+
+/* cs_denoise, denoise.wgsl:52-120 */
+void orc_denoise(const float *accum, const float *gbuf, uint32_t w, uint32_t h, int radius, float sigma_s,
+                 float sigma_d, float normal_pow, float *out) {
+    const int W = (int)w, H = (int)h;
+    float inv2ss = 1.0f / ((2.0f * sigma_s) * sigma_s);
+    float inv2ds = 1.0f / ((2.0f * sigma_d) * sigma_d);
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const float *gp = gbuf + 4 * ((size_t)y * W + x);
+            V3 np = ld3(gp);
+            float dp = gp[3];
+            bool on_sky = dp < 0.0f;
+            V3 acc = {0, 0, 0};
+            float wacc = 0.0f;
+            for (int dy = -radius; dy <= radius; ++dy)
+                for (int dx = -radius; dx <= radius; ++dx) {
+                    int qx = std::min(std::max(x + dx, 0), W - 1);
+                    int qy = std::min(std::max(y + dy, 0), H - 1);
+                    const float *gq = gbuf + 4 * ((size_t)qy * W + qx);
+                    V3 nq = ld3(gq);
+                    float dq = gq[3];
+                    bool q_sky = dq < 0.0f;
+                    if (on_sky != q_sky) continue;
+                    float dist_sq = (float)(dx * dx + dy * dy);
+                    float ws = of_exp(-dist_sq * inv2ss);
+                    float wn = on_sky ? 1.0f : of_pow(fmaxf(0.0f, dot(np, nq)), normal_pow);
+                    float rel = (dp - dq) / fmaxf(dp, 1e-4f);
+                    float wd = on_sky ? 1.0f : of_exp(-(rel * rel) * inv2ds);
+                    float wt = (ws * wn) * wd;
+                    acc = acc + wt * ld3(accum + 4 * ((size_t)qy * W + qx));
+                    wacc += wt;
+                }
+            V3 res = wacc > 0.0f ? acc / wacc : ld3(accum + 4 * ((size_t)y * W + x));
+            float *o = out + 4 * ((size_t)y * W + x);
+            o[0] = res.x; o[1] = res.y; o[2] = res.z; o[3] = 1.0f;
+        }
+}
+
+/* headless.rs:93-98 and the non-finite sanitising at :350-368 */
+void orc_tonemap_rgba8(const float *rgba, uint32_t n, uint8_t *out) {
+    const float inv_gamma = 1.0f / 2.2f;
+    for (uint32_t i = 0; i < n; ++i) {
+        for (int c = 0; c < 3; ++c) {
+            float v = rgba[4 * i + c];
+            if (!std::isfinite(v)) v = 0.0f;
+            v = fmaxf(v, 0.0f);
+            float mapped = v / (v + 1.0f);
+            float g = of_pow(mapped, inv_gamma);
+            g = fminf(fmaxf(g, 0.0f), 1.0f);
+            float q = g * 255.0f + 0.5f;
+            out[4 * i + c] = (uint8_t)std::min(of_f2u_sat(q), 255u);
+        }
+        out[4 * i + 3] = 255;
+    }
+}
+
+/* compare_images, regression.rs:120-181 (RGB only, f64) */
+void orc_compare_images(const uint8_t *a, const uint8_t *b, uint32_t w, uint32_t h, double *out) {
+    if (w == 0 || h == 0) { out[0] = 0.0; out[1] = INFINITY; out[2] = 0.0; return; }
+    double sum = 0.0, mx = 0.0;
+    for (size_t i = 0; i < (size_t)w * h; ++i)
+        for (int c = 0; c < 3; ++c) {
+            double va = a[4 * i + c] / 255.0, vb = b[4 * i + c] / 255.0;
+            double d = std::fabs(va - vb);
+            sum += d * d;
+            if (d > mx) mx = d;
+        }
+    double mse = sum / ((double)w * (double)h * 3.0);
+    out[0] = mse;
+    out[1] = mse == 0.0 ? INFINITY : 10.0 * std::log10(1.0 / mse);
+    out[2] = mx;
+}
+
+void orc_math_eval(int fn, const float *x, const float *y, float *out, uint32_t n) {
+    for (uint32_t i = 0; i < n; ++i) {
+        switch (fn) {
+        case 0: out[i] = of_sin(x[i]); break;
+        case 1: out[i] = of_cos(x[i]); break;
+        case 2: out[i] = of_atan2(x[i], y[i]); break;
+        case 3: out[i] = of_asin(x[i]); break;
+        case 4: out[i] = of_exp(x[i]); break;
+        case 5: out[i] = of_log(x[i]); break;
+        case 6: out[i] = of_pow(x[i], y[i]); break;
+        case 7: out[i] = of_tan(x[i]); break;
+        default: out[i] = NAN;
+        }
+    }
+}
+
+} // extern "C"

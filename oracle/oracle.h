@@ -1,0 +1,108 @@
+/* oracle/oracle.h — C interface of the CPU oracle (test infrastructure only).
+ *
+ * The oracle restates the reference's path-tracing hot path on the CPU:
+ *   - BVH builders            src/bvh.rs:239-463, src/mesh.rs:82-291
+ *   - closest-hit traversal   src/shaders/path_trace.wgsl:248-479
+ *   - path_color / cs_main    src/shaders/path_trace.wgsl:194-242, :485-662
+ *   - joint-bilateral denoise src/shaders/denoise.wgsl:52-120
+ *   - image metrics           src/regression.rs:120-181
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it.
+ */
+#ifndef MCRT_ORACLE_H
+#define MCRT_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct { float center_r[4]; uint32_t mat_and_pad[4]; } orc_sphere;                 /* scene.rs:24-29 */
+typedef struct { float aabb_min[4]; float aabb_max[4]; uint32_t right_or_offset;
+                 uint32_t prim_count; uint32_t pad[2]; } orc_node;                         /* bvh.rs:56-68 */
+typedef struct { float position[4]; float normal[4]; float uv[4]; } orc_vertex;           /* mesh.rs:26-34 */
+typedef struct { uint32_t v[3]; uint32_t mat_idx; } orc_triangle;                         /* mesh.rs:41-46 */
+typedef struct { uint32_t type_pad[4]; float albedo_fuzz[4]; float ior_pad[4]; } orc_material; /* material.rs:37-44 */
+typedef struct { uint32_t mat_count; uint32_t n_emissive; uint32_t pad[2];
+                 orc_material materials[64]; } orc_material_data;                          /* material.rs:56-63 */
+typedef struct { float origin[4]; float lower_left[4]; float horizontal[4]; float vertical[4];
+                 float defocus_u[4]; float defocus_v[4]; uint32_t frame_count;
+                 uint32_t pad[3]; } orc_camera;                                            /* camera.rs:37-53 */
+typedef struct { float org[3]; float tmin; float dir[3]; float tmax; } orc_ray;
+typedef struct { float t; uint32_t prim; float u; float v; } orc_hit;
+
+/* A scene as the oracle traverses it: the reference's buffers after build_bvh /
+ * build_mesh_bvh (ordered primitives + pre-order nodes) plus the original
+ * primitive ids of the ordered slots. */
+typedef struct {
+    const orc_sphere *spheres; uint32_t n_spheres;          /* ordered */
+    const uint32_t *sphere_ids;                             /* original index per ordered slot */
+    const orc_node *sphere_nodes; uint32_t n_sphere_nodes;
+    const orc_vertex *vertices; uint32_t n_vertices;
+    const orc_triangle *triangles; uint32_t n_triangles;    /* ordered */
+    const uint32_t *triangle_ids;
+    const orc_node *mesh_nodes; uint32_t n_mesh_nodes;
+    const orc_material_data *materials;
+    const float *env_rgba; uint32_t env_w; uint32_t env_h;
+} orc_scene;
+
+#define ORC_HIT_MISS 0xffffffffu
+#define ORC_HIT_SPHERE 0x80000000u
+
+/* Build the reference BVH.  out_nodes must hold 2*n entries; out_ordered and
+ * out_ids n entries.  Returns the node count. */
+uint32_t orc_build_sphere_bvh(const orc_sphere *spheres, uint32_t n,
+                              orc_node *out_nodes, orc_sphere *out_ordered, uint32_t *out_ids);
+uint32_t orc_build_mesh_bvh(const orc_vertex *verts, uint32_t nv,
+                            const orc_triangle *tris, uint32_t nt,
+                            orc_node *out_nodes, orc_triangle *out_ordered, uint32_t *out_ids);
+
+/* mode 0: reference traversal order with the tie rule; mode 1: brute force.
+ * stats (optional, 2 entries per ray): nodes visited, primitives tested. */
+void orc_trace(const orc_scene *scene, const orc_ray *rays, uint32_t n, orc_hit *hits,
+               int mode, uint32_t *stats, int threads);
+
+/* Render frames [first_frame, first_frame+spp) with the reference estimator.
+ * out_mean_rgba : (optional) the reference's f32 running mean (path_trace.wgsl:656-661),
+ *                 starting from zero, after the last frame.
+ * out_sum_rgb   : (optional) += f64 sum of samples per pixel (3 doubles per pixel).
+ * out_gbuf      : (optional) primary-hit normal.xyz + depth (path_trace.wgsl:593-601).
+ * max_depth     : bounces (the reference's MAX_BOUNCES is 8). */
+void orc_render(const orc_scene *scene, const orc_camera *cam, uint32_t w, uint32_t h,
+                uint32_t spp, uint32_t first_frame, uint32_t max_depth,
+                float *out_mean_rgba, double *out_sum_rgb, float *out_gbuf, int threads);
+
+/* Render a sub-rectangle of pixels (x0,y0,cw,ch) of a w x h image; outputs are cw*ch sized. */
+void orc_render_rect(const orc_scene *scene, const orc_camera *cam, uint32_t w, uint32_t h,
+                     uint32_t x0, uint32_t y0, uint32_t cw, uint32_t ch,
+                     uint32_t spp, uint32_t first_frame, uint32_t max_depth,
+                     float *out_mean_rgba, double *out_sum_rgb, float *out_gbuf, int threads);
+
+/* orc_render_rect that also returns traversal statistics of every closest-hit
+ * query of the sampled paths: out_stats[0] rays, [1] BVH nodes visited (popped
+ * and box-tested), [2] primitives tested — the per-ray figures of the
+ * bytes-per-ray memory roofline. */
+void orc_render_rect_stats(const orc_scene *scene, const orc_camera *cam, uint32_t w, uint32_t h,
+                           uint32_t x0, uint32_t y0, uint32_t cw, uint32_t ch, uint32_t spp, uint32_t first_frame,
+                           uint32_t max_depth, float *out_mean_rgba, double *out_sum_rgb, float *out_gbuf,
+                           int threads, uint64_t *out_stats);
+
+/* cs_denoise (denoise.wgsl:52-120). */
+void orc_denoise(const float *accum_rgba, const float *gbuf, uint32_t w, uint32_t h,
+                 int radius, float sigma_s, float sigma_d, float normal_pow, float *out_rgba);
+
+/* headless.rs:93-98 tonemap of an RGBA f32 image to RGBA8 (non-finite -> 0, alpha 255). */
+void orc_tonemap_rgba8(const float *rgba, uint32_t n_pixels, uint8_t *out);
+
+/* regression.rs:120-181 on RGBA8 images: out[0]=mse, out[1]=psnr, out[2]=max_delta. */
+void orc_compare_images(const uint8_t *a, const uint8_t *b, uint32_t w, uint32_t h, double *out);
+
+/* Elementary functions (exposed for their error-bound tests). */
+void orc_math_eval(int fn, const float *x, const float *y, float *out, uint32_t n);
+
+uint32_t orc_pcg_hash(uint32_t v);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

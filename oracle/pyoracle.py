@@ -1,0 +1,198 @@
+"""ctypes binding of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, as the checker.  The product never imports it.
+
+``OracleScene`` builds the reference BVHs (src/bvh.rs:239, src/mesh.rs:82) from
+the original primitive arrays with the oracle's restatement of the reference
+builder, and traces / renders with the restatement of path_trace.wgsl.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from ctypes import POINTER, c_double, c_float, c_int, c_uint8, c_uint32, c_void_p
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+SPHERE = np.dtype([("center_r", "<f4", 4), ("mat_and_pad", "<u4", 4)])
+NODE = np.dtype([("aabb_min", "<f4", 4), ("aabb_max", "<f4", 4), ("right_or_offset", "<u4"),
+                 ("prim_count", "<u4"), ("pad", "<u4", 2)])
+VERTEX = np.dtype([("position", "<f4", 4), ("normal", "<f4", 4), ("uv", "<f4", 4)])
+TRIANGLE = np.dtype([("v", "<u4", 3), ("mat_idx", "<u4")])
+RAY = np.dtype([("org", "<f4", 3), ("tmin", "<f4"), ("dir", "<f4", 3), ("tmax", "<f4")])
+HIT = np.dtype([("t", "<f4"), ("prim", "<u4"), ("u", "<f4"), ("v", "<f4")])
+
+
+class _Scene(ctypes.Structure):
+    _fields_ = [("spheres", c_void_p), ("n_spheres", c_uint32), ("sphere_ids", c_void_p),
+                ("sphere_nodes", c_void_p), ("n_sphere_nodes", c_uint32),
+                ("vertices", c_void_p), ("n_vertices", c_uint32),
+                ("triangles", c_void_p), ("n_triangles", c_uint32), ("triangle_ids", c_void_p),
+                ("mesh_nodes", c_void_p), ("n_mesh_nodes", c_uint32),
+                ("materials", c_void_p),
+                ("env_rgba", c_void_p), ("env_w", c_uint32), ("env_h", c_uint32)]
+
+
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.orc_build_sphere_bvh.restype = c_uint32
+        L.orc_build_sphere_bvh.argtypes = [c_void_p, c_uint32, c_void_p, c_void_p, c_void_p]
+        L.orc_build_mesh_bvh.restype = c_uint32
+        L.orc_build_mesh_bvh.argtypes = [c_void_p, c_uint32, c_void_p, c_uint32, c_void_p, c_void_p, c_void_p]
+        L.orc_trace.restype = None
+        L.orc_trace.argtypes = [POINTER(_Scene), c_void_p, c_uint32, c_void_p, c_int, c_void_p, c_int]
+        L.orc_render.restype = None
+        L.orc_render.argtypes = [POINTER(_Scene), c_void_p, c_uint32, c_uint32, c_uint32, c_uint32, c_uint32,
+                                 c_void_p, c_void_p, c_void_p, c_int]
+        L.orc_render_rect.restype = None
+        L.orc_render_rect.argtypes = [POINTER(_Scene), c_void_p, c_uint32, c_uint32, c_uint32, c_uint32, c_uint32,
+                                      c_uint32, c_uint32, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p, c_int]
+        L.orc_render_rect_stats.restype = None
+        L.orc_render_rect_stats.argtypes = [POINTER(_Scene), c_void_p, c_uint32, c_uint32, c_uint32, c_uint32,
+                                            c_uint32, c_uint32, c_uint32, c_uint32, c_uint32, c_void_p, c_void_p,
+                                            c_void_p, c_int, c_void_p]
+        L.orc_denoise.restype = None
+        L.orc_denoise.argtypes = [c_void_p, c_void_p, c_uint32, c_uint32, c_int, c_float, c_float, c_float, c_void_p]
+        L.orc_tonemap_rgba8.restype = None
+        L.orc_tonemap_rgba8.argtypes = [c_void_p, c_uint32, c_void_p]
+        L.orc_compare_images.restype = None
+        L.orc_compare_images.argtypes = [c_void_p, c_void_p, c_uint32, c_uint32, c_void_p]
+        L.orc_math_eval.restype = None
+        L.orc_math_eval.argtypes = [c_int, c_void_p, c_void_p, c_void_p, c_uint32]
+        L.orc_pcg_hash.restype = c_uint32
+        L.orc_pcg_hash.argtypes = [c_uint32]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(c_void_p)
+
+
+def build_sphere_bvh(spheres):
+    spheres = np.ascontiguousarray(spheres, SPHERE)
+    n = len(spheres)
+    nodes = np.zeros(max(2 * n, 1), NODE)
+    ordered = np.zeros(n, SPHERE)
+    ids = np.zeros(n, np.uint32)
+    nn = lib().orc_build_sphere_bvh(_p(spheres), n, _p(nodes), _p(ordered), _p(ids))
+    return nodes[:nn].copy(), ordered, ids
+
+
+def build_mesh_bvh(vertices, triangles):
+    vertices = np.ascontiguousarray(vertices, VERTEX)
+    triangles = np.ascontiguousarray(triangles, TRIANGLE)
+    n = len(triangles)
+    nodes = np.zeros(max(2 * n, 1), NODE)
+    ordered = np.zeros(n, TRIANGLE)
+    ids = np.zeros(n, np.uint32)
+    nn = lib().orc_build_mesh_bvh(_p(vertices), len(vertices), _p(triangles), n, _p(nodes), _p(ordered), _p(ids))
+    return nodes[:nn].copy(), ordered, ids
+
+
+class OracleScene:
+    """A scene as the reference binds it, built by the oracle's reference builder."""
+
+    def __init__(self, *, materials, spheres=None, vertices=None, triangles=None, env=None):
+        self.spheres_in = np.zeros(0, SPHERE) if spheres is None else np.ascontiguousarray(spheres, SPHERE)
+        self.vertices = np.zeros(0, VERTEX) if vertices is None else np.ascontiguousarray(vertices, VERTEX)
+        self.triangles_in = np.zeros(0, TRIANGLE) if triangles is None else np.ascontiguousarray(triangles, TRIANGLE)
+        self.materials = np.ascontiguousarray(materials)
+        self.sphere_nodes, self.spheres, self.sphere_ids = build_sphere_bvh(self.spheres_in)
+        self.mesh_nodes, self.triangles, self.triangle_ids = build_mesh_bvh(self.vertices, self.triangles_in)
+        self.env = None if env is None else np.ascontiguousarray(env, np.float32)
+        s = _Scene()
+        s.spheres, s.n_spheres, s.sphere_ids = _p(self.spheres), len(self.spheres), _p(self.sphere_ids)
+        s.sphere_nodes, s.n_sphere_nodes = _p(self.sphere_nodes), len(self.sphere_nodes)
+        s.vertices, s.n_vertices = _p(self.vertices), len(self.vertices)
+        s.triangles, s.n_triangles, s.triangle_ids = _p(self.triangles), len(self.triangles), _p(self.triangle_ids)
+        s.mesh_nodes, s.n_mesh_nodes = _p(self.mesh_nodes), len(self.mesh_nodes)
+        s.materials = _p(self.materials)
+        if self.env is not None:
+            s.env_rgba, s.env_h, s.env_w = _p(self.env), self.env.shape[0], self.env.shape[1]
+        self._s = s
+
+    def reference_buffers(self):
+        """The buffers the reference's build_scene_buffers would upload (ordered + BVHs + ids)."""
+        return dict(spheres=self.spheres, sphere_bvh=self.sphere_nodes, sphere_order=self.sphere_ids,
+                    vertices=self.vertices, triangles=self.triangles, mesh_bvh=self.mesh_nodes,
+                    triangle_order=self.triangle_ids, materials=self.materials, env=self.env)
+
+    def trace(self, rays, brute_force=False, threads=0, stats=False):
+        rays = np.ascontiguousarray(rays, RAY)
+        hits = np.zeros(len(rays), HIT)
+        st = np.zeros(2 * len(rays), np.uint32) if stats else None
+        lib().orc_trace(ctypes.byref(self._s), _p(rays), len(rays), _p(hits), 1 if brute_force else 0, _p(st),
+                        threads)
+        return (hits, st.reshape(-1, 2)) if stats else hits
+
+    def render(self, camera, w, h, spp, first_frame=0, max_depth=8, threads=0, rect=None, stats=False):
+        cam = np.ascontiguousarray(camera)
+        x0, y0, cw, ch = rect if rect else (0, 0, w, h)
+        mean = np.zeros((ch, cw, 4), np.float32)
+        acc = np.zeros((ch, cw, 3), np.float64)
+        gbuf = np.zeros((ch, cw, 4), np.float32)
+        st = np.zeros(3, np.uint64) if stats else None
+        lib().orc_render_rect_stats(ctypes.byref(self._s), _p(cam), w, h, x0, y0, cw, ch, spp, first_frame,
+                                    max_depth, _p(mean), _p(acc), _p(gbuf), threads, _p(st))
+        out = dict(rgba=mean, sum=acc, gbuf=gbuf)
+        if stats:
+            out["stats"] = dict(rays=int(st[0]), nodes=int(st[1]), prims=int(st[2]))
+        return out
+
+
+def denoise(rgba, gbuf, radius=3, sigma_s=2.0, sigma_d=0.5, normal_pow=8.0):
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    gbuf = np.ascontiguousarray(gbuf, np.float32)
+    h, w = rgba.shape[:2]
+    out = np.zeros_like(rgba)
+    lib().orc_denoise(_p(rgba), _p(gbuf), w, h, radius, sigma_s, sigma_d, normal_pow, _p(out))
+    return out
+
+
+def tonemap_rgba8(rgba):
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    out = np.zeros(rgba.shape[:-1] + (4,), np.uint8)
+    lib().orc_tonemap_rgba8(_p(rgba), rgba.size // 4, _p(out))
+    return out
+
+
+def compare_images(a, b):
+    """regression.rs compare_images on RGBA8 arrays: (mse, psnr, max_delta)."""
+    a = np.ascontiguousarray(a, np.uint8)
+    b = np.ascontiguousarray(b, np.uint8)
+    assert a.shape == b.shape
+    out = np.zeros(3, np.float64)
+    lib().orc_compare_images(_p(a), _p(b), a.shape[1], a.shape[0], _p(out))
+    return float(out[0]), float(out[1]), float(out[2])
+
+
+MATH_FNS = {"sin": 0, "cos": 1, "atan2": 2, "asin": 3, "exp": 4, "log": 5, "pow": 6, "tan": 7}
+
+
+def math_eval(fn, x, y=None):
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.ascontiguousarray(np.zeros_like(x) if y is None else y, np.float32)
+    out = np.zeros_like(x)
+    lib().orc_math_eval(MATH_FNS[fn], _p(x), _p(y), _p(out), x.size)
+    return out
+
+
+def pcg_hash(v):
+    return lib().orc_pcg_hash(v)

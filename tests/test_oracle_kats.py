@@ -1,0 +1,315 @@
+"""The oracle against the reference's own unit-test known answers (CPU only).
+
+Each test names the reference test it restates.  These pin the oracle's BVH
+builder, traversal and metrics before it is trusted as the checker.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import pyoracle as O
+
+
+def sph(cx, cz, r, mat=0):
+    s = np.zeros((), O.SPHERE)
+    s["center_r"] = (cx, 0.0, cz, r)
+    s["mat_and_pad"][0] = mat
+    return s
+
+
+def spheres(lst):
+    return np.array(lst, O.SPHERE)
+
+
+def check_tree(nodes, n_prims):
+    """Structural invariants of bvh.rs:540-677 / mesh.rs:789-831."""
+    n = len(nodes)
+    for i, nd in enumerate(nodes):
+        if nd["prim_count"] > 0:
+            assert nd["right_or_offset"] + nd["prim_count"] <= n_prims
+        else:
+            assert i + 1 < n and nd["right_or_offset"] < n
+    seen = np.zeros(n, bool)
+    stack = [0]
+    while stack:
+        i = stack.pop()
+        if seen[i]:
+            continue
+        seen[i] = True
+        if nodes[i]["prim_count"] == 0:
+            stack += [i + 1, int(nodes[i]["right_or_offset"])]
+    assert seen.all(), "orphan node"
+
+
+# ---------------------------------------------------------------- bvh.rs tests
+def test_empty_scene_produces_empty_result():                       # bvh.rs:478-483
+    nodes, ordered, ids = O.build_sphere_bvh(np.zeros(0, O.SPHERE))
+    assert len(nodes) == 0 and len(ordered) == 0
+
+
+def test_single_sphere_produces_one_leaf():                         # bvh.rs:511-523
+    nodes, ordered, _ = O.build_sphere_bvh(spheres([sph(0, 0, 0.5)]))
+    assert len(nodes) == 1 and nodes[0]["prim_count"] == 1 and nodes[0]["right_or_offset"] == 0
+    assert len(ordered) == 1
+
+
+def test_four_spheres_produce_one_leaf():                           # bvh.rs:525-539
+    nodes, ordered, _ = O.build_sphere_bvh(spheres([sph(i * 2.0, 0, 0.5) for i in range(4)]))
+    assert len(nodes) == 1 and nodes[0]["prim_count"] == 4 and len(ordered) == 4
+
+
+def test_large_scene_node_count_bounded():                          # bvh.rs:541-551
+    s = spheres([sph(i % 8, i // 8, 0.3) for i in range(64)])
+    nodes, ordered, _ = O.build_sphere_bvh(s)
+    assert len(nodes) < 2 * len(s) and len(ordered) == len(s)
+    check_tree(nodes, len(s))
+
+
+def test_ordered_spheres_contain_all_originals():                   # bvh.rs:553-573
+    s = spheres([sph(i, 0, 0.4, i % 4) for i in range(20)])
+    _, ordered, ids = O.build_sphere_bvh(s)
+    assert sorted(ids.tolist()) == list(range(20))
+    for k in range(20):
+        assert np.array_equal(ordered[k]["center_r"], s[ids[k]]["center_r"])
+
+
+def test_root_aabb_contains_all_spheres():                          # bvh.rs:575-590
+    s = spheres([sph(i, 0, 0.5) for i in range(16)])
+    nodes, _, _ = O.build_sphere_bvh(s)
+    for x in s:
+        cx, r = x["center_r"][0], x["center_r"][3]
+        assert cx - r >= nodes[0]["aabb_min"][0] - 1e-4 and cx + r <= nodes[0]["aabb_max"][0] + 1e-4
+
+
+def test_coincident_spheres_do_not_panic():                         # bvh.rs:640-647
+    s = spheres([sph(0, 0, 0.5, i % 4) for i in range(8)])
+    nodes, ordered, _ = O.build_sphere_bvh(s)
+    assert len(nodes) == 1 and nodes[0]["prim_count"] == 8 and len(ordered) == 8
+
+
+def test_no_orphan_nodes_and_children_in_bounds():                  # bvh.rs:592-638, :649-677
+    for s in (spheres([sph(i % 8, i // 8, 0.3) for i in range(48)]),
+              spheres([sph(i * 0.5, 0, 0.2) for i in range(32)]),
+              spheres([sph(i, 0, 0.4) for i in range(32)])):
+        nodes, _, _ = O.build_sphere_bvh(s)
+        check_tree(nodes, len(s))
+
+
+def _np_sphere_t(o, d, s, tmin, tmax):
+    """The reference test helper cpu_sphere_hit (bvh.rs:817-846) in float32 numpy."""
+    f = np.float32
+    c = s["center_r"]
+    oc = np.array(o, f) - c[:3]
+    a = f(d[0] * d[0] + d[1] * d[1]) + f(d[2] * d[2])
+    h = f(oc[0] * d[0] + oc[1] * d[1]) + f(oc[2] * d[2])
+    cc = f(f(oc[0] * oc[0] + oc[1] * oc[1]) + f(oc[2] * oc[2])) - f(c[3] * c[3])
+    disc = f(h * h) - f(a * cc)
+    if disc < 0:
+        return None
+    sq = np.sqrt(disc)
+    for t in (f(-h - sq) / a, f(-h + sq) / a):
+        if tmin < t < tmax:
+            return float(t)
+    return None
+
+
+def test_bvh_traversal_matches_brute_force():                       # bvh.rs:680-734
+    s = spheres([sph(i * 0.6 - 9.0, 0, 0.25) for i in range(32)])
+    sc = O.OracleScene(materials=np.zeros(1, np.uint8).repeat(3088), spheres=s)
+    rays_in = [((0, 5, 0), (0, -1, 0)), ((-10, 0, 5), (1, 0, 0)), ((0, 0, 5), (0, 0, -1)), ((5, 2, 0), (-0.5, -0.5, 0))]
+    rays = np.zeros(len(rays_in), O.RAY)
+    for k, (o, d) in enumerate(rays_in):
+        d = np.array(d, np.float32)
+        d = d / np.float32(np.sqrt(np.float32(d[0] * d[0] + d[1] * d[1]) + np.float32(d[2] * d[2])))
+        rays[k]["org"], rays[k]["dir"], rays[k]["tmin"], rays[k]["tmax"] = o, d, 1e-4, 1e9
+    hits = sc.trace(rays)
+    for k in range(len(rays)):
+        bf = [t for t in (_np_sphere_t(rays[k]["org"], rays[k]["dir"], x, 1e-4, 1e9) for x in s) if t is not None]
+        bf = min(bf) if bf else None
+        if bf is None:
+            assert hits[k]["prim"] == 0xFFFFFFFF
+        else:
+            assert hits[k]["prim"] != 0xFFFFFFFF and abs(hits[k]["t"] - bf) < 1e-4
+
+
+# ---------------------------------------------------------------- mesh.rs tests
+def uv_sphere(center, radius, stacks, slices, mat=0):
+    """The reference test generator build_uv_sphere_mesh (mesh.rs:305-372), restated in numpy."""
+    stacks, slices = max(stacks, 2), max(slices, 3)
+    V = []
+    for i in range(stacks + 1):
+        phi = np.float32(np.pi) * np.float32(i / stacks)
+        for j in range(slices + 1):
+            th = np.float32(2 * np.pi) * np.float32(j / slices)
+            n = np.array([np.sin(phi) * np.cos(th), np.cos(phi), np.sin(phi) * np.sin(th)], np.float32)
+            v = np.zeros((), O.VERTEX)
+            v["position"] = (*(np.array(center, np.float32) + np.float32(radius) * n), 1.0)
+            v["normal"][:3] = n
+            v["uv"][:2] = (j / slices, i / stacks)
+            V.append(v)
+    ring = slices + 1
+    T = []
+    for i in range(stacks):
+        for j in range(slices):
+            v00, v10, v01, v11 = i * ring + j, (i + 1) * ring + j, i * ring + j + 1, (i + 1) * ring + j + 1
+            if i > 0:
+                T.append(((v00, v10, v01), mat))
+            if i + 1 < stacks:
+                T.append(((v01, v10, v11), mat))
+    tri = np.zeros(len(T), O.TRIANGLE)
+    tri["v"] = [t[0] for t in T]
+    tri["mat_idx"] = [t[1] for t in T]
+    return np.array(V, O.VERTEX), tri
+
+
+def torus(major_r, minor_r, major_seg, minor_seg):
+    """build_torus_mesh (mesh.rs:383-445), restated in numpy."""
+    V = []
+    for i in range(major_seg + 1):
+        ph = 2 * np.pi * i / major_seg
+        for j in range(minor_seg + 1):
+            th = 2 * np.pi * j / minor_seg
+            v = np.zeros((), O.VERTEX)
+            v["position"] = ((major_r + minor_r * np.cos(th)) * np.cos(ph), minor_r * np.sin(th),
+                             (major_r + minor_r * np.cos(th)) * np.sin(ph), 1)
+            v["normal"][:3] = (np.cos(th) * np.cos(ph), np.sin(th), np.cos(th) * np.sin(ph))
+            V.append(v)
+    ring = minor_seg + 1
+    T = []
+    for i in range(major_seg):
+        for j in range(minor_seg):
+            v00, v10, v01, v11 = i * ring + j, (i + 1) * ring + j, i * ring + j + 1, (i + 1) * ring + j + 1
+            T += [(v00, v10, v01), (v01, v10, v11)]
+    tri = np.zeros(len(T), O.TRIANGLE)
+    tri["v"] = T
+    return np.array(V, O.VERTEX), tri
+
+
+def test_uv_sphere_and_torus_counts():                              # mesh.rs:733-778
+    v, t = uv_sphere((0, 0, 0), 1.0, 12, 24)
+    assert len(v) == 13 * 25 and len(t) == 2 * 11 * 24
+    v, t = torus(2.0, 0.5, 16, 8)
+    assert len(v) == 17 * 9 and len(t) == 2 * 16 * 8
+
+
+def test_triangle_aabb_flat_plane_has_positive_extent():            # mesh.rs:693-730
+    v = np.zeros(3, O.VERTEX)
+    v["position"][:, :3] = [(-1, 0, -5), (1, 0, -5), (0, 1, -5)]
+    t = np.zeros(1, O.TRIANGLE)
+    t["v"] = (0, 1, 2)
+    nodes, _, _ = O.build_mesh_bvh(v, t)
+    assert nodes[0]["aabb_max"][2] - nodes[0]["aabb_min"][2] > 1e-5
+    assert nodes[0]["aabb_max"][0] - nodes[0]["aabb_min"][0] > 0 and nodes[0]["aabb_max"][1] - nodes[0]["aabb_min"][1] > 0
+
+
+def test_empty_mesh_bvh_is_empty():                                 # mesh.rs:782-787
+    nodes, ordered, _ = O.build_mesh_bvh(np.zeros(0, O.VERTEX), np.zeros(0, O.TRIANGLE))
+    assert len(nodes) == 0 and len(ordered) == 0
+
+
+def test_mesh_bvh_structure():                                      # mesh.rs:789-831
+    v, t = uv_sphere((0, 0, 0), 1.0, 8, 16)
+    nodes, ordered, ids = O.build_mesh_bvh(v, t)
+    assert len(ordered) == len(t) and 0 < len(nodes) < 2 * len(t)
+    assert sorted(ids.tolist()) == list(range(len(t)))
+    check_tree(nodes, len(t))
+    v, t = torus(2.0, 0.5, 12, 8)
+    nodes, _, _ = O.build_mesh_bvh(v, t)
+    check_tree(nodes, len(t))
+
+
+def test_mesh_bvh_traversal_matches_brute_force():                  # mesh.rs:834-879
+    v, t = uv_sphere((0, 0, 0), 1.0, 6, 12)
+    sc = O.OracleScene(materials=np.zeros(3088, np.uint8), vertices=v, triangles=t)
+    rays_in = [((0, 5, 0), (0, -1, 0)), ((0, 0, 5), (0, 0, -1)), ((2, 2, 2), (-1, -1, -1))]
+    rays = np.zeros(len(rays_in), O.RAY)
+    for k, (o, d) in enumerate(rays_in):
+        d = np.array(d, np.float32)
+        d = d / np.float32(np.linalg.norm(d))
+        rays[k]["org"], rays[k]["dir"], rays[k]["tmin"], rays[k]["tmax"] = o, d, 1e-4, 1e9
+    h_bvh = sc.trace(rays)
+    h_bf = sc.trace(rays, brute_force=True)
+    for a, b in zip(h_bvh, h_bf):
+        assert (a["prim"] == 0xFFFFFFFF) == (b["prim"] == 0xFFFFFFFF)
+        if a["prim"] != 0xFFFFFFFF:
+            assert abs(a["t"] - b["t"]) < 1e-3
+            assert a["prim"] == b["prim"] and a["t"] == b["t"]    # stronger: exact, with the tie rule
+
+
+def test_random_rays_bvh_equals_brute_force():
+    """Beyond the reference's 7 rays: 20k seeded rays on a torus + sphere set, exact equality."""
+    rng = np.random.default_rng(7)
+    v, t = torus(2.0, 0.5, 24, 16)
+    s = spheres([sph(float(x), float(z), 0.3, 0) for x, z in rng.uniform(-3, 3, (10, 2))])
+    sc = O.OracleScene(materials=np.zeros(3088, np.uint8), vertices=v, triangles=t, spheres=s)
+    n = 20000
+    org = rng.uniform(-4, 4, (n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.zeros(n, O.RAY)
+    rays["org"], rays["dir"], rays["tmin"], rays["tmax"] = org, d, 1e-4, 1e9
+    a = sc.trace(rays)
+    b = sc.trace(rays, brute_force=True)
+    assert np.array_equal(a["prim"], b["prim"])
+    assert np.array_equal(a["t"].view(np.uint32), b["t"].view(np.uint32))
+    assert (a["prim"] != 0xFFFFFFFF).sum() > n // 10
+
+
+# ---------------------------------------------------------------- regression.rs metric KATs
+def solid(w, h, r, g, b, a=255):
+    x = np.zeros((h, w, 4), np.uint8)
+    x[...] = (r, g, b, a)
+    return x
+
+
+def test_metric_kats():                                             # regression.rs:368-432
+    mse, psnr, mx = O.compare_images(solid(4, 4, 128, 64, 255), solid(4, 4, 128, 64, 255))
+    assert mse == 0.0 and psnr == math.inf and mx == 0.0
+    mse, psnr, mx = O.compare_images(solid(2, 2, 0, 0, 0), solid(2, 2, 255, 255, 255))
+    assert abs(mse - 1.0) < 1e-12 and abs(psnr) < 1e-9 and abs(mx - 1.0) < 1e-12
+    mse, psnr, mx = O.compare_images(solid(1, 1, 128, 0, 0), solid(1, 1, 129, 0, 0))
+    d = 1.0 / 255.0
+    assert abs(mse - d * d / 3) < 1e-15 and abs(psnr - 10 * math.log10(3 / (d * d))) < 1e-6 and abs(mx - d) < 1e-15
+    mse, _, _ = O.compare_images(solid(2, 2, 100, 100, 100, 0), solid(2, 2, 100, 100, 100, 255))
+    assert mse == 0.0
+
+
+# ---------------------------------------------------------------- RNG and elementary functions
+def test_pcg_hash_matches_independent_restatement():                # path_trace.wgsl:194-199
+    def pcg(v):
+        s = (v * 747796405 + 2891336453) & 0xFFFFFFFF
+        rot = s >> 28
+        s = (((s >> (rot + 4)) ^ s) * 277803737) & 0xFFFFFFFF
+        return ((s >> 22) ^ s) & 0xFFFFFFFF
+    for v in [0, 1, 2, 12345, 0xFFFFFFFF, 2654435761] + list(range(1000, 1100)):
+        assert O.pcg_hash(v) == pcg(v)
+
+
+@pytest.mark.parametrize("fn,lo,hi,tol", [("sin", -10, 10, 3e-7), ("cos", -10, 10, 3e-7), ("tan", -1.4, 1.4, 2e-6)])
+def test_trig_error_bounds(fn, lo, hi, tol):
+    x = np.linspace(lo, hi, 200001).astype(np.float32)
+    got = O.math_eval(fn, x).astype(np.float64)
+    ref = getattr(np, fn)(x.astype(np.float64))
+    if fn == "tan":
+        assert np.max(np.abs(got - ref) / np.maximum(1, np.abs(ref))) < tol
+    else:
+        assert np.max(np.abs(got - ref)) < tol
+
+
+def test_inverse_trig_exp_log_pow_error_bounds():
+    rng = np.random.default_rng(0)
+    y = rng.uniform(-5, 5, 100000).astype(np.float32)
+    x = rng.uniform(-5, 5, 100000).astype(np.float32)
+    assert np.max(np.abs(O.math_eval("atan2", y, x) - np.arctan2(y.astype(np.float64), x))) < 5e-7
+    s = np.linspace(-1, 1, 100001).astype(np.float32)
+    assert np.max(np.abs(O.math_eval("asin", s) - np.arcsin(s.astype(np.float64)))) < 5e-6   # steep at |x| -> 1
+    e = np.linspace(-80, 80, 100001).astype(np.float32)
+    assert np.max(np.abs(O.math_eval("exp", e) / np.exp(e.astype(np.float64)) - 1)) < 6e-7
+    l = np.exp(np.linspace(-20, 20, 100001)).astype(np.float32)
+    ref = np.log(l.astype(np.float64))
+    assert np.max(np.abs(O.math_eval("log", l) - ref) / np.maximum(1.0, np.abs(ref))) < 2e-7
+    b = rng.uniform(0.001, 1, 100000).astype(np.float32)
+    for p in (5.0, 8.0, 1 / 2.2, 0.37):
+        got = O.math_eval("pow", b, np.full_like(b, p))
+        assert np.max(np.abs(got / np.power(b.astype(np.float64), p) - 1)) < 3e-6
