@@ -191,7 +191,7 @@ def run_reference(args):
     times = []
     sample = ""
     for i in range(args.warmup + args.steps):
-        t_frame, sample, _, _ = cpu_frame_estimate(sc, cam, rows_total=16, threads=cores)
+        t_frame, sample, _, _ = cpu_frame_estimate(sc, cam, rows_total=64, threads=cores)
         if i >= args.warmup:
             times.append(t_frame)
     t = sum(times) / len(times)
@@ -268,7 +268,7 @@ def run_mcrt(args):
     cpu = None
     st = None
     if not args.no_cpu_baseline:
-        t_frame, sample, st, _ = cpu_frame_estimate(sc, cam, rows_total=16, threads=os.cpu_count() or 1, stats=True)
+        t_frame, sample, st, _ = cpu_frame_estimate(sc, cam, rows_total=128, threads=os.cpu_count() or 1, stats=True)
         cpu = {"value": round(W * H * SPP / t_frame / 1e6, 4), "unit": "Msamples/s", "cores": os.cpu_count() or 1,
                "kind": "port", "sample": sample}
     ext_ms = sum(e[0] for e in ext)

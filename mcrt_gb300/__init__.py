@@ -196,10 +196,13 @@ class Context:
         ver = _arr(vertices, VERTEX)
         tri = _arr(triangles, TRIANGLE)
         mats = _arr(materials, MATERIAL_DATA)
-        sbvh = _arr(sphere_bvh, NODE)
-        mbvh = _arr(mesh_bvh, NODE)
-        sord = _arr(sphere_order, np.uint32)
-        tord = _arr(triangle_order, np.uint32)
+        def opt(a, dt):      # an empty prebuilt BVH / order means "none given"
+            a = _arr(a, dt)
+            return None if a is None or a.size == 0 else a
+        sbvh = opt(sphere_bvh, NODE)
+        mbvh = opt(mesh_bvh, NODE)
+        sord = opt(sphere_order, np.uint32)
+        tord = opt(triangle_order, np.uint32)
         envp = None if env is None else np.ascontiguousarray(env, np.float32)
         d = N.SceneDesc()
         d.spheres, d.n_spheres = ptr(sph), 0 if sph is None else len(sph)
