@@ -196,6 +196,28 @@ mcrt_status mcrt_render(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t 
                         uint32_t spp, uint32_t first_frame, const mcrt_render_opts *opts,
                         float *out_rgba, double *accum_rgb, float *out_gbuf);
 
+/* mcrt_render for callers that may not allocate GPU memory while rendering
+ * (no counterpart in the reference).  Hosts that reserve their GPU memory up
+ * front — an engine or viewer with a fixed memory budget, a renderer embedded
+ * in another application's frame loop — cannot accept cudaMalloc/cudaFree in
+ * the middle of a frame: those calls synchronise the device and can fail with
+ * out-of-memory.  This call allocates nothing: its path state lives in a 64 MiB
+ * statically sized device array that every GPU loading the library holds
+ * until the process exits.
+ *   - d_out_rgba: DEVICE memory owned by the caller, w*h*4 floats; receives the
+ *     f32 running mean of frames first_frame .. first_frame+spp-1 (alpha 1), as
+ *     out_rgba of mcrt_render.
+ *   - w*h must not exceed 262144 pixels (MCRT_ERR_INVALID_ARG otherwise);
+ *     KEEP_ACCUM is not supported; no G-buffer is produced.
+ *   - The scene is the one of an earlier mcrt_upload_scene on ctx.
+ *   - All calls share the one array: calls that overlap on the GPU (other
+ *     threads, streams or contexts on the same device) race; serialise them.
+ *   - The first call on a device resolves the array's device address; make it
+ *     before any stream capture begins on that device.
+ * Synchronous on return. */
+mcrt_status mcrt_render_noalloc(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t w, uint32_t h, uint32_t spp,
+                                uint32_t first_frame, const mcrt_render_opts *opts, float *d_out_rgba);
+
 /* Copy the device accumulation of the last render to the host (any may be NULL). */
 mcrt_status mcrt_read_accum(mcrt_ctx *ctx, float *out_rgba, double *accum_rgb, float *out_gbuf);
 

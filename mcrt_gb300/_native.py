@@ -99,6 +99,8 @@ SIGNATURES = [
     ("mcrt_trace_closest", c_int, [c_void_p, c_void_p, c_uint32, c_void_p, c_uint32]),
     ("mcrt_render", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_uint32, POINTER(RenderOpts),
                             c_void_p, c_void_p, c_void_p]),
+    ("mcrt_render_noalloc", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_uint32,
+                                    POINTER(RenderOpts), c_void_p]),
     ("mcrt_read_accum", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     ("mcrt_last_timings", c_int, [c_void_p, POINTER(c_float), POINTER(c_uint64)]),
     ("mcrt_denoise", c_int, [c_void_p, c_void_p, c_void_p, c_uint32, c_uint32, POINTER(DenoiseParams), c_void_p]),

@@ -727,3 +727,19 @@ mcrt_status mcrt_denoise(mcrt_ctx *ctx, const float *in_rgba, const float *gbuf,
 }
 
 }  // extern "C"
+
+namespace mcrt {
+// The device scene and stream of a context, for entry points defined in other
+// translation units.  *err receives the context's error string.
+bool context_scene(mcrt_ctx *ctx, DeviceScene *out, cudaStream_t *stream, int *device, std::string **err) {
+    *err = &ctx->err;
+    if (!ctx->has_scene) {
+        ctx->err = "no scene uploaded";
+        return false;
+    }
+    *out = device_scene(ctx);
+    *stream = ctx->stream;
+    *device = ctx->device;
+    return true;
+}
+}  // namespace mcrt
