@@ -47,7 +47,14 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="mcrt", choices=["mcrt", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
-    return p.parse_args()
+    p.add_argument("--small", action="store_true",
+                   help="same scene at 480x270, 4 spp: the profiling case (not a bench line)")
+    a = p.parse_args()
+    if a.small:
+        global W, H, SPP, WORKLOAD
+        W, H, SPP = 480, 270, 4
+        WORKLOAD = WORKLOAD.replace("1920x1080_16spp", "480x270_4spp")
+    return a
 
 
 def peaks():
@@ -230,12 +237,15 @@ def run_mcrt(args):
         ctx.update_vertices(sc["vertices"])
         ctx.render(cam, W, H, SPP, first_frame=i * SPP, max_depth=DEPTH, outputs=("rgba",))
 
+    breakdown = {}
+
     def timed(fn, n_warm, n_steps, sampler=None):
         for i in range(n_warm):
             fn(i)
         torch.cuda.synchronize()
         ms, extend = [], []
         launches = 0
+        breakdown.clear()
         for i in range(n_steps):
             flush.fill_(float(i))                         # evict the scene and path state from L2
             barrier(world)
@@ -250,10 +260,13 @@ def run_mcrt(args):
             t = ctx.timings()
             extend.append((t["extend_ms"], t["extend_launches"], t["rays"]))
             launches += t["render_launches"] + t["build_launches"]
+            for k in ("bvh_build_ms", "extend_ms", "shade_ms", "shadow_ms", "resolve_ms", "total_ms"):
+                breakdown[k] = breakdown.get(k, 0.0) + t[k] / n_steps
         return ms, extend, launches
 
     with ClockSampler(local) as clk:
         ms, ext, launches = timed(step_device, args.warmup, args.steps)
+    device_breakdown = {k: round(v, 3) for k, v in breakdown.items()}
     e2e_ms, _, _ = timed(step_e2e, args.warmup, args.steps)
     step_ms = max_over_ranks(sum(ms) / len(ms), world)
     e2e_step_ms = max_over_ranks(sum(e2e_ms) / len(e2e_ms), world)
@@ -299,6 +312,7 @@ def run_mcrt(args):
         "cpu_baseline": cpu,
         "clocks": clocks,
         "extend_ms_per_step": round(ext_ms / len(ext), 3),
+        "breakdown_ms_per_step": device_breakdown,
     }
     print(json.dumps(out))
     barrier(world)
