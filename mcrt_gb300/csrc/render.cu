@@ -333,7 +333,7 @@ __global__ void k_trace_closest(DeviceScene S, const mcrt_ray *rays, uint32_t n,
 __global__ void k_raygen(DeviceScene S, RenderParams P, PathBuffers B) {
     uint32_t n = P.npix * P.spp_pass;
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) { B.counters[0] = n; B.counters[1] = 0; B.counters[2] = 0; }
+    if (i == 0) { B.counters[0] = n; B.counters[1] = 0; B.counters[2] = 0; B.counters[4] = 0; B.counters[5] = 0; }
     if (i >= n) return;
     uint32_t k = i / P.npix;
     uint32_t p = i - k * P.npix;
@@ -349,20 +349,138 @@ __global__ void k_raygen(DeviceScene S, RenderParams P, PathBuffers B) {
     B.q_d[0][i] = make_float4(d.x, d.y, d.z, 0.0f);
 }
 
-__global__ void __launch_bounds__(128) k_extend(DeviceScene S, PathBuffers B, int qi) {
+// Closest hit for the queued rays: persistent warps with dynamic ray refill and
+// speculative while-while traversal of the compact BVH.
+//  * A warp fetches rays for its idle lanes in batches (one atomicAdd on the
+//    work counter counters[4] per batch) whenever at least kRefill lanes are
+//    idle, so lanes do not sit out the longest ray of a fixed assignment.
+//  * Traversal phase: a lane walks internal nodes; a leaf it reaches is
+//    postponed and the lane keeps traversing until every active lane of the
+//    warp holds a postponed leaf (warp vote); then the lanes test their leaves
+//    together.  The vote only shapes scheduling: the set of nodes and leaves
+//    visited per ray is decided by the same cull test (entry distance <=
+//    current closest t) as in the reference order, so the hit is the same.
+// Sphere BVHs (the reference's binding 5) are traversed at ray fetch with the
+// reference-order walk (spheres_hit); their count is small.
+constexpr int kRefill = 8;
+
+__global__ void __launch_bounds__(128, 8) k_extend(DeviceScene S, PathBuffers B, int qi) {
     const uint32_t n = B.counters[qi];
     if (blockIdx.x == 0 && threadIdx.x == 0) { B.counters[qi ^ 1] = 0; B.counters[2] = 0; }
     const float4 *qo = B.q_o[qi];
     const float4 *qd = B.q_d[qi];
+    const uint32_t lane = threadIdx.x & 31u;
+    const bool has_mesh = S.n_mesh_nodes > 0;
+    uint32_t ray = 0xffffffffu;       // queue index of the lane's ray, or none
+    bool exhausted = false;           // the queue has been handed out (warp-uniform)
+    RayInv r;
+    Closest best;
+    uint2 stack[kStackSize];
+    uint32_t sp = 0;
+    uint32_t cur = kNoChild;          // next node code to visit
+    float cur_t = 0.0f;               // its entry distance
+    uint32_t leaf = kNoChild;         // postponed leaf code
     uint32_t traced = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 o4 = qo[i], d4 = qd[i];
-        RayInv r = make_ray(xyz(o4), xyz(d4));
-        uint32_t nn = 0;
-        Closest c = world_hit(S, r, kTMin, kTMax, false, &nn, B.counters + 3);
-        float u = (c.prim != MCRT_HIT_MISS && (c.prim & MCRT_HIT_SPHERE)) ? __uint_as_float(c.slot) : c.u;
-        B.hits[i] = make_float4(c.t, __uint_as_float(c.prim), u, c.v);
-        ++traced;
+    uint32_t nn = 0;
+    for (;;) {
+        // ---- refill idle lanes
+        const bool idle = ray == 0xffffffffu;
+        const unsigned idle_mask = __ballot_sync(0xffffffffu, idle);
+        if (!exhausted && (__popc(idle_mask) >= kRefill || idle_mask == 0xffffffffu)) {
+            const int leader = __ffs(idle_mask) - 1;
+            uint32_t base = 0;
+            if ((int)lane == leader) base = atomicAdd(B.counters + 4, (uint32_t)__popc(idle_mask));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (base + (uint32_t)__popc(idle_mask) >= n) exhausted = true;
+            if (idle) {
+                const uint32_t mine = base + __popc(idle_mask & ((1u << lane) - 1u));
+                if (mine < n) {
+                    ray = mine;
+                    float4 o4 = qo[mine], d4 = qd[mine];
+                    r = make_ray(xyz(o4), xyz(d4));
+                    best = Closest{kTMax, MCRT_HIT_MISS, 0u, 0.0f, 0.0f};
+                    spheres_hit(S, r, kTMin, kTMax, best, &nn);      // path_trace.wgsl:472-474
+                    sp = 0;
+                    leaf = kNoChild;
+                    cur = kNoChild;
+                    if (has_mesh) {
+                        const float4 *np = reinterpret_cast<const float4 *>(S.mesh_nodes);
+                        float4 mn = __ldg(np), mx = __ldg(np + 1);
+                        float te;
+                        if (slab(r, mn.x, mn.y, mn.z, mx.x, mx.y, mx.z, kTMin, best.t, &te)) {
+                            if (S.n_cnodes == 0) {
+                                uint4 meta = __ldg(reinterpret_cast<const uint4 *>(np + 2));
+                                cur = leaf_code(meta.x, meta.y);
+                            } else {
+                                cur = 0;
+                            }
+                            cur_t = te;
+                        }
+                    }
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, ray != 0xffffffffu) == 0) break;   // exhausted and all idle
+        if (ray != 0xffffffffu) {
+            // ---- traversal phase
+            for (;;) {
+                if (cur != kNoChild && cur_t > best.t) cur = kNoChild;      // culled since it was queued
+                if (cur == kNoChild) {                                        // pop the next live entry
+                    while (sp > 0) {
+                        uint2 s = stack[--sp];
+                        if (__uint_as_float(s.y) <= best.t) { cur = s.x; cur_t = __uint_as_float(s.y); break; }
+                    }
+                    if (cur == kNoChild) break;
+                }
+                if (cur & kLeafBit) {
+                    if (leaf != kNoChild) break;                              // one leaf already waits
+                    leaf = cur;
+                    cur = kNoChild;
+                    continue;
+                }
+                const float4 *np = S.cnodes + 4ull * cur;
+                float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
+                uint4 e = __ldg(reinterpret_cast<const uint4 *>(np + 3));
+                ++nn;
+                float tl, tr;
+                bool hl = e.x != kNoChild && slab(r, a.x, a.z, c.x, a.y, a.w, c.y, kTMin, best.t, &tl);
+                bool hr = e.y != kNoChild && slab(r, b.x, b.z, c.z, b.y, b.w, c.w, kTMin, best.t, &tr);
+                if (hl && hr) {
+                    uint32_t near = e.x, far = e.y;
+                    float tnear = tl, tfar = tr;
+                    if (tr < tl) { near = e.y; far = e.x; tnear = tr; tfar = tl; }
+                    if (sp < kStackSize) stack[sp++] = make_uint2(far, __float_as_uint(tfar));
+                    else B.counters[3] = 1u;
+                    cur = near;
+                    cur_t = tnear;
+                } else if (hl) {
+                    cur = e.x; cur_t = tl;
+                } else if (hr) {
+                    cur = e.y; cur_t = tr;
+                } else {
+                    cur = kNoChild;
+                }
+                if (__all_sync(__activemask(), leaf != kNoChild)) break;
+            }
+            // ---- leaf phase
+            while (leaf != kNoChild) {
+                leaf_tris(S, r, (leaf & ~kLeafBit) >> 4, leaf_count(S, leaf), kTMin, best);
+                leaf = kNoChild;
+                if (cur != kNoChild && (cur & kLeafBit) && cur_t <= best.t) {
+                    leaf = cur;
+                    cur = kNoChild;
+                }
+            }
+            // ---- finished ray
+            if (cur == kNoChild && sp == 0) {
+                if (best.prim == MCRT_HIT_MISS) best.t = -1.0f;
+                float u = (best.prim != MCRT_HIT_MISS && (best.prim & MCRT_HIT_SPHERE)) ? __uint_as_float(best.slot)
+                                                                                         : best.u;
+                B.hits[ray] = make_float4(best.t, __uint_as_float(best.prim), u, best.v);
+                ray = 0xffffffffu;
+                ++traced;
+            }
+        }
     }
     if (traced) atomicAdd(B.stats, (unsigned long long)traced);
 }
@@ -372,6 +490,8 @@ __global__ void __launch_bounds__(256) k_shade(DeviceScene S, RenderParams P, Pa
     const uint32_t n = B.counters[qi];
     const bool nee = (P.flags & MCRT_RENDER_NEE) != 0 && S.n_lights > 0;
     const uint32_t lane = threadIdx.x & 31u;
+    // work counters of the next extend and shadow launches (no kernel reads them now)
+    if (blockIdx.x == 0 && threadIdx.x == 0) { B.counters[4] = 0; B.counters[5] = 0; }
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t i = base + threadIdx.x;
@@ -621,8 +741,14 @@ void launch_raygen(const DeviceScene &S, const RenderParams &P, PathBuffers &B, 
 }
 
 void launch_extend(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, cudaStream_t st) {
+    // persistent: as many resident blocks as fit, never more warps than rays
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_extend, 128, 0);
+        if (per_sm <= 0) per_sm = 1;
+    }
     uint32_t nmax = P.npix * P.spp_pass;
-    int blocks = min(grid_blocks_for(nmax, 128), sm_count() * 16);
+    int blocks = min(grid_blocks_for(nmax, 128), sm_count() * per_sm);
     k_extend<<<blocks, 128, 0, st>>>(S, B, qi); ::mcrt::note_launch();
 }
 
