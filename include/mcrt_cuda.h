@@ -129,6 +129,10 @@ typedef struct {
     const uint32_t *triangle_order;
     const mcrt_gpu_material_data *materials;
     const float *env_rgba; uint32_t env_w; uint32_t env_h;
+    /* binding 10: albedo texture array, RGBA8 sRGB, albedo_layers x size x size
+     * (gpu_layout.rs:435-477; 4 x 512 x 512 in the reference).  NULL: the
+     * reference's default layers (mcrt_albedo_layers). */
+    const uint8_t *albedo_rgba8; uint32_t albedo_layers; uint32_t albedo_size;
     uint32_t flags; /* reserved, 0 */
 } mcrt_scene_desc;
 
@@ -286,6 +290,15 @@ mcrt_status mcrt_compute_camera(uint32_t width, uint32_t height, const float loo
 mcrt_status mcrt_load_env_map(const char *path, float *out);
 /* build_gradient_env_map (texture.rs:158-199). */
 mcrt_status mcrt_gradient_env_map(float *out);
+
+/* The reference's albedo texture array (load_all_textures, texture.rs:235-256):
+ * 4 layers of 512 x 512 RGBA8 — layer 0 white, layer 1 the grey checker,
+ * layers 2 and 3 the magenta "missing texture" checker (no texture files are
+ * read; texture.rs:66-110 falls back to it when textures/earth.png is absent).
+ * out must hold 4*512*512*4 bytes. */
+#define MCRT_TEXTURE_SIZE 512
+#define MCRT_TEXTURE_LAYERS 4
+mcrt_status mcrt_albedo_layers(uint8_t *out);
 
 /* tonemap_to_u8 over an RGBA32F image (headless.rs:93-98, :350-368): RGBA8, alpha 255. */
 mcrt_status mcrt_tonemap_rgba8(const float *rgba, uint32_t n_pixels, uint8_t *out);

@@ -118,6 +118,13 @@ def gradient_env_map() -> np.ndarray:
     return out
 
 
+def albedo_layers() -> np.ndarray:
+    """The reference's default albedo texture array (4 x 512 x 512 RGBA8)."""
+    out = np.zeros((4, 512, 512, 4), np.uint8)
+    check(lib().mcrt_albedo_layers(ptr(out)))
+    return out
+
+
 def tonemap_rgba8(rgba: np.ndarray) -> np.ndarray:
     rgba = np.ascontiguousarray(rgba, np.float32)
     out = np.zeros(rgba.shape[:-1] + (4,), np.uint8)
@@ -191,7 +198,7 @@ class Context:
         check(s, self._h)
 
     def upload_scene(self, *, materials, spheres=None, vertices=None, triangles=None, env=None, sphere_bvh=None,
-                     sphere_order=None, mesh_bvh=None, triangle_order=None):
+                     sphere_order=None, mesh_bvh=None, triangle_order=None, albedo=None):
         sph = _arr(spheres, SPHERE)
         ver = _arr(vertices, VERTEX)
         tri = _arr(triangles, TRIANGLE)
@@ -215,6 +222,9 @@ class Context:
         d.materials = ptr(mats)
         if envp is not None:
             d.env_rgba, d.env_h, d.env_w = ptr(envp), envp.shape[0], envp.shape[1]
+        alb = None if albedo is None else np.ascontiguousarray(albedo, np.uint8)
+        if alb is not None:
+            d.albedo_rgba8, d.albedo_layers, d.albedo_size = ptr(alb), alb.shape[0], alb.shape[1]
         self._check(lib().mcrt_upload_scene(self._h, ctypes.byref(d)))
         self.n_triangles = d.n_triangles
 

@@ -61,6 +61,7 @@ class SceneDesc(ctypes.Structure):
                 ("triangle_order", c_void_p),
                 ("materials", c_void_p),
                 ("env_rgba", c_void_p), ("env_w", c_uint32), ("env_h", c_uint32),
+                ("albedo_rgba8", c_void_p), ("albedo_layers", c_uint32), ("albedo_size", c_uint32),
                 ("flags", c_uint32)]
 
 
@@ -113,6 +114,7 @@ SIGNATURES = [
                                     c_float, c_void_p]),
     ("mcrt_load_env_map", c_int, [c_char_p, c_void_p]),
     ("mcrt_gradient_env_map", c_int, [c_void_p]),
+    ("mcrt_albedo_layers", c_int, [c_void_p]),
     ("mcrt_tonemap_rgba8", c_int, [c_void_p, c_uint32, c_void_p]),
     ("mcrt_write_png", c_int, [c_char_p, c_void_p, c_uint32, c_uint32]),
     ("mcrt_headless_run", c_int, [c_char_p, c_char_p, c_uint32, c_uint32, c_uint32, POINTER(RenderOpts)]),

@@ -76,7 +76,9 @@ struct mcrt_ctx {
     // scene
     bool has_scene = false;
     DBuf spheres, sphere_ids, sphere_nodes, vertices, triangles, mesh_nodes, tri_order, trirecs, cnodes, materials,
-        env, lights, light_cdf, tmp, staging;
+        env, lights, light_cdf, tmp, staging, albedo;
+    uint32_t albedo_layers = 0, albedo_size = 0;
+    size_t srgb_lut_offset = 0;
     uint32_t n_spheres = 0, n_sphere_nodes = 0, n_vertices = 0, n_triangles = 0, n_mesh_nodes = 0, n_cnodes = 0,
              n_lights = 0, env_w = 0, env_h = 0;
     float light_total = 0.0f;
@@ -140,6 +142,10 @@ mcrt::DeviceScene device_scene(const mcrt_ctx *c) {
     S.n_lights = c->n_lights;
     S.light_cdf = c->light_cdf.as<float>();
     S.light_total = c->light_total;
+    S.albedo = c->albedo.as<uchar4>();
+    S.albedo_layers = c->albedo_layers;
+    S.albedo_size = c->albedo_size;
+    S.srgb_lut = reinterpret_cast<const float *>(c->albedo.as<char>() + c->srgb_lut_offset);
     return S;
 }
 
@@ -291,7 +297,7 @@ void mcrt_destroy(mcrt_ctx *ctx) {
     cudaStreamSynchronize(ctx->stream);
     DBuf *bufs[] = {&ctx->spheres, &ctx->sphere_ids, &ctx->sphere_nodes, &ctx->vertices, &ctx->triangles,
                     &ctx->mesh_nodes, &ctx->tri_order, &ctx->trirecs, &ctx->cnodes, &ctx->materials, &ctx->env,
-                    &ctx->lights, &ctx->light_cdf, &ctx->tmp, &ctx->staging, &ctx->pbmem, &ctx->mean,
+                    &ctx->lights, &ctx->light_cdf, &ctx->tmp, &ctx->staging, &ctx->albedo, &ctx->pbmem, &ctx->mean,
                     &ctx->sum, &ctx->gbuf, &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->counters};
     for (DBuf *b : bufs) b->release();
     mcrt::free_bvh_scratch(ctx->bvh_scratch);
@@ -405,6 +411,32 @@ mcrt_status mcrt_upload_scene(mcrt_ctx *ctx, const mcrt_scene_desc *d) {
         }
     } else {
         ctx->n_cnodes = 0;
+    }
+    // ---- albedo texture array (binding 10)
+    {
+        uint32_t layers = d->albedo_rgba8 ? d->albedo_layers : MCRT_TEXTURE_LAYERS;
+        uint32_t size = d->albedo_rgba8 ? d->albedo_size : MCRT_TEXTURE_SIZE;
+        if (layers == 0 || size == 0 || (uint64_t)layers * size * size > (1ull << 28))
+            return fail(ctx, MCRT_ERR_INVALID_ARG, "invalid albedo texture array size");
+        size_t bytes = (size_t)layers * size * size * 4;
+        CK(ctx->albedo.ensure(bytes + 1024), "allocate albedo array");
+        std::vector<float> lut(256);
+        for (int i = 0; i < 256; ++i) {
+            double c = i / 255.0;
+            lut[i] = (float)(c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4));
+        }
+        CK(cudaMemcpyAsync(ctx->albedo.as<char>() + bytes, lut.data(), 1024, cudaMemcpyHostToDevice, st), "upload");
+        if (d->albedo_rgba8) {
+            CK(cudaMemcpyAsync(ctx->albedo.p, d->albedo_rgba8, bytes, cudaMemcpyHostToDevice, st), "upload");
+        } else {
+            std::vector<uint8_t> def(bytes);
+            mcrt_albedo_layers(def.data());
+            CK(cudaMemcpyAsync(ctx->albedo.p, def.data(), bytes, cudaMemcpyHostToDevice, st), "upload");
+        }
+        CK(cudaStreamSynchronize(st), "upload");
+        ctx->srgb_lut_offset = bytes;
+        ctx->albedo_layers = layers;
+        ctx->albedo_size = size;
     }
     // ---- materials, environment
     CK(ctx->materials.ensure(sizeof(mcrt_gpu_material_data)), "allocate materials");

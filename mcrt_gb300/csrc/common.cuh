@@ -97,6 +97,11 @@ struct DeviceScene {
     const uint32_t *lights; uint32_t n_lights;      // MCRT_HIT_SPHERE|sphere slot, or triangle id
     const float *light_cdf;                          // n_lights+1 entries, light_cdf[n] = 1
     float light_total;                               // sum of unnormalised weights
+    // albedo texture array (RGBA8 sRGB), layers x size x size texels, and the
+    // sRGB -> linear decode table of an 8-bit channel (IEC 61966-2-1, evaluated
+    // on the host in double precision and rounded to float)
+    const uchar4 *albedo; uint32_t albedo_layers, albedo_size;
+    const float *srgb_lut;
 };
 
 }  // namespace mcrt

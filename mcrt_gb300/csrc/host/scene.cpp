@@ -816,6 +816,24 @@ mcrt_status mcrt_load_env_map(const char *path, float *out) {
     return MCRT_OK;
 }
 
+mcrt_status mcrt_albedo_layers(uint8_t *out) {
+    if (!out) { mcrt::set_global_error("NULL argument"); return MCRT_ERR_INVALID_ARG; }
+    // build_checker_texture (texture.rs:46-61): tiles of size/8 pixels
+    auto checker = [](uint8_t *dst, const uint8_t a[4], const uint8_t b[4]) {
+        const uint32_t n = MCRT_TEXTURE_SIZE, tile = n / 8 ? n / 8 : 1;
+        for (uint32_t y = 0; y < n; ++y)
+            for (uint32_t x = 0; x < n; ++x) memcpy(dst + 4 * ((size_t)y * n + x), ((x / tile + y / tile) % 2 == 0) ? a : b, 4);
+    };
+    const size_t layer = (size_t)MCRT_TEXTURE_SIZE * MCRT_TEXTURE_SIZE * 4;
+    memset(out, 255, layer);                                                        // layer 0: white
+    const uint8_t grey_a[4] = {220, 220, 220, 255}, grey_b[4] = {50, 50, 50, 255};  // texture.rs:245-252
+    const uint8_t mag_a[4] = {200, 0, 200, 255}, mag_b[4] = {30, 30, 30, 255};      // texture.rs:105-107
+    checker(out + layer, grey_a, grey_b);
+    checker(out + 2 * layer, mag_a, mag_b);
+    checker(out + 3 * layer, mag_a, mag_b);
+    return MCRT_OK;
+}
+
 mcrt_status mcrt_gradient_env_map(float *out) {
     if (!out) { mcrt::set_global_error("NULL argument"); return MCRT_ERR_INVALID_ARG; }
     mcrt_host::gradient_env_map(out);

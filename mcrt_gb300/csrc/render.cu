@@ -102,6 +102,64 @@ __device__ __forceinline__ SurfaceHit surface(const DeviceScene &S, f3 o, f3 d, 
     return s;
 }
 
+// Texture coordinates of a hit, evaluated only for textured materials:
+// triangles interpolate vertex uvs (path_trace.wgsl:459), spheres use the
+// longitude/latitude mapping of the outward normal (:288-291).
+__device__ __forceinline__ void hit_uv(const DeviceScene &S, f3 p, float4 h, float *u_out, float *v_out) {
+    uint32_t prim = __float_as_uint(h.y);
+    if (prim & MCRT_HIT_SPHERE) {
+        float4 cr = __ldg(reinterpret_cast<const float4 *>(S.spheres + __float_as_uint(h.z)));
+        f3 outn = (p - xyz(cr)) / cr.w;
+        float phi = dm_atan2(outn.z, outn.x);
+        float theta = dm_asin(fminf(fmaxf(outn.y, -1.0f), 1.0f));
+        *u_out = phi / kTau + 0.5f;
+        *v_out = 0.5f - theta / kPi;
+        return;
+    }
+    mcrt_gpu_triangle tri = S.triangles[prim];
+    const float *ua = S.vertices[tri.v[0]].uv, *ub = S.vertices[tri.v[1]].uv, *uc = S.vertices[tri.v[2]].uv;
+    float u = h.z, v = h.w, w = 1.0f - u - v;
+    *u_out = (w * ua[0] + u * ub[0]) + v * uc[0];
+    *v_out = (w * ua[1] + u * ub[1]) + v * uc[1];
+}
+
+// textureSampleLevel with a linear, repeat sampler (headless.rs:184-191) on an
+// RGBA8 sRGB array: texel centres at (i + 0.5) / N, channels decoded to linear
+// before filtering, weights (1 - f, f) per axis.
+__device__ __forceinline__ f3 sample_albedo(const DeviceScene &S, uint32_t layer, float u, float v) {
+    const int N = (int)S.albedo_size;
+    float x = u * (float)N - 0.5f, y = v * (float)N - 0.5f;
+    if (!(fabsf(x) < 1e8f)) x = 0.0f;
+    if (!(fabsf(y) < 1e8f)) y = 0.0f;
+    float x0 = floorf(x), y0 = floorf(y);
+    float fx = x - x0, fy = y - y0;
+    int ix = (int)x0 % N, iy = (int)y0 % N;
+    if (ix < 0) ix += N;
+    if (iy < 0) iy += N;
+    int ix1 = ix + 1 == N ? 0 : ix + 1, iy1 = iy + 1 == N ? 0 : iy + 1;
+    const uchar4 *base = S.albedo + (size_t)layer * N * N;
+    auto texel = [&](int tx, int ty) {
+        uchar4 t = __ldg(base + (size_t)ty * N + tx);
+        return mk3(__ldg(S.srgb_lut + t.x), __ldg(S.srgb_lut + t.y), __ldg(S.srgb_lut + t.z));
+    };
+    f3 t00 = texel(ix, iy), t10 = texel(ix1, iy), t01 = texel(ix, iy1), t11 = texel(ix1, iy1);
+    float gx = 1.0f - fx, gy = 1.0f - fy;
+    f3 top = gx * t00 + fx * t10;
+    f3 bot = gx * t01 + fx * t11;
+    return gy * top + fy * bot;
+}
+
+// material_albedo, path_trace.wgsl:506-515
+__device__ __forceinline__ f3 material_albedo(const DeviceScene &S, const mcrt_gpu_material &m, f3 p, float4 h) {
+    f3 albedo = ld3(m.albedo_fuzz);
+    uint32_t layer = m.type_pad[1];
+    if (layer == 0u || S.albedo_layers == 0u) return albedo;
+    uint32_t safe = min(layer, S.albedo_layers - 1u);
+    float u, v;
+    hit_uv(S, p, h, &u, &v);
+    return sample_albedo(S, safe, u, v) * albedo;
+}
+
 // GGX conductor (extension): Trowbridge-Reitz distribution, Smith
 // height-correlated masking-shadowing, Schlick Fresnel with F0 = albedo;
 // sampled by visible normals (Heitz 2018, "Sampling the GGX Distribution of
@@ -536,6 +594,7 @@ __global__ void __launch_bounds__(256) k_shade(DeviceScene S, RenderParams P, Pa
                         B.L[slot] = make_float4(e.x, e.y, e.z, 0.0f);
                     }
                 } else {
+                    albedo = material_albedo(S, m, sh.p, h);                    // :506-515
                     f3 dir = {0, 0, 0}, atten = {0, 0, 0};
                     bool absorbed = false;
                     float pdf = -1.0f;

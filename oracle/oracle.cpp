@@ -333,6 +333,128 @@ inline float schlick(float cos_theta, float eta) {
 
 /* path_color, path_trace.wgsl:583-620 (+ G-buffer :592-602) */
 /* stats (optional): [0] rays traced, [1] nodes visited, [2] primitives tested */
+/* uv of a hit: triangles interpolate vertex uvs (path_trace.wgsl:459); spheres
+ * map the outward normal to longitude / latitude (:288-291). */
+void hit_uv(const orc_scene *sc, const Closest &c, V3 p, float *uo, float *vo) {
+    if (c.prim & ORC_HIT_SPHERE) {
+        const orc_sphere &s = sc->spheres[c.slot];
+        V3 outn = (p - ld3(s.center_r)) / s.center_r[3];
+        float phi = of_atan2(outn.z, outn.x);
+        float theta = of_asin(fminf(fmaxf(outn.y, -1.0f), 1.0f));
+        *uo = phi / TAU + 0.5f;
+        *vo = 0.5f - theta / PI_F;
+        return;
+    }
+    const orc_triangle &tri = sc->triangles[c.slot];
+    const float *ua = sc->vertices[tri.v[0]].uv, *ub = sc->vertices[tri.v[1]].uv, *uc = sc->vertices[tri.v[2]].uv;
+    float u = c.u, v = c.v, w = 1.0f - u - v;
+    *uo = (w * ua[0] + u * ub[0]) + v * uc[0];
+    *vo = (w * ua[1] + u * ub[1]) + v * uc[1];
+}
+
+/* sRGB -> linear of an 8-bit channel (IEC 61966-2-1) in double, rounded to float */
+const float *srgb_table() {
+    static float t[256];
+    static bool init = false;
+    if (!init) {
+        for (int i = 0; i < 256; ++i) {
+            double c = i / 255.0;
+            t[i] = (float)(c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4));
+        }
+        init = true;
+    }
+    return t;
+}
+
+/* textureSampleLevel of an Rgba8UnormSrgb array with a linear / repeat sampler
+ * (gpu_layout.rs:435-477, headless.rs:184-191): texel centres at (i+0.5)/N,
+ * decode then filter, weights (1-f, f). */
+V3 sample_albedo(const orc_scene *sc, uint32_t layer, float u, float v) {
+    const int N = (int)sc->albedo_size;
+    const float *lut = srgb_table();
+    float x = u * (float)N - 0.5f, y = v * (float)N - 0.5f;
+    if (!(fabsf(x) < 1e8f)) x = 0.0f;
+    if (!(fabsf(y) < 1e8f)) y = 0.0f;
+    float x0 = floorf(x), y0 = floorf(y);
+    float fx = x - x0, fy = y - y0;
+    int ix = (int)x0 % N, iy = (int)y0 % N;
+    if (ix < 0) ix += N;
+    if (iy < 0) iy += N;
+    int ix1 = ix + 1 == N ? 0 : ix + 1, iy1 = iy + 1 == N ? 0 : iy + 1;
+    const uint8_t *base = sc->albedo_rgba8 + (size_t)layer * N * N * 4;
+    auto texel = [&](int tx, int ty) {
+        const uint8_t *t = base + 4 * ((size_t)ty * N + tx);
+        return V3{lut[t[0]], lut[t[1]], lut[t[2]]};
+    };
+    V3 t00 = texel(ix, iy), t10 = texel(ix1, iy), t01 = texel(ix, iy1), t11 = texel(ix1, iy1);
+    float gx = 1.0f - fx, gy = 1.0f - fy;
+    V3 top = gx * t00 + fx * t10;
+    V3 bot = gx * t01 + fx * t11;
+    return gy * top + fy * bot;
+}
+
+/* material_albedo, path_trace.wgsl:506-515 */
+V3 material_albedo(const orc_scene *sc, const orc_material &m, const Closest &c, V3 p) {
+    V3 albedo = ld3(m.albedo_fuzz);
+    uint32_t layer = m.type_pad[1];
+    if (layer == 0u || sc->albedo_layers == 0u || !sc->albedo_rgba8) return albedo;
+    uint32_t safe = std::min(layer, sc->albedo_layers - 1u);
+    float u, v;
+    hit_uv(sc, c, p, &u, &v);
+    return sample_albedo(sc, safe, u, v) * albedo;
+}
+
+/* GGX conductor (an extension of the reference, material type 4): the same
+ * Trowbridge-Reitz / Smith height-correlated / Schlick model and visible-normal
+ * sampling (Heitz 2018) as the kernels, so the reference estimator with GGX is
+ * reproduced sample for sample. */
+constexpr uint32_t MAT_GGX = 4u;
+inline void onb(V3 n, V3 *t, V3 *b) {   /* Duff et al. 2017 */
+    float sign = n.z >= 0.0f ? 1.0f : -1.0f;
+    float a = -1.0f / (sign + n.z);
+    float bb = n.x * n.y * a;
+    *t = {1.0f + sign * n.x * n.x * a, sign * bb, -sign * n.x};
+    *b = {bb, sign + n.y * n.y * a, -n.y};
+}
+inline float ggx_lambda(float alpha, float cos_t) {
+    float c2 = cos_t * cos_t;
+    float t2 = fmaxf(0.0f, 1.0f - c2) / fmaxf(c2, 1e-12f);
+    return 0.5f * (-1.0f + sqrtf(1.0f + alpha * alpha * t2));
+}
+inline float ggx_d(float alpha, float cos_h) {
+    float a2 = alpha * alpha;
+    float c2 = cos_h * cos_h;
+    float den = c2 * (a2 - 1.0f) + 1.0f;
+    return a2 / (PI_F * den * den);
+}
+bool ggx_sample(V3 wo, float alpha, V3 f0, float r1, float r2, V3 *wi_out, V3 *weight) {
+    V3 vh = normalize({alpha * wo.x, alpha * wo.y, wo.z});
+    float lensq = vh.x * vh.x + vh.y * vh.y;
+    V3 t1 = lensq > 0.0f ? V3{-vh.y, vh.x, 0.0f} / sqrtf(lensq) : V3{1.0f, 0.0f, 0.0f};
+    V3 t2 = cross(vh, t1);
+    float r = sqrtf(r1);
+    float phi = 2.0f * PI_F * r2;
+    float sp, cp;
+    of_sincos(phi, &sp, &cp);
+    float p1 = r * cp;
+    float p2 = r * sp;
+    float s = 0.5f * (1.0f + vh.z);
+    p2 = (1.0f - s) * sqrtf(fmaxf(0.0f, 1.0f - p1 * p1)) + s * p2;
+    V3 nh = (p1 * t1 + p2 * t2) + sqrtf(fmaxf(0.0f, 1.0f - p1 * p1 - p2 * p2)) * vh;
+    V3 m = normalize({alpha * nh.x, alpha * nh.y, fmaxf(1e-6f, nh.z)});
+    float wo_m = dot(wo, m);
+    V3 wi = (2.0f * wo_m) * m - wo;
+    if (wi.z <= 0.0f) return false;
+    float l_o = ggx_lambda(alpha, wo.z), l_i = ggx_lambda(alpha, wi.z);
+    float g1 = 1.0f / (1.0f + l_o);
+    float g2 = 1.0f / ((1.0f + l_o) + l_i);
+    float fw = of_pow(1.0f - fmaxf(0.0f, wo_m), 5.0f);
+    V3 F = f0 + fw * (V3{1.0f, 1.0f, 1.0f} - f0);
+    *weight = (g2 / g1) * F;
+    *wi_out = wi;
+    return true;
+}
+
 V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, float *gbuf, uint64_t *stats) {
     V3 thr = {1.0f, 1.0f, 1.0f};
     bool first = true;
@@ -354,9 +476,24 @@ V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, f
         V3 albedo = ld3(m.albedo_fuzz);
         if (m.type_pad[0] == MAT_EMISSIVE)                                     /* :608-610 */
             return m.ior_pad[0] * (thr * albedo);
+        albedo = material_albedo(sc, m, c, h.p);                               /* :506-515 */
         V3 dir, atten;
         bool absorbed = false;
-        if (m.type_pad[0] == MAT_METAL) {                                      /* :530-541 */
+        if (m.type_pad[0] == MAT_GGX) {
+            V3 t, b;
+            onb(h.n, &t, &b);
+            V3 wo = {-dot(ray.d, t), -dot(ray.d, b), -dot(ray.d, h.n)};
+            float rough = m.albedo_fuzz[3];
+            float alpha = fmaxf(rough * rough, 1e-4f);
+            float r1 = rand_f32(rng), r2 = rand_f32(rng);
+            V3 wi, wgt;
+            if (wo.z > 0.0f && ggx_sample(wo, alpha, albedo, r1, r2, &wi, &wgt)) {
+                dir = normalize((wi.x * t + wi.y * b) + wi.z * h.n);
+                atten = wgt;
+            } else {
+                absorbed = true;
+            }
+        } else if (m.type_pad[0] == MAT_METAL) {                               /* :530-541 */
             float fuzz = m.albedo_fuzz[3];
             V3 refl = reflect_vec(normalize(ray.d), h.n);
             V3 pert = refl + fuzz * random_unit_sphere(rng);

@@ -44,6 +44,7 @@ typedef struct {
     const orc_node *mesh_nodes; uint32_t n_mesh_nodes;
     const orc_material_data *materials;
     const float *env_rgba; uint32_t env_w; uint32_t env_h;
+    const uint8_t *albedo_rgba8; uint32_t albedo_layers; uint32_t albedo_size;  /* binding 10 (sRGB) */
 } orc_scene;
 
 #define ORC_HIT_MISS 0xffffffffu

@@ -35,7 +35,24 @@ class _Scene(ctypes.Structure):
                 ("triangles", c_void_p), ("n_triangles", c_uint32), ("triangle_ids", c_void_p),
                 ("mesh_nodes", c_void_p), ("n_mesh_nodes", c_uint32),
                 ("materials", c_void_p),
-                ("env_rgba", c_void_p), ("env_w", c_uint32), ("env_h", c_uint32)]
+                ("env_rgba", c_void_p), ("env_w", c_uint32), ("env_h", c_uint32),
+                ("albedo", c_void_p), ("albedo_layers", c_uint32), ("albedo_size", c_uint32)]
+
+
+def default_albedo_layers(size=512):
+    """load_all_textures (texture.rs:235-256) without texture files: white, grey
+    checker, magenta checker, magenta checker (build_checker_texture, :46-61)."""
+    tile = max(size // 8, 1)
+    y, x = np.mgrid[0:size, 0:size]
+    sel = ((x // tile + y // tile) % 2 == 0)[..., None]
+    def checker(a, b):
+        return np.where(sel, np.array(a, np.uint8), np.array(b, np.uint8)).astype(np.uint8)
+    out = np.zeros((4, size, size, 4), np.uint8)
+    out[0] = 255
+    out[1] = checker((220, 220, 220, 255), (50, 50, 50, 255))
+    out[2] = checker((200, 0, 200, 255), (30, 30, 30, 255))
+    out[3] = checker((200, 0, 200, 255), (30, 30, 30, 255))
+    return out
 
 
 _lib = None
@@ -109,7 +126,7 @@ def build_mesh_bvh(vertices, triangles):
 class OracleScene:
     """A scene as the reference binds it, built by the oracle's reference builder."""
 
-    def __init__(self, *, materials, spheres=None, vertices=None, triangles=None, env=None):
+    def __init__(self, *, materials, spheres=None, vertices=None, triangles=None, env=None, albedo=None):
         self.spheres_in = np.zeros(0, SPHERE) if spheres is None else np.ascontiguousarray(spheres, SPHERE)
         self.vertices = np.zeros(0, VERTEX) if vertices is None else np.ascontiguousarray(vertices, VERTEX)
         self.triangles_in = np.zeros(0, TRIANGLE) if triangles is None else np.ascontiguousarray(triangles, TRIANGLE)
@@ -126,13 +143,15 @@ class OracleScene:
         s.materials = _p(self.materials)
         if self.env is not None:
             s.env_rgba, s.env_h, s.env_w = _p(self.env), self.env.shape[0], self.env.shape[1]
+        self.albedo = np.ascontiguousarray(default_albedo_layers() if albedo is None else albedo, np.uint8)
+        s.albedo, s.albedo_layers, s.albedo_size = _p(self.albedo), self.albedo.shape[0], self.albedo.shape[1]
         self._s = s
 
     def reference_buffers(self):
         """The buffers the reference's build_scene_buffers would upload (ordered + BVHs + ids)."""
         return dict(spheres=self.spheres, sphere_bvh=self.sphere_nodes, sphere_order=self.sphere_ids,
                     vertices=self.vertices, triangles=self.triangles, mesh_bvh=self.mesh_nodes,
-                    triangle_order=self.triangle_ids, materials=self.materials, env=self.env)
+                    triangle_order=self.triangle_ids, materials=self.materials, env=self.env, albedo=self.albedo)
 
     def trace(self, rays, brute_force=False, threads=0, stats=False):
         rays = np.ascontiguousarray(rays, RAY)
