@@ -122,30 +122,18 @@ class ClockSampler:
 
 
 def dist_init(n):
-    rank, world, local = int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), \
-        int(os.environ.get("LOCAL_RANK", 0))
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    return rank, world, local
+    from mcrt_gb300 import replicas
+    return replicas.init("nccl")
 
 
 def max_over_ranks(x, world):
-    if world == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from mcrt_gb300 import replicas
+    return replicas.max_over_ranks(x, device="cuda") if world > 1 else x
 
 
 def barrier(world):
-    if world > 1:
-        import torch.distributed as dist
-        dist.barrier()
+    from mcrt_gb300 import replicas
+    replicas.barrier()
 
 
 def make_scene():

@@ -225,6 +225,15 @@ mcrt_status mcrt_render_noalloc(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, u
 /* Copy the device accumulation of the last render to the host (any may be NULL). */
 mcrt_status mcrt_read_accum(mcrt_ctx *ctx, float *out_rgba, double *accum_rgb, float *out_gbuf);
 
+/* Tone-map the device accumulation of the last render on the GPU and copy the
+ * RGBA8 result (w*h*4 bytes, alpha 255) to the host:
+ *   MCRT_TONEMAP_REINHARD: non-finite -> 0, v/(v+1), gamma 1/2.2, +0.5 truncate
+ *                          (tonemap_to_u8, headless.rs:93-98, :350-368);
+ *   MCRT_TONEMAP_ACES_SRGB: ACES filmic (Narkowicz) then the sRGB transfer
+ *                          (screenshot_to_u8, gpu.rs:1904-1939). */
+enum { MCRT_TONEMAP_REINHARD = 0, MCRT_TONEMAP_ACES_SRGB = 1 };
+mcrt_status mcrt_read_image_rgba8(mcrt_ctx *ctx, uint32_t mode, uint8_t *out);
+
 /* Per-kernel device time of the last render, from CUDA events on the context
  * stream: [0] total, [1] trace (extend), [2] shade, [3] shadow rays, [4] resolve,
  * [5] BVH build (ms); counters: [0] rays traced, [1] shadow rays, [2] kernel
@@ -302,8 +311,15 @@ mcrt_status mcrt_albedo_layers(uint8_t *out);
 
 /* tonemap_to_u8 over an RGBA32F image (headless.rs:93-98, :350-368): RGBA8, alpha 255. */
 mcrt_status mcrt_tonemap_rgba8(const float *rgba, uint32_t n_pixels, uint8_t *out);
+/* screenshot_to_u8 (ACES + sRGB, gpu.rs:1904-1939) over an RGBA32F image: RGBA8, alpha 255. */
+mcrt_status mcrt_tonemap_aces_rgba8(const float *rgba, uint32_t n_pixels, uint8_t *out);
 /* RGBA8 PNG writer (the image crate's save, headless.rs:380-382). */
 mcrt_status mcrt_write_png(const char *path, const uint8_t *rgba, uint32_t w, uint32_t h);
+/* Radiance RGBE (.hdr) writer of an RGBA32F image (alpha ignored): flat
+ * scanlines, shared exponent from the largest channel, the encoding of the
+ * reference's sky generator (tests/assets/gen_test_skymap.py:44-94); readable by
+ * mcrt_load_env_map. */
+mcrt_status mcrt_write_hdr(const char *path, const float *rgba, uint32_t w, uint32_t h);
 
 /* headless::run (headless.rs:112-386): parameters CLI > sidecar [render] > 512/512/64.
  * width/height/spp = 0 means "not given".  opts may be NULL (reference estimator). */

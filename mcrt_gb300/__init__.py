@@ -132,6 +132,19 @@ def tonemap_rgba8(rgba: np.ndarray) -> np.ndarray:
     return out
 
 
+def tonemap_aces_rgba8(rgba: np.ndarray) -> np.ndarray:
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    out = np.zeros(rgba.shape[:-1] + (4,), np.uint8)
+    check(lib().mcrt_tonemap_aces_rgba8(ptr(rgba), rgba.size // 4, ptr(out)))
+    return out
+
+
+def write_hdr(path: str, rgba: np.ndarray):
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    h, w = rgba.shape[:2]
+    check(lib().mcrt_write_hdr(path.encode(), ptr(rgba), w, h))
+
+
 def write_png(path: str, rgba8: np.ndarray):
     rgba8 = np.ascontiguousarray(rgba8, np.uint8)
     h, w = rgba8.shape[:2]
@@ -260,7 +273,15 @@ class Context:
         gb = np.zeros((height, width, 4), np.float32) if "gbuf" in outputs else None
         self._check(lib().mcrt_render(self._h, ptr(cam), width, height, spp, first_frame, ctypes.byref(o),
                                       ptr(rgba), ptr(acc), ptr(gb)))
+        self._last_hw = (height, width)
         return dict(rgba=rgba, sum=acc, gbuf=gb)
+
+    def image_rgba8(self, aces=False) -> np.ndarray:
+        """Tone-map the last render on the GPU (Reinhard + gamma 2.2, or ACES + sRGB)."""
+        n = ctypes.c_uint32()
+        out = np.zeros((self._last_hw[0], self._last_hw[1], 4), np.uint8)
+        self._check(lib().mcrt_read_image_rgba8(self._h, 1 if aces else 0, ptr(out)))
+        return out
 
     def timings(self):
         ms = (c_float * 6)()

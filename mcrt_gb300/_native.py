@@ -103,6 +103,9 @@ SIGNATURES = [
     ("mcrt_render_noalloc", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_uint32,
                                     POINTER(RenderOpts), c_void_p]),
     ("mcrt_read_accum", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("mcrt_read_image_rgba8", c_int, [c_void_p, c_uint32, c_void_p]),
+    ("mcrt_tonemap_aces_rgba8", c_int, [c_void_p, c_uint32, c_void_p]),
+    ("mcrt_write_hdr", c_int, [c_char_p, c_void_p, c_uint32, c_uint32]),
     ("mcrt_last_timings", c_int, [c_void_p, POINTER(c_float), POINTER(c_uint64)]),
     ("mcrt_denoise", c_int, [c_void_p, c_void_p, c_void_p, c_uint32, c_uint32, POINTER(DenoiseParams), c_void_p]),
     ("mcrt_scene_load_yaml", c_int, [c_char_p, POINTER(c_void_p)]),

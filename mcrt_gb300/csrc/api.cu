@@ -701,6 +701,21 @@ mcrt_status mcrt_read_accum(mcrt_ctx *ctx, float *out_rgba, double *accum_rgb, f
     return MCRT_OK;
 }
 
+mcrt_status mcrt_read_image_rgba8(mcrt_ctx *ctx, uint32_t mode, uint8_t *out) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!out) return fail(ctx, MCRT_ERR_INVALID_ARG, "out is NULL");
+    if (mode > MCRT_TONEMAP_ACES_SRGB) return fail(ctx, MCRT_ERR_INVALID_ARG, "unknown tone-map mode");
+    if (!ctx->acc_valid) return fail(ctx, MCRT_ERR_INVALID_ARG, "no render to read");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const uint32_t npix = ctx->acc_w * ctx->acc_h;
+    CK(ctx->io_c.ensure((size_t)npix * 4), "allocate image");
+    mcrt::launch_tonemap(ctx->mean.as<float4>(), npix, mode, ctx->io_c.as<uchar4>(), ctx->stream);
+    CK(cudaGetLastError(), "tone-map launch");
+    CK(cudaMemcpyAsync(out, ctx->io_c.p, (size_t)npix * 4, cudaMemcpyDeviceToHost, ctx->stream), "read image");
+    CK(cudaStreamSynchronize(ctx->stream), "tone map");
+    return MCRT_OK;
+}
+
 mcrt_status mcrt_last_timings(mcrt_ctx *ctx, float *out_ms, uint64_t *out_counts) {
     if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
     if (out_ms) {

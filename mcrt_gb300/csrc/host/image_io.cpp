@@ -31,6 +31,51 @@ void tonemap_rgba8(const float *rgba, uint32_t n, uint8_t *out) {
     }
 }
 
+// Rust f32::clamp: NaN passes through.
+static inline float rclamp(float x, float lo, float hi) { return x < lo ? lo : (x > hi ? hi : x); }
+
+// screenshot_to_u8 (gpu.rs:1904-1939): ACES filmic (Narkowicz 2016) + sRGB.
+void tonemap_aces_rgba8(const float *rgba, uint32_t n, uint8_t *out) {
+    for (uint32_t i = 0; i < n; ++i) {
+        for (int c = 0; c < 3; ++c) {
+            float x = rgba[4 * (size_t)i + c];
+            x = std::isnan(x) ? 0.0f : std::max(x, 0.0f);                          // f32::max(0.0)
+            float a = rclamp((x * (2.51f * x + 0.03f)) / (x * (2.43f * x + 0.59f) + 0.14f), 0.0f, 1.0f);
+            float s;
+            if (a <= 0.0f) s = 0.0f;
+            else if (a <= 0.0031308f) s = std::min(a * 12.92f, 1.0f);
+            else if (a < 1.0f) s = rclamp(1.055f * mcrt::fm_pow(a, 1.0f / 2.4f) - 0.055f, 0.0f, 1.0f);
+            else s = 1.0f;
+            out[4 * (size_t)i + c] = (uint8_t)std::min(mcrt::fm_f2u_sat(s * 255.0f + 0.5f), 255u);
+        }
+        out[4 * (size_t)i + 3] = 255;
+    }
+}
+
+// RGBE encoding as tests/assets/gen_test_skymap.py:44-94 (flat scanlines).
+bool write_hdr(const std::string &path, const float *rgba, uint32_t w, uint32_t h, std::string *err) {
+    std::vector<uint8_t> px((size_t)w * h * 4, 0);
+    for (size_t i = 0; i < (size_t)w * h; ++i) {
+        float r = rgba[4 * i], g = rgba[4 * i + 1], b = rgba[4 * i + 2];
+        float mx = std::max(r, std::max(g, b));
+        if (!(mx > 1e-32f)) continue;
+        int e = 0;
+        float m = std::frexp(mx, &e);                  // m in [0.5, 1)
+        float scale = m * 256.0f / mx;
+        const float ch[3] = {r, g, b};
+        for (int c = 0; c < 3; ++c) px[4 * i + c] = (uint8_t)std::min(std::max(ch[c] * scale, 0.0f), 255.0f);
+        px[4 * i + 3] = (uint8_t)std::min(std::max(e + 128, 0), 255);
+    }
+    FILE *f = fopen(path.c_str(), "wb");
+    if (!f) { *err = "cannot open '" + path + "' for writing"; return false; }
+    std::string hdr = "#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y " + std::to_string(h) + " +X " + std::to_string(w) + "\n";
+    bool ok = fwrite(hdr.data(), 1, hdr.size(), f) == hdr.size();
+    ok = ok && fwrite(px.data(), 1, px.size(), f) == px.size();
+    ok = (fclose(f) == 0) && ok;
+    if (!ok) *err = "write to '" + path + "' failed";
+    return ok;
+}
+
 namespace {
 uint32_t crc_table[256];
 bool crc_init = false;
@@ -102,6 +147,19 @@ extern "C" {
 mcrt_status mcrt_tonemap_rgba8(const float *rgba, uint32_t n_pixels, uint8_t *out) {
     if ((!rgba || !out) && n_pixels) { mcrt::set_global_error("NULL argument"); return MCRT_ERR_INVALID_ARG; }
     mcrt_host::tonemap_rgba8(rgba, n_pixels, out);
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_tonemap_aces_rgba8(const float *rgba, uint32_t n_pixels, uint8_t *out) {
+    if ((!rgba || !out) && n_pixels) { mcrt::set_global_error("NULL argument"); return MCRT_ERR_INVALID_ARG; }
+    mcrt_host::tonemap_aces_rgba8(rgba, n_pixels, out);
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_write_hdr(const char *path, const float *rgba, uint32_t w, uint32_t h) {
+    if (!path || !rgba || w == 0 || h == 0) { mcrt::set_global_error("invalid HDR arguments"); return MCRT_ERR_INVALID_ARG; }
+    std::string err;
+    if (!mcrt_host::write_hdr(path, rgba, w, h, &err)) { mcrt::set_global_error("I/O error: " + err); return MCRT_ERR_IO; }
     return MCRT_OK;
 }
 

@@ -36,6 +36,8 @@ void compute_camera(uint32_t width, uint32_t height, const float lf[3], const fl
 void gradient_env_map(float *data);
 void load_env_map_data(const char *scene_path, float *out);
 void tonemap_rgba8(const float *rgba, uint32_t n, uint8_t *out);
+void tonemap_aces_rgba8(const float *rgba, uint32_t n, uint8_t *out);
 bool write_png(const std::string &path, const uint8_t *rgba, uint32_t w, uint32_t h, std::string *err);
+bool write_hdr(const std::string &path, const float *rgba, uint32_t w, uint32_t h, std::string *err);
 
 }  // namespace mcrt_host

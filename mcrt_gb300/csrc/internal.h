@@ -52,6 +52,7 @@ void launch_shade(const DeviceScene &S, const RenderParams &P, PathBuffers &B, i
 void launch_shadow(const DeviceScene &S, const RenderParams &P, PathBuffers &B, cudaStream_t st);
 void launch_resolve(const RenderParams &P, const PathBuffers &B, float4 *mean, double *sum, bool keep,
                     cudaStream_t st);
+void launch_tonemap(const float4 *mean, uint32_t npix, uint32_t mode, uchar4 *out, cudaStream_t st);
 
 // BVH (bvh_build.cu)
 struct BvhScratch;

@@ -745,6 +745,41 @@ __global__ void k_resolve(RenderParams P, PathBuffers B, float4 *mean, double *s
     sum[3 * (size_t)p] = s0; sum[3 * (size_t)p + 1] = s1; sum[3 * (size_t)p + 2] = s2;
 }
 
+// Tone map of the running mean into RGBA8 on the device: mode 0 is
+// tonemap_to_u8 (headless.rs:93-98) after the non-finite sanitising
+// (:356-358); mode 1 is screenshot_to_u8 (gpu.rs:1904-1939).
+__device__ __forceinline__ float rclamp(float x, float lo, float hi) { return x < lo ? lo : (x > hi ? hi : x); }
+
+__global__ void k_tonemap(const float4 *mean, uint32_t npix, uint32_t mode, uchar4 *out) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    float4 m = mean[p];
+    float v[3] = {m.x, m.y, m.z};
+    unsigned char q[3];
+    for (int c = 0; c < 3; ++c) {
+        float x = v[c], s;
+        if (mode == MCRT_TONEMAP_ACES_SRGB) {
+            x = isnan(x) ? 0.0f : fmaxf(x, 0.0f);
+            float a = rclamp((x * (2.51f * x + 0.03f)) / (x * (2.43f * x + 0.59f) + 0.14f), 0.0f, 1.0f);
+            if (a <= 0.0f) s = 0.0f;
+            else if (a <= 0.0031308f) s = fminf(a * 12.92f, 1.0f);
+            else if (a < 1.0f) s = rclamp(1.055f * dm_pow(a, 1.0f / 2.4f) - 0.055f, 0.0f, 1.0f);
+            else s = 1.0f;
+        } else {
+            if (!isfinite(x)) x = 0.0f;
+            x = fmaxf(x, 0.0f);
+            float mapped = x / (x + 1.0f);
+            s = fminf(fmaxf(dm_pow(mapped, 1.0f / 2.2f), 0.0f), 1.0f);
+        }
+        q[c] = (unsigned char)min(f2u_sat(s * 255.0f + 0.5f), 255u);
+    }
+    out[p] = make_uchar4(q[0], q[1], q[2], 255);
+}
+
+void launch_tonemap(const float4 *mean, uint32_t npix, uint32_t mode, uchar4 *out, cudaStream_t st) {
+    k_tonemap<<<(npix + 255) / 256, 256, 0, st>>>(mean, npix, mode, out); ::mcrt::note_launch();
+}
+
 // Light-selection CDF: one block; each thread sums a contiguous chunk of light
 // weights, a block scan gives chunk offsets, cdf[k] = prefix / total.
 __global__ void __launch_bounds__(1024) k_light_cdf(DeviceScene S, float *cdf, float *total_out) {

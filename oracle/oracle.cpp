@@ -876,3 +876,25 @@ void orc_math_eval(int fn, const float *x, const float *y, float *out, uint32_t 
 }
 
 } // extern "C"
+
+extern "C" {
+/* screenshot_to_u8 (gpu.rs:1904-1939): ACES filmic (Narkowicz 2016) then the
+ * IEC 61966-2-1 transfer; Rust's f32::clamp lets NaN through. */
+void orc_tonemap_aces_rgba8(const float *rgba, uint32_t n, uint8_t *out) {
+    auto rclamp = [](float x, float lo, float hi) { return x < lo ? lo : (x > hi ? hi : x); };
+    for (uint32_t i = 0; i < n; ++i) {
+        for (int c = 0; c < 3; ++c) {
+            float x = rgba[4 * i + c];
+            x = std::isnan(x) ? 0.0f : fmaxf(x, 0.0f);
+            float a = rclamp((x * (2.51f * x + 0.03f)) / (x * (2.43f * x + 0.59f) + 0.14f), 0.0f, 1.0f);
+            float s;
+            if (a <= 0.0f) s = 0.0f;
+            else if (a <= 0.0031308f) s = fminf(a * 12.92f, 1.0f);
+            else if (a < 1.0f) s = rclamp(1.055f * of_pow(a, 1.0f / 2.4f) - 0.055f, 0.0f, 1.0f);
+            else s = 1.0f;
+            out[4 * i + c] = (uint8_t)std::min(of_f2u_sat(s * 255.0f + 0.5f), 255u);
+        }
+        out[4 * i + 3] = 255;
+    }
+}
+}

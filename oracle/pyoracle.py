@@ -215,3 +215,13 @@ def math_eval(fn, x, y=None):
 
 def pcg_hash(v):
     return lib().orc_pcg_hash(v)
+
+
+def tonemap_aces_rgba8(rgba):
+    L = lib()
+    L.orc_tonemap_aces_rgba8.restype = None
+    L.orc_tonemap_aces_rgba8.argtypes = [c_void_p, c_uint32, c_void_p]
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    out = np.zeros(rgba.shape[:-1] + (4,), np.uint8)
+    L.orc_tonemap_aces_rgba8(_p(rgba), rgba.size // 4, _p(out))
+    return out

@@ -144,3 +144,15 @@ def test_headless_cli_matches_oracle(tmp_path, oracle):
     p = subprocess.run([cli, "--headless", str(tmp_path / "missing.yaml"), "--output", str(out)],
                        capture_output=True, text=True, timeout=60)
     assert p.returncode == 1 and "headless render failed" in p.stderr
+
+
+def test_device_tonemaps_match_host(ctx, oracle):
+    """mcrt_read_image_rgba8: Reinhard + gamma 2.2 and ACES + sRGB on the GPU equal
+    the host restatements applied to the read-back running mean."""
+    s = load_fixture_scene("cornell_box_mini")
+    ctx.upload_scene(spheres=s["spheres"], vertices=s["vertices"], triangles=s["triangles"], materials=s["materials"],
+                     env=M.gradient_env_map())
+    cam = M.compute_camera(64, 48, [0.0, 4.75, 8.0], [0.0, 4.0, 0.0], 60.0, 0.0)
+    rgba = ctx.render(cam, 64, 48, 4, outputs=("rgba",))["rgba"]
+    assert np.array_equal(ctx.image_rgba8(aces=False), oracle.tonemap_rgba8(rgba))
+    assert np.array_equal(ctx.image_rgba8(aces=True), oracle.tonemap_aces_rgba8(rgba))

@@ -322,3 +322,30 @@ def test_png_writer_roundtrip(tmp_path):
         pos += 12 + n
     raw = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(37, 1 + 53 * 4)
     assert (raw[:, 0] == 0).all() and np.array_equal(raw[:, 1:].reshape(37, 53, 4), img)
+
+
+def test_aces_tonemap_matches_oracle(oracle):                       # gpu.rs:1904-1939
+    r = np.random.default_rng(5).exponential(2.0, (40, 30, 4)).astype(np.float32)
+    r[0, 0, :3] = [np.nan, np.inf, -1.0]
+    assert np.array_equal(M.tonemap_aces_rgba8(r), oracle.tonemap_aces_rgba8(r))
+    z = np.zeros((1, 1, 4), np.float32)
+    assert M.tonemap_aces_rgba8(z)[0, 0].tolist() == [0, 0, 0, 255]
+
+
+def test_hdr_writer_roundtrip_and_sky_fixture(tmp_path):
+    """The RGBE writer encodes as the reference's sky generator; the reader decodes
+    the generator's own file (tests/golden/test_sky_128x64.hdr) to within RGBE
+    precision of the float image it was made from."""
+    img = np.random.default_rng(6).exponential(3.0, (512, 1024, 4)).astype(np.float32)
+    p = str(tmp_path / "x.hdr")
+    M.write_hdr(p, img)
+    back = M.load_env_map(p)                                  # 1024x512: no resize
+    rel = np.abs(back[..., :3] - img[..., :3]) / img[..., :3].max(axis=-1, keepdims=True)
+    assert rel.max() < 1.0 / 128 and (back[..., 3] == 1.0).all()
+    here = os.path.dirname(os.path.abspath(__file__))
+    sky = np.load(os.path.join(here, "golden", "test_sky_128x64.npy"))
+    env = M.load_env_map(os.path.join(here, "golden", "test_sky_128x64.hdr"))
+    src = env[::8, ::8, :3]                                    # nearest 8x upsample of 128x64
+    ref = sky.astype(np.float64)
+    tol = ref.max(axis=-1, keepdims=True) / 128 + 1e-30
+    assert (np.abs(src - ref) <= tol).all()
