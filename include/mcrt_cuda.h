@@ -184,8 +184,15 @@ typedef struct {
     uint32_t max_depth;     /* bounces; 0 -> 8 = the reference's MAX_BOUNCES (path_trace.wgsl:61) */
     uint32_t flags;
     uint32_t spp_per_pass;  /* samples traced concurrently; 0 -> automatic */
-    uint32_t reserved;
+    uint32_t variant;       /* closest-hit kernel variant: 0 = the context's (autotuned) choice, k = variant k-1 */
 } mcrt_render_opts;
+
+/* Autotuner (no reference counterpart): renders `spp` frames of w x h with each
+ * closest-hit kernel variant (occupancy / register budget), keeps the fastest
+ * for this context and reports it.  out_ms (optional) receives the extend time
+ * of every variant; its capacity is 8 floats. */
+mcrt_status mcrt_autotune(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t w, uint32_t h, uint32_t spp,
+                          const mcrt_render_opts *opts, uint32_t *out_variant, float *out_ms);
 
 /* Render frames first_frame .. first_frame+spp-1 of a w x h image
  * (headless.rs:249-290: one cs_main dispatch per frame, frame_count = index).

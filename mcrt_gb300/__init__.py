@@ -276,6 +276,16 @@ class Context:
         self._last_hw = (height, width)
         return dict(rgba=rgba, sum=acc, gbuf=gb)
 
+    def autotune(self, camera, width, height, spp, max_depth=0, nee=False):
+        """Pick the fastest closest-hit kernel variant for this scene; returns (variant, extend ms per variant)."""
+        cam = _arr(camera, CAMERA)
+        o = N.RenderOpts(max_depth=max_depth, flags=N.RENDER_NEE if nee else 0)
+        v = c_uint32()
+        ms = (c_float * 8)()
+        self._check(lib().mcrt_autotune(self._h, ptr(cam), width, height, spp, ctypes.byref(o), ctypes.byref(v), ms))
+        self._last_hw = (height, width)
+        return v.value, [ms[i] for i in range(8) if ms[i] > 0]
+
     def image_rgba8(self, aces=False) -> np.ndarray:
         """Tone-map the last render on the GPU (Reinhard + gamma 2.2, or ACES + sRGB)."""
         n = ctypes.c_uint32()

@@ -66,7 +66,7 @@ class SceneDesc(ctypes.Structure):
 
 
 class RenderOpts(ctypes.Structure):
-    _fields_ = [("max_depth", c_uint32), ("flags", c_uint32), ("spp_per_pass", c_uint32), ("reserved", c_uint32)]
+    _fields_ = [("max_depth", c_uint32), ("flags", c_uint32), ("spp_per_pass", c_uint32), ("variant", c_uint32)]
 
 
 class DenoiseParams(ctypes.Structure):
@@ -103,6 +103,8 @@ SIGNATURES = [
     ("mcrt_render_noalloc", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_uint32,
                                     POINTER(RenderOpts), c_void_p]),
     ("mcrt_read_accum", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("mcrt_autotune", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, POINTER(RenderOpts),
+                              POINTER(c_uint32), POINTER(c_float)]),
     ("mcrt_read_image_rgba8", c_int, [c_void_p, c_uint32, c_void_p]),
     ("mcrt_tonemap_aces_rgba8", c_int, [c_void_p, c_uint32, c_void_p]),
     ("mcrt_write_hdr", c_int, [c_char_p, c_void_p, c_uint32, c_uint32]),

@@ -97,6 +97,7 @@ struct mcrt_ctx {
     unsigned long long last_counts[2] = {0, 0};
     unsigned long long last_render_launches = 0, last_build_launches = 0, last_extend_launches = 0;
     float last_build_ms = 0.0f;
+    int extend_variant = 0;   // chosen by mcrt_autotune
 };
 
 namespace {
@@ -615,6 +616,7 @@ mcrt_status mcrt_render(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t 
         P.cam = *cam;
         const bool last_pass = done + P.spp_pass >= spp;
         P.gbuf_plane = (want_gbuf && last_pass) ? (int)P.spp_pass - 1 : -1;
+        P.extend_variant = o.variant ? (int)o.variant - 1 : ctx->extend_variant;
         mcrt::launch_raygen(S, P, ctx->pb, st);
         int qi = 0;
         for (uint32_t b = 0; b < depth; ++b) {
@@ -698,6 +700,31 @@ mcrt_status mcrt_read_accum(mcrt_ctx *ctx, float *out_rgba, double *accum_rgb, f
     if (out_gbuf && ctx->gbuf_valid)
         CK(cudaMemcpyAsync(out_gbuf, ctx->gbuf.p, npix * 16, cudaMemcpyDeviceToHost, st), "read G-buffer");
     CK(cudaStreamSynchronize(st), "read accumulation");
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_autotune(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t w, uint32_t h, uint32_t spp,
+                          const mcrt_render_opts *opts, uint32_t *out_variant, float *out_ms) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    mcrt_render_opts o{};
+    if (opts) o = *opts;
+    o.flags &= ~(uint32_t)MCRT_RENDER_KEEP_ACCUM;
+    const int nv = mcrt::extend_variant_count();
+    float best = 0.0f;
+    int best_v = 0;
+    for (int v = 0; v < nv; ++v) {
+        o.variant = (uint32_t)v + 1;
+        float t = 0.0f;
+        for (int rep = 0; rep < 2; ++rep) {           // the first run warms caches and occupancy queries
+            mcrt_status s = mcrt_render(ctx, cam, w, h, spp, 0, &o, nullptr, nullptr, nullptr);
+            if (s != MCRT_OK) return s;
+            t = ctx->last_ms[1];
+        }
+        if (out_ms && v < 8) out_ms[v] = t;
+        if (v == 0 || t < best) { best = t; best_v = v; }
+    }
+    ctx->extend_variant = best_v;
+    if (out_variant) *out_variant = (uint32_t)best_v;
     return MCRT_OK;
 }
 

@@ -39,8 +39,10 @@ struct RenderParams {
     uint32_t max_depth;
     uint32_t flags;          // MCRT_RENDER_*
     int32_t gbuf_plane;      // plane whose primary hit is stored in the G-buffer (-1: none)
+    int32_t extend_variant;  // closest-hit kernel variant (autotuned)
     mcrt_camera_uniform cam;
 };
+int extend_variant_count();
 
 // Launchers (render.cu)
 void launch_trace_closest(const DeviceScene &S, const mcrt_ray *rays, uint32_t n, mcrt_hit *hits, bool ref_layout,

@@ -422,7 +422,12 @@ __global__ void k_raygen(DeviceScene S, RenderParams P, PathBuffers B) {
 // reference-order walk (spheres_hit); their count is small.
 constexpr int kRefill = 8;
 
-__global__ void __launch_bounds__(128, 8) k_extend(DeviceScene S, PathBuffers B, int qi) {
+// Occupancy variants (minimum resident blocks of 128 threads per SM: the
+// register budget ptxas must meet); chosen per scene by mcrt_autotune.
+constexpr int kExtendVariants = 4;   // instantiated below with 8, 10, 12, 16 blocks
+
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) k_extend(DeviceScene S, PathBuffers B, int qi) {
     const uint32_t n = B.counters[qi];
     if (blockIdx.x == 0 && threadIdx.x == 0) { B.counters[qi ^ 1] = 0; B.counters[2] = 0; }
     const float4 *qo = B.q_o[qi];
@@ -834,16 +839,21 @@ void launch_raygen(const DeviceScene &S, const RenderParams &P, PathBuffers &B, 
     k_raygen<<<(n + 255) / 256, 256, 0, st>>>(S, P, B); ::mcrt::note_launch();
 }
 
+int extend_variant_count() { return kExtendVariants; }
+
 void launch_extend(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, cudaStream_t st) {
+    using Kern = void (*)(DeviceScene, PathBuffers, int);
+    static const Kern kernels[kExtendVariants] = {k_extend<8>, k_extend<10>, k_extend<12>, k_extend<16>};
+    static int per_sm[kExtendVariants] = {0, 0, 0, 0};
+    const int v = (P.extend_variant >= 0 && P.extend_variant < kExtendVariants) ? P.extend_variant : 0;
     // persistent: as many resident blocks as fit, never more warps than rays
-    static int per_sm = 0;
-    if (per_sm == 0) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_extend, 128, 0);
-        if (per_sm <= 0) per_sm = 1;
+    if (per_sm[v] == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[v], kernels[v], 128, 0);
+        if (per_sm[v] <= 0) per_sm[v] = 1;
     }
     uint32_t nmax = P.npix * P.spp_pass;
-    int blocks = min(grid_blocks_for(nmax, 128), sm_count() * per_sm);
-    k_extend<<<blocks, 128, 0, st>>>(S, B, qi); ::mcrt::note_launch();
+    int blocks = min(grid_blocks_for(nmax, 128), sm_count() * per_sm[v]);
+    kernels[v]<<<blocks, 128, 0, st>>>(S, B, qi); ::mcrt::note_launch();
 }
 
 void launch_shade(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, uint32_t bounce,

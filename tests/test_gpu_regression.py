@@ -146,6 +146,26 @@ def test_headless_cli_matches_oracle(tmp_path, oracle):
     assert p.returncode == 1 and "headless render failed" in p.stderr
 
 
+def test_autotuned_variants_are_bit_identical(ctx):
+    from mcrt_gb300 import scenes
+    sc = scenes.displaced_icosphere(seed=3, level=5, width=64, height=48)
+    c = sc["camera"]
+    cam = M.compute_camera(64, 48, c["look_from"], c["look_at"], c["vfov"], 0.0)
+    ctx.upload_scene(vertices=sc["vertices"], triangles=sc["triangles"], materials=sc["materials"], env=sc["env"])
+    v, ms = ctx.autotune(cam, 64, 48, 2, max_depth=12)
+    assert 0 <= v < len(ms) and len(ms) >= 2
+    imgs = []
+    for k in range(len(ms)):
+        o = M._native.RenderOpts(max_depth=12, variant=k + 1)
+        rgba = np.zeros((48, 64, 4), np.float32)
+        import ctypes
+        M.check(M.lib().mcrt_render(ctx._h, M._native.ptr(cam), 64, 48, 3, 0, ctypes.byref(o), M._native.ptr(rgba),
+                                    None, None), ctx._h)
+        imgs.append(rgba)
+    for im in imgs[1:]:
+        assert np.array_equal(bits(im), bits(imgs[0]))
+
+
 def test_device_tonemaps_match_host(ctx, oracle):
     """mcrt_read_image_rgba8: Reinhard + gamma 2.2 and ACES + sRGB on the GPU equal
     the host restatements applied to the read-back running mean."""
