@@ -75,6 +75,8 @@ struct mcrt_ctx {
     std::string err;
     // scene
     bool has_scene = false;
+    DBuf wnodes;
+    uint32_t n_wnodes = 0;
     DBuf spheres, sphere_ids, sphere_nodes, vertices, triangles, mesh_nodes, tri_order, trirecs, cnodes, materials,
         env, lights, light_cdf, tmp, staging, albedo;
     uint32_t albedo_layers = 0, albedo_size = 0;
@@ -135,6 +137,8 @@ mcrt::DeviceScene device_scene(const mcrt_ctx *c) {
     S.tris = c->trirecs.as<mcrt::TriRec>();
     S.cnodes = c->cnodes.as<float4>();
     S.n_cnodes = c->n_cnodes;
+    S.wnodes = c->wnodes.as<uint4>();
+    S.n_wnodes = c->n_wnodes;
     S.materials = c->materials.as<mcrt_gpu_material_data>();
     S.env = c->env.as<float4>();
     S.env_w = c->env_w;
@@ -216,6 +220,12 @@ mcrt_status finish_mesh(mcrt_ctx *ctx) {
                               &ncn, ctx->trirecs.p, ctx->tmp.as<uint32_t>(), tmp_words, st),
        "compact BVH");
     ctx->n_cnodes = ncn;
+    CK(ctx->wnodes.ensure((size_t)(nn / 2 + 1) * 64), "allocate wide nodes");
+    uint32_t nw = 0;
+    CK(mcrt::gpu_make_wide4(ctx->mesh_nodes.as<mcrt_gpu_bvh_node>(), nn, ctx->wnodes.as<uint4>(), &nw,
+                            ctx->tmp.as<uint32_t>(), st),
+       "4-wide BVH");
+    ctx->n_wnodes = nw;
     return MCRT_OK;
 }
 
@@ -298,7 +308,7 @@ void mcrt_destroy(mcrt_ctx *ctx) {
     cudaStreamSynchronize(ctx->stream);
     DBuf *bufs[] = {&ctx->spheres, &ctx->sphere_ids, &ctx->sphere_nodes, &ctx->vertices, &ctx->triangles,
                     &ctx->mesh_nodes, &ctx->tri_order, &ctx->trirecs, &ctx->cnodes, &ctx->materials, &ctx->env,
-                    &ctx->lights, &ctx->light_cdf, &ctx->tmp, &ctx->staging, &ctx->albedo, &ctx->pbmem, &ctx->mean,
+                    &ctx->lights, &ctx->light_cdf, &ctx->tmp, &ctx->staging, &ctx->albedo, &ctx->wnodes, &ctx->pbmem, &ctx->mean,
                     &ctx->sum, &ctx->gbuf, &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->counters};
     for (DBuf *b : bufs) b->release();
     mcrt::free_bvh_scratch(ctx->bvh_scratch);

@@ -691,4 +691,149 @@ cudaError_t gpu_make_compact(const mcrt_gpu_bvh_node *d_nodes, uint32_t n_nodes,
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ quantised 4-wide layout
+// Collapse of the reference-layout binary BVH into 4-wide nodes (64 bytes):
+//   w0: origin.xyz (float, the node box minimum) | exponent bytes ex, ey, ez
+//       (grid step 2^(e-127) per axis) and the child count
+//   w1: qlo.x[4] | qlo.y[4] | qlo.z[4] | qhi.x[4]   (8-bit grid coordinates)
+//   w2: qhi.y[4] | qhi.z[4] | 0 | 0
+//   w3: child codes (internal 4-wide node index, leaf code, or kNoChild)
+// A node takes the two children of a binary node and repeatedly replaces the
+// internal child of largest surface area by its two children until it has
+// four.  Leaves are the reference's leaves.  Child boxes are rounded outward:
+// the builder checks, in the float arithmetic the traversal uses
+// (origin + q * step), that every dequantised plane lies outside the exact
+// child box, so a ray that reaches a leaf of the reference tree also reaches it
+// here.
+namespace {
+
+__device__ __forceinline__ float step_of(uint32_t e) { return __uint_as_float(e << 23); }
+
+// Smallest exponent byte e with extent / 2^(e-127) <= 250 (a normal power of two).
+__device__ __forceinline__ uint32_t grid_exponent(float extent) {
+    if (!(extent > 0.0f)) return 1u;
+    float s = extent / 250.0f;
+    uint32_t e = (__float_as_uint(s) >> 23) & 0xffu;     // 2^(e-127) <= s < 2^(e-126)
+    if (e == 0u) e = 1u;
+    while (e < 254u && step_of(e) * 250.0f < extent) ++e;
+    while (e > 1u && step_of(e - 1u) * 250.0f >= extent) --e;
+    return e;
+}
+
+__device__ __forceinline__ uint32_t quant_lo(float origin, float step, float v) {
+    float q = floorf((v - origin) / step);
+    int qi = q < 0.0f ? 0 : (q > 255.0f ? 255 : (int)q);
+    while (qi > 0 && origin + (float)qi * step > v) --qi;
+    return (uint32_t)qi;
+}
+__device__ __forceinline__ uint32_t quant_hi(float origin, float step, float v, bool *ok) {
+    float q = ceilf((v - origin) / step);
+    int qi = q < 0.0f ? 0 : (q > 255.0f ? 255 : (int)q);
+    while (qi < 255 && origin + (float)qi * step < v) ++qi;
+    if (origin + (float)qi * step < v) *ok = false;
+    return (uint32_t)qi;
+}
+
+__global__ void k_widen(const mcrt_gpu_bvh_node *nodes, const uint32_t *front, uint32_t n_front, uint32_t level_base,
+                        uint32_t next_base, uint32_t *next_front, uint32_t *counter, uint4 *out, uint32_t *bad) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_front) return;
+    const uint32_t i = front[k];
+    uint32_t set[4] = {i + 1, nodes[i].right_or_offset, kNoChild, kNoChild};
+    uint32_t cnt = 2;
+    auto area = [&](uint32_t c) {
+        const mcrt_gpu_bvh_node &nd = nodes[c];
+        float d0 = nd.aabb_max[0] - nd.aabb_min[0], d1 = nd.aabb_max[1] - nd.aabb_min[1],
+              d2 = nd.aabb_max[2] - nd.aabb_min[2];
+        return d0 * d1 + d1 * d2 + d0 * d2;
+    };
+    while (cnt < 4) {
+        int pick = -1;
+        float best = -1.0f;
+        for (uint32_t j = 0; j < cnt; ++j) {
+            if (nodes[set[j]].prim_count != 0) continue;
+            float a = area(set[j]);
+            if (a > best) { best = a; pick = (int)j; }
+        }
+        if (pick < 0) break;
+        uint32_t c = set[pick];
+        set[pick] = c + 1;
+        set[cnt++] = nodes[c].right_or_offset;
+    }
+    uint32_t n_int = 0;
+    for (uint32_t j = 0; j < cnt; ++j) n_int += nodes[set[j]].prim_count == 0 ? 1u : 0u;
+    uint32_t base = n_int ? atomicAdd(counter, n_int) : 0u;
+    const mcrt_gpu_bvh_node &nd = nodes[i];
+    float org[3], stp[3];
+    uint32_t ex[3];
+    for (int a = 0; a < 3; ++a) {
+        org[a] = nd.aabb_min[a];
+        ex[a] = grid_exponent(nd.aabb_max[a] - nd.aabb_min[a]);
+        stp[a] = step_of(ex[a]);
+    }
+    uint32_t qlo[3] = {0, 0, 0}, qhi[3] = {0, 0, 0}, refs[4];
+    bool ok = true;
+    uint32_t r = 0;
+    for (uint32_t j = 0; j < 4; ++j) {
+        if (j >= cnt) { refs[j] = kNoChild; continue; }
+        const mcrt_gpu_bvh_node &c = nodes[set[j]];
+        for (int a = 0; a < 3; ++a) {
+            qlo[a] |= quant_lo(org[a], stp[a], c.aabb_min[a]) << (8 * j);
+            qhi[a] |= quant_hi(org[a], stp[a], c.aabb_max[a], &ok) << (8 * j);
+        }
+        if (c.prim_count == 0) {
+            refs[j] = next_base + base + r;
+            next_front[base + r] = set[j];
+            ++r;
+        } else {
+            refs[j] = leaf_code(c.right_or_offset, c.prim_count);
+        }
+    }
+    if (!ok) atomicOr(bad, 1u);
+    uint4 *o = out + 4ull * (level_base + k);
+    o[0] = make_uint4(__float_as_uint(org[0]), __float_as_uint(org[1]), __float_as_uint(org[2]),
+                      ex[0] | (ex[1] << 8) | (ex[2] << 16) | (cnt << 24));
+    o[1] = make_uint4(qlo[0], qlo[1], qlo[2], qhi[0]);
+    o[2] = make_uint4(qhi[1], qhi[2], 0u, 0u);
+    o[3] = make_uint4(refs[0], refs[1], refs[2], refs[3]);
+}
+
+}  // namespace
+
+// d_tmp: 2 * n_nodes + 4 words.  d_wide: capacity (n_nodes / 2 + 1) nodes of 64 bytes.
+cudaError_t gpu_make_wide4(const mcrt_gpu_bvh_node *d_nodes, uint32_t n_nodes, uint4 *d_wide, uint32_t *n_wide,
+                           uint32_t *d_tmp, cudaStream_t st) {
+    *n_wide = 0;
+    if (n_nodes <= 1) return cudaSuccess;           // a single leaf: traversed without wide nodes
+    uint32_t *front[2] = {d_tmp, d_tmp + n_nodes};
+    uint32_t *counter = d_tmp + 2 * (size_t)n_nodes;
+    uint32_t *bad = counter + 1;
+    uint32_t zero = 0;
+    cudaMemcpyAsync(front[0], &zero, 4, cudaMemcpyHostToDevice, st);   // root
+    cudaMemsetAsync(bad, 0, 4, st);
+    uint32_t n_front = 1, level_base = 0;
+    int cur = 0;
+    for (int guard = 0; n_front > 0; ++guard) {
+        if (guard > 4096) return cudaErrorUnknown;
+        cudaMemsetAsync(counter, 0, 4, st);
+        const uint32_t next_base = level_base + n_front;
+        k_widen<<<(n_front + 127) / 128, 128, 0, st>>>(d_nodes, front[cur], n_front, level_base, next_base,
+                                                      front[cur ^ 1], counter, d_wide, bad); ::mcrt::note_launch();
+        uint32_t n_next = 0;
+        cudaMemcpyAsync(&n_next, counter, 4, cudaMemcpyDeviceToHost, st);
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return e;
+        level_base = next_base;
+        n_front = n_next;
+        cur ^= 1;
+    }
+    uint32_t b = 0;
+    cudaMemcpyAsync(&b, bad, 4, cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
+    if (b) return cudaErrorInvalidValue;            // a child box could not be enclosed on the grid
+    *n_wide = level_base;
+    return cudaSuccess;
+}
+
 }  // namespace mcrt

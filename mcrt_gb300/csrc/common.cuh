@@ -91,6 +91,8 @@ struct DeviceScene {
     const TriRec *tris;
     // compact BVH2 (children boxes in the parent) for the fast traversal
     const float4 *cnodes; uint32_t n_cnodes;
+    // quantised 4-wide BVH collapsed from the same tree
+    const uint4 *wnodes; uint32_t n_wnodes;
     const mcrt_gpu_material_data *materials;
     const float4 *env; uint32_t env_w, env_h;
     // light list for next-event estimation

@@ -424,9 +424,91 @@ constexpr int kRefill = 8;
 
 // Occupancy variants (minimum resident blocks of 128 threads per SM: the
 // register budget ptxas must meet); chosen per scene by mcrt_autotune.
-constexpr int kExtendVariants = 4;   // instantiated below with 8, 10, 12, 16 blocks
+// variants 0-3: compact binary BVH, 4-7: quantised 4-wide BVH, each with 8, 10,
+// 12, 16 resident blocks
+constexpr int kExtendVariants = 8;
 
-template <int MINB>
+// Visit an internal node of the compact binary layout: test both children,
+// continue with the nearer hit child, push the farther one.
+__device__ __forceinline__ void visit_compact2(const DeviceScene &S, const RayInv &r, float tmax, uint32_t *cur,
+                                               float *cur_t, uint2 *stack, uint32_t *sp, uint32_t *overflow) {
+    const float4 *np = S.cnodes + 4ull * *cur;
+    float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
+    uint4 e = __ldg(reinterpret_cast<const uint4 *>(np + 3));
+    float tl, tr;
+    bool hl = e.x != kNoChild && slab(r, a.x, a.z, c.x, a.y, a.w, c.y, kTMin, tmax, &tl);
+    bool hr = e.y != kNoChild && slab(r, b.x, b.z, c.z, b.y, b.w, c.w, kTMin, tmax, &tr);
+    if (hl && hr) {
+        uint32_t near = e.x, far = e.y;
+        float tnear = tl, tfar = tr;
+        if (tr < tl) { near = e.y; far = e.x; tnear = tr; tfar = tl; }
+        if (*sp < kStackSize) stack[(*sp)++] = make_uint2(far, __float_as_uint(tfar));
+        else *overflow = 1u;
+        *cur = near;
+        *cur_t = tnear;
+    } else if (hl) {
+        *cur = e.x; *cur_t = tl;
+    } else if (hr) {
+        *cur = e.y; *cur_t = tr;
+    } else {
+        *cur = kNoChild;
+    }
+}
+
+// Visit a quantised 4-wide node: dequantise each child box on the node's grid
+// (origin + q * step, the float sequence the builder verified to enclose the
+// exact box), slab-test, order the hits by entry distance with a sorting
+// network on (distance bits, child) keys, continue with the nearest and push
+// the others farthest first.
+__device__ __forceinline__ void visit_wide4(const DeviceScene &S, const RayInv &r, float tmax, uint32_t *cur,
+                                            float *cur_t, uint2 *stack, uint32_t *sp, uint32_t *overflow) {
+    const uint4 *np = S.wnodes + 4ull * *cur;
+    const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3);
+    const float ox = __uint_as_float(w0.x), oy = __uint_as_float(w0.y), oz = __uint_as_float(w0.z);
+    const float sx = __uint_as_float((w0.w & 0xffu) << 23), sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23),
+                sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
+    const uint32_t refs[4] = {w3.x, w3.y, w3.z, w3.w};
+    // key = entry distance bits (non-negative floats order as integers) with the
+    // child index in the two low bits: the distance loses at most 3 ulp
+    // downward, which only makes the later cull (distance <= closest t) looser.
+    uint32_t key[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        key[j] = 0xffffffffu;
+        if (refs[j] == kNoChild) continue;
+        const int sh = 8 * j;
+        float lx = ox + (float)((w1.x >> sh) & 0xffu) * sx, ly = oy + (float)((w1.y >> sh) & 0xffu) * sy,
+              lz = oz + (float)((w1.z >> sh) & 0xffu) * sz;
+        float hx = ox + (float)((w1.w >> sh) & 0xffu) * sx, hy = oy + (float)((w2.x >> sh) & 0xffu) * sy,
+              hz = oz + (float)((w2.y >> sh) & 0xffu) * sz;
+        float te;
+        if (slab(r, lx, ly, lz, hx, hy, hz, kTMin, tmax, &te))
+            key[j] = (__float_as_uint(fmaxf(te, 0.0f)) & ~3u) | (uint32_t)j;
+    }
+    auto cx = [](uint32_t &a, uint32_t &b) {
+        uint32_t lo = min(a, b), hi = max(a, b);
+        a = lo; b = hi;
+    };
+    cx(key[0], key[1]); cx(key[2], key[3]); cx(key[0], key[2]); cx(key[1], key[3]); cx(key[1], key[2]);
+    auto ref_of = [&](uint32_t k) {
+        uint32_t j = k & 3u;
+        return j == 0 ? refs[0] : (j == 1 ? refs[1] : (j == 2 ? refs[2] : refs[3]));
+    };
+#pragma unroll
+    for (int j = 3; j >= 1; --j) {
+        if (key[j] == 0xffffffffu) continue;
+        if (*sp < kStackSize) stack[(*sp)++] = make_uint2(ref_of(key[j]), key[j] & ~3u);
+        else *overflow = 1u;
+    }
+    if (key[0] == 0xffffffffu) {
+        *cur = kNoChild;
+    } else {
+        *cur = ref_of(key[0]);
+        *cur_t = __uint_as_float(key[0] & ~3u);
+    }
+}
+
+template <int WIDTH, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_extend(DeviceScene S, PathBuffers B, int qi) {
     const uint32_t n = B.counters[qi];
     if (blockIdx.x == 0 && threadIdx.x == 0) { B.counters[qi ^ 1] = 0; B.counters[2] = 0; }
@@ -501,28 +583,9 @@ __global__ void __launch_bounds__(128, MINB) k_extend(DeviceScene S, PathBuffers
                     cur = kNoChild;
                     continue;
                 }
-                const float4 *np = S.cnodes + 4ull * cur;
-                float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
-                uint4 e = __ldg(reinterpret_cast<const uint4 *>(np + 3));
                 ++nn;
-                float tl, tr;
-                bool hl = e.x != kNoChild && slab(r, a.x, a.z, c.x, a.y, a.w, c.y, kTMin, best.t, &tl);
-                bool hr = e.y != kNoChild && slab(r, b.x, b.z, c.z, b.y, b.w, c.w, kTMin, best.t, &tr);
-                if (hl && hr) {
-                    uint32_t near = e.x, far = e.y;
-                    float tnear = tl, tfar = tr;
-                    if (tr < tl) { near = e.y; far = e.x; tnear = tr; tfar = tl; }
-                    if (sp < kStackSize) stack[sp++] = make_uint2(far, __float_as_uint(tfar));
-                    else B.counters[3] = 1u;
-                    cur = near;
-                    cur_t = tnear;
-                } else if (hl) {
-                    cur = e.x; cur_t = tl;
-                } else if (hr) {
-                    cur = e.y; cur_t = tr;
-                } else {
-                    cur = kNoChild;
-                }
+                if (WIDTH == 4) visit_wide4(S, r, best.t, &cur, &cur_t, stack, &sp, B.counters + 3);
+                else visit_compact2(S, r, best.t, &cur, &cur_t, stack, &sp, B.counters + 3);
                 if (__all_sync(__activemask(), leaf != kNoChild)) break;
             }
             // ---- leaf phase
@@ -843,8 +906,9 @@ int extend_variant_count() { return kExtendVariants; }
 
 void launch_extend(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, cudaStream_t st) {
     using Kern = void (*)(DeviceScene, PathBuffers, int);
-    static const Kern kernels[kExtendVariants] = {k_extend<8>, k_extend<10>, k_extend<12>, k_extend<16>};
-    static int per_sm[kExtendVariants] = {0, 0, 0, 0};
+    static const Kern kernels[kExtendVariants] = {k_extend<2, 8>, k_extend<2, 10>, k_extend<2, 12>, k_extend<2, 16>,
+                                                  k_extend<4, 8>, k_extend<4, 10>, k_extend<4, 12>, k_extend<4, 16>};
+    static int per_sm[kExtendVariants] = {0, 0, 0, 0, 0, 0, 0, 0};
     const int v = (P.extend_variant >= 0 && P.extend_variant < kExtendVariants) ? P.extend_variant : 0;
     // persistent: as many resident blocks as fit, never more warps than rays
     if (per_sm[v] == 0) {

@@ -146,6 +146,24 @@ def test_headless_cli_matches_oracle(tmp_path, oracle):
     assert p.returncode == 1 and "headless render failed" in p.stderr
 
 
+@pytest.mark.parametrize("variant", [1, 5])   # compact binary BVH, quantised 4-wide BVH
+def test_bvh_layouts_bit_exact_against_oracle(ctx, oracle, variant):
+    import ctypes
+    from mcrt_gb300 import scenes
+    sc = scenes.displaced_icosphere(seed=77, level=7, width=96, height=64)
+    c = sc["camera"]
+    cam = M.compute_camera(96, 64, c["look_from"], c["look_at"], c["vfov"], 0.0)
+    ctx.upload_scene(vertices=sc["vertices"], triangles=sc["triangles"], materials=sc["materials"], env=sc["env"])
+    o = M._native.RenderOpts(max_depth=12, variant=variant)
+    rgba = np.zeros((64, 96, 4), np.float32)
+    M.check(M.lib().mcrt_render(ctx._h, M._native.ptr(cam), 96, 64, 4, 0, ctypes.byref(o), M._native.ptr(rgba),
+                                None, None), ctx._h)
+    osc = oracle.OracleScene(materials=sc["materials"], vertices=sc["vertices"], triangles=sc["triangles"],
+                             env=sc["env"])
+    want = osc.render(cam, 96, 64, 4, max_depth=12)["rgba"]
+    assert np.array_equal(bits(rgba), bits(want))
+
+
 def test_autotuned_variants_are_bit_identical(ctx):
     from mcrt_gb300 import scenes
     sc = scenes.displaced_icosphere(seed=3, level=5, width=64, height=48)
