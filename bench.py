@@ -14,6 +14,11 @@ roofline : the closest-hit (extend) kernel against the bytes-per-ray memory roof
            B_ray = 48 N_node + 64 N_tri + 48 bytes, N_node / N_tri = mean nodes visited and
            triangles tested by the reference traversal of the reference BVH (oracle statistics
            over a sample of the workload's own paths).
+time_to_relmse : seeded Cornell box 512x512, depth 8: device time until the running
+           estimate reaches relMSE 1e-3 against a 4096-spp NEE reference, reference
+           estimator ("plain") and next-event estimation.
+adjoint  : path-replay adjoint of the GGX Cornell box, 256x256, 32 spp: paths/s
+           through mcrt_adjoint with host buffers.
 cpu_baseline / --impl reference : the CPU oracle (a restatement of the reference's path:
            its single-threaded SAH build and the path_trace.wgsl estimator on all host cores),
            on a bounded row sample of the frame, extrapolated to one frame.
@@ -204,6 +209,71 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------ GPU arm
+def time_to_relmse(M, ctx, target=1e-3, w=512, h=512, depth=8, ref_spp=4096, max_spp=16384):
+    """Seeded Cornell box at 512 x 512, depth 8: device time for the running
+    estimate to reach relMSE <= target against a 4096-spp NEE reference (mean
+    over pixels and channels of (x - r)^2 / (r^2 + 1e-2)), for the reference
+    estimator and for NEE + MIS.  Estimates grow in chunks (KEEP_ACCUM); relMSE
+    is evaluated between chunks, outside the timed kernels."""
+    from mcrt_gb300 import scenes
+    sc = scenes.cornell_box(SEED)
+    c = sc["camera"]
+    cam = M.compute_camera(w, h, c["look_from"], c["look_at"], c["vfov"], 0.0)
+    ctx.upload_scene(vertices=sc["vertices"], triangles=sc["triangles"], materials=sc["materials"],
+                     env=M.gradient_env_map())
+    ref = ctx.render(cam, w, h, ref_spp, first_frame=1 << 20, max_depth=depth, nee=True, outputs=("sum",))["sum"]
+    ref /= ref_spp
+    out = {"workload": f"cornell_box_seed{SEED}_{w}x{h}_depth{depth}", "target_relmse": target,
+           "reference": f"NEE {ref_spp} spp, independent frames"}
+    for name, nee in (("plain", False), ("nee", True)):
+        total, ms, rel = 0, 0.0, None
+        while total < max_spp:
+            chunk = max(16, total // 8)
+            r = ctx.render(cam, w, h, chunk, first_frame=total, max_depth=depth, nee=nee, keep=total > 0,
+                           outputs=("sum",))
+            ms += ctx.timings()["total_ms"]
+            total += chunk
+            x = r["sum"] / total
+            rel = float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
+            if rel <= target:
+                break
+        out[name] = {"spp": total, "ms": round(ms, 2), "relmse": round(rel, 6), "reached": rel <= target,
+                     "msamples_per_s": round(w * h * total / (ms / 1000.0) / 1e6, 1)}
+    if out["plain"]["reached"] and out["nee"]["reached"]:
+        out["speedup_nee_vs_plain"] = round(out["plain"]["ms"] / out["nee"]["ms"], 2)
+    return out
+
+
+def adjoint_rate(M, ctx, stream, n_warm=3, n_calls=10, w=256, h=256, spp=32, depth=8):
+    """Path-replay adjoint of the GGX Cornell box at 256 x 256, 32 spp (primal +
+    replay), NEE: paths per second through mcrt_adjoint with host buffers
+    (d_image in, gradient out), CUDA events on the library's stream."""
+    import torch
+    from mcrt_gb300 import scenes
+    sc = scenes.cornell_box_ggx(SEED)
+    c = sc["camera"]
+    cam = M.compute_camera(w, h, c["look_from"], c["look_at"], c["vfov"], 0.0)
+    ctx.upload_scene(vertices=sc["vertices"], triangles=sc["triangles"], materials=sc["materials"],
+                     env=M.gradient_env_map())
+    d_img = np.random.default_rng(0).standard_normal((h, w, 4)).astype(np.float32)
+    for i in range(n_warm):
+        ctx.adjoint(cam, w, h, spp, d_img, first_frame=i * spp, max_depth=depth, nee=True)
+    ms, dev = [], []
+    for i in range(n_calls):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.adjoint(cam, w, h, spp, d_img, first_frame=(n_warm + i) * spp, max_depth=depth, nee=True)
+        b.record(stream)
+        b.synchronize()
+        ms.append(a.elapsed_time(b))
+        dev.append(ctx.timings()["total_ms"])
+    t = sum(ms) / len(ms)
+    return {"value": round(w * h * spp / (t / 1000.0), 1), "unit": "paths/s", "ms_per_call": round(t, 3),
+            "device_ms_per_call": round(sum(dev) / len(dev), 3), "calls": n_calls,
+            "workload": f"cornell_box_ggx_seed{SEED}_{w}x{h}_{spp}spp_depth{depth}_nee",
+            "params": "64 material slots x (albedo rgb, roughness)"}
+
+
 def run_mcrt(args):
     import torch
     import mcrt_gb300 as M
@@ -287,6 +357,10 @@ def run_mcrt(args):
                 "n_tri": round(n_tri, 2), "mrays_per_s": round(rays / (ext_ms / 1000.0) / 1e6, 1),
                 "avg_launch_ms": round(ext_ms / max(ext_launches, 1), 4)}
     clocks = clk.summary()
+    quality = adjoint = None
+    if not args.small:
+        quality = time_to_relmse(M, ctx)
+        adjoint = adjoint_rate(M, ctx, stream)
     out = {
         "metric": "Msamples/s", "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 3), "higher_is_better": True,
@@ -303,6 +377,8 @@ def run_mcrt(args):
         "clocks": clocks,
         "extend_ms_per_step": round(ext_ms / len(ext), 3),
         "breakdown_ms_per_step": device_breakdown,
+        "time_to_relmse": quality,
+        "adjoint": adjoint,
     }
     print(json.dumps(out))
     barrier(world)

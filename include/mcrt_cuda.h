@@ -229,6 +229,37 @@ mcrt_status mcrt_render(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t 
 mcrt_status mcrt_render_noalloc(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t w, uint32_t h, uint32_t spp,
                                 uint32_t first_frame, const mcrt_render_opts *opts, float *d_out_rgba);
 
+/* ------------------------------------------------------------------ differentiation */
+
+/* Replace the material table of the uploaded scene (GpuMaterialData,
+ * material.rs:56-63) without re-uploading geometry; the light-selection
+ * weights are recomputed.  Which slots are emissive must not change
+ * (MCRT_ERR_INVALID_ARG).  No counterpart in the reference, which rebuilds
+ * its buffers (gpu_layout.rs:259-390). */
+mcrt_status mcrt_update_materials(mcrt_ctx *ctx, const mcrt_gpu_material_data *materials);
+
+/* Gradient of an image loss with respect to the material parameters by
+ * path-replay backpropagation (no counterpart in the reference).  The call
+ * renders frames first_frame .. first_frame+spp-1 as mcrt_render with the same
+ * opts (the primal pass), then replays every path from its seed and
+ * accumulates
+ *   grad[4*m + k] = sum_pixels sum_c d_image[pixel].c / spp * d(mean of the
+ *                   samples).c / d(param m,k)
+ * for material slot m and k = albedo r, g, b (albedo_fuzz[0..2]) and
+ * roughness (albedo_fuzz[3], GGX materials).  For emissive slots the albedo is
+ * the radiance colour (radiance = ior_pad[0] * albedo).  BSDF sampling, light
+ * choice and MIS weights are held fixed while differentiating (detached
+ * sampling): the estimate is unbiased for the derivative of the expected image.
+ * Metal fuzz, dielectric IOR and texture texels get no gradient.
+ *   d_image : host, w*h*4 floats (alpha ignored) = dLoss/d(image)
+ *   grad    : host, 256 doubles (overwritten)
+ *   out_rgba: optional host w*h*4 floats, the primal running mean (as mcrt_render)
+ * The device accumulation afterwards holds the primal render (mcrt_read_accum).
+ * KEEP_ACCUM is not supported.  Synchronous on return. */
+mcrt_status mcrt_adjoint(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t w, uint32_t h, uint32_t spp,
+                         uint32_t first_frame, const mcrt_render_opts *opts, const float *d_image, double *grad,
+                         float *out_rgba);
+
 /* Copy the device accumulation of the last render to the host (any may be NULL). */
 mcrt_status mcrt_read_accum(mcrt_ctx *ctx, float *out_rgba, double *accum_rgb, float *out_gbuf);
 

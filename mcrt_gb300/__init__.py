@@ -276,6 +276,28 @@ class Context:
         self._last_hw = (height, width)
         return dict(rgba=rgba, sum=acc, gbuf=gb)
 
+    def update_materials(self, materials):
+        """Replace the material table (same emissive slots) without re-uploading geometry."""
+        md = _arr(materials, MATERIAL_DATA)
+        self._check(lib().mcrt_update_materials(self._h, ptr(md)))
+
+    def adjoint(self, camera, width, height, spp, d_image, first_frame=0, max_depth=0, nee=False,
+                with_image=False):
+        """Path-replay backpropagation: gradient of sum(d_image * image) with respect to the
+        material parameters, as a (64, 4) array (albedo r, g, b, roughness per slot).
+        d_image: (height, width, 3 or 4) = dLoss/d(image)."""
+        cam = _arr(camera, CAMERA)
+        d = np.zeros((height, width, 4), np.float32)
+        di = np.asarray(d_image, np.float32).reshape(height, width, -1)
+        d[..., :di.shape[-1]] = di
+        o = N.RenderOpts(max_depth=max_depth, flags=N.RENDER_NEE if nee else 0)
+        grad = np.zeros(256, np.float64)
+        rgba = np.zeros((height, width, 4), np.float32) if with_image else None
+        self._check(lib().mcrt_adjoint(self._h, ptr(cam), width, height, spp, first_frame, ctypes.byref(o), ptr(d),
+                                       ptr(grad), ptr(rgba)))
+        self._last_hw = (height, width)
+        return (grad.reshape(64, 4), rgba) if with_image else grad.reshape(64, 4)
+
     def autotune(self, camera, width, height, spp, max_depth=0, nee=False):
         """Pick the fastest closest-hit kernel variant for this scene; returns (variant, extend ms per variant)."""
         cam = _arr(camera, CAMERA)

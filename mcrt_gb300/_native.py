@@ -103,6 +103,9 @@ SIGNATURES = [
     ("mcrt_render_noalloc", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_uint32,
                                     POINTER(RenderOpts), c_void_p]),
     ("mcrt_read_accum", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("mcrt_update_materials", c_int, [c_void_p, c_void_p]),
+    ("mcrt_adjoint", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_uint32, POINTER(RenderOpts),
+                             c_void_p, c_void_p, c_void_p]),
     ("mcrt_autotune", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, POINTER(RenderOpts),
                               POINTER(c_uint32), POINTER(c_float)]),
     ("mcrt_read_image_rgba8", c_int, [c_void_p, c_uint32, c_void_p]),

@@ -100,6 +100,9 @@ struct mcrt_ctx {
     unsigned long long last_render_launches = 0, last_build_launches = 0, last_extend_launches = 0;
     float last_build_ms = 0.0f;
     int extend_variant = 0;   // chosen by mcrt_autotune
+    // adjoint
+    DBuf dimg, grad;
+    mcrt_gpu_material_data host_materials{};
 };
 
 namespace {
@@ -242,6 +245,35 @@ mcrt_status finish_lights(mcrt_ctx *ctx) {
     CK(cudaStreamSynchronize(ctx->stream), "light cdf");
     ctx->light_total = total;
     if (!(total > 0.0f)) ctx->n_lights = 0;
+    return MCRT_OK;
+}
+
+// Path state for n_slots concurrent samples (structure of arrays in one allocation).
+mcrt_status ensure_path_buffers(mcrt_ctx *ctx, uint32_t n_slots) {
+    if (ctx->pb.n_slots < n_slots) {
+        // thr L aux, q_o q_d x2, hits, sh o d c, pend sh_g
+        size_t per = 16 * 3 + 16 * 4 + 16 + 16 * 3 + 16 * 2;
+        CK(ctx->pbmem.ensure((size_t)n_slots * per + 256), "allocate path state");
+        char *p = ctx->pbmem.as<char>();
+        auto take = [&](size_t bytes) { char *r = p; p += bytes; return r; };
+        ctx->pb.thr = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
+        ctx->pb.L = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
+        ctx->pb.aux = reinterpret_cast<uint4 *>(take((size_t)n_slots * 16));
+        for (int k = 0; k < 2; ++k) {
+            ctx->pb.q_o[k] = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
+            ctx->pb.q_d[k] = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
+        }
+        ctx->pb.hits = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
+        ctx->pb.sh_o = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
+        ctx->pb.sh_d = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
+        ctx->pb.sh_c = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
+        ctx->pb.pend = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
+        ctx->pb.sh_g = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
+        ctx->pb.n_slots = n_slots;
+    }
+    CK(ctx->counters.ensure(256), "allocate counters");
+    ctx->pb.counters = ctx->counters.as<uint32_t>();
+    ctx->pb.stats = reinterpret_cast<unsigned long long *>(ctx->counters.as<char>() + 128);
     return MCRT_OK;
 }
 
@@ -450,6 +482,7 @@ mcrt_status mcrt_upload_scene(mcrt_ctx *ctx, const mcrt_scene_desc *d) {
         ctx->albedo_size = size;
     }
     // ---- materials, environment
+    std::memcpy(&ctx->host_materials, d->materials, sizeof(mcrt_gpu_material_data));
     CK(ctx->materials.ensure(sizeof(mcrt_gpu_material_data)), "allocate materials");
     CK(cudaMemcpyAsync(ctx->materials.p, d->materials, sizeof(mcrt_gpu_material_data), cudaMemcpyHostToDevice, st),
        "upload");
@@ -575,27 +608,10 @@ mcrt_status mcrt_render(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t 
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
     cudaStream_t st = ctx->stream;
     // ---- buffers
-    if (ctx->pb.n_slots < n_slots) {
-        size_t per = 16 * 3 + 16 * 4 + 16 + 16 * 3;   // thr L aux, q_o q_d x2, hits, sh o d c
-        CK(ctx->pbmem.ensure((size_t)n_slots * per + 256), "allocate path state");
-        char *p = ctx->pbmem.as<char>();
-        auto take = [&](size_t bytes) { char *r = p; p += bytes; return r; };
-        ctx->pb.thr = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
-        ctx->pb.L = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
-        ctx->pb.aux = reinterpret_cast<uint4 *>(take((size_t)n_slots * 16));
-        for (int k = 0; k < 2; ++k) {
-            ctx->pb.q_o[k] = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
-            ctx->pb.q_d[k] = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
-        }
-        ctx->pb.hits = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
-        ctx->pb.sh_o = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
-        ctx->pb.sh_d = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
-        ctx->pb.sh_c = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
-        ctx->pb.n_slots = n_slots;
+    {
+        mcrt_status bs = ensure_path_buffers(ctx, n_slots);
+        if (bs != MCRT_OK) return bs;
     }
-    CK(ctx->counters.ensure(256), "allocate counters");
-    ctx->pb.counters = ctx->counters.as<uint32_t>();
-    ctx->pb.stats = reinterpret_cast<unsigned long long *>(ctx->counters.as<char>() + 128);
     if (!keep || ctx->acc_w != w || ctx->acc_h != h) {
         CK(ctx->mean.ensure((size_t)npix * 16), "allocate accumulation");
         CK(ctx->sum.ensure((size_t)npix * 24), "allocate accumulation");
@@ -692,6 +708,124 @@ mcrt_status mcrt_render(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t 
     if (out_gbuf)
         CK(cudaMemcpyAsync(out_gbuf, ctx->gbuf.p, (size_t)npix * 16, cudaMemcpyDeviceToHost, st), "read G-buffer");
     CK(cudaStreamSynchronize(st), "render outputs");
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_update_materials(mcrt_ctx *ctx, const mcrt_gpu_material_data *materials) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!ctx->has_scene) return fail(ctx, MCRT_ERR_NO_SCENE, "no scene uploaded");
+    if (!materials) return fail(ctx, MCRT_ERR_INVALID_ARG, "materials is NULL");
+    for (int k = 0; k < 64; ++k) {
+        const bool was = ctx->host_materials.materials[k].type_pad[0] == MCRT_MAT_EMISSIVE;
+        const bool now = materials->materials[k].type_pad[0] == MCRT_MAT_EMISSIVE;
+        if (was != now)
+            return fail(ctx, MCRT_ERR_INVALID_ARG,
+                        "material " + std::to_string(k) + " changes emissive type (upload the scene instead)");
+    }
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    std::memcpy(&ctx->host_materials, materials, sizeof(mcrt_gpu_material_data));
+    CK(cudaMemcpyAsync(ctx->materials.p, materials, sizeof(mcrt_gpu_material_data), cudaMemcpyHostToDevice,
+                       ctx->stream),
+       "upload materials");
+    // light selection weights depend on the emitted radiance
+    mcrt_status s = finish_lights(ctx);
+    if (s != MCRT_OK) return s;
+    CK(cudaStreamSynchronize(ctx->stream), "update materials");
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_adjoint(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t w, uint32_t h, uint32_t spp,
+                         uint32_t first_frame, const mcrt_render_opts *opts, const float *d_image, double *grad,
+                         float *out_rgba) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!ctx->has_scene) return fail(ctx, MCRT_ERR_NO_SCENE, "no scene uploaded");
+    if (!cam || !d_image || !grad) return fail(ctx, MCRT_ERR_INVALID_ARG, "cam, d_image and grad are required");
+    if (w == 0 || h == 0 || spp == 0) return fail(ctx, MCRT_ERR_INVALID_ARG, "width, height and spp must be > 0");
+    if ((uint64_t)w * h > (1ull << 26)) return fail(ctx, MCRT_ERR_INVALID_ARG, "image too large (max 2^26 pixels)");
+    mcrt_render_opts o{};
+    if (opts) o = *opts;
+    if (o.flags & MCRT_RENDER_KEEP_ACCUM) return fail(ctx, MCRT_ERR_INVALID_ARG, "KEEP_ACCUM is not supported");
+    const uint32_t depth = o.max_depth ? o.max_depth : mcrt::kDefaultBounces;
+    if (depth > 1024) return fail(ctx, MCRT_ERR_INVALID_ARG, "max_depth too large");
+    const uint32_t npix = w * h;
+    const uint64_t kTargetSlots = 1ull << 22, kMaxSlots = 1ull << 24;
+    uint32_t spp_pass = o.spp_per_pass;
+    if (spp_pass == 0) spp_pass = (uint32_t)std::max<uint64_t>(1, (kTargetSlots + npix - 1) / npix);
+    spp_pass = std::min(spp_pass, spp);
+    spp_pass = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(spp_pass, kMaxSlots / npix));
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+    {
+        mcrt_status bs = ensure_path_buffers(ctx, npix * spp_pass);
+        if (bs != MCRT_OK) return bs;
+    }
+    CK(ctx->mean.ensure((size_t)npix * 16), "allocate accumulation");
+    CK(ctx->sum.ensure((size_t)npix * 24), "allocate accumulation");
+    CK(ctx->gbuf.ensure((size_t)npix * 16), "allocate G-buffer");
+    ctx->acc_w = w;
+    ctx->acc_h = h;
+    CK(ctx->dimg.ensure((size_t)npix * 16), "allocate image gradient");
+    CK(ctx->grad.ensure(256 * sizeof(double)), "allocate parameter gradient");
+    CK(cudaMemcpyAsync(ctx->dimg.p, d_image, (size_t)npix * 16, cudaMemcpyHostToDevice, st), "upload d_image");
+    CK(cudaMemsetAsync(ctx->grad.p, 0, 256 * sizeof(double), st), "clear gradient");
+    CK(cudaMemsetAsync(ctx->counters.p, 0, 256, st), "clear counters");
+    mcrt::DeviceScene S = device_scene(ctx);
+    mcrt::AdjointParams A;
+    A.dimg = ctx->dimg.as<float4>();
+    A.inv_spp = 1.0f / (float)spp;
+    A.grad = ctx->grad.as<double>();
+    const bool nee = (o.flags & MCRT_RENDER_NEE) != 0 && ctx->n_lights > 0;
+    const unsigned long long launches0 = mcrt::launch_count();
+    cudaEvent_t e_begin = ev(ctx, 2), e_end = ev(ctx, 3);
+    cudaEventRecord(e_begin, st);
+    uint32_t done = 0;
+    while (done < spp) {
+        mcrt::RenderParams P{};
+        P.w = w; P.h = h; P.npix = npix;
+        P.spp_pass = std::min(spp_pass, spp - done);
+        P.frame0 = first_frame + done;
+        P.max_depth = depth;
+        P.flags = o.flags;
+        P.cam = *cam;
+        P.gbuf_plane = -1;
+        P.extend_variant = o.variant ? (int)o.variant - 1 : ctx->extend_variant;
+        // primal pass: the per-path radiance of these samples
+        mcrt::launch_raygen(S, P, ctx->pb, st);
+        int qi = 0;
+        for (uint32_t b = 0; b < depth; ++b) {
+            mcrt::launch_extend(S, P, ctx->pb, qi, st);
+            mcrt::launch_shade(S, P, ctx->pb, qi, b, nullptr, st);
+            if (nee) mcrt::launch_shadow(S, P, ctx->pb, st);
+            qi ^= 1;
+        }
+        mcrt::launch_resolve(P, ctx->pb, ctx->mean.as<float4>(), ctx->sum.as<double>(), done > 0, st);
+        // adjoint pass: replay the same paths from their seeds
+        mcrt::launch_raygen(S, P, ctx->pb, st, true);
+        qi = 0;
+        for (uint32_t b = 0; b < depth; ++b) {
+            mcrt::launch_extend(S, P, ctx->pb, qi, st);
+            mcrt::launch_shade(S, P, ctx->pb, qi, b, nullptr, st, &A);
+            if (nee) mcrt::launch_shadow(S, P, ctx->pb, st, &A);
+            qi ^= 1;
+        }
+        done += P.spp_pass;
+    }
+    cudaEventRecord(e_end, st);
+    CK(cudaGetLastError(), "adjoint launch");
+    CK(cudaEventSynchronize(e_end), "adjoint");
+    ctx->last_render_launches = mcrt::launch_count() - launches0;
+    ctx->acc_valid = true;
+    ctx->gbuf_valid = false;
+    float ms[6] = {0, 0, 0, 0, 0, ctx->last_build_ms};
+    cudaEventElapsedTime(&ms[0], e_begin, e_end);
+    std::memcpy(ctx->last_ms, ms, sizeof(ms));
+    uint32_t ctr[4];
+    CK(cudaMemcpy(ctr, ctx->counters.p, 16, cudaMemcpyDeviceToHost), "read counters");
+    CK(cudaMemcpy(ctx->last_counts, ctx->pb.stats, 16, cudaMemcpyDeviceToHost), "read counters");
+    if (ctr[3]) return fail(ctx, MCRT_ERR_STACK_OVERFLOW, "traversal stack bound reached");
+    CK(cudaMemcpy(grad, ctx->grad.p, 256 * sizeof(double), cudaMemcpyDeviceToHost), "read gradient");
+    if (out_rgba)
+        CK(cudaMemcpy(out_rgba, ctx->mean.p, (size_t)npix * 16, cudaMemcpyDeviceToHost), "read image");
     return MCRT_OK;
 }
 

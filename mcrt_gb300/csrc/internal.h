@@ -30,6 +30,16 @@ struct PathBuffers {
     float4 *sh_c = nullptr;      // contribution rgb | unused
     uint32_t *counters = nullptr;  // [0],[1] ray queue sizes, [2] shadow queue size, [3] overflow flag, [4..] stats
     unsigned long long *stats = nullptr;  // [0] rays traced, [1] shadow rays
+    // adjoint replay only
+    float4 *pend = nullptr;      // per slot: d log(BSDF weight) / d(albedo rgb | roughness) of the last vertex
+    float4 *sh_g = nullptr;      // per shadow ray: d log(NEE term) / d(albedo rgb | roughness)
+};
+
+// Adjoint (path-replay backpropagation) inputs of the replay kernels.
+struct AdjointParams {
+    const float4 *dimg = nullptr;   // dLoss / d(image), per pixel (rgb)
+    float inv_spp = 0.0f;           // 1 / samples per pixel of the call
+    double *grad = nullptr;         // 64 material slots x (albedo r, g, b, roughness)
 };
 
 struct RenderParams {
@@ -47,11 +57,16 @@ int extend_variant_count();
 // Launchers (render.cu)
 void launch_trace_closest(const DeviceScene &S, const mcrt_ray *rays, uint32_t n, mcrt_hit *hits, bool ref_layout,
                           uint32_t *overflow, cudaStream_t st);
-void launch_raygen(const DeviceScene &S, const RenderParams &P, PathBuffers &B, cudaStream_t st);
+// keep_radiance: replay of the same paths (the per-path radiance of the primal
+// pass stays in B.L as the radiance still to be accounted for).
+void launch_raygen(const DeviceScene &S, const RenderParams &P, PathBuffers &B, cudaStream_t st,
+                   bool keep_radiance = false);
 void launch_extend(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, cudaStream_t st);
+// adj non-null: the adjoint replay variants (same sampling, plus gradient accumulation).
 void launch_shade(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, uint32_t bounce,
-                  float4 *gbuf, cudaStream_t st);
-void launch_shadow(const DeviceScene &S, const RenderParams &P, PathBuffers &B, cudaStream_t st);
+                  float4 *gbuf, cudaStream_t st, const AdjointParams *adj = nullptr);
+void launch_shadow(const DeviceScene &S, const RenderParams &P, PathBuffers &B, cudaStream_t st,
+                   const AdjointParams *adj = nullptr);
 void launch_resolve(const RenderParams &P, const PathBuffers &B, float4 *mean, double *sum, bool keep,
                     cudaStream_t st);
 void launch_tonemap(const float4 *mean, uint32_t npix, uint32_t mode, uchar4 *out, cudaStream_t st);

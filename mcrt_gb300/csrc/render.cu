@@ -185,7 +185,7 @@ __device__ __forceinline__ float ggx_d(float alpha, float cos_h) {
 }
 // Sample wi for wo (both in the local frame, z = normal); returns the weight f*cos/pdf.
 __device__ __forceinline__ bool ggx_sample(f3 wo, float alpha, f3 f0, float r1, float r2, f3 *wi_out, f3 *weight,
-                                           float *pdf_out) {
+                                           float *pdf_out, float *mz_out = nullptr, float *fw_out = nullptr) {
     // stretch
     f3 vh = normalize(mk3(alpha * wo.x, alpha * wo.y, wo.z));
     float lensq = vh.x * vh.x + vh.y * vh.y;
@@ -213,9 +213,12 @@ __device__ __forceinline__ bool ggx_sample(f3 wo, float alpha, f3 f0, float r1, 
     // pdf(wi) = D_v(m) / (4 wo.m) = G1(wo) max(0, wo.m) D(m) / (wo.z 4 wo.m)
     *pdf_out = g1 * ggx_d(alpha, m.z) / (4.0f * wo.z);
     *wi_out = wi;
+    if (mz_out) *mz_out = m.z;
+    if (fw_out) *fw_out = fw;
     return true;
 }
-__device__ __forceinline__ f3 ggx_eval(f3 wo, f3 wi, float alpha, f3 f0, float *pdf_out) {
+__device__ __forceinline__ f3 ggx_eval(f3 wo, f3 wi, float alpha, f3 f0, float *pdf_out, float *mz_out = nullptr,
+                                       float *fw_out = nullptr) {
     // returns f * cos(wi)
     *pdf_out = 0.0f;
     if (wo.z <= 0.0f || wi.z <= 0.0f) return mk3(0.0f, 0.0f, 0.0f);
@@ -228,8 +231,41 @@ __device__ __forceinline__ f3 ggx_eval(f3 wo, f3 wi, float alpha, f3 f0, float *
     float fw = dm_pow(1.0f - fmaxf(0.0f, wo_m), 5.0f);
     f3 F = f0 + fw * (mk3(1.0f, 1.0f, 1.0f) - f0);
     *pdf_out = g1 * D / (4.0f * wo.z);
+    if (mz_out) *mz_out = m.z;
+    if (fw_out) *fw_out = fw;
     return (D * g2 / (4.0f * wo.z)) * F;
 }
+
+// d log(D(m) G2(wo, wi)) / d alpha: the roughness derivative of log(f cos) of
+// the GGX lobe (the Fresnel term does not depend on alpha).
+//   d log D / d a  = 2/a - 4 a c^2 / (c^2 (a^2 - 1) + 1),   c = m.z
+//   d log G2 / d a = -(dL(wo) + dL(wi)) / (1 + L(wo) + L(wi)),
+//   dL/da = a t^2 / (2 sqrt(1 + a^2 t^2)),  t^2 = tan^2 of the direction.
+__device__ __forceinline__ float ggx_dlog_dalpha(float alpha, float mz, float cos_o, float cos_i) {
+    float c2 = mz * mz;
+    float den = c2 * (alpha * alpha - 1.0f) + 1.0f;
+    float dlog_d = 2.0f / alpha - 4.0f * alpha * c2 / den;
+    auto lam = [&](float c, float *dl) {
+        float cc = c * c;
+        float t2 = fmaxf(0.0f, 1.0f - cc) / fmaxf(cc, 1e-12f);
+        float sq = sqrtf(1.0f + alpha * alpha * t2);
+        *dl = 0.5f * alpha * t2 / sq;
+        return 0.5f * (sq - 1.0f);
+    };
+    float dlo, dli;
+    float lo = lam(cos_o, &dlo), li = lam(cos_i, &dli);
+    return dlog_d - (dlo + dli) / ((1.0f + lo) + li);
+}
+
+// Texture factor of a material at a hit (material_albedo = factor * albedo).
+__device__ __forceinline__ f3 material_tex(const DeviceScene &S, const mcrt_gpu_material &m, f3 p, float4 h) {
+    uint32_t layer = m.type_pad[1];
+    if (layer == 0u || S.albedo_layers == 0u) return mk3(1.0f, 1.0f, 1.0f);
+    float u, v;
+    hit_uv(S, p, h, &u, &v);
+    return sample_albedo(S, min(layer, S.albedo_layers - 1u), u, v);
+}
+__device__ __forceinline__ float safe_ratio(float a, float b) { return b != 0.0f ? a / b : 0.0f; }
 
 // ------------------------------------------------------------------ light sampling (NEE)
 // Lights are the emissive triangles (by original id) and emissive spheres (by
@@ -270,7 +306,7 @@ __device__ __forceinline__ uint32_t pick_light(const DeviceScene &S, float u) {
     return lo;
 }
 
-struct LightSample { f3 dir; float dist; float pdf; f3 Le; bool ok; };
+struct LightSample { f3 dir; float dist; float pdf; f3 Le; uint32_t mat; bool ok; };
 
 // Uniform point on an emissive triangle, or a direction in the cone subtended by
 // an emissive sphere.  pdf is per unit solid angle at x (including the choice of
@@ -307,6 +343,7 @@ __device__ __forceinline__ LightSample sample_light(const DeviceScene &S, f3 x, 
         ls.dir = dir;
         ls.dist = dist;
         ls.pdf = prob / (kTau * (1.0f - cosmax));
+        ls.mat = min(S.spheres[slot].mat_and_pad[0], kMaxMatIdx);
         ls.Le = emission_of(S, S.spheres[slot].mat_and_pad[0]);
         ls.ok = dist > 0.0f;
         return ls;
@@ -334,6 +371,7 @@ __device__ __forceinline__ LightSample sample_light(const DeviceScene &S, f3 x, 
     ls.dir = dir;
     ls.dist = dist;
     ls.pdf = prob * dist2 / (cos_l * (0.5f * area2));
+    ls.mat = min(tri.mat_idx & 0x7fffffffu, kMaxMatIdx);
     ls.Le = emission_of(S, tri.mat_idx & 0x7fffffffu);
     ls.ok = true;
     return ls;
@@ -388,7 +426,7 @@ __global__ void k_trace_closest(DeviceScene S, const mcrt_ray *rays, uint32_t n,
     hits[i] = h;
 }
 
-__global__ void k_raygen(DeviceScene S, RenderParams P, PathBuffers B) {
+__global__ void k_raygen(DeviceScene S, RenderParams P, PathBuffers B, int keep_radiance) {
     uint32_t n = P.npix * P.spp_pass;
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) { B.counters[0] = n; B.counters[1] = 0; B.counters[2] = 0; B.counters[4] = 0; B.counters[5] = 0; }
@@ -401,7 +439,7 @@ __global__ void k_raygen(DeviceScene S, RenderParams P, PathBuffers B) {
     f3 o, d;
     camera_ray(P.cam, x, y, P.w, P.h, rng, &o, &d);
     B.thr[i] = make_float4(1.0f, 1.0f, 1.0f, -1.0f);
-    B.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (!keep_radiance) B.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     B.aux[i] = make_uint4(rng, p, frame, kFlagSpecular);
     B.q_o[0][i] = make_float4(o.x, o.y, o.z, __uint_as_float(i));
     B.q_d[0][i] = make_float4(d.x, d.y, d.z, 0.0f);
@@ -611,8 +649,31 @@ __global__ void __launch_bounds__(128, MINB) k_extend(DeviceScene S, PathBuffers
     if (traced) atomicAdd(B.stats, (unsigned long long)traced);
 }
 
+// Shading of the queued hits.  ADJ = false: the forward estimator.  ADJ = true:
+// the adjoint replay of the same paths (path-replay backpropagation, Vicini et
+// al. 2021): the sampling is the forward code's, consuming the same random
+// numbers, and B.L starts as each path's forward radiance and is reduced, vertex
+// by vertex, to the radiance still ahead of the path (Lrem).  With the sampling
+// held fixed (detached), a parameter pi of the vertex's material changes
+//   an emitted term E               by  E * dlog(Le)/dpi,
+//   a next-event term N             by  N * dlog(f)/dpi       (k_shadow),
+//   every term after the BSDF sample by Lrem * dlog(f cos / pdf)/dpi,
+// each weighted by delta = dLoss/dImage(pixel) / spp.  The last one needs Lrem
+// after this vertex's next-event term, which k_shadow subtracts after this
+// kernel: it is stored (B.pend, material in aux.w bits 8..15) and applied at
+// the path's next vertex.  Gradients collect in shared memory per block, then
+// one double atomic per parameter and block.
+template <bool ADJ>
 __global__ void __launch_bounds__(256) k_shade(DeviceScene S, RenderParams P, PathBuffers B, int qi,
-                                                uint32_t bounce, float4 *gbuf) {
+                                                uint32_t bounce, float4 *gbuf, AdjointParams A) {
+    __shared__ float gacc[ADJ ? 256 : 1];
+    if (ADJ) {
+        gacc[threadIdx.x] = 0.0f;
+        __syncthreads();
+    }
+    auto gadd = [&](uint32_t k, float v) {
+        if (ADJ && v != 0.0f) atomicAdd(&gacc[k], v);
+    };
     const uint32_t n = B.counters[qi];
     const bool nee = (P.flags & MCRT_RENDER_NEE) != 0 && S.n_lights > 0;
     const uint32_t lane = threadIdx.x & 31u;
@@ -625,6 +686,8 @@ __global__ void __launch_bounds__(256) k_shade(DeviceScene S, RenderParams P, Pa
         f3 no = {0, 0, 0}, nd = {0, 0, 0}, so = {0, 0, 0}, sd = {0, 0, 0}, sc = {0, 0, 0};
         float smax = 0.0f;
         uint32_t slot = 0;
+        uint32_t sh_bits = 0;                  // adjoint: material | light material << 8
+        float4 sh_dlog = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (i < n) {
             float4 o4 = B.q_o[qi][i], d4 = B.q_d[qi][i];
             float4 h = B.hits[i];
@@ -634,28 +697,53 @@ __global__ void __launch_bounds__(256) k_shade(DeviceScene S, RenderParams P, Pa
             uint4 aux = B.aux[slot];
             f3 thr = xyz(thr4);
             uint32_t rng = aux.x;
+            f3 delta = {0.0f, 0.0f, 0.0f};
+            if (ADJ) {
+                float4 di = A.dimg[aux.y];
+                delta = A.inv_spp * xyz(di);
+                const uint32_t pm = (aux.w >> 8) & 0xffu;
+                if (pm) {                                   // BSDF term of the previous vertex
+                    float4 L = B.L[slot], pd = B.pend[slot];
+                    const uint32_t k0 = 4u * (pm - 1u);
+                    f3 dl = delta * xyz(L);
+                    gadd(k0 + 0, dl.x * pd.x);
+                    gadd(k0 + 1, dl.y * pd.y);
+                    gadd(k0 + 2, dl.z * pd.z);
+                    gadd(k0 + 3, ((dl.x + dl.y) + dl.z) * pd.w);
+                }
+            }
             const bool write_g = gbuf && bounce == 0 && (int)(slot / P.npix) == P.gbuf_plane;
             if (h.x < 0.0f) {                                                   // miss, :592-597
                 if (write_g) gbuf[aux.y] = make_float4(0.0f, 0.0f, 0.0f, kTMax);
-                f3 e = thr * sample_env(S, d);
-                float4 L = B.L[slot];
-                if (nee) B.L[slot] = make_float4(L.x + e.x, L.y + e.y, L.z + e.z, 0.0f);
-                else B.L[slot] = make_float4(e.x, e.y, e.z, 0.0f);
+                if (!ADJ) {
+                    f3 e = thr * sample_env(S, d);
+                    float4 L = B.L[slot];
+                    if (nee) B.L[slot] = make_float4(L.x + e.x, L.y + e.y, L.z + e.z, 0.0f);
+                    else B.L[slot] = make_float4(e.x, e.y, e.z, 0.0f);
+                }
             } else {
                 SurfaceHit sh = surface(S, o, d, h);
                 if (write_g) gbuf[aux.y] = make_float4(sh.n.x, sh.n.y, sh.n.z, sh.t);   // :599-602
-                const mcrt_gpu_material &m = S.materials->materials[min(sh.mat, kMaxMatIdx)];
+                const uint32_t mi = min(sh.mat, kMaxMatIdx);
+                const mcrt_gpu_material &m = S.materials->materials[mi];
                 const uint32_t mtype = m.type_pad[0];
                 f3 albedo = ld3(m.albedo_fuzz);
                 if (mtype == kMatEmissive) {                                    // :608-610
                     f3 e = m.ior_pad[0] * (thr * albedo);
+                    float wmis = 1.0f;
                     if (nee) {
-                        float wmis = 1.0f;
                         if (!(aux.w & kFlagSpecular) && thr4.w > 0.0f) {
                             float pl = light_pdf_of_hit(S, h, o, d);
                             float pb = thr4.w;
                             wmis = (pb * pb) / (pb * pb + pl * pl);
                         }
+                    }
+                    if (ADJ) {                                                  // d E / d(radiance colour)
+                        f3 g = (wmis * m.ior_pad[0]) * (delta * thr);
+                        gadd(4u * mi + 0, g.x);
+                        gadd(4u * mi + 1, g.y);
+                        gadd(4u * mi + 2, g.z);
+                    } else if (nee) {
                         float4 L = B.L[slot];
                         B.L[slot] = make_float4(L.x + wmis * e.x, L.y + wmis * e.y, L.z + wmis * e.z, 0.0f);
                     } else {
@@ -663,9 +751,12 @@ __global__ void __launch_bounds__(256) k_shade(DeviceScene S, RenderParams P, Pa
                     }
                 } else {
                     albedo = material_albedo(S, m, sh.p, h);                    // :506-515
+                    const f3 tex = ADJ ? material_tex(S, m, sh.p, h) : mk3(1.0f, 1.0f, 1.0f);
                     f3 dir = {0, 0, 0}, atten = {0, 0, 0};
                     bool absorbed = false;
                     float pdf = -1.0f;
+                    float4 dlw = make_float4(0.0f, 0.0f, 0.0f, 0.0f);   // adjoint: dlog(weight)/d(params)
+                    bool has_params = false;
                     if (mtype == kMatMetal) {                                   // :530-541
                         float fuzz = m.albedo_fuzz[3];
                         f3 refl = reflect_vec(normalize(d), sh.n);
@@ -673,6 +764,11 @@ __global__ void __launch_bounds__(256) k_shade(DeviceScene S, RenderParams P, Pa
                         dir = normalize(dot(pert, pert) >= 1e-6f ? pert : refl);
                         atten = albedo;
                         absorbed = dot(dir, sh.n) <= 0.0f;
+                        if (ADJ) {
+                            dlw = make_float4(safe_ratio(tex.x, albedo.x), safe_ratio(tex.y, albedo.y),
+                                              safe_ratio(tex.z, albedo.z), 0.0f);
+                            has_params = true;
+                        }
                     } else if (mtype == kMatDielectric) {                       // :543-564
                         atten = mk3(1.0f, 1.0f, 1.0f);
                         float ior = m.ior_pad[0];
@@ -692,24 +788,43 @@ __global__ void __launch_bounds__(256) k_shade(DeviceScene S, RenderParams P, Pa
                         f3 wo = mk3(-dot(d, t), -dot(d, b), -dot(d, sh.n));
                         float rough = m.albedo_fuzz[3];
                         float alpha = fmaxf(rough * rough, 1e-4f);
+                        const float dadr = rough * rough > 1e-4f ? 2.0f * rough : 0.0f;
                         float r1 = rand_f32(rng), r2 = rand_f32(rng);
                         f3 wi, wgt;
-                        float gpdf;
-                        if (wo.z > 0.0f && ggx_sample(wo, alpha, albedo, r1, r2, &wi, &wgt, &gpdf)) {
+                        float gpdf, mz = 0.0f, fw = 0.0f;
+                        if (wo.z > 0.0f && ggx_sample(wo, alpha, albedo, r1, r2, &wi, &wgt, &gpdf, &mz, &fw)) {
                             dir = normalize((wi.x * t + wi.y * b) + wi.z * sh.n);
                             atten = wgt;
                             pdf = gpdf;
+                            if (ADJ) {
+                                const f3 one = mk3(1.0f, 1.0f, 1.0f);
+                                f3 F = albedo + fw * (one - albedo);
+                                dlw = make_float4(safe_ratio((1.0f - fw) * tex.x, F.x),
+                                                  safe_ratio((1.0f - fw) * tex.y, F.y),
+                                                  safe_ratio((1.0f - fw) * tex.z, F.z),
+                                                  ggx_dlog_dalpha(alpha, mz, wo.z, wi.z) * dadr);
+                                has_params = true;
+                            }
                             if (nee) {                                          // light sample at a GGX vertex
                                 LightSample ls = sample_light(S, sh.p, rng);
                                 if (ls.ok) {
                                     f3 wl = mk3(dot(ls.dir, t), dot(ls.dir, b), dot(ls.dir, sh.n));
-                                    float bp;
-                                    f3 fc = ggx_eval(wo, wl, alpha, albedo, &bp);
+                                    float bp, lmz = 0.0f, lfw = 0.0f;
+                                    f3 fc = ggx_eval(wo, wl, alpha, albedo, &bp, &lmz, &lfw);
                                     if (wl.z > 0.0f && (fc.x > 0.0f || fc.y > 0.0f || fc.z > 0.0f)) {
                                         float wmis = (ls.pdf * ls.pdf) / (ls.pdf * ls.pdf + bp * bp);
                                         sc = (wmis / ls.pdf) * (thr * (fc * ls.Le));
                                         so = sh.p; sd = ls.dir; smax = ls.dist * (1.0f - 1e-4f);
                                         shadow = true;
+                                        if (ADJ) {
+                                            const f3 one = mk3(1.0f, 1.0f, 1.0f);
+                                            f3 F = albedo + lfw * (one - albedo);
+                                            sh_dlog = make_float4(safe_ratio((1.0f - lfw) * tex.x, F.x),
+                                                                  safe_ratio((1.0f - lfw) * tex.y, F.y),
+                                                                  safe_ratio((1.0f - lfw) * tex.z, F.z),
+                                                                  ggx_dlog_dalpha(alpha, lmz, wo.z, wl.z) * dadr);
+                                            sh_bits = mi | (ls.mat << 8);
+                                        }
                                     }
                                 }
                             }
@@ -726,22 +841,37 @@ __global__ void __launch_bounds__(256) k_shade(DeviceScene S, RenderParams P, Pa
                                 sc = (wmis * bp / ls.pdf) * (thr * (albedo * ls.Le));
                                 so = sh.p; sd = ls.dir; smax = ls.dist * (1.0f - 1e-4f);
                                 shadow = true;
+                                if (ADJ) {
+                                    sh_dlog = make_float4(safe_ratio(tex.x, albedo.x), safe_ratio(tex.y, albedo.y),
+                                                          safe_ratio(tex.z, albedo.z), 0.0f);
+                                    sh_bits = mi | (ls.mat << 8);
+                                }
                             }
                         }
                         dir = cosine_scatter(rng, sh.n);
                         atten = albedo;
                         pdf = fmaxf(dot(dir, sh.n), 0.0f) / kPi;
+                        if (ADJ) {
+                            dlw = make_float4(safe_ratio(tex.x, albedo.x), safe_ratio(tex.y, albedo.y),
+                                              safe_ratio(tex.z, albedo.z), 0.0f);
+                            has_params = true;
+                        }
                     }
+                    uint32_t pend_bits = 0;
                     if (!absorbed) {
                         thr = thr * atten;
                         if (bounce + 1 < P.max_depth) {
                             cont = true;
                             no = sh.p;
                             nd = dir;
+                            if (ADJ && has_params) {
+                                B.pend[slot] = dlw;
+                                pend_bits = (mi + 1u) << 8;
+                            }
                         }
                         B.thr[slot] = make_float4(thr.x, thr.y, thr.z, pdf);
                     }
-                    B.aux[slot] = make_uint4(rng, aux.y, aux.z, pdf > 0.0f ? 0u : kFlagSpecular);
+                    B.aux[slot] = make_uint4(rng, aux.y, aux.z, (pdf > 0.0f ? 0u : kFlagSpecular) | pend_bits);
                 }
             }
         }
@@ -768,13 +898,33 @@ __global__ void __launch_bounds__(256) k_shade(DeviceScene S, RenderParams P, Pa
                 uint32_t pos = basepos + __popc(smask & ((1u << lane) - 1u));
                 B.sh_o[pos] = make_float4(so.x, so.y, so.z, __uint_as_float(slot));
                 B.sh_d[pos] = make_float4(sd.x, sd.y, sd.z, smax);
-                B.sh_c[pos] = make_float4(sc.x, sc.y, sc.z, 0.0f);
+                B.sh_c[pos] = make_float4(sc.x, sc.y, sc.z, __uint_as_float(sh_bits));
+                if (ADJ) B.sh_g[pos] = sh_dlog;
             }
         }
     }
+    if (ADJ) {
+        __syncthreads();
+        const float v = gacc[threadIdx.x];
+        if (v != 0.0f) atomicAdd(A.grad + threadIdx.x, (double)v);
+    }
 }
 
-__global__ void __launch_bounds__(128) k_shadow(DeviceScene S, PathBuffers B) {
+// Shadow rays of next-event estimation.  ADJ: the replay -- a visible term N
+// leaves the radiance still ahead (B.L -= N) and contributes
+// delta * N * dlog(f)/d(params) to its vertex's material and
+// delta * N / albedo to the emitter's radiance colour.
+template <bool ADJ>
+__global__ void __launch_bounds__(128) k_shadow(DeviceScene S, PathBuffers B, AdjointParams A) {
+    __shared__ float gacc[ADJ ? 256 : 1];
+    if (ADJ) {
+        gacc[threadIdx.x] = 0.0f;
+        gacc[threadIdx.x + 128] = 0.0f;
+        __syncthreads();
+    }
+    auto gadd = [&](uint32_t k, float v) {
+        if (ADJ && v != 0.0f) atomicAdd(&gacc[k], v);
+    };
     const uint32_t n = B.counters[2];
     uint32_t traced = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -785,9 +935,33 @@ __global__ void __launch_bounds__(128) k_shadow(DeviceScene S, PathBuffers B) {
         uint32_t slot = __float_as_uint(o4.w);
         float4 c = B.sh_c[i];
         float4 L = B.L[slot];
-        B.L[slot] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
+        if (!ADJ) {
+            B.L[slot] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
+        } else {
+            B.L[slot] = make_float4(L.x - c.x, L.y - c.y, L.z - c.z, 0.0f);
+            const uint32_t bits = __float_as_uint(c.w);
+            const uint32_t mi = bits & 0xffu, lm = (bits >> 8) & 0xffu;
+            float4 di = A.dimg[B.aux[slot].y];
+            f3 dn = (A.inv_spp * xyz(di)) * xyz(c);
+            float4 g = B.sh_g[i];
+            gadd(4u * mi + 0, dn.x * g.x);
+            gadd(4u * mi + 1, dn.y * g.y);
+            gadd(4u * mi + 2, dn.z * g.z);
+            gadd(4u * mi + 3, ((dn.x + dn.y) + dn.z) * g.w);
+            const float *la = S.materials->materials[lm].albedo_fuzz;
+            gadd(4u * lm + 0, safe_ratio(dn.x, la[0]));
+            gadd(4u * lm + 1, safe_ratio(dn.y, la[1]));
+            gadd(4u * lm + 2, safe_ratio(dn.z, la[2]));
+        }
     }
     if (traced) atomicAdd(B.stats + 1, (unsigned long long)traced);
+    if (ADJ) {
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < 256; k += 128) {
+            const float v = gacc[k];
+            if (v != 0.0f) atomicAdd(A.grad + k, (double)v);
+        }
+    }
 }
 
 // Per pixel, in frame order: the reference's f32 running mean
@@ -897,9 +1071,9 @@ void launch_trace_closest(const DeviceScene &S, const mcrt_ray *rays, uint32_t n
     k_trace_closest<<<(n + 127) / 128, 128, 0, st>>>(S, rays, n, hits, ref_layout ? 1 : 0, overflow); ::mcrt::note_launch();
 }
 
-void launch_raygen(const DeviceScene &S, const RenderParams &P, PathBuffers &B, cudaStream_t st) {
+void launch_raygen(const DeviceScene &S, const RenderParams &P, PathBuffers &B, cudaStream_t st, bool keep_radiance) {
     uint32_t n = P.npix * P.spp_pass;
-    k_raygen<<<(n + 255) / 256, 256, 0, st>>>(S, P, B); ::mcrt::note_launch();
+    k_raygen<<<(n + 255) / 256, 256, 0, st>>>(S, P, B, keep_radiance ? 1 : 0); ::mcrt::note_launch();
 }
 
 int extend_variant_count() { return kExtendVariants; }
@@ -921,16 +1095,21 @@ void launch_extend(const DeviceScene &S, const RenderParams &P, PathBuffers &B, 
 }
 
 void launch_shade(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, uint32_t bounce,
-                  float4 *gbuf, cudaStream_t st) {
+                  float4 *gbuf, cudaStream_t st, const AdjointParams *adj) {
     uint32_t nmax = P.npix * P.spp_pass;
     int blocks = min(grid_blocks_for(nmax, 256), sm_count() * 8);
-    k_shade<<<blocks, 256, 0, st>>>(S, P, B, qi, bounce, gbuf); ::mcrt::note_launch();
+    if (adj) k_shade<true><<<blocks, 256, 0, st>>>(S, P, B, qi, bounce, gbuf, *adj);
+    else k_shade<false><<<blocks, 256, 0, st>>>(S, P, B, qi, bounce, gbuf, AdjointParams{});
+    ::mcrt::note_launch();
 }
 
-void launch_shadow(const DeviceScene &S, const RenderParams &P, PathBuffers &B, cudaStream_t st) {
+void launch_shadow(const DeviceScene &S, const RenderParams &P, PathBuffers &B, cudaStream_t st,
+                   const AdjointParams *adj) {
     uint32_t nmax = P.npix * P.spp_pass;
     int blocks = min(grid_blocks_for(nmax, 128), sm_count() * 16);
-    k_shadow<<<blocks, 128, 0, st>>>(S, B); ::mcrt::note_launch();
+    if (adj) k_shadow<true><<<blocks, 128, 0, st>>>(S, B, *adj);
+    else k_shadow<false><<<blocks, 128, 0, st>>>(S, B, AdjointParams{});
+    ::mcrt::note_launch();
 }
 
 void launch_resolve(const RenderParams &P, const PathBuffers &B, float4 *mean, double *sum, bool keep,

@@ -23,7 +23,7 @@ import numpy as np
 
 from ._native import MATERIAL_DATA, SPHERE, TRIANGLE, VERTEX, MAT_DIELECTRIC, MAT_EMISSIVE, MAT_GGX, MAT_LAMBERTIAN
 
-__all__ = ["cornell_box", "displaced_icosphere", "icosphere", "value_noise3", "smooth_noise_env"]
+__all__ = ["cornell_box", "cornell_box_ggx", "ggx_materials", "displaced_icosphere", "icosphere", "value_noise3", "smooth_noise_env"]
 
 
 def _mat(md, i, t, alb, w=0.0, x=1.0):
@@ -68,7 +68,7 @@ def _box_quads(cx, cz, sx, h, sz, yaw_deg):
     return faces
 
 
-def cornell_box(seed: int = 1234):
+def cornell_box(seed: int = 1234, box_mats=(0, 0)):
     rng = np.random.default_rng(seed)
     md = np.zeros((), MATERIAL_DATA)
     _mat(md, 0, MAT_LAMBERTIAN, (0.73, 0.73, 0.73))
@@ -86,9 +86,9 @@ def cornell_box(seed: int = 1234):
     ]
     _quads_to_mesh([w[0] for w in walls], [w[1] for w in walls], [w[2] for w in walls], verts, tris)
     yaws = rng.uniform(-20.0, 20.0, size=2)
-    for (cx, cz, h), yaw in zip([(0.68, 0.62, 0.3), (0.32, 0.35, 0.6)], yaws):
+    for (cx, cz, h), yaw, bm in zip([(0.68, 0.62, 0.3), (0.32, 0.35, 0.6)], yaws, box_mats):
         faces = _box_quads(cx, cz, 0.28, h, 0.28, yaw)
-        _quads_to_mesh([f[0] for f in faces], [f[1] for f in faces], [0] * 6, verts, tris)
+        _quads_to_mesh([f[0] for f in faces], [f[1] for f in faces], [bm] * 6, verts, tris)
     L = 0.125
     _quads_to_mesh([[(0.5 - L, 0.999, 0.5 - L), (0.5 + L, 0.999, 0.5 - L), (0.5 + L, 0.999, 0.5 + L),
                      (0.5 - L, 0.999, 0.5 + L)]], [(0, -1, 0)], [3], verts, tris)
@@ -99,6 +99,43 @@ def cornell_box(seed: int = 1234):
     camera = dict(look_from=[0.5, 0.5, 2.4], look_at=[0.5, 0.5, 0.0], vfov=40.0, aperture=0.0)
     return dict(vertices=V, triangles=T, materials=md, spheres=np.zeros(0, SPHERE), camera=camera,
                 width=512, height=512, spp=64, max_depth=8)
+
+
+GGX_SLOTS = (0, 1, 2, 4, 5)      # white walls, red wall, green wall, short box, tall box
+LIGHT_SLOT = 3
+
+
+def ggx_materials(albedo, roughness, radiance):
+    """Material table of the differentiable Cornell box: GGX conductors in the
+    slots GGX_SLOTS with per-material albedo (5 x 3) and roughness (5), and the
+    quad light in LIGHT_SLOT with radiance = 1 * albedo (3)."""
+    md = np.zeros((), MATERIAL_DATA)
+    albedo = np.asarray(albedo, np.float32).reshape(5, 3)
+    roughness = np.asarray(roughness, np.float32).reshape(5)
+    for k, slot in enumerate(GGX_SLOTS):
+        _mat(md, slot, MAT_GGX, albedo[k], float(roughness[k]))
+    _mat(md, LIGHT_SLOT, MAT_EMISSIVE, np.asarray(radiance, np.float32).reshape(3), 0.0, 1.0)
+    md["mat_count"] = 6
+    return md
+
+
+def cornell_box_ggx(seed: int = 1234):
+    """The inverse-rendering scene: the seeded Cornell box geometry (boxes in
+    their own material slots) with GGX materials whose target parameters are
+    drawn from the seed -- albedo U[0.1, 0.9]^3 and roughness U[0.1, 0.8] per
+    material, light radiance (17, 12, 4) scaled by U[0.5, 1.5] -- and the
+    optimisation's starting point (albedo 0.5, roughness 0.5, radiance
+    (17, 12, 4)).  Rendered at 256 x 256."""
+    base = cornell_box(seed, box_mats=(4, 5))
+    rng = np.random.default_rng(seed + 1)
+    target = dict(albedo=rng.uniform(0.1, 0.9, (5, 3)).astype(np.float32),
+                  roughness=rng.uniform(0.1, 0.8, 5).astype(np.float32),
+                  radiance=(np.array([17.0, 12.0, 4.0]) * rng.uniform(0.5, 1.5)).astype(np.float32))
+    start = dict(albedo=np.full((5, 3), 0.5, np.float32), roughness=np.full(5, 0.5, np.float32),
+                 radiance=np.array([17.0, 12.0, 4.0], np.float32))
+    base["materials"] = ggx_materials(**target)
+    base.update(target=target, start=start, width=256, height=256, spp=32)
+    return base
 
 
 def icosphere(level: int):

@@ -331,8 +331,6 @@ inline float schlick(float cos_theta, float eta) {
     return r0 + (1.0f - r0) * of_pow(1.0f - cos_theta, 5.0f);
 }
 
-/* path_color, path_trace.wgsl:583-620 (+ G-buffer :592-602) */
-/* stats (optional): [0] rays traced, [1] nodes visited, [2] primitives tested */
 /* uv of a hit: triangles interpolate vertex uvs (path_trace.wgsl:459); spheres
  * map the outward normal to longitude / latitude (:288-291). */
 void hit_uv(const orc_scene *sc, const Closest &c, V3 p, float *uo, float *vo) {
@@ -427,7 +425,8 @@ inline float ggx_d(float alpha, float cos_h) {
     float den = c2 * (a2 - 1.0f) + 1.0f;
     return a2 / (PI_F * den * den);
 }
-bool ggx_sample(V3 wo, float alpha, V3 f0, float r1, float r2, V3 *wi_out, V3 *weight) {
+struct GgxSample { V3 wi; V3 weight; float pdf; float mz; float fw; };
+bool ggx_sample(V3 wo, float alpha, V3 f0, float r1, float r2, GgxSample *out) {
     V3 vh = normalize({alpha * wo.x, alpha * wo.y, wo.z});
     float lensq = vh.x * vh.x + vh.y * vh.y;
     V3 t1 = lensq > 0.0f ? V3{-vh.y, vh.x, 0.0f} / sqrtf(lensq) : V3{1.0f, 0.0f, 0.0f};
@@ -450,21 +449,282 @@ bool ggx_sample(V3 wo, float alpha, V3 f0, float r1, float r2, V3 *wi_out, V3 *w
     float g2 = 1.0f / ((1.0f + l_o) + l_i);
     float fw = of_pow(1.0f - fmaxf(0.0f, wo_m), 5.0f);
     V3 F = f0 + fw * (V3{1.0f, 1.0f, 1.0f} - f0);
-    *weight = (g2 / g1) * F;
-    *wi_out = wi;
+    out->weight = (g2 / g1) * F;
+    out->pdf = g1 * ggx_d(alpha, m.z) / (4.0f * wo.z);     /* D_v(m) / (4 wo.m) */
+    out->wi = wi;
+    out->mz = m.z;
+    out->fw = fw;
     return true;
 }
 
-V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, float *gbuf, uint64_t *stats) {
+/* f(wo, wi) * cos(wi) and the visible-normal pdf of wi (zero below the surface). */
+V3 ggx_eval(V3 wo, V3 wi, float alpha, V3 f0, float *pdf_out, float *mz_out, float *fw_out) {
+    *pdf_out = 0.0f;
+    if (wo.z <= 0.0f || wi.z <= 0.0f) return {0.0f, 0.0f, 0.0f};
+    V3 m = normalize(wo + wi);
+    float l_o = ggx_lambda(alpha, wo.z), l_i = ggx_lambda(alpha, wi.z);
+    float g1 = 1.0f / (1.0f + l_o);
+    float g2 = 1.0f / ((1.0f + l_o) + l_i);
+    float D = ggx_d(alpha, m.z);
+    float wo_m = dot(wo, m);
+    float fw = of_pow(1.0f - fmaxf(0.0f, wo_m), 5.0f);
+    V3 F = f0 + fw * (V3{1.0f, 1.0f, 1.0f} - f0);
+    *pdf_out = g1 * D / (4.0f * wo.z);
+    *mz_out = m.z;
+    *fw_out = fw;
+    return (D * g2 / (4.0f * wo.z)) * F;
+}
+
+/* Derivative with respect to alpha of D(m) * G2(wo, wi), in double precision,
+ * by the product rule: dD/da = D (2/a - 4 a c^2 / (c^2 (a^2 - 1) + 1)),
+ * dG2/da = -G2^2 (dL(wo)/da + dL(wi)/da), dL/da = a t^2 / (2 sqrt(1 + a^2 t^2)). */
+void ggx_dg_dalpha(double alpha, double mz, double cos_o, double cos_i, double *dg_out, double *dgd_out) {
+    double c2 = mz * mz;
+    double den = c2 * (alpha * alpha - 1.0) + 1.0;
+    double D = alpha * alpha / (3.141592653589793 * den * den);
+    double dD = D * (2.0 / alpha - 4.0 * alpha * c2 / den);
+    auto lam = [&](double c, double *dl) {
+        double cc = c * c;
+        double t2 = std::max(0.0, 1.0 - cc) / std::max(cc, 1e-12);
+        double s = std::sqrt(1.0 + alpha * alpha * t2);
+        *dl = 0.5 * alpha * t2 / s;
+        return 0.5 * (-1.0 + s);
+    };
+    double dlo, dli;
+    double lo = lam(cos_o, &dlo), li = lam(cos_i, &dli);
+    double G2 = 1.0 / (1.0 + lo + li);
+    double dG2 = -G2 * G2 * (dlo + dli);
+    *dg_out = dD * G2 + D * dG2;   /* d(D G2)/da */
+    *dgd_out = D * G2;
+}
+
+/* ------------------------------------------------------------------ next-event estimation
+ * An extension of the reference, which reaches emitters only by hitting them.
+ * The light list holds the emissive triangles (original ids, ascending) and then
+ * the emissive spheres (ordered slots).  A light is picked with probability
+ * proportional to area * luminance(emission) from a CDF summed in a fixed order:
+ * 1024 contiguous chunks, then a sequential scan of the chunk sums.  Emitters
+ * reached by BSDF sampling are weighted by the power heuristic.  The kernels do
+ * exactly this, so renders with NEE are compared bit for bit. */
+struct Lights {
+    std::vector<uint32_t> codes;     /* triangle original id, or ORC_HIT_SPHERE | ordered sphere slot */
+    std::vector<float> cdf;          /* n + 1 entries */
+    std::vector<uint32_t> slot_of;   /* original triangle id -> ordered slot */
+    float total = 0.0f;
+    uint32_t n = 0;
+};
+inline float luminance(V3 c) { return (0.2126f * c.x + 0.7152f * c.y) + 0.0722f * c.z; }
+inline bool is_emissive(const orc_scene *sc, uint32_t mat) {
+    return sc->materials->materials[std::min(mat & 0x7fffffffu, MAX_MAT_IDX)].type_pad[0] == MAT_EMISSIVE;
+}
+inline V3 emission_of(const orc_scene *sc, uint32_t mat) {
+    const orc_material &m = sc->materials->materials[std::min(mat, MAX_MAT_IDX)];
+    if (m.type_pad[0] != MAT_EMISSIVE) return {0.0f, 0.0f, 0.0f};
+    return m.ior_pad[0] * ld3(m.albedo_fuzz);
+}
+inline void tri_positions(const orc_scene *sc, const orc_triangle &tri, V3 *a, V3 *b, V3 *c) {
+    *a = ld3(sc->vertices[tri.v[0]].position);
+    *b = ld3(sc->vertices[tri.v[1]].position);
+    *c = ld3(sc->vertices[tri.v[2]].position);
+}
+float light_weight(const orc_scene *sc, const Lights &L, uint32_t code) {
+    if (code & ORC_HIT_SPHERE) {
+        const orc_sphere &s = sc->spheres[code & ~ORC_HIT_SPHERE];
+        float r = s.center_r[3];
+        return ((4.0f * PI_F) * (r * r)) * luminance(emission_of(sc, s.mat_and_pad[0]));
+    }
+    const orc_triangle &tri = sc->triangles[L.slot_of[code]];
+    V3 a, b, c;
+    tri_positions(sc, tri, &a, &b, &c);
+    V3 ng = cross(b - a, c - a);
+    return (0.5f * sqrtf(dot(ng, ng))) * luminance(emission_of(sc, tri.mat_idx & 0x7fffffffu));
+}
+void make_lights(const orc_scene *sc, Lights &L) {
+    L.slot_of.assign(sc->n_triangles, 0u);
+    std::vector<uint32_t> tris;
+    for (uint32_t s = 0; s < sc->n_triangles; ++s) {
+        uint32_t id = sc->triangle_ids ? sc->triangle_ids[s] : s;
+        L.slot_of[id] = s;
+        if (is_emissive(sc, sc->triangles[s].mat_idx)) tris.push_back(id);
+    }
+    std::sort(tris.begin(), tris.end());
+    L.codes = tris;
+    for (uint32_t s = 0; s < sc->n_spheres; ++s)
+        if (is_emissive(sc, sc->spheres[s].mat_and_pad[0])) L.codes.push_back(s | ORC_HIT_SPHERE);
+    const uint32_t n = (uint32_t)L.codes.size();
+    L.n = n;
+    L.cdf.assign(n + 1, 0.0f);
+    if (n == 0) return;
+    const uint32_t chunk = (n + 1023) / 1024;
+    std::vector<float> part(1024, 0.0f);
+    for (uint32_t t = 0; t < 1024; ++t) {
+        float local = 0.0f;
+        for (uint32_t k = t * chunk; k < std::min(t * chunk + chunk, n); ++k) local += light_weight(sc, L, L.codes[k]);
+        part[t] = local;
+    }
+    float run = 0.0f;
+    for (uint32_t k = 0; k < 1024; ++k) { float v = part[k]; part[k] = run; run += v; }
+    const float total = run;
+    for (uint32_t t = 0; t < 1024; ++t) {
+        float r = part[t];
+        for (uint32_t k = t * chunk; k < std::min(t * chunk + chunk, n); ++k) {
+            L.cdf[k] = total > 0.0f ? r / total : 0.0f;
+            r += light_weight(sc, L, L.codes[k]);
+        }
+    }
+    L.cdf[0] = 0.0f;
+    L.cdf[n] = 1.0f;
+    L.total = total;
+    if (!(total > 0.0f)) L.n = 0;
+}
+inline uint32_t pick_light(const Lights &L, float u) {       /* largest k with cdf[k] <= u */
+    uint32_t lo = 0, hi = L.n;
+    while (lo + 1 < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (L.cdf[mid] <= u) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+struct LightSample { V3 dir; float dist; float pdf; V3 Le; uint32_t mat; bool ok; };
+/* A uniform point on an emissive triangle, or a direction in the cone of an
+ * emissive sphere; pdf per unit solid angle at x, including the light choice. */
+LightSample sample_light(const orc_scene *sc, const Lights &L, V3 x, uint32_t &rng) {
+    LightSample ls{};
+    ls.ok = false;
+    uint32_t code = L.codes[pick_light(L, rand_f32(rng))];
+    float prob = light_weight(sc, L, code) / L.total;
+    float r1 = rand_f32(rng), r2 = rand_f32(rng);
+    if (!(prob > 0.0f)) return ls;
+    if (code & ORC_HIT_SPHERE) {
+        const orc_sphere &s = sc->spheres[code & ~ORC_HIT_SPHERE];
+        V3 wc = ld3(s.center_r) - x;
+        float d2 = dot(wc, wc);
+        float r2s = s.center_r[3] * s.center_r[3];
+        if (d2 <= r2s) return ls;
+        float dc = sqrtf(d2);
+        V3 w = wc / dc;
+        float cosmax = sqrtf(fmaxf(0.0f, 1.0f - r2s / d2));
+        if (!(cosmax < 1.0f)) return ls;
+        float cos_t = (1.0f - r1) + r1 * cosmax;
+        float sin_t = sqrtf(fmaxf(0.0f, 1.0f - cos_t * cos_t));
+        float sp, cp;
+        of_sincos(TAU * r2, &sp, &cp);
+        V3 t, b;
+        onb(w, &t, &b);
+        V3 dir = normalize(((sin_t * cp) * t + (sin_t * sp) * b) + cos_t * w);
+        float proj = dot(wc, dir);
+        float disc = r2s - (d2 - proj * proj);
+        float dist = proj - sqrtf(fmaxf(0.0f, disc));
+        ls.dir = dir;
+        ls.dist = dist;
+        ls.pdf = prob / (TAU * (1.0f - cosmax));
+        ls.mat = std::min(s.mat_and_pad[0], MAX_MAT_IDX);
+        ls.Le = emission_of(sc, s.mat_and_pad[0]);
+        ls.ok = dist > 0.0f;
+        return ls;
+    }
+    const orc_triangle &tri = sc->triangles[L.slot_of[code]];
+    V3 a, bq, cq;
+    tri_positions(sc, tri, &a, &bq, &cq);
+    float su = sqrtf(r1);
+    float b0 = 1.0f - su, b1 = r2 * su, b2 = (1.0f - b0) - b1;
+    V3 y = (b0 * a + b1 * bq) + b2 * cq;
+    V3 ng = cross(bq - a, cq - a);
+    float area2 = sqrtf(dot(ng, ng));
+    if (!(area2 > 0.0f)) return ls;
+    V3 wv = y - x;
+    float dist2 = dot(wv, wv);
+    float dist = sqrtf(dist2);
+    if (!(dist > 0.0f)) return ls;
+    V3 dir = wv / dist;
+    float cos_l = fabsf(dot(ng, dir)) / area2;
+    if (!(cos_l > 1e-7f)) return ls;
+    if (tri.mat_idx & 0x80000000u) {                  /* invisible from behind (path_trace.wgsl:452) */
+        V3 ns = tri_normal(sc, tri, b1, b2);
+        if (!(dot(dir, ns) < 0.0f)) return ls;
+    }
+    ls.dir = dir;
+    ls.dist = dist;
+    ls.pdf = prob * dist2 / (cos_l * (0.5f * area2));
+    ls.mat = std::min(tri.mat_idx & 0x7fffffffu, MAX_MAT_IDX);
+    ls.Le = emission_of(sc, tri.mat_idx & 0x7fffffffu);
+    ls.ok = true;
+    return ls;
+}
+/* Solid-angle pdf at o with which sample_light produces the emitter hit c along d. */
+float light_pdf_of_hit(const orc_scene *sc, const Lights &L, const Closest &c, V3 o, V3 d) {
+    if (c.prim & ORC_HIT_SPHERE) {
+        float prob = light_weight(sc, L, c.slot | ORC_HIT_SPHERE) / L.total;
+        const orc_sphere &s = sc->spheres[c.slot];
+        V3 wc = ld3(s.center_r) - o;
+        float d2 = dot(wc, wc);
+        float r2s = s.center_r[3] * s.center_r[3];
+        if (d2 <= r2s) return 0.0f;
+        float cosmax = sqrtf(fmaxf(0.0f, 1.0f - r2s / d2));
+        if (!(cosmax < 1.0f)) return 0.0f;
+        return prob / (TAU * (1.0f - cosmax));
+    }
+    float prob = light_weight(sc, L, c.prim) / L.total;
+    V3 a, bq, cq;
+    tri_positions(sc, sc->triangles[c.slot], &a, &bq, &cq);
+    V3 ng = cross(bq - a, cq - a);
+    float area2 = sqrtf(dot(ng, ng));
+    if (!(area2 > 0.0f)) return 0.0f;
+    float cos_l = fabsf(dot(ng, d)) / area2;
+    if (!(cos_l > 1e-7f)) return 0.0f;
+    return prob * (c.t * c.t) / (cos_l * (0.5f * area2));
+}
+
+/* Texture factor of a material at a hit: material_albedo = factor * albedo. */
+V3 material_tex(const orc_scene *sc, const orc_material &m, const Closest &c, V3 p) {
+    uint32_t layer = m.type_pad[1];
+    if (layer == 0u || sc->albedo_layers == 0u || !sc->albedo_rgba8) return {1.0f, 1.0f, 1.0f};
+    float u, v;
+    hit_uv(sc, c, p, &u, &v);
+    return sample_albedo(sc, std::min(layer, sc->albedo_layers - 1u), u, v);
+}
+
+/* Forward-mode derivatives of one path's radiance with respect to the material
+ * parameters (4 per material slot: albedo r, g, b and roughness), carried in
+ * double precision alongside the float path: dthr = d(throughput)/dparam,
+ * dL = d(radiance)/dparam.  This is the brute-force counterpart of the
+ * kernels' path-replay adjoint: same estimator (BSDF sampling, light choice and
+ * MIS weights held fixed), derivatives propagated forward instead of replayed
+ * backward. */
+struct Deriv {
+    uint32_t np = 0;
+    std::vector<double> dthr, dL;   /* np x 3 */
+};
+
+/* path_color, path_trace.wgsl:583-620 (+ G-buffer :592-602).
+ * stats (optional): [0] rays traced, [1] nodes visited, [2] primitives tested.
+ * lights: next-event estimation with MIS when non-null.  D: derivatives when non-null. */
+V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, float *gbuf, uint64_t *stats,
+              const Lights *lights, Deriv *D) {
+    const bool nee = lights && lights->n > 0;
     V3 thr = {1.0f, 1.0f, 1.0f};
+    V3 Lacc = {0.0f, 0.0f, 0.0f};
+    float prev_pdf = -1.0f;
     bool first = true;
+    const uint32_t np = D ? D->np : 0;
+    if (D) {
+        std::fill(D->dthr.begin(), D->dthr.end(), 0.0);
+        std::fill(D->dL.begin(), D->dL.end(), 0.0);
+    }
+    auto dthr = [&](uint32_t p, int c) -> double & { return D->dthr[3 * p + c]; };
+    auto dL = [&](uint32_t p, int c) -> double & { return D->dL[3 * p + c]; };
+    auto comp = [](V3 v, int c) { return c == 0 ? v.x : (c == 1 ? v.y : v.z); };
     for (uint32_t bounce = 0; bounce < max_depth; ++bounce) {
         uint32_t nv = 0, pt = 0;
         Closest c = world_hit(sc, ray, T_MIN, T_MAX, &nv, &pt);
         if (stats) { stats[0] += 1; stats[1] += nv; stats[2] += pt; }
         if (c.t < 0.0f) {
             if (first && gbuf) { gbuf[0] = 0; gbuf[1] = 0; gbuf[2] = 0; gbuf[3] = T_MAX; }
-            return thr * sample_env(sc, ray.d);
+            V3 e = thr * sample_env(sc, ray.d);
+            if (D)
+                for (uint32_t p = 0; p < np; ++p)
+                    for (int k = 0; k < 3; ++k) dL(p, k) += dthr(p, k) * (double)comp(sample_env(sc, ray.d), k);
+            return nee ? Lacc + e : e;
         }
         HitRec h = make_hitrec(sc, ray, c);
         if (first) {
@@ -474,22 +734,91 @@ V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, f
         uint32_t mi = std::min(h.mat, MAX_MAT_IDX);
         const orc_material &m = sc->materials->materials[mi];
         V3 albedo = ld3(m.albedo_fuzz);
-        if (m.type_pad[0] == MAT_EMISSIVE)                                     /* :608-610 */
-            return m.ior_pad[0] * (thr * albedo);
+        if (m.type_pad[0] == MAT_EMISSIVE) {                                   /* :608-610 */
+            V3 e = m.ior_pad[0] * (thr * albedo);
+            float wmis = 1.0f;
+            if (nee && prev_pdf > 0.0f) {
+                float pl = light_pdf_of_hit(sc, *lights, c, ray.o, ray.d);
+                wmis = (prev_pdf * prev_pdf) / (prev_pdf * prev_pdf + pl * pl);
+            }
+            if (D) {
+                const double s = (double)wmis * (double)m.ior_pad[0];
+                for (uint32_t p = 0; p < np; ++p)
+                    for (int k = 0; k < 3; ++k) dL(p, k) += s * (double)comp(albedo, k) * dthr(p, k);
+                if (4 * mi + 3 < np)
+                    for (int k = 0; k < 3; ++k) dL(4 * mi + k, k) += s * (double)comp(thr, k);
+            }
+            return nee ? Lacc + wmis * e : e;
+        }
         albedo = material_albedo(sc, m, c, h.p);                               /* :506-515 */
-        V3 dir, atten;
+        const V3 tex = D ? material_tex(sc, m, c, h.p) : V3{1.0f, 1.0f, 1.0f};
+        const bool own = D && 4 * mi + 3 < np;
+        V3 dir = {0, 0, 0}, atten = {0, 0, 0};
         bool absorbed = false;
+        float pdf = -1.0f;
+        /* local derivatives of this vertex's throughput factor: d atten_k / d param */
+        double datt_alb[3] = {0, 0, 0}, datt_rough[3] = {0, 0, 0};
+        bool have_shadow = false;
+        V3 sc_c = {0, 0, 0}, sh_o = {0, 0, 0}, sh_d = {0, 0, 0};
+        float sh_max = 0.0f;
+        double dsc_alb[3] = {0, 0, 0}, dsc_rough[3] = {0, 0, 0}, dsc_light[3] = {0, 0, 0}, sc_scale = 0.0;
+        V3 sc_f = {0, 0, 0};   /* the per-channel factor multiplying thr in the NEE term */
+        uint32_t sc_lmat = 0;
         if (m.type_pad[0] == MAT_GGX) {
             V3 t, b;
             onb(h.n, &t, &b);
             V3 wo = {-dot(ray.d, t), -dot(ray.d, b), -dot(ray.d, h.n)};
             float rough = m.albedo_fuzz[3];
             float alpha = fmaxf(rough * rough, 1e-4f);
+            const double dadr = rough * rough > 1e-4f ? 2.0 * (double)rough : 0.0;
             float r1 = rand_f32(rng), r2 = rand_f32(rng);
-            V3 wi, wgt;
-            if (wo.z > 0.0f && ggx_sample(wo, alpha, albedo, r1, r2, &wi, &wgt)) {
-                dir = normalize((wi.x * t + wi.y * b) + wi.z * h.n);
-                atten = wgt;
+            GgxSample gs;
+            if (wo.z > 0.0f && ggx_sample(wo, alpha, albedo, r1, r2, &gs)) {
+                dir = normalize((gs.wi.x * t + gs.wi.y * b) + gs.wi.z * h.n);
+                atten = gs.weight;
+                pdf = gs.pdf;
+                if (own) {
+                    double dg, dgd;
+                    ggx_dg_dalpha(alpha, gs.mz, wo.z, gs.wi.z, &dg, &dgd);
+                    for (int k = 0; k < 3; ++k) {
+                        double f0 = comp(albedo, k);
+                        double F = f0 + (double)gs.fw * (1.0 - f0);
+                        /* weight = D G2 F / (4 cos_o) / pdf, the sampling pdf held fixed */
+                        datt_alb[k] = (dgd * 0.25 / (double)wo.z) / (double)gs.pdf * (1.0 - gs.fw) * comp(tex, k);
+                        datt_rough[k] = F * dg * 0.25 / (double)wo.z / (double)gs.pdf * dadr;
+                    }
+                }
+                if (nee) {
+                    LightSample ls = sample_light(sc, *lights, h.p, rng);
+                    if (ls.ok) {
+                        V3 wl = {dot(ls.dir, t), dot(ls.dir, b), dot(ls.dir, h.n)};
+                        float bp, mz, fw;
+                        V3 fc = ggx_eval(wo, wl, alpha, albedo, &bp, &mz, &fw);
+                        if (wl.z > 0.0f && (fc.x > 0.0f || fc.y > 0.0f || fc.z > 0.0f)) {
+                            float wmis = (ls.pdf * ls.pdf) / (ls.pdf * ls.pdf + bp * bp);
+                            sc_c = (wmis / ls.pdf) * (thr * (fc * ls.Le));
+                            sh_o = h.p; sh_d = ls.dir; sh_max = ls.dist * (1.0f - 1e-4f);
+                            have_shadow = true;
+                            if (D) {
+                                sc_scale = (double)(wmis / ls.pdf);
+                                sc_f = fc * ls.Le;
+                                sc_lmat = ls.mat;
+                                double dg, dgd;
+                                ggx_dg_dalpha(alpha, mz, wo.z, wl.z, &dg, &dgd);
+                                const orc_material &lm = sc->materials->materials[ls.mat];
+                                for (int k = 0; k < 3; ++k) {
+                                    double f0 = comp(albedo, k);
+                                    double F = f0 + (double)fw * (1.0 - f0);
+                                    dsc_alb[k] = sc_scale * comp(thr, k) * comp(ls.Le, k) *
+                                                 (dgd * 0.25 / (double)wo.z) * (1.0 - fw) * comp(tex, k);
+                                    dsc_rough[k] = sc_scale * comp(thr, k) * comp(ls.Le, k) * F * dg * 0.25 /
+                                                   (double)wo.z * dadr;
+                                    dsc_light[k] = sc_scale * comp(thr, k) * comp(fc, k) * (double)lm.ior_pad[0];
+                                }
+                            }
+                        }
+                    }
+                }
             } else {
                 absorbed = true;
             }
@@ -500,6 +829,7 @@ V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, f
             dir = normalize(dot(pert, pert) >= 1e-6f ? pert : refl);
             atten = albedo;
             absorbed = dot(dir, h.n) <= 0.0f;
+            for (int k = 0; k < 3; ++k) datt_alb[k] = comp(tex, k);
         } else if (m.type_pad[0] == MAT_DIELECTRIC) {                          /* :543-564 */
             atten = {1.0f, 1.0f, 1.0f};
             float ior = m.ior_pad[0];
@@ -516,14 +846,65 @@ V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, f
             else
                 dir = normalize(refract_vec(ray.d, h.n, eta));
         } else {                                                               /* :521-528 */
+            if (nee) {
+                LightSample ls = sample_light(sc, *lights, h.p, rng);
+                float cs = dot(ls.dir, h.n);
+                if (ls.ok && cs > 0.0f) {
+                    float bp = cs / PI_F;
+                    float wmis = (ls.pdf * ls.pdf) / (ls.pdf * ls.pdf + bp * bp);
+                    sc_c = (wmis * bp / ls.pdf) * (thr * (albedo * ls.Le));
+                    sh_o = h.p; sh_d = ls.dir; sh_max = ls.dist * (1.0f - 1e-4f);
+                    have_shadow = true;
+                    if (D) {
+                        sc_scale = (double)(wmis * bp / ls.pdf);
+                        sc_f = albedo * ls.Le;
+                        sc_lmat = ls.mat;
+                        const orc_material &lm = sc->materials->materials[ls.mat];
+                        for (int k = 0; k < 3; ++k) {
+                            dsc_alb[k] = sc_scale * comp(thr, k) * comp(tex, k) * comp(ls.Le, k);
+                            dsc_light[k] = sc_scale * comp(thr, k) * comp(albedo, k) * (double)lm.ior_pad[0];
+                        }
+                    }
+                }
+            }
             dir = cosine_scatter(rng, h.n);
             atten = albedo;
+            pdf = fmaxf(dot(dir, h.n), 0.0f) / PI_F;
+            for (int k = 0; k < 3; ++k) datt_alb[k] = comp(tex, k);
         }
-        if (absorbed) return {0.0f, 0.0f, 0.0f};
+        if (have_shadow) {
+            uint32_t snv = 0, spt = 0;
+            Closest occ = world_hit(sc, Ray{sh_o, sh_d}, T_MIN, sh_max, &snv, &spt);
+            if (occ.prim == ORC_HIT_MISS) {
+                Lacc = Lacc + sc_c;
+                if (D) {
+                    for (uint32_t p = 0; p < np; ++p)
+                        for (int k = 0; k < 3; ++k) dL(p, k) += sc_scale * dthr(p, k) * (double)comp(sc_f, k);
+                    if (own)
+                        for (int k = 0; k < 3; ++k) {
+                            dL(4 * mi + k, k) += dsc_alb[k];
+                            dL(4 * mi + 3, k) += dsc_rough[k];
+                        }
+                    if (4 * sc_lmat + 3 < np)
+                        for (int k = 0; k < 3; ++k) dL(4 * sc_lmat + k, k) += dsc_light[k];
+                }
+            }
+        }
+        if (absorbed) return Lacc;
+        if (D) {
+            for (uint32_t p = 0; p < np; ++p)
+                for (int k = 0; k < 3; ++k) dthr(p, k) *= (double)comp(atten, k);
+            if (own)
+                for (int k = 0; k < 3; ++k) {
+                    dthr(4 * mi + k, k) += (double)comp(thr, k) * datt_alb[k];
+                    dthr(4 * mi + 3, k) += (double)comp(thr, k) * datt_rough[k];
+                }
+        }
         thr = thr * atten;
+        prev_pdf = pdf;
         ray = {h.p, dir};
     }
-    return {0.0f, 0.0f, 0.0f};
+    return Lacc;
 }
 
 /* cs_main raygen, path_trace.wgsl:626-652 */
@@ -728,11 +1109,16 @@ void orc_trace(const orc_scene *sc, const orc_ray *rays, uint32_t n, orc_hit *hi
     }
 }
 
-void orc_render_rect_stats(const orc_scene *sc, const orc_camera *cam, uint32_t w, uint32_t h,
-                           uint32_t x0, uint32_t y0, uint32_t cw, uint32_t ch, uint32_t spp, uint32_t first_frame,
-                           uint32_t max_depth, float *out_mean, double *out_sum, float *out_gbuf, int threads,
-                           uint64_t *out_stats) {
+void orc_render_ex(const orc_scene *sc, const orc_camera *cam, uint32_t w, uint32_t h, uint32_t x0, uint32_t y0,
+                   uint32_t cw, uint32_t ch, uint32_t spp, uint32_t first_frame, uint32_t max_depth, uint32_t flags,
+                   float *out_mean, double *out_sum, float *out_gbuf, int threads, uint64_t *out_stats) {
     int64_t npx = (int64_t)cw * ch;
+    Lights lights;
+    const Lights *lp = nullptr;
+    if (flags & ORC_RENDER_NEE) {
+        make_lights(sc, lights);
+        lp = &lights;
+    }
     uint64_t tot[3] = {0, 0, 0};
 #pragma omp parallel num_threads(n_threads(threads))
     {
@@ -749,7 +1135,7 @@ void orc_render_rect_stats(const orc_scene *sc, const orc_camera *cam, uint32_t 
             uint32_t frame = first_frame + k;
             uint32_t rng = pcg_hash(pcg_hash(x + y * w) ^ (frame * 2654435761u));   /* :636-637 */
             Ray r = camera_ray(cam, x, y, w, h, rng);
-            V3 s = path_color(sc, r, rng, max_depth, g, st);
+            V3 s = path_color(sc, r, rng, max_depth, g, st, lp, nullptr);
             float wgt = 1.0f / (float)(std::min(frame, MAX_FRAME_COUNT) + 1u);      /* :657 */
             float omw = 1.0f - wgt;
             mean[0] = mean[0] * omw + s.x * wgt;                                     /* :659 mix */
@@ -770,6 +1156,63 @@ void orc_render_rect_stats(const orc_scene *sc, const orc_camera *cam, uint32_t 
     }
     }
     if (out_stats) for (int k = 0; k < 3; ++k) out_stats[k] = tot[k];
+}
+
+void orc_render_rect_stats(const orc_scene *sc, const orc_camera *cam, uint32_t w, uint32_t h,
+                           uint32_t x0, uint32_t y0, uint32_t cw, uint32_t ch, uint32_t spp, uint32_t first_frame,
+                           uint32_t max_depth, float *out_mean, double *out_sum, float *out_gbuf, int threads,
+                           uint64_t *out_stats) {
+    orc_render_ex(sc, cam, w, h, x0, y0, cw, ch, spp, first_frame, max_depth, 0u, out_mean, out_sum, out_gbuf,
+                  threads, out_stats);
+}
+
+void orc_adjoint(const orc_scene *sc, const orc_camera *cam, uint32_t w, uint32_t h, uint32_t spp,
+                 uint32_t first_frame, uint32_t max_depth, uint32_t flags, const float *d_image, double *grad,
+                 double *out_sum, int threads) {
+    Lights lights;
+    const Lights *lp = nullptr;
+    if (flags & ORC_RENDER_NEE) {
+        make_lights(sc, lights);
+        lp = &lights;
+    }
+    /* parameters of the material slots the scene references */
+    uint32_t nmat = 0;
+    for (uint32_t s = 0; s < sc->n_triangles; ++s)
+        nmat = std::max(nmat, std::min(sc->triangles[s].mat_idx & 0x7fffffffu, MAX_MAT_IDX) + 1u);
+    for (uint32_t s = 0; s < sc->n_spheres; ++s)
+        nmat = std::max(nmat, std::min(sc->spheres[s].mat_and_pad[0], MAX_MAT_IDX) + 1u);
+    const uint32_t np = 4 * nmat;
+    std::vector<double> total(4 * 64, 0.0);
+    const int64_t npx = (int64_t)w * h;
+    const double inv_spp = 1.0 / (double)spp;
+#pragma omp parallel num_threads(n_threads(threads))
+    {
+        Deriv D;
+        D.np = np;
+        D.dthr.assign(3 * (size_t)np, 0.0);
+        D.dL.assign(3 * (size_t)np, 0.0);
+        std::vector<double> loc(4 * 64, 0.0);
+#pragma omp for schedule(dynamic, 16)
+        for (int64_t i = 0; i < npx; ++i) {
+            uint32_t x = (uint32_t)(i % w), y = (uint32_t)(i / w);
+            const double dx = d_image[4 * i] * inv_spp, dy = d_image[4 * i + 1] * inv_spp,
+                         dz = d_image[4 * i + 2] * inv_spp;
+            double sum[3] = {0, 0, 0};
+            for (uint32_t k = 0; k < spp; ++k) {
+                uint32_t frame = first_frame + k;
+                uint32_t rng = pcg_hash(pcg_hash(x + y * w) ^ (frame * 2654435761u));
+                Ray r = camera_ray(cam, x, y, w, h, rng);
+                V3 s = path_color(sc, r, rng, max_depth, nullptr, nullptr, lp, &D);
+                sum[0] += (double)s.x; sum[1] += (double)s.y; sum[2] += (double)s.z;
+                for (uint32_t p = 0; p < np; ++p)
+                    loc[p] += (dx * D.dL[3 * p] + dy * D.dL[3 * p + 1]) + dz * D.dL[3 * p + 2];
+            }
+            if (out_sum) { out_sum[3 * i] += sum[0]; out_sum[3 * i + 1] += sum[1]; out_sum[3 * i + 2] += sum[2]; }
+        }
+#pragma omp critical
+        for (uint32_t p = 0; p < np; ++p) total[p] += loc[p];
+    }
+    for (int p = 0; p < 4 * 64; ++p) grad[p] = total[p];
 }
 
 void orc_render_rect(const orc_scene *sc, const orc_camera *cam, uint32_t w, uint32_t h, uint32_t x0, uint32_t y0,
@@ -857,6 +1300,10 @@ void orc_compare_images(const uint8_t *a, const uint8_t *b, uint32_t w, uint32_t
     out[0] = mse;
     out[1] = mse == 0.0 ? INFINITY : 10.0 * std::log10(1.0 / mse);
     out[2] = mx;
+}
+
+void orc_ggx_dg(double alpha, double mz, double cos_o, double cos_i, double *out) {
+    ggx_dg_dalpha(alpha, mz, cos_o, cos_i, &out[0], &out[1]);
 }
 
 void orc_math_eval(int fn, const float *x, const float *y, float *out, uint32_t n) {

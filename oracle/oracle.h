@@ -88,6 +88,27 @@ void orc_render_rect_stats(const orc_scene *scene, const orc_camera *cam, uint32
                            uint32_t max_depth, float *out_mean_rgba, double *out_sum_rgb, float *out_gbuf,
                            int threads, uint64_t *out_stats);
 
+/* orc_render_rect_stats with render flags: ORC_RENDER_NEE adds next-event
+ * estimation with power-heuristic MIS (an extension of the reference, which
+ * has none), in the same order of operations as the kernels. */
+#define ORC_RENDER_NEE 1u
+void orc_render_ex(const orc_scene *scene, const orc_camera *cam, uint32_t w, uint32_t h,
+                   uint32_t x0, uint32_t y0, uint32_t cw, uint32_t ch, uint32_t spp, uint32_t first_frame,
+                   uint32_t max_depth, uint32_t flags, float *out_mean_rgba, double *out_sum_rgb, float *out_gbuf,
+                   int threads, uint64_t *out_stats);
+
+/* Brute-force gradient of an image loss with respect to the material
+ * parameters, by forward-mode differentiation of every sampled path:
+ *   grad[4*m + k] = sum_pixels sum_c d_image[pixel].c / spp * d(sample mean).c / d(param m,k)
+ * with params (albedo r, albedo g, albedo b, roughness) of material slot m
+ * (for emissive slots the albedo is the radiance colour, radiance = strength *
+ * albedo).  BSDF sampling, light choice and MIS weights are held fixed
+ * (detached sampling).  d_image: w*h RGBA floats (alpha ignored); grad: 256
+ * doubles (out); out_sum_rgb: optional += f64 sums as orc_render. */
+void orc_adjoint(const orc_scene *scene, const orc_camera *cam, uint32_t w, uint32_t h, uint32_t spp,
+                 uint32_t first_frame, uint32_t max_depth, uint32_t flags, const float *d_image, double *grad,
+                 double *out_sum_rgb, int threads);
+
 /* cs_denoise (denoise.wgsl:52-120). */
 void orc_denoise(const float *accum_rgba, const float *gbuf, uint32_t w, uint32_t h,
                  int radius, float sigma_s, float sigma_d, float normal_pow, float *out_rgba);
@@ -97,6 +118,10 @@ void orc_tonemap_rgba8(const float *rgba, uint32_t n_pixels, uint8_t *out);
 
 /* regression.rs:120-181 on RGBA8 images: out[0]=mse, out[1]=psnr, out[2]=max_delta. */
 void orc_compare_images(const uint8_t *a, const uint8_t *b, uint32_t w, uint32_t h, double *out);
+
+/* out[0] = d(D(m) G2(wo, wi))/d alpha and out[1] = D G2 of the GGX lobe (the
+ * derivative the brute-force gradient uses; exposed for its finite-difference test). */
+void orc_ggx_dg(double alpha, double mz, double cos_o, double cos_i, double *out);
 
 /* Elementary functions (exposed for their error-bound tests). */
 void orc_math_eval(int fn, const float *x, const float *y, float *out, uint32_t n);

@@ -26,6 +26,7 @@ VERTEX = np.dtype([("position", "<f4", 4), ("normal", "<f4", 4), ("uv", "<f4", 4
 TRIANGLE = np.dtype([("v", "<u4", 3), ("mat_idx", "<u4")])
 RAY = np.dtype([("org", "<f4", 3), ("tmin", "<f4"), ("dir", "<f4", 3), ("tmax", "<f4")])
 HIT = np.dtype([("t", "<f4"), ("prim", "<u4"), ("u", "<f4"), ("v", "<f4")])
+NEE = 1   # ORC_RENDER_NEE
 
 
 class _Scene(ctypes.Structure):
@@ -84,6 +85,13 @@ def lib():
         L.orc_render_rect_stats.argtypes = [POINTER(_Scene), c_void_p, c_uint32, c_uint32, c_uint32, c_uint32,
                                             c_uint32, c_uint32, c_uint32, c_uint32, c_uint32, c_void_p, c_void_p,
                                             c_void_p, c_int, c_void_p]
+        L.orc_render_ex.restype = None
+        L.orc_render_ex.argtypes = [POINTER(_Scene), c_void_p, c_uint32, c_uint32, c_uint32, c_uint32, c_uint32,
+                                    c_uint32, c_uint32, c_uint32, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p,
+                                    c_int, c_void_p]
+        L.orc_adjoint.restype = None
+        L.orc_adjoint.argtypes = [POINTER(_Scene), c_void_p, c_uint32, c_uint32, c_uint32, c_uint32, c_uint32,
+                                  c_uint32, c_void_p, c_void_p, c_void_p, c_int]
         L.orc_denoise.restype = None
         L.orc_denoise.argtypes = [c_void_p, c_void_p, c_uint32, c_uint32, c_int, c_float, c_float, c_float, c_void_p]
         L.orc_tonemap_rgba8.restype = None
@@ -161,19 +169,30 @@ class OracleScene:
                         threads)
         return (hits, st.reshape(-1, 2)) if stats else hits
 
-    def render(self, camera, w, h, spp, first_frame=0, max_depth=8, threads=0, rect=None, stats=False):
+    def render(self, camera, w, h, spp, first_frame=0, max_depth=8, threads=0, rect=None, stats=False, nee=False):
         cam = np.ascontiguousarray(camera)
         x0, y0, cw, ch = rect if rect else (0, 0, w, h)
         mean = np.zeros((ch, cw, 4), np.float32)
         acc = np.zeros((ch, cw, 3), np.float64)
         gbuf = np.zeros((ch, cw, 4), np.float32)
         st = np.zeros(3, np.uint64) if stats else None
-        lib().orc_render_rect_stats(ctypes.byref(self._s), _p(cam), w, h, x0, y0, cw, ch, spp, first_frame,
-                                    max_depth, _p(mean), _p(acc), _p(gbuf), threads, _p(st))
+        lib().orc_render_ex(ctypes.byref(self._s), _p(cam), w, h, x0, y0, cw, ch, spp, first_frame, max_depth,
+                            NEE if nee else 0, _p(mean), _p(acc), _p(gbuf), threads, _p(st))
         out = dict(rgba=mean, sum=acc, gbuf=gbuf)
         if stats:
             out["stats"] = dict(rays=int(st[0]), nodes=int(st[1]), prims=int(st[2]))
         return out
+
+    def adjoint(self, camera, w, h, spp, d_image, first_frame=0, max_depth=8, nee=False, threads=0):
+        """Brute-force (forward-mode) gradient of sum(d_image * image) with respect to
+        the 64 x 4 material parameters (albedo rgb, roughness); also returns the f64 sums."""
+        cam = np.ascontiguousarray(camera)
+        d = np.ascontiguousarray(d_image, np.float32).reshape(h, w, 4)
+        grad = np.zeros(256, np.float64)
+        acc = np.zeros((h, w, 3), np.float64)
+        lib().orc_adjoint(ctypes.byref(self._s), _p(cam), w, h, spp, first_frame, max_depth, NEE if nee else 0,
+                          _p(d), _p(grad), _p(acc), threads)
+        return grad.reshape(64, 4), acc
 
 
 def denoise(rgba, gbuf, radius=3, sigma_s=2.0, sigma_d=0.5, normal_pow=8.0):
@@ -211,6 +230,16 @@ def math_eval(fn, x, y=None):
     out = np.zeros_like(x)
     lib().orc_math_eval(MATH_FNS[fn], _p(x), _p(y), _p(out), x.size)
     return out
+
+
+def ggx_dg(alpha, mz, cos_o, cos_i):
+    """(d(D G2)/d alpha, D G2) of the GGX lobe."""
+    L = lib()
+    L.orc_ggx_dg.restype = None
+    L.orc_ggx_dg.argtypes = [c_double, c_double, c_double, c_double, c_void_p]
+    out = np.zeros(2, np.float64)
+    L.orc_ggx_dg(alpha, mz, cos_o, cos_i, _p(out))
+    return float(out[0]), float(out[1])
 
 
 def pcg_hash(v):
