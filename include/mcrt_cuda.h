@@ -133,8 +133,21 @@ typedef struct {
      * (gpu_layout.rs:435-477; 4 x 512 x 512 in the reference).  NULL: the
      * reference's default layers (mcrt_albedo_layers). */
     const uint8_t *albedo_rgba8; uint32_t albedo_layers; uint32_t albedo_size;
-    uint32_t flags; /* reserved, 0 */
+    uint32_t flags; /* MCRT_SCENE_* */
+    /* Directional light (an extension; the reference's sky is its environment
+     * map alone): direction towards the light (normalised here) and the
+     * irradiance it delivers at normal incidence (RGB).  All-zero irradiance:
+     * no directional light.  Sampled by next-event estimation only (a delta
+     * light: BSDF-sampled rays never reach it). */
+    float sun_dir[4];
+    float sun_irradiance[4];
 } mcrt_scene_desc;
+
+enum {
+    /* take the triangle mesh from the context's last mcrt_world_mesh
+     * (vertices / triangles must be NULL); the mesh BVH is built on the GPU */
+    MCRT_SCENE_WORLD_MESH = 1u << 0
+};
 
 /* Upload (or replace) the scene.  Replaces gpu_layout::build_scene_buffers
  * (gpu_layout.rs:259-390). */
@@ -229,6 +242,58 @@ mcrt_status mcrt_render(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t 
 mcrt_status mcrt_render_noalloc(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t w, uint32_t h, uint32_t spp,
                                 uint32_t first_frame, const mcrt_render_opts *opts, float *d_out_rgba);
 
+/* ------------------------------------------------------------------ voxel world */
+
+/* Seeded terrain generator (the reference's world/generator.rs:109-200 builds
+ * its chunks on the host from the noise crate's Perlin / SuperSimplex fBm; this
+ * generator is the project's own, on the GPU, with lattice value noise).
+ * Column rule: limestone with gravel patches, 3 blocks of red soil, a grass top
+ * (sand at and below sand_line), caves carved where the 3D fBm exceeds
+ * cave_threshold (y >= cave_min_y), cave-glow flora on some cave floors, water
+ * above the surface up to sea_level, shrubs on some grass tops — block ids of
+ * the reference's registry (world/block.rs:14-24). */
+typedef struct {
+    uint32_t nx, ny, nz;             /* voxels; nx, nz multiples of 16, 2 <= ny <= 1024 */
+    uint32_t seed;
+    int32_t chunk_x0, chunk_z0;      /* chunk coordinates of the grid's first chunk column */
+    float height_base, height_amp;   /* surface height = base + amp * (2 fbm - 1), in voxels */
+    float height_freq;               /* first-octave frequency, cycles per voxel */
+    uint32_t height_octaves;
+    float lacunarity, gain;
+    float cave_freq;
+    uint32_t cave_octaves;
+    float cave_threshold;
+    float cave_contrast;             /* cave value = 0.5 + (fbm - 0.5) * contrast */
+    uint32_t cave_min_y;
+    float sea_level, sand_line;      /* in voxels */
+} mcrt_world_params;
+
+/* Generate the voxel grid on the device (kept in the context).  out_voxels
+ * (optional, host, nx*ny*nz bytes): a copy, index (x*ny + y)*nz + z. */
+mcrt_status mcrt_world_generate(mcrt_ctx *ctx, const mcrt_world_params *params, uint8_t *out_voxels);
+
+/* Replace the context's voxel grid with a host one (same layout; block ids as
+ * world/block.rs: 1..10 opaque, 0 and others air). */
+mcrt_status mcrt_world_upload(mcrt_ctx *ctx, const uint8_t *voxels, uint32_t nx, uint32_t ny, uint32_t nz,
+                              int32_t chunk_x0, int32_t chunk_z0);
+
+enum { MCRT_MESH_GREEDY = 0, MCRT_MESH_FACES = 1 };
+
+/* Mesh the context's voxel grid on the GPU, 16 x ny x 16 chunk by chunk.
+ * MCRT_MESH_GREEDY restates mesh_chunk (world/mesher.rs:97-366) over every
+ * chunk of the grid with its neighbours, concatenated as merge_chunk_meshes
+ * (:377-400) in (chunk x outer, chunk z inner) order; MCRT_MESH_FACES emits one
+ * quad per visible face in the same order.  4 vertices and 2 triangles per
+ * quad; block_material[id] is the material slot of block id (256 entries);
+ * voxel_size is VOXEL_SIZE (chunk.rs:20, 0.125).  The mesh stays on the device
+ * (see MCRT_SCENE_WORLD_MESH and mcrt_world_read_mesh). */
+mcrt_status mcrt_world_mesh(mcrt_ctx *ctx, uint32_t mode, const uint32_t *block_material, float voxel_size,
+                            uint32_t *out_n_vertices, uint32_t *out_n_triangles);
+
+/* Copy the last world mesh to the host (capacities in elements). */
+mcrt_status mcrt_world_read_mesh(mcrt_ctx *ctx, mcrt_gpu_vertex *vertices, uint32_t vertex_capacity,
+                                 mcrt_gpu_triangle *triangles, uint32_t triangle_capacity);
+
 /* ------------------------------------------------------------------ differentiation */
 
 /* Replace the material table of the uploaded scene (GpuMaterialData,
@@ -300,6 +365,12 @@ typedef struct {
 /* cs_denoise (denoise.wgsl:52-120) over host images (w*h*4 floats each). */
 mcrt_status mcrt_denoise(mcrt_ctx *ctx, const float *in_rgba, const float *gbuf, uint32_t w, uint32_t h,
                          const mcrt_denoise_params *params, float *out_rgba);
+
+/* cs_denoise of the device accumulation of the last mcrt_render with its
+ * G-buffer (the reference's dispatch after the frame loop, gpu.rs:166-185), no
+ * host copies in between; out_rgba (optional, host w*h*4 floats) receives the
+ * result.  The filter's device time replaces timing [0] of mcrt_last_timings. */
+mcrt_status mcrt_denoise_accum(mcrt_ctx *ctx, const mcrt_denoise_params *params, float *out_rgba);
 
 /* ------------------------------------------------------------------ host-side scene API
  * (the reference's Scene/Material/Camera/YAML API, run on the CPU exactly as

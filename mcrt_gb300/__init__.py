@@ -189,6 +189,7 @@ class Context:
         self._h = c_void_p()
         check(lib().mcrt_create(device, c_void_p(stream) if stream else None, ctypes.byref(self._h)))
         self._keep = []
+        self._world_tris = 0
 
     def close(self):
         if self._h:
@@ -211,7 +212,10 @@ class Context:
         check(s, self._h)
 
     def upload_scene(self, *, materials, spheres=None, vertices=None, triangles=None, env=None, sphere_bvh=None,
-                     sphere_order=None, mesh_bvh=None, triangle_order=None, albedo=None):
+                     sphere_order=None, mesh_bvh=None, triangle_order=None, albedo=None, sun_dir=None,
+                     sun_irradiance=None, world_mesh=False):
+        """world_mesh: take the triangles from the last world_mesh() call (no host geometry).
+        sun_dir / sun_irradiance: a directional light sampled by next-event estimation."""
         sph = _arr(spheres, SPHERE)
         ver = _arr(vertices, VERTEX)
         tri = _arr(triangles, TRIANGLE)
@@ -238,8 +242,47 @@ class Context:
         alb = None if albedo is None else np.ascontiguousarray(albedo, np.uint8)
         if alb is not None:
             d.albedo_rgba8, d.albedo_layers, d.albedo_size = ptr(alb), alb.shape[0], alb.shape[1]
+        if sun_irradiance is not None:
+            for k in range(3):
+                d.sun_dir[k] = float(sun_dir[k])
+                d.sun_irradiance[k] = float(sun_irradiance[k])
+        if world_mesh:
+            d.flags |= N.SCENE_WORLD_MESH
         self._check(lib().mcrt_upload_scene(self._h, ctypes.byref(d)))
-        self.n_triangles = d.n_triangles
+        self.n_triangles = self._world_tris if world_mesh else d.n_triangles
+
+    # ---------------------------------------------------------------- voxel world
+    def world_generate(self, params, read_back=False):
+        """Generate the voxel grid on the GPU from a dict of mcrt_world_params fields;
+        returns the grid (nx, ny, nz) uint8 when read_back."""
+        p = N.WorldParams(**params)
+        vox = np.zeros((p.nx, p.ny, p.nz), np.uint8) if read_back else None
+        self._check(lib().mcrt_world_generate(self._h, ctypes.byref(p), ptr(vox)))
+        return vox
+
+    def world_upload(self, voxels, chunk_x0=0, chunk_z0=0):
+        v = np.ascontiguousarray(voxels, np.uint8)
+        nx, ny, nz = v.shape
+        self._check(lib().mcrt_world_upload(self._h, ptr(v), nx, ny, nz, chunk_x0, chunk_z0))
+
+    def world_mesh(self, block_material, voxel_size=0.125, greedy=True):
+        """Mesh the device voxel grid; returns (n_vertices, n_triangles)."""
+        mm = np.zeros(256, np.uint32)
+        bm = np.asarray(block_material, np.uint32).ravel()
+        mm[:len(bm)] = bm
+        nv, nt = c_uint32(), c_uint32()
+        self._check(lib().mcrt_world_mesh(self._h, N.MESH_GREEDY if greedy else N.MESH_FACES, ptr(mm),
+                                          float(voxel_size), ctypes.byref(nv), ctypes.byref(nt)))
+        self._world_tris = nt.value
+        return nv.value, nt.value
+
+    def world_read_mesh(self):
+        nt = self._world_tris
+        nv = 2 * nt
+        v = np.zeros(nv, VERTEX)
+        t = np.zeros(nt, TRIANGLE)
+        self._check(lib().mcrt_world_read_mesh(self._h, ptr(v), nv, ptr(t), nt))
+        return v, t
 
     def update_vertices(self, vertices):
         ver = _arr(vertices, VERTEX)
@@ -327,6 +370,16 @@ class Context:
         d["build_launches"] = cnt[3]
         d["extend_launches"] = cnt[4]
         return d
+
+    def denoise_accum(self, radius=3, sigma_s=2.0, sigma_d=0.5, normal_pow=8.0, sigma_color=0.0, sigma_normal=0.0,
+                      read_back=True):
+        """Denoise the device accumulation of the last render with its G-buffer."""
+        h, w = self._last_hw
+        p = N.DenoiseParams(radius=radius, sigma_s=sigma_s, sigma_d=sigma_d, normal_pow=normal_pow,
+                            sigma_color=sigma_color, sigma_normal=sigma_normal)
+        out = np.zeros((h, w, 4), np.float32) if read_back else None
+        self._check(lib().mcrt_denoise_accum(self._h, ctypes.byref(p), ptr(out)))
+        return out
 
     def denoise(self, rgba, gbuf, radius=3, sigma_s=2.0, sigma_d=0.5, normal_pow=8.0, sigma_color=0.0,
                 sigma_normal=0.0):

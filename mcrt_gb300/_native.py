@@ -62,7 +62,20 @@ class SceneDesc(ctypes.Structure):
                 ("materials", c_void_p),
                 ("env_rgba", c_void_p), ("env_w", c_uint32), ("env_h", c_uint32),
                 ("albedo_rgba8", c_void_p), ("albedo_layers", c_uint32), ("albedo_size", c_uint32),
-                ("flags", c_uint32)]
+                ("flags", c_uint32), ("sun_dir", c_float * 4), ("sun_irradiance", c_float * 4)]
+
+
+SCENE_WORLD_MESH = 1
+MESH_GREEDY, MESH_FACES = 0, 1
+
+
+class WorldParams(ctypes.Structure):
+    _fields_ = [("nx", c_uint32), ("ny", c_uint32), ("nz", c_uint32), ("seed", c_uint32),
+                ("chunk_x0", c_int32), ("chunk_z0", c_int32),
+                ("height_base", c_float), ("height_amp", c_float), ("height_freq", c_float),
+                ("height_octaves", c_uint32), ("lacunarity", c_float), ("gain", c_float),
+                ("cave_freq", c_float), ("cave_octaves", c_uint32), ("cave_threshold", c_float),
+                ("cave_contrast", c_float), ("cave_min_y", c_uint32), ("sea_level", c_float), ("sand_line", c_float)]
 
 
 class RenderOpts(ctypes.Structure):
@@ -104,6 +117,11 @@ SIGNATURES = [
                                     POINTER(RenderOpts), c_void_p]),
     ("mcrt_read_accum", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     ("mcrt_update_materials", c_int, [c_void_p, c_void_p]),
+    ("mcrt_denoise_accum", c_int, [c_void_p, POINTER(DenoiseParams), c_void_p]),
+    ("mcrt_world_generate", c_int, [c_void_p, POINTER(WorldParams), c_void_p]),
+    ("mcrt_world_upload", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_int32, c_int32]),
+    ("mcrt_world_mesh", c_int, [c_void_p, c_uint32, c_void_p, c_float, POINTER(c_uint32), POINTER(c_uint32)]),
+    ("mcrt_world_read_mesh", c_int, [c_void_p, c_void_p, c_uint32, c_void_p, c_uint32]),
     ("mcrt_adjoint", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_uint32, POINTER(RenderOpts),
                              c_void_p, c_void_p, c_void_p]),
     ("mcrt_autotune", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, POINTER(RenderOpts),

@@ -43,30 +43,7 @@ void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 unsigned long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 }  // namespace mcrt
 
-namespace {
-
-struct DBuf {
-    void *p = nullptr;
-    size_t cap = 0;
-    cudaError_t ensure(size_t bytes) {
-        if (bytes == 0) bytes = 16;
-        if (bytes <= cap && p) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-        cudaError_t e = cudaMalloc(&p, bytes);
-        if (e == cudaSuccess) cap = bytes;
-        return e;
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-    }
-    template <typename T> T *as() const { return static_cast<T *>(p); }
-};
-
-}  // namespace
+using mcrt::DBuf;
 
 struct mcrt_ctx {
     int device = 0;
@@ -103,6 +80,15 @@ struct mcrt_ctx {
     // adjoint
     DBuf dimg, grad;
     mcrt_gpu_material_data host_materials{};
+    // directional light
+    float sun_dir[4] = {0, 1, 0, 0}, sun_E[4] = {0, 0, 0, 0};
+    bool has_sun = false;
+    // voxel world
+    DBuf world_vox, world_matmap;
+    uint32_t world_nx = 0, world_ny = 0, world_nz = 0;
+    int32_t world_cx0 = 0, world_cz0 = 0;
+    mcrt::WorldMeshBuffers wmesh;
+    bool wmesh_valid = false;
 };
 
 namespace {
@@ -154,6 +140,9 @@ mcrt::DeviceScene device_scene(const mcrt_ctx *c) {
     S.albedo_layers = c->albedo_layers;
     S.albedo_size = c->albedo_size;
     S.srgb_lut = reinterpret_cast<const float *>(c->albedo.as<char>() + c->srgb_lut_offset);
+    S.has_sun = c->has_sun ? 1 : 0;
+    S.sun_dir = make_float4(c->sun_dir[0], c->sun_dir[1], c->sun_dir[2], 0.0f);
+    S.sun_E = make_float4(c->sun_E[0], c->sun_E[1], c->sun_E[2], 0.0f);
     return S;
 }
 
@@ -197,6 +186,19 @@ __global__ void k_gather_spheres(const mcrt_gpu_sphere *orig, const uint32_t *or
 __global__ void k_iota(uint32_t *p, uint32_t n) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) p[i] = i;
+}
+// Emissive-triangle list, ascending original id: flag, exclusive scan, scatter.
+__global__ void k_emissive_flags(const mcrt_gpu_triangle *t, uint32_t n, const mcrt_gpu_material_data *m,
+                                 uint32_t *flags) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n) return;
+    if (i == n) { flags[n] = 0u; return; }
+    uint32_t mat = min(t[i].mat_idx & 0x7fffffffu, 63u);
+    flags[i] = m->materials[mat].type_pad[0] == MCRT_MAT_EMISSIVE ? 1u : 0u;
+}
+__global__ void k_emissive_scatter(const uint32_t *flags, const uint32_t *pos, uint32_t n, uint32_t *out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && flags[i]) out[pos[i]] = i;
 }
 
 cudaEvent_t ev(mcrt_ctx *ctx, size_t i) {
@@ -341,7 +343,9 @@ void mcrt_destroy(mcrt_ctx *ctx) {
     DBuf *bufs[] = {&ctx->spheres, &ctx->sphere_ids, &ctx->sphere_nodes, &ctx->vertices, &ctx->triangles,
                     &ctx->mesh_nodes, &ctx->tri_order, &ctx->trirecs, &ctx->cnodes, &ctx->materials, &ctx->env,
                     &ctx->lights, &ctx->light_cdf, &ctx->tmp, &ctx->staging, &ctx->albedo, &ctx->wnodes, &ctx->pbmem, &ctx->mean,
-                    &ctx->sum, &ctx->gbuf, &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->counters};
+                    &ctx->sum, &ctx->gbuf, &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->counters, &ctx->dimg,
+                    &ctx->grad, &ctx->world_vox, &ctx->world_matmap, &ctx->wmesh.counts, &ctx->wmesh.vertices,
+                    &ctx->wmesh.triangles};
     for (DBuf *b : bufs) b->release();
     mcrt::free_bvh_scratch(ctx->bvh_scratch);
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
@@ -354,6 +358,15 @@ mcrt_status mcrt_upload_scene(mcrt_ctx *ctx, const mcrt_scene_desc *d) {
     if (!d) return fail(ctx, MCRT_ERR_INVALID_ARG, "desc is NULL");
     if (!d->materials) return fail(ctx, MCRT_ERR_INVALID_ARG, "materials is NULL");
     if (d->n_spheres && !d->spheres) return fail(ctx, MCRT_ERR_INVALID_ARG, "spheres is NULL");
+    const bool world_mesh = (d->flags & MCRT_SCENE_WORLD_MESH) != 0;
+    if (world_mesh) {
+        if (d->vertices || d->triangles || d->n_vertices || d->n_triangles || d->mesh_bvh)
+            return fail(ctx, MCRT_ERR_INVALID_ARG, "MCRT_SCENE_WORLD_MESH takes no host vertices, triangles or BVH");
+        if (!ctx->wmesh_valid) return fail(ctx, MCRT_ERR_INVALID_ARG, "no world mesh (call mcrt_world_mesh first)");
+    }
+    for (int k = 0; k < 3; ++k)
+        if (!std::isfinite(d->sun_dir[k]) || !std::isfinite(d->sun_irradiance[k]) || d->sun_irradiance[k] < 0.0f)
+            return fail(ctx, MCRT_ERR_INVALID_ARG, "sun direction / irradiance must be finite, irradiance >= 0");
     if (d->n_triangles && (!d->triangles || !d->vertices))
         return fail(ctx, MCRT_ERR_INVALID_ARG, "triangles or vertices is NULL");
     if (d->n_triangles >= (1u << 27) - 1) return fail(ctx, MCRT_ERR_INVALID_ARG, "too many triangles (max 2^27-2)");
@@ -385,7 +398,9 @@ mcrt_status mcrt_upload_scene(mcrt_ctx *ctx, const mcrt_scene_desc *d) {
     cudaStream_t st = ctx->stream;
     ctx->has_scene = false;
     ctx->acc_valid = false;
-    const uint32_t ns = d->n_spheres, nv = d->n_vertices, nt = d->n_triangles;
+    const uint32_t ns = d->n_spheres;
+    const uint32_t nv = world_mesh ? 4 * ctx->wmesh.n_quads : d->n_vertices;
+    const uint32_t nt = world_mesh ? 2 * ctx->wmesh.n_quads : d->n_triangles;
 
     // ---- spheres, stored in BVH order, with their original ids
     CK(ctx->spheres.ensure((size_t)ns * 32), "allocate spheres");
@@ -422,7 +437,10 @@ mcrt_status mcrt_upload_scene(mcrt_ctx *ctx, const mcrt_scene_desc *d) {
     }
     // ---- vertices
     CK(ctx->vertices.ensure((size_t)nv * 48), "allocate vertices");
-    if (nv) CK(cudaMemcpyAsync(ctx->vertices.p, d->vertices, (size_t)nv * 48, cudaMemcpyHostToDevice, st), "upload");
+    if (nv)
+        CK(cudaMemcpyAsync(ctx->vertices.p, world_mesh ? ctx->wmesh.vertices.p : (const void *)d->vertices,
+                           (size_t)nv * 48, world_mesh ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st),
+           "upload");
     ctx->n_vertices = nv;
     // ---- triangles (kept in original order on the device) and the mesh BVH
     CK(ctx->triangles.ensure((size_t)nt * 16), "allocate triangles");
@@ -448,7 +466,9 @@ mcrt_status mcrt_upload_scene(mcrt_ctx *ctx, const mcrt_scene_desc *d) {
             mcrt_status s = finish_mesh(ctx);
             if (s != MCRT_OK) return s;
         } else {
-            CK(cudaMemcpyAsync(ctx->triangles.p, d->triangles, (size_t)nt * 16, cudaMemcpyHostToDevice, st), "upload");
+            CK(cudaMemcpyAsync(ctx->triangles.p, world_mesh ? ctx->wmesh.triangles.p : (const void *)d->triangles,
+                               (size_t)nt * 16, world_mesh ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st),
+               "upload");
             mcrt_status s = build_mesh_bvh_gpu(ctx);
             if (s != MCRT_OK) return s;
         }
@@ -492,29 +512,56 @@ mcrt_status mcrt_upload_scene(mcrt_ctx *ctx, const mcrt_scene_desc *d) {
     if (d->env_w)
         CK(cudaMemcpyAsync(ctx->env.p, d->env_rgba, (size_t)d->env_w * d->env_h * 16, cudaMemcpyHostToDevice, st),
            "upload");
-    // ---- lights: emissive triangles by original id, emissive spheres by ordered slot
-    std::vector<uint32_t> lights;
+    // ---- lights: emissive triangles by original id (device flag + scan), then
+    //      emissive spheres by ordered slot
     auto emissive = [&](uint32_t mat) {
         const mcrt_gpu_material &m = d->materials->materials[std::min(mat & 0x7fffffffu, 63u)];
         return m.type_pad[0] == MCRT_MAT_EMISSIVE;
     };
-    for (uint32_t i = 0; i < nt; ++i) {
-        uint32_t id = (d->mesh_bvh && d->triangle_order) ? d->triangle_order[i] : i;
-        if (emissive(d->triangles[i].mat_idx)) lights.push_back(id);
-    }
-    std::sort(lights.begin(), lights.end());
+    std::vector<uint32_t> sphere_lights;
     if (ns) {
         std::vector<mcrt_gpu_sphere> ordered(ns);
         CK(cudaMemcpyAsync(ordered.data(), ctx->spheres.p, (size_t)ns * 32, cudaMemcpyDeviceToHost, st),
            "read spheres");
         CK(cudaStreamSynchronize(st), "sync");
         for (uint32_t s = 0; s < ns; ++s)
-            if (emissive(ordered[s].mat_and_pad[0])) lights.push_back(s | MCRT_HIT_SPHERE);
+            if (emissive(ordered[s].mat_and_pad[0])) sphere_lights.push_back(s | MCRT_HIT_SPHERE);
     }
-    ctx->n_lights = (uint32_t)lights.size();
-    CK(ctx->lights.ensure(lights.size() * 4), "allocate lights");
-    if (!lights.empty())
-        CK(cudaMemcpyAsync(ctx->lights.p, lights.data(), lights.size() * 4, cudaMemcpyHostToDevice, st), "upload");
+    uint32_t n_tri_lights = 0;
+    uint32_t *lflags = nullptr, *lpos = nullptr;
+    if (nt) {
+        const size_t sw = mcrt::scan_tmp_words(nt + 1);
+        CK(ctx->tmp.ensure((2 * ((size_t)nt + 1) + sw) * 4), "allocate scratch");
+        lflags = ctx->tmp.as<uint32_t>();
+        lpos = lflags + nt + 1;
+        k_emissive_flags<<<(nt + 256) / 256, 256, 0, st>>>(ctx->triangles.as<mcrt_gpu_triangle>(), nt,
+                                                          ctx->materials.as<mcrt_gpu_material_data>(), lflags);
+        ::mcrt::note_launch();
+        mcrt::exclusive_scan_u32(lflags, lpos, nt + 1, lpos + nt + 1, st);
+        CK(cudaMemcpyAsync(&n_tri_lights, lpos + nt, 4, cudaMemcpyDeviceToHost, st), "count lights");
+        CK(cudaStreamSynchronize(st), "count lights");
+    }
+    ctx->n_lights = n_tri_lights + (uint32_t)sphere_lights.size();
+    CK(ctx->lights.ensure((size_t)ctx->n_lights * 4), "allocate lights");
+    if (n_tri_lights) {
+        k_emissive_scatter<<<(nt + 255) / 256, 256, 0, st>>>(lflags, lpos, nt, ctx->lights.as<uint32_t>());
+        ::mcrt::note_launch();
+    }
+    if (!sphere_lights.empty())
+        CK(cudaMemcpyAsync(ctx->lights.as<uint32_t>() + n_tri_lights, sphere_lights.data(), sphere_lights.size() * 4,
+                           cudaMemcpyHostToDevice, st),
+           "upload");
+    // ---- directional light
+    ctx->has_sun = d->sun_irradiance[0] > 0.0f || d->sun_irradiance[1] > 0.0f || d->sun_irradiance[2] > 0.0f;
+    if (ctx->has_sun) {
+        const double len = std::sqrt((double)d->sun_dir[0] * d->sun_dir[0] + (double)d->sun_dir[1] * d->sun_dir[1] +
+                                     (double)d->sun_dir[2] * d->sun_dir[2]);
+        if (!(len > 0.0)) return fail(ctx, MCRT_ERR_INVALID_ARG, "sun direction is zero");
+        for (int k = 0; k < 3; ++k) {
+            ctx->sun_dir[k] = (float)(d->sun_dir[k] / len);
+            ctx->sun_E[k] = d->sun_irradiance[k];
+        }
+    }
     mcrt_status s = finish_lights(ctx);
     if (s != MCRT_OK) return s;
     CK(cudaStreamSynchronize(st), "scene upload");
@@ -629,7 +676,7 @@ mcrt_status mcrt_render(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t 
     std::vector<std::pair<size_t, int>> marks;   // (event index, category)
     cudaEvent_t e_begin = ev(ctx, evi++);
     cudaEventRecord(e_begin, st);
-    const bool nee = (o.flags & MCRT_RENDER_NEE) != 0 && ctx->n_lights > 0;
+    const bool nee = (o.flags & MCRT_RENDER_NEE) != 0 && (ctx->n_lights > 0 || ctx->has_sun);
     uint32_t done = 0;
     bool first_pass = true;
     while (done < spp) {
@@ -774,7 +821,7 @@ mcrt_status mcrt_adjoint(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t
     A.dimg = ctx->dimg.as<float4>();
     A.inv_spp = 1.0f / (float)spp;
     A.grad = ctx->grad.as<double>();
-    const bool nee = (o.flags & MCRT_RENDER_NEE) != 0 && ctx->n_lights > 0;
+    const bool nee = (o.flags & MCRT_RENDER_NEE) != 0 && (ctx->n_lights > 0 || ctx->has_sun);
     const unsigned long long launches0 = mcrt::launch_count();
     cudaEvent_t e_begin = ev(ctx, 2), e_end = ev(ctx, 3);
     cudaEventRecord(e_begin, st);
@@ -826,6 +873,102 @@ mcrt_status mcrt_adjoint(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t
     CK(cudaMemcpy(grad, ctx->grad.p, 256 * sizeof(double), cudaMemcpyDeviceToHost), "read gradient");
     if (out_rgba)
         CK(cudaMemcpy(out_rgba, ctx->mean.p, (size_t)npix * 16, cudaMemcpyDeviceToHost), "read image");
+    return MCRT_OK;
+}
+
+static mcrt_status check_world_dims(mcrt_ctx *ctx, uint32_t nx, uint32_t ny, uint32_t nz) {
+    if (nx == 0 || nz == 0 || nx % 16 || nz % 16)
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "world nx and nz must be positive multiples of 16");
+    if (ny < 2 || ny > 1024) return fail(ctx, MCRT_ERR_INVALID_ARG, "world ny must be in [2, 1024]");
+    if ((uint64_t)nx * ny * nz > (1ull << 32)) return fail(ctx, MCRT_ERR_INVALID_ARG, "world grid too large");
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_world_generate(mcrt_ctx *ctx, const mcrt_world_params *p, uint8_t *out_voxels) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!p) return fail(ctx, MCRT_ERR_INVALID_ARG, "params is NULL");
+    mcrt_status ds = check_world_dims(ctx, p->nx, p->ny, p->nz);
+    if (ds != MCRT_OK) return ds;
+    if (p->height_octaves == 0 || p->height_octaves > 16 || p->cave_octaves > 16)
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "octaves must be in [1, 16] (caves [0, 16])");
+    const float fs[] = {p->height_base, p->height_amp, p->height_freq, p->lacunarity, p->gain, p->cave_freq,
+                        p->cave_threshold, p->cave_contrast, p->sea_level, p->sand_line};
+    for (float f : fs)
+        if (!std::isfinite(f)) return fail(ctx, MCRT_ERR_INVALID_ARG, "world parameters must be finite");
+    if (std::abs((int64_t)p->chunk_x0) > (1 << 22) || std::abs((int64_t)p->chunk_z0) > (1 << 22))
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "chunk coordinates out of range");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const size_t n = (size_t)p->nx * p->ny * p->nz;
+    CK(ctx->world_vox.ensure(n), "allocate voxel grid");
+    mcrt::launch_world_generate(*p, ctx->world_vox.as<uint8_t>(), ctx->stream);
+    CK(cudaGetLastError(), "world generate");
+    ctx->world_nx = p->nx; ctx->world_ny = p->ny; ctx->world_nz = p->nz;
+    ctx->world_cx0 = p->chunk_x0; ctx->world_cz0 = p->chunk_z0;
+    ctx->wmesh_valid = false;
+    if (out_voxels) CK(cudaMemcpyAsync(out_voxels, ctx->world_vox.p, n, cudaMemcpyDeviceToHost, ctx->stream), "read");
+    CK(cudaStreamSynchronize(ctx->stream), "world generate");
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_world_upload(mcrt_ctx *ctx, const uint8_t *voxels, uint32_t nx, uint32_t ny, uint32_t nz,
+                              int32_t chunk_x0, int32_t chunk_z0) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!voxels) return fail(ctx, MCRT_ERR_INVALID_ARG, "voxels is NULL");
+    mcrt_status ds = check_world_dims(ctx, nx, ny, nz);
+    if (ds != MCRT_OK) return ds;
+    if (std::abs((int64_t)chunk_x0) > (1 << 22) || std::abs((int64_t)chunk_z0) > (1 << 22))
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "chunk coordinates out of range");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const size_t n = (size_t)nx * ny * nz;
+    CK(ctx->world_vox.ensure(n), "allocate voxel grid");
+    CK(cudaMemcpyAsync(ctx->world_vox.p, voxels, n, cudaMemcpyHostToDevice, ctx->stream), "upload voxels");
+    CK(cudaStreamSynchronize(ctx->stream), "upload voxels");
+    ctx->world_nx = nx; ctx->world_ny = ny; ctx->world_nz = nz;
+    ctx->world_cx0 = chunk_x0; ctx->world_cz0 = chunk_z0;
+    ctx->wmesh_valid = false;
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_world_mesh(mcrt_ctx *ctx, uint32_t mode, const uint32_t *block_material, float voxel_size,
+                            uint32_t *out_n_vertices, uint32_t *out_n_triangles) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!ctx->world_nx) return fail(ctx, MCRT_ERR_INVALID_ARG, "no voxel grid (generate or upload one first)");
+    if (!block_material) return fail(ctx, MCRT_ERR_INVALID_ARG, "block_material is NULL");
+    if (mode != MCRT_MESH_GREEDY && mode != MCRT_MESH_FACES) return fail(ctx, MCRT_ERR_INVALID_ARG, "unknown mode");
+    if (!(voxel_size > 0.0f) || !std::isfinite(voxel_size))
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "voxel_size must be positive");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+    CK(ctx->world_matmap.ensure(256 * 4), "allocate material map");
+    CK(cudaMemcpyAsync(ctx->world_matmap.p, block_material, 256 * 4, cudaMemcpyHostToDevice, st), "upload map");
+    ctx->wmesh_valid = false;
+    cudaError_t e = mcrt::world_mesh(ctx->world_vox.as<uint8_t>(), ctx->world_nx, ctx->world_ny, ctx->world_nz,
+                                     ctx->world_cx0, ctx->world_cz0, mode == MCRT_MESH_GREEDY,
+                                     ctx->world_matmap.as<uint32_t>(), voxel_size, ctx->wmesh, st);
+    if (e == cudaErrorInvalidValue) return fail(ctx, MCRT_ERR_INVALID_ARG, "world mesh too large for the tracer");
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "world mesh");
+    CK(cudaStreamSynchronize(st), "world mesh");
+    ctx->wmesh_valid = true;
+    if (out_n_vertices) *out_n_vertices = 4 * ctx->wmesh.n_quads;
+    if (out_n_triangles) *out_n_triangles = 2 * ctx->wmesh.n_quads;
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_world_read_mesh(mcrt_ctx *ctx, mcrt_gpu_vertex *vertices, uint32_t vertex_capacity,
+                                 mcrt_gpu_triangle *triangles, uint32_t triangle_capacity) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!ctx->wmesh_valid) return fail(ctx, MCRT_ERR_INVALID_ARG, "no world mesh");
+    const uint32_t nv = 4 * ctx->wmesh.n_quads, nt = 2 * ctx->wmesh.n_quads;
+    if ((vertices && vertex_capacity < nv) || (triangles && triangle_capacity < nt))
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "capacity too small");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if (vertices && nv)
+        CK(cudaMemcpy(vertices, ctx->wmesh.vertices.p, (size_t)nv * sizeof(mcrt_gpu_vertex), cudaMemcpyDeviceToHost),
+           "read vertices");
+    if (triangles && nt)
+        CK(cudaMemcpy(triangles, ctx->wmesh.triangles.p, (size_t)nt * sizeof(mcrt_gpu_triangle),
+                      cudaMemcpyDeviceToHost),
+           "read triangles");
     return MCRT_OK;
 }
 
@@ -937,6 +1080,32 @@ mcrt_status mcrt_denoise(mcrt_ctx *ctx, const float *in_rgba, const float *gbuf,
     cudaEventRecord(b, st);
     CK(cudaGetLastError(), "denoise launch");
     CK(cudaMemcpyAsync(out_rgba, ctx->io_c.p, bytes, cudaMemcpyDeviceToHost, st), "read");
+    CK(cudaStreamSynchronize(st), "denoise");
+    float t = 0.0f;
+    cudaEventElapsedTime(&t, a, b);
+    ctx->last_ms[0] = t;
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_denoise_accum(mcrt_ctx *ctx, const mcrt_denoise_params *params, float *out_rgba) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!params) return fail(ctx, MCRT_ERR_INVALID_ARG, "params is NULL");
+    if (!ctx->acc_valid || !ctx->gbuf_valid)
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "no render with a G-buffer to denoise");
+    if (params->radius < 0 || params->radius > 64) return fail(ctx, MCRT_ERR_INVALID_ARG, "radius must be in [0, 64]");
+    if (!(params->sigma_s > 0.0f) || !(params->sigma_d > 0.0f))
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "sigma_s and sigma_d must be > 0");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+    const uint32_t w = ctx->acc_w, h = ctx->acc_h;
+    const size_t bytes = (size_t)w * h * 16;
+    CK(ctx->io_c.ensure(bytes), "allocate");
+    cudaEvent_t a = ev(ctx, 0), b = ev(ctx, 1);
+    cudaEventRecord(a, st);
+    mcrt::launch_denoise(ctx->mean.as<float4>(), ctx->gbuf.as<float4>(), w, h, *params, ctx->io_c.as<float4>(), st);
+    cudaEventRecord(b, st);
+    CK(cudaGetLastError(), "denoise launch");
+    if (out_rgba) CK(cudaMemcpyAsync(out_rgba, ctx->io_c.p, bytes, cudaMemcpyDeviceToHost, st), "read");
     CK(cudaStreamSynchronize(st), "denoise");
     float t = 0.0f;
     cudaEventElapsedTime(&t, a, b);

@@ -104,6 +104,9 @@ struct DeviceScene {
     // on the host in double precision and rounded to float)
     const uchar4 *albedo; uint32_t albedo_layers, albedo_size;
     const float *srgb_lut;
+    // directional light: unit direction towards it, irradiance at normal incidence
+    int has_sun;
+    float4 sun_dir, sun_E;
 };
 
 }  // namespace mcrt

@@ -9,6 +9,28 @@
 
 namespace mcrt {
 
+// A growable device allocation.
+struct DBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes == 0) bytes = 16;
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e == cudaSuccess) cap = bytes;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <typename T> T *as() const { return static_cast<T *>(p); }
+};
+
 // Process-wide count of kernel launches issued by this library (every launch
 // site calls note_launch()); reported per call by mcrt_last_timings.
 void note_launch();
@@ -87,6 +109,17 @@ cudaError_t gpu_make_compact(const mcrt_gpu_bvh_node *d_nodes, uint32_t n_nodes,
 // Collapse into the quantised 4-wide layout (d_tmp: 2*n_nodes + 4 words).
 cudaError_t gpu_make_wide4(const mcrt_gpu_bvh_node *d_nodes, uint32_t n_nodes, uint4 *d_wide, uint32_t *n_wide,
                            uint32_t *d_tmp, cudaStream_t st);
+
+// Voxel world (world.cu)
+struct WorldMeshBuffers {
+    DBuf counts, vertices, triangles;
+    uint32_t n_quads = 0;
+};
+void launch_world_generate(const mcrt_world_params &P, uint8_t *vox, cudaStream_t st);
+// Mesh the device voxel grid (greedy: the reference's greedy mesher, else one
+// quad per visible face) into M.vertices / M.triangles (4 and 2 per quad).
+cudaError_t world_mesh(const uint8_t *d_vox, uint32_t nx, uint32_t ny, uint32_t nz, int32_t chunk_x0, int32_t chunk_z0,
+                       bool greedy, const uint32_t *d_mat_of, float voxel, WorldMeshBuffers &M, cudaStream_t st);
 
 // Denoiser (denoise.cu)
 void launch_denoise(const float4 *in, const float4 *gbuf, uint32_t w, uint32_t h, const mcrt_denoise_params &p,

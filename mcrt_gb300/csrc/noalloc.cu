@@ -112,7 +112,7 @@ extern "C" mcrt_status mcrt_render_noalloc(mcrt_ctx *ctx, const mcrt_camera_unif
     // state and the sums are fully written by ray generation and the first resolve)
     e = cudaMemsetAsync(B.counters, 0, kCounterBytes, st);
     if (e != cudaSuccess) return fail(MCRT_ERR_CUDA, "clearing the no-alloc counters failed");
-    const bool nee = (o.flags & MCRT_RENDER_NEE) != 0 && S.n_lights > 0;
+    const bool nee = (o.flags & MCRT_RENDER_NEE) != 0 && (S.n_lights > 0 || S.has_sun);
     uint32_t done = 0;
     while (done < spp) {
         mcrt::RenderParams P{};

@@ -306,17 +306,39 @@ __device__ __forceinline__ uint32_t pick_light(const DeviceScene &S, float u) {
     return lo;
 }
 
-struct LightSample { f3 dir; float dist; float pdf; f3 Le; uint32_t mat; bool ok; };
+struct LightSample { f3 dir; float dist; float pdf; f3 Le; uint32_t mat; bool ok; bool delta; };
+
+// Probability of choosing among the area lights: with a directional light as
+// well, each kind is chosen with probability 1/2.
+__device__ __forceinline__ float area_light_selection(const DeviceScene &S) {
+    return (S.has_sun && S.n_lights > 0) ? 0.5f : 1.0f;
+}
 
 // Uniform point on an emissive triangle, or a direction in the cone subtended by
 // an emissive sphere.  pdf is per unit solid angle at x (including the choice of
-// the light).
+// the light).  The directional light is a delta light: pdf is its selection
+// probability, dist reaches past the scene, and no MIS applies.
 __device__ __forceinline__ LightSample sample_light(const DeviceScene &S, f3 x, uint32_t &rng) {
     LightSample ls{};
     ls.ok = false;
+    ls.delta = false;
+    const float sel = area_light_selection(S);
+    if (S.has_sun) {
+        const bool sun = S.n_lights == 0 || rand_f32(rng) < 0.5f;
+        if (sun) {
+            ls.dir = xyz(S.sun_dir);
+            ls.dist = kTMax;
+            ls.pdf = sel;
+            ls.Le = xyz(S.sun_E);
+            ls.mat = 0xffu;
+            ls.ok = true;
+            ls.delta = true;
+            return ls;
+        }
+    }
     uint32_t li = pick_light(S, rand_f32(rng));
     uint32_t code = __ldg(S.lights + li);
-    float prob = light_weight(S, code) / S.light_total;
+    float prob = sel * (light_weight(S, code) / S.light_total);
     float r1 = rand_f32(rng), r2 = rand_f32(rng);
     if (!(prob > 0.0f)) return ls;
     if (code & MCRT_HIT_SPHERE) {
@@ -381,9 +403,10 @@ __device__ __forceinline__ LightSample sample_light(const DeviceScene &S, f3 x, 
 // emitter hit h along d.
 __device__ __forceinline__ float light_pdf_of_hit(const DeviceScene &S, float4 h, f3 o, f3 d) {
     uint32_t prim = __float_as_uint(h.y);
+    const float sel = area_light_selection(S);
     if (prim & MCRT_HIT_SPHERE) {
         uint32_t slot = __float_as_uint(h.z);
-        float prob = light_weight(S, slot | MCRT_HIT_SPHERE) / S.light_total;
+        float prob = sel * (light_weight(S, slot | MCRT_HIT_SPHERE) / S.light_total);
         float4 cr = __ldg(reinterpret_cast<const float4 *>(S.spheres + slot));
         f3 wc = xyz(cr) - o;
         float d2 = dot(wc, wc);
@@ -393,7 +416,7 @@ __device__ __forceinline__ float light_pdf_of_hit(const DeviceScene &S, float4 h
         if (!(cosmax < 1.0f)) return 0.0f;
         return prob / (kTau * (1.0f - cosmax));
     }
-    float prob = light_weight(S, prim) / S.light_total;
+    float prob = sel * (light_weight(S, prim) / S.light_total);
     mcrt_gpu_triangle tri = S.triangles[prim];
     f3 a = ld3(S.vertices[tri.v[0]].position), bq = ld3(S.vertices[tri.v[1]].position),
        cq = ld3(S.vertices[tri.v[2]].position);
@@ -675,7 +698,7 @@ __global__ void __launch_bounds__(256) k_shade(DeviceScene S, RenderParams P, Pa
         if (ADJ && v != 0.0f) atomicAdd(&gacc[k], v);
     };
     const uint32_t n = B.counters[qi];
-    const bool nee = (P.flags & MCRT_RENDER_NEE) != 0 && S.n_lights > 0;
+    const bool nee = (P.flags & MCRT_RENDER_NEE) != 0 && (S.n_lights > 0 || S.has_sun);
     const uint32_t lane = threadIdx.x & 31u;
     // work counters of the next extend and shadow launches (no kernel reads them now)
     if (blockIdx.x == 0 && threadIdx.x == 0) { B.counters[4] = 0; B.counters[5] = 0; }
@@ -732,7 +755,7 @@ __global__ void __launch_bounds__(256) k_shade(DeviceScene S, RenderParams P, Pa
                     f3 e = m.ior_pad[0] * (thr * albedo);
                     float wmis = 1.0f;
                     if (nee) {
-                        if (!(aux.w & kFlagSpecular) && thr4.w > 0.0f) {
+                        if (!(aux.w & kFlagSpecular) && thr4.w > 0.0f && S.n_lights > 0) {
                             float pl = light_pdf_of_hit(S, h, o, d);
                             float pb = thr4.w;
                             wmis = (pb * pb) / (pb * pb + pl * pl);
@@ -812,7 +835,7 @@ __global__ void __launch_bounds__(256) k_shade(DeviceScene S, RenderParams P, Pa
                                     float bp, lmz = 0.0f, lfw = 0.0f;
                                     f3 fc = ggx_eval(wo, wl, alpha, albedo, &bp, &lmz, &lfw);
                                     if (wl.z > 0.0f && (fc.x > 0.0f || fc.y > 0.0f || fc.z > 0.0f)) {
-                                        float wmis = (ls.pdf * ls.pdf) / (ls.pdf * ls.pdf + bp * bp);
+                                        float wmis = ls.delta ? 1.0f : (ls.pdf * ls.pdf) / (ls.pdf * ls.pdf + bp * bp);
                                         sc = (wmis / ls.pdf) * (thr * (fc * ls.Le));
                                         so = sh.p; sd = ls.dir; smax = ls.dist * (1.0f - 1e-4f);
                                         shadow = true;
@@ -837,7 +860,7 @@ __global__ void __launch_bounds__(256) k_shade(DeviceScene S, RenderParams P, Pa
                             float cs = dot(ls.dir, sh.n);
                             if (ls.ok && cs > 0.0f) {
                                 float bp = cs / kPi;
-                                float wmis = (ls.pdf * ls.pdf) / (ls.pdf * ls.pdf + bp * bp);
+                                float wmis = ls.delta ? 1.0f : (ls.pdf * ls.pdf) / (ls.pdf * ls.pdf + bp * bp);
                                 sc = (wmis * bp / ls.pdf) * (thr * (albedo * ls.Le));
                                 so = sh.p; sd = ls.dir; smax = ls.dist * (1.0f - 1e-4f);
                                 shadow = true;
@@ -948,10 +971,12 @@ __global__ void __launch_bounds__(128) k_shadow(DeviceScene S, PathBuffers B, Ad
             gadd(4u * mi + 1, dn.y * g.y);
             gadd(4u * mi + 2, dn.z * g.z);
             gadd(4u * mi + 3, ((dn.x + dn.y) + dn.z) * g.w);
-            const float *la = S.materials->materials[lm].albedo_fuzz;
-            gadd(4u * lm + 0, safe_ratio(dn.x, la[0]));
-            gadd(4u * lm + 1, safe_ratio(dn.y, la[1]));
-            gadd(4u * lm + 2, safe_ratio(dn.z, la[2]));
+            if (lm <= kMaxMatIdx) {                       // not the directional light
+                const float *la = S.materials->materials[lm].albedo_fuzz;
+                gadd(4u * lm + 0, safe_ratio(dn.x, la[0]));
+                gadd(4u * lm + 1, safe_ratio(dn.y, la[1]));
+                gadd(4u * lm + 2, safe_ratio(dn.z, la[2]));
+            }
         }
     }
     if (traced) atomicAdd(B.stats + 1, (unsigned long long)traced);

@@ -138,6 +138,51 @@ def cornell_box_ggx(seed: int = 1234):
     return base
 
 
+# Block ids of the reference's registry (world/block.rs:14-24) that the world
+# generator places, their material slots and Lambertian albedos (the registry's
+# tints, block.rs:64-125, where it has them).
+WORLD_BLOCKS = [  # (block id, name, albedo)
+    (1, "limestone", (0.82, 0.78, 0.70)),
+    (2, "red_soil", (0.55, 0.25, 0.15)),
+    (3, "grass", (0.35, 0.42, 0.18)),
+    (4, "sand", (0.86, 0.78, 0.56)),
+    (5, "water", (0.10, 0.25, 0.40)),
+    (8, "shrub", (0.22, 0.36, 0.12)),
+    (9, "gravel", (0.50, 0.48, 0.45)),
+    (10, "cave_glow", (0.40, 0.80, 0.60)),
+]
+
+
+def world_params(seed: int = 1234, nx: int = 256, ny: int = 128, nz: int = 256):
+    """mcrt_world_params of the voxel-world workload: a seeded 2D fBm heightmap
+    (4 octaves, lacunarity 2, gain 0.5) and 3D-noise caves carved where the
+    value exceeds 0.6; the grid is centred on the origin."""
+    return dict(nx=nx, ny=ny, nz=nz, seed=seed, chunk_x0=-(nx // 32), chunk_z0=-(nz // 32),
+                height_base=0.6 * ny, height_amp=0.3 * ny, height_freq=1.0 / 80.0, height_octaves=4,
+                lacunarity=2.0, gain=0.5, cave_freq=0.25, cave_octaves=2, cave_threshold=0.6, cave_contrast=1.5,
+                cave_min_y=2, sea_level=0.42 * ny, sand_line=0.45 * ny)
+
+
+def voxel_world(seed: int = 1234, nx: int = 256, ny: int = 128, nz: int = 256):
+    """The voxel-world scene: world parameters, the block -> material map and
+    the 8 Lambertian block materials, a sun (directional light) over the
+    gradient sky, a camera over the terrain; rendered at 1280 x 720, 8 spp,
+    depth 6, then denoised (5 x 5, sigma_color 0.1, sigma_normal 0.2)."""
+    md = np.zeros((), MATERIAL_DATA)
+    block_material = np.zeros(256, np.uint32)
+    for slot, (bid, _, alb) in enumerate(WORLD_BLOCKS):
+        _mat(md, slot, MAT_LAMBERTIAN, alb)
+        block_material[bid] = slot
+    md["mat_count"] = len(WORLD_BLOCKS)
+    s = 0.125                                    # VOXEL_SIZE, world/chunk.rs:20
+    ext_x, ext_z, ext_y = nx * s, nz * s, ny * s
+    camera = dict(look_from=[-0.42 * ext_x, 0.95 * ext_y, -0.42 * ext_z], look_at=[0.1 * ext_x, 0.35 * ext_y, 0.1 * ext_z],
+                  vfov=55.0, aperture=0.0)
+    return dict(params=world_params(seed, nx, ny, nz), block_material=block_material, materials=md, voxel_size=s,
+                camera=camera, sun_dir=[0.45, 0.8, 0.25], sun_irradiance=[3.2, 3.0, 2.7], width=1280, height=720,
+                spp=8, max_depth=6, denoise=dict(radius=2, sigma_color=0.1, sigma_normal=0.2))
+
+
 def icosphere(level: int):
     """Unit icosphere: (positions float64 (n,3), triangles int64 (m,3)), 20*4**level faces."""
     t = (1.0 + 5.0 ** 0.5) / 2.0

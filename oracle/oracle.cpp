@@ -507,6 +507,8 @@ void ggx_dg_dalpha(double alpha, double mz, double cos_o, double cos_i, double *
  * reached by BSDF sampling are weighted by the power heuristic.  The kernels do
  * exactly this, so renders with NEE are compared bit for bit. */
 struct Lights {
+    bool has_sun = false;            /* directional light: unit direction towards it, irradiance */
+    V3 sun_dir = {0, 0, 0}, sun_E = {0, 0, 0};
     std::vector<uint32_t> codes;     /* triangle original id, or ORC_HIT_SPHERE | ordered sphere slot */
     std::vector<float> cdf;          /* n + 1 entries */
     std::vector<uint32_t> slot_of;   /* original triangle id -> ordered slot */
@@ -540,6 +542,13 @@ float light_weight(const orc_scene *sc, const Lights &L, uint32_t code) {
     return (0.5f * sqrtf(dot(ng, ng))) * luminance(emission_of(sc, tri.mat_idx & 0x7fffffffu));
 }
 void make_lights(const orc_scene *sc, Lights &L) {
+    L.has_sun = sc->sun_irradiance[0] > 0.0f || sc->sun_irradiance[1] > 0.0f || sc->sun_irradiance[2] > 0.0f;
+    if (L.has_sun) {
+        const double len = std::sqrt((double)sc->sun_dir[0] * sc->sun_dir[0] + (double)sc->sun_dir[1] * sc->sun_dir[1] +
+                                     (double)sc->sun_dir[2] * sc->sun_dir[2]);
+        L.sun_dir = {(float)(sc->sun_dir[0] / len), (float)(sc->sun_dir[1] / len), (float)(sc->sun_dir[2] / len)};
+        L.sun_E = ld3(sc->sun_irradiance);
+    }
     L.slot_of.assign(sc->n_triangles, 0u);
     std::vector<uint32_t> tris;
     for (uint32_t s = 0; s < sc->n_triangles; ++s) {
@@ -585,14 +594,28 @@ inline uint32_t pick_light(const Lights &L, float u) {       /* largest k with c
     }
     return lo;
 }
-struct LightSample { V3 dir; float dist; float pdf; V3 Le; uint32_t mat; bool ok; };
+struct LightSample { V3 dir; float dist; float pdf; V3 Le; uint32_t mat; bool ok; bool delta; };
+/* With both a directional light and area lights, each kind is chosen with probability 1/2. */
+inline float area_selection(const Lights &L) { return (L.has_sun && L.n > 0) ? 0.5f : 1.0f; }
 /* A uniform point on an emissive triangle, or a direction in the cone of an
  * emissive sphere; pdf per unit solid angle at x, including the light choice. */
 LightSample sample_light(const orc_scene *sc, const Lights &L, V3 x, uint32_t &rng) {
     LightSample ls{};
     ls.ok = false;
+    ls.delta = false;
+    const float sel = area_selection(L);
+    if (L.has_sun && (L.n == 0 || rand_f32(rng) < 0.5f)) {     /* the directional (delta) light */
+        ls.dir = L.sun_dir;
+        ls.dist = T_MAX;
+        ls.pdf = sel;
+        ls.Le = L.sun_E;
+        ls.mat = 0xffu;
+        ls.ok = true;
+        ls.delta = true;
+        return ls;
+    }
     uint32_t code = L.codes[pick_light(L, rand_f32(rng))];
-    float prob = light_weight(sc, L, code) / L.total;
+    float prob = sel * (light_weight(sc, L, code) / L.total);
     float r1 = rand_f32(rng), r2 = rand_f32(rng);
     if (!(prob > 0.0f)) return ls;
     if (code & ORC_HIT_SPHERE) {
@@ -654,7 +677,7 @@ LightSample sample_light(const orc_scene *sc, const Lights &L, V3 x, uint32_t &r
 /* Solid-angle pdf at o with which sample_light produces the emitter hit c along d. */
 float light_pdf_of_hit(const orc_scene *sc, const Lights &L, const Closest &c, V3 o, V3 d) {
     if (c.prim & ORC_HIT_SPHERE) {
-        float prob = light_weight(sc, L, c.slot | ORC_HIT_SPHERE) / L.total;
+        float prob = area_selection(L) * (light_weight(sc, L, c.slot | ORC_HIT_SPHERE) / L.total);
         const orc_sphere &s = sc->spheres[c.slot];
         V3 wc = ld3(s.center_r) - o;
         float d2 = dot(wc, wc);
@@ -664,7 +687,7 @@ float light_pdf_of_hit(const orc_scene *sc, const Lights &L, const Closest &c, V
         if (!(cosmax < 1.0f)) return 0.0f;
         return prob / (TAU * (1.0f - cosmax));
     }
-    float prob = light_weight(sc, L, c.prim) / L.total;
+    float prob = area_selection(L) * (light_weight(sc, L, c.prim) / L.total);
     V3 a, bq, cq;
     tri_positions(sc, sc->triangles[c.slot], &a, &bq, &cq);
     V3 ng = cross(bq - a, cq - a);
@@ -701,7 +724,7 @@ struct Deriv {
  * lights: next-event estimation with MIS when non-null.  D: derivatives when non-null. */
 V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, float *gbuf, uint64_t *stats,
               const Lights *lights, Deriv *D) {
-    const bool nee = lights && lights->n > 0;
+    const bool nee = lights && (lights->n > 0 || lights->has_sun);
     V3 thr = {1.0f, 1.0f, 1.0f};
     V3 Lacc = {0.0f, 0.0f, 0.0f};
     float prev_pdf = -1.0f;
@@ -737,7 +760,7 @@ V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, f
         if (m.type_pad[0] == MAT_EMISSIVE) {                                   /* :608-610 */
             V3 e = m.ior_pad[0] * (thr * albedo);
             float wmis = 1.0f;
-            if (nee && prev_pdf > 0.0f) {
+            if (nee && prev_pdf > 0.0f && lights->n > 0) {
                 float pl = light_pdf_of_hit(sc, *lights, c, ray.o, ray.d);
                 wmis = (prev_pdf * prev_pdf) / (prev_pdf * prev_pdf + pl * pl);
             }
@@ -795,7 +818,7 @@ V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, f
                         float bp, mz, fw;
                         V3 fc = ggx_eval(wo, wl, alpha, albedo, &bp, &mz, &fw);
                         if (wl.z > 0.0f && (fc.x > 0.0f || fc.y > 0.0f || fc.z > 0.0f)) {
-                            float wmis = (ls.pdf * ls.pdf) / (ls.pdf * ls.pdf + bp * bp);
+                            float wmis = ls.delta ? 1.0f : (ls.pdf * ls.pdf) / (ls.pdf * ls.pdf + bp * bp);
                             sc_c = (wmis / ls.pdf) * (thr * (fc * ls.Le));
                             sh_o = h.p; sh_d = ls.dir; sh_max = ls.dist * (1.0f - 1e-4f);
                             have_shadow = true;
@@ -805,7 +828,7 @@ V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, f
                                 sc_lmat = ls.mat;
                                 double dg, dgd;
                                 ggx_dg_dalpha(alpha, mz, wo.z, wl.z, &dg, &dgd);
-                                const orc_material &lm = sc->materials->materials[ls.mat];
+                                const double lstrength = ls.mat <= MAX_MAT_IDX ? (double)sc->materials->materials[ls.mat].ior_pad[0] : 0.0;
                                 for (int k = 0; k < 3; ++k) {
                                     double f0 = comp(albedo, k);
                                     double F = f0 + (double)fw * (1.0 - f0);
@@ -813,7 +836,7 @@ V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, f
                                                  (dgd * 0.25 / (double)wo.z) * (1.0 - fw) * comp(tex, k);
                                     dsc_rough[k] = sc_scale * comp(thr, k) * comp(ls.Le, k) * F * dg * 0.25 /
                                                    (double)wo.z * dadr;
-                                    dsc_light[k] = sc_scale * comp(thr, k) * comp(fc, k) * (double)lm.ior_pad[0];
+                                    dsc_light[k] = sc_scale * comp(thr, k) * comp(fc, k) * lstrength;
                                 }
                             }
                         }
@@ -851,7 +874,7 @@ V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, f
                 float cs = dot(ls.dir, h.n);
                 if (ls.ok && cs > 0.0f) {
                     float bp = cs / PI_F;
-                    float wmis = (ls.pdf * ls.pdf) / (ls.pdf * ls.pdf + bp * bp);
+                    float wmis = ls.delta ? 1.0f : (ls.pdf * ls.pdf) / (ls.pdf * ls.pdf + bp * bp);
                     sc_c = (wmis * bp / ls.pdf) * (thr * (albedo * ls.Le));
                     sh_o = h.p; sh_d = ls.dir; sh_max = ls.dist * (1.0f - 1e-4f);
                     have_shadow = true;
@@ -859,10 +882,10 @@ V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, f
                         sc_scale = (double)(wmis * bp / ls.pdf);
                         sc_f = albedo * ls.Le;
                         sc_lmat = ls.mat;
-                        const orc_material &lm = sc->materials->materials[ls.mat];
+                        const double lstrength = ls.mat <= MAX_MAT_IDX ? (double)sc->materials->materials[ls.mat].ior_pad[0] : 0.0;
                         for (int k = 0; k < 3; ++k) {
                             dsc_alb[k] = sc_scale * comp(thr, k) * comp(tex, k) * comp(ls.Le, k);
-                            dsc_light[k] = sc_scale * comp(thr, k) * comp(albedo, k) * (double)lm.ior_pad[0];
+                            dsc_light[k] = sc_scale * comp(thr, k) * comp(albedo, k) * lstrength;
                         }
                     }
                 }
@@ -1231,9 +1254,22 @@ void orc_render(const orc_scene *sc, const orc_camera *cam, uint32_t w, uint32_t
 /* cs_denoise, denoise.wgsl:52-120 */
 void orc_denoise(const float *accum, const float *gbuf, uint32_t w, uint32_t h, int radius, float sigma_s,
                  float sigma_d, float normal_pow, float *out) {
+    orc_denoise_ex(accum, gbuf, w, h, radius, sigma_s, sigma_d, normal_pow, 0.0f, 0.0f, out);
+}
+
+/* cs_denoise with the two extension terms (0 = off): a colour term
+ * exp(-|c_p - c_q|^2 / (2 sigma_color^2)) multiplied into the weight, and a
+ * Gaussian normal term exp(-(1 - n_p.n_q)^2 / (2 sigma_normal^2)) in place of
+ * max(0, n_p.n_q)^normal_pow. */
+void orc_denoise_ex(const float *accum, const float *gbuf, uint32_t w, uint32_t h, int radius, float sigma_s,
+                    float sigma_d, float normal_pow, float sigma_color, float sigma_normal, float *out) {
     const int W = (int)w, H = (int)h;
     float inv2ss = 1.0f / ((2.0f * sigma_s) * sigma_s);
     float inv2ds = 1.0f / ((2.0f * sigma_d) * sigma_d);
+    const bool color_term = sigma_color > 0.0f;
+    const float inv2cs = color_term ? 1.0f / ((2.0f * sigma_color) * sigma_color) : 0.0f;
+    const bool gauss_normal = sigma_normal > 0.0f;
+    const float inv2ns = gauss_normal ? 1.0f / ((2.0f * sigma_normal) * sigma_normal) : 0.0f;
 #pragma omp parallel for schedule(static)
     for (int y = 0; y < H; ++y)
         for (int x = 0; x < W; ++x) {
@@ -1254,10 +1290,23 @@ void orc_denoise(const float *accum, const float *gbuf, uint32_t w, uint32_t h, 
                     if (on_sky != q_sky) continue;
                     float dist_sq = (float)(dx * dx + dy * dy);
                     float ws = of_exp(-dist_sq * inv2ss);
-                    float wn = on_sky ? 1.0f : of_pow(fmaxf(0.0f, dot(np, nq)), normal_pow);
+                    float wn = 1.0f;
+                    if (!on_sky) {
+                        float nd = dot(np, nq);
+                        if (gauss_normal) {
+                            float e = 1.0f - nd;
+                            wn = of_exp(-(e * e) * inv2ns);
+                        } else {
+                            wn = of_pow(fmaxf(0.0f, nd), normal_pow);
+                        }
+                    }
                     float rel = (dp - dq) / fmaxf(dp, 1e-4f);
                     float wd = on_sky ? 1.0f : of_exp(-(rel * rel) * inv2ds);
                     float wt = (ws * wn) * wd;
+                    if (color_term) {
+                        V3 dc = ld3(accum + 4 * ((size_t)qy * W + qx)) - ld3(accum + 4 * ((size_t)y * W + x));
+                        wt = wt * of_exp(-dot(dc, dc) * inv2cs);
+                    }
                     acc = acc + wt * ld3(accum + 4 * ((size_t)qy * W + qx));
                     wacc += wt;
                 }

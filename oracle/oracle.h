@@ -45,6 +45,8 @@ typedef struct {
     const orc_material_data *materials;
     const float *env_rgba; uint32_t env_w; uint32_t env_h;
     const uint8_t *albedo_rgba8; uint32_t albedo_layers; uint32_t albedo_size;  /* binding 10 (sRGB) */
+    float sun_dir[4];          /* directional light (ORC_RENDER_NEE only): towards the light */
+    float sun_irradiance[4];   /* all zero: none */
 } orc_scene;
 
 #define ORC_HIT_MISS 0xffffffffu
@@ -109,9 +111,37 @@ void orc_adjoint(const orc_scene *scene, const orc_camera *cam, uint32_t w, uint
                  uint32_t first_frame, uint32_t max_depth, uint32_t flags, const float *d_image, double *grad,
                  double *out_sum_rgb, int threads);
 
+/* Voxel world (world.cpp).  Parameters as mcrt_world_params. */
+typedef struct {
+    uint32_t nx, ny, nz;
+    uint32_t seed;
+    int32_t chunk_x0, chunk_z0;
+    float height_base, height_amp;
+    float height_freq;
+    uint32_t height_octaves;
+    float lacunarity, gain;
+    float cave_freq;
+    uint32_t cave_octaves;
+    float cave_threshold;
+    float cave_contrast;
+    uint32_t cave_min_y;
+    float sea_level, sand_line;
+} orc_world_params;
+void orc_world_generate(const orc_world_params *params, uint8_t *out_voxels);
+/* The reference's greedy chunk mesher over the grid (greedy = 0: one quad per
+ * visible face).  Returns the quad count; fills out_v / out_t (4 vertices and 2
+ * triangles per quad) only when both are given and cap_quads suffices. */
+uint64_t orc_world_mesh(const uint8_t *voxels, uint32_t nx, uint32_t ny, uint32_t nz, int32_t chunk_x0,
+                        int32_t chunk_z0, int greedy, const uint32_t *block_material, float voxel_size,
+                        orc_vertex *out_v, orc_triangle *out_t, uint64_t cap_quads);
+
 /* cs_denoise (denoise.wgsl:52-120). */
 void orc_denoise(const float *accum_rgba, const float *gbuf, uint32_t w, uint32_t h,
                  int radius, float sigma_s, float sigma_d, float normal_pow, float *out_rgba);
+
+/* cs_denoise with the library's extension terms (sigma_color, sigma_normal; 0 = off). */
+void orc_denoise_ex(const float *accum_rgba, const float *gbuf, uint32_t w, uint32_t h, int radius, float sigma_s,
+                    float sigma_d, float normal_pow, float sigma_color, float sigma_normal, float *out_rgba);
 
 /* headless.rs:93-98 tonemap of an RGBA f32 image to RGBA8 (non-finite -> 0, alpha 255). */
 void orc_tonemap_rgba8(const float *rgba, uint32_t n_pixels, uint8_t *out);

@@ -37,7 +37,8 @@ class _Scene(ctypes.Structure):
                 ("mesh_nodes", c_void_p), ("n_mesh_nodes", c_uint32),
                 ("materials", c_void_p),
                 ("env_rgba", c_void_p), ("env_w", c_uint32), ("env_h", c_uint32),
-                ("albedo", c_void_p), ("albedo_layers", c_uint32), ("albedo_size", c_uint32)]
+                ("albedo", c_void_p), ("albedo_layers", c_uint32), ("albedo_size", c_uint32),
+                ("sun_dir", c_float * 4), ("sun_irradiance", c_float * 4)]
 
 
 def default_albedo_layers(size=512):
@@ -134,7 +135,8 @@ def build_mesh_bvh(vertices, triangles):
 class OracleScene:
     """A scene as the reference binds it, built by the oracle's reference builder."""
 
-    def __init__(self, *, materials, spheres=None, vertices=None, triangles=None, env=None, albedo=None):
+    def __init__(self, *, materials, spheres=None, vertices=None, triangles=None, env=None, albedo=None,
+                 sun_dir=None, sun_irradiance=None):
         self.spheres_in = np.zeros(0, SPHERE) if spheres is None else np.ascontiguousarray(spheres, SPHERE)
         self.vertices = np.zeros(0, VERTEX) if vertices is None else np.ascontiguousarray(vertices, VERTEX)
         self.triangles_in = np.zeros(0, TRIANGLE) if triangles is None else np.ascontiguousarray(triangles, TRIANGLE)
@@ -153,6 +155,10 @@ class OracleScene:
             s.env_rgba, s.env_h, s.env_w = _p(self.env), self.env.shape[0], self.env.shape[1]
         self.albedo = np.ascontiguousarray(default_albedo_layers() if albedo is None else albedo, np.uint8)
         s.albedo, s.albedo_layers, s.albedo_size = _p(self.albedo), self.albedo.shape[0], self.albedo.shape[1]
+        if sun_irradiance is not None:
+            for k in range(3):
+                s.sun_dir[k] = float(sun_dir[k])
+                s.sun_irradiance[k] = float(sun_irradiance[k])
         self._s = s
 
     def reference_buffers(self):
@@ -195,12 +201,17 @@ class OracleScene:
         return grad.reshape(64, 4), acc
 
 
-def denoise(rgba, gbuf, radius=3, sigma_s=2.0, sigma_d=0.5, normal_pow=8.0):
+def denoise(rgba, gbuf, radius=3, sigma_s=2.0, sigma_d=0.5, normal_pow=8.0, sigma_color=0.0, sigma_normal=0.0):
+    L = lib()
+    L.orc_denoise_ex.restype = None
+    L.orc_denoise_ex.argtypes = [c_void_p, c_void_p, c_uint32, c_uint32, c_int, c_float, c_float, c_float, c_float,
+                                 c_float, c_void_p]
     rgba = np.ascontiguousarray(rgba, np.float32)
     gbuf = np.ascontiguousarray(gbuf, np.float32)
     h, w = rgba.shape[:2]
     out = np.zeros_like(rgba)
-    lib().orc_denoise(_p(rgba), _p(gbuf), w, h, radius, sigma_s, sigma_d, normal_pow, _p(out))
+    L.orc_denoise_ex(_p(rgba), _p(gbuf), w, h, radius, sigma_s, sigma_d, normal_pow, sigma_color, sigma_normal,
+                     _p(out))
     return out
 
 
@@ -230,6 +241,46 @@ def math_eval(fn, x, y=None):
     out = np.zeros_like(x)
     lib().orc_math_eval(MATH_FNS[fn], _p(x), _p(y), _p(out), x.size)
     return out
+
+
+class _WorldParams(ctypes.Structure):
+    _fields_ = [("nx", c_uint32), ("ny", c_uint32), ("nz", c_uint32), ("seed", c_uint32),
+                ("chunk_x0", ctypes.c_int32), ("chunk_z0", ctypes.c_int32),
+                ("height_base", c_float), ("height_amp", c_float), ("height_freq", c_float),
+                ("height_octaves", c_uint32), ("lacunarity", c_float), ("gain", c_float),
+                ("cave_freq", c_float), ("cave_octaves", c_uint32), ("cave_threshold", c_float),
+                ("cave_contrast", c_float), ("cave_min_y", c_uint32), ("sea_level", c_float), ("sand_line", c_float)]
+
+
+def world_generate(params):
+    """The voxel grid (nx, ny, nz) uint8 of the world generator."""
+    L = lib()
+    L.orc_world_generate.restype = None
+    L.orc_world_generate.argtypes = [POINTER(_WorldParams), c_void_p]
+    p = _WorldParams(**params)
+    vox = np.zeros((p.nx, p.ny, p.nz), np.uint8)
+    L.orc_world_generate(ctypes.byref(p), _p(vox))
+    return vox
+
+
+def world_mesh(voxels, block_material, voxel_size=0.125, greedy=True, chunk_x0=0, chunk_z0=0):
+    """The reference's greedy chunk mesher (or one quad per face) over a voxel grid:
+    (vertices, triangles)."""
+    L = lib()
+    L.orc_world_mesh.restype = ctypes.c_uint64
+    L.orc_world_mesh.argtypes = [c_void_p, c_uint32, c_uint32, c_uint32, ctypes.c_int32, ctypes.c_int32, c_int,
+                                 c_void_p, c_float, c_void_p, c_void_p, ctypes.c_uint64]
+    v = np.ascontiguousarray(voxels, np.uint8)
+    nx, ny, nz = v.shape
+    mm = np.zeros(256, np.uint32)
+    bm = np.asarray(block_material, np.uint32).ravel()
+    mm[:len(bm)] = bm
+    q = L.orc_world_mesh(_p(v), nx, ny, nz, chunk_x0, chunk_z0, 1 if greedy else 0, _p(mm), voxel_size, None, None, 0)
+    verts = np.zeros(4 * q, VERTEX)
+    tris = np.zeros(2 * q, TRIANGLE)
+    L.orc_world_mesh(_p(v), nx, ny, nz, chunk_x0, chunk_z0, 1 if greedy else 0, _p(mm), voxel_size, _p(verts),
+                     _p(tris), q)
+    return verts, tris
 
 
 def ggx_dg(alpha, mz, cos_o, cos_i):
