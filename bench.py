@@ -315,6 +315,44 @@ def voxel_world_rate(M, ctx, stream, n_warm=2, n_steps=3):
             "frame_msamples_per_s": round(W2 * H2 * S2 / (total / 1000.0) / 1e6, 1)}
 
 
+def batched_views_rate(M, ctx, stream, spp=4, n_warm=1, n_steps=3):
+    """16 seeded views of uneven sizes (256^2 .. 1920 x 1080) over the voxel
+    world (the scene of voxel_world_rate, left uploaded), depth 6, sun NEE:
+    all views in one batched render per frame (each bounce one launch over every
+    view, the passes replayed as a CUDA graph) against the same views rendered
+    one call each."""
+    import torch
+    from mcrt_gb300 import scenes
+    w = scenes.voxel_world(SEED)
+    vs = scenes.world_views(w, seed=SEED)
+    views = [(M.compute_camera(v["width"], v["height"], v["look_from"], v["look_at"], v["vfov"], 0.0),
+              v["width"], v["height"]) for v in vs]
+    depth = w["max_depth"]
+    px = sum(v[1] * v[2] for v in views)
+
+    def timed(fn):
+        ms = []
+        for i in range(n_warm + n_steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn(i)
+            b.record(stream)
+            b.synchronize()
+            if i >= n_warm:
+                ms.append(a.elapsed_time(b))
+        return sum(ms) / len(ms)
+
+    t_batch = timed(lambda i: ctx.render_views(views, spp, first_frame=i * spp, max_depth=depth, nee=True, graph=True,
+                                               read_back=False))
+    t_seq = timed(lambda i: [ctx.render(cam, vw, vh, spp, first_frame=i * spp, max_depth=depth, nee=True, outputs=())
+                             for cam, vw, vh in views])
+    return {"workload": f"voxel_world_16_views_seed{SEED}_{px / 1e6:.2f}Mpix_{spp}spp_depth{depth}_sun_nee",
+            "batched_graph_ms": round(t_batch, 3), "per_view_calls_ms": round(t_seq, 3),
+            "batched_msamples_per_s": round(px * spp / (t_batch / 1000.0) / 1e6, 1),
+            "per_view_msamples_per_s": round(px * spp / (t_seq / 1000.0) / 1e6, 1),
+            "speedup": round(t_seq / t_batch, 3)}
+
+
 def run_mcrt(args):
     import torch
     import mcrt_gb300 as M
@@ -398,11 +436,12 @@ def run_mcrt(args):
                 "n_tri": round(n_tri, 2), "mrays_per_s": round(rays / (ext_ms / 1000.0) / 1e6, 1),
                 "avg_launch_ms": round(ext_ms / max(ext_launches, 1), 4)}
     clocks = clk.summary()
-    quality = adjoint = voxel = None
+    quality = adjoint = voxel = views = None
     if not args.small:
         quality = time_to_relmse(M, ctx)
         adjoint = adjoint_rate(M, ctx, stream)
         voxel = voxel_world_rate(M, ctx, stream)
+        views = batched_views_rate(M, ctx, stream)
     out = {
         "metric": "Msamples/s", "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 3), "higher_is_better": True,
@@ -410,7 +449,8 @@ def run_mcrt(args):
         "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": SPP, "max_depth": DEPTH,
                    "triangles": int(len(sc["triangles"])), "seed": SEED, "estimator": "reference (no NEE)",
                    "parallelism": f"replicas{world}", "l2": "256 MB buffer written between timed steps",
-                   "extend_variant": variant, "autotune_extend_ms_2spp": [round(x, 3) for x in tune_ms]},
+                   "extend_variant": variant, "extend_variant_info": M.variant_info(variant),
+                   "autotune_extend_ms_2spp": [round(x, 3) for x in tune_ms]},
         "e2e": {"value": round(e2e_value, 3), "unit": "Msamples/s",
                 "h2d_bytes_per_step": int(sc["vertices"].nbytes), "d2h_bytes_per_step": W * H * 16},
         "gpu_launches": int(launches),
@@ -422,6 +462,7 @@ def run_mcrt(args):
         "time_to_relmse": quality,
         "adjoint": adjoint,
         "voxel_world": voxel,
+        "batched_views": views,
     }
     print(json.dumps(out))
     barrier(world)

@@ -190,7 +190,9 @@ mcrt_status mcrt_trace_closest(mcrt_ctx *ctx, const mcrt_ray *rays, uint32_t n, 
 enum {
     MCRT_RENDER_NEE = 1u << 0,        /* next-event estimation + MIS (else the reference estimator) */
     MCRT_RENDER_GBUFFER = 1u << 1,    /* keep the primary-hit G-buffer (path_trace.wgsl:593-601) */
-    MCRT_RENDER_KEEP_ACCUM = 1u << 2  /* continue the device running mean / f64 sum of the previous call */
+    MCRT_RENDER_KEEP_ACCUM = 1u << 2, /* continue the device running mean / f64 sum of the previous call */
+    MCRT_RENDER_GRAPH = 1u << 3       /* replay the passes as one captured CUDA graph (same results; no
+                                         per-kernel timings for the replayed passes) */
 };
 
 typedef struct {
@@ -201,9 +203,13 @@ typedef struct {
 } mcrt_render_opts;
 
 /* Autotuner (no reference counterpart): renders `spp` frames of w x h with each
- * closest-hit kernel variant (occupancy / register budget), keeps the fastest
- * for this context and reports it.  out_ms (optional) receives the extend time
- * of every variant; its capacity is 8 floats. */
+ * closest-hit kernel variant — BVH width (compact binary / quantised 4-wide),
+ * block size, register budget (minimum resident blocks) and traversal stack
+ * depth, see mcrt_variant_info — keeps the fastest for this context and
+ * reports it.  A variant whose stack overflows on this scene is not a
+ * candidate (its time is reported as -1).  out_ms (optional) receives the
+ * extend time of every variant; its capacity is 8 floats. */
+mcrt_status mcrt_variant_info(uint32_t variant, uint32_t *out4);   /* width, block, min blocks, stack */
 mcrt_status mcrt_autotune(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t w, uint32_t h, uint32_t spp,
                           const mcrt_render_opts *opts, uint32_t *out_variant, float *out_ms);
 
@@ -219,6 +225,22 @@ mcrt_status mcrt_autotune(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_
 mcrt_status mcrt_render(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t w, uint32_t h,
                         uint32_t spp, uint32_t first_frame, const mcrt_render_opts *opts,
                         float *out_rgba, double *accum_rgb, float *out_gbuf);
+
+/* Batched views (no reference counterpart; the reference renders one camera
+ * per headless run): n_views cameras of uneven sizes traced together — every
+ * bounce of every view is one launch of each wavefront kernel over the
+ * concatenated pixels.  Pixel (x, y) of view v is seeded as in mcrt_render,
+ * so each view's image equals mcrt_render of that view alone, bit for bit.
+ * out_rgba (optional): n_views host pointers (each NULL or w*h*4 floats) that
+ * receive the views' running means.  The device accumulation afterwards is the
+ * flat concatenation of the views' pixels. */
+typedef struct {
+    mcrt_camera_uniform cam;
+    uint32_t width, height;
+    uint32_t _pad[2];
+} mcrt_view;
+mcrt_status mcrt_render_views(mcrt_ctx *ctx, const mcrt_view *views, uint32_t n_views, uint32_t spp,
+                              uint32_t first_frame, const mcrt_render_opts *opts, float *const *out_rgba);
 
 /* mcrt_render for callers that may not allocate GPU memory while rendering
  * (no counterpart in the reference).  Hosts that reserve their GPU memory up

@@ -171,6 +171,13 @@ def materials(entries) -> np.ndarray:
     return md
 
 
+def variant_info(variant: int) -> dict:
+    """Closest-hit kernel variant: BVH width, block size, minimum resident blocks, stack depth."""
+    out = (c_uint32 * 4)()
+    check(lib().mcrt_variant_info(variant, out))
+    return dict(width=out[0], block=out[1], min_blocks=out[2], stack=out[3])
+
+
 def make_rays(org, dirs, tmin=1e-4, tmax=1e9) -> np.ndarray:
     org = np.asarray(org, np.float32).reshape(-1, 3)
     dirs = np.asarray(dirs, np.float32).reshape(-1, 3)
@@ -307,10 +314,11 @@ class Context:
         return hits
 
     def render(self, camera, width, height, spp, first_frame=0, max_depth=0, nee=False, spp_per_pass=0,
-               keep=False, outputs=("rgba", "sum", "gbuf")):
+               keep=False, outputs=("rgba", "sum", "gbuf"), graph=False):
         cam = _arr(camera, CAMERA)
         o = N.RenderOpts(max_depth=max_depth, flags=(N.RENDER_NEE if nee else 0) |
-                         (N.RENDER_KEEP_ACCUM if keep else 0), spp_per_pass=spp_per_pass)
+                         (N.RENDER_KEEP_ACCUM if keep else 0) | (N.RENDER_GRAPH if graph else 0),
+                         spp_per_pass=spp_per_pass)
         rgba = np.zeros((height, width, 4), np.float32) if "rgba" in outputs else None
         acc = np.zeros((height, width, 3), np.float64) if "sum" in outputs else None
         gb = np.zeros((height, width, 4), np.float32) if "gbuf" in outputs else None
@@ -318,6 +326,24 @@ class Context:
                                       ptr(rgba), ptr(acc), ptr(gb)))
         self._last_hw = (height, width)
         return dict(rgba=rgba, sum=acc, gbuf=gb)
+
+    def render_views(self, views, spp, first_frame=0, max_depth=0, nee=False, spp_per_pass=0, graph=False,
+                     read_back=True):
+        """Trace several cameras of uneven sizes together.  views: list of (camera, width, height);
+        returns the views' running means (list of (h, w, 4) arrays) when read_back."""
+        vv = np.zeros(len(views), N.VIEW)
+        for k, (cam, w, h) in enumerate(views):
+            vv[k]["cam"] = _arr(cam, CAMERA)
+            vv[k]["width"], vv[k]["height"] = w, h
+        o = N.RenderOpts(max_depth=max_depth, flags=(N.RENDER_NEE if nee else 0) | (N.RENDER_GRAPH if graph else 0),
+                         spp_per_pass=spp_per_pass)
+        outs = [np.zeros((h, w, 4), np.float32) for (_, w, h) in views] if read_back else []
+        ptrs = (c_void_p * len(views))(*[o_.ctypes.data for o_ in outs]) if read_back else None
+        self._check(lib().mcrt_render_views(self._h, ptr(vv), len(views), spp, first_frame, ctypes.byref(o),
+                                            ctypes.cast(ptrs, c_void_p) if read_back else None))
+        total = int(sum(w * h for (_, w, h) in views))
+        self._last_hw = (1, total)
+        return outs
 
     def update_materials(self, materials):
         """Replace the material table (same emissive slots) without re-uploading geometry."""
@@ -349,7 +375,7 @@ class Context:
         ms = (c_float * 8)()
         self._check(lib().mcrt_autotune(self._h, ptr(cam), width, height, spp, ctypes.byref(o), ctypes.byref(v), ms))
         self._last_hw = (height, width)
-        return v.value, [ms[i] for i in range(8) if ms[i] > 0]
+        return v.value, [ms[i] for i in range(8)]      # -1: the variant's stack overflowed on this scene
 
     def image_rgba8(self, aces=False) -> np.ndarray:
         """Tone-map the last render on the GPU (Reinhard + gamma 2.2, or ACES + sRGB)."""

@@ -43,7 +43,8 @@ BACKFACE_CULL_FLAG = 0x80000000
 HIT_MISS = 0xFFFFFFFF
 HIT_SPHERE = 0x80000000
 TRACE_REFERENCE_LAYOUT = 1
-RENDER_NEE, RENDER_GBUFFER, RENDER_KEEP_ACCUM = 1, 2, 4
+RENDER_NEE, RENDER_GBUFFER, RENDER_KEEP_ACCUM, RENDER_GRAPH = 1, 2, 4, 8
+VIEW = np.dtype([("cam", CAMERA), ("width", "<u4"), ("height", "<u4"), ("_pad", "<u4", 2)])   # mcrt_view
 ENV_W, ENV_H = 1024, 512
 
 STATUS = {0: "OK", -1: "INVALID_ARG", -2: "OOM", -3: "CUDA", -4: "TIMEOUT", -5: "STACK_OVERFLOW",
@@ -117,6 +118,8 @@ SIGNATURES = [
                                     POINTER(RenderOpts), c_void_p]),
     ("mcrt_read_accum", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     ("mcrt_update_materials", c_int, [c_void_p, c_void_p]),
+    ("mcrt_render_views", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, POINTER(RenderOpts), c_void_p]),
+    ("mcrt_variant_info", c_int, [c_uint32, c_void_p]),
     ("mcrt_denoise_accum", c_int, [c_void_p, POINTER(DenoiseParams), c_void_p]),
     ("mcrt_world_generate", c_int, [c_void_p, POINTER(WorldParams), c_void_p]),
     ("mcrt_world_upload", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_int32, c_int32]),

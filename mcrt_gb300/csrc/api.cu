@@ -89,6 +89,12 @@ struct mcrt_ctx {
     int32_t world_cx0 = 0, world_cz0 = 0;
     mcrt::WorldMeshBuffers wmesh;
     bool wmesh_valid = false;
+    // batched views and graph replay
+    DBuf views, pass_state;
+    std::vector<char> view_blob, graph_key;
+    std::vector<uint32_t> view_px;
+    cudaGraphExec_t graph_exec = nullptr;
+    unsigned long long graph_captures = 0;
 };
 
 namespace {
@@ -345,8 +351,9 @@ void mcrt_destroy(mcrt_ctx *ctx) {
                     &ctx->lights, &ctx->light_cdf, &ctx->tmp, &ctx->staging, &ctx->albedo, &ctx->wnodes, &ctx->pbmem, &ctx->mean,
                     &ctx->sum, &ctx->gbuf, &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->counters, &ctx->dimg,
                     &ctx->grad, &ctx->world_vox, &ctx->world_matmap, &ctx->wmesh.counts, &ctx->wmesh.vertices,
-                    &ctx->wmesh.triangles};
+                    &ctx->wmesh.triangles, &ctx->views, &ctx->pass_state};
     for (DBuf *b : bufs) b->release();
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     mcrt::free_bvh_scratch(ctx->bvh_scratch);
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
@@ -629,19 +636,42 @@ mcrt_status mcrt_trace_closest(mcrt_ctx *ctx, const mcrt_ray *rays, uint32_t n, 
     return MCRT_OK;
 }
 
-mcrt_status mcrt_render(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t w, uint32_t h, uint32_t spp,
-                        uint32_t first_frame, const mcrt_render_opts *opts, float *out_rgba, double *accum_rgb,
-                        float *out_gbuf) {
-    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+__global__ void k_pass_advance(uint32_t *pass_state, uint32_t spp_pass) {
+    pass_state[0] += spp_pass;
+    pass_state[1] = 1u;
+}
+
+// One render call: frames first_frame .. first_frame+spp-1 of a single w x h
+// view (views == NULL) or of n_views views traced together, their pixels
+// concatenated (the accumulation is then a flat row of all pixels).
+static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t w, uint32_t h,
+                               const mcrt_view *views, uint32_t n_views, uint32_t spp, uint32_t first_frame,
+                               const mcrt_render_opts *opts) {
     if (!ctx->has_scene) return fail(ctx, MCRT_ERR_NO_SCENE, "no scene uploaded");
-    if (!cam) return fail(ctx, MCRT_ERR_INVALID_ARG, "cam is NULL");
-    if (w == 0 || h == 0 || spp == 0) return fail(ctx, MCRT_ERR_INVALID_ARG, "width, height and spp must be > 0");
-    if ((uint64_t)w * h > (1ull << 26)) return fail(ctx, MCRT_ERR_INVALID_ARG, "image too large (max 2^26 pixels)");
+    if (spp == 0) return fail(ctx, MCRT_ERR_INVALID_ARG, "spp must be > 0");
+    uint64_t total = 0;
+    if (views) {
+        if (n_views == 0 || n_views > 4096) return fail(ctx, MCRT_ERR_INVALID_ARG, "n_views must be in [1, 4096]");
+        for (uint32_t v = 0; v < n_views; ++v) {
+            if (views[v].width == 0 || views[v].height == 0)
+                return fail(ctx, MCRT_ERR_INVALID_ARG, "view " + std::to_string(v) + " has a zero size");
+            total += (uint64_t)views[v].width * views[v].height;
+        }
+    } else {
+        if (!cam) return fail(ctx, MCRT_ERR_INVALID_ARG, "cam is NULL");
+        if (w == 0 || h == 0) return fail(ctx, MCRT_ERR_INVALID_ARG, "width and height must be > 0");
+        total = (uint64_t)w * h;
+    }
+    if (total > (1ull << 26)) return fail(ctx, MCRT_ERR_INVALID_ARG, "image too large (max 2^26 pixels)");
     mcrt_render_opts o{};
     if (opts) o = *opts;
     const uint32_t depth = o.max_depth ? o.max_depth : mcrt::kDefaultBounces;
     if (depth > 1024) return fail(ctx, MCRT_ERR_INVALID_ARG, "max_depth too large");
-    const uint32_t npix = w * h;
+    const uint32_t npix = (uint32_t)total;
+    if (views) {
+        w = npix;
+        h = 1;
+    }
     const bool keep = (o.flags & MCRT_RENDER_KEEP_ACCUM) != 0;
     if (keep && (!ctx->acc_valid || ctx->acc_w != w || ctx->acc_h != h))
         return fail(ctx, MCRT_ERR_INVALID_ARG, "KEEP_ACCUM needs a previous render of the same size");
@@ -669,6 +699,30 @@ mcrt_status mcrt_render(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t 
     CK(cudaMemsetAsync(ctx->counters.p, 0, 256, st), "clear counters");
     mcrt::DeviceScene S = device_scene(ctx);
     const bool want_gbuf = true;
+    // ---- view tables: pixel prefix sums, sizes, cameras
+    if (views) {
+        const size_t off_px = 0, off_wh = ((size_t)(n_views + 1) * 4 + 15) / 16 * 16,
+                     off_cam = off_wh + ((size_t)n_views * 8 + 15) / 16 * 16;
+        std::vector<char> blob(off_cam + (size_t)n_views * sizeof(mcrt_camera_uniform));
+        uint32_t *px = reinterpret_cast<uint32_t *>(blob.data() + off_px);
+        uint32_t acc = 0;
+        for (uint32_t v = 0; v < n_views; ++v) {
+            px[v] = acc;
+            acc += views[v].width * views[v].height;
+            reinterpret_cast<uint32_t *>(blob.data() + off_wh)[2 * v] = views[v].width;
+            reinterpret_cast<uint32_t *>(blob.data() + off_wh)[2 * v + 1] = views[v].height;
+            std::memcpy(blob.data() + off_cam + (size_t)v * sizeof(mcrt_camera_uniform), &views[v].cam,
+                        sizeof(mcrt_camera_uniform));
+        }
+        px[n_views] = acc;
+        if (ctx->view_blob != blob) {
+            CK(ctx->views.ensure(blob.size()), "allocate view table");
+            CK(cudaMemcpyAsync(ctx->views.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, st), "upload views");
+            CK(cudaStreamSynchronize(st), "upload views");
+            ctx->view_blob = blob;
+        }
+        ctx->view_px.assign(px, px + n_views + 1);
+    }
     // ---- passes
     const unsigned long long launches0 = mcrt::launch_count();
     unsigned long long extend_launches = 0;
@@ -677,48 +731,115 @@ mcrt_status mcrt_render(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t 
     cudaEvent_t e_begin = ev(ctx, evi++);
     cudaEventRecord(e_begin, st);
     const bool nee = (o.flags & MCRT_RENDER_NEE) != 0 && (ctx->n_lights > 0 || ctx->has_sun);
-    uint32_t done = 0;
-    bool first_pass = true;
-    while (done < spp) {
+    const bool use_graph = (o.flags & MCRT_RENDER_GRAPH) != 0;
+    auto make_params = [&](uint32_t planes, uint32_t frame0) {
         mcrt::RenderParams P{};
         P.w = w; P.h = h; P.npix = npix;
-        P.spp_pass = std::min(spp_pass, spp - done);
-        P.frame0 = first_frame + done;
+        P.spp_pass = planes;
+        P.frame0 = frame0;
         P.max_depth = depth;
         P.flags = o.flags;
-        P.cam = *cam;
-        const bool last_pass = done + P.spp_pass >= spp;
-        P.gbuf_plane = (want_gbuf && last_pass) ? (int)P.spp_pass - 1 : -1;
+        if (cam) P.cam = *cam;
         P.extend_variant = o.variant ? (int)o.variant - 1 : ctx->extend_variant;
+        if (views) {
+            const size_t off_wh = ((size_t)(n_views + 1) * 4 + 15) / 16 * 16,
+                         off_cam = off_wh + ((size_t)n_views * 8 + 15) / 16 * 16;
+            P.n_views = n_views;
+            P.view_px = ctx->views.as<uint32_t>();
+            P.view_wh = reinterpret_cast<const uint2 *>(ctx->views.as<char>() + off_wh);
+            P.view_cam = reinterpret_cast<const mcrt_camera_uniform *>(ctx->views.as<char>() + off_cam);
+        }
+        return P;
+    };
+    // one pass: raygen, the bounces, resolve (into the accumulation)
+    auto enqueue_pass = [&](const mcrt::RenderParams &P, bool keep_pass, bool timed) {
         mcrt::launch_raygen(S, P, ctx->pb, st);
         int qi = 0;
         for (uint32_t b = 0; b < depth; ++b) {
-            size_t a0 = evi++;
-            cudaEventRecord(ev(ctx, a0), st);
+            size_t a0 = 0, a1 = 0, a2 = 0;
+            if (timed) { a0 = evi++; cudaEventRecord(ev(ctx, a0), st); }
             mcrt::launch_extend(S, P, ctx->pb, qi, st);
             ++extend_launches;
-            size_t a1 = evi++;
-            cudaEventRecord(ev(ctx, a1), st);
+            if (timed) { a1 = evi++; cudaEventRecord(ev(ctx, a1), st); }
             mcrt::launch_shade(S, P, ctx->pb, qi, b, ctx->gbuf.as<float4>(), st);
-            size_t a2 = evi++;
-            cudaEventRecord(ev(ctx, a2), st);
-            marks.push_back({a0, 1});
-            marks.push_back({a1, 2});
+            if (timed) {
+                a2 = evi++;
+                cudaEventRecord(ev(ctx, a2), st);
+                marks.push_back({a0, 1});
+                marks.push_back({a1, 2});
+            }
             if (nee) {
                 mcrt::launch_shadow(S, P, ctx->pb, st);
-                size_t a3 = evi++;
-                cudaEventRecord(ev(ctx, a3), st);
-                marks.push_back({a2, 3});
+                if (timed) {
+                    size_t a3 = evi++;
+                    cudaEventRecord(ev(ctx, a3), st);
+                    marks.push_back({a2, 3});
+                }
             }
             qi ^= 1;
         }
-        size_t r0 = evi++;
-        cudaEventRecord(ev(ctx, r0), st);
-        mcrt::launch_resolve(P, ctx->pb, ctx->mean.as<float4>(), ctx->sum.as<double>(), keep || !first_pass, st);
-        size_t r1 = evi++;
-        cudaEventRecord(ev(ctx, r1), st);
-        marks.push_back({r0, 4});
-        (void)r1;
+        size_t r0 = 0;
+        if (timed) { r0 = evi++; cudaEventRecord(ev(ctx, r0), st); }
+        mcrt::launch_resolve(P, ctx->pb, ctx->mean.as<float4>(), ctx->sum.as<double>(), keep_pass, st);
+        if (timed) {
+            cudaEventRecord(ev(ctx, evi++), st);
+            marks.push_back({r0, 4});
+        }
+    };
+    uint32_t done = 0;
+    bool first_pass = true;
+    // ---- CUDA-graph replay of the full passes: the pass is captured once (per
+    //      configuration) with its frame index and keep flag in device memory;
+    //      a last kernel of the graph advances them for the next replay.
+    const uint32_t full_passes = use_graph ? spp / spp_pass : 0;
+    if (full_passes > 0) {
+        CK(ctx->pass_state.ensure(16), "allocate pass state");
+        mcrt::RenderParams P = make_params(spp_pass, 0);
+        P.gbuf_plane = want_gbuf ? (int)spp_pass - 1 : -1;
+        P.pass_state = ctx->pass_state.as<uint32_t>();
+        // configuration key: everything the captured launches bake in
+        std::vector<char> key(sizeof(S) + sizeof(P) + sizeof(mcrt::PathBuffers) + 3 * sizeof(void *) + 8);
+        {
+            char *k = key.data();
+            std::memcpy(k, &S, sizeof(S)); k += sizeof(S);
+            std::memcpy(k, &P, sizeof(P)); k += sizeof(P);
+            std::memcpy(k, &ctx->pb, sizeof(mcrt::PathBuffers)); k += sizeof(mcrt::PathBuffers);
+            void *bufs[3] = {ctx->mean.p, ctx->sum.p, ctx->gbuf.p};
+            std::memcpy(k, bufs, sizeof(bufs)); k += sizeof(bufs);
+            uint32_t extra[2] = {depth, nee ? 1u : 0u};
+            std::memcpy(k, extra, sizeof(extra));
+        }
+        if (!ctx->graph_exec || ctx->graph_key != key) {
+            if (ctx->graph_exec) { cudaGraphExecDestroy(ctx->graph_exec); ctx->graph_exec = nullptr; }
+            mcrt::prepare_extend_variants();   // occupancy queries outside the capture
+            cudaGraph_t graph = nullptr;
+            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+            enqueue_pass(P, false, false);
+            k_pass_advance<<<1, 1, 0, st>>>(ctx->pass_state.as<uint32_t>(), spp_pass);
+            ::mcrt::note_launch();
+            cudaError_t ce = cudaStreamEndCapture(st, &graph);
+            if (ce != cudaSuccess) return cuda_fail(ctx, ce, "capture render pass");
+            ce = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (ce != cudaSuccess) { ctx->graph_exec = nullptr; return cuda_fail(ctx, ce, "instantiate graph"); }
+            ctx->graph_key = key;
+            ++ctx->graph_captures;
+        }
+        const uint32_t init[2] = {first_frame, keep ? 1u : 0u};
+        CK(cudaMemcpyAsync(ctx->pass_state.p, init, 8, cudaMemcpyHostToDevice, st), "pass state");
+        for (uint32_t k = 0; k < full_passes; ++k) {
+            CK(cudaGraphLaunch(ctx->graph_exec, st), "graph launch");
+            ::mcrt::note_launch();
+        }
+        CK(cudaStreamSynchronize(st), "graph passes");   // the pass state copy above reads host memory
+        done = full_passes * spp_pass;
+        first_pass = false;
+    }
+    while (done < spp) {
+        mcrt::RenderParams P = make_params(std::min(spp_pass, spp - done), first_frame + done);
+        const bool last_pass = done + P.spp_pass >= spp;
+        P.gbuf_plane = (want_gbuf && last_pass) ? (int)P.spp_pass - 1 : -1;
+        enqueue_pass(P, keep || !first_pass, true);
         done += P.spp_pass;
         first_pass = false;
     }
@@ -743,6 +864,17 @@ mcrt_status mcrt_render(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t 
     CK(cudaMemcpy(ctr, ctx->counters.p, 16, cudaMemcpyDeviceToHost), "read counters");
     CK(cudaMemcpy(ctx->last_counts, ctx->pb.stats, 16, cudaMemcpyDeviceToHost), "read counters");
     if (ctr[3]) return fail(ctx, MCRT_ERR_STACK_OVERFLOW, "traversal stack bound reached");
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_render(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t w, uint32_t h, uint32_t spp,
+                        uint32_t first_frame, const mcrt_render_opts *opts, float *out_rgba, double *accum_rgb,
+                        float *out_gbuf) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    mcrt_status s = render_core(ctx, cam, w, h, nullptr, 0, spp, first_frame, opts);
+    if (s != MCRT_OK) return s;
+    cudaStream_t st = ctx->stream;
+    const uint32_t npix = w * h;
     // ---- outputs
     if (out_rgba)
         CK(cudaMemcpyAsync(out_rgba, ctx->mean.p, (size_t)npix * 16, cudaMemcpyDeviceToHost, st), "read image");
@@ -755,6 +887,22 @@ mcrt_status mcrt_render(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t 
     if (out_gbuf)
         CK(cudaMemcpyAsync(out_gbuf, ctx->gbuf.p, (size_t)npix * 16, cudaMemcpyDeviceToHost, st), "read G-buffer");
     CK(cudaStreamSynchronize(st), "render outputs");
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_render_views(mcrt_ctx *ctx, const mcrt_view *views, uint32_t n_views, uint32_t spp,
+                              uint32_t first_frame, const mcrt_render_opts *opts, float *const *out_rgba) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!views) return fail(ctx, MCRT_ERR_INVALID_ARG, "views is NULL");
+    mcrt_status s = render_core(ctx, nullptr, 0, 0, views, n_views, spp, first_frame, opts);
+    if (s != MCRT_OK) return s;
+    if (out_rgba)
+        for (uint32_t v = 0; v < n_views; ++v)
+            if (out_rgba[v])
+                CK(cudaMemcpyAsync(out_rgba[v], ctx->mean.as<float4>() + ctx->view_px[v],
+                                   (size_t)views[v].width * views[v].height * 16, cudaMemcpyDeviceToHost, ctx->stream),
+                   "read view");
+    CK(cudaStreamSynchronize(ctx->stream), "render outputs");
     return MCRT_OK;
 }
 
@@ -990,6 +1138,15 @@ mcrt_status mcrt_read_accum(mcrt_ctx *ctx, float *out_rgba, double *accum_rgb, f
     return MCRT_OK;
 }
 
+mcrt_status mcrt_variant_info(uint32_t variant, uint32_t *out4) {
+    if (!out4 || variant >= (uint32_t)mcrt::extend_variant_count())
+        return fail(nullptr, MCRT_ERR_INVALID_ARG, "variant out of range or out4 NULL");
+    int info[4];
+    mcrt::extend_variant_info((int)variant, info);
+    for (int k = 0; k < 4; ++k) out4[k] = (uint32_t)info[k];
+    return MCRT_OK;
+}
+
 mcrt_status mcrt_autotune(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t w, uint32_t h, uint32_t spp,
                           const mcrt_render_opts *opts, uint32_t *out_variant, float *out_ms) {
     if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
@@ -998,18 +1155,21 @@ mcrt_status mcrt_autotune(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_
     o.flags &= ~(uint32_t)MCRT_RENDER_KEEP_ACCUM;
     const int nv = mcrt::extend_variant_count();
     float best = 0.0f;
-    int best_v = 0;
+    int best_v = -1;
     for (int v = 0; v < nv; ++v) {
         o.variant = (uint32_t)v + 1;
         float t = 0.0f;
-        for (int rep = 0; rep < 2; ++rep) {           // the first run warms caches and occupancy queries
+        bool ok = true;
+        for (int rep = 0; rep < 2 && ok; ++rep) {     // the first run warms caches and occupancy queries
             mcrt_status s = mcrt_render(ctx, cam, w, h, spp, 0, &o, nullptr, nullptr, nullptr);
-            if (s != MCRT_OK) return s;
+            if (s == MCRT_ERR_STACK_OVERFLOW) ok = false;   // stack too short for this scene: not a candidate
+            else if (s != MCRT_OK) return s;
             t = ctx->last_ms[1];
         }
-        if (out_ms && v < 8) out_ms[v] = t;
-        if (v == 0 || t < best) { best = t; best_v = v; }
+        if (out_ms && v < 8) out_ms[v] = ok ? t : -1.0f;
+        if (ok && (best_v < 0 || t < best)) { best = t; best_v = v; }
     }
+    if (best_v < 0) return fail(ctx, MCRT_ERR_STACK_OVERFLOW, "every closest-hit variant overflowed its stack");
     ctx->extend_variant = best_v;
     if (out_variant) *out_variant = (uint32_t)best_v;
     return MCRT_OK;

@@ -73,8 +73,21 @@ struct RenderParams {
     int32_t gbuf_plane;      // plane whose primary hit is stored in the G-buffer (-1: none)
     int32_t extend_variant;  // closest-hit kernel variant (autotuned)
     mcrt_camera_uniform cam;
+    // batched views (n_views > 0): pixel p of the concatenation belongs to view v
+    // with view_px[v] <= p < view_px[v + 1]; its size and camera
+    uint32_t n_views;
+    const uint32_t *view_px;
+    const uint2 *view_wh;
+    const mcrt_camera_uniform *view_cam;
+    // graph replay: [0] frame index of plane 0, [1] keep flag of the resolve,
+    // read from device memory instead of frame0 / the launch argument
+    const uint32_t *pass_state;
 };
 int extend_variant_count();
+// (BVH width, block size, minimum resident blocks, stack depth) of a variant.
+void extend_variant_info(int v, int out[4]);
+// Occupancy queries of every variant; call before capturing launches in a graph.
+void prepare_extend_variants();
 
 // Launchers (render.cu)
 void launch_trace_closest(const DeviceScene &S, const mcrt_ray *rays, uint32_t n, mcrt_hit *hits, bool ref_layout,

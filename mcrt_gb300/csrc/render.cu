@@ -456,11 +456,27 @@ __global__ void k_raygen(DeviceScene S, RenderParams P, PathBuffers B, int keep_
     if (i >= n) return;
     uint32_t k = i / P.npix;
     uint32_t p = i - k * P.npix;
-    uint32_t x = p % P.w, y = p / P.w;
-    uint32_t frame = P.frame0 + k;
-    uint32_t rng = pcg_hash(pcg_hash(x + y * P.w) ^ (frame * 2654435761u));   // path_trace.wgsl:636-637
+    uint32_t frame = (P.pass_state ? P.pass_state[0] : P.frame0) + k;
+    uint32_t x, y, w, h;
+    const mcrt_camera_uniform *cam = &P.cam;
+    if (P.n_views) {                       // the view holding pixel p: largest v with view_px[v] <= p
+        uint32_t lo = 0, hi = P.n_views;
+        while (lo + 1 < hi) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (__ldg(P.view_px + mid) <= p) lo = mid; else hi = mid;
+        }
+        const uint2 wh = __ldg(P.view_wh + lo);
+        const uint32_t lp = p - __ldg(P.view_px + lo);
+        w = wh.x; h = wh.y;
+        x = lp % w; y = lp / w;
+        cam = P.view_cam + lo;
+    } else {
+        w = P.w; h = P.h;
+        x = p % w; y = p / w;
+    }
+    uint32_t rng = pcg_hash(pcg_hash(x + y * w) ^ (frame * 2654435761u));   // path_trace.wgsl:636-637
     f3 o, d;
-    camera_ray(P.cam, x, y, P.w, P.h, rng, &o, &d);
+    camera_ray(*cam, x, y, w, h, rng, &o, &d);
     B.thr[i] = make_float4(1.0f, 1.0f, 1.0f, -1.0f);
     if (!keep_radiance) B.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     B.aux[i] = make_uint4(rng, p, frame, kFlagSpecular);
@@ -483,14 +499,21 @@ __global__ void k_raygen(DeviceScene S, RenderParams P, PathBuffers B, int keep_
 // reference-order walk (spheres_hit); their count is small.
 constexpr int kRefill = 8;
 
-// Occupancy variants (minimum resident blocks of 128 threads per SM: the
-// register budget ptxas must meet); chosen per scene by mcrt_autotune.
-// variants 0-3: compact binary BVH, 4-7: quantised 4-wide BVH, each with 8, 10,
-// 12, 16 resident blocks
+// Closest-hit kernel variants, chosen per scene by mcrt_autotune: BVH width
+// (compact binary or quantised 4-wide), block size, minimum resident blocks per
+// SM (the register budget ptxas must meet) and traversal stack depth (entries
+// of 8 bytes in local memory; a ray that would overflow it raises the overflow
+// flag and the render reports MCRT_ERR_STACK_OVERFLOW, so the autotuner drops
+// a variant whose stack is too short for the scene).
+struct ExtendVariant { int width, block, min_blocks, stack; };
 constexpr int kExtendVariants = 8;
+constexpr ExtendVariant kVariantTable[kExtendVariants] = {
+    {2, 128, 8, 64}, {2, 128, 8, 32}, {2, 128, 12, 32}, {2, 256, 4, 64},
+    {2, 64, 16, 32}, {4, 128, 8, 64}, {4, 128, 8, 32}, {4, 128, 12, 32}};
 
 // Visit an internal node of the compact binary layout: test both children,
 // continue with the nearer hit child, push the farther one.
+template <int STACK>
 __device__ __forceinline__ void visit_compact2(const DeviceScene &S, const RayInv &r, float tmax, uint32_t *cur,
                                                float *cur_t, uint2 *stack, uint32_t *sp, uint32_t *overflow) {
     const float4 *np = S.cnodes + 4ull * *cur;
@@ -503,7 +526,7 @@ __device__ __forceinline__ void visit_compact2(const DeviceScene &S, const RayIn
         uint32_t near = e.x, far = e.y;
         float tnear = tl, tfar = tr;
         if (tr < tl) { near = e.y; far = e.x; tnear = tr; tfar = tl; }
-        if (*sp < kStackSize) stack[(*sp)++] = make_uint2(far, __float_as_uint(tfar));
+        if (*sp < (uint32_t)STACK) stack[(*sp)++] = make_uint2(far, __float_as_uint(tfar));
         else *overflow = 1u;
         *cur = near;
         *cur_t = tnear;
@@ -521,6 +544,7 @@ __device__ __forceinline__ void visit_compact2(const DeviceScene &S, const RayIn
 // exact box), slab-test, order the hits by entry distance with a sorting
 // network on (distance bits, child) keys, continue with the nearest and push
 // the others farthest first.
+template <int STACK>
 __device__ __forceinline__ void visit_wide4(const DeviceScene &S, const RayInv &r, float tmax, uint32_t *cur,
                                             float *cur_t, uint2 *stack, uint32_t *sp, uint32_t *overflow) {
     const uint4 *np = S.wnodes + 4ull * *cur;
@@ -558,7 +582,7 @@ __device__ __forceinline__ void visit_wide4(const DeviceScene &S, const RayInv &
 #pragma unroll
     for (int j = 3; j >= 1; --j) {
         if (key[j] == 0xffffffffu) continue;
-        if (*sp < kStackSize) stack[(*sp)++] = make_uint2(ref_of(key[j]), key[j] & ~3u);
+        if (*sp < (uint32_t)STACK) stack[(*sp)++] = make_uint2(ref_of(key[j]), key[j] & ~3u);
         else *overflow = 1u;
     }
     if (key[0] == 0xffffffffu) {
@@ -569,8 +593,8 @@ __device__ __forceinline__ void visit_wide4(const DeviceScene &S, const RayInv &
     }
 }
 
-template <int WIDTH, int MINB>
-__global__ void __launch_bounds__(128, MINB) k_extend(DeviceScene S, PathBuffers B, int qi) {
+template <int WIDTH, int BLOCK, int MINB, int STACK>
+__global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffers B, int qi) {
     const uint32_t n = B.counters[qi];
     if (blockIdx.x == 0 && threadIdx.x == 0) { B.counters[qi ^ 1] = 0; B.counters[2] = 0; }
     const float4 *qo = B.q_o[qi];
@@ -581,7 +605,7 @@ __global__ void __launch_bounds__(128, MINB) k_extend(DeviceScene S, PathBuffers
     bool exhausted = false;           // the queue has been handed out (warp-uniform)
     RayInv r;
     Closest best;
-    uint2 stack[kStackSize];
+    uint2 stack[STACK];
     uint32_t sp = 0;
     uint32_t cur = kNoChild;          // next node code to visit
     float cur_t = 0.0f;               // its entry distance
@@ -645,8 +669,8 @@ __global__ void __launch_bounds__(128, MINB) k_extend(DeviceScene S, PathBuffers
                     continue;
                 }
                 ++nn;
-                if (WIDTH == 4) visit_wide4(S, r, best.t, &cur, &cur_t, stack, &sp, B.counters + 3);
-                else visit_compact2(S, r, best.t, &cur, &cur_t, stack, &sp, B.counters + 3);
+                if (WIDTH == 4) visit_wide4<STACK>(S, r, best.t, &cur, &cur_t, stack, &sp, B.counters + 3);
+                else visit_compact2<STACK>(S, r, best.t, &cur, &cur_t, stack, &sp, B.counters + 3);
                 if (__all_sync(__activemask(), leaf != kNoChild)) break;
             }
             // ---- leaf phase
@@ -994,12 +1018,14 @@ __global__ void __launch_bounds__(128) k_shadow(DeviceScene S, PathBuffers B, Ad
 __global__ void k_resolve(RenderParams P, PathBuffers B, float4 *mean, double *sum, int keep) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P.npix) return;
+    if (P.pass_state) keep = (int)P.pass_state[1];
+    const uint32_t frame0 = P.pass_state ? P.pass_state[0] : P.frame0;
     float4 m = keep ? mean[p] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     double s0 = keep ? sum[3 * (size_t)p] : 0.0, s1 = keep ? sum[3 * (size_t)p + 1] : 0.0,
            s2 = keep ? sum[3 * (size_t)p + 2] : 0.0;
     for (uint32_t k = 0; k < P.spp_pass; ++k) {
         float4 s = B.L[(size_t)k * P.npix + p];
-        uint32_t frame = P.frame0 + k;
+        uint32_t frame = frame0 + k;
         float w = 1.0f / (float)(min(frame, kMaxFrameCount) + 1u);
         float omw = 1.0f - w;
         m.x = m.x * omw + s.x * w;
@@ -1103,20 +1129,42 @@ void launch_raygen(const DeviceScene &S, const RenderParams &P, PathBuffers &B, 
 
 int extend_variant_count() { return kExtendVariants; }
 
+namespace {
+using ExtendKernel = void (*)(DeviceScene, PathBuffers, int);
+#define MCRT_EXTEND_KERNEL(i)                                                                            \
+    k_extend<kVariantTable[i].width, kVariantTable[i].block, kVariantTable[i].min_blocks, kVariantTable[i].stack>
+const ExtendKernel kExtendKernels[kExtendVariants] = {MCRT_EXTEND_KERNEL(0), MCRT_EXTEND_KERNEL(1),
+                                                      MCRT_EXTEND_KERNEL(2), MCRT_EXTEND_KERNEL(3),
+                                                      MCRT_EXTEND_KERNEL(4), MCRT_EXTEND_KERNEL(5),
+                                                      MCRT_EXTEND_KERNEL(6), MCRT_EXTEND_KERNEL(7)};
+#undef MCRT_EXTEND_KERNEL
+int g_extend_per_sm[kExtendVariants] = {0, 0, 0, 0, 0, 0, 0, 0};
+}  // namespace
+
+void extend_variant_info(int v, int out[4]) {
+    const ExtendVariant &e = kVariantTable[(v >= 0 && v < kExtendVariants) ? v : 0];
+    out[0] = e.width; out[1] = e.block; out[2] = e.min_blocks; out[3] = e.stack;
+}
+
+// Resident blocks per SM of every variant (an occupancy query, made before any
+// stream capture of a render).
+void prepare_extend_variants() {
+    for (int v = 0; v < kExtendVariants; ++v)
+        if (g_extend_per_sm[v] == 0) {
+            int n = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kExtendKernels[v], kVariantTable[v].block, 0);
+            g_extend_per_sm[v] = n > 0 ? n : 1;
+        }
+}
+
 void launch_extend(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, cudaStream_t st) {
-    using Kern = void (*)(DeviceScene, PathBuffers, int);
-    static const Kern kernels[kExtendVariants] = {k_extend<2, 8>, k_extend<2, 10>, k_extend<2, 12>, k_extend<2, 16>,
-                                                  k_extend<4, 8>, k_extend<4, 10>, k_extend<4, 12>, k_extend<4, 16>};
-    static int per_sm[kExtendVariants] = {0, 0, 0, 0, 0, 0, 0, 0};
     const int v = (P.extend_variant >= 0 && P.extend_variant < kExtendVariants) ? P.extend_variant : 0;
+    prepare_extend_variants();
     // persistent: as many resident blocks as fit, never more warps than rays
-    if (per_sm[v] == 0) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[v], kernels[v], 128, 0);
-        if (per_sm[v] <= 0) per_sm[v] = 1;
-    }
+    const int block = kVariantTable[v].block;
     uint32_t nmax = P.npix * P.spp_pass;
-    int blocks = min(grid_blocks_for(nmax, 128), sm_count() * per_sm[v]);
-    kernels[v]<<<blocks, 128, 0, st>>>(S, B, qi); ::mcrt::note_launch();
+    int blocks = min(grid_blocks_for(nmax, block), sm_count() * g_extend_per_sm[v]);
+    kExtendKernels[v]<<<blocks, block, 0, st>>>(S, B, qi); ::mcrt::note_launch();
 }
 
 void launch_shade(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, uint32_t bounce,

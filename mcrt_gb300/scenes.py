@@ -183,6 +183,28 @@ def voxel_world(seed: int = 1234, nx: int = 256, ny: int = 128, nz: int = 256):
                 spp=8, max_depth=6, denoise=dict(radius=2, sigma_color=0.1, sigma_normal=0.2))
 
 
+def world_views(world, seed: int = 1234, n: int = 16):
+    """Seeded camera poses over a voxel world (the batched workload): n views of
+    distinct, uneven sizes in [256, 1920] x [256, 1080], each looking from above
+    the terrain at a point near the centre."""
+    rng = np.random.default_rng(seed)
+    p, s = world["params"], world["voxel_size"]
+    ext_x, ext_y, ext_z = p["nx"] * s, p["ny"] * s, p["nz"] * s
+    out, seen = [], set()
+    while len(out) < n:
+        w, h = int(rng.integers(256, 1921)), int(rng.integers(256, 1081))
+        if (w, h) in seen:
+            continue
+        seen.add((w, h))
+        ang = rng.uniform(0.0, 2.0 * np.pi)
+        r = rng.uniform(0.25, 0.48) * ext_x
+        look_from = [r * np.cos(ang), rng.uniform(0.75, 1.0) * ext_y, r * np.sin(ang) * ext_z / ext_x]
+        look_at = [rng.uniform(-0.2, 0.2) * ext_x, rng.uniform(0.3, 0.5) * ext_y, rng.uniform(-0.2, 0.2) * ext_z]
+        out.append(dict(width=w, height=h, look_from=[float(v) for v in look_from],
+                        look_at=[float(v) for v in look_at], vfov=float(rng.uniform(40.0, 70.0))))
+    return out
+
+
 def icosphere(level: int):
     """Unit icosphere: (positions float64 (n,3), triangles int64 (m,3)), 20*4**level faces."""
     t = (1.0 + 5.0 ** 0.5) / 2.0

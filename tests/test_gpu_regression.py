@@ -171,9 +171,10 @@ def test_autotuned_variants_are_bit_identical(ctx):
     cam = M.compute_camera(64, 48, c["look_from"], c["look_at"], c["vfov"], 0.0)
     ctx.upload_scene(vertices=sc["vertices"], triangles=sc["triangles"], materials=sc["materials"], env=sc["env"])
     v, ms = ctx.autotune(cam, 64, 48, 2, max_depth=12)
-    assert 0 <= v < len(ms) and len(ms) >= 2
+    assert 0 <= v < len(ms) and len(ms) == 8 and ms[v] > 0
+    assert {M.variant_info(k)["width"] for k in range(8)} == {2, 4}
     imgs = []
-    for k in range(len(ms)):
+    for k in [k for k in range(len(ms)) if ms[k] > 0]:
         o = M._native.RenderOpts(max_depth=12, variant=k + 1)
         rgba = np.zeros((48, 64, 4), np.float32)
         import ctypes
