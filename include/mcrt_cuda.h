@@ -316,6 +316,17 @@ mcrt_status mcrt_world_mesh(mcrt_ctx *ctx, uint32_t mode, const uint32_t *block_
 mcrt_status mcrt_world_read_mesh(mcrt_ctx *ctx, mcrt_gpu_vertex *vertices, uint32_t vertex_capacity,
                                  mcrt_gpu_triangle *triangles, uint32_t triangle_capacity);
 
+/* ------------------------------------------------------------------ radiance-cache MLP */
+
+/* Probe of one tensor-core product (no reference counterpart; it pins the
+ * operand layouts of the MLP kernels): D[128 x N] = A[128 x K] * B[N x K]^T with
+ * A, B bf16 bit patterns in row-major host arrays and D f32, computed by
+ * tcgen05.mma with the operands staged K-major or, with flags bit 0 / bit 1,
+ * MN-major (as the backward pass reads its tiles).  K in {16, 32, 48, 64},
+ * N in {16, 32, 48, 64}. */
+mcrt_status mcrt_mlp_gemm_probe(int device, const uint16_t *A, const uint16_t *B, uint32_t K, uint32_t N,
+                                uint32_t flags, float *D);
+
 /* ------------------------------------------------------------------ differentiation */
 
 /* Replace the material table of the uploaded scene (GpuMaterialData,

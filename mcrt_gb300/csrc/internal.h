@@ -35,6 +35,8 @@ struct DBuf {
 // site calls note_launch()); reported per call by mcrt_last_timings.
 void note_launch();
 unsigned long long launch_count();
+// Error message of calls that have no context (mcrt_last_error(NULL)).
+void set_global_error(const std::string &msg);
 
 struct DeviceScene;
 
