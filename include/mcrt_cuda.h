@@ -327,6 +327,32 @@ mcrt_status mcrt_world_read_mesh(mcrt_ctx *ctx, mcrt_gpu_vertex *vertices, uint3
 mcrt_status mcrt_mlp_gemm_probe(int device, const uint16_t *A, const uint16_t *B, uint32_t K, uint32_t N,
                                 uint32_t flags, float *D);
 
+/* Radiance cache (no reference counterpart): a small MLP predicting the
+ * radiance scattered from a surface point towards a direction.  Inputs per
+ * query, 12 floats: position p, outgoing direction w_o (towards the previous
+ * vertex), shading normal n, albedo a.  Encoding (96 features): u = clamp((p -
+ * lo) / (hi - lo), 0, 1); sin and cos of u * pi * 2^k for k = 0..11 per axis;
+ * w_o, n, a, u; zeros.  Network: 5 hidden layers of 64 ReLU units, 3 linear
+ * outputs; bf16 weights and activations on the tensor cores, fp32
+ * accumulation, fp32 master parameters (mcrt_cache_param_count floats: W_l
+ * row-major [out][in] then b_l per layer; the output layer is stored 16 wide,
+ * rows 3..15 zero).  Training: relative L2 loss (y - t)^2 / (y^2 + 0.01) with y
+ * held fixed in the denominator, averaged over samples and channels, Adam
+ * (beta1 0.9, beta2 0.99, eps 1e-8). */
+uint32_t mcrt_cache_param_count(void);
+mcrt_status mcrt_cache_init(mcrt_ctx *ctx, uint32_t seed);              /* He-uniform weights, zero biases */
+mcrt_status mcrt_cache_set_params(mcrt_ctx *ctx, const float *params);  /* also resets the Adam moments */
+mcrt_status mcrt_cache_get_params(mcrt_ctx *ctx, float *out);
+mcrt_status mcrt_cache_set_bounds(mcrt_ctx *ctx, const float *lo3, const float *hi3);
+/* out: n x 3 predictions for n x 12 queries (host). */
+mcrt_status mcrt_cache_infer(mcrt_ctx *ctx, const float *queries, uint32_t n, float *out);
+/* samples: n x 16 (query 12, target 3, weight 0 or 1).  `steps` Adam steps on
+ * consecutive batches of `batch` samples (wrapping); steps = 0 computes the
+ * gradient of the first batch only.  out_loss (optional): the loss sum of each
+ * step; out_grad (optional): the gradient of the first step. */
+mcrt_status mcrt_cache_train(mcrt_ctx *ctx, const float *samples, uint32_t n, uint32_t steps, uint32_t batch,
+                             float lr, float *out_loss, float *out_grad);
+
 /* ------------------------------------------------------------------ differentiation */
 
 /* Replace the material table of the uploaded scene (GpuMaterialData,

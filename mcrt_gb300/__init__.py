@@ -345,6 +345,41 @@ class Context:
         self._last_hw = (1, total)
         return outs
 
+    # ---------------------------------------------------------------- radiance cache
+    def cache_init(self, seed=0):
+        self._check(lib().mcrt_cache_init(self._h, seed))
+
+    def cache_params(self) -> np.ndarray:
+        p = np.zeros(lib().mcrt_cache_param_count(), np.float32)
+        self._check(lib().mcrt_cache_get_params(self._h, ptr(p)))
+        return p
+
+    def cache_set_params(self, params):
+        p = np.ascontiguousarray(params, np.float32)
+        assert p.size == lib().mcrt_cache_param_count()
+        self._check(lib().mcrt_cache_set_params(self._h, ptr(p)))
+
+    def cache_set_bounds(self, lo, hi):
+        lo = np.ascontiguousarray(lo, np.float32)
+        hi = np.ascontiguousarray(hi, np.float32)
+        self._check(lib().mcrt_cache_set_bounds(self._h, ptr(lo), ptr(hi)))
+
+    def cache_infer(self, queries) -> np.ndarray:
+        """Predictions (n, 3) for (n, 12) queries: position, outgoing direction, normal, albedo."""
+        q = np.ascontiguousarray(queries, np.float32).reshape(-1, 12)
+        out = np.zeros((len(q), 3), np.float32)
+        self._check(lib().mcrt_cache_infer(self._h, ptr(q), len(q), ptr(out)))
+        return out
+
+    def cache_train(self, samples, steps=1, batch=0, lr=1e-3, want_grad=False):
+        """Adam steps on (n, 16) samples (query, target, weight); returns (loss per step,
+        gradient of the first step or None).  steps=0: gradient only."""
+        s = np.ascontiguousarray(samples, np.float32).reshape(-1, 16)
+        loss = np.zeros(max(steps, 1), np.float32)
+        grad = np.zeros(lib().mcrt_cache_param_count(), np.float32) if want_grad else None
+        self._check(lib().mcrt_cache_train(self._h, ptr(s), len(s), steps, batch, float(lr), ptr(loss), ptr(grad)))
+        return loss, grad
+
     def update_materials(self, materials):
         """Replace the material table (same emissive slots) without re-uploading geometry."""
         md = _arr(materials, MATERIAL_DATA)

@@ -119,6 +119,13 @@ SIGNATURES = [
     ("mcrt_read_accum", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     ("mcrt_update_materials", c_int, [c_void_p, c_void_p]),
     ("mcrt_mlp_gemm_probe", c_int, [c_int, c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_void_p]),
+    ("mcrt_cache_param_count", c_uint32, []),
+    ("mcrt_cache_init", c_int, [c_void_p, c_uint32]),
+    ("mcrt_cache_set_params", c_int, [c_void_p, c_void_p]),
+    ("mcrt_cache_get_params", c_int, [c_void_p, c_void_p]),
+    ("mcrt_cache_set_bounds", c_int, [c_void_p, c_void_p, c_void_p]),
+    ("mcrt_cache_infer", c_int, [c_void_p, c_void_p, c_uint32, c_void_p]),
+    ("mcrt_cache_train", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_float, c_void_p, c_void_p]),
     ("mcrt_render_views", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, POINTER(RenderOpts), c_void_p]),
     ("mcrt_variant_info", c_int, [c_uint32, c_void_p]),
     ("mcrt_denoise_accum", c_int, [c_void_p, POINTER(DenoiseParams), c_void_p]),

@@ -11,6 +11,7 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include "mlp_net.cuh"
 
 static_assert(sizeof(mcrt_gpu_sphere) == 32, "GpuSphere is 32 bytes (scene.rs:24-29)");
 static_assert(sizeof(mcrt_gpu_bvh_node) == 48, "GpuBvhNode is 48 bytes (bvh.rs:56-68)");
@@ -95,6 +96,8 @@ struct mcrt_ctx {
     std::vector<uint32_t> view_px;
     cudaGraphExec_t graph_exec = nullptr;
     unsigned long long graph_captures = 0;
+    // radiance cache
+    mcrt::CacheState *cache = nullptr;
 };
 
 namespace {
@@ -354,6 +357,7 @@ void mcrt_destroy(mcrt_ctx *ctx) {
                     &ctx->wmesh.triangles, &ctx->views, &ctx->pass_state};
     for (DBuf *b : bufs) b->release();
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    mcrt::cache_destroy(ctx->cache);
     mcrt::free_bvh_scratch(ctx->bvh_scratch);
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
@@ -1244,6 +1248,94 @@ mcrt_status mcrt_denoise(mcrt_ctx *ctx, const float *in_rgba, const float *gbuf,
     float t = 0.0f;
     cudaEventElapsedTime(&t, a, b);
     ctx->last_ms[0] = t;
+    return MCRT_OK;
+}
+
+// ------------------------------------------------------------------ radiance cache
+uint32_t mcrt_cache_param_count(void) { return (uint32_t)mcrt::mlp::kParams; }
+
+static mcrt::CacheState *cache_of(mcrt_ctx *ctx) {
+    if (!ctx->cache) ctx->cache = mcrt::cache_create();
+    return ctx->cache;
+}
+
+mcrt_status mcrt_cache_set_params(mcrt_ctx *ctx, const float *params) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!params) return fail(ctx, MCRT_ERR_INVALID_ARG, "params is NULL");
+    for (int p = 0; p < mcrt::mlp::kParams; ++p)
+        if (!std::isfinite(params[p])) return fail(ctx, MCRT_ERR_INVALID_ARG, "parameters must be finite");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    CK(mcrt::cache_set_params(cache_of(ctx), params, ctx->stream), "cache parameters");
+    CK(cudaStreamSynchronize(ctx->stream), "cache parameters");
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_cache_init(mcrt_ctx *ctx, uint32_t seed) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    // He-uniform weights U(-sqrt(6 / fan_in), +) from a PCG stream, zero biases,
+    // output rows 3..15 zero
+    std::vector<float> p(mcrt::mlp::kParams, 0.0f);
+    uint32_t state = seed * 2654435761u + 12345u;
+    for (int l = 0; l < mcrt::mlp::kLayers; ++l) {
+        const int nin = mcrt::mlp::in_of(l), nout = mcrt::mlp::out_of(l);
+        const double bound = std::sqrt(6.0 / (double)nin);
+        for (int o = 0; o < nout; ++o)
+            for (int i = 0; i < nin; ++i) {
+                state = mcrt::pcg_hash(state);
+                const double u = (double)(state >> 8) / 16777216.0;
+                const bool live = l < mcrt::mlp::kLayers - 1 || o < mcrt::mlp::kOut;
+                p[mcrt::mlp::w_off(l) + o * nin + i] = live ? (float)((2.0 * u - 1.0) * bound) : 0.0f;
+            }
+    }
+    return mcrt_cache_set_params(ctx, p.data());
+}
+
+mcrt_status mcrt_cache_get_params(mcrt_ctx *ctx, float *out) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!out) return fail(ctx, MCRT_ERR_INVALID_ARG, "out is NULL");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaError_t e = mcrt::cache_get_params(cache_of(ctx), out, ctx->stream);
+    if (e == cudaErrorInvalidValue) return fail(ctx, MCRT_ERR_INVALID_ARG, "cache parameters not set");
+    CK(e, "cache parameters");
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_cache_set_bounds(mcrt_ctx *ctx, const float *lo3, const float *hi3) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!lo3 || !hi3) return fail(ctx, MCRT_ERR_INVALID_ARG, "bounds are NULL");
+    for (int a = 0; a < 3; ++a)
+        if (!std::isfinite(lo3[a]) || !std::isfinite(hi3[a]) || !(hi3[a] > lo3[a]))
+            return fail(ctx, MCRT_ERR_INVALID_ARG, "bounds must be finite with hi > lo");
+    mcrt::cache_set_bounds(cache_of(ctx), lo3, hi3);
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_cache_infer(mcrt_ctx *ctx, const float *queries, uint32_t n, float *out) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!queries || !out || n == 0 || n > (1u << 24))
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "queries / out NULL or n out of [1, 2^24]");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    bool timed_out = false;
+    cudaError_t e = mcrt::cache_infer_host(cache_of(ctx), queries, n, out, ctx->stream, &timed_out);
+    if (e == cudaErrorInvalidValue) return fail(ctx, MCRT_ERR_INVALID_ARG, "cache parameters not set");
+    CK(e, "cache inference");
+    if (timed_out) return fail(ctx, MCRT_ERR_TIMEOUT, "tensor-core product did not complete");
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_cache_train(mcrt_ctx *ctx, const float *samples, uint32_t n, uint32_t steps, uint32_t batch,
+                             float lr, float *out_loss, float *out_grad) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!samples || n == 0 || n > (1u << 24))
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "samples NULL or n out of [1, 2^24]");
+    if (!(lr >= 0.0f) || !std::isfinite(lr)) return fail(ctx, MCRT_ERR_INVALID_ARG, "lr must be >= 0");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    bool timed_out = false;
+    cudaError_t e = mcrt::cache_train_host(cache_of(ctx), samples, n, steps, batch, lr, out_loss, out_grad,
+                                           ctx->stream, &timed_out);
+    if (e == cudaErrorInvalidValue) return fail(ctx, MCRT_ERR_INVALID_ARG, "cache parameters not set");
+    CK(e, "cache training");
+    if (timed_out) return fail(ctx, MCRT_ERR_TIMEOUT, "tensor-core product did not complete");
     return MCRT_OK;
 }
 

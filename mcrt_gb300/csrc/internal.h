@@ -35,6 +35,8 @@ struct DBuf {
 // site calls note_launch()); reported per call by mcrt_last_timings.
 void note_launch();
 unsigned long long launch_count();
+// Streaming multiprocessors of the current device (cached).
+int sm_count();
 // Error message of calls that have no context (mcrt_last_error(NULL)).
 void set_global_error(const std::string &msg);
 
@@ -135,6 +137,22 @@ void launch_world_generate(const mcrt_world_params &P, uint8_t *vox, cudaStream_
 // quad per visible face) into M.vertices / M.triangles (4 and 2 per quad).
 cudaError_t world_mesh(const uint8_t *d_vox, uint32_t nx, uint32_t ny, uint32_t nz, int32_t chunk_x0, int32_t chunk_z0,
                        bool greedy, const uint32_t *d_mat_of, float voxel, WorldMeshBuffers &M, cudaStream_t st);
+
+// Radiance-cache MLP (mlp.cu)
+struct CacheState;
+CacheState *cache_create();
+void cache_destroy(CacheState *c);
+void cache_set_bounds(CacheState *c, const float lo[3], const float hi[3]);
+cudaError_t cache_set_params(CacheState *c, const float *host_params, cudaStream_t st);
+cudaError_t cache_get_params(CacheState *c, float *host_params, cudaStream_t st);
+cudaError_t cache_infer_host(CacheState *c, const float *q12, uint32_t n, float *out3, cudaStream_t st,
+                             bool *timed_out);
+cudaError_t cache_train_host(CacheState *c, const float *samples16, uint32_t n, uint32_t steps, uint32_t batch,
+                             float lr, float *out_loss, float *out_grad, cudaStream_t st, bool *timed_out);
+cudaError_t cache_infer_device(CacheState *c, const float4 *q, const uint32_t *d_count, uint32_t max_n, float *out,
+                               float4 *L, const float4 *thr, cudaStream_t st);
+cudaError_t cache_step_device(CacheState *c, const float *d_samples, uint32_t n, uint32_t n_valid, float lr,
+                              cudaStream_t st);
 
 // Denoiser (denoise.cu)
 void launch_denoise(const float4 *in, const float4 *gbuf, uint32_t w, uint32_t h, const mcrt_denoise_params &p,

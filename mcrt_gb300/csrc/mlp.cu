@@ -4,10 +4,15 @@
 // This file starts with the probe of one tensor-core product, which pins the
 // operand layouts and descriptors of tc.cuh against a CPU product.
 #include <algorithm>
+#include <cmath>
 #include <string>
+#include <vector>
+
+#include <cuda_bf16.h>
 
 #include "common.cuh"
 #include "internal.h"
+#include "mlp_net.cuh"
 #include "tc.cuh"
 
 namespace mcrt {
@@ -66,7 +71,7 @@ __global__ void __launch_bounds__(128) k_gemm_probe(const uint16_t *A, const uin
         }
         tc::commit(mbar);
     }
-    const bool ok = tc::mbar_wait(mbar, 0, kPollLimit);
+    const bool ok = __syncthreads_and(tc::mbar_wait(mbar, 0, kPollLimit) ? 1 : 0) != 0;   // uniform
     tc::fence_after_sync();
     if (!ok) {
         if (t == 0) status[0] = 1u;
@@ -88,6 +93,601 @@ __global__ void __launch_bounds__(128) k_gemm_probe(const uint16_t *A, const uin
 }
 
 }  // namespace
+
+// ============================================================================ radiance-cache MLP
+namespace {
+
+using namespace mlp;
+
+// Device view of the network: bf16 weight image (operand layout, rows = out),
+// fp32 biases (layer l at l * 64), encoding bounds.
+struct NetDev {
+    const uint8_t *img;
+    const float *bias;
+    float lo[3], inv_ext[3];
+};
+
+constexpr uint32_t kSmemImg = 0;
+constexpr uint32_t kSmemBias = kSmemImg + kImgBytes;                       // 47104
+constexpr uint32_t kSmemAct = kSmemBias + kBiasFloats * 4;                 // 48448
+constexpr uint32_t kTileIn = kTile * kIn * 2;                              // 24576
+constexpr uint32_t kTileHid = kTile * kHid * 2;                            // 16384
+// inference: image | bias | one activation tile | mbarrier | TMEM slot
+constexpr uint32_t kInferSmem = kSmemAct + kTileIn + 64;
+// training: image | bias | X0 | H1..H5 | G (128 x 128, upper half zero) | bias grads | misc
+constexpr uint32_t kTrainX0 = kSmemAct;
+constexpr uint32_t kTrainH = kTrainX0 + kTileIn;
+constexpr uint32_t kTrainG = kTrainH + 5 * kTileHid;
+constexpr uint32_t kTrainDb = kTrainG + 2 * kTileHid;
+constexpr uint32_t kTrainMisc = kTrainDb + kBiasFloats * 4;
+constexpr uint32_t kTrainSmem = kTrainMisc + 64;
+static_assert(kTrainSmem <= 227 * 1024, "training kernel shared memory");
+// TMEM columns of the training kernel: forward / backward-data accumulator at
+// 0, weight-gradient accumulators of layer l at kDwCol[l] (in_of(l) columns)
+__device__ constexpr uint32_t kDwCol[kLayers] = {64, 160, 224, 288, 352, 416};
+
+__device__ __forceinline__ uint32_t bf16_bits(float x) {
+    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(x));
+}
+__device__ __forceinline__ float bf16_float(uint32_t b) { return __uint_as_float(b << 16); }
+__device__ __forceinline__ uint32_t pack2(float a, float b) { return bf16_bits(a) | (bf16_bits(b) << 16); }
+// ReLU with a canonical +0 for every non-positive (and NaN) input.
+__device__ __forceinline__ float relu(float x) { return x > 0.0f ? x : 0.0f; }
+
+// Stage the weight image and biases in shared memory (16-byte vector copies).
+__device__ void load_net(const NetDev &net, uint8_t *smem) {
+    const uint4 *src = reinterpret_cast<const uint4 *>(net.img);
+    uint4 *dst = reinterpret_cast<uint4 *>(smem + kSmemImg);
+    for (uint32_t i = threadIdx.x; i < kImgBytes / 16; i += blockDim.x) dst[i] = src[i];
+    float *b = reinterpret_cast<float *>(smem + kSmemBias);
+    for (uint32_t i = threadIdx.x; i < kBiasFloats; i += blockDim.x) b[i] = net.bias[i];
+}
+
+// Encode the query of this thread's row into the input tile (bf16, 12 chunks of 8).
+__device__ void encode_row(const NetDev &net, const float q[12], bool valid, uint8_t *tile, uint32_t row) {
+    float f[kIn];
+    if (valid) encode(q, net.lo, net.inv_ext, f);
+    else for (int k = 0; k < kIn; ++k) f[k] = 0.0f;
+#pragma unroll
+    for (int c = 0; c < kIn / 8; ++c) {
+        uint4 v = make_uint4(pack2(f[8 * c], f[8 * c + 1]), pack2(f[8 * c + 2], f[8 * c + 3]),
+                             pack2(f[8 * c + 4], f[8 * c + 5]), pack2(f[8 * c + 6], f[8 * c + 7]));
+        *reinterpret_cast<uint4 *>(tile + tc::op_offset(row, 8 * c, kTile)) = v;
+    }
+}
+
+// Issue D = A * B for a K-major activation tile A (128 rows) and the K-major
+// weight tile of layer l (rows = out), then commit.  One thread.
+__device__ __forceinline__ void issue_forward(uint32_t d_tmem, const uint8_t *act, const uint8_t *w, int l,
+                                              uint64_t *mbar) {
+    const uint32_t K = in_of(l), N = out_of(l);
+    const uint32_t idesc = tc::idesc_bf16(kTile, N, false, false);
+    for (uint32_t kk = 0; kk < K / 16; ++kk) {
+        uint64_t ad = tc::make_desc(tc::smem_u32(act) + kk * 2u * (kTile / 8) * 128u, (kTile / 8) * 128u, 128u);
+        uint64_t bd = tc::make_desc(tc::smem_u32(w) + kk * 2u * (N / 8) * 128u, (N / 8) * 128u, 128u);
+        tc::mma_bf16(d_tmem, ad, bd, idesc, kk > 0 ? 1u : 0u);
+    }
+    tc::commit(mbar);
+}
+
+// Sync the CTA around shared-memory operand writes and TMEM traffic.
+__device__ __forceinline__ void operand_sync() {
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+}
+
+struct InferIO {
+    const float4 *q;          // 4 float4 per query: p | slot bits, w_o, n, a
+    const uint32_t *count;    // device query count (tracer), or nullptr: n
+    uint32_t n;
+    float4 *L;                // tracer: L[slot] += thr[slot] * y
+    const float4 *thr;
+    float *out;               // host queries: out[3 i + c] = y_c
+};
+
+// Inference over tiles of 128 queries: the five hidden layers and the output
+// layer as tensor-core products with the accumulator in TMEM; the epilogue
+// (bias, ReLU, bf16) writes the next layer's operand in place.
+__global__ void __launch_bounds__(128) k_cache_infer(NetDev net, InferIO io, uint32_t *status) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t *act = smem + kSmemAct;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + kSmemAct + kTileIn);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 1);
+    const float *bias = reinterpret_cast<const float *>(smem + kSmemBias);
+    const uint32_t t = threadIdx.x, warp = t >> 5, row = t;
+    const uint32_t n = io.count ? min(*io.count, io.n) : io.n;
+    load_net(net, smem);
+    if (warp == 0) tc::tmem_alloc(tslot, 64);
+    if (t == 0) tc::mbar_init(mbar, 1);
+    operand_sync();
+    const uint32_t taddr = *tslot;
+    const uint32_t lane_base = (warp * 32u) << 16;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (uint32_t tile = blockIdx.x; ok && tile * kTile < n; tile += gridDim.x) {
+        const uint32_t i = tile * kTile + row;
+        const bool valid = i < n;
+        float q[12];
+        uint32_t slot = 0;
+        if (valid) {
+            float4 a = io.q[4 * (size_t)i], b = io.q[4 * (size_t)i + 1], c = io.q[4 * (size_t)i + 2],
+                   d = io.q[4 * (size_t)i + 3];
+            q[0] = a.x; q[1] = a.y; q[2] = a.z; slot = __float_as_uint(a.w);
+            q[3] = b.x; q[4] = b.y; q[5] = b.z;
+            q[6] = c.x; q[7] = c.y; q[8] = c.z;
+            q[9] = d.x; q[10] = d.y; q[11] = d.z;
+        }
+        encode_row(net, q, valid, act, row);
+        operand_sync();
+        for (int l = 0; l < kLayers; ++l) {
+            if (t == 0) issue_forward(taddr, act, smem + kSmemImg + img_off(l), l, mbar);
+            ok = __syncthreads_and(tc::mbar_wait(mbar, phase & 1u, kPollLimit) ? 1 : 0) != 0;   // uniform
+            ++phase;
+            tc::fence_after_sync();
+            if (!ok) break;
+            if (l < kLayers - 1) {
+                for (uint32_t c = 0; c < (uint32_t)kHid; c += 16) {
+                    float v[16];
+                    tc::tmem_ld16(taddr + lane_base + c, v);
+                    float h[16];
+                    for (int j = 0; j < 16; ++j) h[j] = relu(v[j] + bias[bias_idx(l) + c + j]);
+                    *reinterpret_cast<uint4 *>(act + tc::op_offset(row, c, kTile)) =
+                        make_uint4(pack2(h[0], h[1]), pack2(h[2], h[3]), pack2(h[4], h[5]), pack2(h[6], h[7]));
+                    *reinterpret_cast<uint4 *>(act + tc::op_offset(row, c + 8, kTile)) =
+                        make_uint4(pack2(h[8], h[9]), pack2(h[10], h[11]), pack2(h[12], h[13]), pack2(h[14], h[15]));
+                }
+                operand_sync();
+            } else {
+                float v[16];
+                tc::tmem_ld16(taddr + lane_base, v);
+                const float y0 = v[0] + bias[bias_idx(l)], y1 = v[1] + bias[bias_idx(l) + 1],
+                            y2 = v[2] + bias[bias_idx(l) + 2];
+                if (valid) {
+                    if (io.out) {
+                        io.out[3 * (size_t)i] = y0;
+                        io.out[3 * (size_t)i + 1] = y1;
+                        io.out[3 * (size_t)i + 2] = y2;
+                    } else {
+                        const float4 th = io.thr[slot];
+                        float4 L = io.L[slot];
+                        io.L[slot] = make_float4(L.x + th.x * fmaxf(y0, 0.0f), L.y + th.y * fmaxf(y1, 0.0f),
+                                                 L.z + th.z * fmaxf(y2, 0.0f), L.w);
+                    }
+                }
+                tc::fence_before_sync();
+                __syncthreads();
+                tc::fence_after_sync();
+            }
+        }
+    }
+    if (!ok && t == 0) atomicExch(status, 1u);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::tmem_dealloc(taddr, 64);
+        tc::tmem_relinquish();
+    }
+}
+
+struct TrainIO {
+    const float *samples;     // 16 floats per sample: query (12), target (3), weight (0 or 1)
+    uint32_t n;
+    float loss_scale;         // 1 / (3 * valid samples)
+    float *partial;           // per CTA: kParams floats (weight and bias gradients)
+    float *loss;              // per CTA: sum of the relative L2 terms
+};
+
+// One training step's gradients.  Per tile of 128 samples: forward with every
+// layer's output kept in shared memory; relative L2 loss (y - t)^2 / (y^2 + 0.01)
+// with y held fixed in the denominator; then per layer from the output down:
+//   dW_l += G^T * H_l     (tensor cores; G and H_l read as MN-major operands,
+//                          G's rows padded to 128 with zeros; the sums stay in
+//                          TMEM across the CTA's tiles)
+//   G    <- (G * W_l) .* [H_l > 0]    (tensor cores; W_l read MN-major)
+// Bias gradients are column sums of G (shared-memory atomics).  At the end the
+// CTA writes its partial gradients; k_cache_reduce sums them in a fixed order.
+__global__ void __launch_bounds__(128, 1) k_cache_train(NetDev net, TrainIO io, uint32_t *status) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t *x0 = smem + kTrainX0;
+    uint8_t *G = smem + kTrainG;
+    float *dbias = reinterpret_cast<float *>(smem + kTrainDb);
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + kTrainMisc);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + kTrainMisc + 8);
+    float *loss_acc = reinterpret_cast<float *>(smem + kTrainMisc + 16);
+    const float *bias = reinterpret_cast<const float *>(smem + kSmemBias);
+    auto H = [&](int l) { return smem + kTrainH + (uint32_t)(l - 1) * kTileHid; };   // input of layer l >= 1
+    const uint32_t t = threadIdx.x, warp = t >> 5, row = t;
+    load_net(net, smem);
+    for (uint32_t k = t; k < 2 * kTileHid / 16; k += blockDim.x) reinterpret_cast<uint4 *>(G)[k] = make_uint4(0, 0, 0, 0);
+    for (uint32_t k = t; k < (uint32_t)kBiasFloats; k += blockDim.x) dbias[k] = 0.0f;
+    if (t == 0) *loss_acc = 0.0f;
+    if (warp == 0) tc::tmem_alloc(tslot, 512);
+    if (t == 0) tc::mbar_init(mbar, 1);
+    operand_sync();
+    const uint32_t taddr = *tslot;
+    const uint32_t lane_base = (warp * 32u) << 16;
+    uint32_t phase = 0;
+    bool ok = true, first = true;
+    for (uint32_t tile = blockIdx.x; ok && tile * kTile < io.n; tile += gridDim.x) {
+        const uint32_t i = tile * kTile + row;
+        const float *s = io.samples + 16 * (size_t)min(i, io.n - 1);
+        const float wgt = i < io.n ? s[15] : 0.0f;
+        float q[12];
+        for (int k = 0; k < 12; ++k) q[k] = s[k];
+        const float tg0 = s[12], tg1 = s[13], tg2 = s[14];
+        encode_row(net, q, wgt > 0.0f, x0, row);
+        operand_sync();
+        // ---- forward
+        for (int l = 0; l < kLayers && ok; ++l) {
+            const uint8_t *in = l == 0 ? x0 : H(l);
+            if (t == 0) issue_forward(taddr, in, smem + kSmemImg + img_off(l), l, mbar);
+            ok = __syncthreads_and(tc::mbar_wait(mbar, phase & 1u, kPollLimit) ? 1 : 0) != 0;   // uniform
+            ++phase;
+            tc::fence_after_sync();
+            if (!ok) break;
+            if (l < kLayers - 1) {
+                uint8_t *out = H(l + 1);
+                for (uint32_t c = 0; c < (uint32_t)kHid; c += 16) {
+                    float v[16], h[16];
+                    tc::tmem_ld16(taddr + lane_base + c, v);
+                    for (int j = 0; j < 16; ++j) h[j] = relu(v[j] + bias[bias_idx(l) + c + j]);
+                    *reinterpret_cast<uint4 *>(out + tc::op_offset(row, c, kTile)) =
+                        make_uint4(pack2(h[0], h[1]), pack2(h[2], h[3]), pack2(h[4], h[5]), pack2(h[6], h[7]));
+                    *reinterpret_cast<uint4 *>(out + tc::op_offset(row, c + 8, kTile)) =
+                        make_uint4(pack2(h[8], h[9]), pack2(h[10], h[11]), pack2(h[12], h[13]), pack2(h[14], h[15]));
+                }
+            } else {
+                float v[16];
+                tc::tmem_ld16(taddr + lane_base, v);
+                const float y[3] = {v[0] + bias[bias_idx(l)], v[1] + bias[bias_idx(l) + 1],
+                                    v[2] + bias[bias_idx(l) + 2]};
+                const float tg[3] = {tg0, tg1, tg2};
+                float g[3], lsum = 0.0f;
+                for (int c = 0; c < 3; ++c) {
+                    const float e = y[c] - tg[c], den = y[c] * y[c] + 0.01f;
+                    lsum += wgt * ((e * e) / den);
+                    g[c] = bf16_float(bf16_bits(wgt * (2.0f * e / den) * io.loss_scale));
+                }
+                atomicAdd(loss_acc, lsum);
+                for (int c = 0; c < 3; ++c) atomicAdd(&dbias[bias_idx(l) + c], g[c]);
+                *reinterpret_cast<uint4 *>(G + tc::op_offset(row, 0, kTile)) =
+                    make_uint4(pack2(g[0], g[1]), pack2(g[2], 0.0f), 0u, 0u);
+                for (uint32_t c = 8; c < (uint32_t)kHid; c += 8)
+                    *reinterpret_cast<uint4 *>(G + tc::op_offset(row, c, kTile)) = make_uint4(0, 0, 0, 0);
+            }
+            operand_sync();
+        }
+        if (!ok) break;
+        // ---- backward
+        for (int l = kLayers - 1; l >= 0 && ok; --l) {
+            const uint8_t *in = l == 0 ? x0 : H(l);
+            if (t == 0) {
+                // dW_l += G^T * H_l: M = 128 (out rows, zero beyond out_of(l)), N = in_of(l), K = 128 samples
+                const uint32_t idw = tc::idesc_bf16(kTile, in_of(l), true, true);
+                for (uint32_t ks = 0; ks < kTile / 16; ++ks) {
+                    uint64_t ad = tc::make_desc(tc::smem_u32(G) + ks * 256u, 128u, (kTile / 8) * 128u);
+                    uint64_t bd = tc::make_desc(tc::smem_u32(in) + ks * 256u, 128u, (kTile / 8) * 128u);
+                    tc::mma_bf16(taddr + kDwCol[l], ad, bd, idw, (first && ks == 0) ? 0u : 1u);
+                }
+                if (l > 0) {
+                    // G' = G * W_l: M = 128 samples, K = out_of(l), N = in_of(l) = 64
+                    const uint32_t K = out_of(l);
+                    const uint8_t *w = smem + kSmemImg + img_off(l);
+                    const uint32_t idb = tc::idesc_bf16(kTile, kHid, false, true);
+                    for (uint32_t kk = 0; kk < K / 16; ++kk) {
+                        uint64_t ad = tc::make_desc(tc::smem_u32(G) + kk * 2u * (kTile / 8) * 128u,
+                                                    (kTile / 8) * 128u, 128u);
+                        uint64_t bd = tc::make_desc(tc::smem_u32(w) + kk * 256u, 128u, (K / 8) * 128u);
+                        tc::mma_bf16(taddr, ad, bd, idb, kk > 0 ? 1u : 0u);
+                    }
+                }
+                tc::commit(mbar);
+            }
+            ok = __syncthreads_and(tc::mbar_wait(mbar, phase & 1u, kPollLimit) ? 1 : 0) != 0;   // uniform
+            ++phase;
+            tc::fence_after_sync();
+            if (!ok) break;
+            if (l > 0) {
+                const uint8_t *hl = H(l);
+                for (uint32_t c = 0; c < (uint32_t)kHid; c += 16) {
+                    float v[16], g[16];
+                    tc::tmem_ld16(taddr + lane_base + c, v);
+                    const uint4 ha = *reinterpret_cast<const uint4 *>(hl + tc::op_offset(row, c, kTile));
+                    const uint4 hb = *reinterpret_cast<const uint4 *>(hl + tc::op_offset(row, c + 8, kTile));
+                    const uint32_t hw[8] = {ha.x, ha.y, ha.z, ha.w, hb.x, hb.y, hb.z, hb.w};
+                    for (int j = 0; j < 16; ++j) {
+                        const uint32_t hbits = (hw[j >> 1] >> (16 * (j & 1))) & 0xffffu;
+                        g[j] = bf16_float(bf16_bits(hbits != 0u ? v[j] : 0.0f));   // ReLU output > 0 <=> bits != 0
+                        float s = g[j];                                  // column sum over the warp's rows
+                        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+                        if ((t & 31u) == 0) atomicAdd(&dbias[bias_idx(l - 1) + c + j], s);
+                    }
+                    *reinterpret_cast<uint4 *>(G + tc::op_offset(row, c, kTile)) =
+                        make_uint4(pack2(g[0], g[1]), pack2(g[2], g[3]), pack2(g[4], g[5]), pack2(g[6], g[7]));
+                    *reinterpret_cast<uint4 *>(G + tc::op_offset(row, c + 8, kTile)) =
+                        make_uint4(pack2(g[8], g[9]), pack2(g[10], g[11]), pack2(g[12], g[13]), pack2(g[14], g[15]));
+                }
+                operand_sync();
+            }
+        }
+        first = false;
+    }
+    if (!ok && t == 0) atomicExch(status, 1u);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    // ---- partial gradients of this CTA
+    float *part = io.partial + (size_t)blockIdx.x * kParams;
+    for (int l = 0; l < kLayers; ++l) {
+        const uint32_t nin = in_of(l), nout = out_of(l);
+        if (warp * 32u < nout) {                      // TMEM lane = output row
+            const uint32_t o = warp * 32u + (t & 31u);
+            for (uint32_t c = 0; c < nin; c += 16) {
+                float v[16];
+                if (ok && !first) tc::tmem_ld16(taddr + lane_base + kDwCol[l] + c, v);
+                else for (int j = 0; j < 16; ++j) v[j] = 0.0f;
+                if (o < nout)
+                    for (int j = 0; j < 16; ++j) part[w_off(l) + o * nin + c + j] = v[j];
+            }
+        }
+        for (uint32_t o = t; o < nout; o += blockDim.x) part[b_off(l) + o] = dbias[bias_idx(l) + o];
+    }
+    if (t == 0) io.loss[blockIdx.x] = *loss_acc;
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::tmem_dealloc(taddr, 512);
+        tc::tmem_relinquish();
+    }
+}
+
+// grad[p] = sum over CTAs of partial[cta][p], in CTA order.
+__global__ void k_cache_reduce(const float *partial, uint32_t n_cta, const float *loss_part, float *grad,
+                               float *loss_out) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < (uint32_t)kParams) {
+        float s = 0.0f;
+        for (uint32_t c = 0; c < n_cta; ++c) s += partial[(size_t)c * kParams + p];
+        grad[p] = s;
+    }
+    if (p == 0) {
+        float s = 0.0f;
+        for (uint32_t c = 0; c < n_cta; ++c) s += loss_part[c];
+        *loss_out = s;
+    }
+}
+
+__device__ __forceinline__ void param_where(uint32_t p, int *layer, bool *is_bias, uint32_t *o, uint32_t *i) {
+    int l = 0;
+    while (l + 1 < kLayers && p >= (uint32_t)w_off(l + 1)) ++l;
+    *layer = l;
+    const uint32_t r = p - (uint32_t)w_off(l);
+    const uint32_t nw = (uint32_t)(out_of(l) * in_of(l));
+    *is_bias = r >= nw;
+    if (*is_bias) { *o = r - nw; *i = 0; }
+    else { *o = r / in_of(l); *i = r - *o * in_of(l); }
+}
+
+// Adam (Kingma & Ba 2015) on the fp32 parameters; refreshes the bf16 weight
+// image and the bias copy the kernels read.
+__global__ void k_cache_adam(float *params, float *m, float *v, const float *grad, float lr, float beta1, float beta2,
+                             float eps, float bc1, float bc2, uint8_t *img, float *bias) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (uint32_t)kParams) return;
+    const float g = grad[p];
+    const float mi = beta1 * m[p] + (1.0f - beta1) * g;
+    const float vi = beta2 * v[p] + (1.0f - beta2) * (g * g);
+    m[p] = mi;
+    v[p] = vi;
+    const float w = params[p] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+    params[p] = w;
+    int l;
+    bool is_bias;
+    uint32_t o, i;
+    param_where(p, &l, &is_bias, &o, &i);
+    if (is_bias) bias[bias_idx(l) + o] = w;
+    else *reinterpret_cast<uint16_t *>(img + img_off(l) + tc::op_offset(o, i, out_of(l))) = (uint16_t)bf16_bits(w);
+}
+
+// Weight image and bias copy from the fp32 parameters (after they are set).
+__global__ void k_cache_refresh(const float *params, uint8_t *img, float *bias) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (uint32_t)kParams) return;
+    int l;
+    bool is_bias;
+    uint32_t o, i;
+    param_where(p, &l, &is_bias, &o, &i);
+    if (is_bias) bias[bias_idx(l) + o] = params[p];
+    else *reinterpret_cast<uint16_t *>(img + img_off(l) + tc::op_offset(o, i, out_of(l))) = (uint16_t)bf16_bits(params[p]);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------- cache state
+struct CacheState {
+    DBuf params, m, v, img, bias, grad, partial, loss_part, loss, samples, queries, status;
+    uint32_t n_cta_partial = 0;
+    uint64_t step = 0;
+    float lo[3] = {0, 0, 0}, inv_ext[3] = {1, 1, 1};
+    bool has_params = false;
+    bool configured = false;
+};
+
+CacheState *cache_create() { return new CacheState(); }
+void cache_destroy(CacheState *c) {
+    if (!c) return;
+    DBuf *bufs[] = {&c->params, &c->m, &c->v, &c->img, &c->bias, &c->grad, &c->partial, &c->loss_part,
+                    &c->loss, &c->samples, &c->queries, &c->status};
+    for (DBuf *b : bufs) b->release();
+    delete c;
+}
+
+void cache_set_bounds(CacheState *c, const float lo[3], const float hi[3]) {
+    for (int a = 0; a < 3; ++a) {
+        c->lo[a] = lo[a];
+        const float ext = hi[a] - lo[a];
+        c->inv_ext[a] = ext > 0.0f ? 1.0f / ext : 0.0f;
+    }
+}
+
+static NetDev net_of(const CacheState *c) {
+    NetDev n;
+    n.img = c->img.as<uint8_t>();
+    n.bias = c->bias.as<float>();
+    for (int a = 0; a < 3; ++a) { n.lo[a] = c->lo[a]; n.inv_ext[a] = c->inv_ext[a]; }
+    return n;
+}
+
+static cudaError_t ensure_net(CacheState *c) {
+    cudaError_t e;
+    if ((e = c->params.ensure(kParams * 4)) != cudaSuccess) return e;
+    if ((e = c->m.ensure(kParams * 4)) != cudaSuccess) return e;
+    if ((e = c->v.ensure(kParams * 4)) != cudaSuccess) return e;
+    if ((e = c->grad.ensure(kParams * 4)) != cudaSuccess) return e;
+    if ((e = c->img.ensure(kImgBytes)) != cudaSuccess) return e;
+    if ((e = c->bias.ensure(kBiasFloats * 4)) != cudaSuccess) return e;
+    if ((e = c->loss.ensure(16)) != cudaSuccess) return e;
+    if ((e = c->status.ensure(16)) != cudaSuccess) return e;
+    return cudaSuccess;
+}
+
+cudaError_t cache_set_params(CacheState *c, const float *host, cudaStream_t st) {
+    cudaError_t e = ensure_net(c);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(c->params.p, host, kParams * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(c->m.p, 0, kParams * 4, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(c->v.p, 0, kParams * 4, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(c->img.p, 0, kImgBytes, st)) != cudaSuccess) return e;
+    k_cache_refresh<<<(kParams + 255) / 256, 256, 0, st>>>(c->params.as<float>(), c->img.as<uint8_t>(),
+                                                          c->bias.as<float>());
+    note_launch();
+    c->step = 0;
+    c->has_params = true;
+    return cudaGetLastError();
+}
+
+cudaError_t cache_get_params(CacheState *c, float *host, cudaStream_t st) {
+    if (!c->has_params) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemcpyAsync(host, c->params.p, kParams * 4, cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(st);
+}
+
+static cudaError_t check_status(CacheState *c, cudaStream_t st, bool *timed_out) {
+    uint32_t s = 0;
+    cudaError_t e = cudaMemcpyAsync(&s, c->status.p, 4, cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    *timed_out = s != 0;
+    return cudaSuccess;
+}
+
+// Inference over device queries (4 float4 each); either out (host layout) or
+// the tracer's L / thr.
+cudaError_t cache_infer_device(CacheState *c, const float4 *q, const uint32_t *d_count, uint32_t max_n, float *out,
+                               float4 *L, const float4 *thr, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_cache_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    if (max_n == 0) return cudaSuccess;
+    InferIO io{q, d_count, max_n, L, thr, out};
+    const uint32_t tiles = (max_n + kTile - 1) / kTile;
+    const int blocks = (int)std::min<uint32_t>(tiles, (uint32_t)sm_count() * 3u);
+    k_cache_infer<<<blocks, 128, kInferSmem, st>>>(net_of(c), io, c->status.as<uint32_t>());
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t cache_infer_host(CacheState *c, const float *q12, uint32_t n, float *out3, cudaStream_t st,
+                             bool *timed_out) {
+    if (!c->has_params) return cudaErrorInvalidValue;
+    cudaError_t e;
+    if ((e = c->queries.ensure((size_t)n * 64 + (size_t)n * 12)) != cudaSuccess) return e;
+    std::vector<float> q((size_t)n * 16, 0.0f);
+    for (uint32_t i = 0; i < n; ++i) {
+        for (int k = 0; k < 3; ++k) {
+            q[16 * (size_t)i + k] = q12[12 * (size_t)i + k];
+            q[16 * (size_t)i + 4 + k] = q12[12 * (size_t)i + 3 + k];
+            q[16 * (size_t)i + 8 + k] = q12[12 * (size_t)i + 6 + k];
+            q[16 * (size_t)i + 12 + k] = q12[12 * (size_t)i + 9 + k];
+        }
+    }
+    float *d_out = reinterpret_cast<float *>(c->queries.as<char>() + (size_t)n * 64);
+    if ((e = cudaMemcpyAsync(c->queries.p, q.data(), (size_t)n * 64, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return e;
+    if ((e = cudaMemsetAsync(c->status.p, 0, 4, st)) != cudaSuccess) return e;
+    if ((e = cache_infer_device(c, c->queries.as<float4>(), nullptr, n, d_out, nullptr, nullptr, st)) != cudaSuccess)
+        return e;
+    if ((e = cudaMemcpyAsync(out3, d_out, (size_t)n * 12, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    return check_status(c, st, timed_out);
+}
+
+// One optimisation step on n device samples (16 floats each): gradients into
+// c->grad (and the loss into c->loss), then Adam when lr > 0.
+cudaError_t cache_step_device(CacheState *c, const float *d_samples, uint32_t n, uint32_t n_valid, float lr,
+                              cudaStream_t st) {
+    static bool attr = false;
+    cudaError_t e;
+    if (!attr) {
+        if ((e = cudaFuncSetAttribute(k_cache_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem)) !=
+            cudaSuccess)
+            return e;
+        attr = true;
+    }
+    const uint32_t tiles = (n + kTile - 1) / kTile;
+    const uint32_t blocks = std::max(1u, std::min<uint32_t>(tiles, (uint32_t)sm_count()));
+    if ((e = c->partial.ensure((size_t)blocks * kParams * 4)) != cudaSuccess) return e;
+    if ((e = c->loss_part.ensure((size_t)blocks * 4)) != cudaSuccess) return e;
+    TrainIO io{d_samples, n, 1.0f / (3.0f * (float)std::max(n_valid, 1u)), c->partial.as<float>(),
+               c->loss_part.as<float>()};
+    k_cache_train<<<blocks, 128, kTrainSmem, st>>>(net_of(c), io, c->status.as<uint32_t>());
+    note_launch();
+    k_cache_reduce<<<(kParams + 255) / 256, 256, 0, st>>>(c->partial.as<float>(), blocks, c->loss_part.as<float>(),
+                                                          c->grad.as<float>(), c->loss.as<float>());
+    note_launch();
+    if (lr > 0.0f) {
+        ++c->step;
+        const float b1 = 0.9f, b2 = 0.99f;
+        const float bc1 = 1.0f - (float)std::pow((double)b1, (double)c->step);
+        const float bc2 = 1.0f - (float)std::pow((double)b2, (double)c->step);
+        k_cache_adam<<<(kParams + 255) / 256, 256, 0, st>>>(c->params.as<float>(), c->m.as<float>(), c->v.as<float>(),
+                                                            c->grad.as<float>(), lr, b1, b2, 1e-8f, bc1, bc2,
+                                                            c->img.as<uint8_t>(), c->bias.as<float>());
+        note_launch();
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t cache_train_host(CacheState *c, const float *samples16, uint32_t n, uint32_t steps, uint32_t batch,
+                             float lr, float *out_loss, float *out_grad, cudaStream_t st, bool *timed_out) {
+    if (!c->has_params) return cudaErrorInvalidValue;
+    cudaError_t e;
+    if ((e = c->samples.ensure((size_t)n * 64)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(c->samples.p, samples16, (size_t)n * 64, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return e;
+    if ((e = cudaMemsetAsync(c->status.p, 0, 4, st)) != cudaSuccess) return e;
+    if (batch == 0 || batch > n) batch = n;
+    for (uint32_t s = 0; s < std::max(steps, 1u); ++s) {
+        const uint32_t first = (uint32_t)(((uint64_t)s * batch) % n);
+        const uint32_t cnt = std::min(batch, n - first);
+        uint32_t valid = 0;
+        for (uint32_t i = first; i < first + cnt; ++i) valid += samples16[16 * (size_t)i + 15] > 0.0f ? 1u : 0u;
+        if ((e = cache_step_device(c, c->samples.as<float>() + 16 * (size_t)first, cnt, valid, steps ? lr : 0.0f,
+                                   st)) != cudaSuccess)
+            return e;
+        if (out_loss && (e = cudaMemcpyAsync(out_loss + s, c->loss.p, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+            return e;
+        if (s == 0 && out_grad &&
+            (e = cudaMemcpyAsync(out_grad, c->grad.p, kParams * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+            return e;
+    }
+    return check_status(c, st, timed_out);
+}
 
 }  // namespace mcrt
 

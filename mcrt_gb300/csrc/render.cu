@@ -1105,7 +1105,7 @@ void launch_light_cdf(const DeviceScene &S, float *d_cdf, float *d_total, cudaSt
 
 // ------------------------------------------------------------------ launchers
 
-static int sm_count() {
+int sm_count() {
     static int n = 0;
     if (n == 0) {
         int dev = 0;

@@ -135,6 +135,14 @@ uint64_t orc_world_mesh(const uint8_t *voxels, uint32_t nx, uint32_t ny, uint32_
                         int32_t chunk_z0, int greedy, const uint32_t *block_material, float voxel_size,
                         orc_vertex *out_v, orc_triangle *out_t, uint64_t cap_quads);
 
+/* Radiance-cache MLP (mlp.cpp): encoding, forward pass, and the gradient and
+ * loss sum of one training step, with the kernels' bf16 rounding points. */
+void orc_mlp_encode(const float *q12, const float *lo3, const float *inv3, float *out96);
+void orc_mlp_forward(const float *params, const float *lo3, const float *inv3, const float *q12, uint32_t n,
+                     float *out3);
+void orc_mlp_grad(const float *params, const float *lo3, const float *inv3, const float *samples, uint32_t n,
+                  double *grad, double *loss_out);
+
 /* cs_denoise (denoise.wgsl:52-120). */
 void orc_denoise(const float *accum_rgba, const float *gbuf, uint32_t w, uint32_t h,
                  int radius, float sigma_s, float sigma_d, float normal_pow, float *out_rgba);

@@ -283,6 +283,50 @@ def world_mesh(voxels, block_material, voxel_size=0.125, greedy=True, chunk_x0=0
     return verts, tris
 
 
+def _inv_extent(lo, hi):
+    lo = np.asarray(lo, np.float32)
+    ext = np.asarray(hi, np.float32) - lo
+    return lo, np.where(ext > 0, np.float32(1.0) / ext, np.float32(0.0)).astype(np.float32)
+
+
+def mlp_forward(params, lo, hi, queries):
+    """Radiance-cache MLP predictions (n, 3) for (n, 12) queries."""
+    L = lib()
+    L.orc_mlp_forward.restype = None
+    L.orc_mlp_forward.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_uint32, c_void_p]
+    lo32, inv = _inv_extent(lo, hi)
+    p = np.ascontiguousarray(params, np.float32)
+    q = np.ascontiguousarray(queries, np.float32).reshape(-1, 12)
+    out = np.zeros((len(q), 3), np.float32)
+    L.orc_mlp_forward(_p(p), _p(lo32), _p(inv), _p(q), len(q), _p(out))
+    return out
+
+
+def mlp_grad(params, lo, hi, samples):
+    """(gradient (float64, params), loss sum) of one training step on (n, 16) samples."""
+    L = lib()
+    L.orc_mlp_grad.restype = None
+    L.orc_mlp_grad.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_uint32, c_void_p, c_void_p]
+    lo32, inv = _inv_extent(lo, hi)
+    p = np.ascontiguousarray(params, np.float32)
+    s = np.ascontiguousarray(samples, np.float32).reshape(-1, 16)
+    g = np.zeros(len(p), np.float64)
+    loss = np.zeros(1, np.float64)
+    L.orc_mlp_grad(_p(p), _p(lo32), _p(inv), _p(s), len(s), _p(g), _p(loss))
+    return g, float(loss[0])
+
+
+def mlp_encode(query, lo, hi):
+    L = lib()
+    L.orc_mlp_encode.restype = None
+    L.orc_mlp_encode.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p]
+    lo32, inv = _inv_extent(lo, hi)
+    q = np.ascontiguousarray(query, np.float32)
+    out = np.zeros(96, np.float32)
+    L.orc_mlp_encode(_p(q), _p(lo32), _p(inv), _p(out))
+    return out
+
+
 def ggx_dg(alpha, mz, cos_o, cos_i):
     """(d(D G2)/d alpha, D G2) of the GGX lobe."""
     L = lib()

@@ -1,0 +1,97 @@
+"""GPU: the radiance-cache MLP on the tensor cores — forward pass and training
+gradients against the CPU oracle (same bf16 rounding points), and online
+training that fits a smooth radiance field."""
+import numpy as np
+import pytest
+
+import mcrt_gb300 as M
+
+pytestmark = pytest.mark.gpu
+
+LO, HI = np.array([-1.0, -0.5, -2.0], np.float32), np.array([1.0, 1.5, 0.0], np.float32)
+
+
+def _unit(rng, n):
+    v = rng.standard_normal((n, 3))
+    return (v / np.linalg.norm(v, axis=1, keepdims=True)).astype(np.float32)
+
+
+def _queries(rng, n):
+    p = LO + (HI - LO) * rng.uniform(-0.05, 1.05, (n, 3))
+    return np.concatenate([p, _unit(rng, n), _unit(rng, n), rng.uniform(0, 1, (n, 3))], 1).astype(np.float32)
+
+
+def _field(q):
+    """A smooth radiance field of position, direction and albedo."""
+    p, w, a = q[:, 0:3], q[:, 3:6], q[:, 9:12]
+    base = 0.6 + 0.3 * np.sin(2.5 * p[:, 0:1]) * np.cos(1.7 * p[:, 2:3]) + 0.2 * w[:, 1:2]
+    return (base * (0.3 + a)).astype(np.float32)
+
+
+@pytest.fixture
+def cache_ctx():
+    with M.Context(0) as ctx:
+        ctx.cache_set_bounds(LO, HI)
+        ctx.cache_init(seed=7)
+        yield ctx
+
+
+def test_cache_forward_matches_oracle(cache_ctx, oracle):
+    rng = np.random.default_rng(1)
+    q = _queries(rng, 1000)                        # 7 full tiles and a ragged one
+    got = cache_ctx.cache_infer(q)
+    want = oracle.mlp_forward(cache_ctx.cache_params(), LO, HI, q)
+    scale = np.abs(want).max()
+    assert scale > 1e-3
+    assert np.abs(got - want).max() <= 2e-2 * scale, np.abs(got - want).max() / scale
+
+
+def test_cache_gradients_match_oracle(cache_ctx, oracle):
+    rng = np.random.default_rng(2)
+    n = 700
+    q = _queries(rng, n)
+    s = np.zeros((n, 16), np.float32)
+    s[:, :12] = q
+    s[:, 12:15] = _field(q)
+    s[:, 15] = 1.0
+    s[-37:, 15] = 0.0                              # unweighted samples contribute nothing
+    p = cache_ctx.cache_params()
+    loss, grad = cache_ctx.cache_train(s, steps=0, want_grad=True)
+    want, want_loss = oracle.mlp_grad(p, LO, HI, s)
+    assert abs(loss[0] - want_loss) <= 1e-3 * want_loss
+    # per layer: W then b, relative error in norm
+    offs = [0]
+    for l in range(6):
+        nin, nout = (96 if l == 0 else 64), (16 if l == 5 else 64)
+        offs += [offs[-1] + nout * nin, offs[-1] + nout * nin + nout]
+    for a, b in zip(offs[:-1], offs[1:]):
+        ref = want[a:b]
+        if np.linalg.norm(ref) == 0:
+            assert np.all(grad[a:b] == 0)
+            continue
+        assert np.linalg.norm(grad[a:b] - ref) <= 3e-2 * np.linalg.norm(ref), (a, b)
+    # the unused output rows stay exactly zero
+    w5 = grad[offs[10]:offs[11]].reshape(16, 64)
+    assert not w5[3:].any()
+
+
+def test_cache_learns_a_radiance_field(cache_ctx):
+    rng = np.random.default_rng(3)
+    n = 1 << 15
+    q = _queries(rng, n)
+    s = np.zeros((n, 16), np.float32)
+    s[:, :12], s[:, 12:15], s[:, 15] = q, _field(q), 1.0
+    q_test = _queries(rng, 4096)
+    t_test = _field(q_test)
+
+    def rel_err():
+        y = cache_ctx.cache_infer(q_test)
+        return float(np.mean((y - t_test) ** 2 / (t_test ** 2 + 1e-2)))
+
+    before = rel_err()
+    loss, _ = cache_ctx.cache_train(s, steps=400, batch=1 << 14, lr=1e-3)
+    after = rel_err()
+    print("held-out relative L2", before, "->", after, "train loss", loss[0], "->", loss[-1])
+    assert np.all(np.isfinite(loss))
+    assert loss[-1] < 0.1 * loss[0]
+    assert after < 0.1 * before
