@@ -225,12 +225,20 @@ def time_to_relmse(M, ctx, target=1e-3, w=512, h=512, depth=8, ref_spp=4096, max
     ref /= ref_spp
     out = {"workload": f"cornell_box_seed{SEED}_{w}x{h}_depth{depth}", "target_relmse": target,
            "reference": f"NEE {ref_spp} spp, independent frames"}
-    for name, nee in (("plain", False), ("nee", True)):
+    cache_cfg = dict(query_vertex=2, train_stride=16, train_steps=4, train_batch=1 << 14, lr=1e-3)
+    for name, nee, cache in (("plain", False, False), ("nee", True, False), ("cache", True, True)):
         total, ms, rel = 0, 0.0, None
+        if cache:                                    # online training from scratch, timed
+            ctx.cache_config(**cache_cfg)
+            ctx.cache_init(0)
+            for i in range(40):
+                ctx.render(cam, w, h, 4, first_frame=(1 << 21) + 4 * i, max_depth=depth, nee=True, cache=True,
+                           outputs=())
+                ms += ctx.timings()["total_ms"]
         while total < max_spp:
             chunk = max(16, total // 8)
             r = ctx.render(cam, w, h, chunk, first_frame=total, max_depth=depth, nee=nee, keep=total > 0,
-                           outputs=("sum",))
+                           outputs=("sum",), cache=cache)
             ms += ctx.timings()["total_ms"]
             total += chunk
             x = r["sum"] / total
@@ -239,8 +247,10 @@ def time_to_relmse(M, ctx, target=1e-3, w=512, h=512, depth=8, ref_spp=4096, max
                 break
         out[name] = {"spp": total, "ms": round(ms, 2), "relmse": round(rel, 6), "reached": rel <= target,
                      "msamples_per_s": round(w * h * total / (ms / 1000.0) / 1e6, 1)}
-    if out["plain"]["reached"] and out["nee"]["reached"]:
-        out["speedup_nee_vs_plain"] = round(out["plain"]["ms"] / out["nee"]["ms"], 2)
+    out["cache"]["config"] = dict(cache_cfg, warmup="40 passes x 4 spp, in the time")
+    for name in ("nee", "cache"):
+        if out["plain"]["reached"] and out[name]["reached"]:
+            out[f"speedup_{name}_vs_plain"] = round(out["plain"]["ms"] / out[name]["ms"], 2)
     return out
 
 

@@ -191,8 +191,10 @@ enum {
     MCRT_RENDER_NEE = 1u << 0,        /* next-event estimation + MIS (else the reference estimator) */
     MCRT_RENDER_GBUFFER = 1u << 1,    /* keep the primary-hit G-buffer (path_trace.wgsl:593-601) */
     MCRT_RENDER_KEEP_ACCUM = 1u << 2, /* continue the device running mean / f64 sum of the previous call */
-    MCRT_RENDER_GRAPH = 1u << 3       /* replay the passes as one captured CUDA graph (same results; no
+    MCRT_RENDER_GRAPH = 1u << 3,      /* replay the passes as one captured CUDA graph (same results; no
                                          per-kernel timings for the replayed passes) */
+    MCRT_RENDER_CACHE = 1u << 4       /* terminate paths into the radiance cache and train it online
+                                         (mcrt_cache_config); not replayed as a graph */
 };
 
 typedef struct {
@@ -340,6 +342,26 @@ mcrt_status mcrt_mlp_gemm_probe(int device, const uint16_t *A, const uint16_t *B
  * held fixed in the denominator, averaged over samples and channels, Adam
  * (beta1 0.9, beta2 0.99, eps 1e-8). */
 uint32_t mcrt_cache_param_count(void);
+
+/* Rendering with the cache (MCRT_RENDER_CACHE).  In every pass, one path in
+ * `train_stride` slots is a training path: it is traced to full depth and
+ * records each non-emissive vertex (position, w_o, normal, albedo, throughput,
+ * radiance gathered so far); every other path stops at its non-emissive
+ * vertex number `query_vertex` (0 = the primary hit) and adds throughput x the
+ * cache's prediction there, with no next-event sample at that vertex.  After
+ * the pass the training paths' vertices become samples (target = radiance the
+ * path gathered from that vertex on / throughput at it) and `train_steps` Adam
+ * steps of `train_batch` samples run.  lo / hi: the encoding bounds (hi <= lo
+ * on every axis: the scene's bounding box). */
+typedef struct {
+    uint32_t query_vertex;
+    uint32_t train_stride;
+    uint32_t train_steps;
+    uint32_t train_batch;
+    float lr;
+    float lo[3], hi[3];
+} mcrt_cache_params;
+mcrt_status mcrt_cache_config(mcrt_ctx *ctx, const mcrt_cache_params *params);
 mcrt_status mcrt_cache_init(mcrt_ctx *ctx, uint32_t seed);              /* He-uniform weights, zero biases */
 mcrt_status mcrt_cache_set_params(mcrt_ctx *ctx, const float *params);  /* also resets the Adam moments */
 mcrt_status mcrt_cache_get_params(mcrt_ctx *ctx, float *out);

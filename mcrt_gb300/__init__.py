@@ -314,11 +314,11 @@ class Context:
         return hits
 
     def render(self, camera, width, height, spp, first_frame=0, max_depth=0, nee=False, spp_per_pass=0,
-               keep=False, outputs=("rgba", "sum", "gbuf"), graph=False):
+               keep=False, outputs=("rgba", "sum", "gbuf"), graph=False, cache=False):
         cam = _arr(camera, CAMERA)
         o = N.RenderOpts(max_depth=max_depth, flags=(N.RENDER_NEE if nee else 0) |
-                         (N.RENDER_KEEP_ACCUM if keep else 0) | (N.RENDER_GRAPH if graph else 0),
-                         spp_per_pass=spp_per_pass)
+                         (N.RENDER_KEEP_ACCUM if keep else 0) | (N.RENDER_GRAPH if graph else 0) |
+                         (N.RENDER_CACHE if cache else 0), spp_per_pass=spp_per_pass)
         rgba = np.zeros((height, width, 4), np.float32) if "rgba" in outputs else None
         acc = np.zeros((height, width, 3), np.float64) if "sum" in outputs else None
         gb = np.zeros((height, width, 4), np.float32) if "gbuf" in outputs else None
@@ -346,6 +346,16 @@ class Context:
         return outs
 
     # ---------------------------------------------------------------- radiance cache
+    def cache_config(self, query_vertex=1, train_stride=64, train_steps=4, train_batch=1 << 14, lr=1e-3, lo=None,
+                     hi=None):
+        """Rendering with the cache (render(..., cache=True)); lo / hi None: the scene's bounds."""
+        p = N.CacheParams(query_vertex=query_vertex, train_stride=train_stride, train_steps=train_steps,
+                          train_batch=train_batch, lr=lr)
+        if lo is not None:
+            for k in range(3):
+                p.lo[k], p.hi[k] = float(lo[k]), float(hi[k])
+        self._check(lib().mcrt_cache_config(self._h, ctypes.byref(p)))
+
     def cache_init(self, seed=0):
         self._check(lib().mcrt_cache_init(self._h, seed))
 

@@ -66,6 +66,12 @@ class SceneDesc(ctypes.Structure):
                 ("flags", c_uint32), ("sun_dir", c_float * 4), ("sun_irradiance", c_float * 4)]
 
 
+class CacheParams(ctypes.Structure):
+    _fields_ = [("query_vertex", c_uint32), ("train_stride", c_uint32), ("train_steps", c_uint32),
+                ("train_batch", c_uint32), ("lr", c_float), ("lo", c_float * 3), ("hi", c_float * 3)]
+
+
+RENDER_CACHE = 16
 SCENE_WORLD_MESH = 1
 MESH_GREEDY, MESH_FACES = 0, 1
 
@@ -120,6 +126,7 @@ SIGNATURES = [
     ("mcrt_update_materials", c_int, [c_void_p, c_void_p]),
     ("mcrt_mlp_gemm_probe", c_int, [c_int, c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_void_p]),
     ("mcrt_cache_param_count", c_uint32, []),
+    ("mcrt_cache_config", c_int, [c_void_p, POINTER(CacheParams)]),
     ("mcrt_cache_init", c_int, [c_void_p, c_uint32]),
     ("mcrt_cache_set_params", c_int, [c_void_p, c_void_p]),
     ("mcrt_cache_get_params", c_int, [c_void_p, c_void_p]),

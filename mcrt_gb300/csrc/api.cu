@@ -98,6 +98,10 @@ struct mcrt_ctx {
     unsigned long long graph_captures = 0;
     // radiance cache
     mcrt::CacheState *cache = nullptr;
+    mcrt_cache_params cache_cfg{};
+    bool cache_cfg_set = false;
+    DBuf cache_q, cache_rec;
+    uint32_t last_train_samples = 0;
 };
 
 namespace {
@@ -354,7 +358,7 @@ void mcrt_destroy(mcrt_ctx *ctx) {
                     &ctx->lights, &ctx->light_cdf, &ctx->tmp, &ctx->staging, &ctx->albedo, &ctx->wnodes, &ctx->pbmem, &ctx->mean,
                     &ctx->sum, &ctx->gbuf, &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->counters, &ctx->dimg,
                     &ctx->grad, &ctx->world_vox, &ctx->world_matmap, &ctx->wmesh.counts, &ctx->wmesh.vertices,
-                    &ctx->wmesh.triangles, &ctx->views, &ctx->pass_state};
+                    &ctx->wmesh.triangles, &ctx->views, &ctx->pass_state, &ctx->cache_q, &ctx->cache_rec};
     for (DBuf *b : bufs) b->release();
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     mcrt::cache_destroy(ctx->cache);
@@ -735,7 +739,16 @@ static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, ui
     cudaEvent_t e_begin = ev(ctx, evi++);
     cudaEventRecord(e_begin, st);
     const bool nee = (o.flags & MCRT_RENDER_NEE) != 0 && (ctx->n_lights > 0 || ctx->has_sun);
-    const bool use_graph = (o.flags & MCRT_RENDER_GRAPH) != 0;
+    const bool use_cache = (o.flags & MCRT_RENDER_CACHE) != 0;
+    if (use_cache && !ctx->cache_cfg_set) return fail(ctx, MCRT_ERR_INVALID_ARG, "radiance cache not configured");
+    const bool use_graph = (o.flags & MCRT_RENDER_GRAPH) != 0 && !use_cache;
+    const uint32_t train_stride = use_cache ? ctx->cache_cfg.train_stride : 1u;
+    if (use_cache) {
+        const size_t n_train = (n_slots + train_stride - 1) / train_stride;
+        CK(ctx->cache_q.ensure((size_t)n_slots * 64), "allocate cache queries");
+        CK(ctx->cache_rec.ensure(n_train * depth * mcrt::kTrainRecordFloat4 * 16), "allocate training records");
+    }
+    ctx->last_train_samples = 0;
     auto make_params = [&](uint32_t planes, uint32_t frame0) {
         mcrt::RenderParams P{};
         P.w = w; P.h = h; P.npix = npix;
@@ -753,8 +766,15 @@ static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, ui
             P.view_wh = reinterpret_cast<const uint2 *>(ctx->views.as<char>() + off_wh);
             P.view_cam = reinterpret_cast<const mcrt_camera_uniform *>(ctx->views.as<char>() + off_cam);
         }
+        if (use_cache) {
+            P.cache_query_vertex = ctx->cache_cfg.query_vertex + 1;
+            P.train_stride = train_stride;
+            P.cache_queries = ctx->cache_q.as<float4>();
+            P.train_records = ctx->cache_rec.as<float4>();
+        }
         return P;
     };
+    mcrt_status cache_status = MCRT_OK;
     // one pass: raygen, the bounces, resolve (into the accumulation)
     auto enqueue_pass = [&](const mcrt::RenderParams &P, bool keep_pass, bool timed) {
         mcrt::launch_raygen(S, P, ctx->pb, st);
@@ -782,12 +802,27 @@ static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, ui
             }
             qi ^= 1;
         }
+        if (use_cache) {                              // the terminated paths take the cache's prediction
+            cudaError_t e = mcrt::cache_infer_device(ctx->cache, ctx->cache_q.as<float4>(), ctx->pb.counters + 6,
+                                                     P.npix * P.spp_pass, nullptr, ctx->pb.L, ctx->pb.thr, st);
+            if (e != cudaSuccess) cache_status = cuda_fail(ctx, e, "cache inference");
+        }
         size_t r0 = 0;
         if (timed) { r0 = evi++; cudaEventRecord(ev(ctx, r0), st); }
         mcrt::launch_resolve(P, ctx->pb, ctx->mean.as<float4>(), ctx->sum.as<double>(), keep_pass, st);
         if (timed) {
             cudaEventRecord(ev(ctx, evi++), st);
             marks.push_back({r0, 4});
+        }
+        if (use_cache && cache_status == MCRT_OK) {   // train on this pass's training paths
+            const mcrt_cache_params &c = ctx->cache_cfg;
+            const uint32_t n_train = (P.npix * P.spp_pass + train_stride - 1) / train_stride;
+            uint32_t ns = 0;
+            cudaError_t e = mcrt::cache_train_records(ctx->cache, ctx->cache_rec.as<float4>(), n_train, depth,
+                                                      train_stride, ctx->pb.L, c.train_steps, c.train_batch, c.lr,
+                                                      st, &ns);
+            if (e != cudaSuccess) cache_status = cuda_fail(ctx, e, "cache training");
+            ctx->last_train_samples += ns;
         }
     };
     uint32_t done = 0;
@@ -851,6 +886,7 @@ static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, ui
     cudaEventRecord(e_end, st);
     CK(cudaGetLastError(), "render launch");
     CK(cudaEventSynchronize(e_end), "render");
+    if (cache_status != MCRT_OK) return cache_status;
     ctx->last_render_launches = mcrt::launch_count() - launches0;
     ctx->last_extend_launches = extend_launches;
     ctx->acc_valid = true;
@@ -1307,6 +1343,53 @@ mcrt_status mcrt_cache_set_bounds(mcrt_ctx *ctx, const float *lo3, const float *
         if (!std::isfinite(lo3[a]) || !std::isfinite(hi3[a]) || !(hi3[a] > lo3[a]))
             return fail(ctx, MCRT_ERR_INVALID_ARG, "bounds must be finite with hi > lo");
     mcrt::cache_set_bounds(cache_of(ctx), lo3, hi3);
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_cache_config(mcrt_ctx *ctx, const mcrt_cache_params *p) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!p) return fail(ctx, MCRT_ERR_INVALID_ARG, "params is NULL");
+    if (p->train_stride == 0) return fail(ctx, MCRT_ERR_INVALID_ARG, "train_stride must be >= 1");
+    if (!(p->lr >= 0.0f) || !std::isfinite(p->lr)) return fail(ctx, MCRT_ERR_INVALID_ARG, "lr must be >= 0");
+    if (p->query_vertex > 1023) return fail(ctx, MCRT_ERR_INVALID_ARG, "query_vertex too large");
+    float lo[3], hi[3];
+    bool given = true;
+    for (int a = 0; a < 3; ++a) {
+        if (!std::isfinite(p->lo[a]) || !std::isfinite(p->hi[a]))
+            return fail(ctx, MCRT_ERR_INVALID_ARG, "bounds must be finite");
+        lo[a] = p->lo[a];
+        hi[a] = p->hi[a];
+        given = given && hi[a] > lo[a];
+    }
+    if (!given) {                                  // the scene's bounding box (root nodes of the BVHs)
+        if (!ctx->has_scene) return fail(ctx, MCRT_ERR_NO_SCENE, "no scene to take the bounds from");
+        CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+        for (int a = 0; a < 3; ++a) { lo[a] = INFINITY; hi[a] = -INFINITY; }
+        auto take = [&](const DBuf &nodes, uint32_t n) -> cudaError_t {
+            if (n == 0) return cudaSuccess;
+            mcrt_gpu_bvh_node root;
+            cudaError_t e = cudaMemcpy(&root, nodes.p, sizeof(root), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) return e;
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = std::min(lo[a], root.aabb_min[a]);
+                hi[a] = std::max(hi[a], root.aabb_max[a]);
+            }
+            return cudaSuccess;
+        };
+        CK(take(ctx->mesh_nodes, ctx->n_mesh_nodes), "read scene bounds");
+        CK(take(ctx->sphere_nodes, ctx->n_sphere_nodes), "read scene bounds");
+        for (int a = 0; a < 3; ++a)
+            if (!(hi[a] > lo[a])) { lo[a] -= 0.5f; hi[a] += 0.5f; }
+        if (!std::isfinite(lo[0])) return fail(ctx, MCRT_ERR_INVALID_ARG, "empty scene");
+    }
+    mcrt::cache_set_bounds(cache_of(ctx), lo, hi);
+    ctx->cache_cfg = *p;
+    for (int a = 0; a < 3; ++a) { ctx->cache_cfg.lo[a] = lo[a]; ctx->cache_cfg.hi[a] = hi[a]; }
+    ctx->cache_cfg_set = true;
+    if (!mcrt::cache_ready(ctx->cache)) {
+        mcrt_status s = mcrt_cache_init(ctx, 0);
+        if (s != MCRT_OK) return s;
+    }
     return MCRT_OK;
 }
 

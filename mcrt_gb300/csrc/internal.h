@@ -86,7 +86,16 @@ struct RenderParams {
     // graph replay: [0] frame index of plane 0, [1] keep flag of the resolve,
     // read from device memory instead of frame0 / the launch argument
     const uint32_t *pass_state;
+    // radiance cache (cache_query_vertex == 0: off): non-training paths stop at
+    // that non-emissive vertex (1-based) and append a query; slots with
+    // slot % train_stride == 0 are training paths recording their vertices
+    uint32_t cache_query_vertex;
+    uint32_t train_stride;
+    float4 *cache_queries;      // 4 float4 per query: p | slot, w_o, n, albedo
+    float4 *train_records;      // per training path and vertex: 6 float4 (p | valid, w_o, n, albedo, thr, L so far)
 };
+
+constexpr uint32_t kTrainRecordFloat4 = 6;
 int extend_variant_count();
 // (BVH width, block size, minimum resident blocks, stack depth) of a variant.
 void extend_variant_info(int v, int out[4]);
@@ -153,6 +162,11 @@ cudaError_t cache_infer_device(CacheState *c, const float4 *q, const uint32_t *d
                                float4 *L, const float4 *thr, cudaStream_t st);
 cudaError_t cache_step_device(CacheState *c, const float *d_samples, uint32_t n, uint32_t n_valid, float lr,
                               cudaStream_t st);
+// Samples from the training paths' records (L: final path radiance per slot), then `steps` Adam steps.
+cudaError_t cache_train_records(CacheState *c, const float4 *rec, uint32_t n_train, uint32_t depth, uint32_t stride,
+                                const float4 *L, uint32_t steps, uint32_t batch, float lr, cudaStream_t st,
+                                uint32_t *n_samples_out);
+bool cache_ready(const CacheState *c);
 
 // Denoiser (denoise.cu)
 void launch_denoise(const float4 *in, const float4 *gbuf, uint32_t w, uint32_t h, const mcrt_denoise_params &p,

@@ -503,6 +503,44 @@ __global__ void k_cache_refresh(const float *params, uint8_t *img, float *bias) 
     else *reinterpret_cast<uint16_t *>(img + img_off(l) + tc::op_offset(o, i, out_of(l))) = (uint16_t)bf16_bits(params[p]);
 }
 
+// Training samples from the recorded vertices of the training paths: for
+// recorded vertex j of training path t, query = (p, w_o, n, albedo) and target
+// = (L_final - L_j) / thr_j, the radiance the path gathered from vertex j on per
+// unit throughput; appended (warp-aggregated) when finite.
+__global__ void k_cache_targets(const float4 *rec, uint32_t n_train, uint32_t depth, uint32_t stride,
+                                const float4 *L, float *samples, uint32_t *count) {
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31u;
+    bool ok = false;
+    float s[16];
+    if (idx < n_train * depth) {
+        const float4 *r = rec + (size_t)idx * kTrainRecordFloat4;
+        const float4 p = r[0];
+        if (p.w > 0.0f) {
+            const float4 wo = r[1], nn = r[2], al = r[3], th = r[4], l0 = r[5];
+            const float4 lf = L[(size_t)(idx / depth) * stride];
+            const float tx = (lf.x - l0.x) / th.x, ty = (lf.y - l0.y) / th.y, tz = (lf.z - l0.z) / th.z;
+            ok = th.x > 0.0f && th.y > 0.0f && th.z > 0.0f && isfinite(tx) && isfinite(ty) && isfinite(tz);
+            s[0] = p.x; s[1] = p.y; s[2] = p.z; s[3] = wo.x; s[4] = wo.y; s[5] = wo.z;
+            s[6] = nn.x; s[7] = nn.y; s[8] = nn.z; s[9] = al.x; s[10] = al.y; s[11] = al.z;
+            s[12] = fmaxf(tx, 0.0f); s[13] = fmaxf(ty, 0.0f); s[14] = fmaxf(tz, 0.0f); s[15] = 1.0f;
+        }
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, ok);
+    if (!mask) return;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if ((int)lane == leader) base = atomicAdd(count, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (ok) {
+        float4 *dst = reinterpret_cast<float4 *>(samples + 16 * (size_t)(base + __popc(mask & ((1u << lane) - 1u))));
+        dst[0] = make_float4(s[0], s[1], s[2], s[3]);
+        dst[1] = make_float4(s[4], s[5], s[6], s[7]);
+        dst[2] = make_float4(s[8], s[9], s[10], s[11]);
+        dst[3] = make_float4(s[12], s[13], s[14], s[15]);
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------- cache state
@@ -662,6 +700,37 @@ cudaError_t cache_step_device(CacheState *c, const float *d_samples, uint32_t n,
     }
     return cudaGetLastError();
 }
+
+cudaError_t cache_train_records(CacheState *c, const float4 *rec, uint32_t n_train, uint32_t depth, uint32_t stride,
+                                const float4 *L, uint32_t steps, uint32_t batch, float lr, cudaStream_t st,
+                                uint32_t *n_samples_out) {
+    if (!c->has_params) return cudaErrorInvalidValue;
+    cudaError_t e;
+    const size_t cap = (size_t)n_train * depth;
+    if ((e = c->samples.ensure(cap * 64 + 64)) != cudaSuccess) return e;
+    uint32_t *count = reinterpret_cast<uint32_t *>(c->samples.as<char>() + cap * 64);
+    if ((e = cudaMemsetAsync(count, 0, 4, st)) != cudaSuccess) return e;
+    if (cap) {
+        k_cache_targets<<<(uint32_t)((cap + 255) / 256), 256, 0, st>>>(rec, n_train, depth, stride, L,
+                                                                      c->samples.as<float>(), count);
+        note_launch();
+    }
+    uint32_t n = 0;
+    if ((e = cudaMemcpyAsync(&n, count, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    if (n_samples_out) *n_samples_out = n;
+    if (n == 0) return cudaSuccess;
+    if (batch == 0 || batch > n) batch = n;
+    for (uint32_t s = 0; s < steps; ++s) {
+        const uint32_t first = (uint32_t)(((uint64_t)s * batch) % n);
+        const uint32_t cnt = std::min(batch, n - first);
+        if ((e = cache_step_device(c, c->samples.as<float>() + 16 * (size_t)first, cnt, cnt, lr, st)) != cudaSuccess)
+            return e;
+    }
+    return cudaSuccess;
+}
+
+bool cache_ready(const CacheState *c) { return c && c->has_params; }
 
 cudaError_t cache_train_host(CacheState *c, const float *samples16, uint32_t n, uint32_t steps, uint32_t batch,
                              float lr, float *out_loss, float *out_grad, cudaStream_t st, bool *timed_out) {

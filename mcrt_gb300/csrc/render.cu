@@ -452,8 +452,15 @@ __global__ void k_trace_closest(DeviceScene S, const mcrt_ray *rays, uint32_t n,
 __global__ void k_raygen(DeviceScene S, RenderParams P, PathBuffers B, int keep_radiance) {
     uint32_t n = P.npix * P.spp_pass;
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) { B.counters[0] = n; B.counters[1] = 0; B.counters[2] = 0; B.counters[4] = 0; B.counters[5] = 0; }
+    if (i == 0) {
+        B.counters[0] = n; B.counters[1] = 0; B.counters[2] = 0; B.counters[4] = 0; B.counters[5] = 0;
+        B.counters[6] = 0;
+    }
     if (i >= n) return;
+    if (P.cache_query_vertex && i % P.train_stride == 0u) {        // training path: no vertex recorded yet
+        float4 *rec = P.train_records + (size_t)(i / P.train_stride) * P.max_depth * kTrainRecordFloat4;
+        for (uint32_t j = 0; j < P.max_depth; ++j) rec[(size_t)j * kTrainRecordFloat4].w = 0.0f;
+    }
     uint32_t k = i / P.npix;
     uint32_t p = i - k * P.npix;
     uint32_t frame = (P.pass_state ? P.pass_state[0] : P.frame0) + k;
@@ -729,8 +736,9 @@ __global__ void __launch_bounds__(256) k_shade(DeviceScene S, RenderParams P, Pa
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t i = base + threadIdx.x;
-        bool cont = false, shadow = false;
+        bool cont = false, shadow = false, queried = false;
         f3 no = {0, 0, 0}, nd = {0, 0, 0}, so = {0, 0, 0}, sd = {0, 0, 0}, sc = {0, 0, 0};
+        float4 cq0, cq1, cq2, cq3;             // radiance-cache query of this path
         float smax = 0.0f;
         uint32_t slot = 0;
         uint32_t sh_bits = 0;                  // adjoint: material | light material << 8
@@ -804,7 +812,28 @@ __global__ void __launch_bounds__(256) k_shade(DeviceScene S, RenderParams P, Pa
                     float pdf = -1.0f;
                     float4 dlw = make_float4(0.0f, 0.0f, 0.0f, 0.0f);   // adjoint: dlog(weight)/d(params)
                     bool has_params = false;
-                    if (mtype == kMatMetal) {                                   // :530-541
+                    if (!ADJ && P.cache_query_vertex) {                         // radiance cache
+                        if (slot % P.train_stride == 0u) {                      // training path: record the vertex
+                            float4 *rec = P.train_records +
+                                          ((size_t)(slot / P.train_stride) * P.max_depth + bounce) * kTrainRecordFloat4;
+                            const float4 Lnow = B.L[slot];
+                            rec[0] = make_float4(sh.p.x, sh.p.y, sh.p.z, 1.0f);
+                            rec[1] = make_float4(-d.x, -d.y, -d.z, 0.0f);
+                            rec[2] = make_float4(sh.n.x, sh.n.y, sh.n.z, 0.0f);
+                            rec[3] = make_float4(albedo.x, albedo.y, albedo.z, 0.0f);
+                            rec[4] = make_float4(thr.x, thr.y, thr.z, 0.0f);
+                            rec[5] = make_float4(Lnow.x, Lnow.y, Lnow.z, 0.0f);
+                        } else if (bounce + 1 == P.cache_query_vertex) {        // stop here: ask the cache
+                            queried = true;
+                            cq0 = make_float4(sh.p.x, sh.p.y, sh.p.z, __uint_as_float(slot));
+                            cq1 = make_float4(-d.x, -d.y, -d.z, 0.0f);
+                            cq2 = make_float4(sh.n.x, sh.n.y, sh.n.z, 0.0f);
+                            cq3 = make_float4(albedo.x, albedo.y, albedo.z, 0.0f);
+                        }
+                    }
+                    if (queried) {
+                        absorbed = true;
+                    } else if (mtype == kMatMetal) {                            // :530-541
                         float fuzz = m.albedo_fuzz[3];
                         f3 refl = reflect_vec(normalize(d), sh.n);
                         f3 pert = refl + fuzz * random_unit_sphere(rng);
@@ -947,6 +976,20 @@ __global__ void __launch_bounds__(256) k_shade(DeviceScene S, RenderParams P, Pa
                 B.sh_d[pos] = make_float4(sd.x, sd.y, sd.z, smax);
                 B.sh_c[pos] = make_float4(sc.x, sc.y, sc.z, __uint_as_float(sh_bits));
                 if (ADJ) B.sh_g[pos] = sh_dlog;
+            }
+        }
+        if (!ADJ && P.cache_query_vertex) {
+            unsigned qmask = __ballot_sync(0xffffffffu, queried);
+            if (qmask) {
+                int leader = __ffs(qmask) - 1;
+                uint32_t basepos = 0;
+                if ((int)lane == leader) basepos = atomicAdd(B.counters + 6, (uint32_t)__popc(qmask));
+                basepos = __shfl_sync(0xffffffffu, basepos, leader);
+                if (queried) {
+                    uint32_t pos = basepos + __popc(qmask & ((1u << lane) - 1u));
+                    float4 *q = P.cache_queries + 4 * (size_t)pos;
+                    q[0] = cq0; q[1] = cq1; q[2] = cq2; q[3] = cq3;
+                }
             }
         }
     }

@@ -722,8 +722,12 @@ struct Deriv {
 /* path_color, path_trace.wgsl:583-620 (+ G-buffer :592-602).
  * stats (optional): [0] rays traced, [1] nodes visited, [2] primitives tested.
  * lights: next-event estimation with MIS when non-null.  D: derivatives when non-null. */
+/* A path stopped into a radiance cache whose prediction is the constant c: at
+ * its non-emissive vertex number `bounce` it adds thr * max(c, 0) and ends. */
+struct CacheStop { uint32_t bounce; V3 c; };
+
 V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, float *gbuf, uint64_t *stats,
-              const Lights *lights, Deriv *D) {
+              const Lights *lights, Deriv *D, const CacheStop *stop = nullptr) {
     const bool nee = lights && (lights->n > 0 || lights->has_sun);
     V3 thr = {1.0f, 1.0f, 1.0f};
     V3 Lacc = {0.0f, 0.0f, 0.0f};
@@ -774,6 +778,9 @@ V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, f
             return nee ? Lacc + wmis * e : e;
         }
         albedo = material_albedo(sc, m, c, h.p);                               /* :506-515 */
+        if (stop && bounce == stop->bounce)
+            return Lacc + V3{thr.x * fmaxf(stop->c.x, 0.0f), thr.y * fmaxf(stop->c.y, 0.0f),
+                             thr.z * fmaxf(stop->c.z, 0.0f)};
         const V3 tex = D ? material_tex(sc, m, c, h.p) : V3{1.0f, 1.0f, 1.0f};
         const bool own = D && 4 * mi + 3 < np;
         V3 dir = {0, 0, 0}, atten = {0, 0, 0};
@@ -1179,6 +1186,45 @@ void orc_render_ex(const orc_scene *sc, const orc_camera *cam, uint32_t w, uint3
     }
     }
     if (out_stats) for (int k = 0; k < 3; ++k) out_stats[k] = tot[k];
+}
+
+void orc_render_cache_const(const orc_scene *sc, const orc_camera *cam, uint32_t w, uint32_t h, uint32_t spp,
+                            uint32_t first_frame, uint32_t max_depth, uint32_t flags, uint32_t spp_pass,
+                            uint32_t train_stride, uint32_t query_vertex, const float *c3, float *out_mean,
+                            double *out_sum, int threads) {
+    const int64_t npx = (int64_t)w * h;
+    Lights lights;
+    const Lights *lp = nullptr;
+    if (flags & ORC_RENDER_NEE) {
+        make_lights(sc, lights);
+        lp = &lights;
+    }
+    const CacheStop stop{query_vertex, ld3(c3)};
+#pragma omp parallel for schedule(dynamic, 16) num_threads(n_threads(threads))
+    for (int64_t i = 0; i < npx; ++i) {
+        uint32_t x = (uint32_t)(i % w), y = (uint32_t)(i / w);
+        float mean[3] = {0, 0, 0};
+        double sum[3] = {0, 0, 0};
+        for (uint32_t k = 0; k < spp; ++k) {
+            uint32_t frame = first_frame + k;
+            uint32_t rng = pcg_hash(pcg_hash(x + y * w) ^ (frame * 2654435761u));
+            Ray r = camera_ray(cam, x, y, w, h, rng);
+            const uint64_t slot = (uint64_t)(k % spp_pass) * (uint64_t)npx + (uint64_t)i;
+            const bool training = slot % train_stride == 0;
+            V3 s = path_color(sc, r, rng, max_depth, nullptr, nullptr, lp, nullptr, training ? nullptr : &stop);
+            float wgt = 1.0f / (float)(std::min(frame, MAX_FRAME_COUNT) + 1u);
+            float omw = 1.0f - wgt;
+            mean[0] = mean[0] * omw + s.x * wgt;
+            mean[1] = mean[1] * omw + s.y * wgt;
+            mean[2] = mean[2] * omw + s.z * wgt;
+            sum[0] += (double)s.x; sum[1] += (double)s.y; sum[2] += (double)s.z;
+        }
+        if (out_mean) {
+            out_mean[4 * i] = mean[0]; out_mean[4 * i + 1] = mean[1]; out_mean[4 * i + 2] = mean[2];
+            out_mean[4 * i + 3] = 1.0f;
+        }
+        if (out_sum) { out_sum[3 * i] += sum[0]; out_sum[3 * i + 1] += sum[1]; out_sum[3 * i + 2] += sum[2]; }
+    }
 }
 
 void orc_render_rect_stats(const orc_scene *sc, const orc_camera *cam, uint32_t w, uint32_t h,

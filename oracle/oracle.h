@@ -99,6 +99,16 @@ void orc_render_ex(const orc_scene *scene, const orc_camera *cam, uint32_t w, ui
                    uint32_t max_depth, uint32_t flags, float *out_mean_rgba, double *out_sum_rgb, float *out_gbuf,
                    int threads, uint64_t *out_stats);
 
+/* orc_render_ex with paths stopped into a radiance cache whose prediction is the
+ * constant c3: the sample of frame k, pixel p occupies slot (k mod spp_pass) *
+ * w*h + p of its pass; slots with slot % train_stride == 0 are traced in full,
+ * the others add throughput * max(c, 0) at their vertex number query_vertex
+ * (0 = primary hit) when it is not emissive, and end. */
+void orc_render_cache_const(const orc_scene *scene, const orc_camera *cam, uint32_t w, uint32_t h, uint32_t spp,
+                            uint32_t first_frame, uint32_t max_depth, uint32_t flags, uint32_t spp_pass,
+                            uint32_t train_stride, uint32_t query_vertex, const float *c3, float *out_mean_rgba,
+                            double *out_sum_rgb, int threads);
+
 /* Brute-force gradient of an image loss with respect to the material
  * parameters, by forward-mode differentiation of every sampled path:
  *   grad[4*m + k] = sum_pixels sum_c d_image[pixel].c / spp * d(sample mean).c / d(param m,k)

@@ -189,6 +189,23 @@ class OracleScene:
             out["stats"] = dict(rays=int(st[0]), nodes=int(st[1]), prims=int(st[2]))
         return out
 
+    def render_cache_const(self, camera, w, h, spp, c3, spp_pass, train_stride, query_vertex, first_frame=0,
+                           max_depth=8, nee=False, threads=0):
+        """Render with paths stopped into a constant radiance cache (see oracle.h)."""
+        L = lib()
+        L.orc_render_cache_const.restype = None
+        L.orc_render_cache_const.argtypes = [POINTER(_Scene), c_void_p, c_uint32, c_uint32, c_uint32, c_uint32,
+                                             c_uint32, c_uint32, c_uint32, c_uint32, c_uint32, c_void_p, c_void_p,
+                                             c_void_p, c_int]
+        cam = np.ascontiguousarray(camera)
+        c = np.ascontiguousarray(c3, np.float32)
+        mean = np.zeros((h, w, 4), np.float32)
+        acc = np.zeros((h, w, 3), np.float64)
+        L.orc_render_cache_const(ctypes.byref(self._s), _p(cam), w, h, spp, first_frame, max_depth,
+                                 NEE if nee else 0, spp_pass, train_stride, query_vertex, _p(c), _p(mean), _p(acc),
+                                 threads)
+        return dict(rgba=mean, sum=acc)
+
     def adjoint(self, camera, w, h, spp, d_image, first_frame=0, max_depth=8, nee=False, threads=0):
         """Brute-force (forward-mode) gradient of sum(d_image * image) with respect to
         the 64 x 4 material parameters (albedo rgb, roughness); also returns the f64 sums."""

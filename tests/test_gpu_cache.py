@@ -95,3 +95,59 @@ def test_cache_learns_a_radiance_field(cache_ctx):
     assert np.all(np.isfinite(loss))
     assert loss[-1] < 0.1 * loss[0]
     assert after < 0.1 * before
+
+
+def test_cache_stop_bit_exact(ctx, oracle):
+    """Paths stopped into a cache that predicts a constant: the render equals the
+    oracle's, bit for bit (training paths traced in full, the others ending at
+    their second vertex with throughput x prediction)."""
+    from mcrt_gb300 import scenes
+    sc = scenes.cornell_box(5)
+    c = sc["camera"]
+    cam = M.compute_camera(48, 40, c["look_from"], c["look_at"], c["vfov"], 0.0)
+    ctx.upload_scene(vertices=sc["vertices"], triangles=sc["triangles"], materials=sc["materials"],
+                     env=M.gradient_env_map())
+    ctx.cache_config(query_vertex=1, train_stride=7, train_steps=0, lr=0.0)
+    p = np.zeros(ctx.cache_params().size, np.float32)
+    const = np.array([0.3, 0.2, 0.1], np.float32)
+    p[-16:-13] = const                              # output bias
+    ctx.cache_set_params(p)
+    for nee in (False, True):
+        r = ctx.render(cam, 48, 40, 6, max_depth=8, nee=nee, spp_per_pass=3, cache=True)
+        o = oracle.OracleScene(materials=sc["materials"], vertices=sc["vertices"], triangles=sc["triangles"],
+                               env=M.gradient_env_map()).render_cache_const(cam, 48, 40, 6, const, 3, 7, 1,
+                                                                            max_depth=8, nee=nee)
+        assert np.array_equal(r["rgba"].view(np.uint32), o["rgba"].view(np.uint32))
+        assert np.array_equal(r["sum"].view(np.uint64), o["sum"].view(np.uint64))
+
+
+def test_trained_cache_gains_over_untrained_and_plain(ctx):
+    """Cornell box 128 x 128: the tracer with the online-trained cache (paths
+    stopped at their third vertex) against the same tracer with an untrained
+    network and against the plain (reference) estimator at equal spp, all
+    measured as relMSE against a 4096-spp NEE reference."""
+    from mcrt_gb300 import scenes
+    sc = scenes.cornell_box(1234)
+    c = sc["camera"]
+    W = H = 128
+    cam = M.compute_camera(W, H, c["look_from"], c["look_at"], c["vfov"], 0.0)
+    ctx.upload_scene(vertices=sc["vertices"], triangles=sc["triangles"], materials=sc["materials"],
+                     env=M.gradient_env_map())
+    ref = ctx.render(cam, W, H, 4096, first_frame=1 << 20, max_depth=8, nee=True, outputs=("sum",))["sum"] / 4096
+
+    def rel(x):
+        return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+    spp = 256
+    plain = rel(ctx.render(cam, W, H, spp, max_depth=8, outputs=("sum",))["sum"] / spp)
+    ctx.cache_config(query_vertex=2, train_stride=16, train_steps=0, lr=0.0)
+    ctx.cache_init(1)
+    untrained = rel(ctx.render(cam, W, H, spp, max_depth=8, nee=True, cache=True, outputs=("sum",))["sum"] / spp)
+    ctx.cache_config(query_vertex=2, train_stride=16, train_steps=4, lr=1e-3)
+    ctx.cache_init(1)
+    for i in range(40):
+        ctx.render(cam, W, H, 4, first_frame=100000 + 4 * i, max_depth=8, nee=True, cache=True, outputs=())
+    trained = rel(ctx.render(cam, W, H, spp, max_depth=8, nee=True, cache=True, outputs=("sum",))["sum"] / spp)
+    print("relMSE plain", plain, "untrained cache", untrained, "trained cache", trained)
+    assert trained < untrained / 3
+    assert trained < plain / 3
