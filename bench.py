@@ -363,6 +363,33 @@ def batched_views_rate(M, ctx, stream, spp=4, n_warm=1, n_steps=3):
             "speedup": round(t_seq / t_batch, 3)}
 
 
+MLP_FLOP_INFER = 2 * (96 * 64 + 4 * 64 * 64 + 64 * 16)                    # per query
+MLP_FLOP_TRAIN = MLP_FLOP_INFER + 2 * (16 * 64 + 4 * 64 * 64) + MLP_FLOP_INFER   # + backward data + weight grads
+
+
+def mlp_rate(M, ctx, n=1 << 20, reps=10):
+    """Radiance-cache MLP on the tensor cores: inference over 2^20 synthetic
+    queries and one training step on 2^20 samples (device time), against the
+    measured bf16 peak (algorithmic FLOPs of the 96-64x5-3 network, output layer
+    counted 16 wide)."""
+    t_inf, t_train = ctx.cache_bench(n, reps)
+    peak = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak = json.load(f)["bf16_tflops"]
+    except (OSError, KeyError, ValueError):
+        peak = 1900.0
+    tf_inf = n * MLP_FLOP_INFER / (t_inf / 1000.0) / 1e12
+    tf_train = n * MLP_FLOP_TRAIN / (t_train / 1000.0) / 1e12
+    return {"queries": n, "infer_ms": round(t_inf, 4), "train_step_ms": round(t_train, 4),
+            "infer_queries_per_s": round(n / (t_inf / 1000.0), 1),
+            "train_samples_per_s": round(n / (t_train / 1000.0), 1),
+            "roofline": {"bound": "tensor", "unit": "TFLOP/s", "peak": peak,
+                         "infer_achieved": round(tf_inf, 2), "infer_frac": round(tf_inf / peak, 4),
+                         "train_achieved": round(tf_train, 2), "train_frac": round(tf_train / peak, 4),
+                         "flop_per_query": MLP_FLOP_INFER, "flop_per_train_sample": MLP_FLOP_TRAIN}}
+
+
 def run_mcrt(args):
     import torch
     import mcrt_gb300 as M
@@ -446,8 +473,9 @@ def run_mcrt(args):
                 "n_tri": round(n_tri, 2), "mrays_per_s": round(rays / (ext_ms / 1000.0) / 1e6, 1),
                 "avg_launch_ms": round(ext_ms / max(ext_launches, 1), 4)}
     clocks = clk.summary()
-    quality = adjoint = voxel = views = None
+    quality = adjoint = voxel = views = mlp = None
     if not args.small:
+        mlp = mlp_rate(M, ctx)
         quality = time_to_relmse(M, ctx)
         adjoint = adjoint_rate(M, ctx, stream)
         voxel = voxel_world_rate(M, ctx, stream)
@@ -473,6 +501,7 @@ def run_mcrt(args):
         "adjoint": adjoint,
         "voxel_world": voxel,
         "batched_views": views,
+        "radiance_cache_mlp": mlp,
     }
     print(json.dumps(out))
     barrier(world)

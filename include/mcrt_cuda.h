@@ -333,8 +333,9 @@ mcrt_status mcrt_mlp_gemm_probe(int device, const uint16_t *A, const uint16_t *B
  * radiance scattered from a surface point towards a direction.  Inputs per
  * query, 12 floats: position p, outgoing direction w_o (towards the previous
  * vertex), shading normal n, albedo a.  Encoding (96 features): u = clamp((p -
- * lo) / (hi - lo), 0, 1); sin and cos of u * pi * 2^k for k = 0..11 per axis;
- * w_o, n, a, u; zeros.  Network: 5 hidden layers of 64 ReLU units, 3 linear
+ * lo) / (hi - lo), 0, 1); sin and cos of u * pi * 2^k for k = 0..11 per axis
+ * (from sin / cos of pi u by the double-angle recurrence s' = 2sc,
+ * c' = c^2 - s^2); w_o, n, a, u; zeros.  Network: 5 hidden layers of 64 ReLU units, 3 linear
  * outputs; bf16 weights and activations on the tensor cores, fp32
  * accumulation, fp32 master parameters (mcrt_cache_param_count floats: W_l
  * row-major [out][in] then b_l per layer; the output layer is stored 16 wide,
@@ -362,6 +363,12 @@ typedef struct {
     float lo[3], hi[3];
 } mcrt_cache_params;
 mcrt_status mcrt_cache_config(mcrt_ctx *ctx, const mcrt_cache_params *params);
+
+/* Device time (CUDA events) of cache inference over n synthetic queries and of
+ * one training step on n synthetic samples, averaged over reps:
+ * out_ms[0] inference, out_ms[1] training step.  Leaves the parameters
+ * trained by reps + 1 tiny steps (learning rate 1e-6). */
+mcrt_status mcrt_cache_bench(mcrt_ctx *ctx, uint32_t n, uint32_t reps, float *out_ms);
 mcrt_status mcrt_cache_init(mcrt_ctx *ctx, uint32_t seed);              /* He-uniform weights, zero biases */
 mcrt_status mcrt_cache_set_params(mcrt_ctx *ctx, const float *params);  /* also resets the Adam moments */
 mcrt_status mcrt_cache_get_params(mcrt_ctx *ctx, float *out);

@@ -356,6 +356,12 @@ class Context:
                 p.lo[k], p.hi[k] = float(lo[k]), float(hi[k])
         self._check(lib().mcrt_cache_config(self._h, ctypes.byref(p)))
 
+    def cache_bench(self, n=1 << 20, reps=10):
+        """(inference ms, training-step ms) on n synthetic queries / samples (device time)."""
+        out = (c_float * 2)()
+        self._check(lib().mcrt_cache_bench(self._h, n, reps, out))
+        return out[0], out[1]
+
     def cache_init(self, seed=0):
         self._check(lib().mcrt_cache_init(self._h, seed))
 

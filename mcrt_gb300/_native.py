@@ -127,6 +127,7 @@ SIGNATURES = [
     ("mcrt_mlp_gemm_probe", c_int, [c_int, c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_void_p]),
     ("mcrt_cache_param_count", c_uint32, []),
     ("mcrt_cache_config", c_int, [c_void_p, POINTER(CacheParams)]),
+    ("mcrt_cache_bench", c_int, [c_void_p, c_uint32, c_uint32, c_void_p]),
     ("mcrt_cache_init", c_int, [c_void_p, c_uint32]),
     ("mcrt_cache_set_params", c_int, [c_void_p, c_void_p]),
     ("mcrt_cache_get_params", c_int, [c_void_p, c_void_p]),

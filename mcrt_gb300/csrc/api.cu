@@ -1346,6 +1346,21 @@ mcrt_status mcrt_cache_set_bounds(mcrt_ctx *ctx, const float *lo3, const float *
     return MCRT_OK;
 }
 
+mcrt_status mcrt_cache_bench(mcrt_ctx *ctx, uint32_t n, uint32_t reps, float *out_ms) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!out_ms || n == 0 || n > (1u << 24) || reps == 0 || reps > 1000)
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "out_ms NULL, n out of [1, 2^24] or reps out of [1, 1000]");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    mcrt::CacheState *c = cache_of(ctx);
+    if (!mcrt::cache_ready(c)) {
+        mcrt_status s = mcrt_cache_init(ctx, 0);
+        if (s != MCRT_OK) return s;
+    }
+    cudaError_t e = mcrt::cache_bench(c, n, reps, &out_ms[0], &out_ms[1], ctx->stream);
+    CK(e, "cache benchmark");
+    return MCRT_OK;
+}
+
 mcrt_status mcrt_cache_config(mcrt_ctx *ctx, const mcrt_cache_params *p) {
     if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
     if (!p) return fail(ctx, MCRT_ERR_INVALID_ARG, "params is NULL");

@@ -167,6 +167,7 @@ cudaError_t cache_train_records(CacheState *c, const float4 *rec, uint32_t n_tra
                                 const float4 *L, uint32_t steps, uint32_t batch, float lr, cudaStream_t st,
                                 uint32_t *n_samples_out);
 bool cache_ready(const CacheState *c);
+cudaError_t cache_bench(CacheState *c, uint32_t n, uint32_t reps, float *ms_infer, float *ms_train, cudaStream_t st);
 
 // Denoiser (denoise.cu)
 void launch_denoise(const float4 *in, const float4 *gbuf, uint32_t w, uint32_t h, const mcrt_denoise_params &p,

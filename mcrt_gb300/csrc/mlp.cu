@@ -113,7 +113,8 @@ constexpr uint32_t kSmemAct = kSmemBias + kBiasFloats * 4;                 // 48
 constexpr uint32_t kTileIn = kTile * kIn * 2;                              // 24576
 constexpr uint32_t kTileHid = kTile * kHid * 2;                            // 16384
 // inference: image | bias | one activation tile | mbarrier | TMEM slot
-constexpr uint32_t kInferSmem = kSmemAct + kTileIn + 64;
+constexpr uint32_t kInferGroups = 2;
+constexpr uint32_t kInferSmem = kSmemAct + kInferGroups * kTileIn + 64;
 // training: image | bias | X0 | H1..H5 | G (128 x 128, upper half zero) | bias grads | misc
 constexpr uint32_t kTrainX0 = kSmemAct;
 constexpr uint32_t kTrainH = kTrainX0 + kTileIn;
@@ -189,24 +190,48 @@ struct InferIO {
 
 // Inference over tiles of 128 queries: the five hidden layers and the output
 // layer as tensor-core products with the accumulator in TMEM; the epilogue
-// (bias, ReLU, bf16) writes the next layer's operand in place.
-__global__ void __launch_bounds__(128) k_cache_infer(NetDev net, InferIO io, uint32_t *status) {
+// (bias, ReLU, bf16) writes the next layer's operand in place.  A CTA runs
+// kInferGroups independent tile pipelines (128 threads each, own operand tile,
+// TMEM columns and mbarrier, synchronised by named barriers) over one copy of
+// the weights, so one group's epilogue overlaps another's tensor-core work.
+__device__ __forceinline__ void group_bar(uint32_t id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+__device__ __forceinline__ bool group_and(uint32_t id, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.and.pred q, %2, 128, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(r)
+        : "r"(v ? 1u : 0u), "r"(id)
+        : "memory");
+    return r != 0;
+}
+__device__ __forceinline__ void group_operand_sync(uint32_t id) {
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    group_bar(id);
+    tc::fence_after_sync();
+}
+
+__global__ void __launch_bounds__(128 * kInferGroups) k_cache_infer(NetDev net, InferIO io, uint32_t *status) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t *act = smem + kSmemAct;
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + kSmemAct + kTileIn);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 1);
+    const uint32_t t = threadIdx.x, warp = t >> 5, g = t / 128u, row = t % 128u;
+    uint8_t *act = smem + kSmemAct + g * kTileIn;
+    uint8_t *misc = smem + kSmemAct + kInferGroups * kTileIn;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(misc) + g;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(misc + 8 * kInferGroups);
     const float *bias = reinterpret_cast<const float *>(smem + kSmemBias);
-    const uint32_t t = threadIdx.x, warp = t >> 5, row = t;
+    const uint32_t bar_id = 1 + g;
     const uint32_t n = io.count ? min(*io.count, io.n) : io.n;
     load_net(net, smem);
-    if (warp == 0) tc::tmem_alloc(tslot, 64);
-    if (t == 0) tc::mbar_init(mbar, 1);
+    if (warp == 0) tc::tmem_alloc(tslot, 64 * kInferGroups);
+    if (t == 0)
+        for (uint32_t k = 0; k < kInferGroups; ++k) tc::mbar_init(reinterpret_cast<uint64_t *>(misc) + k, 1);
     operand_sync();
-    const uint32_t taddr = *tslot;
-    const uint32_t lane_base = (warp * 32u) << 16;
+    const uint32_t taddr = *tslot + 64u * g;
+    const uint32_t lane_base = ((warp & 3u) * 32u) << 16;
     uint32_t phase = 0;
     bool ok = true;
-    for (uint32_t tile = blockIdx.x; ok && tile * kTile < n; tile += gridDim.x) {
+    for (uint32_t tile = blockIdx.x * kInferGroups + g; ok && tile * kTile < n; tile += gridDim.x * kInferGroups) {
         const uint32_t i = tile * kTile + row;
         const bool valid = i < n;
         float q[12];
@@ -220,10 +245,10 @@ __global__ void __launch_bounds__(128) k_cache_infer(NetDev net, InferIO io, uin
             q[9] = d.x; q[10] = d.y; q[11] = d.z;
         }
         encode_row(net, q, valid, act, row);
-        operand_sync();
+        group_operand_sync(bar_id);
         for (int l = 0; l < kLayers; ++l) {
-            if (t == 0) issue_forward(taddr, act, smem + kSmemImg + img_off(l), l, mbar);
-            ok = __syncthreads_and(tc::mbar_wait(mbar, phase & 1u, kPollLimit) ? 1 : 0) != 0;   // uniform
+            if (row == 0) issue_forward(taddr, act, smem + kSmemImg + img_off(l), l, mbar);
+            ok = group_and(bar_id, tc::mbar_wait(mbar, phase & 1u, kPollLimit));   // uniform in the group
             ++phase;
             tc::fence_after_sync();
             if (!ok) break;
@@ -238,7 +263,7 @@ __global__ void __launch_bounds__(128) k_cache_infer(NetDev net, InferIO io, uin
                     *reinterpret_cast<uint4 *>(act + tc::op_offset(row, c + 8, kTile)) =
                         make_uint4(pack2(h[8], h[9]), pack2(h[10], h[11]), pack2(h[12], h[13]), pack2(h[14], h[15]));
                 }
-                operand_sync();
+                group_operand_sync(bar_id);
             } else {
                 float v[16];
                 tc::tmem_ld16(taddr + lane_base, v);
@@ -257,16 +282,16 @@ __global__ void __launch_bounds__(128) k_cache_infer(NetDev net, InferIO io, uin
                     }
                 }
                 tc::fence_before_sync();
-                __syncthreads();
+                group_bar(bar_id);
                 tc::fence_after_sync();
             }
         }
     }
-    if (!ok && t == 0) atomicExch(status, 1u);
+    if (!ok && row == 0) atomicExch(status, 1u);
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) {
-        tc::tmem_dealloc(taddr, 64);
+        tc::tmem_dealloc(*tslot, 64 * kInferGroups);
         tc::tmem_relinquish();
     }
 }
@@ -541,6 +566,26 @@ __global__ void k_cache_targets(const float4 *rec, uint32_t n_train, uint32_t de
     }
 }
 
+// Synthetic queries (4 float4 each, slot = index) and training samples (16
+// floats) inside the encoding bounds, for the throughput measurement.
+__global__ void k_cache_synth(uint32_t n, NetDev net, float4 *q, float *samples) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t h = pcg_hash(i * 2654435761u + 17u);
+    auto rnd = [&]() { h = pcg_hash(h); return (float)(h >> 8) * (1.0f / 16777216.0f); };
+    float s[16];
+    for (int a = 0; a < 3; ++a) s[a] = net.lo[a] + rnd() / fmaxf(net.inv_ext[a], 1e-30f);
+    for (int k = 3; k < 9; ++k) s[k] = 2.0f * rnd() - 1.0f;
+    for (int k = 9; k < 15; ++k) s[k] = rnd();
+    s[15] = 1.0f;
+    q[4 * (size_t)i] = make_float4(s[0], s[1], s[2], __uint_as_float(i));
+    q[4 * (size_t)i + 1] = make_float4(s[3], s[4], s[5], 0.0f);
+    q[4 * (size_t)i + 2] = make_float4(s[6], s[7], s[8], 0.0f);
+    q[4 * (size_t)i + 3] = make_float4(s[9], s[10], s[11], 0.0f);
+    float4 *d = reinterpret_cast<float4 *>(samples + 16 * (size_t)i);
+    for (int k = 0; k < 4; ++k) d[k] = make_float4(s[4 * k], s[4 * k + 1], s[4 * k + 2], s[4 * k + 3]);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------- cache state
@@ -635,8 +680,8 @@ cudaError_t cache_infer_device(CacheState *c, const float4 *q, const uint32_t *d
     if (max_n == 0) return cudaSuccess;
     InferIO io{q, d_count, max_n, L, thr, out};
     const uint32_t tiles = (max_n + kTile - 1) / kTile;
-    const int blocks = (int)std::min<uint32_t>(tiles, (uint32_t)sm_count() * 3u);
-    k_cache_infer<<<blocks, 128, kInferSmem, st>>>(net_of(c), io, c->status.as<uint32_t>());
+    const int blocks = (int)std::max<uint32_t>(1u, std::min<uint32_t>((tiles + kInferGroups - 1) / kInferGroups, (uint32_t)sm_count() * 2u));
+    k_cache_infer<<<blocks, 128 * kInferGroups, kInferSmem, st>>>(net_of(c), io, c->status.as<uint32_t>());
     note_launch();
     return cudaGetLastError();
 }
@@ -731,6 +776,42 @@ cudaError_t cache_train_records(CacheState *c, const float4 *rec, uint32_t n_tra
 }
 
 bool cache_ready(const CacheState *c) { return c && c->has_params; }
+
+// Device time of inference over n synthetic queries and of one training step
+// (gradients, reduction, Adam) on n synthetic samples, averaged over reps.
+cudaError_t cache_bench(CacheState *c, uint32_t n, uint32_t reps, float *ms_infer, float *ms_train, cudaStream_t st) {
+    if (!c->has_params) return cudaErrorInvalidValue;
+    cudaError_t e;
+    if ((e = c->queries.ensure((size_t)n * 64 + (size_t)n * 12)) != cudaSuccess) return e;
+    if ((e = c->samples.ensure((size_t)n * 64 + 64)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(c->status.p, 0, 4, st)) != cudaSuccess) return e;
+    k_cache_synth<<<(n + 255) / 256, 256, 0, st>>>(n, net_of(c), c->queries.as<float4>(), c->samples.as<float>());
+    note_launch();
+    float *out = reinterpret_cast<float *>(c->queries.as<char>() + (size_t)n * 64);
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    auto timed = [&](auto fn, float *ms_out) -> cudaError_t {
+        cudaError_t err = fn();                        // warm-up
+        if (err != cudaSuccess) return err;
+        cudaEventRecord(a, st);
+        for (uint32_t r = 0; r < reps; ++r)
+            if ((err = fn()) != cudaSuccess) return err;
+        cudaEventRecord(b, st);
+        if ((err = cudaEventSynchronize(b)) != cudaSuccess) return err;
+        float t = 0.0f;
+        cudaEventElapsedTime(&t, a, b);
+        *ms_out = t / (float)std::max(reps, 1u);
+        return cudaSuccess;
+    };
+    e = timed([&]() { return cache_infer_device(c, c->queries.as<float4>(), nullptr, n, out, nullptr, nullptr, st); },
+              ms_infer);
+    if (e == cudaSuccess)
+        e = timed([&]() { return cache_step_device(c, c->samples.as<float>(), n, n, 1e-6f, st); }, ms_train);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return e;
+}
 
 cudaError_t cache_train_host(CacheState *c, const float *samples16, uint32_t n, uint32_t steps, uint32_t batch,
                              float lr, float *out_loss, float *out_grad, cudaStream_t st, bool *timed_out) {

@@ -49,18 +49,23 @@ __host__ __device__ inline float band_freq(int k) {
     return f[k];
 }
 
-// The 96 features of a query (12 floats: p, w_o, n, a).
+// The 96 features of a query (12 floats: p, w_o, n, a).  The bands come from
+// one sine / cosine of pi * u per axis by the double-angle recurrence
+// s' = (2 s) c, c' = c c - s s (each band doubles the frequency).
 __host__ __device__ inline void encode(const float q[12], const float lo[3], const float inv_ext[3],
                                        float f[kIn]) {
     float u[3];
     for (int a = 0; a < 3; ++a) {
         float v = (q[a] - lo[a]) * inv_ext[a];
         u[a] = v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v);
+        float s, c;
+        fm_sincos(u[a] * band_freq(0), &s, &c);
         for (int k = 0; k < kBands; ++k) {
-            float s, c;
-            fm_sincos(u[a] * band_freq(k), &s, &c);
             f[24 * a + 2 * k] = s;
             f[24 * a + 2 * k + 1] = c;
+            const float s2 = (2.0f * s) * c, c2 = c * c - s * s;
+            s = s2;
+            c = c2;
         }
     }
     for (int k = 0; k < 9; ++k) f[72 + k] = q[3 + k];

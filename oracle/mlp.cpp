@@ -41,11 +41,14 @@ void encode(const float *q, const float *lo, const float *inv, float *f) {
     for (int a = 0; a < 3; ++a) {
         float v = (q[a] - lo[a]) * inv[a];
         u[a] = v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v);
+        float s, c;                                  /* band k = sin / cos of pi 2^k u, by doubling */
+        of_sincos(u[a] * 3.141592653589793f, &s, &c);
         for (int k = 0; k < BANDS; ++k) {
-            float s, c;
-            of_sincos(u[a] * (float)(3.141592653589793 * (double)(1 << k)), &s, &c);
             f[24 * a + 2 * k] = s;
             f[24 * a + 2 * k + 1] = c;
+            const float s2 = (2.0f * s) * c, c2 = c * c - s * s;
+            s = s2;
+            c = c2;
         }
     }
     for (int k = 0; k < 9; ++k) f[72 + k] = q[3 + k];
