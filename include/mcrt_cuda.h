@@ -211,7 +211,9 @@ typedef struct {
  * reports it.  A variant whose stack overflows on this scene is not a
  * candidate (its time is reported as -1).  out_ms (optional) receives the
  * extend time of every variant; its capacity is 8 floats. */
-mcrt_status mcrt_variant_info(uint32_t variant, uint32_t *out4);   /* width, block, min blocks, stack */
+/* out5: BVH width, block size, minimum resident blocks per SM, stack depth,
+ * idle lanes at which a warp fetches new rays */
+mcrt_status mcrt_variant_info(uint32_t variant, uint32_t *out5);
 mcrt_status mcrt_autotune(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t w, uint32_t h, uint32_t spp,
                           const mcrt_render_opts *opts, uint32_t *out_variant, float *out_ms);
 

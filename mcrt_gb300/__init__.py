@@ -173,9 +173,9 @@ def materials(entries) -> np.ndarray:
 
 def variant_info(variant: int) -> dict:
     """Closest-hit kernel variant: BVH width, block size, minimum resident blocks, stack depth."""
-    out = (c_uint32 * 4)()
+    out = (c_uint32 * 5)()
     check(lib().mcrt_variant_info(variant, out))
-    return dict(width=out[0], block=out[1], min_blocks=out[2], stack=out[3])
+    return dict(width=out[0], block=out[1], min_blocks=out[2], stack=out[3], refill=out[4])
 
 
 def make_rays(org, dirs, tmin=1e-4, tmax=1e9) -> np.ndarray:

@@ -1178,12 +1178,12 @@ mcrt_status mcrt_read_accum(mcrt_ctx *ctx, float *out_rgba, double *accum_rgb, f
     return MCRT_OK;
 }
 
-mcrt_status mcrt_variant_info(uint32_t variant, uint32_t *out4) {
-    if (!out4 || variant >= (uint32_t)mcrt::extend_variant_count())
-        return fail(nullptr, MCRT_ERR_INVALID_ARG, "variant out of range or out4 NULL");
-    int info[4];
+mcrt_status mcrt_variant_info(uint32_t variant, uint32_t *out5) {
+    if (!out5 || variant >= (uint32_t)mcrt::extend_variant_count())
+        return fail(nullptr, MCRT_ERR_INVALID_ARG, "variant out of range or out5 NULL");
+    int info[5];
     mcrt::extend_variant_info((int)variant, info);
-    for (int k = 0; k < 4; ++k) out4[k] = (uint32_t)info[k];
+    for (int k = 0; k < 5; ++k) out5[k] = (uint32_t)info[k];
     return MCRT_OK;
 }
 

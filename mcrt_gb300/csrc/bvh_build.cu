@@ -139,8 +139,12 @@ struct BuildState {
     uint32_t *n_a, *n_b;              // internal: left bfs, right bfs; leaf: start, count
     uint32_t *n_leaf;                 // 1 = leaf
     uint32_t *n_size, *n_pre;         // subtree size, pre-order index
-    uint32_t *counters;               // [0] next task count, [1] bfs node count
+    uint32_t *counters;               // [0] next task count, [1] bfs node count, [2] tasks of the
+                                      // current level (small-task levels), [3] largest new task
+    uint32_t *level_end;              // small-task levels: bfs node count after each level
 };
+constexpr uint32_t kSmallTask = 256;       // tasks up to this size are built by one warp each
+constexpr uint32_t kMaxLevels = 4096;
 }  // namespace
 
 struct BvhScratch {
@@ -336,16 +340,16 @@ __device__ __forceinline__ uint32_t new_bfs_node(BuildState &S, const Aabb &b) {
     return id;
 }
 
-// One thread per task: SAH split selection (bvh.rs:388-463) and child creation.
-__global__ void k_split(BuildState S, int cur, uint32_t ntasks) {
-    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntasks) return;
-    uint32_t start = S.t_start[cur][t], n = S.t_count[cur][t], node = S.t_node[cur][t];
-    const float *tb = S.t_bounds[cur] + 6 * t;
+// SAH split selection of one task (bvh.rs:388-463) from its node bounds tb,
+// centroid bounds cb and bins, and child creation: child nodes, and child
+// tasks (buffer cur ^ 1) for children above the leaf size.  Returns the split
+// (axis * 16 + bin) or -1 when the task becomes a leaf; *lcount = primitives
+// going left; child_task[c] = the child's task id or -1 (leaf).
+__device__ int split_task(BuildState &S, int cur, uint32_t start, uint32_t n, uint32_t node, const float *tb,
+                          const float *cb, const float *bins, uint32_t *lcount, int child_task[2]) {
+    child_task[0] = child_task[1] = -1;
     Aabb nb;
     for (int a = 0; a < 3; ++a) { nb.mn[a] = tb[a]; nb.mx[a] = tb[3 + a]; }
-    const float *cb = S.t_cb + 6 * t;
-    const float *bins = S.t_bins + (size_t)t * kTaskBinWords;
     float parent = fmaxf(half_area(nb), 1e-8f);
     float best_cost = (float)n;
     int best_axis = 0, best_bin = 0;
@@ -381,12 +385,10 @@ __global__ void k_split(BuildState S, int cur, uint32_t ntasks) {
         }
     }
     if (!(found && best_split > 0 && best_split < n)) {
-        S.t_split[t] = -1;
         S.n_leaf[node] = 1; S.n_a[node] = start; S.n_b[node] = n;
-        return;
+        return -1;
     }
-    S.t_split[t] = best_axis * 16 + best_bin;
-    S.t_lcount[t] = best_split;
+    *lcount = best_split;
     S.n_leaf[node] = 0;
     uint32_t counts[2] = {best_split, n - best_split};
     uint32_t starts[2] = {start, start + best_split};
@@ -398,6 +400,7 @@ __global__ void k_split(BuildState S, int cur, uint32_t ntasks) {
             S.n_leaf[child[c]] = 1; S.n_a[child[c]] = starts[c]; S.n_b[child[c]] = counts[c];
         } else {
             S.n_leaf[child[c]] = 0;
+            atomicMax(S.counters + 3, counts[c]);
             uint32_t nt2 = atomicAdd(S.counters, 1u);
             S.t_start[cur ^ 1][nt2] = starts[c];
             S.t_count[cur ^ 1][nt2] = counts[c];
@@ -408,10 +411,132 @@ __global__ void k_split(BuildState S, int cur, uint32_t ntasks) {
             }
             // the child's positions learn their new task id in k_scatter through this map
             S.n_size[child[c]] = nt2;      // temporary: child node -> task id
+            child_task[c] = (int)nt2;
         }
     }
     S.n_a[node] = child[0];
     S.n_b[node] = child[1];
+    return best_axis * 16 + best_bin;
+}
+
+// One thread per task: split selection and child creation.
+__global__ void k_split(BuildState S, int cur, uint32_t ntasks) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntasks) return;
+    uint32_t lcount = 0;
+    int child_task[2];
+    const int sp = split_task(S, cur, S.t_start[cur][t], S.t_count[cur][t], S.t_node[cur][t], S.t_bounds[cur] + 6 * t,
+                              S.t_cb + 6 * t, S.t_bins + (size_t)t * kTaskBinWords, &lcount, child_task);
+    S.t_split[t] = sp;
+    if (sp >= 0) S.t_lcount[t] = lcount;
+}
+
+// Levels whose tasks are all small: one warp per task does what the per-level
+// kernels above do for the whole array — centroid bounds (warp reduction),
+// bins (shared-memory atomics private to the warp), the split of lane 0, and a
+// stable partition by ballot — so a level is one launch.  Positions that land
+// in a leaf are written to both permutation buffers (they never move again).
+__global__ void __launch_bounds__(256) k_small_level(BuildState S, int cur) {
+    __shared__ float wbins[8][kTaskBinWords];
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t ntasks = S.counters[2];
+    if (t >= ntasks) return;                                   // whole warps leave together
+    const uint32_t start = S.t_start[cur][t], n = S.t_count[cur][t], node = S.t_node[cur][t];
+    const uint32_t *perm_in = S.perm[cur];
+    // centroid bounds
+    float cmn[3], cmx[3];
+    for (int k = 0; k < 3; ++k) { cmn[k] = __int_as_float(0x7f800000); cmx[k] = __int_as_float(0xff800000); }
+    for (uint32_t i = start + lane; i < start + n; i += 32) {
+        const float4 c = S.pcen[perm_in[i]];
+        cmn[0] = fminf(cmn[0], c.x); cmn[1] = fminf(cmn[1], c.y); cmn[2] = fminf(cmn[2], c.z);
+        cmx[0] = fmaxf(cmx[0], c.x); cmx[1] = fmaxf(cmx[1], c.y); cmx[2] = fmaxf(cmx[2], c.z);
+    }
+    for (int off = 16; off > 0; off >>= 1)
+        for (int k = 0; k < 3; ++k) {
+            cmn[k] = fminf(cmn[k], __shfl_xor_sync(0xffffffffu, cmn[k], off));
+            cmx[k] = fmaxf(cmx[k], __shfl_xor_sync(0xffffffffu, cmx[k], off));
+        }
+    const float cb[6] = {cmn[0], cmn[1], cmn[2], cmx[0], cmx[1], cmx[2]};
+    // bins
+    float *bins = wbins[w];
+    for (int k = lane; k < kTaskBinWords; k += 32) {
+        const uint32_t f = k % kBinStride;
+        bins[k] = f == 0 ? 0.0f : __int_as_float(f < 4 ? 0x7f800000 : 0xff800000);
+    }
+    __syncwarp();
+    for (uint32_t i = start + lane; i < start + n; i += 32) {
+        const uint32_t id = perm_in[i];
+        const float4 c = S.pcen[id], bmn = S.pmin[id], bmx = S.pmax[id];
+        const float cc[3] = {c.x, c.y, c.z};
+        for (int axis = 0; axis < 3; ++axis) {
+            const float len = cb[3 + axis] - cb[axis];
+            if (len < 1e-8f) continue;
+            const uint32_t b = bin_of(cc[axis], cb[axis], len);
+            float *dst = bins + (axis * kBins + (int)b) * kBinStride;
+            atomicAdd(reinterpret_cast<unsigned *>(dst), 1u);
+            atomic_min_f(dst + 1, bmn.x); atomic_min_f(dst + 2, bmn.y); atomic_min_f(dst + 3, bmn.z);
+            atomic_max_f(dst + 4, bmx.x); atomic_max_f(dst + 5, bmx.y); atomic_max_f(dst + 6, bmx.z);
+        }
+    }
+    __syncwarp();
+    // split (lane 0), broadcast
+    int sp = -1, ct0 = -1, ct1 = -1;
+    uint32_t lcount = 0;
+    if (lane == 0) {
+        int child_task[2];
+        sp = split_task(S, cur, start, n, node, S.t_bounds[cur] + 6 * t, cb, bins, &lcount, child_task);
+        ct0 = child_task[0];
+        ct1 = child_task[1];
+    }
+    sp = __shfl_sync(0xffffffffu, sp, 0);
+    lcount = __shfl_sync(0xffffffffu, lcount, 0);
+    ct0 = __shfl_sync(0xffffffffu, ct0, 0);
+    ct1 = __shfl_sync(0xffffffffu, ct1, 0);
+    uint32_t *out0 = S.perm[cur ^ 1], *out1 = S.perm[cur];
+    if (sp < 0) {                                              // a leaf: positions stay
+        for (uint32_t i = start + lane; i < start + n; i += 32) out0[i] = perm_in[i];
+        return;
+    }
+    // stable partition by ballot, in position order
+    const int axis = sp >> 4, bin = sp & 15;
+    const float len = cb[3 + axis] - cb[axis];
+    uint32_t lbase = start, rbase = start + lcount;
+    for (uint32_t base = start; base < start + n; base += 32) {
+        const uint32_t i = base + lane;
+        const bool valid = i < start + n;
+        uint32_t id = 0;
+        bool left = false;
+        if (valid) {
+            id = perm_in[i];
+            const float4 c = S.pcen[id];
+            const float cc = axis == 0 ? c.x : (axis == 1 ? c.y : c.z);
+            left = bin_of(cc, cb[axis], len) <= (uint32_t)bin;
+        }
+        const unsigned lm = __ballot_sync(0xffffffffu, valid && left);
+        const unsigned rm = __ballot_sync(0xffffffffu, valid && !left);
+        const unsigned below = (1u << lane) - 1u;
+        if (valid) out0[left ? lbase + __popc(lm & below) : rbase + __popc(rm & below)] = id;
+        lbase += __popc(lm);
+        rbase += __popc(rm);
+    }
+    // a child that is a leaf: its positions are final, copy them into the input
+    // buffer too (after every read of that buffer above)
+    __syncwarp();
+    if (ct0 < 0)
+        for (uint32_t i = start + lane; i < start + lcount; i += 32) out1[i] = out0[i];
+    if (ct1 < 0)
+        for (uint32_t i = start + lcount + lane; i < start + n; i += 32) out1[i] = out0[i];
+}
+
+// Between small-task levels: the next level's task count, the node count of
+// the level just built, and a fresh child-task counter.
+__global__ void k_level_advance(BuildState S, uint32_t level) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        S.counters[2] = S.counters[0];
+        S.counters[0] = 0;
+        S.level_end[level] = S.counters[1];
+    }
 }
 
 __global__ void k_flags(BuildState S, int cur) {
@@ -511,6 +636,7 @@ static cudaError_t gpu_build(const mcrt_gpu_vertex *d_verts, const mcrt_gpu_tria
         acc(tc * 24); acc(tc * 4 * kTaskBinWords); acc(tc * 4); acc(tc * 4);
         acc(nn * 16); acc(nn * 16); acc(nn * 4); acc(nn * 4); acc(nn * 4); acc(nn * 4); acc(nn * 4);
         acc(64);
+        acc(kMaxLevels * 4);
         acc(scan_tmp_words(nt) * 4);
         cudaError_t e = cudaMalloc(&sc->mem, bytes);
         if (e != cudaSuccess) { if (err) *err = "BVH scratch allocation failed"; return e; }
@@ -531,6 +657,7 @@ static cudaError_t gpu_build(const mcrt_gpu_vertex *d_verts, const mcrt_gpu_tria
         S.n_a = carve<uint32_t>(p, nn); S.n_b = carve<uint32_t>(p, nn); S.n_leaf = carve<uint32_t>(p, nn);
         S.n_size = carve<uint32_t>(p, nn); S.n_pre = carve<uint32_t>(p, nn);
         S.counters = carve<uint32_t>(p, 16);
+        S.level_end = carve<uint32_t>(p, kMaxLevels);
         sc->scan_tmp = carve<uint32_t>(p, scan_tmp_words(nt));
     }
     BuildState S = sc->s;
@@ -564,11 +691,14 @@ static cudaError_t gpu_build(const mcrt_gpu_vertex *d_verts, const mcrt_gpu_tria
     level_begin.push_back(0);
     uint32_t ntasks = 1;
     int cur = 0;
-    uint32_t host_counters[2] = {0, 1};
+    uint32_t host_counters[4] = {0, 1, 0, 0};
+    uint32_t max_task = nt;
     int guard = 0;
-    while (ntasks > 0) {
-        if (++guard > 4096) { if (err) *err = "BVH build exceeded 4096 levels"; return cudaErrorUnknown; }
+    // levels with a large task: per-level kernels over the whole array
+    while (ntasks > 0 && max_task > kSmallTask) {
+        if (++guard > (int)kMaxLevels) { if (err) *err = "BVH build exceeded 4096 levels"; return cudaErrorUnknown; }
         cudaMemsetAsync(S.counters, 0, 4, st);
+        cudaMemsetAsync(S.counters + 3, 0, 4, st);
         uint32_t nw = ntasks * (6 + kTaskBinWords);
         k_task_reset<<<(nw + TB - 1) / TB, TB, 0, st>>>(S, ntasks); ::mcrt::note_launch();
         k_centroid_bounds<<<nb, TB, 0, st>>>(S, cur); ::mcrt::note_launch();
@@ -577,28 +707,64 @@ static cudaError_t gpu_build(const mcrt_gpu_vertex *d_verts, const mcrt_gpu_tria
         k_flags<<<nb, TB, 0, st>>>(S, cur); ::mcrt::note_launch();
         exclusive_scan_u32(S.flags, S.scan, nt, sc->scan_tmp, st);
         k_scatter<<<nb, TB, 0, st>>>(S, cur); ::mcrt::note_launch();
-        cudaMemcpyAsync(host_counters, S.counters, 8, cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(host_counters, S.counters, 16, cudaMemcpyDeviceToHost, st);
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) { if (err) *err = "BVH build level failed"; return e; }
-        level_begin.push_back(level_begin.back());   // placeholder, fixed below
+        level_begin.push_back(host_counters[1]);      // the nodes this level created: [previous, this)
         ntasks = host_counters[0];
+        max_task = host_counters[3];
         cur ^= 1;
     }
+    // the remaining levels: every task small, one warp per task, launched in
+    // batches with one host round trip per batch
+    if (ntasks > 0) {
+        const uint32_t tcap = nt / 4 + 1;                // tasks hold > 4 primitives
+        // finished positions so far live in perm[cur]; give the other buffer them too
+        cudaMemcpyAsync(S.perm[cur ^ 1], S.perm[cur], 4 * (size_t)nt, cudaMemcpyDeviceToDevice, st);
+        host_counters[0] = ntasks;                        // the tasks of buffer cur
+        cudaMemcpyAsync(S.counters, host_counters, 4, cudaMemcpyHostToDevice, st);
+        uint32_t level = 0;
+        uint64_t bound = ntasks;                          // upper bound of the next level's tasks
+        while (ntasks > 0) {
+            for (int k = 0; k < 8; ++k) {
+                if (level + 1 >= kMaxLevels) { if (err) *err = "BVH build exceeded 4096 levels"; return cudaErrorUnknown; }
+                k_level_advance<<<1, 1, 0, st>>>(S, level++); ::mcrt::note_launch();
+                const uint32_t warps = (uint32_t)std::min<uint64_t>(bound, tcap);
+                k_small_level<<<(warps + 7) / 8, 256, 0, st>>>(S, cur); ::mcrt::note_launch();
+                cur ^= 1;
+                bound = std::min<uint64_t>(2 * bound, tcap);
+            }
+            cudaMemcpyAsync(host_counters, S.counters, 16, cudaMemcpyDeviceToHost, st);
+            cudaError_t e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) { if (err) *err = "BVH build level failed"; return e; }
+            ntasks = host_counters[0];
+            bound = ntasks;
+        }
+        k_level_advance<<<1, 1, 0, st>>>(S, level++); ::mcrt::note_launch();
+        std::vector<uint32_t> ends(level);
+        cudaMemcpyAsync(ends.data(), S.level_end, 4 * (size_t)level, cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(host_counters, S.counters, 16, cudaMemcpyDeviceToHost, st);
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) { if (err) *err = "BVH build level failed"; return e; }
+        for (uint32_t k = 1; k < level; ++k) level_begin.push_back(ends[k]);   // ends[0]: the last level above
+    }
     const uint32_t n_bfs = host_counters[1];
-    // BFS ids are allocated level by level, but children of one level are
-    // appended in parallel; sizes therefore are computed by repeated sweeps over
-    // all nodes in decreasing id order of levels.  Node ids of a level are all
-    // greater than those of the previous level, so a reverse sweep per level of
-    // creation is exact; we recover the level boundaries from a parent walk.
+    // BFS ids are allocated level by level: the children of the nodes created by
+    // one level are all created by the next, so subtree sizes are exact when the
+    // levels are swept bottom-up and pre-order indices when swept top-down.
     {
-        // compute depth-ordered processing with a simple iterative approach:
-        // repeat k_sizes over all nodes `depth` times (depth = number of levels + 1).
-        uint32_t levels = (uint32_t)level_begin.size();
-        for (uint32_t it = 0; it <= levels; ++it)
-            k_sizes<<<(n_bfs + TB - 1) / TB, TB, 0, st>>>(S, 0, n_bfs); ::mcrt::note_launch();
+        level_begin[0] = 0;
+        level_begin.insert(level_begin.begin() + 1, 1u);   // level 0 is the root alone
+        const size_t nl = level_begin.size() - 1;
+        for (size_t k = nl; k-- > 0;) {
+            const uint32_t b = level_begin[k], e = level_begin[k + 1];
+            if (e > b) { k_sizes<<<(e - b + TB - 1) / TB, TB, 0, st>>>(S, b, e); ::mcrt::note_launch(); }
+        }
         cudaMemsetAsync(S.n_pre, 0, 4, st);
-        for (uint32_t it = 0; it <= levels; ++it)
-            k_preorder<<<(n_bfs + TB - 1) / TB, TB, 0, st>>>(S, 0, n_bfs); ::mcrt::note_launch();
+        for (size_t k = 0; k < nl; ++k) {
+            const uint32_t b = level_begin[k], e = level_begin[k + 1];
+            if (e > b) { k_preorder<<<(e - b + TB - 1) / TB, TB, 0, st>>>(S, b, e); ::mcrt::note_launch(); }
+        }
     }
     k_emit<<<(n_bfs + TB - 1) / TB, TB, 0, st>>>(S, n_bfs, d_nodes); ::mcrt::note_launch();
     cudaMemcpyAsync(d_order, S.perm[cur], 4 * (size_t)nt, cudaMemcpyDeviceToDevice, st);

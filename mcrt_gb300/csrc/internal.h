@@ -97,8 +97,8 @@ struct RenderParams {
 
 constexpr uint32_t kTrainRecordFloat4 = 6;
 int extend_variant_count();
-// (BVH width, block size, minimum resident blocks, stack depth) of a variant.
-void extend_variant_info(int v, int out[4]);
+// (BVH width, block size, minimum resident blocks, stack depth, refill lanes) of a variant.
+void extend_variant_info(int v, int out[5]);
 // Occupancy queries of every variant; call before capturing launches in a graph.
 void prepare_extend_variants();
 

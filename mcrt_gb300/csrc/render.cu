@@ -504,19 +504,19 @@ __global__ void k_raygen(DeviceScene S, RenderParams P, PathBuffers B, int keep_
 //    current closest t) as in the reference order, so the hit is the same.
 // Sphere BVHs (the reference's binding 5) are traversed at ray fetch with the
 // reference-order walk (spheres_hit); their count is small.
-constexpr int kRefill = 8;
 
 // Closest-hit kernel variants, chosen per scene by mcrt_autotune: BVH width
 // (compact binary or quantised 4-wide), block size, minimum resident blocks per
-// SM (the register budget ptxas must meet) and traversal stack depth (entries
-// of 8 bytes in local memory; a ray that would overflow it raises the overflow
-// flag and the render reports MCRT_ERR_STACK_OVERFLOW, so the autotuner drops
-// a variant whose stack is too short for the scene).
-struct ExtendVariant { int width, block, min_blocks, stack; };
+// SM (the register budget ptxas must meet), traversal stack depth (entries of 8
+// bytes in local memory; a ray that would overflow it raises the overflow flag
+// and the render reports MCRT_ERR_STACK_OVERFLOW, so the autotuner drops a
+// variant whose stack is too short for the scene) and the number of idle lanes
+// at which a warp fetches new rays.
+struct ExtendVariant { int width, block, min_blocks, stack, refill; };
 constexpr int kExtendVariants = 8;
 constexpr ExtendVariant kVariantTable[kExtendVariants] = {
-    {2, 128, 8, 64}, {2, 128, 8, 32}, {2, 128, 12, 32}, {2, 256, 4, 64},
-    {2, 64, 16, 32}, {4, 128, 8, 64}, {4, 128, 8, 32}, {4, 128, 12, 32}};
+    {2, 128, 8, 64, 8}, {2, 128, 8, 32, 8}, {2, 64, 16, 32, 4}, {2, 256, 4, 64, 8},
+    {2, 64, 16, 32, 8}, {4, 128, 8, 64, 8}, {4, 128, 8, 32, 8}, {2, 64, 16, 32, 16}};
 
 // Visit an internal node of the compact binary layout: test both children,
 // continue with the nearer hit child, push the farther one.
@@ -600,7 +600,7 @@ __device__ __forceinline__ void visit_wide4(const DeviceScene &S, const RayInv &
     }
 }
 
-template <int WIDTH, int BLOCK, int MINB, int STACK>
+template <int WIDTH, int BLOCK, int MINB, int STACK, int REFILL>
 __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffers B, int qi) {
     const uint32_t n = B.counters[qi];
     if (blockIdx.x == 0 && threadIdx.x == 0) { B.counters[qi ^ 1] = 0; B.counters[2] = 0; }
@@ -623,7 +623,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
         // ---- refill idle lanes
         const bool idle = ray == 0xffffffffu;
         const unsigned idle_mask = __ballot_sync(0xffffffffu, idle);
-        if (!exhausted && (__popc(idle_mask) >= kRefill || idle_mask == 0xffffffffu)) {
+        if (!exhausted && (__popc(idle_mask) >= REFILL || idle_mask == 0xffffffffu)) {
             const int leader = __ffs(idle_mask) - 1;
             uint32_t base = 0;
             if ((int)lane == leader) base = atomicAdd(B.counters + 4, (uint32_t)__popc(idle_mask));
@@ -1175,7 +1175,8 @@ int extend_variant_count() { return kExtendVariants; }
 namespace {
 using ExtendKernel = void (*)(DeviceScene, PathBuffers, int);
 #define MCRT_EXTEND_KERNEL(i)                                                                            \
-    k_extend<kVariantTable[i].width, kVariantTable[i].block, kVariantTable[i].min_blocks, kVariantTable[i].stack>
+    k_extend<kVariantTable[i].width, kVariantTable[i].block, kVariantTable[i].min_blocks, kVariantTable[i].stack, \
+             kVariantTable[i].refill>
 const ExtendKernel kExtendKernels[kExtendVariants] = {MCRT_EXTEND_KERNEL(0), MCRT_EXTEND_KERNEL(1),
                                                       MCRT_EXTEND_KERNEL(2), MCRT_EXTEND_KERNEL(3),
                                                       MCRT_EXTEND_KERNEL(4), MCRT_EXTEND_KERNEL(5),
@@ -1184,9 +1185,9 @@ const ExtendKernel kExtendKernels[kExtendVariants] = {MCRT_EXTEND_KERNEL(0), MCR
 int g_extend_per_sm[kExtendVariants] = {0, 0, 0, 0, 0, 0, 0, 0};
 }  // namespace
 
-void extend_variant_info(int v, int out[4]) {
+void extend_variant_info(int v, int out[5]) {
     const ExtendVariant &e = kVariantTable[(v >= 0 && v < kExtendVariants) ? v : 0];
-    out[0] = e.width; out[1] = e.block; out[2] = e.min_blocks; out[3] = e.stack;
+    out[0] = e.width; out[1] = e.block; out[2] = e.min_blocks; out[3] = e.stack; out[4] = e.refill;
 }
 
 // Resident blocks per SM of every variant (an occupancy query, made before any
