@@ -16,8 +16,10 @@
 //     reference consecutive ranges of the ordered triangle list.
 // All arithmetic is the same IEEE sequence (compiled with -fmad=false), so the
 // output nodes equal the reference builder's bit for bit; only the order of the
-// primitives inside a leaf may differ (the partition here is stable by the
-// previous order, the reference uses an unstable sort).
+// primitives inside a leaf may differ (the partition here is stable, starting
+// from the Morton order of the centroids; the reference uses an unstable sort).
+#include <algorithm>
+#include <utility>
 #include <vector>
 
 #include "common.cuh"
@@ -99,6 +101,22 @@ __device__ __forceinline__ void atomic_max_f(float *a, float v) {
     else atomicMin(reinterpret_cast<unsigned *>(a), __float_as_uint(v));
 }
 
+// Order-preserving map of floats onto unsigned integers (the order the float
+// atomics above use: -0 below +0), so min / max reduce as integers (redux.sync).
+__device__ __forceinline__ unsigned f2ord(float f) {
+    const unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned o) {
+    return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
+constexpr unsigned kOrdPosInf = 0xff800000u;     // f2ord(+inf): empty minimum
+constexpr unsigned kOrdNegInf = 0x007fffffu;     // f2ord(-inf): empty maximum
+constexpr unsigned kFull = 0xffffffffu;
+
+// Positions per block of the whole-array passes (4 per thread).
+constexpr uint32_t kPosPerBlock = 1024;
+
 constexpr int kBins = 8;
 constexpr uint32_t kLeafMax = 4;
 constexpr int kBinStride = 7;                    // count, min xyz, max xyz
@@ -139,11 +157,25 @@ struct BuildState {
     uint32_t *n_a, *n_b;              // internal: left bfs, right bfs; leaf: start, count
     uint32_t *n_leaf;                 // 1 = leaf
     uint32_t *n_size, *n_pre;         // subtree size, pre-order index
-    uint32_t *counters;               // [0] next task count, [1] bfs node count, [2] tasks of the
-                                      // current level (small-task levels), [3] largest new task
-    uint32_t *level_end;              // small-task levels: bfs node count after each level
+    // Tasks of a level: large ones (above kSmallTask primitives) at indices
+    // 0, 1, ... of a task buffer, built by the whole-array passes; small ones
+    // at tcap - 1, tcap - 2, ... of the same buffer, one warp each; tiny ones
+    // (at most kTinyTask) in their own buffers, one thread each.
+    uint32_t tcap;                    // task buffer capacity (a level has at most nt / 5 tasks)
+    uint32_t *y_start[2], *y_count[2], *y_node[2];
+    float *y_bounds[2];               // tiny tasks (double-buffered), 6 bounds each
+    uint32_t *counters;               // [0] large tasks of the next level, [1] bfs node count,
+                                      // [4] small tasks of the next level, [5] of the current level,
+                                      // [6] tiny tasks of the next level, [7] of the current level
+    uint32_t *level_end;              // bfs node count at the start of each level
+    // spatial order: primitives are built in the order of their centroids'
+    // Morton codes (radix-sorted), so a warp's positions are neighbours
+    uint32_t *rkey[2], *rval[2];      // sort keys / primitive ids (ping-pong)
+    uint32_t *rhist, *roffs;          // digit counts per tile and their exclusive scan
+    float4 *qmin, *qmax, *qcen;       // second set of primitive bounds: the reordering target
 };
 constexpr uint32_t kSmallTask = 256;       // tasks up to this size are built by one warp each
+constexpr uint32_t kTinyTask = 8;          // and up to this size by one thread each
 constexpr uint32_t kMaxLevels = 4096;
 }  // namespace
 
@@ -209,27 +241,144 @@ __global__ void k_root_init(BuildState S) {
             S.t_bounds[0][a] = __int_as_float(0x7f800000);
             S.t_bounds[0][3 + a] = __int_as_float(0xff800000);
         }
-        S.counters[1] = 1;
+    }
+    if (blockIdx.x == 0 && threadIdx.x < 16) S.counters[threadIdx.x] = threadIdx.x == 1 ? 1u : 0u;
+}
+
+// Root bounds: per-thread min / max over 4 primitives, warp and block
+// reductions on the ordered integers, six global atomics per block.
+__global__ void __launch_bounds__(256) k_root_bounds(BuildState S) {
+    __shared__ unsigned sh[6];
+    if (threadIdx.x < 6) sh[threadIdx.x] = threadIdx.x < 3 ? kOrdPosInf : kOrdNegInf;
+    __syncthreads();
+    const uint32_t first = blockIdx.x * kPosPerBlock, end = min(first + kPosPerBlock, S.nt);
+    unsigned o[6] = {kFull, kFull, kFull, 0u, 0u, 0u};
+    for (uint32_t i = first + threadIdx.x; i < end; i += 256) {
+        const float4 a = S.pmin[i], b = S.pmax[i];
+        o[0] = min(o[0], f2ord(a.x)); o[1] = min(o[1], f2ord(a.y)); o[2] = min(o[2], f2ord(a.z));
+        o[3] = max(o[3], f2ord(b.x)); o[4] = max(o[4], f2ord(b.y)); o[5] = max(o[5], f2ord(b.z));
+    }
+    for (int a = 0; a < 3; ++a) {
+        o[a] = __reduce_min_sync(kFull, o[a]);
+        o[3 + a] = __reduce_max_sync(kFull, o[3 + a]);
+    }
+    if ((threadIdx.x & 31u) == 0)
+        for (int a = 0; a < 3; ++a) { atomicMin(&sh[a], o[a]); atomicMax(&sh[3 + a], o[3 + a]); }
+    __syncthreads();
+    if (threadIdx.x < 3) atomic_min_f(&S.t_bounds[0][threadIdx.x], ord2f(sh[threadIdx.x]));
+    else if (threadIdx.x < 6) atomic_max_f(&S.t_bounds[0][threadIdx.x], ord2f(sh[threadIdx.x]));
+}
+
+// ---- spatial order of the primitives
+// The tree does not depend on the order the primitives start in (binning and
+// the stable partition are decided by centroids alone); only the order inside
+// a leaf does.  Starting from Morton order keeps the 32 positions of a warp
+// neighbours in space at every level, so their bins mostly agree and the
+// warp reductions above take one pass.
+
+__device__ __forceinline__ uint32_t morton_expand10(uint32_t v) {
+    v &= 1023u;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+// 30-bit Morton code of each centroid on a 1024^3 grid over the root bounds.
+__global__ void k_morton(BuildState S) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.nt) return;
+    const float4 c = S.pcen[i];
+    const float cc[3] = {c.x, c.y, c.z};
+    uint32_t q[3];
+    for (int a = 0; a < 3; ++a) {
+        const float lo = S.t_bounds[0][a], ext = S.t_bounds[0][3 + a] - lo;
+        const float f = ext > 0.0f ? (cc[a] - lo) / ext * 1024.0f : 0.0f;
+        q[a] = min(f2u_sat(f), 1023u);
+    }
+    S.rkey[0][i] = (morton_expand10(q[0]) << 2) | (morton_expand10(q[1]) << 1) | morton_expand10(q[2]);
+    S.rval[0][i] = i;
+}
+
+constexpr uint32_t kRadixTile = 2048;      // keys per block of a radix pass (256 threads x 8 rounds)
+
+// Digit counts of one tile, stored digit-major (digit * tiles + tile) so that
+// their exclusive scan is each tile's output offset per digit.
+__global__ void __launch_bounds__(256) k_radix_hist(const uint32_t *keys, uint32_t n, int shift, uint32_t tiles,
+                                                    uint32_t *hist) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t base = blockIdx.x * kRadixTile;
+    for (uint32_t k = threadIdx.x; k < kRadixTile; k += 256) {
+        const uint32_t i = base + k;
+        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// Stable scatter of one tile by its digit: rounds of 256 keys in tile order;
+// within a round, a key's rank = the tile's running offset of its digit + the
+// counts of earlier warps + the lanes before it with the same digit.
+__global__ void __launch_bounds__(256) k_radix_scatter(const uint32_t *kin, const uint32_t *vin, uint32_t n, int shift,
+                                                       uint32_t tiles, const uint32_t *offs, uint32_t *kout,
+                                                       uint32_t *vout) {
+    __shared__ uint32_t wcnt[8][256];
+    __shared__ uint32_t wpre[8][256];
+    __shared__ uint32_t run[256];
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    for (int k = 0; k < 8; ++k) wcnt[k][threadIdx.x] = 0;
+    run[threadIdx.x] = offs[threadIdx.x * tiles + blockIdx.x];
+    __syncthreads();
+    const uint32_t base = blockIdx.x * kRadixTile;
+    const unsigned lanes_below = (1u << lane) - 1u;
+    for (uint32_t r = 0; r < kRadixTile / 256; ++r) {
+        const uint32_t i = base + r * 256 + threadIdx.x;
+        const bool valid = i < n;
+        uint32_t key = 0, val = 0, d = 256;             // 256: no key (its own group)
+        if (valid) { key = kin[i]; val = vin[i]; d = (key >> shift) & 255u; }
+        const unsigned peers = __match_any_sync(kFull, d);
+        const uint32_t prank = __popc(peers & lanes_below);
+        if (valid && prank == 0) wcnt[w][d] = __popc(peers);
+        __syncthreads();
+        {
+            const uint32_t dd = threadIdx.x;             // one digit per thread: prefix over the warps
+            uint32_t acc = run[dd];
+            for (int k = 0; k < 8; ++k) {
+                const uint32_t c = wcnt[k][dd];
+                wpre[k][dd] = acc;
+                acc += c;
+                wcnt[k][dd] = 0;
+            }
+            run[dd] = acc;
+        }
+        __syncthreads();
+        if (valid) {
+            const uint32_t pos = wpre[w][d] + prank;
+            kout[pos] = key;
+            vout[pos] = val;
+        }
     }
 }
 
-__global__ void k_root_bounds(BuildState S) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    float mn[3], mx[3];
-    bool valid = i < S.nt;
-    if (valid) {
-        float4 a = S.pmin[i], b = S.pmax[i];
-        mn[0] = a.x; mn[1] = a.y; mn[2] = a.z; mx[0] = b.x; mx[1] = b.y; mx[2] = b.z;
-    } else {
-        for (int k = 0; k < 3; ++k) { mn[k] = __int_as_float(0x7f800000); mx[k] = __int_as_float(0xff800000); }
-    }
-    for (int off = 16; off > 0; off >>= 1)
-        for (int k = 0; k < 3; ++k) {
-            mn[k] = fminf(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], off));
-            mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], off));
-        }
-    if ((threadIdx.x & 31) == 0)
-        for (int k = 0; k < 3; ++k) { atomic_min_f(&S.t_bounds[0][k], mn[k]); atomic_max_f(&S.t_bounds[0][3 + k], mx[k]); }
+// Primitive bounds into Morton order; positions start as the identity of that order.
+__global__ void k_reorder(BuildState S) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= S.nt) return;
+    const uint32_t id = S.rval[0][j];
+    S.qmin[j] = S.pmin[id];
+    S.qmax[j] = S.pmax[id];
+    S.qcen[j] = S.pcen[id];
+    S.perm[0][j] = j;
+    S.ptask[0][j] = 0;
+}
+
+// Output order: the primitive ids of the final positions (Morton index -> id).
+__global__ void k_final_order(const uint32_t *perm, const uint32_t *sorted_ids, uint32_t n, uint32_t *out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = sorted_ids[perm[i]];
 }
 
 __global__ void k_task_reset(BuildState S, uint32_t ntasks) {
@@ -246,32 +395,67 @@ __global__ void k_task_reset(BuildState S, uint32_t ntasks) {
     }
 }
 
-// Warp-level segmented reduction helper: lanes with the same task combine first.
-__global__ void k_centroid_bounds(BuildState S, int cur) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    int task = i < S.nt ? S.ptask[cur][i] : -1;
-    float c[3] = {0, 0, 0};
-    if (task >= 0) {
-        float4 cc = S.pcen[S.perm[cur][i]];
-        c[0] = cc.x; c[1] = cc.y; c[2] = cc.z;
-    }
-    unsigned same = __match_any_sync(0xffffffffu, task);
-    int leader = __ffs(same) - 1;
-    float mn[3] = {c[0], c[1], c[2]}, mx[3] = {c[0], c[1], c[2]};
-    if (same == 0xffffffffu) {
-        for (int off = 16; off > 0; off >>= 1)
-            for (int k = 0; k < 3; ++k) {
-                mn[k] = fminf(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], off));
-                mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], off));
-            }
-        if ((threadIdx.x & 31) != 0 || task < 0) return;
-    } else if (task < 0) {
+// First and last position of a block; the block's task if every position in
+// between belongs to it (tasks are contiguous ranges, so the ends decide), else -1.
+__device__ __forceinline__ int block_single_task(const BuildState &S, int cur, uint32_t first, uint32_t end) {
+    const int t0 = S.ptask[cur][first], t1 = S.ptask[cur][end - 1];
+    return (t0 == t1 && t0 >= 0) ? t0 : -1;
+}
+
+// Centroid bounds per task.  Lanes reduce first (one pass per distinct task in
+// the warp, redux.sync on the ordered integers); a block inside one task
+// combines its warps in shared memory and issues six global atomics.
+__global__ void __launch_bounds__(256) k_centroid_bounds(BuildState S, int cur) {
+    __shared__ unsigned sh[6];
+    __shared__ int block_task;
+    const uint32_t first = blockIdx.x * kPosPerBlock;
+    const uint32_t end = min(first + kPosPerBlock, S.nt);
+    const uint32_t lane = threadIdx.x & 31u;
+    if (threadIdx.x == 0) block_task = block_single_task(S, cur, first, end);
+    if (threadIdx.x < 6) sh[threadIdx.x] = threadIdx.x < 3 ? kOrdPosInf : kOrdNegInf;
+    __syncthreads();
+    const int bt = block_task;
+    if (bt >= 0) {
+        unsigned o[6] = {kFull, kFull, kFull, 0u, 0u, 0u};
+        for (uint32_t i = first + threadIdx.x; i < end; i += 256) {
+            const float4 c = S.pcen[S.perm[cur][i]];
+            const unsigned q[3] = {f2ord(c.x), f2ord(c.y), f2ord(c.z)};
+            for (int a = 0; a < 3; ++a) { o[a] = min(o[a], q[a]); o[3 + a] = max(o[3 + a], q[a]); }
+        }
+        for (int a = 0; a < 3; ++a) {
+            o[a] = __reduce_min_sync(kFull, o[a]);
+            o[3 + a] = __reduce_max_sync(kFull, o[3 + a]);
+        }
+        if (lane == 0)
+            for (int a = 0; a < 3; ++a) { atomicMin(&sh[a], o[a]); atomicMax(&sh[3 + a], o[3 + a]); }
+        __syncthreads();
+        if (threadIdx.x < 3) atomic_min_f(&S.t_cb[6 * bt + threadIdx.x], ord2f(sh[threadIdx.x]));
+        else if (threadIdx.x < 6) atomic_max_f(&S.t_cb[6 * bt + threadIdx.x], ord2f(sh[threadIdx.x]));
         return;
     }
-    (void)leader;
-    for (int k = 0; k < 3; ++k) {
-        atomic_min_f(&S.t_cb[6 * task + k], mn[k]);
-        atomic_max_f(&S.t_cb[6 * task + 3 + k], mx[k]);
+    for (uint32_t base = first + (threadIdx.x & ~31u); base < end; base += 256) {   // warp-uniform
+        const uint32_t i = base + lane;
+        const int task = i < end ? S.ptask[cur][i] : -1;
+        float4 c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (task >= 0) c = S.pcen[S.perm[cur][i]];
+        const unsigned q[3] = {f2ord(c.x), f2ord(c.y), f2ord(c.z)};
+        unsigned pending = __ballot_sync(kFull, task >= 0);
+        while (pending) {
+            const int leader = __ffs(pending) - 1;
+            const int lt = __shfl_sync(kFull, task, leader);
+            const bool mine = task == lt;
+            pending &= ~__ballot_sync(kFull, mine);
+            unsigned r[6];
+            for (int a = 0; a < 3; ++a) {
+                r[a] = __reduce_min_sync(kFull, mine ? q[a] : kFull);
+                r[3 + a] = __reduce_max_sync(kFull, mine ? q[a] : 0u);
+            }
+            if ((int)lane == leader)
+                for (int a = 0; a < 3; ++a) {
+                    atomic_min_f(&S.t_cb[6 * lt + a], ord2f(r[a]));
+                    atomic_max_f(&S.t_cb[6 * lt + 3 + a], ord2f(r[3 + a]));
+                }
+        }
     }
 }
 
@@ -281,152 +465,373 @@ __device__ __forceinline__ uint32_t bin_of(float c, float cmin, float len) {
     return b > (uint32_t)(kBins - 1) ? (uint32_t)(kBins - 1) : b;
 }
 
-// Bin accumulation.  A block whose positions all belong to one task reduces in
-// shared memory first; otherwise each primitive adds to global bins.
+// One warp's contribution to the bins of one axis: lanes with the same
+// (task, bin) key form a group (match.any) and reduce within it (redux.sync
+// on the group's mask, the ordered integers); the group's first lane adds the
+// result — into the shared bins `sh` (ordered-integer form) when given, else
+// into the task's global bins.
+__device__ __forceinline__ void bin_axis_warp(BuildState &S, unsigned *sh, int axis, bool valid, int task,
+                                              uint32_t b, const unsigned mn[3], const unsigned mx[3],
+                                              uint32_t lane) {
+    const unsigned key = valid ? ((unsigned)task << 3) | b : kFull;
+    const unsigned peers = __match_any_sync(kFull, key);
+    if (!valid) return;
+    unsigned r[6];
+    for (int a = 0; a < 3; ++a) {
+        r[a] = __reduce_min_sync(peers, mn[a]);
+        r[3 + a] = __reduce_max_sync(peers, mx[a]);
+    }
+    if ((int)lane != __ffs(peers) - 1) return;
+    const int o = (axis * kBins + (int)b) * kBinStride;
+    if (sh) {
+        atomicAdd(sh + o, (unsigned)__popc(peers));
+        for (int a = 0; a < 3; ++a) { atomicMin(sh + o + 1 + a, r[a]); atomicMax(sh + o + 4 + a, r[3 + a]); }
+    } else {
+        float *g = S.t_bins + (size_t)task * kTaskBinWords + o;
+        atomicAdd(reinterpret_cast<unsigned *>(g), (unsigned)__popc(peers));
+        for (int a = 0; a < 3; ++a) {
+            atomic_min_f(g + 1 + a, ord2f(r[a]));
+            atomic_max_f(g + 4 + a, ord2f(r[3 + a]));
+        }
+    }
+}
+
+// One warp's contribution to the bins of all three axes (task < 0: lane
+// without a primitive).  An axis on which every lane has the same (task, bin)
+// adds the warp's union of primitive bounds, reduced once for all such axes;
+// the other axes reduce by groups (bin_axis_warp).  b[axis] = the lane's bin
+// on each axis with an extent (0 otherwise).
+__device__ __forceinline__ void bins_warp(BuildState &S, unsigned *sh, int task, float4 c, const float cb[6],
+                                          const unsigned mn[3], const unsigned mx[3], uint32_t lane,
+                                          uint32_t b[3]) {
+    const float cc[3] = {c.x, c.y, c.z};
+    bool valid[3];
+    bool uni[3];
+    for (int axis = 0; axis < 3; ++axis) {
+        const float len = cb[3 + axis] - cb[axis];
+        valid[axis] = task >= 0 && !(len < 1e-8f);
+        b[axis] = valid[axis] ? bin_of(cc[axis], cb[axis], len) : 0u;
+        const unsigned key = valid[axis] ? ((unsigned)task << 3) | b[axis] : kFull;
+        const unsigned k0 = __shfl_sync(kFull, key, 0);
+        uni[axis] = __all_sync(kFull, key == k0) && k0 != kFull;
+    }
+    if (uni[0] || uni[1] || uni[2]) {                 // warp-uniform; every lane holds a primitive
+        unsigned r[6];
+        for (int a = 0; a < 3; ++a) {
+            r[a] = __reduce_min_sync(kFull, mn[a]);
+            r[3 + a] = __reduce_max_sync(kFull, mx[a]);
+        }
+        if (lane == 0)
+            for (int axis = 0; axis < 3; ++axis) {
+                if (!uni[axis]) continue;
+                const int o = (axis * kBins + (int)b[axis]) * kBinStride;
+                if (sh) {
+                    atomicAdd(sh + o, 32u);
+                    for (int a = 0; a < 3; ++a) { atomicMin(sh + o + 1 + a, r[a]); atomicMax(sh + o + 4 + a, r[3 + a]); }
+                } else {
+                    float *g = S.t_bins + (size_t)task * kTaskBinWords + o;
+                    atomicAdd(reinterpret_cast<unsigned *>(g), 32u);
+                    for (int a = 0; a < 3; ++a) {
+                        atomic_min_f(g + 1 + a, ord2f(r[a]));
+                        atomic_max_f(g + 4 + a, ord2f(r[3 + a]));
+                    }
+                }
+            }
+    }
+    for (int axis = 0; axis < 3; ++axis)
+        if (!uni[axis]) bin_axis_warp(S, sh, axis, valid[axis], task, b[axis], mn, mx, lane);
+}
+
+// Bin accumulation (count and primitive-bounds union per bin and axis).  Warps
+// reduce lanes of equal (task, bin) first; a block inside one task collects
+// its warps in shared memory and adds the block's bins to the global ones.
 __global__ void __launch_bounds__(256) k_bins(BuildState S, int cur) {
-    __shared__ float sh[kTaskBinWords];
+    __shared__ unsigned sh[kTaskBinWords];
     __shared__ int block_task;
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    int task = i < S.nt ? S.ptask[cur][i] : -1;
-    uint32_t last = min((uint32_t)(blockIdx.x + 1) * blockDim.x, S.nt) - 1;
-    if (threadIdx.x == 0) {
-        int t0 = S.ptask[cur][blockIdx.x * blockDim.x];
-        int t1 = S.ptask[cur][last];
-        block_task = (t0 == t1 && t0 >= 0) ? t0 : -1;
-    }
+    const uint32_t first = blockIdx.x * kPosPerBlock;
+    const uint32_t end = min(first + kPosPerBlock, S.nt);
+    const uint32_t lane = threadIdx.x & 31u;
+    if (threadIdx.x == 0) block_task = block_single_task(S, cur, first, end);
     for (int k = threadIdx.x; k < kTaskBinWords; k += blockDim.x) {
-        uint32_t f = k % kBinStride;
-        sh[k] = f == 0 ? 0.0f : __int_as_float(f < 4 ? 0x7f800000 : 0xff800000);
+        const uint32_t f = k % kBinStride;
+        sh[k] = f == 0 ? 0u : (f < 4 ? kOrdPosInf : kOrdNegInf);
     }
     __syncthreads();
-    // a block is single-task only if every position agrees (tasks are contiguous, so ends suffice)
-    const bool shared_mode = block_task >= 0;
-    if (task >= 0) {
-        uint32_t id = S.perm[cur][i];
-        float4 c = S.pcen[id], bmn = S.pmin[id], bmx = S.pmax[id];
-        const float *cb = S.t_cb + 6 * task;
-        float cc[3] = {c.x, c.y, c.z};
-        for (int axis = 0; axis < 3; ++axis) {
-            float len = cb[3 + axis] - cb[axis];
-            if (len < 1e-8f) continue;
-            uint32_t b = bin_of(cc[axis], cb[axis], len);
-            int o = (axis * kBins + (int)b) * kBinStride;
-            float *dst = shared_mode ? sh : S.t_bins + (size_t)task * kTaskBinWords;
-            atomicAdd(reinterpret_cast<unsigned *>(dst + o), 1u);
-            atomic_min_f(dst + o + 1, bmn.x); atomic_min_f(dst + o + 2, bmn.y); atomic_min_f(dst + o + 3, bmn.z);
-            atomic_max_f(dst + o + 4, bmx.x); atomic_max_f(dst + o + 5, bmx.y); atomic_max_f(dst + o + 6, bmx.z);
+    const int bt = block_task;
+    unsigned *dst = bt >= 0 ? sh : nullptr;
+    for (uint32_t base = first + (threadIdx.x & ~31u); base < end; base += 256) {   // warp-uniform
+        const uint32_t i = base + lane;
+        const int task = i < end ? S.ptask[cur][i] : -1;
+        if (__all_sync(kFull, task < 0)) continue;              // leaves and small tasks only
+        float4 c = make_float4(0.0f, 0.0f, 0.0f, 0.0f), bmn = c, bmx = c;
+        float cb[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        if (task >= 0) {
+            const uint32_t id = S.perm[cur][i];
+            c = S.pcen[id]; bmn = S.pmin[id]; bmx = S.pmax[id];
+            for (int k = 0; k < 6; ++k) cb[k] = S.t_cb[6 * task + k];
         }
+        const unsigned mn[3] = {f2ord(bmn.x), f2ord(bmn.y), f2ord(bmn.z)};
+        const unsigned mx[3] = {f2ord(bmx.x), f2ord(bmx.y), f2ord(bmx.z)};
+        uint32_t b[3];
+        bins_warp(S, dst, task, c, cb, mn, mx, lane, b);
     }
-    if (!shared_mode) return;
+    if (bt < 0) return;
     __syncthreads();
-    float *g = S.t_bins + (size_t)block_task * kTaskBinWords;
+    float *g = S.t_bins + (size_t)bt * kTaskBinWords;
     for (int k = threadIdx.x; k < kTaskBinWords; k += blockDim.x) {
-        uint32_t f = k % kBinStride;
+        const uint32_t f = k % kBinStride;
         if (f == 0) {
-            uint32_t cnt = __float_as_uint(sh[k]);
-            if (cnt) atomicAdd(reinterpret_cast<unsigned *>(g + k), cnt);
+            if (sh[k]) atomicAdd(reinterpret_cast<unsigned *>(g + k), sh[k]);
         } else if (f < 4) {
-            if (sh[k] != __int_as_float(0x7f800000)) atomic_min_f(g + k, sh[k]);
+            if (sh[k] != kOrdPosInf) atomic_min_f(g + k, ord2f(sh[k]));
         } else {
-            if (sh[k] != __int_as_float(0xff800000)) atomic_max_f(g + k, sh[k]);
+            if (sh[k] != kOrdNegInf) atomic_max_f(g + k, ord2f(sh[k]));
         }
     }
 }
 
-__device__ __forceinline__ uint32_t new_bfs_node(BuildState &S, const Aabb &b) {
-    uint32_t id = atomicAdd(S.counters + 1, 1u);
-    S.n_min[id] = make_float4(b.mn[0], b.mn[1], b.mn[2], 0.0f);
-    S.n_max[id] = make_float4(b.mx[0], b.mx[1], b.mx[2], 0.0f);
-    return id;
+// SAH split choice of one task (bvh.rs:388-463) from its node bounds tb,
+// centroid bounds cb and bins.  Returns the split (axis * 16 + bin), or -1 when
+// the task stays a leaf; *lcount = primitives going left, *bl / *br = the
+// children's bounds.
+// Best split so far of the serial SAH sweep.
+struct SplitBest {
+    float cost;                    // starts at the leaf cost n
+    int axis = 0, bin = 0;
+    uint32_t l = 0;
+    bool found = false;
+    Aabb lb, rb;
+};
+__device__ __forceinline__ SplitBest split_best_init(uint32_t n) {
+    SplitBest b;
+    b.cost = (float)n;
+    b.lb = aabb_empty();
+    b.rb = aabb_empty();
+    return b;
 }
 
-// SAH split selection of one task (bvh.rs:388-463) from its node bounds tb,
-// centroid bounds cb and bins, and child creation: child nodes, and child
-// tasks (buffer cur ^ 1) for children above the leaf size.  Returns the split
-// (axis * 16 + bin) or -1 when the task becomes a leaf; *lcount = primitives
-// going left; child_task[c] = the child's task id or -1 (leaf).
-__device__ int split_task(BuildState &S, int cur, uint32_t start, uint32_t n, uint32_t node, const float *tb,
-                          const float *cb, const float *bins, uint32_t *lcount, int child_task[2]) {
-    child_task[0] = child_task[1] = -1;
+// One axis of the SAH sweep (bvh.rs:388-463): prefix unions of bins 0..s,
+// suffix unions of bins 7..s+1, cost (A_l * n_l + A_r * n_r) / A_parent,
+// replaced only on a strictly smaller cost.  get(k, f) = field f of bin k
+// (0: count as bits, 1-3: min, 4-6: max).
+template <class Get>
+__device__ __forceinline__ void split_axis(int axis, float parent, Get get, SplitBest &best) {
+    Aabb bb[kBins];
+    uint32_t bc[kBins];
+    for (int k = 0; k < kBins; ++k) {
+        bc[k] = __float_as_uint(get(k, 0));
+        for (int a = 0; a < 3; ++a) { bb[k].mn[a] = get(k, 1 + a); bb[k].mx[a] = get(k, 4 + a); }
+    }
+    Aabb lb[kBins];
+    uint32_t lc[kBins];
+    lb[0] = bb[0]; lc[0] = bc[0];
+    for (int k = 1; k < kBins; ++k) { lb[k] = aabb_union(lb[k - 1], bb[k]); lc[k] = lc[k - 1] + bc[k]; }
+    Aabb rb = aabb_empty();
+    uint32_t rc = 0;
+    for (int s = kBins - 2; s >= 0; --s) {
+        rb = aabb_union(rb, bb[s + 1]);
+        rc += bc[s + 1];
+        const uint32_t l = lc[s];
+        if (l == 0 || rc == 0) continue;
+        const float cost = (half_area(lb[s]) * (float)l + half_area(rb) * (float)rc) / parent;
+        if (cost < best.cost) {
+            best.cost = cost; best.axis = axis; best.bin = s; best.l = l; best.found = true;
+            best.lb = lb[s]; best.rb = rb;
+        }
+    }
+}
+
+// The split of a finished sweep: axis * 16 + bin, or -1 for a leaf.
+__device__ __forceinline__ int split_result(const SplitBest &best, uint32_t n, uint32_t *lcount, Aabb *bl, Aabb *br) {
+    if (!(best.found && best.l > 0 && best.l < n)) return -1;
+    *lcount = best.l;
+    *bl = best.lb;
+    *br = best.rb;
+    return best.axis * 16 + best.bin;
+}
+
+__device__ __forceinline__ float node_half_area(const float *tb) {
     Aabb nb;
     for (int a = 0; a < 3; ++a) { nb.mn[a] = tb[a]; nb.mx[a] = tb[3 + a]; }
-    float parent = fmaxf(half_area(nb), 1e-8f);
-    float best_cost = (float)n;
-    int best_axis = 0, best_bin = 0;
-    uint32_t best_split = 0;
-    bool found = false;
-    Aabb best_l = aabb_empty(), best_r = aabb_empty();
-    for (int axis = 0; axis < 3; ++axis) {
-        float len = cb[3 + axis] - cb[axis];
-        if (len < 1e-8f) continue;
-        Aabb bb[kBins];
-        uint32_t bc[kBins];
-        for (int k = 0; k < kBins; ++k) {
-            const float *q = bins + (axis * kBins + k) * kBinStride;
-            bc[k] = __float_as_uint(q[0]);
-            for (int a = 0; a < 3; ++a) { bb[k].mn[a] = q[1 + a]; bb[k].mx[a] = q[4 + a]; }
-        }
-        Aabb lb[kBins];
-        uint32_t lc[kBins];
-        lb[0] = bb[0]; lc[0] = bc[0];
-        for (int k = 1; k < kBins; ++k) { lb[k] = aabb_union(lb[k - 1], bb[k]); lc[k] = lc[k - 1] + bc[k]; }
-        Aabb rb = aabb_empty();
-        uint32_t rc = 0;
-        for (int s = kBins - 2; s >= 0; --s) {
-            rb = aabb_union(rb, bb[s + 1]);
-            rc += bc[s + 1];
-            uint32_t l = lc[s];
-            if (l == 0 || rc == 0) continue;
-            float cost = (half_area(lb[s]) * (float)l + half_area(rb) * (float)rc) / parent;
-            if (cost < best_cost) {
-                best_cost = cost; best_axis = axis; best_bin = s; best_split = l; found = true;
-                best_l = lb[s]; best_r = rb;
-            }
-        }
-    }
-    if (!(found && best_split > 0 && best_split < n)) {
-        S.n_leaf[node] = 1; S.n_a[node] = start; S.n_b[node] = n;
-        return -1;
-    }
-    *lcount = best_split;
-    S.n_leaf[node] = 0;
-    uint32_t counts[2] = {best_split, n - best_split};
-    uint32_t starts[2] = {start, start + best_split};
-    const Aabb *cbx[2] = {&best_l, &best_r};
-    uint32_t child[2];
-    for (int c = 0; c < 2; ++c) {
-        child[c] = new_bfs_node(S, *cbx[c]);
-        if (counts[c] <= kLeafMax) {
-            S.n_leaf[child[c]] = 1; S.n_a[child[c]] = starts[c]; S.n_b[child[c]] = counts[c];
-        } else {
-            S.n_leaf[child[c]] = 0;
-            atomicMax(S.counters + 3, counts[c]);
-            uint32_t nt2 = atomicAdd(S.counters, 1u);
-            S.t_start[cur ^ 1][nt2] = starts[c];
-            S.t_count[cur ^ 1][nt2] = counts[c];
-            S.t_node[cur ^ 1][nt2] = child[c];
-            for (int a = 0; a < 3; ++a) {
-                S.t_bounds[cur ^ 1][6 * nt2 + a] = cbx[c]->mn[a];
-                S.t_bounds[cur ^ 1][6 * nt2 + 3 + a] = cbx[c]->mx[a];
-            }
-            // the child's positions learn their new task id in k_scatter through this map
-            S.n_size[child[c]] = nt2;      // temporary: child node -> task id
-            child_task[c] = (int)nt2;
-        }
-    }
-    S.n_a[node] = child[0];
-    S.n_b[node] = child[1];
-    return best_axis * 16 + best_bin;
+    return fmaxf(half_area(nb), 1e-8f);
 }
 
-// One thread per task: split selection and child creation.
+__device__ int choose_split(uint32_t n, const float *tb, const float *cb, const float *bins, uint32_t *lcount,
+                            Aabb *bl, Aabb *br) {
+    const float parent = node_half_area(tb);
+    SplitBest best = split_best_init(n);
+    for (int axis = 0; axis < 3; ++axis) {
+        const float len = cb[3 + axis] - cb[axis];
+        if (len < 1e-8f) continue;
+        const float *q = bins + axis * kBins * kBinStride;
+        split_axis(axis, parent, [&](int k, int f) { return q[k * kBinStride + f]; }, best);
+    }
+    return split_result(best, n, lcount, bl, br);
+}
+
+// choose_split evaluated by a warp.  Lane j < 21 takes the serial loop's j-th
+// candidate (axis j / 7, split 6 - j % 7) and forms its left union over bins
+// 0..s ascending and its right union over bins 7..s+1 descending — the serial
+// loop's operation order, so every cost has the same bits — and the cheapest
+// candidate below the leaf cost wins, ties to the earliest (the serial loop
+// replaces only on a strictly smaller cost).  Every lane gets the result.
+__device__ int choose_split_warp(uint32_t n, const float *tb, const float *cb, const float *bins, uint32_t lane,
+                                 uint32_t *lcount, Aabb *bl, Aabb *br) {
+    Aabb nb;
+    for (int a = 0; a < 3; ++a) { nb.mn[a] = tb[a]; nb.mx[a] = tb[3 + a]; }
+    const float parent = fmaxf(half_area(nb), 1e-8f);
+    const int axis = (int)lane / 7, s = 6 - (int)lane % 7;
+    bool ok = lane < 21u;
+    float cost = 0.0f;
+    uint32_t l = 0, rc = 0;
+    Aabb lb = aabb_empty(), rb = aabb_empty();
+    if (ok) {
+        const float len = cb[3 + axis] - cb[axis];
+        if (len < 1e-8f) {
+            ok = false;
+        } else {
+            const float *q = bins + axis * kBins * kBinStride;
+            auto box = [&](int k) {
+                Aabb b;
+                for (int a = 0; a < 3; ++a) { b.mn[a] = q[k * kBinStride + 1 + a]; b.mx[a] = q[k * kBinStride + 4 + a]; }
+                return b;
+            };
+            lb = box(0);
+            l = __float_as_uint(q[0]);
+            for (int k = 1; k <= s; ++k) { lb = aabb_union(lb, box(k)); l += __float_as_uint(q[k * kBinStride]); }
+            for (int k = kBins - 1; k > s; --k) { rb = aabb_union(rb, box(k)); rc += __float_as_uint(q[k * kBinStride]); }
+            if (l == 0 || rc == 0) ok = false;
+            else cost = (half_area(lb) * (float)l + half_area(rb) * (float)rc) / parent;
+            ok = ok && cost < (float)n;
+        }
+    }
+    const unsigned oc = ok ? f2ord(cost) : kFull;
+    const unsigned best = __reduce_min_sync(kFull, oc);
+    if (best == kFull) return -1;
+    const int win = (int)__reduce_min_sync(kFull, (ok && oc == best) ? lane : kFull);
+    *lcount = __shfl_sync(kFull, l, win);
+    for (int a = 0; a < 3; ++a) {
+        bl->mn[a] = __shfl_sync(kFull, lb.mn[a], win); bl->mx[a] = __shfl_sync(kFull, lb.mx[a], win);
+        br->mn[a] = __shfl_sync(kFull, rb.mn[a], win); br->mx[a] = __shfl_sync(kFull, rb.mx[a], win);
+    }
+    return (win / 7) * 16 + (6 - win % 7);
+}
+
+// Child tasks a split creates, by class: large (above kSmallTask primitives),
+// small (above kTinyTask) and tiny (above the leaf size).
+__device__ __forceinline__ uint32_t child_large(uint32_t n, uint32_t lcount) {
+    return (lcount > kSmallTask ? 1u : 0u) + (n - lcount > kSmallTask ? 1u : 0u);
+}
+__device__ __forceinline__ uint32_t child_small(uint32_t n, uint32_t lcount) {
+    auto small = [](uint32_t c) { return c > kTinyTask && c <= kSmallTask; };
+    return (small(lcount) ? 1u : 0u) + (small(n - lcount) ? 1u : 0u);
+}
+__device__ __forceinline__ uint32_t child_tiny(uint32_t n, uint32_t lcount) {
+    auto tiny = [](uint32_t c) { return c > kLeafMax && c <= kTinyTask; };
+    return (tiny(lcount) ? 1u : 0u) + (tiny(n - lcount) ? 1u : 0u);
+}
+constexpr uint32_t kSmallFlag = 0x80000000u;     // task map: the child is a small or tiny task
+
+// Node records of a task.  A leaf (sp < 0) keeps its range.  A split gets the
+// BFS ids child0, child0 + 1 for its children; its large children get the task
+// ids large0, large0 + 1, its small children small0, small0 + 1 (a small task
+// k is stored at index tcap - 1 - k) and its tiny children tiny0, tiny0 + 1
+// (in child order) in buffer nxt.  child_task[c] = -1 for a leaf child.  Ids
+// come from the caller, which reserves them for a whole warp with one atomic
+// each (same-address atomics per task serialise at the L2).
+__device__ void record_task(BuildState &S, int nxt, uint32_t start, uint32_t n, uint32_t node, int sp,
+                            uint32_t lcount, const Aabb &bl, const Aabb &br, uint32_t child0, uint32_t large0,
+                            uint32_t small0, uint32_t tiny0, int child_task[2]) {
+    child_task[0] = child_task[1] = -1;
+    if (sp < 0) {
+        S.n_leaf[node] = 1; S.n_a[node] = start; S.n_b[node] = n;
+        return;
+    }
+    S.n_leaf[node] = 0;
+    const uint32_t counts[2] = {lcount, n - lcount};
+    const uint32_t starts[2] = {start, start + lcount};
+    const Aabb *cbx[2] = {&bl, &br};
+    for (int c = 0; c < 2; ++c) {
+        const uint32_t id = child0 + (uint32_t)c;
+        S.n_min[id] = make_float4(cbx[c]->mn[0], cbx[c]->mn[1], cbx[c]->mn[2], 0.0f);
+        S.n_max[id] = make_float4(cbx[c]->mx[0], cbx[c]->mx[1], cbx[c]->mx[2], 0.0f);
+        if (counts[c] <= kLeafMax) {
+            S.n_leaf[id] = 1; S.n_a[id] = starts[c]; S.n_b[id] = counts[c];
+            continue;
+        }
+        S.n_leaf[id] = 0;
+        if (counts[c] <= kTinyTask) {
+            const uint32_t task = tiny0++;
+            S.y_start[nxt][task] = starts[c];
+            S.y_count[nxt][task] = counts[c];
+            S.y_node[nxt][task] = id;
+            for (int a = 0; a < 3; ++a) {
+                S.y_bounds[nxt][6 * task + a] = cbx[c]->mn[a];
+                S.y_bounds[nxt][6 * task + 3 + a] = cbx[c]->mx[a];
+            }
+            S.n_size[id] = kSmallFlag;
+            child_task[c] = (int)task;
+            continue;
+        }
+        const bool small = counts[c] <= kSmallTask;
+        const uint32_t task = small ? S.tcap - 1u - small0++ : large0++;
+        S.t_start[nxt][task] = starts[c];
+        S.t_count[nxt][task] = counts[c];
+        S.t_node[nxt][task] = id;
+        for (int a = 0; a < 3; ++a) {
+            S.t_bounds[nxt][6 * task + a] = cbx[c]->mn[a];
+            S.t_bounds[nxt][6 * task + 3 + a] = cbx[c]->mx[a];
+        }
+        // the child's positions learn their new task id in k_scatter through this map
+        S.n_size[id] = small ? kSmallFlag : task;      // temporary: child node -> task id
+        child_task[c] = (int)task;
+    }
+    S.n_a[node] = child0;
+    S.n_b[node] = child0 + 1;
+}
+
+// One thread per task: split choice, then ids for the children reserved per
+// warp (prefix sums by shuffles, one atomic per counter).
 __global__ void k_split(BuildState S, int cur, uint32_t ntasks) {
-    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntasks) return;
-    uint32_t lcount = 0;
-    int child_task[2];
-    const int sp = split_task(S, cur, S.t_start[cur][t], S.t_count[cur][t], S.t_node[cur][t], S.t_bounds[cur] + 6 * t,
-                              S.t_cb + 6 * t, S.t_bins + (size_t)t * kTaskBinWords, &lcount, child_task);
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31u;
+    if ((t & ~31u) >= ntasks) return;                     // whole warps
+    const bool active = t < ntasks;
+    uint32_t start = 0, n = 0, node = 0, lcount = 0;
+    int sp = -1;
+    Aabb bl = aabb_empty(), br = aabb_empty();
+    if (active) {
+        start = S.t_start[cur][t]; n = S.t_count[cur][t]; node = S.t_node[cur][t];
+        sp = choose_split(n, S.t_bounds[cur] + 6 * t, S.t_cb + 6 * t, S.t_bins + (size_t)t * kTaskBinWords, &lcount,
+                          &bl, &br);
+    }
+    const uint32_t my_nodes = sp >= 0 ? 2u : 0u;
+    const uint32_t my_large = sp >= 0 ? child_large(n, lcount) : 0u;
+    const uint32_t my_small = sp >= 0 ? child_small(n, lcount) : 0u;
+    const uint32_t my_tiny = sp >= 0 ? child_tiny(n, lcount) : 0u;
+    uint32_t pn = my_nodes, pl = my_large, ps = my_small, py = my_tiny;   // inclusive prefix sums over the warp
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t a = __shfl_up_sync(kFull, pn, off), b = __shfl_up_sync(kFull, pl, off);
+        const uint32_t c = __shfl_up_sync(kFull, ps, off), d = __shfl_up_sync(kFull, py, off);
+        if ((int)lane >= off) { pn += a; pl += b; ps += c; py += d; }
+    }
+    const uint32_t tn = __shfl_sync(kFull, pn, 31), tl = __shfl_sync(kFull, pl, 31);
+    const uint32_t ts = __shfl_sync(kFull, ps, 31), ty = __shfl_sync(kFull, py, 31);
+    uint32_t bn = 0, bl0 = 0, bs = 0, by = 0;
+    if (lane == 0) {
+        if (tn) bn = atomicAdd(S.counters + 1, tn);
+        if (tl) bl0 = atomicAdd(S.counters, tl);
+        if (ts) bs = atomicAdd(S.counters + 4, ts);
+        if (ty) by = atomicAdd(S.counters + 6, ty);
+    }
+    bn = __shfl_sync(kFull, bn, 0);
+    bl0 = __shfl_sync(kFull, bl0, 0);
+    bs = __shfl_sync(kFull, bs, 0);
+    by = __shfl_sync(kFull, by, 0);
+    if (!active) return;
+    int ct[2];
+    record_task(S, cur ^ 1, start, n, node, sp, lcount, bl, br, bn + pn - my_nodes, bl0 + pl - my_large,
+                bs + ps - my_small, by + py - my_tiny, ct);
     S.t_split[t] = sp;
     if (sp >= 0) S.t_lcount[t] = lcount;
 }
@@ -439,67 +844,119 @@ __global__ void k_split(BuildState S, int cur, uint32_t ntasks) {
 __global__ void __launch_bounds__(256) k_small_level(BuildState S, int cur) {
     __shared__ float wbins[8][kTaskBinWords];
     const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
-    const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t ntasks = S.counters[2];
-    if (t >= ntasks) return;                                   // whole warps leave together
+    const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (k >= S.counters[5]) return;                            // whole warps leave together
+    const uint32_t t = S.tcap - 1u - k;                        // small tasks from the top of the buffer
     const uint32_t start = S.t_start[cur][t], n = S.t_count[cur][t], node = S.t_node[cur][t];
     const uint32_t *perm_in = S.perm[cur];
+    // A task of at most 32 primitives keeps one per lane in registers for all
+    // passes (one load each); a larger one streams chunks of 32 per pass.
+    const bool one = n <= 32u;                                 // warp-uniform
+    const bool in0 = one && lane < n;
+    uint32_t id0 = 0;
+    float4 c0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), mn0 = c0, mx0 = c0;
+    if (in0) {
+        id0 = perm_in[start + lane];
+        c0 = S.pcen[id0]; mn0 = S.pmin[id0]; mx0 = S.pmax[id0];
+    }
     // centroid bounds
-    float cmn[3], cmx[3];
-    for (int k = 0; k < 3; ++k) { cmn[k] = __int_as_float(0x7f800000); cmx[k] = __int_as_float(0xff800000); }
-    for (uint32_t i = start + lane; i < start + n; i += 32) {
-        const float4 c = S.pcen[perm_in[i]];
-        cmn[0] = fminf(cmn[0], c.x); cmn[1] = fminf(cmn[1], c.y); cmn[2] = fminf(cmn[2], c.z);
-        cmx[0] = fmaxf(cmx[0], c.x); cmx[1] = fmaxf(cmx[1], c.y); cmx[2] = fmaxf(cmx[2], c.z);
+    unsigned co[6] = {kFull, kFull, kFull, 0u, 0u, 0u};
+    auto add_centroid = [&](float4 c) {
+        const unsigned q[3] = {f2ord(c.x), f2ord(c.y), f2ord(c.z)};
+        for (int a = 0; a < 3; ++a) { co[a] = min(co[a], q[a]); co[3 + a] = max(co[3 + a], q[a]); }
+    };
+    if (one) {
+        if (in0) add_centroid(c0);
+    } else {
+        for (uint32_t i = start + lane; i < start + n; i += 32) add_centroid(S.pcen[perm_in[i]]);
     }
-    for (int off = 16; off > 0; off >>= 1)
-        for (int k = 0; k < 3; ++k) {
-            cmn[k] = fminf(cmn[k], __shfl_xor_sync(0xffffffffu, cmn[k], off));
-            cmx[k] = fmaxf(cmx[k], __shfl_xor_sync(0xffffffffu, cmx[k], off));
-        }
-    const float cb[6] = {cmn[0], cmn[1], cmn[2], cmx[0], cmx[1], cmx[2]};
-    // bins
-    float *bins = wbins[w];
-    for (int k = lane; k < kTaskBinWords; k += 32) {
-        const uint32_t f = k % kBinStride;
-        bins[k] = f == 0 ? 0.0f : __int_as_float(f < 4 ? 0x7f800000 : 0xff800000);
+    float cb[6];
+    for (int a = 0; a < 3; ++a) {
+        cb[a] = ord2f(__reduce_min_sync(kFull, co[a]));
+        cb[3 + a] = ord2f(__reduce_max_sync(kFull, co[3 + a]));
     }
-    __syncwarp();
-    for (uint32_t i = start + lane; i < start + n; i += 32) {
-        const uint32_t id = perm_in[i];
-        const float4 c = S.pcen[id], bmn = S.pmin[id], bmx = S.pmax[id];
-        const float cc[3] = {c.x, c.y, c.z};
-        for (int axis = 0; axis < 3; ++axis) {
-            const float len = cb[3 + axis] - cb[axis];
-            if (len < 1e-8f) continue;
-            const uint32_t b = bin_of(cc[axis], cb[axis], len);
-            float *dst = bins + (axis * kBins + (int)b) * kBinStride;
-            atomicAdd(reinterpret_cast<unsigned *>(dst), 1u);
-            atomic_min_f(dst + 1, bmn.x); atomic_min_f(dst + 2, bmn.y); atomic_min_f(dst + 3, bmn.z);
-            atomic_max_f(dst + 4, bmx.x); atomic_max_f(dst + 5, bmx.y); atomic_max_f(dst + 6, bmx.z);
-        }
+    // bins (ordered-integer form while accumulating, then floats for the split);
+    // lane j < 24 initialises and converts bin j
+    unsigned *ubins = reinterpret_cast<unsigned *>(wbins[w]);
+    if (lane < 3u * kBins) {
+        unsigned *q = ubins + lane * kBinStride;
+        q[0] = 0u;
+        for (int a = 0; a < 3; ++a) { q[1 + a] = kOrdPosInf; q[4 + a] = kOrdNegInf; }
     }
     __syncwarp();
-    // split (lane 0), broadcast
-    int sp = -1, ct0 = -1, ct1 = -1;
+    uint32_t b0[3] = {0u, 0u, 0u};                             // one: the lane's bins
+    if (one) {
+        const unsigned mn[3] = {f2ord(mn0.x), f2ord(mn0.y), f2ord(mn0.z)};
+        const unsigned mx[3] = {f2ord(mx0.x), f2ord(mx0.y), f2ord(mx0.z)};
+        bins_warp(S, ubins, in0 ? 0 : -1, c0, cb, mn, mx, lane, b0);
+    } else {
+        for (uint32_t base = start; base < start + n; base += 32) {     // warp-uniform
+            const uint32_t i = base + lane;
+            const bool in = i < start + n;
+            float4 c = make_float4(0.0f, 0.0f, 0.0f, 0.0f), bmn = c, bmx = c;
+            if (in) {
+                const uint32_t id = perm_in[i];
+                c = S.pcen[id]; bmn = S.pmin[id]; bmx = S.pmax[id];
+            }
+            const unsigned mn[3] = {f2ord(bmn.x), f2ord(bmn.y), f2ord(bmn.z)};
+            const unsigned mx[3] = {f2ord(bmx.x), f2ord(bmx.y), f2ord(bmx.z)};
+            uint32_t b[3];
+            bins_warp(S, ubins, in ? 0 : -1, c, cb, mn, mx, lane, b);
+        }
+    }
+    __syncwarp();
+    if (lane < 3u * kBins) {
+        unsigned *q = ubins + lane * kBinStride;
+        for (int j = 1; j < kBinStride; ++j) q[j] = __float_as_uint(ord2f(q[j]));
+    }
+    __syncwarp();
+    const float *bins = wbins[w];
+    // split (the whole warp), child ids (lane 0)
+    int ct0 = -1, ct1 = -1;
     uint32_t lcount = 0;
+    Aabb bl = aabb_empty(), br = aabb_empty();
+    const int sp = choose_split_warp(n, S.t_bounds[cur] + 6 * t, cb, bins, lane, &lcount, &bl, &br);
     if (lane == 0) {
-        int child_task[2];
-        sp = split_task(S, cur, start, n, node, S.t_bounds[cur] + 6 * t, cb, bins, &lcount, child_task);
-        ct0 = child_task[0];
-        ct1 = child_task[1];
+        uint32_t c0 = 0, s0 = 0, y0 = 0;
+        if (sp >= 0) {
+            c0 = atomicAdd(S.counters + 1, 2u);
+            const uint32_t m = child_small(n, lcount);           // a small task has no large child
+            if (m) s0 = atomicAdd(S.counters + 4, m);
+            const uint32_t q = child_tiny(n, lcount);
+            if (q) y0 = atomicAdd(S.counters + 6, q);
+        }
+        int ct[2];
+        record_task(S, cur ^ 1, start, n, node, sp, lcount, bl, br, c0, 0u, s0, y0, ct);
+        ct0 = ct[0];
+        ct1 = ct[1];
     }
-    sp = __shfl_sync(0xffffffffu, sp, 0);
-    lcount = __shfl_sync(0xffffffffu, lcount, 0);
     ct0 = __shfl_sync(0xffffffffu, ct0, 0);
     ct1 = __shfl_sync(0xffffffffu, ct1, 0);
     uint32_t *out0 = S.perm[cur ^ 1], *out1 = S.perm[cur];
+    const unsigned below = (1u << lane) - 1u;
+    const int axis = sp >> 4, bin = sp & 15;
+    if (one) {
+        if (sp < 0) {                                          // a leaf: positions stay
+            if (in0) out0[start + lane] = id0;
+            return;
+        }
+        // the split axis has an extent, so b0[axis] is the lane's bin on it
+        const uint32_t my_bin = axis == 0 ? b0[0] : (axis == 1 ? b0[1] : b0[2]);
+        const bool left = in0 && my_bin <= (uint32_t)bin;
+        const unsigned lm = __ballot_sync(kFull, left);
+        const unsigned rm = __ballot_sync(kFull, in0 && !left);
+        if (in0) {
+            const uint32_t pos = left ? start + __popc(lm & below) : start + lcount + __popc(rm & below);
+            out0[pos] = id0;
+            if ((left ? ct0 : ct1) < 0) out1[pos] = id0;       // in a leaf: final in both buffers
+        }
+        return;
+    }
     if (sp < 0) {                                              // a leaf: positions stay
         for (uint32_t i = start + lane; i < start + n; i += 32) out0[i] = perm_in[i];
         return;
     }
     // stable partition by ballot, in position order
-    const int axis = sp >> 4, bin = sp & 15;
     const float len = cb[3 + axis] - cb[axis];
     uint32_t lbase = start, rbase = start + lcount;
     for (uint32_t base = start; base < start + n; base += 32) {
@@ -515,7 +972,6 @@ __global__ void __launch_bounds__(256) k_small_level(BuildState S, int cur) {
         }
         const unsigned lm = __ballot_sync(0xffffffffu, valid && left);
         const unsigned rm = __ballot_sync(0xffffffffu, valid && !left);
-        const unsigned below = (1u << lane) - 1u;
         if (valid) out0[left ? lbase + __popc(lm & below) : rbase + __popc(rm & below)] = id;
         lbase += __popc(lm);
         rbase += __popc(rm);
@@ -529,12 +985,118 @@ __global__ void __launch_bounds__(256) k_small_level(BuildState S, int cur) {
         for (uint32_t i = start + lcount + lane; i < start + n; i += 32) out1[i] = out0[i];
 }
 
+constexpr int kTinyThreads = 128;
+
+// Tiny tasks (at most kTinyTask primitives): one thread each runs the serial
+// algorithm — centroid bounds, the 8 bins of one axis at a time in its own
+// column of shared memory (a column per thread, so lanes never share a bank),
+// the sweep of split_axis, and the stable partition.  Child ids are reserved
+// per warp; every child of a tiny task is a leaf or tiny.
+__global__ void __launch_bounds__(kTinyThreads) k_tiny_level(BuildState S, int cur) {
+    __shared__ unsigned sb[kBins * kBinStride][kTinyThreads];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u;
+    const uint32_t k = blockIdx.x * kTinyThreads + tid;
+    const uint32_t ntiny = S.counters[7];
+    if ((k & ~31u) >= ntiny) return;                           // whole warps
+    const bool active = k < ntiny;
+    uint32_t start = 0, n = 0, node = 0;
+    if (active) { start = S.y_start[cur][k]; n = S.y_count[cur][k]; node = S.y_node[cur][k]; }
+    const uint32_t *perm_in = S.perm[cur];
+    unsigned co[6] = {kFull, kFull, kFull, 0u, 0u, 0u};
+    for (uint32_t j = 0; j < n; ++j) {
+        const float4 c = S.pcen[perm_in[start + j]];
+        const unsigned q[3] = {f2ord(c.x), f2ord(c.y), f2ord(c.z)};
+        for (int a = 0; a < 3; ++a) { co[a] = min(co[a], q[a]); co[3 + a] = max(co[3 + a], q[a]); }
+    }
+    float cb[6], tb[6];
+    for (int a = 0; a < 6; ++a) {
+        cb[a] = ord2f(co[a]);
+        tb[a] = active ? S.y_bounds[cur][6 * k + a] : 0.0f;
+    }
+    const float parent = node_half_area(tb);
+    SplitBest best = split_best_init(n);
+    for (int axis = 0; axis < 3; ++axis) {
+        const float len = cb[3 + axis] - cb[axis];
+        if (!active || len < 1e-8f) continue;
+        for (int b = 0; b < kBins; ++b) {
+            sb[b * kBinStride][tid] = 0u;
+            for (int a = 0; a < 3; ++a) {
+                sb[b * kBinStride + 1 + a][tid] = kOrdPosInf;
+                sb[b * kBinStride + 4 + a][tid] = kOrdNegInf;
+            }
+        }
+        for (uint32_t j = 0; j < n; ++j) {
+            const uint32_t id = perm_in[start + j];
+            const float4 c = S.pcen[id], bmn = S.pmin[id], bmx = S.pmax[id];
+            const float cc = axis == 0 ? c.x : (axis == 1 ? c.y : c.z);
+            const uint32_t o = bin_of(cc, cb[axis], len) * kBinStride;
+            const unsigned mn[3] = {f2ord(bmn.x), f2ord(bmn.y), f2ord(bmn.z)};
+            const unsigned mx[3] = {f2ord(bmx.x), f2ord(bmx.y), f2ord(bmx.z)};
+            sb[o][tid] += 1u;
+            for (int a = 0; a < 3; ++a) {
+                sb[o + 1 + a][tid] = min(sb[o + 1 + a][tid], mn[a]);
+                sb[o + 4 + a][tid] = max(sb[o + 4 + a][tid], mx[a]);
+            }
+        }
+        split_axis(axis, parent, [&](int b, int f) {
+            const unsigned v = sb[b * kBinStride + f][tid];
+            return f == 0 ? __uint_as_float(v) : ord2f(v);
+        }, best);
+    }
+    uint32_t lcount = 0;
+    Aabb bl = aabb_empty(), br = aabb_empty();
+    const int sp = active ? split_result(best, n, &lcount, &bl, &br) : -1;
+    // child ids for the warp: prefix sums by shuffles, one atomic per counter
+    const uint32_t my_nodes = sp >= 0 ? 2u : 0u;
+    const uint32_t my_tiny = sp >= 0 ? child_tiny(n, lcount) : 0u;
+    uint32_t pn = my_nodes, py = my_tiny;
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t a = __shfl_up_sync(kFull, pn, off), b = __shfl_up_sync(kFull, py, off);
+        if ((int)lane >= off) { pn += a; py += b; }
+    }
+    const uint32_t tn = __shfl_sync(kFull, pn, 31), ty = __shfl_sync(kFull, py, 31);
+    uint32_t bn = 0, by = 0;
+    if (lane == 0) {
+        if (tn) bn = atomicAdd(S.counters + 1, tn);
+        if (ty) by = atomicAdd(S.counters + 6, ty);
+    }
+    bn = __shfl_sync(kFull, bn, 0);
+    by = __shfl_sync(kFull, by, 0);
+    if (!active) return;
+    int ct[2];
+    record_task(S, cur ^ 1, start, n, node, sp, lcount, bl, br, bn + pn - my_nodes, 0u, 0u, by + py - my_tiny, ct);
+    uint32_t *out0 = S.perm[cur ^ 1], *out1 = S.perm[cur];
+    if (sp < 0) {                                              // a leaf: positions stay
+        for (uint32_t j = 0; j < n; ++j) out0[start + j] = perm_in[start + j];
+        return;
+    }
+    // stable partition, then the positions of leaf children into the input
+    // buffer too (after every read of it)
+    const int axis = sp >> 4, bin = sp & 15;
+    const float len = cb[3 + axis] - cb[axis];
+    uint32_t lp = start, rp = start + lcount;
+    for (uint32_t j = 0; j < n; ++j) {
+        const uint32_t id = perm_in[start + j];
+        const float4 c = S.pcen[id];
+        const float cc = axis == 0 ? c.x : (axis == 1 ? c.y : c.z);
+        const bool left = bin_of(cc, cb[axis], len) <= (uint32_t)bin;
+        out0[left ? lp++ : rp++] = id;
+    }
+    if (ct[0] < 0)
+        for (uint32_t p = start; p < start + lcount; ++p) out1[p] = out0[p];
+    if (ct[1] < 0)
+        for (uint32_t p = start + lcount; p < start + n; ++p) out1[p] = out0[p];
+}
+
 // Between small-task levels: the next level's task count, the node count of
 // the level just built, and a fresh child-task counter.
 __global__ void k_level_advance(BuildState S, uint32_t level) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
-        S.counters[2] = S.counters[0];
         S.counters[0] = 0;
+        S.counters[5] = S.counters[4];
+        S.counters[4] = 0;
+        S.counters[7] = S.counters[6];
+        S.counters[6] = 0;
         S.level_end[level] = S.counters[1];
     }
 }
@@ -562,6 +1124,7 @@ __global__ void k_scatter(BuildState S, int cur) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= S.nt) return;
     int task = S.ptask[cur][i];
+    if (task == -2) { S.ptask[cur ^ 1][i] = -2; return; }     // a small task's position: k_small_level moves it
     uint32_t id = S.perm[cur][i];
     if (task < 0) { S.perm[cur ^ 1][i] = id; S.ptask[cur ^ 1][i] = -1; return; }
     int sp = S.t_split[task];
@@ -574,7 +1137,8 @@ __global__ void k_scatter(BuildState S, int cur) {
     if (S.flags[i]) { pos = start + left_rank; child = S.n_a[node]; }
     else { pos = start + lcount + ((i - start) - left_rank); child = S.n_b[node]; }
     S.perm[cur ^ 1][pos] = id;
-    S.ptask[cur ^ 1][pos] = S.n_leaf[child] ? -1 : (int)S.n_size[child];
+    const uint32_t map = S.n_size[child];
+    S.ptask[cur ^ 1][pos] = S.n_leaf[child] ? -1 : (map == kSmallFlag ? -2 : (int)map);
 }
 
 // subtree sizes, bottom-up over a BFS id range
@@ -637,7 +1201,13 @@ static cudaError_t gpu_build(const mcrt_gpu_vertex *d_verts, const mcrt_gpu_tria
         acc(nn * 16); acc(nn * 16); acc(nn * 4); acc(nn * 4); acc(nn * 4); acc(nn * 4); acc(nn * 4);
         acc(64);
         acc(kMaxLevels * 4);
-        acc(scan_tmp_words(nt) * 4);
+        const size_t tiles = (n + kRadixTile - 1) / kRadixTile;
+        const size_t scan_words = std::max(scan_tmp_words(nt), scan_tmp_words((uint32_t)(256 * tiles)));
+        acc(scan_words * 4);
+        acc(n * 4); acc(n * 4); acc(n * 4); acc(n * 4);      // sort keys, ids (ping-pong)
+        acc(256 * tiles * 4); acc(256 * tiles * 4);          // digit counts, offsets
+        acc(n * 16); acc(n * 16); acc(n * 16);               // reordered bounds
+        for (int k = 0; k < 2; ++k) { acc(tc * 4); acc(tc * 4); acc(tc * 4); acc(tc * 24); }   // tiny tasks
         cudaError_t e = cudaMalloc(&sc->mem, bytes);
         if (e != cudaSuccess) { if (err) *err = "BVH scratch allocation failed"; return e; }
         sc->cap = nt;
@@ -658,17 +1228,26 @@ static cudaError_t gpu_build(const mcrt_gpu_vertex *d_verts, const mcrt_gpu_tria
         S.n_size = carve<uint32_t>(p, nn); S.n_pre = carve<uint32_t>(p, nn);
         S.counters = carve<uint32_t>(p, 16);
         S.level_end = carve<uint32_t>(p, kMaxLevels);
-        sc->scan_tmp = carve<uint32_t>(p, scan_tmp_words(nt));
+        sc->scan_tmp = carve<uint32_t>(p, scan_words);
+        S.rkey[0] = carve<uint32_t>(p, n); S.rkey[1] = carve<uint32_t>(p, n);
+        S.rval[0] = carve<uint32_t>(p, n); S.rval[1] = carve<uint32_t>(p, n);
+        S.rhist = carve<uint32_t>(p, 256 * tiles); S.roffs = carve<uint32_t>(p, 256 * tiles);
+        S.qmin = carve<float4>(p, n); S.qmax = carve<float4>(p, n); S.qcen = carve<float4>(p, n);
+        for (int k = 0; k < 2; ++k) {
+            S.y_start[k] = carve<uint32_t>(p, tc); S.y_count[k] = carve<uint32_t>(p, tc);
+            S.y_node[k] = carve<uint32_t>(p, tc); S.y_bounds[k] = carve<float>(p, 6 * tc);
+        }
     }
     BuildState S = sc->s;
     S.nt = nt;
+    S.tcap = nt / 4 + 1;                                 // tasks hold > 4 primitives
     const uint32_t TB = 256;
     const uint32_t nb = (nt + TB - 1) / TB;
     if (d_sph) k_sphere_bounds<<<nb, TB, 0, st>>>(d_sph, S);
     else k_prim_bounds<<<nb, TB, 0, st>>>(d_verts, d_tris, S);
     ::mcrt::note_launch();
     k_root_init<<<1, 32, 0, st>>>(S); ::mcrt::note_launch();
-    k_root_bounds<<<nb, TB, 0, st>>>(S); ::mcrt::note_launch();
+    k_root_bounds<<<(nt + kPosPerBlock - 1) / kPosPerBlock, 256, 0, st>>>(S); ::mcrt::note_launch();
     if (nt <= kLeafMax) {
         // the root is a single leaf (bvh.rs:301-304)
         std::vector<float> tb(6);
@@ -684,77 +1263,111 @@ static cudaError_t gpu_build(const mcrt_gpu_vertex *d_verts, const mcrt_gpu_tria
         *n_nodes_out = 1;
         return e;
     }
+    // Morton order: 4 stable radix passes of 8 bits over the 30-bit codes
+    // (ends in buffer 0), then the bounds are gathered into that order and the
+    // build runs on Morton indices; the output order maps them back to ids.
+    {
+        const uint32_t tiles = (nt + kRadixTile - 1) / kRadixTile;
+        k_morton<<<nb, TB, 0, st>>>(S); ::mcrt::note_launch();
+        for (int pass = 0; pass < 4; ++pass) {
+            const int in = pass & 1;
+            k_radix_hist<<<tiles, 256, 0, st>>>(S.rkey[in], nt, 8 * pass, tiles, S.rhist); ::mcrt::note_launch();
+            exclusive_scan_u32(S.rhist, S.roffs, 256 * tiles, sc->scan_tmp, st);
+            k_radix_scatter<<<tiles, 256, 0, st>>>(S.rkey[in], S.rval[in], nt, 8 * pass, tiles, S.roffs,
+                                                  S.rkey[in ^ 1], S.rval[in ^ 1]);
+            ::mcrt::note_launch();
+        }
+        k_reorder<<<nb, TB, 0, st>>>(S); ::mcrt::note_launch();
+        std::swap(S.pmin, S.qmin);
+        std::swap(S.pmax, S.qmax);
+        std::swap(S.pcen, S.qcen);
+    }
     // BFS node 0 = root
     cudaMemcpyAsync(S.n_min, S.t_bounds[0], 12, cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(S.n_max, S.t_bounds[0] + 3, 12, cudaMemcpyDeviceToDevice, st);
-    std::vector<uint32_t> level_begin;
-    level_begin.push_back(0);
-    uint32_t ntasks = 1;
+    // Levels.  Round r builds the tasks of level r: the large ones by the
+    // whole-array passes (while any exist; the host reads their count after
+    // each round), the small ones by k_small_level in the same round.  Once no
+    // large task is left, rounds run in batches of 8 with one host round trip
+    // per batch.  level_end[r] = the BFS node count when round r starts, so
+    // round r creates the nodes [level_end[r], level_end[r + 1]).
+    const uint32_t tcap = S.tcap;
+    const uint32_t nbp = (nt + kPosPerBlock - 1) / kPosPerBlock;
+    uint32_t n_large = 1, n_small = 0, n_tiny = 0;       // tasks of the current level
+    uint32_t level = 0;
     int cur = 0;
-    uint32_t host_counters[4] = {0, 1, 0, 0};
-    uint32_t max_task = nt;
-    int guard = 0;
-    // levels with a large task: per-level kernels over the whole array
-    while (ntasks > 0 && max_task > kSmallTask) {
-        if (++guard > (int)kMaxLevels) { if (err) *err = "BVH build exceeded 4096 levels"; return cudaErrorUnknown; }
-        cudaMemsetAsync(S.counters, 0, 4, st);
-        cudaMemsetAsync(S.counters + 3, 0, 4, st);
-        uint32_t nw = ntasks * (6 + kTaskBinWords);
-        k_task_reset<<<(nw + TB - 1) / TB, TB, 0, st>>>(S, ntasks); ::mcrt::note_launch();
-        k_centroid_bounds<<<nb, TB, 0, st>>>(S, cur); ::mcrt::note_launch();
-        k_bins<<<nb, TB, 0, st>>>(S, cur); ::mcrt::note_launch();
-        k_split<<<(ntasks + 127) / 128, 128, 0, st>>>(S, cur, ntasks); ::mcrt::note_launch();
+    uint32_t host_counters[8] = {};
+    auto advance = [&]() -> bool {
+        if (level + 1 >= kMaxLevels) {
+            if (err) *err = "BVH build exceeded 4096 levels";
+            return false;
+        }
+        k_level_advance<<<1, 1, 0, st>>>(S, level++); ::mcrt::note_launch();
+        return true;
+    };
+    // small and tiny tasks of the current level (bounds: at least their counts)
+    auto small_round = [&](uint64_t small_bound, uint64_t tiny_bound) {
+        const uint32_t warps = (uint32_t)std::min<uint64_t>(small_bound, tcap);
+        if (warps) { k_small_level<<<(warps + 7) / 8, 256, 0, st>>>(S, cur); ::mcrt::note_launch(); }
+        const uint32_t threads = (uint32_t)std::min<uint64_t>(tiny_bound, tcap);
+        if (threads) {
+            k_tiny_level<<<(threads + kTinyThreads - 1) / kTinyThreads, kTinyThreads, 0, st>>>(S, cur);
+            ::mcrt::note_launch();
+        }
+    };
+    while (n_large > 0) {
+        if (!advance()) return cudaErrorUnknown;
+        const uint32_t nw = n_large * (6 + kTaskBinWords);
+        k_task_reset<<<(nw + TB - 1) / TB, TB, 0, st>>>(S, n_large); ::mcrt::note_launch();
+        k_centroid_bounds<<<nbp, 256, 0, st>>>(S, cur); ::mcrt::note_launch();
+        k_bins<<<nbp, 256, 0, st>>>(S, cur); ::mcrt::note_launch();
+        k_split<<<(n_large + 127) / 128, 128, 0, st>>>(S, cur, n_large); ::mcrt::note_launch();
         k_flags<<<nb, TB, 0, st>>>(S, cur); ::mcrt::note_launch();
         exclusive_scan_u32(S.flags, S.scan, nt, sc->scan_tmp, st);
         k_scatter<<<nb, TB, 0, st>>>(S, cur); ::mcrt::note_launch();
-        cudaMemcpyAsync(host_counters, S.counters, 16, cudaMemcpyDeviceToHost, st);
-        cudaError_t e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) { if (err) *err = "BVH build level failed"; return e; }
-        level_begin.push_back(host_counters[1]);      // the nodes this level created: [previous, this)
-        ntasks = host_counters[0];
-        max_task = host_counters[3];
+        small_round(n_small, n_tiny);
         cur ^= 1;
-    }
-    // the remaining levels: every task small, one warp per task, launched in
-    // batches with one host round trip per batch
-    if (ntasks > 0) {
-        const uint32_t tcap = nt / 4 + 1;                // tasks hold > 4 primitives
-        // finished positions so far live in perm[cur]; give the other buffer them too
-        cudaMemcpyAsync(S.perm[cur ^ 1], S.perm[cur], 4 * (size_t)nt, cudaMemcpyDeviceToDevice, st);
-        host_counters[0] = ntasks;                        // the tasks of buffer cur
-        cudaMemcpyAsync(S.counters, host_counters, 4, cudaMemcpyHostToDevice, st);
-        uint32_t level = 0;
-        uint64_t bound = ntasks;                          // upper bound of the next level's tasks
-        while (ntasks > 0) {
-            for (int k = 0; k < 8; ++k) {
-                if (level + 1 >= kMaxLevels) { if (err) *err = "BVH build exceeded 4096 levels"; return cudaErrorUnknown; }
-                k_level_advance<<<1, 1, 0, st>>>(S, level++); ::mcrt::note_launch();
-                const uint32_t warps = (uint32_t)std::min<uint64_t>(bound, tcap);
-                k_small_level<<<(warps + 7) / 8, 256, 0, st>>>(S, cur); ::mcrt::note_launch();
-                cur ^= 1;
-                bound = std::min<uint64_t>(2 * bound, tcap);
-            }
-            cudaMemcpyAsync(host_counters, S.counters, 16, cudaMemcpyDeviceToHost, st);
-            cudaError_t e = cudaStreamSynchronize(st);
-            if (e != cudaSuccess) { if (err) *err = "BVH build level failed"; return e; }
-            ntasks = host_counters[0];
-            bound = ntasks;
-        }
-        k_level_advance<<<1, 1, 0, st>>>(S, level++); ::mcrt::note_launch();
-        std::vector<uint32_t> ends(level);
-        cudaMemcpyAsync(ends.data(), S.level_end, 4 * (size_t)level, cudaMemcpyDeviceToHost, st);
-        cudaMemcpyAsync(host_counters, S.counters, 16, cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(host_counters, S.counters, sizeof(host_counters), cudaMemcpyDeviceToHost, st);
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) { if (err) *err = "BVH build level failed"; return e; }
-        for (uint32_t k = 1; k < level; ++k) level_begin.push_back(ends[k]);   // ends[0]: the last level above
+        n_large = host_counters[0];
+        n_small = host_counters[4];
+        n_tiny = host_counters[6];
     }
-    const uint32_t n_bfs = host_counters[1];
+    // positions the whole-array passes finished (leaves) are in perm[cur] only
+    cudaMemcpyAsync(S.perm[cur ^ 1], S.perm[cur], 4 * (size_t)nt, cudaMemcpyDeviceToDevice, st);
+    // upper bounds of a level's small and tiny tasks: a small task has at most
+    // two small or tiny children, a tiny one at most two tiny children
+    uint64_t small_bound = n_small, tiny_bound = n_tiny;
+    while (n_small > 0 || n_tiny > 0) {
+        for (int k = 0; k < 8; ++k) {
+            if (!advance()) return cudaErrorUnknown;
+            small_round(small_bound, tiny_bound);
+            cur ^= 1;
+            tiny_bound = std::min<uint64_t>(2 * (small_bound + tiny_bound), tcap);
+            small_bound = std::min<uint64_t>(2 * small_bound, tcap);
+        }
+        cudaMemcpyAsync(host_counters, S.counters, sizeof(host_counters), cudaMemcpyDeviceToHost, st);
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) { if (err) *err = "BVH build level failed"; return e; }
+        n_small = host_counters[4];
+        n_tiny = host_counters[6];
+        small_bound = n_small;
+        tiny_bound = n_tiny;
+    }
+    if (!advance()) return cudaErrorUnknown;             // the node count after the last level
+    std::vector<uint32_t> level_begin(level + 1);
+    level_begin[0] = 0;                                  // level 0 is the root alone: [0, 1)
+    cudaMemcpyAsync(level_begin.data() + 1, S.level_end, 4 * (size_t)level, cudaMemcpyDeviceToHost, st);
+    {
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) { if (err) *err = "BVH build level failed"; return e; }
+    }
+    const uint32_t n_bfs = level_begin[level];
     // BFS ids are allocated level by level: the children of the nodes created by
     // one level are all created by the next, so subtree sizes are exact when the
     // levels are swept bottom-up and pre-order indices when swept top-down.
     {
-        level_begin[0] = 0;
-        level_begin.insert(level_begin.begin() + 1, 1u);   // level 0 is the root alone
         const size_t nl = level_begin.size() - 1;
         for (size_t k = nl; k-- > 0;) {
             const uint32_t b = level_begin[k], e = level_begin[k + 1];
@@ -767,7 +1380,7 @@ static cudaError_t gpu_build(const mcrt_gpu_vertex *d_verts, const mcrt_gpu_tria
         }
     }
     k_emit<<<(n_bfs + TB - 1) / TB, TB, 0, st>>>(S, n_bfs, d_nodes); ::mcrt::note_launch();
-    cudaMemcpyAsync(d_order, S.perm[cur], 4 * (size_t)nt, cudaMemcpyDeviceToDevice, st);
+    k_final_order<<<nb, TB, 0, st>>>(S.perm[cur], S.rval[0], nt, d_order); ::mcrt::note_launch();
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { if (err) *err = "BVH emit failed"; return e; }
     *n_nodes_out = n_bfs;
