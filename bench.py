@@ -54,6 +54,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--small", action="store_true",
                    help="same scene at 480x270, 4 spp: the profiling case (not a bench line)")
+    p.add_argument("--leg", choices=["bvh_build", "cache_mlp"],
+                   help="profiling case: only the GPU BVH builds of the workload's mesh, or only the "
+                        "radiance-cache MLP (2^18 queries); prints its timings, not a bench line")
     a = p.parse_args()
     if a.small:
         global W, H, SPP, WORKLOAD
@@ -400,7 +403,21 @@ def run_mcrt(args):
     sc = make_scene()
     cam = camera(sc)
     ctx = M.Context(local, stream=stream.cuda_stream)
+    if args.leg == "cache_mlp":
+        ctx.cache_init(0)
+        print(json.dumps(mlp_rate(M, ctx, n=1 << 18, reps=args.steps)))
+        return
     ctx.upload_scene(vertices=sc["vertices"], triangles=sc["triangles"], materials=sc["materials"], env=sc["env"])
+    if args.leg == "bvh_build":
+        builds = []
+        for _ in range(args.warmup + args.steps):
+            ctx.rebuild_bvh()
+            t = ctx.timings()
+            builds.append((t["bvh_build_ms"], t["build_launches"]))
+        ms = [b[0] for b in builds[args.warmup:]]
+        print(json.dumps({"leg": "bvh_build", "triangles": int(len(sc["triangles"])), "ms": ms,
+                          "launches_per_build": builds[-1][1]}))
+        return
     variant, tune_ms = ctx.autotune(cam, W, H, 2, max_depth=DEPTH)      # set-up, outside the timed region
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # > 129 MB L2
 

@@ -296,6 +296,30 @@ __global__ void __launch_bounds__(128 * kInferGroups) k_cache_infer(NetDev net, 
     }
 }
 
+// Column sums over a warp's 32 rows: x[k] = the calling lane's value in column
+// k.  A reduce-scatter butterfly (31 shuffles, each round's exchanges
+// independent): after the round of distance h a lane keeps the half of its
+// columns on its side of bit h, plus its partner's values of them; in the end
+// lane c holds the sum of column c.  The order of additions is fixed.
+__device__ __forceinline__ float warp_column_sums32(float x[32], uint32_t lane) {
+#pragma unroll
+    for (int h = 16; h >= 1; h >>= 1) {
+        const bool upper = (lane & (uint32_t)h) != 0u;
+#pragma unroll
+        for (int k = 0; k < h; ++k) {
+            const float send = upper ? x[k] : x[k + h];
+            const float keep = upper ? x[k + h] : x[k];
+            x[k] = keep + __shfl_xor_sync(0xffffffffu, send, h);
+        }
+    }
+    return x[0];
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
 struct TrainIO {
     const float *samples;     // 16 floats per sample: query (12), target (3), weight (0 or 1)
     uint32_t n;
@@ -311,8 +335,10 @@ struct TrainIO {
 //                          G's rows padded to 128 with zeros; the sums stay in
 //                          TMEM across the CTA's tiles)
 //   G    <- (G * W_l) .* [H_l > 0]    (tensor cores; W_l read MN-major)
-// Bias gradients are column sums of G (shared-memory atomics).  At the end the
-// CTA writes its partial gradients; k_cache_reduce sums them in a fixed order.
+// Bias gradients are column sums of G: per warp by warp_column_sums32, kept in
+// registers across tiles (lane c: columns c and c + 32 of every layer), and
+// combined over the warps in a fixed order at the end.  The CTA then writes
+// its partial gradients; k_cache_reduce sums them in a fixed order.
 __global__ void __launch_bounds__(128, 1) k_cache_train(NetDev net, TrainIO io, uint32_t *status) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t *x0 = smem + kTrainX0;
@@ -333,6 +359,11 @@ __global__ void __launch_bounds__(128, 1) k_cache_train(NetDev net, TrainIO io, 
     operand_sync();
     const uint32_t taddr = *tslot;
     const uint32_t lane_base = (warp * 32u) << 16;
+    const uint32_t lane = t & 31u;
+    float db[kLayers - 1][2];                    // bias-gradient column sums of this warp's rows
+    for (int l = 0; l < kLayers - 1; ++l) db[l][0] = db[l][1] = 0.0f;
+    float db_out = 0.0f;                         // output layer: column = lane (lanes < 3)
+    float loss_sum = 0.0f;                       // lane 0
     uint32_t phase = 0;
     bool ok = true, first = true;
     for (uint32_t tile = blockIdx.x; ok && tile * kTile < io.n; tile += gridDim.x) {
@@ -375,8 +406,12 @@ __global__ void __launch_bounds__(128, 1) k_cache_train(NetDev net, TrainIO io, 
                     lsum += wgt * ((e * e) / den);
                     g[c] = bf16_float(bf16_bits(wgt * (2.0f * e / den) * io.loss_scale));
                 }
-                atomicAdd(loss_acc, lsum);
-                for (int c = 0; c < 3; ++c) atomicAdd(&dbias[bias_idx(l) + c], g[c]);
+                lsum = warp_sum(lsum);
+                if (lane == 0) loss_sum += lsum;
+                for (int c = 0; c < 3; ++c) {
+                    const float s = warp_sum(g[c]);
+                    if (lane == (uint32_t)c) db_out += s;
+                }
                 *reinterpret_cast<uint4 *>(G + tc::op_offset(row, 0, kTile)) =
                     make_uint4(pack2(g[0], g[1]), pack2(g[2], 0.0f), 0u, 0u);
                 for (uint32_t c = 8; c < (uint32_t)kHid; c += 8)
@@ -416,23 +451,30 @@ __global__ void __launch_bounds__(128, 1) k_cache_train(NetDev net, TrainIO io, 
             if (!ok) break;
             if (l > 0) {
                 const uint8_t *hl = H(l);
-                for (uint32_t c = 0; c < (uint32_t)kHid; c += 16) {
-                    float v[16], g[16];
-                    tc::tmem_ld16(taddr + lane_base + c, v);
-                    const uint4 ha = *reinterpret_cast<const uint4 *>(hl + tc::op_offset(row, c, kTile));
-                    const uint4 hb = *reinterpret_cast<const uint4 *>(hl + tc::op_offset(row, c + 8, kTile));
-                    const uint32_t hw[8] = {ha.x, ha.y, ha.z, ha.w, hb.x, hb.y, hb.z, hb.w};
-                    for (int j = 0; j < 16; ++j) {
-                        const uint32_t hbits = (hw[j >> 1] >> (16 * (j & 1))) & 0xffffu;
-                        g[j] = bf16_float(bf16_bits(hbits != 0u ? v[j] : 0.0f));   // ReLU output > 0 <=> bits != 0
-                        float s = g[j];                                  // column sum over the warp's rows
-                        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-                        if ((t & 31u) == 0) atomicAdd(&dbias[bias_idx(l - 1) + c + j], s);
+#pragma unroll
+                for (uint32_t half = 0; half < 2; ++half) {
+                    float g[32];
+#pragma unroll
+                    for (uint32_t q = 0; q < 2; ++q) {
+                        const uint32_t c = half * 32u + q * 16u;
+                        float v[16];
+                        tc::tmem_ld16(taddr + lane_base + c, v);
+                        const uint4 ha = *reinterpret_cast<const uint4 *>(hl + tc::op_offset(row, c, kTile));
+                        const uint4 hb = *reinterpret_cast<const uint4 *>(hl + tc::op_offset(row, c + 8, kTile));
+                        const uint32_t hw[8] = {ha.x, ha.y, ha.z, ha.w, hb.x, hb.y, hb.z, hb.w};
+                        float *gq = g + q * 16u;
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            const uint32_t hbits = (hw[j >> 1] >> (16 * (j & 1))) & 0xffffu;
+                            gq[j] = bf16_float(bf16_bits(hbits != 0u ? v[j] : 0.0f));   // ReLU output > 0 <=> bits != 0
+                        }
+                        *reinterpret_cast<uint4 *>(G + tc::op_offset(row, c, kTile)) =
+                            make_uint4(pack2(gq[0], gq[1]), pack2(gq[2], gq[3]), pack2(gq[4], gq[5]), pack2(gq[6], gq[7]));
+                        *reinterpret_cast<uint4 *>(G + tc::op_offset(row, c + 8, kTile)) =
+                            make_uint4(pack2(gq[8], gq[9]), pack2(gq[10], gq[11]), pack2(gq[12], gq[13]),
+                                       pack2(gq[14], gq[15]));
                     }
-                    *reinterpret_cast<uint4 *>(G + tc::op_offset(row, c, kTile)) =
-                        make_uint4(pack2(g[0], g[1]), pack2(g[2], g[3]), pack2(g[4], g[5]), pack2(g[6], g[7]));
-                    *reinterpret_cast<uint4 *>(G + tc::op_offset(row, c + 8, kTile)) =
-                        make_uint4(pack2(g[8], g[9]), pack2(g[10], g[11]), pack2(g[12], g[13]), pack2(g[14], g[15]));
+                    db[l - 1][half] += warp_column_sums32(g, lane);      // column half * 32 + lane
                 }
                 operand_sync();
             }
@@ -440,6 +482,18 @@ __global__ void __launch_bounds__(128, 1) k_cache_train(NetDev net, TrainIO io, 
         first = false;
     }
     if (!ok && t == 0) atomicExch(status, 1u);
+    // the warps' bias-gradient sums and losses, added warp by warp (fixed order)
+    for (uint32_t w = 0; w < 4u; ++w) {
+        if (warp == w) {
+            for (int l = 0; l < kLayers - 1; ++l) {
+                dbias[bias_idx(l) + lane] += db[l][0];
+                dbias[bias_idx(l) + 32u + lane] += db[l][1];
+            }
+            if (lane < 3u) dbias[bias_idx(kLayers - 1) + lane] += db_out;
+            if (lane == 0) *loss_acc += loss_sum;
+        }
+        __syncthreads();
+    }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
