@@ -146,7 +146,7 @@ def test_headless_cli_matches_oracle(tmp_path, oracle):
     assert p.returncode == 1 and "headless render failed" in p.stderr
 
 
-@pytest.mark.parametrize("variant", [1, 5])   # compact binary BVH, quantised 4-wide BVH
+@pytest.mark.parametrize("variant", [1, 6])   # compact binary BVH, quantised 4-wide BVH (kernel variants 0, 5)
 def test_bvh_layouts_bit_exact_against_oracle(ctx, oracle, variant):
     import ctypes
     from mcrt_gb300 import scenes
