@@ -113,8 +113,10 @@ constexpr uint32_t kSmemAct = kSmemBias + kBiasFloats * 4;                 // 48
 constexpr uint32_t kTileIn = kTile * kIn * 2;                              // 24576
 constexpr uint32_t kTileHid = kTile * kHid * 2;                            // 16384
 // inference: image | bias | one activation tile | mbarrier | TMEM slot
-constexpr uint32_t kInferGroups = 2;
+constexpr uint32_t kInferGroups = 5;                     // one CTA per SM (shared memory), 640 threads
 constexpr uint32_t kInferSmem = kSmemAct + kInferGroups * kTileIn + 64;
+constexpr uint32_t kInferTmemCols = 64 * kInferGroups <= 128 ? 128 : (64 * kInferGroups <= 256 ? 256 : 512);   // a power of 2
+static_assert(64 * kInferGroups <= 512, "TMEM columns of the inference pipelines");
 // training: image | bias | X0 | H1..H5 | G (128 x 128, upper half zero) | bias grads | misc
 constexpr uint32_t kTrainX0 = kSmemAct;
 constexpr uint32_t kTrainH = kTrainX0 + kTileIn;
@@ -223,7 +225,7 @@ __global__ void __launch_bounds__(128 * kInferGroups) k_cache_infer(NetDev net, 
     const uint32_t bar_id = 1 + g;
     const uint32_t n = io.count ? min(*io.count, io.n) : io.n;
     load_net(net, smem);
-    if (warp == 0) tc::tmem_alloc(tslot, 64 * kInferGroups);
+    if (warp == 0) tc::tmem_alloc(tslot, kInferTmemCols);
     if (t == 0)
         for (uint32_t k = 0; k < kInferGroups; ++k) tc::mbar_init(reinterpret_cast<uint64_t *>(misc) + k, 1);
     operand_sync();
@@ -291,7 +293,7 @@ __global__ void __launch_bounds__(128 * kInferGroups) k_cache_infer(NetDev net, 
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) {
-        tc::tmem_dealloc(*tslot, 64 * kInferGroups);
+        tc::tmem_dealloc(*tslot, kInferTmemCols);
         tc::tmem_relinquish();
     }
 }
@@ -734,7 +736,9 @@ cudaError_t cache_infer_device(CacheState *c, const float4 *q, const uint32_t *d
     if (max_n == 0) return cudaSuccess;
     InferIO io{q, d_count, max_n, L, thr, out};
     const uint32_t tiles = (max_n + kTile - 1) / kTile;
-    const int blocks = (int)std::max<uint32_t>(1u, std::min<uint32_t>((tiles + kInferGroups - 1) / kInferGroups, (uint32_t)sm_count() * 2u));
+    const uint32_t per_sm = std::max<uint32_t>(1u, (227u * 1024u) / kInferSmem);   // resident CTAs (shared memory)
+    const int blocks = (int)std::max<uint32_t>(1u, std::min<uint32_t>((tiles + kInferGroups - 1) / kInferGroups,
+                                                                      (uint32_t)sm_count() * per_sm));
     k_cache_infer<<<blocks, 128 * kInferGroups, kInferSmem, st>>>(net_of(c), io, c->status.as<uint32_t>());
     note_launch();
     return cudaGetLastError();
