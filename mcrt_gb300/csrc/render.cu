@@ -717,8 +717,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
 // kernel: it is stored (B.pend, material in aux.w bits 8..15) and applied at
 // the path's next vertex.  Gradients collect in shared memory per block, then
 // one double atomic per parameter and block.
+// Four resident blocks per SM (a 64-register budget) for the forward kernel:
+// it is bound by the latency of its scattered loads, and at the natural 88
+// registers only two blocks fit.  The replay variant keeps its registers.
 template <bool ADJ>
-__global__ void __launch_bounds__(256) k_shade(DeviceScene S, RenderParams P, PathBuffers B, int qi,
+__global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, RenderParams P, PathBuffers B, int qi,
                                                 uint32_t bounce, float4 *gbuf, AdjointParams A) {
     __shared__ float gacc[ADJ ? 256 : 1];
     if (ADJ) {
