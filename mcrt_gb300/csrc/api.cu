@@ -683,8 +683,12 @@ static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, ui
     const bool keep = (o.flags & MCRT_RENDER_KEEP_ACCUM) != 0;
     if (keep && (!ctx->acc_valid || ctx->acc_w != w || ctx->acc_h != h))
         return fail(ctx, MCRT_ERR_INVALID_ARG, "KEEP_ACCUM needs a previous render of the same size");
-    // samples traced at once: enough paths in flight to fill the GPU, bounded memory
-    const uint64_t kTargetSlots = 1ull << 22, kMaxSlots = 1ull << 24;
+    // samples traced at once: enough paths in flight that each closest-hit
+    // launch's tail (the last, longest traversals, while most SMs idle) is a
+    // small part of it — a 1080p frame of 16 spp traces 1.45x faster as one
+    // pass of 16 sample planes than as 8 passes of 2, with the same result —
+    // with bounded memory (208 B of path state per slot: 7 GB at 2^25 slots)
+    const uint64_t kTargetSlots = 1ull << 25, kMaxSlots = 1ull << 25;
     uint32_t spp_pass = o.spp_per_pass;
     if (spp_pass == 0) spp_pass = (uint32_t)std::max<uint64_t>(1, (kTargetSlots + npix - 1) / npix);
     spp_pass = std::min(spp_pass, spp);
