@@ -3,7 +3,9 @@
 // shadow rays and per-pixel resolve; plus the closest-hit parity probe.
 //
 // One render pass traces `spp_pass` sample planes of the image at once (slot =
-// plane * npix + pixel).  Each bounce is extend -> shade (-> shadow); shade
+// pixel * spp_pass + plane: a pixel's samples sit in neighbouring lanes, so a
+// warp's rays start together and stay close for the first bounces).  Each
+// bounce is extend -> shade (-> shadow); shade
 // appends surviving paths to the next ray queue with warp-aggregated atomics
 // (one atomicAdd per warp), so later bounces run on compacted queues.  All
 // per-path state is indexed by slot and every path owns its radiance, so the
@@ -461,8 +463,8 @@ __global__ void k_raygen(DeviceScene S, RenderParams P, PathBuffers B, int keep_
         float4 *rec = P.train_records + (size_t)(i / P.train_stride) * P.max_depth * kTrainRecordFloat4;
         for (uint32_t j = 0; j < P.max_depth; ++j) rec[(size_t)j * kTrainRecordFloat4].w = 0.0f;
     }
-    uint32_t k = i / P.npix;
-    uint32_t p = i - k * P.npix;
+    uint32_t p = i / P.spp_pass;
+    uint32_t k = i - p * P.spp_pass;
     uint32_t frame = (P.pass_state ? P.pass_state[0] : P.frame0) + k;
     uint32_t x, y, w, h;
     const mcrt_camera_uniform *cam = &P.cam;
@@ -770,7 +772,7 @@ __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, Rende
                     gadd(k0 + 3, ((dl.x + dl.y) + dl.z) * pd.w);
                 }
             }
-            const bool write_g = gbuf && bounce == 0 && (int)(slot / P.npix) == P.gbuf_plane;
+            const bool write_g = gbuf && bounce == 0 && (int)(slot % P.spp_pass) == P.gbuf_plane;
             if (h.x < 0.0f) {                                                   // miss, :592-597
                 if (write_g) gbuf[aux.y] = make_float4(0.0f, 0.0f, 0.0f, kTMax);
                 if (!ADJ) {
@@ -1070,7 +1072,7 @@ __global__ void k_resolve(RenderParams P, PathBuffers B, float4 *mean, double *s
     double s0 = keep ? sum[3 * (size_t)p] : 0.0, s1 = keep ? sum[3 * (size_t)p + 1] : 0.0,
            s2 = keep ? sum[3 * (size_t)p + 2] : 0.0;
     for (uint32_t k = 0; k < P.spp_pass; ++k) {
-        float4 s = B.L[(size_t)k * P.npix + p];
+        float4 s = B.L[(size_t)p * P.spp_pass + k];
         uint32_t frame = frame0 + k;
         float w = 1.0f / (float)(min(frame, kMaxFrameCount) + 1u);
         float omw = 1.0f - w;

@@ -1209,7 +1209,8 @@ void orc_render_cache_const(const orc_scene *sc, const orc_camera *cam, uint32_t
             uint32_t frame = first_frame + k;
             uint32_t rng = pcg_hash(pcg_hash(x + y * w) ^ (frame * 2654435761u));
             Ray r = camera_ray(cam, x, y, w, h, rng);
-            const uint64_t slot = (uint64_t)(k % spp_pass) * (uint64_t)npx + (uint64_t)i;
+            const uint32_t pass_start = k - k % spp_pass, planes = std::min(spp_pass, spp - pass_start);
+            const uint64_t slot = (uint64_t)i * planes + (k - pass_start);
             const bool training = slot % train_stride == 0;
             V3 s = path_color(sc, r, rng, max_depth, nullptr, nullptr, lp, nullptr, training ? nullptr : &stop);
             float wgt = 1.0f / (float)(std::min(frame, MAX_FRAME_COUNT) + 1u);

@@ -100,8 +100,9 @@ void orc_render_ex(const orc_scene *scene, const orc_camera *cam, uint32_t w, ui
                    int threads, uint64_t *out_stats);
 
 /* orc_render_ex with paths stopped into a radiance cache whose prediction is the
- * constant c3: the sample of frame k, pixel p occupies slot (k mod spp_pass) *
- * w*h + p of its pass; slots with slot % train_stride == 0 are traced in full,
+ * constant c3: frames are traced in passes of spp_pass (the last one shorter);
+ * the sample of frame k, pixel p occupies slot p * planes + (k - pass start) of
+ * its pass of `planes` frames; slots with slot % train_stride == 0 are traced in full,
  * the others add throughput * max(c, 0) at their vertex number query_vertex
  * (0 = primary hit) when it is not emissive, and end. */
 void orc_render_cache_const(const orc_scene *scene, const orc_camera *cam, uint32_t w, uint32_t h, uint32_t spp,
