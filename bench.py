@@ -43,6 +43,9 @@ sys.path.insert(0, ROOT)
 
 W, H, SPP, DEPTH, LEVEL, SEED = 1920, 1080, 16, 12, 8, 1234
 WORKLOAD = "displaced_icosphere_l8_1.31Mtri_1920x1080_16spp_depth12_gpu_rebuild"
+# DRAM bytes (read + write) per traced ray of the closest-hit kernel on this
+# workload, from one ncu capture of a frame's 12 launches (10.26 GB / 71.5 M rays)
+EXTEND_DRAM_BYTES_PER_RAY = 143.4
 
 
 def parse():
@@ -54,9 +57,11 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--small", action="store_true",
                    help="same scene at 480x270, 4 spp: the profiling case (not a bench line)")
-    p.add_argument("--leg", choices=["bvh_build", "cache_mlp"],
-                   help="profiling case: only the GPU BVH builds of the workload's mesh, or only the "
-                        "radiance-cache MLP (2^18 queries); prints its timings, not a bench line")
+    p.add_argument("--leg", choices=["bvh_build", "cache_mlp", "frame"],
+                   help="profiling case: only the GPU BVH builds of the workload's mesh, only the "
+                        "radiance-cache MLP (2^18 queries), or only frames of the workload (rebuild + render "
+                        "with the default closest-hit variant, 12 extend launches per frame); prints its "
+                        "timings, not a bench line")
     a = p.parse_args()
     if a.small:
         global W, H, SPP, WORKLOAD
@@ -418,6 +423,16 @@ def run_mcrt(args):
         print(json.dumps({"leg": "bvh_build", "triangles": int(len(sc["triangles"])), "ms": ms,
                           "launches_per_build": builds[-1][1]}))
         return
+    if args.leg == "frame":
+        frames = []
+        for i in range(args.warmup + args.steps):
+            ctx.rebuild_bvh()
+            ctx.render(cam, W, H, SPP, first_frame=i * SPP, max_depth=DEPTH, outputs=())
+            t = ctx.timings()
+            frames.append({k: round(t[k], 3) for k in ("extend_ms", "shade_ms", "total_ms")} |
+                          {"rays": t["rays"], "extend_launches": t["extend_launches"]})
+        print(json.dumps({"leg": "frame", "workload": WORKLOAD, "frames": frames[args.warmup:]}))
+        return
     variant, tune_ms = ctx.autotune(cam, W, H, 2, max_depth=DEPTH)      # set-up, outside the timed region
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # > 129 MB L2
 
@@ -484,8 +499,15 @@ def run_mcrt(args):
         n_node, n_tri = st["nodes"] / st["rays"], st["prims"] / st["rays"]
         b_ray = 48 * n_node + 64 * n_tri + 32 + 16
         achieved = rays * b_ray / (ext_ms / 1000.0) / 1e9
+        rays_per_launch = rays / max(ext_launches, 1)
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": peak_kind,
+                "frac": round(achieved / peak, 4),
+                # measured DRAM bytes per launch: ncu dram__bytes_read.sum + dram__bytes_write.sum over one
+                # frame of this workload (profiles/k_extend_displaced_icosphere_1080p16.md), per ray, times
+                # this run's rays per launch
+                "traffic": round(EXTEND_DRAM_BYTES_PER_RAY * rays_per_launch),
+                "traffic_unit": "B per launch", "traffic_per_ray": EXTEND_DRAM_BYTES_PER_RAY,
+                "peak_kind": peak_kind,
                 "kernel": "k_extend", "bytes_per_ray": round(b_ray, 1), "n_node": round(n_node, 2),
                 "n_tri": round(n_tri, 2), "mrays_per_s": round(rays / (ext_ms / 1000.0) / 1e6, 1),
                 "avg_launch_ms": round(ext_ms / max(ext_launches, 1), 4)}
