@@ -56,7 +56,7 @@ struct mcrt_ctx {
     DBuf wnodes;
     uint32_t n_wnodes = 0;
     DBuf spheres, sphere_ids, sphere_nodes, vertices, triangles, mesh_nodes, tri_order, trirecs, cnodes, materials,
-        env, lights, light_cdf, tmp, staging, albedo;
+        env, lights, light_cdf, tmp, staging, albedo, shade_recs;
     uint32_t albedo_layers = 0, albedo_size = 0;
     size_t srgb_lut_offset = 0;
     uint32_t n_spheres = 0, n_sphere_nodes = 0, n_vertices = 0, n_triangles = 0, n_mesh_nodes = 0, n_cnodes = 0,
@@ -137,6 +137,7 @@ mcrt::DeviceScene device_scene(const mcrt_ctx *c) {
     S.n_mesh_nodes = c->n_mesh_nodes;
     S.tri_ids = c->tri_order.as<uint32_t>();
     S.tris = c->trirecs.as<mcrt::TriRec>();
+    S.shade_recs = c->shade_recs.as<float4>();
     S.cnodes = c->cnodes.as<float4>();
     S.n_cnodes = c->n_cnodes;
     S.wnodes = c->wnodes.as<uint4>();
@@ -228,6 +229,9 @@ mcrt_status finish_mesh(mcrt_ctx *ctx) {
     cudaStream_t st = ctx->stream;
     uint32_t nt = ctx->n_triangles, nn = ctx->n_mesh_nodes;
     CK(ctx->trirecs.ensure((size_t)std::max(nt, 1u) * sizeof(mcrt::TriRec)), "allocate triangle records");
+    CK(ctx->shade_recs.ensure((size_t)std::max(nt, 1u) * 48), "allocate shading records");
+    mcrt::launch_shade_recs(ctx->vertices.as<mcrt_gpu_vertex>(), ctx->triangles.as<mcrt_gpu_triangle>(), nt,
+                            ctx->shade_recs.as<float4>(), st);
     CK(ctx->cnodes.ensure((size_t)(nn / 2 + 1) * 64), "allocate compact nodes");
     size_t tmp_words = 2 * (size_t)std::max(nn, 1u) + mcrt::scan_tmp_words(std::max(nn, 1u));
     CK(ctx->tmp.ensure(tmp_words * 4), "allocate scan scratch");
@@ -358,7 +362,8 @@ void mcrt_destroy(mcrt_ctx *ctx) {
                     &ctx->lights, &ctx->light_cdf, &ctx->tmp, &ctx->staging, &ctx->albedo, &ctx->wnodes, &ctx->pbmem, &ctx->mean,
                     &ctx->sum, &ctx->gbuf, &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->counters, &ctx->dimg,
                     &ctx->grad, &ctx->world_vox, &ctx->world_matmap, &ctx->wmesh.counts, &ctx->wmesh.vertices,
-                    &ctx->wmesh.triangles, &ctx->views, &ctx->pass_state, &ctx->cache_q, &ctx->cache_rec};
+                    &ctx->wmesh.triangles, &ctx->views, &ctx->pass_state, &ctx->cache_q, &ctx->cache_rec,
+                    &ctx->shade_recs};
     for (DBuf *b : bufs) b->release();
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     mcrt::cache_destroy(ctx->cache);

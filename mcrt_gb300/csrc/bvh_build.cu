@@ -1421,6 +1421,19 @@ __global__ void k_compact(const mcrt_gpu_bvh_node *nodes, uint32_t n, const uint
     o[3] = make_float4(__uint_as_float(child_code(nodes, rank, l)), __uint_as_float(child_code(nodes, rank, r)),
                        0.0f, 0.0f);
 }
+// Shading records in original triangle order: the three vertex normals, the
+// first carrying the material word.
+__global__ void k_shade_recs(const mcrt_gpu_vertex *verts, const mcrt_gpu_triangle *tris, uint32_t nt, float4 *out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt) return;
+    const mcrt_gpu_triangle t = tris[i];
+    float4 *r = out + 3ull * i;
+    for (int k = 0; k < 3; ++k) {
+        const float *n = verts[t.v[k]].normal;
+        r[k] = make_float4(n[0], n[1], n[2], k == 0 ? __uint_as_float(t.mat_idx) : 0.0f);
+    }
+}
+
 __global__ void k_trirecs(const uint32_t *order, const mcrt_gpu_vertex *verts, const mcrt_gpu_triangle *tris,
                           uint32_t nt, TriRec *out) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1441,6 +1454,12 @@ __global__ void k_leaf_counts(const mcrt_gpu_bvh_node *nodes, uint32_t n, TriRec
     recs[nodes[i].right_or_offset].e2.w = __uint_as_float(nodes[i].prim_count);
 }
 }  // namespace
+
+void launch_shade_recs(const mcrt_gpu_vertex *d_verts, const mcrt_gpu_triangle *d_tris, uint32_t nt, float4 *out,
+                       cudaStream_t st) {
+    if (nt == 0) return;
+    k_shade_recs<<<(nt + 255) / 256, 256, 0, st>>>(d_verts, d_tris, nt, out); ::mcrt::note_launch();
+}
 
 cudaError_t gpu_make_compact(const mcrt_gpu_bvh_node *d_nodes, uint32_t n_nodes, const uint32_t *d_order,
                              const mcrt_gpu_vertex *d_verts, const mcrt_gpu_triangle *d_tris, uint32_t nt,

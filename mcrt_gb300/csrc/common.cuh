@@ -85,6 +85,10 @@ struct DeviceScene {
     // triangles in original order (shading) and vertices
     const mcrt_gpu_vertex *vertices; uint32_t n_vertices;
     const mcrt_gpu_triangle *triangles; uint32_t n_triangles;
+    // shading records, 3 float4 per triangle in original order: the three
+    // vertex normals, the first with the triangle's material word in w (48 B:
+    // two 32-byte sectors per record instead of one per vertex and triangle)
+    const float4 *shade_recs;
     // reference-layout mesh BVH, ordered slots -> original ids, fast leaf-ordered records
     const mcrt_gpu_bvh_node *mesh_nodes; uint32_t n_mesh_nodes;
     const uint32_t *tri_ids;

@@ -132,6 +132,11 @@ cudaError_t gpu_make_compact(const mcrt_gpu_bvh_node *d_nodes, uint32_t n_nodes,
                              float4 **d_cnodes, uint32_t *n_cnodes, void *d_trirecs, uint32_t *d_tmp,
                              size_t tmp_words, cudaStream_t st);
 
+// Shading records (3 float4 per triangle, DeviceScene::shade_recs) from the
+// vertices and triangles in original order.
+void launch_shade_recs(const mcrt_gpu_vertex *d_verts, const mcrt_gpu_triangle *d_tris, uint32_t nt, float4 *out,
+                       cudaStream_t st);
+
 // Collapse into the quantised 4-wide layout (d_tmp: 2*n_nodes + 4 words).
 cudaError_t gpu_make_wide4(const mcrt_gpu_bvh_node *d_nodes, uint32_t n_nodes, uint4 *d_wide, uint32_t *n_wide,
                            uint32_t *d_tmp, cudaStream_t st);

@@ -99,7 +99,7 @@ __device__ __forceinline__ SurfaceHit surface(const DeviceScene &S, f3 o, f3 d, 
         f3 n = tri_shading_normal(S, prim, h.z, h.w);
         s.front = dot(d, n) < 0.0f;
         s.n = s.front ? n : -n;
-        s.mat = S.triangles[prim].mat_idx & 0x7fffffffu;
+        s.mat = tri_material_word(S, prim) & 0x7fffffffu;
     }
     return s;
 }

@@ -95,14 +95,18 @@ __device__ __forceinline__ bool tie_better_tri(float t, uint32_t id, const Close
     return t == b.t && b.prim != MCRT_HIT_MISS && !(b.prim & MCRT_HIT_SPHERE) && id < b.prim;
 }
 
-// Interpolated shading normal (path_trace.wgsl:448-450).
+// Interpolated shading normal (path_trace.wgsl:448-450), from the triangle's
+// shading record (the vertex normals, copied bit for bit).
 __device__ __forceinline__ f3 tri_shading_normal(const DeviceScene &S, uint32_t tri_id, float u, float v) {
-    mcrt_gpu_triangle tri = S.triangles[tri_id];
-    f3 na = ld3(S.vertices[tri.v[0]].normal);
-    f3 nb = ld3(S.vertices[tri.v[1]].normal);
-    f3 nc = ld3(S.vertices[tri.v[2]].normal);
+    const float4 *r = S.shade_recs + 3ull * tri_id;
+    f3 na = xyz(__ldg(r)), nb = xyz(__ldg(r + 1)), nc = xyz(__ldg(r + 2));
     float w = 1.0f - u - v;
     return normalize((w * na + u * nb) + v * nc);
+}
+
+// The triangle's material word (bit 31: backface flag), from its shading record.
+__device__ __forceinline__ uint32_t tri_material_word(const DeviceScene &S, uint32_t tri_id) {
+    return __float_as_uint(__ldg(S.shade_recs + 3ull * tri_id).w);
 }
 
 // Test the triangles of one leaf (fast records) and update best.
