@@ -433,7 +433,8 @@ def run_mcrt(args):
                           {"rays": t["rays"], "extend_launches": t["extend_launches"]})
         print(json.dumps({"leg": "frame", "workload": WORKLOAD, "frames": frames[args.warmup:]}))
         return
-    variant, tune_ms = ctx.autotune(cam, W, H, 2, max_depth=DEPTH)      # set-up, outside the timed region
+    # set-up, outside the timed region: one frame of the workload per variant
+    variant, tune_ms = ctx.autotune(cam, W, H, SPP, max_depth=DEPTH)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # > 129 MB L2
 
     def step_device(i):
@@ -527,7 +528,7 @@ def run_mcrt(args):
                    "triangles": int(len(sc["triangles"])), "seed": SEED, "estimator": "reference (no NEE)",
                    "parallelism": f"replicas{world}", "l2": "256 MB buffer written between timed steps",
                    "extend_variant": variant, "extend_variant_info": M.variant_info(variant),
-                   "autotune_extend_ms_2spp": [round(x, 3) for x in tune_ms]},
+                   "autotune_extend_ms_per_frame": [round(x, 3) for x in tune_ms]},
         "e2e": {"value": round(e2e_value, 3), "unit": "Msamples/s",
                 "h2d_bytes_per_step": int(sc["vertices"].nbytes), "d2h_bytes_per_step": W * H * 16},
         "gpu_launches": int(launches),
