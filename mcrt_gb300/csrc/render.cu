@@ -517,8 +517,8 @@ __global__ void k_raygen(DeviceScene S, RenderParams P, PathBuffers B, int keep_
 struct ExtendVariant { int width, block, min_blocks, stack, refill; };
 constexpr int kExtendVariants = 8;
 constexpr ExtendVariant kVariantTable[kExtendVariants] = {
-    {2, 128, 8, 64, 8}, {2, 64, 20, 32, 8}, {2, 64, 16, 32, 4}, {2, 64, 20, 32, 16},
-    {2, 64, 16, 32, 8}, {4, 128, 8, 64, 8}, {2, 128, 10, 32, 16}, {2, 64, 16, 32, 16}};
+    {2, 128, 8, 64, 8}, {2, 64, 20, 32, 8}, {2, 64, 20, 32, 4}, {2, 64, 20, 32, 16},
+    {2, 64, 22, 32, 8}, {4, 128, 8, 64, 8}, {2, 128, 10, 32, 8}, {2, 64, 18, 32, 8}};
 
 // Visit an internal node of the compact binary layout: test both children,
 // continue with the nearer hit child, push the farther one.
