@@ -371,6 +371,55 @@ def batched_views_rate(M, ctx, stream, spp=4, n_warm=1, n_steps=3):
             "speedup": round(t_seq / t_batch, 3)}
 
 
+def views_cache_relmse(M, ctx, target=1e-3, ref_spp=1024, max_spp=1024):
+    """The batched workload with the radiance cache: the 16 uneven views of the
+    voxel world (left uploaded by voxel_world_rate), depth 6, sun NEE + sky.
+    Device time for the views' estimates (f64 sums / samples) to reach relMSE
+    <= target (over every pixel of every view) against a ref_spp NEE
+    reference, for the tracer without the cache (passes replayed as a CUDA
+    graph) and with the online-trained cache (warm-up and training inside the
+    time); each estimator stops at max_spp.  The reference is 1024 spp rather
+    than 4096 to keep the leg within about a minute (12 Mpix); its own noise
+    then adds about 1/4 of the target to the relMSE the tracer without the
+    cache reaches, equally for both estimators."""
+    from mcrt_gb300 import scenes
+    w = scenes.voxel_world(SEED)
+    vs = scenes.world_views(w, seed=SEED)
+    views = [(M.compute_camera(v["width"], v["height"], v["look_from"], v["look_at"], v["vfov"], 0.0),
+              v["width"], v["height"]) for v in vs]
+    depth = w["max_depth"]
+    px = sum(v[1] * v[2] for v in views)
+    ctx.render_views(views, ref_spp, first_frame=1 << 20, max_depth=depth, nee=True, read_back=False)
+    ref = ctx.read_accum()[1].reshape(-1, 3) / ref_spp
+    out = {"workload": f"voxel_world_16_views_seed{SEED}_{px / 1e6:.2f}Mpix_depth{depth}_sun_nee",
+           "target_relmse": target, "reference": f"NEE {ref_spp} spp, independent frames"}
+    cache_cfg = dict(query_vertex=3, train_stride=16, train_steps=16, train_batch=1 << 14, lr=1e-3)
+    for name, cache in (("nee", False), ("nee_cache", True)):
+        total, ms, rel = 0, 0.0, None
+        if cache:
+            ctx.cache_config(**cache_cfg)
+            ctx.cache_init(0)
+            for i in range(20):
+                ctx.render_views(views, 2, first_frame=(1 << 21) + 2 * i, max_depth=depth, nee=True, cache=True,
+                                 read_back=False)
+                ms += ctx.timings()["total_ms"]
+        while total < max_spp:
+            chunk = max(8, total // 8)
+            ctx.render_views(views, chunk, first_frame=total, max_depth=depth, nee=True, keep=total > 0,
+                             cache=cache, graph=not cache, read_back=False)
+            ms += ctx.timings()["total_ms"]
+            total += chunk
+            x = ctx.read_accum()[1].reshape(-1, 3) / total
+            rel = float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
+            if rel <= target:
+                break
+        out[name] = {"spp": total, "ms": round(ms, 2), "relmse": round(rel, 6), "reached": rel <= target}
+    out["nee_cache"]["config"] = dict(cache_cfg, warmup="20 passes x 2 spp over all views, in the time")
+    if out["nee"]["reached"] and out["nee_cache"]["reached"]:
+        out["speedup_cache_vs_nee"] = round(out["nee"]["ms"] / out["nee_cache"]["ms"], 3)
+    return out
+
+
 MLP_FLOP_INFER = 2 * (96 * 64 + 4 * 64 * 64 + 64 * 16)                    # per query
 MLP_FLOP_TRAIN = MLP_FLOP_INFER + 2 * (16 * 64 + 4 * 64 * 64) + MLP_FLOP_INFER   # + backward data + weight grads
 
@@ -513,13 +562,14 @@ def run_mcrt(args):
                 "n_tri": round(n_tri, 2), "mrays_per_s": round(rays / (ext_ms / 1000.0) / 1e6, 1),
                 "avg_launch_ms": round(ext_ms / max(ext_launches, 1), 4)}
     clocks = clk.summary()
-    quality = adjoint = voxel = views = mlp = None
+    quality = adjoint = voxel = views = views_cache = mlp = None
     if not args.small:
         mlp = mlp_rate(M, ctx)
         quality = time_to_relmse(M, ctx)
         adjoint = adjoint_rate(M, ctx, stream)
         voxel = voxel_world_rate(M, ctx, stream)
         views = batched_views_rate(M, ctx, stream)
+        views_cache = views_cache_relmse(M, ctx)
     out = {
         "metric": "Msamples/s", "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 3), "higher_is_better": True,
@@ -541,6 +591,7 @@ def run_mcrt(args):
         "adjoint": adjoint,
         "voxel_world": voxel,
         "batched_views": views,
+        "batched_views_cache_time_to_relmse": views_cache,
         "radiance_cache_mlp": mlp,
     }
     print(json.dumps(out))

@@ -327,15 +327,26 @@ class Context:
         self._last_hw = (height, width)
         return dict(rgba=rgba, sum=acc, gbuf=gb)
 
+    def read_accum(self):
+        """The last render's accumulation: the running mean (h, w, 4) and the f64 sums (h, w, 3); after
+        render_views, one row holding every view's pixels in view order."""
+        h, w = self._last_hw
+        mean = np.zeros((h, w, 4), np.float32)
+        acc = np.zeros((h, w, 3), np.float64)
+        self._check(lib().mcrt_read_accum(self._h, ptr(mean), ptr(acc), None))
+        return mean, acc
+
     def render_views(self, views, spp, first_frame=0, max_depth=0, nee=False, spp_per_pass=0, graph=False,
-                     read_back=True):
+                     read_back=True, keep=False, cache=False):
         """Trace several cameras of uneven sizes together.  views: list of (camera, width, height);
-        returns the views' running means (list of (h, w, 4) arrays) when read_back."""
+        returns the views' running means (list of (h, w, 4) arrays) when read_back.  keep continues
+        the previous call's accumulation; cache terminates paths into the radiance cache."""
         vv = np.zeros(len(views), N.VIEW)
         for k, (cam, w, h) in enumerate(views):
             vv[k]["cam"] = _arr(cam, CAMERA)
             vv[k]["width"], vv[k]["height"] = w, h
-        o = N.RenderOpts(max_depth=max_depth, flags=(N.RENDER_NEE if nee else 0) | (N.RENDER_GRAPH if graph else 0),
+        o = N.RenderOpts(max_depth=max_depth, flags=(N.RENDER_NEE if nee else 0) | (N.RENDER_GRAPH if graph else 0) |
+                         (N.RENDER_KEEP_ACCUM if keep else 0) | (N.RENDER_CACHE if cache else 0),
                          spp_per_pass=spp_per_pass)
         outs = [np.zeros((h, w, 4), np.float32) for (_, w, h) in views] if read_back else []
         ptrs = (c_void_p * len(views))(*[o_.ctypes.data for o_ in outs]) if read_back else None
