@@ -17,8 +17,17 @@ roofline : the closest-hit (extend) kernel against the bytes-per-ray memory roof
 time_to_relmse : seeded Cornell box 512x512, depth 8: device time until the running
            estimate reaches relMSE 1e-3 against a 4096-spp NEE reference, reference
            estimator ("plain") and next-event estimation.
+           The same with the radiance cache (online training inside the time).
 adjoint  : path-replay adjoint of the GGX Cornell box, 256x256, 32 spp: paths/s
            through mcrt_adjoint with host buffers.
+voxel_world : the 256x128x256 voxel world generated, meshed (4.94 M triangles),
+           uploaded with a GPU BVH build, rendered 1280x720 8 spp depth 6 with the
+           sun and sky, denoised 5x5: device time per stage.
+batched_views : 16 uneven views of the voxel world traced together (CUDA graph)
+           against one call per view; batched_views_cache_time_to_relmse: the
+           same views' time to relMSE 1e-3 with and without the radiance cache.
+radiance_cache_mlp : inference and one training step of the cache MLP on 2^20
+           queries / samples against the measured bf16 tensor peak.
 cpu_baseline / --impl reference : the CPU oracle (a restatement of the reference's path:
            its single-threaded SAH build and the path_trace.wgsl estimator on all host cores),
            on a bounded row sample of the frame, extrapolated to one frame.
@@ -59,9 +68,9 @@ def parse():
                    help="same scene at 480x270, 4 spp: the profiling case (not a bench line)")
     p.add_argument("--leg", choices=["bvh_build", "cache_mlp", "frame"],
                    help="profiling case: only the GPU BVH builds of the workload's mesh, only the "
-                        "radiance-cache MLP (2^18 queries), or only frames of the workload (rebuild + render "
-                        "with the default closest-hit variant, 12 extend launches per frame); prints its "
-                        "timings, not a bench line")
+                        "radiance-cache MLP (2^18 queries), or only frames of the workload (autotune: 8 "
+                        "frames, then rebuild + render with the chosen closest-hit variant, 12 extend "
+                        "launches per frame); prints its timings, not a bench line")
     a = p.parse_args()
     if a.small:
         global W, H, SPP, WORKLOAD
@@ -473,6 +482,7 @@ def run_mcrt(args):
                           "launches_per_build": builds[-1][1]}))
         return
     if args.leg == "frame":
+        variant, _ = ctx.autotune(cam, W, H, SPP, max_depth=DEPTH)        # 8 frames, 12 extend launches each
         frames = []
         for i in range(args.warmup + args.steps):
             ctx.rebuild_bvh()

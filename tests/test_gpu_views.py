@@ -79,3 +79,24 @@ def test_world_views_workload(ctx):
     sizes = [(v["width"], v["height"]) for v in views]
     assert all(256 <= a <= 1920 and 256 <= b <= 1080 for a, b in sizes)
     assert len(set(sizes)) == 16
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_views_keep_accum_and_read_accum(ctx, ico, graph):
+    """render_views in two calls with keep equals one call with all the samples
+    (f64 sums from read_accum, running mean from the read-back), and each view's
+    slice of the sums equals its own single render's sums."""
+    views = _views(ico, [(40, 30), (23, 17), (9, 31)])
+    whole = ctx.render_views(views, 8, first_frame=0, max_depth=8, nee=True, graph=graph)
+    _, sum_whole = ctx.read_accum()
+    ctx.render_views(views, 3, first_frame=0, max_depth=8, nee=True, graph=graph, read_back=False)
+    split = ctx.render_views(views, 5, first_frame=3, max_depth=8, nee=True, graph=graph, keep=True)
+    _, sum_split = ctx.read_accum()
+    assert np.array_equal(sum_whole.view(np.uint64), sum_split.view(np.uint64))
+    for a, b in zip(whole, split):
+        assert np.array_equal(bits(a), bits(b))
+    off = 0
+    for cam, w, h in views:
+        want = ctx.render(cam, w, h, 8, max_depth=8, nee=True, outputs=("sum",))["sum"].reshape(-1, 3)
+        assert np.array_equal(sum_whole[0, off:off + w * h].view(np.uint64), want.view(np.uint64))
+        off += w * h
