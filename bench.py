@@ -500,9 +500,14 @@ def run_mcrt(args):
         ctx.rebuild_bvh()
         ctx.render(cam, W, H, SPP, first_frame=i * SPP, max_depth=DEPTH, outputs=())
 
+    # the end-to-end step's host buffers: the vertices in and the image out, in pinned memory
+    pin_vertices = torch.empty(sc["vertices"].nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(M.VERTEX)
+    np.copyto(pin_vertices, sc["vertices"])
+    pin_image = torch.empty(H * W * 4, dtype=torch.float32, pin_memory=True).numpy().reshape(H, W, 4)
+
     def step_e2e(i):
-        ctx.update_vertices(sc["vertices"])
-        ctx.render(cam, W, H, SPP, first_frame=i * SPP, max_depth=DEPTH, outputs=("rgba",))
+        ctx.update_vertices(pin_vertices)
+        ctx.render(cam, W, H, SPP, first_frame=i * SPP, max_depth=DEPTH, outputs=(), out_rgba=pin_image)
 
     breakdown = {}
 
@@ -587,6 +592,7 @@ def run_mcrt(args):
         "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": SPP, "max_depth": DEPTH,
                    "triangles": int(len(sc["triangles"])), "seed": SEED, "estimator": "reference (no NEE)",
                    "parallelism": f"replicas{world}", "l2": "256 MB buffer written between timed steps",
+                   "e2e_host_buffers": "pinned (vertices in, f32 RGBA image out)",
                    "extend_variant": variant, "extend_variant_info": M.variant_info(variant),
                    "autotune_extend_ms_per_frame": [round(x, 3) for x in tune_ms]},
         "e2e": {"value": round(e2e_value, 3), "unit": "Msamples/s",

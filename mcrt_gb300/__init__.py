@@ -314,12 +314,20 @@ class Context:
         return hits
 
     def render(self, camera, width, height, spp, first_frame=0, max_depth=0, nee=False, spp_per_pass=0,
-               keep=False, outputs=("rgba", "sum", "gbuf"), graph=False, cache=False):
+               keep=False, outputs=("rgba", "sum", "gbuf"), graph=False, cache=False, out_rgba=None):
+        """Render; outputs names the host arrays to return.  out_rgba: a caller-owned (height, width, 4)
+        float32 C-contiguous array (pinned host memory for the fastest copy) that receives the image."""
         cam = _arr(camera, CAMERA)
         o = N.RenderOpts(max_depth=max_depth, flags=(N.RENDER_NEE if nee else 0) |
                          (N.RENDER_KEEP_ACCUM if keep else 0) | (N.RENDER_GRAPH if graph else 0) |
                          (N.RENDER_CACHE if cache else 0), spp_per_pass=spp_per_pass)
-        rgba = np.zeros((height, width, 4), np.float32) if "rgba" in outputs else None
+        if out_rgba is not None:
+            if (out_rgba.dtype != np.float32 or out_rgba.shape != (height, width, 4)
+                    or not out_rgba.flags["C_CONTIGUOUS"]):
+                raise TypeError("out_rgba must be a C-contiguous float32 array of shape (height, width, 4)")
+            rgba = out_rgba
+        else:
+            rgba = np.zeros((height, width, 4), np.float32) if "rgba" in outputs else None
         acc = np.zeros((height, width, 3), np.float64) if "sum" in outputs else None
         gb = np.zeros((height, width, 4), np.float32) if "gbuf" in outputs else None
         self._check(lib().mcrt_render(self._h, ptr(cam), width, height, spp, first_frame, ctypes.byref(o),
