@@ -55,6 +55,7 @@ struct mcrt_ctx {
     bool has_scene = false;
     DBuf wnodes;
     uint32_t n_wnodes = 0;
+    bool wide_valid = false;    // wnodes matches the current mesh BVH
     DBuf spheres, sphere_ids, sphere_nodes, vertices, triangles, mesh_nodes, tri_order, trirecs, cnodes, materials,
         env, lights, light_cdf, tmp, staging, albedo, shade_recs;
     uint32_t albedo_layers = 0, albedo_size = 0;
@@ -242,12 +243,40 @@ mcrt_status finish_mesh(mcrt_ctx *ctx) {
                               &ncn, ctx->trirecs.p, ctx->tmp.as<uint32_t>(), tmp_words, st),
        "compact BVH");
     ctx->n_cnodes = ncn;
-    CK(ctx->wnodes.ensure((size_t)(nn / 2 + 1) * 64), "allocate wide nodes");
-    uint32_t nw = 0;
-    CK(mcrt::gpu_make_wide4(ctx->mesh_nodes.as<mcrt_gpu_bvh_node>(), nn, ctx->wnodes.as<uint4>(), &nw,
-                            ctx->tmp.as<uint32_t>(), st),
-       "4-wide BVH");
-    ctx->n_wnodes = nw;
+    ctx->wide_valid = false;                  // the 4-wide layout is built when a render first needs it
+    ctx->n_wnodes = 0;
+    return MCRT_OK;
+}
+
+// The quantised 4-wide BVH of the current mesh BVH, built on first use after
+// each (re)build: only the 4-wide closest-hit variants read it.
+mcrt_status ensure_wide(mcrt_ctx *ctx) {
+    if (ctx->wide_valid) return MCRT_OK;
+    const uint32_t nn = ctx->n_mesh_nodes;
+    if (nn) {
+        CK(ctx->wnodes.ensure((size_t)(nn / 2 + 1) * 64), "allocate wide nodes");
+        uint32_t nw = 0;
+        CK(mcrt::gpu_make_wide4(ctx->mesh_nodes.as<mcrt_gpu_bvh_node>(), nn, ctx->wnodes.as<uint4>(), &nw,
+                                ctx->tmp.as<uint32_t>(), ctx->stream),
+           "4-wide BVH");
+        ctx->n_wnodes = nw;
+    }
+    ctx->wide_valid = true;
+    return MCRT_OK;
+}
+
+// Closest-hit variant of a render (opts variant k + 1, else the context's),
+// with the layout it reads made ready.
+mcrt_status render_variant(mcrt_ctx *ctx, const mcrt_render_opts &o, int *variant) {
+    const int v = o.variant ? (int)o.variant - 1 : ctx->extend_variant;
+    if (v < 0 || v >= mcrt::extend_variant_count()) return fail(ctx, MCRT_ERR_INVALID_ARG, "variant out of range");
+    int info[5];
+    mcrt::extend_variant_info(v, info);
+    if (info[0] == 4) {
+        mcrt_status s = ensure_wide(ctx);
+        if (s != MCRT_OK) return s;
+    }
+    *variant = v;
     return MCRT_OK;
 }
 
@@ -714,6 +743,11 @@ static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, ui
         ctx->acc_h = h;
     }
     CK(cudaMemsetAsync(ctx->counters.p, 0, 256, st), "clear counters");
+    int variant = 0;
+    {
+        mcrt_status vs = render_variant(ctx, o, &variant);
+        if (vs != MCRT_OK) return vs;
+    }
     mcrt::DeviceScene S = device_scene(ctx);
     const bool want_gbuf = true;
     // ---- view tables: pixel prefix sums, sizes, cameras
@@ -766,7 +800,7 @@ static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, ui
         P.max_depth = depth;
         P.flags = o.flags;
         if (cam) P.cam = *cam;
-        P.extend_variant = o.variant ? (int)o.variant - 1 : ctx->extend_variant;
+        P.extend_variant = variant;
         if (views) {
             const size_t off_wh = ((size_t)(n_views + 1) * 4 + 15) / 16 * 16,
                          off_cam = off_wh + ((size_t)n_views * 8 + 15) / 16 * 16;
@@ -1013,6 +1047,11 @@ mcrt_status mcrt_adjoint(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t
     CK(cudaMemcpyAsync(ctx->dimg.p, d_image, (size_t)npix * 16, cudaMemcpyHostToDevice, st), "upload d_image");
     CK(cudaMemsetAsync(ctx->grad.p, 0, 256 * sizeof(double), st), "clear gradient");
     CK(cudaMemsetAsync(ctx->counters.p, 0, 256, st), "clear counters");
+    int variant = 0;
+    {
+        mcrt_status vs = render_variant(ctx, o, &variant);
+        if (vs != MCRT_OK) return vs;
+    }
     mcrt::DeviceScene S = device_scene(ctx);
     mcrt::AdjointParams A;
     A.dimg = ctx->dimg.as<float4>();
@@ -1032,7 +1071,7 @@ mcrt_status mcrt_adjoint(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t
         P.flags = o.flags;
         P.cam = *cam;
         P.gbuf_plane = -1;
-        P.extend_variant = o.variant ? (int)o.variant - 1 : ctx->extend_variant;
+        P.extend_variant = variant;
         // primal pass: the per-path radiance of these samples
         mcrt::launch_raygen(S, P, ctx->pb, st);
         int qi = 0;
