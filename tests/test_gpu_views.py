@@ -100,3 +100,17 @@ def test_views_keep_accum_and_read_accum(ctx, ico, graph):
         want = ctx.render(cam, w, h, 8, max_depth=8, nee=True, outputs=("sum",))["sum"].reshape(-1, 3)
         assert np.array_equal(sum_whole[0, off:off + w * h].view(np.uint64), want.view(np.uint64))
         off += w * h
+
+
+def test_render_into_caller_buffer(ctx, ico):
+    """render(out_rgba=...) fills a caller-owned (here pinned) array with the
+    same image as the returned one; a wrong shape or dtype is refused."""
+    torch = pytest.importorskip("torch")
+    c = ico["camera"]
+    cam = M.compute_camera(40, 24, c["look_from"], c["look_at"], c["vfov"], 0.0)
+    want = ctx.render(cam, 40, 24, 4, max_depth=8, outputs=("rgba",))["rgba"]
+    buf = torch.empty(24 * 40 * 4, dtype=torch.float32, pin_memory=True).numpy().reshape(24, 40, 4)
+    ctx.render(cam, 40, 24, 4, max_depth=8, outputs=(), out_rgba=buf)
+    assert np.array_equal(bits(buf), bits(want))
+    with pytest.raises(TypeError):
+        ctx.render(cam, 40, 24, 4, max_depth=8, outputs=(), out_rgba=np.zeros((24, 40, 3), np.float32))
