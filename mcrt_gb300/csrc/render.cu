@@ -635,7 +635,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
                 const uint32_t mine = base + __popc(idle_mask & ((1u << lane) - 1u));
                 if (mine < n) {
                     ray = mine;
-                    float4 o4 = qo[mine], d4 = qd[mine];
+                    float4 o4 = __ldcs(qo + mine), d4 = __ldcs(qd + mine);   // streamed: evict first
                     r = make_ray(xyz(o4), xyz(d4));
                     best = Closest{kTMax, MCRT_HIT_MISS, 0u, 0.0f, 0.0f};
                     spheres_hit(S, r, kTMin, kTMax, best, &nn);      // path_trace.wgsl:472-474
@@ -696,7 +696,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
                 if (best.prim == MCRT_HIT_MISS) best.t = -1.0f;
                 float u = (best.prim != MCRT_HIT_MISS && (best.prim & MCRT_HIT_SPHERE)) ? __uint_as_float(best.slot)
                                                                                          : best.u;
-                B.hits[ray] = make_float4(best.t, __uint_as_float(best.prim), u, best.v);
+                __stcs(B.hits + ray, make_float4(best.t, __uint_as_float(best.prim), u, best.v));
                 ray = 0xffffffffu;
                 ++traced;
             }
@@ -749,8 +749,10 @@ __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, Rende
         uint32_t sh_bits = 0;                  // adjoint: material | light material << 8
         float4 sh_dlog = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (i < n) {
-            float4 o4 = B.q_o[qi][i], d4 = B.q_d[qi][i];
-            float4 h = B.hits[i];
+            // the queues and hits are streamed once per bounce (GBs per frame):
+            // cache-streaming accesses keep them from evicting the BVH in L2
+            float4 o4 = __ldcs(B.q_o[qi] + i), d4 = __ldcs(B.q_d[qi] + i);
+            float4 h = __ldcs(B.hits + i);
             slot = __float_as_uint(o4.w);
             f3 o = xyz(o4), d = xyz(d4);
             float4 thr4 = B.thr[slot];
@@ -965,8 +967,8 @@ __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, Rende
             basepos = __shfl_sync(0xffffffffu, basepos, leader);
             if (cont) {
                 uint32_t pos = basepos + __popc(mask & ((1u << lane) - 1u));
-                B.q_o[qi ^ 1][pos] = make_float4(no.x, no.y, no.z, __uint_as_float(slot));
-                B.q_d[qi ^ 1][pos] = make_float4(nd.x, nd.y, nd.z, 0.0f);
+                __stcs(B.q_o[qi ^ 1] + pos, make_float4(no.x, no.y, no.z, __uint_as_float(slot)));
+                __stcs(B.q_d[qi ^ 1] + pos, make_float4(nd.x, nd.y, nd.z, 0.0f));
             }
         }
         unsigned smask = __ballot_sync(0xffffffffu, shadow);
