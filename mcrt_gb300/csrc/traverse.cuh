@@ -271,14 +271,90 @@ __device__ __forceinline__ Closest world_hit(const DeviceScene &S, const RayInv 
 
 // Any hit in (tmin, tmax) with the same visibility rules (backface-culled
 // triangles are invisible from behind); used by shadow rays.
+// Any triangle of a leaf that mesh_hit_fast would accept as a hit before its
+// first one: tri_test passes, t < tmax, not culled by the backface flag.
+__device__ __forceinline__ bool leaf_any(const DeviceScene &S, const RayInv &r, uint32_t first, uint32_t count,
+                                         float tmin, float tmax) {
+    for (uint32_t j = 0; j < count; ++j) {
+        const TriRec *tr = S.tris + first + j;
+        float4 a = __ldg(&tr->v0), b = __ldg(&tr->e1), c = __ldg(&tr->e2);
+        float t, u, v;
+        if (!tri_test(r, xyz(a), xyz(b), xyz(c), tmin, &t, &u, &v)) continue;
+        if (!(t < tmax)) continue;
+        if (__float_as_uint(b.w) & MCRT_BACKFACE_CULL_FLAG) {       // path_trace.wgsl:438-452
+            f3 n = tri_shading_normal(S, __float_as_uint(a.w), u, v);
+            if (!(dot(r.d, n) < 0.0f)) continue;
+        }
+        return true;
+    }
+    return false;
+}
+
+// Is there a mesh hit in [tmin, tmax)?  mesh_hit_fast's traversal (same
+// order, same cull against tmax) up to its first accepted hit, which alone
+// decides whether it finds one, so the answer is the same; it stops there.
+__device__ __forceinline__ bool mesh_any_hit(const DeviceScene &S, const RayInv &r, float tmin, float tmax,
+                                             uint32_t *overflow) {
+    if (S.n_mesh_nodes == 0) return false;
+    const float4 *root = reinterpret_cast<const float4 *>(S.mesh_nodes);
+    {
+        float4 mn = __ldg(root), mx = __ldg(root + 1);
+        float te;
+        if (!slab(r, mn.x, mn.y, mn.z, mx.x, mx.y, mx.z, tmin, tmax, &te)) return false;
+    }
+    if (S.n_cnodes == 0) {                       // the whole tree is one leaf
+        uint4 meta = __ldg(reinterpret_cast<const uint4 *>(root + 2));
+        return leaf_any(S, r, meta.x, meta.y, tmin, tmax);
+    }
+    uint2 stack[kStackSize];
+    uint32_t sp = 0;
+    uint32_t node = 0;
+    for (;;) {
+        const float4 *np = S.cnodes + 4ull * node;
+        float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
+        uint4 e = __ldg(reinterpret_cast<const uint4 *>(np + 3));
+        float tl, tr;
+        bool hl = e.x != kNoChild && slab(r, a.x, a.z, c.x, a.y, a.w, c.y, tmin, tmax, &tl);
+        bool hr = e.y != kNoChild && slab(r, b.x, b.z, c.z, b.y, b.w, c.w, tmin, tmax, &tr);
+        uint32_t next = kNoChild;
+        if (hl && hr) {
+            uint32_t near = e.x, far = e.y;
+            float tfar = tr;
+            if (tr < tl) { near = e.y; far = e.x; tfar = tl; }
+            if (sp < kStackSize) stack[sp++] = make_uint2(far, __float_as_uint(tfar));
+            else *overflow = 1u;
+            next = near;
+        } else if (hl) {
+            next = e.x;
+        } else if (hr) {
+            next = e.y;
+        }
+        for (;;) {
+            if (next == kNoChild) {
+                while (sp > 0) {
+                    uint2 s = stack[--sp];
+                    if (__uint_as_float(s.y) <= tmax) { next = s.x; break; }
+                }
+                if (next == kNoChild) return false;
+            }
+            if (next & kLeafBit) {
+                if (leaf_any(S, r, (next & ~kLeafBit) >> 4, leaf_count(S, next), tmin, tmax)) return true;
+                next = kNoChild;
+                continue;
+            }
+            break;
+        }
+        node = next;
+    }
+}
+
 __device__ __forceinline__ bool occluded(const DeviceScene &S, const RayInv &r, float tmin, float tmax,
                                          uint32_t *overflow) {
     uint32_t nn = 0;
     Closest best{tmax, MCRT_HIT_MISS, 0u, 0.0f, 0.0f};
     spheres_hit(S, r, tmin, tmax, best, &nn);
     if (best.prim != MCRT_HIT_MISS) return true;
-    mesh_hit_fast(S, r, tmin, best, &nn, overflow);
-    return best.prim != MCRT_HIT_MISS;
+    return mesh_any_hit(S, r, tmin, tmax, overflow);
 }
 
 }  // namespace mcrt
