@@ -602,12 +602,19 @@ __device__ __forceinline__ void visit_wide4(const DeviceScene &S, const RayInv &
     }
 }
 
-template <int WIDTH, int BLOCK, int MINB, int STACK, int REFILL>
+// ANY = true: the same persistent, refilled, speculative traversal for the
+// shadow-ray queue of next-event estimation, as an any-hit test: the cull
+// threshold stays the ray's t_max, so the set of boxes entered does not depend
+// on the visit order, and any accepted triangle hit in it (leaf_any) proves
+// the ray occluded, the answer of the closest-hit test; an unoccluded ray
+// adds its contribution to its path's radiance.
+template <int WIDTH, int BLOCK, int MINB, int STACK, int REFILL, bool ANY>
 __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffers B, int qi) {
-    const uint32_t n = B.counters[qi];
-    if (blockIdx.x == 0 && threadIdx.x == 0) { B.counters[qi ^ 1] = 0; B.counters[2] = 0; }
-    const float4 *qo = B.q_o[qi];
-    const float4 *qd = B.q_d[qi];
+    const uint32_t n = ANY ? B.counters[2] : B.counters[qi];
+    if (!ANY && blockIdx.x == 0 && threadIdx.x == 0) { B.counters[qi ^ 1] = 0; B.counters[2] = 0; }
+    const float4 *qo = ANY ? B.sh_o : B.q_o[qi];
+    const float4 *qd = ANY ? B.sh_d : B.q_d[qi];
+    uint32_t *work = B.counters + (ANY ? 5 : 4);    // the queue's next unclaimed entry
     const uint32_t lane = threadIdx.x & 31u;
     const bool has_mesh = S.n_mesh_nodes > 0;
     uint32_t ray = 0xffffffffu;       // queue index of the lane's ray, or none
@@ -621,6 +628,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
     uint32_t leaf = kNoChild;         // postponed leaf code
     uint32_t traced = 0;
     uint32_t nn = 0;
+    uint32_t slot = 0;                // ANY: the shadow ray's path
+    bool occl = false;                // ANY: an accepted hit was found
     for (;;) {
         // ---- refill idle lanes
         const bool idle = ray == 0xffffffffu;
@@ -628,7 +637,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
         if (!exhausted && (__popc(idle_mask) >= REFILL || idle_mask == 0xffffffffu)) {
             const int leader = __ffs(idle_mask) - 1;
             uint32_t base = 0;
-            if ((int)lane == leader) base = atomicAdd(B.counters + 4, (uint32_t)__popc(idle_mask));
+            if ((int)lane == leader) base = atomicAdd(work, (uint32_t)__popc(idle_mask));
             base = __shfl_sync(0xffffffffu, base, leader);
             if (base + (uint32_t)__popc(idle_mask) >= n) exhausted = true;
             if (idle) {
@@ -637,12 +646,18 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
                     ray = mine;
                     float4 o4 = __ldcs(qo + mine), d4 = __ldcs(qd + mine);   // streamed: evict first
                     r = make_ray(xyz(o4), xyz(d4));
-                    best = Closest{kTMax, MCRT_HIT_MISS, 0u, 0.0f, 0.0f};
-                    spheres_hit(S, r, kTMin, kTMax, best, &nn);      // path_trace.wgsl:472-474
+                    const float tmax = ANY ? d4.w : kTMax;
+                    best = Closest{tmax, MCRT_HIT_MISS, 0u, 0.0f, 0.0f};
+                    spheres_hit(S, r, kTMin, tmax, best, &nn);       // path_trace.wgsl:472-474
                     sp = 0;
                     leaf = kNoChild;
                     cur = kNoChild;
-                    if (has_mesh) {
+                    if (ANY) {
+                        slot = __float_as_uint(o4.w);
+                        occl = best.prim != MCRT_HIT_MISS;
+                        best.t = tmax;
+                    }
+                    if (has_mesh && !(ANY && occl)) {
                         const float4 *np = reinterpret_cast<const float4 *>(S.mesh_nodes);
                         float4 mn = __ldg(np), mx = __ldg(np + 1);
                         float te;
@@ -684,7 +699,15 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
             }
             // ---- leaf phase
             while (leaf != kNoChild) {
-                leaf_tris(S, r, (leaf & ~kLeafBit) >> 4, leaf_count(S, leaf), kTMin, best);
+                if (ANY) {
+                    if (leaf_any(S, r, (leaf & ~kLeafBit) >> 4, leaf_count(S, leaf), kTMin, best.t)) {
+                        occl = true;                                          // done: drop what is left
+                        cur = kNoChild;
+                        sp = 0;
+                    }
+                } else {
+                    leaf_tris(S, r, (leaf & ~kLeafBit) >> 4, leaf_count(S, leaf), kTMin, best);
+                }
                 leaf = kNoChild;
                 if (cur != kNoChild && (cur & kLeafBit) && cur_t <= best.t) {
                     leaf = cur;
@@ -693,16 +716,24 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
             }
             // ---- finished ray
             if (cur == kNoChild && sp == 0) {
-                if (best.prim == MCRT_HIT_MISS) best.t = -1.0f;
-                float u = (best.prim != MCRT_HIT_MISS && (best.prim & MCRT_HIT_SPHERE)) ? __uint_as_float(best.slot)
-                                                                                         : best.u;
-                __stcs(B.hits + ray, make_float4(best.t, __uint_as_float(best.prim), u, best.v));
+                if (ANY) {
+                    if (!occl) {                       // one shadow ray per path and bounce: no race on L
+                        const float4 c = B.sh_c[ray];
+                        const float4 L = B.L[slot];
+                        B.L[slot] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
+                    }
+                } else {
+                    if (best.prim == MCRT_HIT_MISS) best.t = -1.0f;
+                    float u = (best.prim != MCRT_HIT_MISS && (best.prim & MCRT_HIT_SPHERE))
+                                  ? __uint_as_float(best.slot) : best.u;
+                    __stcs(B.hits + ray, make_float4(best.t, __uint_as_float(best.prim), u, best.v));
+                }
                 ray = 0xffffffffu;
                 ++traced;
             }
         }
     }
-    if (traced) atomicAdd(B.stats, (unsigned long long)traced);
+    if (traced) atomicAdd(B.stats + (ANY ? 1 : 0), (unsigned long long)traced);
 }
 
 // Shading of the queued hits.  ADJ = false: the forward estimator.  ADJ = true:
@@ -1181,15 +1212,21 @@ int extend_variant_count() { return kExtendVariants; }
 
 namespace {
 using ExtendKernel = void (*)(DeviceScene, PathBuffers, int);
-#define MCRT_EXTEND_KERNEL(i)                                                                            \
+#define MCRT_EXTEND_KERNEL(i, any)                                                                       \
     k_extend<kVariantTable[i].width, kVariantTable[i].block, kVariantTable[i].min_blocks, kVariantTable[i].stack, \
-             kVariantTable[i].refill>
-const ExtendKernel kExtendKernels[kExtendVariants] = {MCRT_EXTEND_KERNEL(0), MCRT_EXTEND_KERNEL(1),
-                                                      MCRT_EXTEND_KERNEL(2), MCRT_EXTEND_KERNEL(3),
-                                                      MCRT_EXTEND_KERNEL(4), MCRT_EXTEND_KERNEL(5),
-                                                      MCRT_EXTEND_KERNEL(6), MCRT_EXTEND_KERNEL(7)};
+             kVariantTable[i].refill, any>
+const ExtendKernel kExtendKernels[kExtendVariants] = {
+    MCRT_EXTEND_KERNEL(0, false), MCRT_EXTEND_KERNEL(1, false), MCRT_EXTEND_KERNEL(2, false),
+    MCRT_EXTEND_KERNEL(3, false), MCRT_EXTEND_KERNEL(4, false), MCRT_EXTEND_KERNEL(5, false),
+    MCRT_EXTEND_KERNEL(6, false), MCRT_EXTEND_KERNEL(7, false)};
+// the any-hit instantiations, for the shadow rays of next-event estimation
+const ExtendKernel kShadowKernels[kExtendVariants] = {
+    MCRT_EXTEND_KERNEL(0, true), MCRT_EXTEND_KERNEL(1, true), MCRT_EXTEND_KERNEL(2, true),
+    MCRT_EXTEND_KERNEL(3, true), MCRT_EXTEND_KERNEL(4, true), MCRT_EXTEND_KERNEL(5, true),
+    MCRT_EXTEND_KERNEL(6, true), MCRT_EXTEND_KERNEL(7, true)};
 #undef MCRT_EXTEND_KERNEL
 int g_extend_per_sm[kExtendVariants] = {0, 0, 0, 0, 0, 0, 0, 0};
+int g_shadow_per_sm[kExtendVariants] = {0, 0, 0, 0, 0, 0, 0, 0};
 }  // namespace
 
 void extend_variant_info(int v, int out[5]) {
@@ -1200,12 +1237,18 @@ void extend_variant_info(int v, int out[5]) {
 // Resident blocks per SM of every variant (an occupancy query, made before any
 // stream capture of a render).
 void prepare_extend_variants() {
-    for (int v = 0; v < kExtendVariants; ++v)
+    for (int v = 0; v < kExtendVariants; ++v) {
         if (g_extend_per_sm[v] == 0) {
             int n = 0;
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kExtendKernels[v], kVariantTable[v].block, 0);
             g_extend_per_sm[v] = n > 0 ? n : 1;
         }
+        if (g_shadow_per_sm[v] == 0) {
+            int n = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kShadowKernels[v], kVariantTable[v].block, 0);
+            g_shadow_per_sm[v] = n > 0 ? n : 1;
+        }
+    }
 }
 
 void launch_extend(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, cudaStream_t st) {
@@ -1230,9 +1273,16 @@ void launch_shade(const DeviceScene &S, const RenderParams &P, PathBuffers &B, i
 void launch_shadow(const DeviceScene &S, const RenderParams &P, PathBuffers &B, cudaStream_t st,
                    const AdjointParams *adj) {
     uint32_t nmax = P.npix * P.spp_pass;
-    int blocks = min(grid_blocks_for(nmax, 128), sm_count() * 16);
-    if (adj) k_shadow<true><<<blocks, 128, 0, st>>>(S, B, *adj);
-    else k_shadow<false><<<blocks, 128, 0, st>>>(S, B, AdjointParams{});
+    if (adj) {                                  // the replay: gradients per shadow ray, one thread each
+        int blocks = min(grid_blocks_for(nmax, 128), sm_count() * 16);
+        k_shadow<true><<<blocks, 128, 0, st>>>(S, B, *adj);
+    } else {                                    // persistent any-hit traversal, the render's variant
+        const int v = (P.extend_variant >= 0 && P.extend_variant < kExtendVariants) ? P.extend_variant : 0;
+        prepare_extend_variants();
+        const int block = kVariantTable[v].block;
+        int blocks = min(grid_blocks_for(nmax, block), sm_count() * g_shadow_per_sm[v]);
+        kShadowKernels[v]<<<blocks, block, 0, st>>>(S, B, 0);
+    }
     ::mcrt::note_launch();
 }
 
