@@ -66,11 +66,12 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--small", action="store_true",
                    help="same scene at 480x270, 4 spp: the profiling case (not a bench line)")
-    p.add_argument("--leg", choices=["bvh_build", "cache_mlp", "frame"],
+    p.add_argument("--leg", choices=["bvh_build", "cache_mlp", "frame", "adjoint"],
                    help="profiling case: only the GPU BVH builds of the workload's mesh, only the "
-                        "radiance-cache MLP (2^18 queries), or only frames of the workload (autotune: 8 "
+                        "radiance-cache MLP (2^18 queries), only frames of the workload (autotune: 8 "
                         "frames, then rebuild + render with the chosen closest-hit variant, 12 extend "
-                        "launches per frame); prints its timings, not a bench line")
+                        "launches per frame), or only the adjoint calls of the adjoint leg; prints its "
+                        "timings, not a bench line")
     a = p.parse_args()
     if a.small:
         global W, H, SPP, WORKLOAD
@@ -469,6 +470,9 @@ def run_mcrt(args):
     if args.leg == "cache_mlp":
         ctx.cache_init(0)
         print(json.dumps(mlp_rate(M, ctx, n=1 << 18, reps=args.steps)))
+        return
+    if args.leg == "adjoint":
+        print(json.dumps(adjoint_rate(M, ctx, stream, n_warm=args.warmup, n_calls=args.steps)))
         return
     ctx.upload_scene(vertices=sc["vertices"], triangles=sc["triangles"], materials=sc["materials"], env=sc["env"])
     if args.leg == "bvh_build":

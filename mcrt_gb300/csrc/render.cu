@@ -608,8 +608,18 @@ __device__ __forceinline__ void visit_wide4(const DeviceScene &S, const RayInv &
 // on the visit order, and any accepted triangle hit in it (leaf_any) proves
 // the ray occluded, the answer of the closest-hit test; an unoccluded ray
 // adds its contribution to its path's radiance.
-template <int WIDTH, int BLOCK, int MINB, int STACK, int REFILL, bool ANY>
-__global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffers B, int qi) {
+// ADJ (with ANY): the adjoint replay's shadow rays.  An unoccluded ray's
+// next-event term N leaves the radiance still ahead of its path (B.L -= N) and
+// contributes delta * N * dlog(f)/d(params) to its vertex's material and
+// delta * N / albedo to the emitter's radiance colour, collected in shared
+// memory per block and added once per block at the end.
+template <int WIDTH, int BLOCK, int MINB, int STACK, int REFILL, bool ANY, bool ADJ>
+__global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffers B, int qi, AdjointParams A) {
+    __shared__ float gacc[ADJ ? 256 : 1];
+    if (ADJ) {
+        for (uint32_t k = threadIdx.x; k < 256u; k += BLOCK) gacc[k] = 0.0f;
+        __syncthreads();
+    }
     const uint32_t n = ANY ? B.counters[2] : B.counters[qi];
     if (!ANY && blockIdx.x == 0 && threadIdx.x == 0) { B.counters[qi ^ 1] = 0; B.counters[2] = 0; }
     const float4 *qo = ANY ? B.sh_o : B.q_o[qi];
@@ -720,7 +730,29 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
                     if (!occl) {                       // one shadow ray per path and bounce: no race on L
                         const float4 c = B.sh_c[ray];
                         const float4 L = B.L[slot];
-                        B.L[slot] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
+                        if (!ADJ) {
+                            B.L[slot] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
+                        } else {
+                            B.L[slot] = make_float4(L.x - c.x, L.y - c.y, L.z - c.z, 0.0f);
+                            auto gadd = [&](uint32_t k, float v) {
+                                if (v != 0.0f) atomicAdd(&gacc[k], v);
+                            };
+                            const uint32_t bits = __float_as_uint(c.w);
+                            const uint32_t mi = bits & 0xffu, lm = (bits >> 8) & 0xffu;
+                            const float4 di = A.dimg[B.aux[slot].y];
+                            const f3 dn = (A.inv_spp * xyz(di)) * xyz(c);
+                            const float4 g = B.sh_g[ray];
+                            gadd(4u * mi + 0, dn.x * g.x);
+                            gadd(4u * mi + 1, dn.y * g.y);
+                            gadd(4u * mi + 2, dn.z * g.z);
+                            gadd(4u * mi + 3, ((dn.x + dn.y) + dn.z) * g.w);
+                            if (lm <= kMaxMatIdx) {                       // not the directional light
+                                const float *la = S.materials->materials[lm].albedo_fuzz;
+                                gadd(4u * lm + 0, safe_ratio(dn.x, la[0]));
+                                gadd(4u * lm + 1, safe_ratio(dn.y, la[1]));
+                                gadd(4u * lm + 2, safe_ratio(dn.z, la[2]));
+                            }
+                        }
                     }
                 } else {
                     if (best.prim == MCRT_HIT_MISS) best.t = -1.0f;
@@ -734,6 +766,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
         }
     }
     if (traced) atomicAdd(B.stats + (ANY ? 1 : 0), (unsigned long long)traced);
+    if (ADJ) {
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < 256u; k += BLOCK) {
+            const float v = gacc[k];
+            if (v != 0.0f) atomicAdd(A.grad + k, (double)v);
+        }
+    }
 }
 
 // Shading of the queued hits.  ADJ = false: the forward estimator.  ADJ = true:
@@ -743,10 +782,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
 // by vertex, to the radiance still ahead of the path (Lrem).  With the sampling
 // held fixed (detached), a parameter pi of the vertex's material changes
 //   an emitted term E               by  E * dlog(Le)/dpi,
-//   a next-event term N             by  N * dlog(f)/dpi       (k_shadow),
+//   a next-event term N             by  N * dlog(f)/dpi       (shadow rays),
 //   every term after the BSDF sample by Lrem * dlog(f cos / pdf)/dpi,
 // each weighted by delta = dLoss/dImage(pixel) / spp.  The last one needs Lrem
-// after this vertex's next-event term, which k_shadow subtracts after this
+// after this vertex's next-event term, which the shadow rays subtract after this
 // kernel: it is stored (B.pend, material in aux.w bits 8..15) and applied at
 // the path's next vertex.  Gradients collect in shared memory per block, then
 // one double atomic per parameter and block.
@@ -1038,62 +1077,6 @@ __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, Rende
     }
 }
 
-// Shadow rays of next-event estimation.  ADJ: the replay -- a visible term N
-// leaves the radiance still ahead (B.L -= N) and contributes
-// delta * N * dlog(f)/d(params) to its vertex's material and
-// delta * N / albedo to the emitter's radiance colour.
-template <bool ADJ>
-__global__ void __launch_bounds__(128) k_shadow(DeviceScene S, PathBuffers B, AdjointParams A) {
-    __shared__ float gacc[ADJ ? 256 : 1];
-    if (ADJ) {
-        gacc[threadIdx.x] = 0.0f;
-        gacc[threadIdx.x + 128] = 0.0f;
-        __syncthreads();
-    }
-    auto gadd = [&](uint32_t k, float v) {
-        if (ADJ && v != 0.0f) atomicAdd(&gacc[k], v);
-    };
-    const uint32_t n = B.counters[2];
-    uint32_t traced = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 o4 = B.sh_o[i], d4 = B.sh_d[i];
-        RayInv r = make_ray(xyz(o4), xyz(d4));
-        ++traced;
-        if (occluded(S, r, kTMin, d4.w, B.counters + 3)) continue;
-        uint32_t slot = __float_as_uint(o4.w);
-        float4 c = B.sh_c[i];
-        float4 L = B.L[slot];
-        if (!ADJ) {
-            B.L[slot] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
-        } else {
-            B.L[slot] = make_float4(L.x - c.x, L.y - c.y, L.z - c.z, 0.0f);
-            const uint32_t bits = __float_as_uint(c.w);
-            const uint32_t mi = bits & 0xffu, lm = (bits >> 8) & 0xffu;
-            float4 di = A.dimg[B.aux[slot].y];
-            f3 dn = (A.inv_spp * xyz(di)) * xyz(c);
-            float4 g = B.sh_g[i];
-            gadd(4u * mi + 0, dn.x * g.x);
-            gadd(4u * mi + 1, dn.y * g.y);
-            gadd(4u * mi + 2, dn.z * g.z);
-            gadd(4u * mi + 3, ((dn.x + dn.y) + dn.z) * g.w);
-            if (lm <= kMaxMatIdx) {                       // not the directional light
-                const float *la = S.materials->materials[lm].albedo_fuzz;
-                gadd(4u * lm + 0, safe_ratio(dn.x, la[0]));
-                gadd(4u * lm + 1, safe_ratio(dn.y, la[1]));
-                gadd(4u * lm + 2, safe_ratio(dn.z, la[2]));
-            }
-        }
-    }
-    if (traced) atomicAdd(B.stats + 1, (unsigned long long)traced);
-    if (ADJ) {
-        __syncthreads();
-        for (uint32_t k = threadIdx.x; k < 256; k += 128) {
-            const float v = gacc[k];
-            if (v != 0.0f) atomicAdd(A.grad + k, (double)v);
-        }
-    }
-}
-
 // Per pixel, in frame order: the reference's f32 running mean
 // (path_trace.wgsl:656-661, mix = a*(1-t) + b*t) and the f64 sum.
 __global__ void k_resolve(RenderParams P, PathBuffers B, float4 *mean, double *sum, int keep) {
@@ -1211,22 +1194,24 @@ void launch_raygen(const DeviceScene &S, const RenderParams &P, PathBuffers &B, 
 int extend_variant_count() { return kExtendVariants; }
 
 namespace {
-using ExtendKernel = void (*)(DeviceScene, PathBuffers, int);
-#define MCRT_EXTEND_KERNEL(i, any)                                                                       \
+using ExtendKernel = void (*)(DeviceScene, PathBuffers, int, AdjointParams);
+#define MCRT_EXTEND_KERNEL(i, any, adj)                                                                  \
     k_extend<kVariantTable[i].width, kVariantTable[i].block, kVariantTable[i].min_blocks, kVariantTable[i].stack, \
-             kVariantTable[i].refill, any>
-const ExtendKernel kExtendKernels[kExtendVariants] = {
-    MCRT_EXTEND_KERNEL(0, false), MCRT_EXTEND_KERNEL(1, false), MCRT_EXTEND_KERNEL(2, false),
-    MCRT_EXTEND_KERNEL(3, false), MCRT_EXTEND_KERNEL(4, false), MCRT_EXTEND_KERNEL(5, false),
-    MCRT_EXTEND_KERNEL(6, false), MCRT_EXTEND_KERNEL(7, false)};
+             kVariantTable[i].refill, any, adj>
+#define MCRT_EXTEND_TABLE(any, adj)                                                                      \
+    {MCRT_EXTEND_KERNEL(0, any, adj), MCRT_EXTEND_KERNEL(1, any, adj), MCRT_EXTEND_KERNEL(2, any, adj),    \
+     MCRT_EXTEND_KERNEL(3, any, adj), MCRT_EXTEND_KERNEL(4, any, adj), MCRT_EXTEND_KERNEL(5, any, adj),    \
+     MCRT_EXTEND_KERNEL(6, any, adj), MCRT_EXTEND_KERNEL(7, any, adj)}
+const ExtendKernel kExtendKernels[kExtendVariants] = MCRT_EXTEND_TABLE(false, false);
 // the any-hit instantiations, for the shadow rays of next-event estimation
-const ExtendKernel kShadowKernels[kExtendVariants] = {
-    MCRT_EXTEND_KERNEL(0, true), MCRT_EXTEND_KERNEL(1, true), MCRT_EXTEND_KERNEL(2, true),
-    MCRT_EXTEND_KERNEL(3, true), MCRT_EXTEND_KERNEL(4, true), MCRT_EXTEND_KERNEL(5, true),
-    MCRT_EXTEND_KERNEL(6, true), MCRT_EXTEND_KERNEL(7, true)};
+const ExtendKernel kShadowKernels[kExtendVariants] = MCRT_EXTEND_TABLE(true, false);
+// the same for the adjoint replay, which adds gradients per unoccluded shadow ray
+const ExtendKernel kShadowAdjKernels[kExtendVariants] = MCRT_EXTEND_TABLE(true, true);
+#undef MCRT_EXTEND_TABLE
 #undef MCRT_EXTEND_KERNEL
 int g_extend_per_sm[kExtendVariants] = {0, 0, 0, 0, 0, 0, 0, 0};
 int g_shadow_per_sm[kExtendVariants] = {0, 0, 0, 0, 0, 0, 0, 0};
+int g_shadow_adj_per_sm[kExtendVariants] = {0, 0, 0, 0, 0, 0, 0, 0};
 }  // namespace
 
 void extend_variant_info(int v, int out[5]) {
@@ -1248,6 +1233,11 @@ void prepare_extend_variants() {
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kShadowKernels[v], kVariantTable[v].block, 0);
             g_shadow_per_sm[v] = n > 0 ? n : 1;
         }
+        if (g_shadow_adj_per_sm[v] == 0) {
+            int n = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kShadowAdjKernels[v], kVariantTable[v].block, 0);
+            g_shadow_adj_per_sm[v] = n > 0 ? n : 1;
+        }
     }
 }
 
@@ -1258,7 +1248,7 @@ void launch_extend(const DeviceScene &S, const RenderParams &P, PathBuffers &B, 
     const int block = kVariantTable[v].block;
     uint32_t nmax = P.npix * P.spp_pass;
     int blocks = min(grid_blocks_for(nmax, block), sm_count() * g_extend_per_sm[v]);
-    kExtendKernels[v]<<<blocks, block, 0, st>>>(S, B, qi); ::mcrt::note_launch();
+    kExtendKernels[v]<<<blocks, block, 0, st>>>(S, B, qi, AdjointParams{}); ::mcrt::note_launch();
 }
 
 void launch_shade(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, uint32_t bounce,
@@ -1272,17 +1262,16 @@ void launch_shade(const DeviceScene &S, const RenderParams &P, PathBuffers &B, i
 
 void launch_shadow(const DeviceScene &S, const RenderParams &P, PathBuffers &B, cudaStream_t st,
                    const AdjointParams *adj) {
+    // persistent any-hit traversal with the render's variant; the adjoint
+    // replay's instantiation also adds the gradients of unoccluded rays
     uint32_t nmax = P.npix * P.spp_pass;
-    if (adj) {                                  // the replay: gradients per shadow ray, one thread each
-        int blocks = min(grid_blocks_for(nmax, 128), sm_count() * 16);
-        k_shadow<true><<<blocks, 128, 0, st>>>(S, B, *adj);
-    } else {                                    // persistent any-hit traversal, the render's variant
-        const int v = (P.extend_variant >= 0 && P.extend_variant < kExtendVariants) ? P.extend_variant : 0;
-        prepare_extend_variants();
-        const int block = kVariantTable[v].block;
-        int blocks = min(grid_blocks_for(nmax, block), sm_count() * g_shadow_per_sm[v]);
-        kShadowKernels[v]<<<blocks, block, 0, st>>>(S, B, 0);
-    }
+    const int v = (P.extend_variant >= 0 && P.extend_variant < kExtendVariants) ? P.extend_variant : 0;
+    prepare_extend_variants();
+    const int block = kVariantTable[v].block;
+    const int per_sm = adj ? g_shadow_adj_per_sm[v] : g_shadow_per_sm[v];
+    int blocks = min(grid_blocks_for(nmax, block), sm_count() * per_sm);
+    if (adj) kShadowAdjKernels[v]<<<blocks, block, 0, st>>>(S, B, 0, *adj);
+    else kShadowKernels[v]<<<blocks, block, 0, st>>>(S, B, 0, AdjointParams{});
     ::mcrt::note_launch();
 }
 
