@@ -55,6 +55,10 @@ WORKLOAD = "displaced_icosphere_l8_1.31Mtri_1920x1080_16spp_depth12_gpu_rebuild"
 # DRAM bytes (read + write) per traced ray of the closest-hit kernel on this
 # workload, from one ncu capture of a frame's 12 launches (10.26 GB / 71.5 M rays)
 EXTEND_DRAM_BYTES_PER_RAY = 143.4
+# the reference traversal's mean nodes visited / triangles tested per ray on the
+# reference BVH of this workload (oracle statistics over a sample of its paths),
+# used when a run skips the oracle sample (--no-cpu-baseline)
+REF_NODES_PER_RAY, REF_TRIS_PER_RAY = 46.3, 6.26
 
 
 def parse():
@@ -564,21 +568,23 @@ def run_mcrt(args):
     ext_launches = sum(e[1] for e in ext)
     rays = sum(e[2] for e in ext)
     roof = None
-    if st and st["rays"]:
-        n_node, n_tri = st["nodes"] / st["rays"], st["prims"] / st["rays"]
+    if not args.small:
+        if st and st["rays"]:
+            n_node, n_tri, n_source = st["nodes"] / st["rays"], st["prims"] / st["rays"], "oracle sample of this run"
+        else:
+            n_node, n_tri, n_source = REF_NODES_PER_RAY, REF_TRIS_PER_RAY, "recorded oracle statistics"
         b_ray = 48 * n_node + 64 * n_tri + 32 + 16
         achieved = rays * b_ray / (ext_ms / 1000.0) / 1e9
         rays_per_launch = rays / max(ext_launches, 1)
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4),
-                # measured DRAM bytes per launch: ncu dram__bytes_read.sum + dram__bytes_write.sum over one
-                # frame of this workload (profiles/k_extend_displaced_icosphere_1080p16.md), per ray, times
-                # this run's rays per launch
+                # measured DRAM bytes per launch: ncu dram__bytes_read.sum + dram__bytes_write.sum over the
+                # 12 extend launches of one frame of this workload, per ray, times this run's rays per launch
                 "traffic": round(EXTEND_DRAM_BYTES_PER_RAY * rays_per_launch),
                 "traffic_unit": "B per launch", "traffic_per_ray": EXTEND_DRAM_BYTES_PER_RAY,
                 "peak_kind": peak_kind,
                 "kernel": "k_extend", "bytes_per_ray": round(b_ray, 1), "n_node": round(n_node, 2),
-                "n_tri": round(n_tri, 2), "mrays_per_s": round(rays / (ext_ms / 1000.0) / 1e6, 1),
+                "n_tri": round(n_tri, 2), "n_source": n_source, "mrays_per_s": round(rays / (ext_ms / 1000.0) / 1e6, 1),
                 "avg_launch_ms": round(ext_ms / max(ext_launches, 1), 4)}
     clocks = clk.summary()
     quality = adjoint = voxel = views = views_cache = mlp = None
