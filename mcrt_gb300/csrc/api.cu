@@ -825,7 +825,7 @@ static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, ui
         for (uint32_t b = 0; b < depth; ++b) {
             size_t a0 = 0, a1 = 0, a2 = 0;
             if (timed) { a0 = evi++; cudaEventRecord(ev(ctx, a0), st); }
-            mcrt::launch_extend(S, P, ctx->pb, qi, st);
+            mcrt::launch_extend(S, P, ctx->pb, qi, st, b == 0);
             ++extend_launches;
             if (timed) { a1 = evi++; cudaEventRecord(ev(ctx, a1), st); }
             mcrt::launch_shade(S, P, ctx->pb, qi, b, ctx->gbuf.as<float4>(), st);
@@ -1076,7 +1076,7 @@ mcrt_status mcrt_adjoint(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t
         mcrt::launch_raygen(S, P, ctx->pb, st);
         int qi = 0;
         for (uint32_t b = 0; b < depth; ++b) {
-            mcrt::launch_extend(S, P, ctx->pb, qi, st);
+            mcrt::launch_extend(S, P, ctx->pb, qi, st, b == 0);
             mcrt::launch_shade(S, P, ctx->pb, qi, b, nullptr, st);
             if (nee) mcrt::launch_shadow(S, P, ctx->pb, st);
             qi ^= 1;
@@ -1086,7 +1086,7 @@ mcrt_status mcrt_adjoint(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t
         mcrt::launch_raygen(S, P, ctx->pb, st, true);
         qi = 0;
         for (uint32_t b = 0; b < depth; ++b) {
-            mcrt::launch_extend(S, P, ctx->pb, qi, st);
+            mcrt::launch_extend(S, P, ctx->pb, qi, st, b == 0);
             mcrt::launch_shade(S, P, ctx->pb, qi, b, nullptr, st, &A);
             if (nee) mcrt::launch_shadow(S, P, ctx->pb, st, &A);
             qi ^= 1;

@@ -109,7 +109,9 @@ void launch_trace_closest(const DeviceScene &S, const mcrt_ray *rays, uint32_t n
 // pass stays in B.L as the radiance still to be accounted for).
 void launch_raygen(const DeviceScene &S, const RenderParams &P, PathBuffers &B, cudaStream_t st,
                    bool keep_radiance = false);
-void launch_extend(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, cudaStream_t st);
+// primary: the queue holds the pass's camera rays in slot order (bounce 0).
+void launch_extend(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, cudaStream_t st,
+                   bool primary = false);
 // adj non-null: the adjoint replay variants (same sampling, plus gradient accumulation).
 void launch_shade(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, uint32_t bounce,
                   float4 *gbuf, cudaStream_t st, const AdjointParams *adj = nullptr);

@@ -126,7 +126,7 @@ extern "C" mcrt_status mcrt_render_noalloc(mcrt_ctx *ctx, const mcrt_camera_unif
         mcrt::launch_raygen(S, P, B, st);
         int qi = 0;
         for (uint32_t b = 0; b < depth; ++b) {
-            mcrt::launch_extend(S, P, B, qi, st);
+            mcrt::launch_extend(S, P, B, qi, st, b == 0);
             mcrt::launch_shade(S, P, B, qi, b, nullptr, st);
             if (nee) mcrt::launch_shadow(S, P, B, st);
             qi ^= 1;

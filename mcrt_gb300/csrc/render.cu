@@ -775,6 +775,117 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
     }
 }
 
+// Closest hit for the primary rays (bounce 0), one warp per packet of 32
+// consecutive queue entries.  Slots are pixel-major, so a packet holds a pixel's
+// samples: nearly the same ray 32 times.  The warp walks one node stream: a
+// child is entered when any lane's ray enters its box before that lane's
+// closest t (each lane culls with its own), and every lane tests the same
+// node and leaf records from one broadcast load, so a packet costs about one
+// ray's traversal with all lanes busy.  The set of boxes a lane sees is a
+// superset of its own traversal's and every triangle test is exact, so the
+// closest hit under the tie rule is the per-ray kernel's.
+//  * Near child: the one most lanes enter first.
+//  * Stack: distributed over the lanes (entry k in lane k % 32, register
+//    k / 32), each entry the child code and the smallest entry distance of the
+//    lanes that entered it; popped entries no lane can still reach are dropped.
+constexpr int kPacketBlock = 128;
+constexpr uint32_t kPacketStack = 64;
+__global__ void __launch_bounds__(kPacketBlock) k_extend_packet(DeviceScene S, PathBuffers B, int qi) {
+    const uint32_t n = B.counters[qi];
+    if (blockIdx.x == 0 && threadIdx.x == 0) { B.counters[qi ^ 1] = 0; B.counters[2] = 0; }
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warp = (blockIdx.x * kPacketBlock + threadIdx.x) >> 5;
+    const uint32_t n_warps = (gridDim.x * kPacketBlock) >> 5;
+    const bool has_mesh = S.n_mesh_nodes > 0;
+    uint32_t traced = 0, nn = 0;
+    for (uint32_t base = warp * 32u; base < n; base += n_warps * 32u) {
+        const uint32_t ray = base + lane;
+        const bool active = ray < n;
+        RayInv r;
+        Closest best{kTMax, MCRT_HIT_MISS, 0u, 0.0f, 0.0f};
+        bool want = false;
+        if (active) {
+            const float4 o4 = __ldcs(B.q_o[qi] + ray), d4 = __ldcs(B.q_d[qi] + ray);
+            r = make_ray(xyz(o4), xyz(d4));
+            spheres_hit(S, r, kTMin, kTMax, best, &nn);                   // path_trace.wgsl:472-474
+            if (has_mesh) {
+                const float4 *np = reinterpret_cast<const float4 *>(S.mesh_nodes);
+                const float4 mn = __ldg(np), mx = __ldg(np + 1);
+                float te;
+                want = slab(r, mn.x, mn.y, mn.z, mx.x, mx.y, mx.z, kTMin, best.t, &te);
+            }
+        }
+        uint32_t cur = kNoChild;
+        if (__any_sync(0xffffffffu, want)) {
+            if (S.n_cnodes == 0) {
+                const uint4 meta = __ldg(reinterpret_cast<const uint4 *>(S.mesh_nodes) + 2);
+                cur = leaf_code(meta.x, meta.y);
+            } else {
+                cur = 0;
+            }
+        }
+        uint32_t sn0 = 0, sn1 = 0, st0 = 0, st1 = 0;   // this lane's stack entries k = lane, lane + 32
+        uint32_t sp = 0;
+        while (cur != kNoChild) {
+            if (cur & kLeafBit) {
+                if (active) leaf_tris(S, r, (cur & ~kLeafBit) >> 4, leaf_count(S, cur), kTMin, best);
+                cur = kNoChild;
+            } else {
+                const float4 *np = S.cnodes + 4ull * cur;
+                const float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
+                const uint4 e = __ldg(reinterpret_cast<const uint4 *>(np + 3));
+                float tl = 0.0f, tr = 0.0f;
+                const bool hl = active && e.x != kNoChild && slab(r, a.x, a.z, c.x, a.y, a.w, c.y, kTMin, best.t, &tl);
+                const bool hr = active && e.y != kNoChild && slab(r, b.x, b.z, c.z, b.y, b.w, c.w, kTMin, best.t, &tr);
+                const uint32_t ml = __ballot_sync(0xffffffffu, hl), mr = __ballot_sync(0xffffffffu, hr);
+                if (ml && mr) {
+                    const uint32_t pref_r = __ballot_sync(0xffffffffu, hr && (!hl || tr < tl));
+                    const bool right_first = 2u * __popc(pref_r) > (uint32_t)__popc(ml | mr);
+                    const bool hit_far = right_first ? hl : hr;
+                    const float t_far = right_first ? tl : tr;
+                    // entry distances >= 0 order as their bits; no lane: +inf
+                    const uint32_t key = hit_far ? __float_as_uint(fmaxf(t_far, 0.0f)) : 0x7f800000u;
+                    const uint32_t far_t = __reduce_min_sync(0xffffffffu, key);
+                    const uint32_t far = right_first ? e.x : e.y;
+                    if (sp < kPacketStack) {
+                        if (lane == (sp & 31u)) {
+                            if (sp < 32u) { sn0 = far; st0 = far_t; } else { sn1 = far; st1 = far_t; }
+                        }
+                        ++sp;
+                    } else if (lane == 0) {
+                        B.counters[3] = 1u;
+                    }
+                    cur = right_first ? e.y : e.x;
+                } else if (ml) {
+                    cur = e.x;
+                } else if (mr) {
+                    cur = e.y;
+                } else {
+                    cur = kNoChild;
+                }
+            }
+            if (cur == kNoChild && sp > 0) {
+                // pop the next entry some lane can still reach
+                const uint32_t reach = __reduce_max_sync(0xffffffffu, active ? __float_as_uint(best.t) : 0u);
+                while (sp > 0) {
+                    --sp;
+                    const uint32_t node = __shfl_sync(0xffffffffu, sp < 32u ? sn0 : sn1, sp & 31u);
+                    const uint32_t t = __shfl_sync(0xffffffffu, sp < 32u ? st0 : st1, sp & 31u);
+                    if (t <= reach) { cur = node; break; }
+                }
+            }
+        }
+        if (active) {
+            if (best.prim == MCRT_HIT_MISS) best.t = -1.0f;
+            const float u = (best.prim != MCRT_HIT_MISS && (best.prim & MCRT_HIT_SPHERE))
+                                ? __uint_as_float(best.slot) : best.u;
+            __stcs(B.hits + ray, make_float4(best.t, __uint_as_float(best.prim), u, best.v));
+            ++traced;
+        }
+    }
+    if (traced) atomicAdd(B.stats, (unsigned long long)traced);
+}
+
 // Shading of the queued hits.  ADJ = false: the forward estimator.  ADJ = true:
 // the adjoint replay of the same paths (path-replay backpropagation, Vicini et
 // al. 2021): the sampling is the forward code's, consuming the same random
@@ -1212,6 +1323,7 @@ const ExtendKernel kShadowAdjKernels[kExtendVariants] = MCRT_EXTEND_TABLE(true, 
 int g_extend_per_sm[kExtendVariants] = {0, 0, 0, 0, 0, 0, 0, 0};
 int g_shadow_per_sm[kExtendVariants] = {0, 0, 0, 0, 0, 0, 0, 0};
 int g_shadow_adj_per_sm[kExtendVariants] = {0, 0, 0, 0, 0, 0, 0, 0};
+int g_packet_per_sm = 0;
 }  // namespace
 
 void extend_variant_info(int v, int out[5]) {
@@ -1219,9 +1331,14 @@ void extend_variant_info(int v, int out[5]) {
     out[0] = e.width; out[1] = e.block; out[2] = e.min_blocks; out[3] = e.stack; out[4] = e.refill;
 }
 
-// Resident blocks per SM of every variant (an occupancy query, made before any
-// stream capture of a render).
+// Resident blocks per SM of every variant and of the packet kernel (occupancy
+// queries, made before any stream capture of a render).
 void prepare_extend_variants() {
+    if (g_packet_per_sm == 0) {
+        int n = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_extend_packet, kPacketBlock, 0);
+        g_packet_per_sm = n > 0 ? n : 1;
+    }
     for (int v = 0; v < kExtendVariants; ++v) {
         if (g_extend_per_sm[v] == 0) {
             int n = 0;
@@ -1241,9 +1358,16 @@ void prepare_extend_variants() {
     }
 }
 
-void launch_extend(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, cudaStream_t st) {
+void launch_extend(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, cudaStream_t st,
+                   bool primary) {
     const int v = (P.extend_variant >= 0 && P.extend_variant < kExtendVariants) ? P.extend_variant : 0;
     prepare_extend_variants();
+    if (primary) {                    // the camera rays: warp packets, every warp resident at once
+        const uint32_t nmax = P.npix * P.spp_pass;
+        const int blocks = min(grid_blocks_for(nmax, kPacketBlock), sm_count() * g_packet_per_sm);
+        k_extend_packet<<<blocks, kPacketBlock, 0, st>>>(S, B, qi); ::mcrt::note_launch();
+        return;
+    }
     // persistent: as many resident blocks as fit, never more warps than rays
     const int block = kVariantTable[v].block;
     uint32_t nmax = P.npix * P.spp_pass;
