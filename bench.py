@@ -33,6 +33,8 @@ cpu_baseline / --impl reference : the CPU oracle (a restatement of the reference
            on a bounded row sample of the frame, extrapolated to one frame.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Profiling cases (--leg bvh_build | cache_mlp | frame | adjoint | nee, and --small)
+print their own timings, not a bench line.
 Under torchrun each rank renders an independent replica (the path does not
 shard: "replicas only"); value = all ranks' samples / max step time.
 """
@@ -70,12 +72,13 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--small", action="store_true",
                    help="same scene at 480x270, 4 spp: the profiling case (not a bench line)")
-    p.add_argument("--leg", choices=["bvh_build", "cache_mlp", "frame", "adjoint"],
+    p.add_argument("--leg", choices=["bvh_build", "cache_mlp", "frame", "adjoint", "nee"],
                    help="profiling case: only the GPU BVH builds of the workload's mesh, only the "
                         "radiance-cache MLP (2^18 queries), only frames of the workload (autotune: 8 "
                         "frames, then rebuild + render with the chosen closest-hit variant, 12 extend "
-                        "launches per frame), or only the adjoint calls of the adjoint leg; prints its "
-                        "timings, not a bench line")
+                        "launches per frame), only the adjoint calls of the adjoint leg, or only renders "
+                        "of the time-to-relMSE scene (Cornell 512x512, 128 spp, depth 8) without and with "
+                        "NEE; prints its timings, not a bench line")
     a = p.parse_args()
     if a.small:
         global W, H, SPP, WORKLOAD
@@ -231,6 +234,30 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------ GPU arm
+def nee_rate(M, ctx, n_warm=1, n_calls=2, w=512, h=512, spp=128, depth=8):
+    """Renders of the time-to-relMSE scene (seeded Cornell box, 512 x 512, 128
+    spp, depth 8) with the reference estimator and with NEE + MIS: per-kernel
+    device times of each call (the NEE shadow rays go through the persistent
+    any-hit traversal)."""
+    from mcrt_gb300 import scenes
+    sc = scenes.cornell_box(SEED)
+    c = sc["camera"]
+    cam = M.compute_camera(w, h, c["look_from"], c["look_at"], c["vfov"], 0.0)
+    ctx.upload_scene(vertices=sc["vertices"], triangles=sc["triangles"], materials=sc["materials"],
+                     env=M.gradient_env_map())
+    out = {"leg": "nee", "workload": f"cornell_box_seed{SEED}_{w}x{h}_{spp}spp_depth{depth}"}
+    for name, nee in (("plain", False), ("nee", True)):
+        calls = []
+        for i in range(n_warm + n_calls):
+            ctx.render(cam, w, h, spp, first_frame=i * spp, max_depth=depth, nee=nee, outputs=())
+            t = ctx.timings()
+            calls.append({k: round(t[k], 3) for k in ("extend_ms", "shade_ms", "shadow_ms", "total_ms")} |
+                         {"rays": t["rays"], "shadow_rays": t["shadow_rays"],
+                          "msamples_per_s": round(w * h * spp / t["total_ms"] / 1e3, 1)})
+        out[name] = calls[n_warm:]
+    return out
+
+
 def time_to_relmse(M, ctx, target=1e-3, w=512, h=512, depth=8, ref_spp=4096, max_spp=16384):
     """Seeded Cornell box at 512 x 512, depth 8: device time for the running
     estimate to reach relMSE <= target against a 4096-spp NEE reference (mean
@@ -477,6 +504,9 @@ def run_mcrt(args):
         return
     if args.leg == "adjoint":
         print(json.dumps(adjoint_rate(M, ctx, stream, n_warm=args.warmup, n_calls=args.steps)))
+        return
+    if args.leg == "nee":
+        print(json.dumps(nee_rate(M, ctx, n_warm=args.warmup, n_calls=args.steps)))
         return
     ctx.upload_scene(vertices=sc["vertices"], triangles=sc["triangles"], materials=sc["materials"], env=sc["env"])
     if args.leg == "bvh_build":
