@@ -47,7 +47,7 @@ struct PathBuffers {
     uint32_t n_slots = 0;
     float4 *thr = nullptr;       // throughput rgb | previous-bounce BSDF pdf (< 0: no MIS)
     float4 *L = nullptr;         // radiance rgb | unused
-    uint4 *aux = nullptr;        // rng | pixel | frame | flags
+    uint2 *aux = nullptr;        // rng | flags (pixel = slot / planes, frame = first frame + slot % planes)
     float4 *q_o[2] = {nullptr, nullptr};   // ray queues: origin | slot bits
     float4 *q_d[2] = {nullptr, nullptr};   // direction | unused
     float4 *hits = nullptr;      // t | prim bits | u | v, in queue order
@@ -66,6 +66,7 @@ struct AdjointParams {
     const float4 *dimg = nullptr;   // dLoss / d(image), per pixel (rgb)
     float inv_spp = 0.0f;           // 1 / samples per pixel of the call
     double *grad = nullptr;         // 64 material slots x (albedo r, g, b, roughness)
+    uint32_t planes = 1;            // sample planes of the pass: a slot's pixel is slot / planes
 };
 
 struct RenderParams {

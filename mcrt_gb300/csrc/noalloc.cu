@@ -99,7 +99,7 @@ extern "C" mcrt_status mcrt_render_noalloc(mcrt_ctx *ctx, const mcrt_camera_unif
     B.n_slots = (uint32_t)n_slots;
     B.thr = take(n_slots * 16);
     B.L = take(n_slots * 16);
-    B.aux = reinterpret_cast<uint4 *>(take(n_slots * 16));
+    B.aux = reinterpret_cast<uint2 *>(take(n_slots * 16));   // 8 B used per slot
     for (int k = 0; k < 2; ++k) {
         B.q_o[k] = take(n_slots * 16);
         B.q_d[k] = take(n_slots * 16);

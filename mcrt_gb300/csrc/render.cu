@@ -488,7 +488,7 @@ __global__ void k_raygen(DeviceScene S, RenderParams P, PathBuffers B, int keep_
     camera_ray(*cam, x, y, w, h, rng, &o, &d);
     B.thr[i] = make_float4(1.0f, 1.0f, 1.0f, -1.0f);
     if (!keep_radiance) B.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    B.aux[i] = make_uint4(rng, p, frame, kFlagSpecular);
+    B.aux[i] = make_uint2(rng, kFlagSpecular);
     B.q_o[0][i] = make_float4(o.x, o.y, o.z, __uint_as_float(i));
     B.q_d[0][i] = make_float4(d.x, d.y, d.z, 0.0f);
 }
@@ -739,7 +739,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
                             };
                             const uint32_t bits = __float_as_uint(c.w);
                             const uint32_t mi = bits & 0xffu, lm = (bits >> 8) & 0xffu;
-                            const float4 di = A.dimg[B.aux[slot].y];
+                            const float4 di = A.dimg[slot / A.planes];
                             const f3 dn = (A.inv_spp * xyz(di)) * xyz(c);
                             const float4 g = B.sh_g[ray];
                             gadd(4u * mi + 0, dn.x * g.x);
@@ -937,14 +937,15 @@ __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, Rende
             slot = __float_as_uint(o4.w);
             f3 o = xyz(o4), d = xyz(d4);
             float4 thr4 = B.thr[slot];
-            uint4 aux = B.aux[slot];
+            const uint2 aux = B.aux[slot];
+            const uint32_t pixel = slot / P.spp_pass;
             f3 thr = xyz(thr4);
             uint32_t rng = aux.x;
             f3 delta = {0.0f, 0.0f, 0.0f};
             if (ADJ) {
-                float4 di = A.dimg[aux.y];
+                float4 di = A.dimg[pixel];
                 delta = A.inv_spp * xyz(di);
-                const uint32_t pm = (aux.w >> 8) & 0xffu;
+                const uint32_t pm = (aux.y >> 8) & 0xffu;
                 if (pm) {                                   // BSDF term of the previous vertex
                     float4 L = B.L[slot], pd = B.pend[slot];
                     const uint32_t k0 = 4u * (pm - 1u);
@@ -957,7 +958,7 @@ __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, Rende
             }
             const bool write_g = gbuf && bounce == 0 && (int)(slot % P.spp_pass) == P.gbuf_plane;
             if (h.x < 0.0f) {                                                   // miss, :592-597
-                if (write_g) gbuf[aux.y] = make_float4(0.0f, 0.0f, 0.0f, kTMax);
+                if (write_g) gbuf[pixel] = make_float4(0.0f, 0.0f, 0.0f, kTMax);
                 if (!ADJ) {
                     f3 e = thr * sample_env(S, d);
                     float4 L = B.L[slot];
@@ -966,7 +967,7 @@ __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, Rende
                 }
             } else {
                 SurfaceHit sh = surface(S, o, d, h);
-                if (write_g) gbuf[aux.y] = make_float4(sh.n.x, sh.n.y, sh.n.z, sh.t);   // :599-602
+                if (write_g) gbuf[pixel] = make_float4(sh.n.x, sh.n.y, sh.n.z, sh.t);   // :599-602
                 const uint32_t mi = min(sh.mat, kMaxMatIdx);
                 const mcrt_gpu_material &m = S.materials->materials[mi];
                 const uint32_t mtype = m.type_pad[0];
@@ -975,7 +976,7 @@ __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, Rende
                     f3 e = m.ior_pad[0] * (thr * albedo);
                     float wmis = 1.0f;
                     if (nee) {
-                        if (!(aux.w & kFlagSpecular) && thr4.w > 0.0f && S.n_lights > 0) {
+                        if (!(aux.y & kFlagSpecular) && thr4.w > 0.0f && S.n_lights > 0) {
                             float pl = light_pdf_of_hit(S, h, o, d);
                             float pb = thr4.w;
                             wmis = (pb * pb) / (pb * pb + pl * pl);
@@ -1135,7 +1136,7 @@ __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, Rende
                         }
                         B.thr[slot] = make_float4(thr.x, thr.y, thr.z, pdf);
                     }
-                    B.aux[slot] = make_uint4(rng, aux.y, aux.z, (pdf > 0.0f ? 0u : kFlagSpecular) | pend_bits);
+                    B.aux[slot] = make_uint2(rng, (pdf > 0.0f ? 0u : kFlagSpecular) | pend_bits);
                 }
             }
         }
