@@ -299,8 +299,9 @@ mcrt_status finish_lights(mcrt_ctx *ctx) {
 // Path state for n_slots concurrent samples (structure of arrays in one allocation).
 mcrt_status ensure_path_buffers(mcrt_ctx *ctx, uint32_t n_slots) {
     if (ctx->pb.n_slots < n_slots) {
-        // thr L, q_o q_d x2, hits, sh o d c, pend sh_g (16 B each), aux (8 B, last: keeps the others aligned)
-        size_t per = 16 * 2 + 16 * 4 + 16 + 16 * 3 + 16 * 2 + 8;
+        // thr L, q_o q_d x2, hits, sh o d c, pend sh_g (16 B each), pend_mat (4 B, last: keeps the
+        // others aligned); a path's random state travels in its ray's direction w
+        size_t per = 16 * 2 + 16 * 4 + 16 + 16 * 3 + 16 * 2 + 4;
         CK(ctx->pbmem.ensure((size_t)n_slots * per + 256), "allocate path state");
         char *p = ctx->pbmem.as<char>();
         auto take = [&](size_t bytes) { char *r = p; p += bytes; return r; };
@@ -316,7 +317,7 @@ mcrt_status ensure_path_buffers(mcrt_ctx *ctx, uint32_t n_slots) {
         ctx->pb.sh_c = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
         ctx->pb.pend = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
         ctx->pb.sh_g = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
-        ctx->pb.aux = reinterpret_cast<uint2 *>(take((size_t)n_slots * 8));
+        ctx->pb.pend_mat = reinterpret_cast<uint32_t *>(take((size_t)n_slots * 4));
         ctx->pb.n_slots = n_slots;
     }
     CK(ctx->counters.ensure(256), "allocate counters");
@@ -721,7 +722,7 @@ static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, ui
     // launch's tail (the last, longest traversals, while most SMs idle) is a
     // small part of it — a 1080p frame of 16 spp traces 1.45x faster as one
     // pass of 16 sample planes than as 8 passes of 2, with the same result —
-    // with bounded memory (200 B of path state per slot: 6.7 GB at 2^25 slots)
+    // with bounded memory (196 B of path state per slot: 6.6 GB at 2^25 slots)
     const uint64_t kTargetSlots = 1ull << 25, kMaxSlots = 1ull << 25;
     uint32_t spp_pass = o.spp_per_pass;
     if (spp_pass == 0) spp_pass = (uint32_t)std::max<uint64_t>(1, (kTargetSlots + npix - 1) / npix);

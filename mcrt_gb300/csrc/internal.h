@@ -47,7 +47,6 @@ struct PathBuffers {
     uint32_t n_slots = 0;
     float4 *thr = nullptr;       // throughput rgb | previous-bounce BSDF pdf (< 0: no MIS)
     float4 *L = nullptr;         // radiance rgb | unused
-    uint2 *aux = nullptr;        // rng | flags (pixel = slot / planes, frame = first frame + slot % planes)
     float4 *q_o[2] = {nullptr, nullptr};   // ray queues: origin | slot bits
     float4 *q_d[2] = {nullptr, nullptr};   // direction | unused
     float4 *hits = nullptr;      // t | prim bits | u | v, in queue order
@@ -58,6 +57,7 @@ struct PathBuffers {
     unsigned long long *stats = nullptr;  // [0] rays traced, [1] shadow rays
     // adjoint replay only
     float4 *pend = nullptr;      // per slot: d log(BSDF weight) / d(albedo rgb | roughness) of the last vertex
+    uint32_t *pend_mat = nullptr;  // per slot: (material + 1) << 8 of that term, 0: none
     float4 *sh_g = nullptr;      // per shadow ray: d log(NEE term) / d(albedo rgb | roughness)
 };
 

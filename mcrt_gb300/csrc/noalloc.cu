@@ -33,7 +33,7 @@ namespace {
 constexpr size_t kNoAllocScratchBytes = 64ull << 20;
 constexpr uint32_t kNoAllocMaxPixels = 262144;          // e.g. 512 x 512
 constexpr size_t kCounterBytes = 256;
-constexpr size_t kSlotBytes = 16 * 11;                  // thr, L, aux, q_o x2, q_d x2, hits, sh_o, sh_d, sh_c
+constexpr size_t kSlotBytes = 16 * 11;                  // thr, L, pend_mat, q_o x2, q_d x2, hits, sh_o, sh_d, sh_c
 constexpr size_t kSumBytesPerPixel = 24;                // f64 rgb
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
@@ -99,7 +99,7 @@ extern "C" mcrt_status mcrt_render_noalloc(mcrt_ctx *ctx, const mcrt_camera_unif
     B.n_slots = (uint32_t)n_slots;
     B.thr = take(n_slots * 16);
     B.L = take(n_slots * 16);
-    B.aux = reinterpret_cast<uint2 *>(take(n_slots * 16));   // 8 B used per slot
+    B.pend_mat = reinterpret_cast<uint32_t *>(take(n_slots * 16));   // 4 B used per slot
     for (int k = 0; k < 2; ++k) {
         B.q_o[k] = take(n_slots * 16);
         B.q_d[k] = take(n_slots * 16);

@@ -19,7 +19,6 @@ namespace mcrt {
 namespace {
 
 constexpr uint32_t kMatMetal = 1u, kMatDielectric = 2u, kMatEmissive = 3u, kMatGgx = 4u;
-constexpr uint32_t kFlagSpecular = 1u;   // aux.w: last bounce had no MIS-able pdf
 
 inline int grid_blocks_for(uint32_t n, int threads) { return (int)((n + threads - 1) / threads); }
 
@@ -488,9 +487,10 @@ __global__ void k_raygen(DeviceScene S, RenderParams P, PathBuffers B, int keep_
     camera_ray(*cam, x, y, w, h, rng, &o, &d);
     B.thr[i] = make_float4(1.0f, 1.0f, 1.0f, -1.0f);
     if (!keep_radiance) B.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    B.aux[i] = make_uint2(rng, kFlagSpecular);
+    if (keep_radiance) B.pend_mat[i] = 0u;
+    // the path's random state travels with its ray (the direction's w)
     B.q_o[0][i] = make_float4(o.x, o.y, o.z, __uint_as_float(i));
-    B.q_d[0][i] = make_float4(d.x, d.y, d.z, 0.0f);
+    B.q_d[0][i] = make_float4(d.x, d.y, d.z, __uint_as_float(rng));
 }
 
 // Closest hit for the queued rays: persistent warps with dynamic ray refill and
@@ -897,7 +897,7 @@ __global__ void __launch_bounds__(kPacketBlock) k_extend_packet(DeviceScene S, P
 //   every term after the BSDF sample by Lrem * dlog(f cos / pdf)/dpi,
 // each weighted by delta = dLoss/dImage(pixel) / spp.  The last one needs Lrem
 // after this vertex's next-event term, which the shadow rays subtract after this
-// kernel: it is stored (B.pend, material in aux.w bits 8..15) and applied at
+// kernel: it is stored (B.pend, material in B.pend_mat bits 8..15) and applied at
 // the path's next vertex.  Gradients collect in shared memory per block, then
 // one double atomic per parameter and block.
 // Four resident blocks per SM (a 64-register budget) for the forward kernel:
@@ -927,6 +927,7 @@ __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, Rende
         float4 cq0, cq1, cq2, cq3;             // radiance-cache query of this path
         float smax = 0.0f;
         uint32_t slot = 0;
+        uint32_t rng_next = 0;                 // random state of the continuing ray
         uint32_t sh_bits = 0;                  // adjoint: material | light material << 8
         float4 sh_dlog = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (i < n) {
@@ -937,15 +938,14 @@ __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, Rende
             slot = __float_as_uint(o4.w);
             f3 o = xyz(o4), d = xyz(d4);
             float4 thr4 = B.thr[slot];
-            const uint2 aux = B.aux[slot];
             const uint32_t pixel = slot / P.spp_pass;
             f3 thr = xyz(thr4);
-            uint32_t rng = aux.x;
+            uint32_t rng = __float_as_uint(d4.w);
             f3 delta = {0.0f, 0.0f, 0.0f};
             if (ADJ) {
                 float4 di = A.dimg[pixel];
                 delta = A.inv_spp * xyz(di);
-                const uint32_t pm = (aux.y >> 8) & 0xffu;
+                const uint32_t pm = (B.pend_mat[slot] >> 8) & 0xffu;
                 if (pm) {                                   // BSDF term of the previous vertex
                     float4 L = B.L[slot], pd = B.pend[slot];
                     const uint32_t k0 = 4u * (pm - 1u);
@@ -976,7 +976,7 @@ __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, Rende
                     f3 e = m.ior_pad[0] * (thr * albedo);
                     float wmis = 1.0f;
                     if (nee) {
-                        if (!(aux.y & kFlagSpecular) && thr4.w > 0.0f && S.n_lights > 0) {
+                        if (thr4.w > 0.0f && S.n_lights > 0) {   // pdf <= 0: specular or camera
                             float pl = light_pdf_of_hit(S, h, o, d);
                             float pb = thr4.w;
                             wmis = (pb * pb) / (pb * pb + pl * pl);
@@ -1136,7 +1136,8 @@ __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, Rende
                         }
                         B.thr[slot] = make_float4(thr.x, thr.y, thr.z, pdf);
                     }
-                    B.aux[slot] = make_uint2(rng, (pdf > 0.0f ? 0u : kFlagSpecular) | pend_bits);
+                    if (ADJ) B.pend_mat[slot] = pend_bits;
+                    rng_next = rng;
                 }
             }
         }
@@ -1150,7 +1151,7 @@ __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, Rende
             if (cont) {
                 uint32_t pos = basepos + __popc(mask & ((1u << lane) - 1u));
                 __stcs(B.q_o[qi ^ 1] + pos, make_float4(no.x, no.y, no.z, __uint_as_float(slot)));
-                __stcs(B.q_d[qi ^ 1] + pos, make_float4(nd.x, nd.y, nd.z, 0.0f));
+                __stcs(B.q_d[qi ^ 1] + pos, make_float4(nd.x, nd.y, nd.z, __uint_as_float(rng_next)));
             }
         }
         unsigned smask = __ballot_sync(0xffffffffu, shadow);
