@@ -274,14 +274,14 @@ def time_to_relmse(M, ctx, target=1e-3, w=512, h=512, depth=8, ref_spp=4096, max
     ref /= ref_spp
     out = {"workload": f"cornell_box_seed{SEED}_{w}x{h}_depth{depth}", "target_relmse": target,
            "reference": f"NEE {ref_spp} spp, independent frames"}
-    cache_cfg = dict(query_vertex=2, train_stride=16, train_steps=4, train_batch=1 << 14, lr=1e-3)
+    cache_cfg = dict(query_vertex=2, train_stride=64, train_steps=8, train_batch=1 << 14, lr=1e-3)
     for name, nee, cache in (("plain", False, False), ("nee", True, False), ("cache", True, True)):
         total, ms, rel = 0, 0.0, None
         if cache:                                    # online training from scratch, timed
             ctx.cache_config(**cache_cfg)
             ctx.cache_init(0)
-            for i in range(40):
-                ctx.render(cam, w, h, 4, first_frame=(1 << 21) + 4 * i, max_depth=depth, nee=True, cache=True,
+            for i in range(5):
+                ctx.render(cam, w, h, 8, first_frame=(1 << 21) + 8 * i, max_depth=depth, nee=True, cache=True,
                            outputs=())
                 ms += ctx.timings()["total_ms"]
         while total < max_spp:
@@ -296,10 +296,12 @@ def time_to_relmse(M, ctx, target=1e-3, w=512, h=512, depth=8, ref_spp=4096, max
                 break
         out[name] = {"spp": total, "ms": round(ms, 2), "relmse": round(rel, 6), "reached": rel <= target,
                      "msamples_per_s": round(w * h * total / (ms / 1000.0) / 1e6, 1)}
-    out["cache"]["config"] = dict(cache_cfg, warmup="40 passes x 4 spp, in the time")
+    out["cache"]["config"] = dict(cache_cfg, warmup="5 passes x 8 spp, in the time")
     for name in ("nee", "cache"):
         if out["plain"]["reached"] and out[name]["reached"]:
             out[f"speedup_{name}_vs_plain"] = round(out["plain"]["ms"] / out[name]["ms"], 2)
+    if out["nee"]["reached"] and out["cache"]["reached"]:
+        out["speedup_cache_vs_nee"] = round(out["nee"]["ms"] / out["cache"]["ms"], 2)
     return out
 
 
@@ -434,7 +436,7 @@ def views_cache_relmse(M, ctx, target=1e-3, ref_spp=1024, max_spp=1024):
     ref = ctx.read_accum()[1].reshape(-1, 3) / ref_spp
     out = {"workload": f"voxel_world_16_views_seed{SEED}_{px / 1e6:.2f}Mpix_depth{depth}_sun_nee",
            "target_relmse": target, "reference": f"NEE {ref_spp} spp, independent frames"}
-    cache_cfg = dict(query_vertex=3, train_stride=16, train_steps=16, train_batch=1 << 14, lr=1e-3)
+    cache_cfg = dict(query_vertex=3, train_stride=256, train_steps=16, train_batch=1 << 14, lr=3e-3)
     for name, cache in (("nee", False), ("nee_cache", True)):
         total, ms, rel = 0, 0.0, None
         if cache:

@@ -354,7 +354,9 @@ uint32_t mcrt_cache_param_count(void);
  * cache's prediction there, with no next-event sample at that vertex.  After
  * the pass the training paths' vertices become samples (target = radiance the
  * path gathered from that vertex on / throughput at it) and `train_steps` Adam
- * steps of `train_batch` samples run.  lo / hi: the encoding bounds (hi <= lo
+ * steps of `train_batch` samples run; each step's batch is a stratified draw
+ * over all of the pass's samples (so over the whole image), and a stride that
+ * yields about train_steps x train_batch samples per pass wastes none.  lo / hi: the encoding bounds (hi <= lo
  * on every axis: the scene's bounding box). */
 typedef struct {
     uint32_t query_vertex;

@@ -622,6 +622,26 @@ __global__ void k_cache_targets(const float4 *rec, uint32_t n_train, uint32_t de
     }
 }
 
+// The batch of training step s of one pass, drawn from all n of the pass's
+// samples: entry k takes stratum j = k * steps + s of steps * batch equal
+// strata of [0, n), at a hashed offset inside the stratum.  The samples come in
+// slot order (pixel-major), so neighbouring samples are neighbouring pixels:
+// every step then sees the whole image, and successive passes (seeds) see
+// different samples of each stratum.
+__global__ void k_cache_gather(const float4 *src, uint32_t n, uint32_t steps, uint32_t s, uint32_t batch,
+                               uint32_t seed, float4 *dst) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= batch) return;
+    const uint64_t total = (uint64_t)steps * batch;
+    const uint64_t j = (uint64_t)k * steps + s;                             // < total
+    const uint64_t r24 = pcg_hash(k ^ pcg_hash(seed + s)) >> 8;             // [0, 2^24)
+    uint64_t idx = (j * n + ((r24 * n) >> 24)) / total;                     // < n
+    if (idx >= n) idx = n - 1;
+    const float4 *a = src + 4 * idx;
+    float4 *d = dst + 4 * (size_t)k;
+    d[0] = a[0]; d[1] = a[1]; d[2] = a[2]; d[3] = a[3];
+}
+
 // Synthetic queries (4 float4 each, slot = index) and training samples (16
 // floats) inside the encoding bounds, for the throughput measurement.
 __global__ void k_cache_synth(uint32_t n, NetDev net, float4 *q, float *samples) {
@@ -646,9 +666,10 @@ __global__ void k_cache_synth(uint32_t n, NetDev net, float4 *q, float *samples)
 
 // ---------------------------------------------------------------------------- cache state
 struct CacheState {
-    DBuf params, m, v, img, bias, grad, partial, loss_part, loss, samples, queries, status;
+    DBuf params, m, v, img, bias, grad, partial, loss_part, loss, samples, queries, status, batch;
     uint32_t n_cta_partial = 0;
     uint64_t step = 0;
+    uint32_t passes = 0;          // training passes from recorded paths (the batch draws' seed)
     float lo[3] = {0, 0, 0}, inv_ext[3] = {1, 1, 1};
     bool has_params = false;
     bool configured = false;
@@ -658,7 +679,7 @@ CacheState *cache_create() { return new CacheState(); }
 void cache_destroy(CacheState *c) {
     if (!c) return;
     DBuf *bufs[] = {&c->params, &c->m, &c->v, &c->img, &c->bias, &c->grad, &c->partial, &c->loss_part,
-                    &c->loss, &c->samples, &c->queries, &c->status};
+                    &c->loss, &c->samples, &c->queries, &c->status, &c->batch};
     for (DBuf *b : bufs) b->release();
     delete c;
 }
@@ -824,11 +845,14 @@ cudaError_t cache_train_records(CacheState *c, const float4 *rec, uint32_t n_tra
     if (n_samples_out) *n_samples_out = n;
     if (n == 0) return cudaSuccess;
     if (batch == 0 || batch > n) batch = n;
-    for (uint32_t s = 0; s < steps; ++s) {
-        const uint32_t first = (uint32_t)(((uint64_t)s * batch) % n);
-        const uint32_t cnt = std::min(batch, n - first);
-        if ((e = cache_step_device(c, c->samples.as<float>() + 16 * (size_t)first, cnt, cnt, lr, st)) != cudaSuccess)
-            return e;
+    if (steps == 0) return cudaSuccess;
+    if ((e = c->batch.ensure((size_t)batch * 64)) != cudaSuccess) return e;
+    const uint32_t seed = pcg_hash(++c->passes);
+    for (uint32_t s = 0; s < steps; ++s) {       // each step's batch spread over all samples of the pass
+        k_cache_gather<<<(batch + 255) / 256, 256, 0, st>>>(c->samples.as<float4>(), n, steps, s, batch, seed,
+                                                            c->batch.as<float4>());
+        note_launch();
+        if ((e = cache_step_device(c, c->batch.as<float>(), batch, batch, lr, st)) != cudaSuccess) return e;
     }
     return cudaSuccess;
 }
