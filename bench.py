@@ -54,9 +54,9 @@ sys.path.insert(0, ROOT)
 
 W, H, SPP, DEPTH, LEVEL, SEED = 1920, 1080, 16, 12, 8, 1234
 WORKLOAD = "displaced_icosphere_l8_1.31Mtri_1920x1080_16spp_depth12_gpu_rebuild"
-# DRAM bytes (read + write) per traced ray of the closest-hit kernel on this
-# workload, from one ncu capture of a frame's 12 launches (10.26 GB / 71.5 M rays)
-EXTEND_DRAM_BYTES_PER_RAY = 143.4
+# DRAM bytes (read + write) per traced ray of the closest-hit kernels on this
+# workload, from one ncu capture of a frame's 12 launches (9.97 GB / 71.5 M rays)
+EXTEND_DRAM_BYTES_PER_RAY = 139.4
 # the reference traversal's mean nodes visited / triangles tested per ray on the
 # reference BVH of this workload (oracle statistics over a sample of its paths),
 # used when a run skips the oracle sample (--no-cpu-baseline)
