@@ -436,7 +436,7 @@ def views_cache_relmse(M, ctx, target=1e-3, ref_spp=1024, max_spp=1024):
     ref = ctx.read_accum()[1].reshape(-1, 3) / ref_spp
     out = {"workload": f"voxel_world_16_views_seed{SEED}_{px / 1e6:.2f}Mpix_depth{depth}_sun_nee",
            "target_relmse": target, "reference": f"NEE {ref_spp} spp, independent frames"}
-    cache_cfg = dict(query_vertex=3, train_stride=256, train_steps=16, train_batch=1 << 14, lr=3e-3)
+    cache_cfg = dict(query_vertex=2, train_stride=256, train_steps=16, train_batch=1 << 14, lr=3e-3)
     for name, cache in (("nee", False), ("nee_cache", True)):
         total, ms, rel = 0, 0.0, None
         if cache:

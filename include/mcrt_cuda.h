@@ -350,10 +350,11 @@ uint32_t mcrt_cache_param_count(void);
  * `train_stride` slots is a training path: it is traced to full depth and
  * records each non-emissive vertex (position, w_o, normal, albedo, throughput,
  * radiance gathered so far); every other path stops at its non-emissive
- * vertex number `query_vertex` (0 = the primary hit) and adds throughput x the
- * cache's prediction there, with no next-event sample at that vertex.  After
- * the pass the training paths' vertices become samples (target = radiance the
- * path gathered from that vertex on / throughput at it) and `train_steps` Adam
+ * vertex number `query_vertex` (0 = the primary hit): it keeps that vertex's
+ * next-event sample and adds throughput x the cache's prediction in place of
+ * everything BSDF sampling would have gathered from there.  After the pass the
+ * training paths' vertices become samples (target = radiance the path gathered
+ * after that vertex's next-event sample / throughput at it) and `train_steps` Adam
  * steps of `train_batch` samples run; each step's batch is a stratified draw
  * over all of the pass's samples (so over the whole image), and a stride that
  * yields about train_steps x train_batch samples per pass wastes none.  lo / hi: the encoding bounds (hi <= lo

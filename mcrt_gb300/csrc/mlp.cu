@@ -586,8 +586,13 @@ __global__ void k_cache_refresh(const float *params, uint8_t *img, float *bias) 
 
 // Training samples from the recorded vertices of the training paths: for
 // recorded vertex j of training path t, query = (p, w_o, n, albedo) and target
-// = (L_final - L_j) / thr_j, the radiance the path gathered from vertex j on per
-// unit throughput; appended (warp-aggregated) when finite.
+// = (L_final - L_next) / thr_j, the radiance the path gathered after vertex j's
+// light sample, per unit throughput: L_next is the radiance recorded at the
+// path's next event (its next vertex, or the miss or emitter that ended it;
+// the shadow ray of vertex j is resolved before that event is shaded), or
+// L_final when the path ended at vertex j.  A path stopped into the cache at a
+// vertex keeps that vertex's light sample, so this is what the cache stands
+// for.  Appended (warp-aggregated) when finite.
 __global__ void k_cache_targets(const float4 *rec, uint32_t n_train, uint32_t depth, uint32_t stride,
                                 const float4 *L, float *samples, uint32_t *count) {
     const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -598,9 +603,11 @@ __global__ void k_cache_targets(const float4 *rec, uint32_t n_train, uint32_t de
         const float4 *r = rec + (size_t)idx * kTrainRecordFloat4;
         const float4 p = r[0];
         if (p.w > 0.0f) {
-            const float4 wo = r[1], nn = r[2], al = r[3], th = r[4], l0 = r[5];
+            const float4 wo = r[1], nn = r[2], al = r[3], th = r[4];
             const float4 lf = L[(size_t)(idx / depth) * stride];
-            const float tx = (lf.x - l0.x) / th.x, ty = (lf.y - l0.y) / th.y, tz = (lf.z - l0.z) / th.z;
+            float4 ln = lf;
+            if (idx % depth + 1 < depth && r[kTrainRecordFloat4].w != 0.0f) ln = r[kTrainRecordFloat4 + 5];
+            const float tx = (lf.x - ln.x) / th.x, ty = (lf.y - ln.y) / th.y, tz = (lf.z - ln.z) / th.z;
             ok = th.x > 0.0f && th.y > 0.0f && th.z > 0.0f && isfinite(tx) && isfinite(ty) && isfinite(tz);
             s[0] = p.x; s[1] = p.y; s[2] = p.z; s[3] = wo.x; s[4] = wo.y; s[5] = wo.z;
             s[6] = nn.x; s[7] = nn.y; s[8] = nn.z; s[9] = al.x; s[10] = al.y; s[11] = al.z;

@@ -903,6 +903,15 @@ __global__ void __launch_bounds__(kPacketBlock) k_extend_packet(DeviceScene S, P
 // Four resident blocks per SM (a 64-register budget) for the forward kernel:
 // it is bound by the latency of its scattered loads, and at the natural 88
 // registers only two blocks fit.  The replay variant keeps its registers.
+// Radiance-cache training path: the path ends at this bounce (a miss or an
+// emitter); record the radiance gathered before this event (which includes the
+// previous vertex's light sample) in place of a vertex.
+__device__ __forceinline__ void record_end(const RenderParams &P, uint32_t slot, uint32_t bounce, float4 L) {
+    float4 *rec = P.train_records + ((size_t)(slot / P.train_stride) * P.max_depth + bounce) * kTrainRecordFloat4;
+    rec[0] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+    rec[5] = make_float4(L.x, L.y, L.z, 0.0f);
+}
+
 template <bool ADJ>
 __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, RenderParams P, PathBuffers B, int qi,
                                                 uint32_t bounce, float4 *gbuf, AdjointParams A) {
@@ -961,6 +970,8 @@ __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, Rende
                 if (write_g) gbuf[pixel] = make_float4(0.0f, 0.0f, 0.0f, kTMax);
                 if (!ADJ) {
                     f3 e = thr * sample_env(S, d);
+                    if (P.cache_query_vertex && slot % P.train_stride == 0u)   // training path ends here
+                        record_end(P, slot, bounce, B.L[slot]);
                     float4 L = B.L[slot];
                     if (nee) B.L[slot] = make_float4(L.x + e.x, L.y + e.y, L.z + e.z, 0.0f);
                     else B.L[slot] = make_float4(e.x, e.y, e.z, 0.0f);
@@ -987,11 +998,15 @@ __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, Rende
                         gadd(4u * mi + 0, g.x);
                         gadd(4u * mi + 1, g.y);
                         gadd(4u * mi + 2, g.z);
-                    } else if (nee) {
-                        float4 L = B.L[slot];
-                        B.L[slot] = make_float4(L.x + wmis * e.x, L.y + wmis * e.y, L.z + wmis * e.z, 0.0f);
                     } else {
-                        B.L[slot] = make_float4(e.x, e.y, e.z, 0.0f);
+                        if (P.cache_query_vertex && slot % P.train_stride == 0u)   // training path ends here
+                            record_end(P, slot, bounce, B.L[slot]);
+                        if (nee) {
+                            float4 L = B.L[slot];
+                            B.L[slot] = make_float4(L.x + wmis * e.x, L.y + wmis * e.y, L.z + wmis * e.z, 0.0f);
+                        } else {
+                            B.L[slot] = make_float4(e.x, e.y, e.z, 0.0f);
+                        }
                     }
                 } else {
                     albedo = material_albedo(S, m, sh.p, h);                    // :506-515
@@ -1020,9 +1035,7 @@ __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, Rende
                             cq3 = make_float4(albedo.x, albedo.y, albedo.z, 0.0f);
                         }
                     }
-                    if (queried) {
-                        absorbed = true;
-                    } else if (mtype == kMatMetal) {                            // :530-541
+                    if (mtype == kMatMetal) {                                   // :530-541
                         float fuzz = m.albedo_fuzz[3];
                         f3 refl = reflect_vec(normalize(d), sh.n);
                         f3 pert = refl + fuzz * random_unit_sphere(rng);
@@ -1122,6 +1135,9 @@ __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, Rende
                             has_params = true;
                         }
                     }
+                    // a cache stop keeps this vertex's light sample (above) and ends
+                    // the path: the cache stands for what BSDF sampling would gather
+                    if (queried) absorbed = true;
                     uint32_t pend_bits = 0;
                     if (!absorbed) {
                         thr = thr * atten;

@@ -723,7 +723,8 @@ struct Deriv {
  * stats (optional): [0] rays traced, [1] nodes visited, [2] primitives tested.
  * lights: next-event estimation with MIS when non-null.  D: derivatives when non-null. */
 /* A path stopped into a radiance cache whose prediction is the constant c: at
- * its non-emissive vertex number `bounce` it adds thr * max(c, 0) and ends. */
+ * its non-emissive vertex number `bounce` it keeps that vertex's light sample
+ * (next-event estimation), then adds thr * max(c, 0) and ends. */
 struct CacheStop { uint32_t bounce; V3 c; };
 
 V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, float *gbuf, uint64_t *stats,
@@ -778,9 +779,6 @@ V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, f
             return nee ? Lacc + wmis * e : e;
         }
         albedo = material_albedo(sc, m, c, h.p);                               /* :506-515 */
-        if (stop && bounce == stop->bounce)
-            return Lacc + V3{thr.x * fmaxf(stop->c.x, 0.0f), thr.y * fmaxf(stop->c.y, 0.0f),
-                             thr.z * fmaxf(stop->c.z, 0.0f)};
         const V3 tex = D ? material_tex(sc, m, c, h.p) : V3{1.0f, 1.0f, 1.0f};
         const bool own = D && 4 * mi + 3 < np;
         V3 dir = {0, 0, 0}, atten = {0, 0, 0};
@@ -920,6 +918,9 @@ V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, f
                 }
             }
         }
+        if (stop && bounce == stop->bounce)
+            return Lacc + V3{thr.x * fmaxf(stop->c.x, 0.0f), thr.y * fmaxf(stop->c.y, 0.0f),
+                             thr.z * fmaxf(stop->c.z, 0.0f)};
         if (absorbed) return Lacc;
         if (D) {
             for (uint32_t p = 0; p < np; ++p)

@@ -103,8 +103,9 @@ void orc_render_ex(const orc_scene *scene, const orc_camera *cam, uint32_t w, ui
  * constant c3: frames are traced in passes of spp_pass (the last one shorter);
  * the sample of frame k, pixel p occupies slot p * planes + (k - pass start) of
  * its pass of `planes` frames; slots with slot % train_stride == 0 are traced in full,
- * the others add throughput * max(c, 0) at their vertex number query_vertex
- * (0 = primary hit) when it is not emissive, and end. */
+ * the others, at their vertex number query_vertex (0 = primary hit) when it is
+ * not emissive, keep that vertex's next-event sample, add throughput * max(c, 0)
+ * and end. */
 void orc_render_cache_const(const orc_scene *scene, const orc_camera *cam, uint32_t w, uint32_t h, uint32_t spp,
                             uint32_t first_frame, uint32_t max_depth, uint32_t flags, uint32_t spp_pass,
                             uint32_t train_stride, uint32_t query_vertex, const float *c3, float *out_mean_rgba,

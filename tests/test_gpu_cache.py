@@ -100,7 +100,8 @@ def test_cache_learns_a_radiance_field(cache_ctx):
 def test_cache_stop_bit_exact(ctx, oracle):
     """Paths stopped into a cache that predicts a constant: the render equals the
     oracle's, bit for bit (training paths traced in full, the others ending at
-    their second vertex with throughput x prediction)."""
+    their second vertex with that vertex's next-event sample and throughput x
+    prediction)."""
     from mcrt_gb300 import scenes
     sc = scenes.cornell_box(5)
     c = sc["camera"]
