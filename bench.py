@@ -296,6 +296,8 @@ def time_to_relmse(M, ctx, target=1e-3, w=512, h=512, depth=8, ref_spp=4096, max
                 break
         out[name] = {"spp": total, "ms": round(ms, 2), "relmse": round(rel, 6), "reached": rel <= target,
                      "msamples_per_s": round(w * h * total / (ms / 1000.0) / 1e6, 1)}
+        if cache:                                    # the bias judge's verdict on the last chunk
+            out[name]["judged_bias"] = [round(b, 4) for b in ctx.cache_stats()["bias"]]
     out["cache"]["config"] = dict(cache_cfg, warmup="5 passes x 8 spp, in the time")
     for name in ("nee", "cache"):
         if out["plain"]["reached"] and out[name]["reached"]:
@@ -457,6 +459,8 @@ def views_cache_relmse(M, ctx, target=1e-3, ref_spp=1024, max_spp=1024):
             if rel <= target:
                 break
         out[name] = {"spp": total, "ms": round(ms, 2), "relmse": round(rel, 6), "reached": rel <= target}
+        if cache:
+            out[name]["judged_bias"] = [round(b, 4) for b in ctx.cache_stats()["bias"]]
     out["nee_cache"]["config"] = dict(cache_cfg, warmup="20 passes x 2 spp over all views, in the time")
     if out["nee"]["reached"] and out["nee_cache"]["reached"]:
         out["speedup_cache_vs_nee"] = round(out["nee"]["ms"] / out["nee_cache"]["ms"], 3)

@@ -366,8 +366,23 @@ typedef struct {
     uint32_t train_batch;
     float lr;
     float lo[3], hi[3];
+    /* Fallback to the plain tracer: > 0 and the bias judge's last measurement
+     * (mcrt_cache_stats) above it in any channel: the next render stops no
+     * path into the cache (every path is traced in full, as without the cache)
+     * while training goes on; 0: the cache is always used. */
+    float max_bias;
 } mcrt_cache_params;
 mcrt_status mcrt_cache_config(mcrt_ctx *ctx, const mcrt_cache_params *params);
+
+/* The bias judge of the last render with MCRT_RENDER_CACHE: before each
+ * pass's training steps, the network (as that pass used it) is evaluated on
+ * the pass's training samples, whose targets are what the full-length training
+ * paths (the plain tracer) gathered.  out[0..2]: relative bias per channel,
+ * sum(max(prediction, 0) - target) / sum(target) over those samples (NaN when
+ * a sum of targets is 0); out[3]: samples judged; out[4]: 1 when that render
+ * stopped paths into the cache, 0 when it ran as the plain tracer (max_bias
+ * fallback).  No reference counterpart (the reference has no radiance cache). */
+mcrt_status mcrt_cache_stats(mcrt_ctx *ctx, double *out5);
 
 /* Device time (CUDA events) of cache inference over n synthetic queries and of
  * one training step on n synthetic samples, averaged over reps:

@@ -17,7 +17,7 @@ reference's interfaces for the path:
 from __future__ import annotations
 
 import ctypes
-from ctypes import c_float, c_uint32, c_uint64, c_void_p
+from ctypes import c_double, c_float, c_uint32, c_uint64, c_void_p
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -366,14 +366,23 @@ class Context:
 
     # ---------------------------------------------------------------- radiance cache
     def cache_config(self, query_vertex=1, train_stride=64, train_steps=4, train_batch=1 << 14, lr=1e-3, lo=None,
-                     hi=None):
-        """Rendering with the cache (render(..., cache=True)); lo / hi None: the scene's bounds."""
+                     hi=None, max_bias=0.0):
+        """Rendering with the cache (render(..., cache=True)); lo / hi None: the scene's bounds.
+        max_bias > 0: render as the plain tracer (training on) while the judged bias exceeds it."""
         p = N.CacheParams(query_vertex=query_vertex, train_stride=train_stride, train_steps=train_steps,
-                          train_batch=train_batch, lr=lr)
+                          train_batch=train_batch, lr=lr, max_bias=max_bias)
         if lo is not None:
             for k in range(3):
                 p.lo[k], p.hi[k] = float(lo[k]), float(hi[k])
         self._check(lib().mcrt_cache_config(self._h, ctypes.byref(p)))
+
+    def cache_stats(self):
+        """The bias judge of the last cached render: relative bias per channel
+        (sum of prediction - target over sum of target, on the training paths'
+        samples), samples judged, and whether paths stopped into the cache."""
+        out = (c_double * 5)()
+        self._check(lib().mcrt_cache_stats(self._h, out))
+        return {"bias": [out[0], out[1], out[2]], "samples": int(out[3]), "stopped": bool(out[4])}
 
     def cache_bench(self, n=1 << 20, reps=10):
         """(inference ms, training-step ms) on n synthetic queries / samples (device time)."""

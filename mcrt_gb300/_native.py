@@ -68,7 +68,8 @@ class SceneDesc(ctypes.Structure):
 
 class CacheParams(ctypes.Structure):
     _fields_ = [("query_vertex", c_uint32), ("train_stride", c_uint32), ("train_steps", c_uint32),
-                ("train_batch", c_uint32), ("lr", c_float), ("lo", c_float * 3), ("hi", c_float * 3)]
+                ("train_batch", c_uint32), ("lr", c_float), ("lo", c_float * 3), ("hi", c_float * 3),
+                ("max_bias", c_float)]
 
 
 RENDER_CACHE = 16
@@ -127,6 +128,7 @@ SIGNATURES = [
     ("mcrt_mlp_gemm_probe", c_int, [c_int, c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_void_p]),
     ("mcrt_cache_param_count", c_uint32, []),
     ("mcrt_cache_config", c_int, [c_void_p, POINTER(CacheParams)]),
+    ("mcrt_cache_stats", c_int, [c_void_p, c_void_p]),
     ("mcrt_cache_bench", c_int, [c_void_p, c_uint32, c_uint32, c_void_p]),
     ("mcrt_cache_init", c_int, [c_void_p, c_uint32]),
     ("mcrt_cache_set_params", c_int, [c_void_p, c_void_p]),

@@ -101,6 +101,9 @@ struct mcrt_ctx {
     mcrt::CacheState *cache = nullptr;
     mcrt_cache_params cache_cfg{};
     bool cache_cfg_set = false;
+    // bias judge of the last cached render: relative bias rgb, samples, stopped
+    double cache_stats[5] = {NAN, NAN, NAN, 0.0, 0.0};
+    bool cache_fallback = false;   // the judge's last bias exceeds cache_cfg.max_bias
     DBuf cache_q, cache_rec;
     uint32_t last_train_samples = 0;
 };
@@ -787,10 +790,14 @@ static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, ui
     if (use_cache && !ctx->cache_cfg_set) return fail(ctx, MCRT_ERR_INVALID_ARG, "radiance cache not configured");
     const bool use_graph = (o.flags & MCRT_RENDER_GRAPH) != 0 && !use_cache;
     const uint32_t train_stride = use_cache ? ctx->cache_cfg.train_stride : 1u;
+    // fallback to the plain tracer while the judged bias is too large: no path
+    // stops (no vertex index matches), the training paths still record
+    const bool cache_stops = use_cache && !ctx->cache_fallback;
     if (use_cache) {
         const size_t n_train = (n_slots + train_stride - 1) / train_stride;
         CK(ctx->cache_q.ensure((size_t)n_slots * 64), "allocate cache queries");
         CK(ctx->cache_rec.ensure(n_train * depth * mcrt::kTrainRecordFloat4 * 16), "allocate training records");
+        CK(mcrt::cache_judge_reset(ctx->cache, st), "bias judge");
     }
     ctx->last_train_samples = 0;
     auto make_params = [&](uint32_t planes, uint32_t frame0) {
@@ -811,7 +818,7 @@ static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, ui
             P.view_cam = reinterpret_cast<const mcrt_camera_uniform *>(ctx->views.as<char>() + off_cam);
         }
         if (use_cache) {
-            P.cache_query_vertex = ctx->cache_cfg.query_vertex + 1;
+            P.cache_query_vertex = cache_stops ? ctx->cache_cfg.query_vertex + 1 : 0xffffffffu;
             P.train_stride = train_stride;
             P.cache_queries = ctx->cache_q.as<float4>();
             P.train_records = ctx->cache_rec.as<float4>();
@@ -931,6 +938,18 @@ static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, ui
     CK(cudaGetLastError(), "render launch");
     CK(cudaEventSynchronize(e_end), "render");
     if (cache_status != MCRT_OK) return cache_status;
+    if (use_cache) {                               // the judge's verdict on this render's passes
+        double j[8];
+        CK(mcrt::cache_judge_read(ctx->cache, j, st), "bias judge");
+        bool over = false;
+        for (int c = 0; c < 3; ++c) {
+            ctx->cache_stats[c] = j[3 + c] > 0.0 ? j[c] / j[3 + c] : NAN;
+            over = over || !(std::fabs(ctx->cache_stats[c]) <= (double)ctx->cache_cfg.max_bias);
+        }
+        ctx->cache_stats[3] = j[6];
+        ctx->cache_stats[4] = cache_stops ? 1.0 : 0.0;
+        if (j[6] > 0.0) ctx->cache_fallback = ctx->cache_cfg.max_bias > 0.0f && over;
+    }
     ctx->last_render_launches = mcrt::launch_count() - launches0;
     ctx->last_extend_launches = extend_launches;
     ctx->acc_valid = true;
@@ -1417,6 +1436,7 @@ mcrt_status mcrt_cache_config(mcrt_ctx *ctx, const mcrt_cache_params *p) {
     if (p->train_stride == 0) return fail(ctx, MCRT_ERR_INVALID_ARG, "train_stride must be >= 1");
     if (!(p->lr >= 0.0f) || !std::isfinite(p->lr)) return fail(ctx, MCRT_ERR_INVALID_ARG, "lr must be >= 0");
     if (p->query_vertex > 1023) return fail(ctx, MCRT_ERR_INVALID_ARG, "query_vertex too large");
+    if (!(p->max_bias >= 0.0f)) return fail(ctx, MCRT_ERR_INVALID_ARG, "max_bias must be >= 0");
     float lo[3], hi[3];
     bool given = true;
     for (int a = 0; a < 3; ++a) {
@@ -1451,10 +1471,18 @@ mcrt_status mcrt_cache_config(mcrt_ctx *ctx, const mcrt_cache_params *p) {
     ctx->cache_cfg = *p;
     for (int a = 0; a < 3; ++a) { ctx->cache_cfg.lo[a] = lo[a]; ctx->cache_cfg.hi[a] = hi[a]; }
     ctx->cache_cfg_set = true;
+    ctx->cache_fallback = false;
     if (!mcrt::cache_ready(ctx->cache)) {
         mcrt_status s = mcrt_cache_init(ctx, 0);
         if (s != MCRT_OK) return s;
     }
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_cache_stats(mcrt_ctx *ctx, double *out5) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!out5) return fail(ctx, MCRT_ERR_INVALID_ARG, "out5 is NULL");
+    for (int k = 0; k < 5; ++k) out5[k] = ctx->cache_stats[k];
     return MCRT_OK;
 }
 

@@ -175,6 +175,10 @@ cudaError_t cache_train_records(CacheState *c, const float4 *rec, uint32_t n_tra
                                 const float4 *L, uint32_t steps, uint32_t batch, float lr, cudaStream_t st,
                                 uint32_t *n_samples_out);
 bool cache_ready(const CacheState *c);
+// Bias judge of the training passes (cache_train_records): clear the sums, and
+// read them ([0..2] sum of prediction - target, [3..5] sum of target, [6] samples).
+cudaError_t cache_judge_reset(CacheState *c, cudaStream_t st);
+cudaError_t cache_judge_read(CacheState *c, double out[8], cudaStream_t st);
 cudaError_t cache_bench(CacheState *c, uint32_t n, uint32_t reps, float *ms_infer, float *ms_train, cudaStream_t st);
 
 // Denoiser (denoise.cu)

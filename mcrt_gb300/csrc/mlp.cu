@@ -649,6 +649,43 @@ __global__ void k_cache_gather(const float4 *src, uint32_t n, uint32_t steps, ui
     d[0] = a[0]; d[1] = a[1]; d[2] = a[2]; d[3] = a[3];
 }
 
+// The bias judge: the training samples of a pass as inference queries (4
+// float4 each: p | index, w_o, n, albedo), so the network can be compared with
+// the radiance the full-length training paths actually gathered.
+__global__ void k_cache_judge_queries(const float4 *s, uint32_t n, float4 *q) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 a = s[4 * (size_t)i], b = s[4 * (size_t)i + 1], c = s[4 * (size_t)i + 2];
+    q[4 * (size_t)i] = make_float4(a.x, a.y, a.z, __uint_as_float(i));
+    q[4 * (size_t)i + 1] = make_float4(a.w, b.x, b.y, 0.0f);
+    q[4 * (size_t)i + 2] = make_float4(b.z, b.w, c.x, 0.0f);
+    q[4 * (size_t)i + 3] = make_float4(c.y, c.z, c.w, 0.0f);
+}
+
+// acc[0..2] += sum of (max(y, 0) - target), acc[3..5] += sum of target, per
+// channel over the weighted samples; acc[6] += their number.  Sums of
+// differences, not of ratios: their quotient is the cache's relative bias on
+// the radiance it stands for, and the per-sample noise of the targets averages
+// out of the numerator.
+__global__ void k_cache_judge(const float4 *s, const float *y, uint32_t n, double *acc) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float v[7] = {0, 0, 0, 0, 0, 0, 0};
+    if (i < n) {
+        const float4 t = s[4 * (size_t)i + 3];
+        if (t.w > 0.0f) {
+            v[0] = fmaxf(y[3 * (size_t)i], 0.0f) - t.x;
+            v[1] = fmaxf(y[3 * (size_t)i + 1], 0.0f) - t.y;
+            v[2] = fmaxf(y[3 * (size_t)i + 2], 0.0f) - t.z;
+            v[3] = t.x; v[4] = t.y; v[5] = t.z; v[6] = 1.0f;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+        const float w = warp_sum(v[k]);
+        if ((threadIdx.x & 31u) == 0u && w != 0.0f) atomicAdd(acc + k, (double)w);
+    }
+}
+
 // Synthetic queries (4 float4 each, slot = index) and training samples (16
 // floats) inside the encoding bounds, for the throughput measurement.
 __global__ void k_cache_synth(uint32_t n, NetDev net, float4 *q, float *samples) {
@@ -673,7 +710,7 @@ __global__ void k_cache_synth(uint32_t n, NetDev net, float4 *q, float *samples)
 
 // ---------------------------------------------------------------------------- cache state
 struct CacheState {
-    DBuf params, m, v, img, bias, grad, partial, loss_part, loss, samples, queries, status, batch;
+    DBuf params, m, v, img, bias, grad, partial, loss_part, loss, samples, queries, status, batch, judge;
     uint32_t n_cta_partial = 0;
     uint64_t step = 0;
     uint32_t passes = 0;          // training passes from recorded paths (the batch draws' seed)
@@ -686,7 +723,7 @@ CacheState *cache_create() { return new CacheState(); }
 void cache_destroy(CacheState *c) {
     if (!c) return;
     DBuf *bufs[] = {&c->params, &c->m, &c->v, &c->img, &c->bias, &c->grad, &c->partial, &c->loss_part,
-                    &c->loss, &c->samples, &c->queries, &c->status, &c->batch};
+                    &c->loss, &c->samples, &c->queries, &c->status, &c->batch, &c->judge};
     for (DBuf *b : bufs) b->release();
     delete c;
 }
@@ -851,6 +888,16 @@ cudaError_t cache_train_records(CacheState *c, const float4 *rec, uint32_t n_tra
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
     if (n_samples_out) *n_samples_out = n;
     if (n == 0) return cudaSuccess;
+    if (c->judge.p) {                              // judge the network on this pass's samples before training
+        if ((e = c->queries.ensure((size_t)n * 64 + (size_t)n * 12)) != cudaSuccess) return e;
+        float4 *q = c->queries.as<float4>();
+        float *y = reinterpret_cast<float *>(c->queries.as<char>() + (size_t)n * 64);
+        k_cache_judge_queries<<<(n + 255) / 256, 256, 0, st>>>(c->samples.as<float4>(), n, q);
+        note_launch();
+        if ((e = cache_infer_device(c, q, nullptr, n, y, nullptr, nullptr, st)) != cudaSuccess) return e;
+        k_cache_judge<<<(n + 255) / 256, 256, 0, st>>>(c->samples.as<float4>(), y, n, c->judge.as<double>());
+        note_launch();
+    }
     if (batch == 0 || batch > n) batch = n;
     if (steps == 0) return cudaSuccess;
     if ((e = c->batch.ensure((size_t)batch * 64)) != cudaSuccess) return e;
@@ -865,6 +912,20 @@ cudaError_t cache_train_records(CacheState *c, const float4 *rec, uint32_t n_tra
 }
 
 bool cache_ready(const CacheState *c) { return c && c->has_params; }
+
+cudaError_t cache_judge_reset(CacheState *c, cudaStream_t st) {
+    cudaError_t e = c->judge.ensure(8 * sizeof(double));
+    if (e != cudaSuccess) return e;
+    return cudaMemsetAsync(c->judge.p, 0, 8 * sizeof(double), st);
+}
+
+cudaError_t cache_judge_read(CacheState *c, double out[8], cudaStream_t st) {
+    for (int k = 0; k < 8; ++k) out[k] = 0.0;
+    if (!c->judge.p) return cudaSuccess;
+    cudaError_t e = cudaMemcpyAsync(out, c->judge.p, 8 * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(st);
+}
 
 // Device time of inference over n synthetic queries and of one training step
 // (gradients, reduction, Adam) on n synthetic samples, averaged over reps.

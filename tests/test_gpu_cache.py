@@ -152,3 +152,38 @@ def test_trained_cache_gains_over_untrained_and_plain(ctx):
     print("relMSE plain", plain, "untrained cache", untrained, "trained cache", trained)
     assert trained < untrained / 3
     assert trained < plain / 3
+
+
+def test_cache_bias_judge_and_fallback(ctx):
+    """The bias judge compares the cache with what the plain tracer's training
+    paths gathered.  A cache that predicts far too much light is judged biased;
+    with max_bias set, the next render falls back to the plain tracer (bit for
+    bit the render without the cache) while the judge keeps measuring.  An
+    online-trained cache is judged close to unbiased and stops paths again."""
+    from mcrt_gb300 import scenes
+    sc = scenes.cornell_box(1234)
+    c = sc["camera"]
+    W = H = 64
+    cam = M.compute_camera(W, H, c["look_from"], c["look_at"], c["vfov"], 0.0)
+    ctx.upload_scene(vertices=sc["vertices"], triangles=sc["triangles"], materials=sc["materials"],
+                     env=M.gradient_env_map())
+    ctx.cache_config(query_vertex=1, train_stride=4, train_steps=0, lr=0.0, max_bias=0.25)
+    p = np.zeros(ctx.cache_params().size, np.float32)
+    p[-16:-13] = 20.0                               # output bias: a constant far above the scene's radiance
+    ctx.cache_set_params(p)
+    ctx.render(cam, W, H, 8, max_depth=8, nee=True, cache=True, outputs=())
+    judged = ctx.cache_stats()
+    assert judged["stopped"] and judged["samples"] > 1000 and min(judged["bias"]) > 1.0, judged
+    r = ctx.render(cam, W, H, 8, first_frame=8, max_depth=8, nee=True, cache=True, outputs=("sum",))
+    fallback = ctx.cache_stats()
+    assert not fallback["stopped"] and min(fallback["bias"]) > 1.0, fallback
+    plain = ctx.render(cam, W, H, 8, first_frame=8, max_depth=8, nee=True, outputs=("sum",))
+    assert np.array_equal(r["sum"].view(np.uint64), plain["sum"].view(np.uint64))
+
+    ctx.cache_config(query_vertex=1, train_stride=16, train_steps=8, lr=1e-3, max_bias=0.25)
+    ctx.cache_init(1)
+    for i in range(40):
+        ctx.render(cam, W, H, 16, first_frame=1000 + 16 * i, max_depth=8, nee=True, cache=True, outputs=())
+    trained = ctx.cache_stats()
+    print("judged bias: constant cache", judged["bias"], "trained cache", trained["bias"])
+    assert trained["stopped"] and max(abs(b) for b in trained["bias"]) < 0.25, trained
