@@ -421,9 +421,10 @@ def views_cache_relmse(M, ctx, target=1e-3, ref_spp=1024, max_spp=1024):
     voxel world (left uploaded by voxel_world_rate), depth 6, sun NEE + sky.
     Device time for the views' estimates (f64 sums / samples) to reach relMSE
     <= target (over every pixel of every view) against a ref_spp NEE
-    reference, for the tracer without the cache (passes replayed as a CUDA
-    graph) and with the online-trained cache (warm-up and training inside the
-    time); each estimator stops at max_spp.  The reference is 1024 spp rather
+    reference, for the tracer without the cache and with the online-trained
+    cache (warm-up and training inside the time), both replaying their passes
+    as CUDA graphs (the cached passes with their training); each estimator
+    stops at max_spp.  The reference is 1024 spp rather
     than 4096 to keep the leg within about a minute (12 Mpix); its own noise
     then adds about 1/4 of the target to the relMSE the tracer without the
     cache reaches, equally for both estimators."""
@@ -446,12 +447,12 @@ def views_cache_relmse(M, ctx, target=1e-3, ref_spp=1024, max_spp=1024):
             ctx.cache_init(0)
             for i in range(20):
                 ctx.render_views(views, 2, first_frame=(1 << 21) + 2 * i, max_depth=depth, nee=True, cache=True,
-                                 read_back=False)
+                                 graph=True, read_back=False)
                 ms += ctx.timings()["total_ms"]
         while total < max_spp:
             chunk = max(8, total // 8)
             ctx.render_views(views, chunk, first_frame=total, max_depth=depth, nee=True, keep=total > 0,
-                             cache=cache, graph=not cache, read_back=False)
+                             cache=cache, graph=True, read_back=False)
             ms += ctx.timings()["total_ms"]
             total += chunk
             x = ctx.read_accum()[1].reshape(-1, 3) / total

@@ -194,7 +194,8 @@ enum {
     MCRT_RENDER_GRAPH = 1u << 3,      /* replay the passes as one captured CUDA graph (same results; no
                                          per-kernel timings for the replayed passes) */
     MCRT_RENDER_CACHE = 1u << 4       /* terminate paths into the radiance cache and train it online
-                                         (mcrt_cache_config); not replayed as a graph */
+                                         (mcrt_cache_config); with MCRT_RENDER_GRAPH the cached passes,
+                                         training included, are replayed as a graph too */
 };
 
 typedef struct {

@@ -788,7 +788,7 @@ static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, ui
     const bool nee = (o.flags & MCRT_RENDER_NEE) != 0 && (ctx->n_lights > 0 || ctx->has_sun);
     const bool use_cache = (o.flags & MCRT_RENDER_CACHE) != 0;
     if (use_cache && !ctx->cache_cfg_set) return fail(ctx, MCRT_ERR_INVALID_ARG, "radiance cache not configured");
-    const bool use_graph = (o.flags & MCRT_RENDER_GRAPH) != 0 && !use_cache;
+    const bool use_graph = (o.flags & MCRT_RENDER_GRAPH) != 0;
     const uint32_t train_stride = use_cache ? ctx->cache_cfg.train_stride : 1u;
     // fallback to the plain tracer while the judged bias is too large: no path
     // stops (no vertex index matches), the training paths still record
@@ -797,6 +797,8 @@ static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, ui
         const size_t n_train = (n_slots + train_stride - 1) / train_stride;
         CK(ctx->cache_q.ensure((size_t)n_slots * 64), "allocate cache queries");
         CK(ctx->cache_rec.ensure(n_train * depth * mcrt::kTrainRecordFloat4 * 16), "allocate training records");
+        // every buffer of a pass's training is allocated here, not in the passes (which a graph may capture)
+        CK(mcrt::cache_prepare(ctx->cache, n_train * depth, ctx->cache_cfg.train_batch), "cache buffers");
         CK(mcrt::cache_judge_reset(ctx->cache, st), "bias judge");
     }
     ctx->last_train_samples = 0;
@@ -868,12 +870,10 @@ static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, ui
         if (use_cache && cache_status == MCRT_OK) {   // train on this pass's training paths
             const mcrt_cache_params &c = ctx->cache_cfg;
             const uint32_t n_train = (P.npix * P.spp_pass + train_stride - 1) / train_stride;
-            uint32_t ns = 0;
             cudaError_t e = mcrt::cache_train_records(ctx->cache, ctx->cache_rec.as<float4>(), n_train, depth,
                                                       train_stride, ctx->pb.L, c.train_steps, c.train_batch, c.lr,
-                                                      st, &ns);
+                                                      st);
             if (e != cudaSuccess) cache_status = cuda_fail(ctx, e, "cache training");
-            ctx->last_train_samples += ns;
         }
     };
     uint32_t done = 0;
@@ -888,7 +888,15 @@ static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, ui
         P.gbuf_plane = want_gbuf ? (int)spp_pass - 1 : -1;
         P.pass_state = ctx->pass_state.as<uint32_t>();
         // configuration key: everything the captured launches bake in
-        std::vector<char> key(sizeof(S) + sizeof(P) + sizeof(mcrt::PathBuffers) + 3 * sizeof(void *) + 8);
+        // (with the cache: its settings and buffers, which the captured training bakes in)
+        const void *cbufs[12] = {};
+        mcrt_cache_params ccfg{};
+        if (use_cache) {
+            mcrt::cache_buffer_ptrs(ctx->cache, cbufs);
+            ccfg = ctx->cache_cfg;
+        }
+        std::vector<char> key(sizeof(S) + sizeof(P) + sizeof(mcrt::PathBuffers) + 3 * sizeof(void *) + 8 +
+                              sizeof(cbufs) + sizeof(ccfg));
         {
             char *k = key.data();
             std::memcpy(k, &S, sizeof(S)); k += sizeof(S);
@@ -897,7 +905,9 @@ static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, ui
             void *bufs[3] = {ctx->mean.p, ctx->sum.p, ctx->gbuf.p};
             std::memcpy(k, bufs, sizeof(bufs)); k += sizeof(bufs);
             uint32_t extra[2] = {depth, nee ? 1u : 0u};
-            std::memcpy(k, extra, sizeof(extra));
+            std::memcpy(k, extra, sizeof(extra)); k += sizeof(extra);
+            std::memcpy(k, cbufs, sizeof(cbufs)); k += sizeof(cbufs);
+            std::memcpy(k, &ccfg, sizeof(ccfg));
         }
         if (!ctx->graph_exec || ctx->graph_key != key) {
             if (ctx->graph_exec) { cudaGraphExecDestroy(ctx->graph_exec); ctx->graph_exec = nullptr; }
@@ -948,6 +958,7 @@ static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, ui
         }
         ctx->cache_stats[3] = j[6];
         ctx->cache_stats[4] = cache_stops ? 1.0 : 0.0;
+        ctx->last_train_samples = (uint32_t)std::min(j[6], 4294967295.0);
         if (j[6] > 0.0) ctx->cache_fallback = ctx->cache_cfg.max_bias > 0.0f && over;
     }
     ctx->last_render_launches = mcrt::launch_count() - launches0;

@@ -170,10 +170,12 @@ cudaError_t cache_infer_device(CacheState *c, const float4 *q, const uint32_t *d
                                float4 *L, const float4 *thr, cudaStream_t st);
 cudaError_t cache_step_device(CacheState *c, const float *d_samples, uint32_t n, uint32_t n_valid, float lr,
                               cudaStream_t st);
-// Samples from the training paths' records (L: final path radiance per slot), then `steps` Adam steps.
+// Samples from the training paths' records (L: final path radiance per slot), the bias judge, then
+// `steps` Adam steps; no host round trip (capturable once cache_prepare has run for the capacity).
 cudaError_t cache_train_records(CacheState *c, const float4 *rec, uint32_t n_train, uint32_t depth, uint32_t stride,
-                                const float4 *L, uint32_t steps, uint32_t batch, float lr, cudaStream_t st,
-                                uint32_t *n_samples_out);
+                                const float4 *L, uint32_t steps, uint32_t batch, float lr, cudaStream_t st);
+cudaError_t cache_prepare(CacheState *c, size_t cap, uint32_t batch);
+void cache_buffer_ptrs(const CacheState *c, const void *out[12]);
 bool cache_ready(const CacheState *c);
 // Bias judge of the training passes (cache_train_records): clear the sums, and
 // read them ([0..2] sum of prediction - target, [3..5] sum of target, [6] samples).

@@ -526,7 +526,7 @@ __global__ void __launch_bounds__(128, 1) k_cache_train(NetDev net, TrainIO io, 
 
 // grad[p] = sum over CTAs of partial[cta][p], in CTA order.
 __global__ void k_cache_reduce(const float *partial, uint32_t n_cta, const float *loss_part, float *grad,
-                               float *loss_out) {
+                               float *loss_out, uint32_t *adam_step) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p < (uint32_t)kParams) {
         float s = 0.0f;
@@ -537,6 +537,7 @@ __global__ void k_cache_reduce(const float *partial, uint32_t n_cta, const float
         float s = 0.0f;
         for (uint32_t c = 0; c < n_cta; ++c) s += loss_part[c];
         *loss_out = s;
+        if (adam_step) *adam_step += 1u;           // the Adam step that follows (kept on the device)
     }
 }
 
@@ -554,9 +555,11 @@ __device__ __forceinline__ void param_where(uint32_t p, int *layer, bool *is_bia
 // Adam (Kingma & Ba 2015) on the fp32 parameters; refreshes the bf16 weight
 // image and the bias copy the kernels read.
 __global__ void k_cache_adam(float *params, float *m, float *v, const float *grad, float lr, float beta1, float beta2,
-                             float eps, float bc1, float bc2, uint8_t *img, float *bias) {
+                             float eps, const uint32_t *adam_step, uint8_t *img, float *bias) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= (uint32_t)kParams) return;
+    const float t = (float)*adam_step;                 // bias corrections of step t
+    const float bc1 = 1.0f - powf(beta1, t), bc2 = 1.0f - powf(beta2, t);
     const float g = grad[p];
     const float mi = beta1 * m[p] + (1.0f - beta1) * g;
     const float vi = beta2 * v[p] + (1.0f - beta2) * (g * g);
@@ -635,10 +638,15 @@ __global__ void k_cache_targets(const float4 *rec, uint32_t n_train, uint32_t de
 // slot order (pixel-major), so neighbouring samples are neighbouring pixels:
 // every step then sees the whole image, and successive passes (seeds) see
 // different samples of each stratum.
-__global__ void k_cache_gather(const float4 *src, uint32_t n, uint32_t steps, uint32_t s, uint32_t batch,
+__global__ void k_cache_gather(const float4 *src, const uint32_t *count, uint32_t steps, uint32_t s, uint32_t batch,
                                uint32_t seed, float4 *dst) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= batch) return;
+    const uint32_t n = *count;
+    if (n == 0) {                                                           // no sample: zero weights
+        for (int c = 0; c < 4; ++c) dst[4 * (size_t)k + c] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return;
+    }
     const uint64_t total = (uint64_t)steps * batch;
     const uint64_t j = (uint64_t)k * steps + s;                             // < total
     const uint64_t r24 = pcg_hash(k ^ pcg_hash(seed + s)) >> 8;             // [0, 2^24)
@@ -652,9 +660,9 @@ __global__ void k_cache_gather(const float4 *src, uint32_t n, uint32_t steps, ui
 // The bias judge: the training samples of a pass as inference queries (4
 // float4 each: p | index, w_o, n, albedo), so the network can be compared with
 // the radiance the full-length training paths actually gathered.
-__global__ void k_cache_judge_queries(const float4 *s, uint32_t n, float4 *q) {
+__global__ void k_cache_judge_queries(const float4 *s, const uint32_t *count, float4 *q) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= *count) return;
     const float4 a = s[4 * (size_t)i], b = s[4 * (size_t)i + 1], c = s[4 * (size_t)i + 2];
     q[4 * (size_t)i] = make_float4(a.x, a.y, a.z, __uint_as_float(i));
     q[4 * (size_t)i + 1] = make_float4(a.w, b.x, b.y, 0.0f);
@@ -667,8 +675,9 @@ __global__ void k_cache_judge_queries(const float4 *s, uint32_t n, float4 *q) {
 // differences, not of ratios: their quotient is the cache's relative bias on
 // the radiance it stands for, and the per-sample noise of the targets averages
 // out of the numerator.
-__global__ void k_cache_judge(const float4 *s, const float *y, uint32_t n, double *acc) {
+__global__ void k_cache_judge(const float4 *s, const float *y, const uint32_t *count, double *acc) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = *count;
     float v[7] = {0, 0, 0, 0, 0, 0, 0};
     if (i < n) {
         const float4 t = s[4 * (size_t)i + 3];
@@ -711,8 +720,8 @@ __global__ void k_cache_synth(uint32_t n, NetDev net, float4 *q, float *samples)
 // ---------------------------------------------------------------------------- cache state
 struct CacheState {
     DBuf params, m, v, img, bias, grad, partial, loss_part, loss, samples, queries, status, batch, judge;
+    DBuf adam_step;               // device Adam step counter (advanced by k_cache_reduce)
     uint32_t n_cta_partial = 0;
-    uint64_t step = 0;
     uint32_t passes = 0;          // training passes from recorded paths (the batch draws' seed)
     float lo[3] = {0, 0, 0}, inv_ext[3] = {1, 1, 1};
     bool has_params = false;
@@ -723,7 +732,8 @@ CacheState *cache_create() { return new CacheState(); }
 void cache_destroy(CacheState *c) {
     if (!c) return;
     DBuf *bufs[] = {&c->params, &c->m, &c->v, &c->img, &c->bias, &c->grad, &c->partial, &c->loss_part,
-                    &c->loss, &c->samples, &c->queries, &c->status, &c->batch, &c->judge};
+                    &c->loss, &c->samples, &c->queries, &c->status, &c->batch, &c->judge,
+                    &c->adam_step};
     for (DBuf *b : bufs) b->release();
     delete c;
 }
@@ -767,7 +777,8 @@ cudaError_t cache_set_params(CacheState *c, const float *host, cudaStream_t st) 
     k_cache_refresh<<<(kParams + 255) / 256, 256, 0, st>>>(c->params.as<float>(), c->img.as<uint8_t>(),
                                                           c->bias.as<float>());
     note_launch();
-    c->step = 0;
+    if ((e = c->adam_step.ensure(16)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(c->adam_step.p, 0, 16, st)) != cudaSuccess) return e;
     c->has_params = true;
     return cudaGetLastError();
 }
@@ -790,13 +801,16 @@ static cudaError_t check_status(CacheState *c, cudaStream_t st, bool *timed_out)
 
 // Inference over device queries (4 float4 each); either out (host layout) or
 // the tracer's L / thr.
+// Shared-memory attributes of the two tensor-core kernels, set once (before
+// any capture: cache_prepare sets them too).
+static bool g_infer_attr = false, g_train_attr = false;
+
 cudaError_t cache_infer_device(CacheState *c, const float4 *q, const uint32_t *d_count, uint32_t max_n, float *out,
                                float4 *L, const float4 *thr, cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) {
+    if (!g_infer_attr) {
         cudaError_t e = cudaFuncSetAttribute(k_cache_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem);
         if (e != cudaSuccess) return e;
-        attr = true;
+        g_infer_attr = true;
     }
     if (max_n == 0) return cudaSuccess;
     InferIO io{q, d_count, max_n, L, thr, out};
@@ -837,13 +851,12 @@ cudaError_t cache_infer_host(CacheState *c, const float *q12, uint32_t n, float 
 // c->grad (and the loss into c->loss), then Adam when lr > 0.
 cudaError_t cache_step_device(CacheState *c, const float *d_samples, uint32_t n, uint32_t n_valid, float lr,
                               cudaStream_t st) {
-    static bool attr = false;
     cudaError_t e;
-    if (!attr) {
+    if (!g_train_attr) {
         if ((e = cudaFuncSetAttribute(k_cache_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem)) !=
             cudaSuccess)
             return e;
-        attr = true;
+        g_train_attr = true;
     }
     const uint32_t tiles = (n + kTile - 1) / kTile;
     const uint32_t blocks = std::max(1u, std::min<uint32_t>(tiles, (uint32_t)sm_count()));
@@ -853,60 +866,88 @@ cudaError_t cache_step_device(CacheState *c, const float *d_samples, uint32_t n,
                c->loss_part.as<float>()};
     k_cache_train<<<blocks, 128, kTrainSmem, st>>>(net_of(c), io, c->status.as<uint32_t>());
     note_launch();
+    uint32_t *adam_step = lr > 0.0f ? c->adam_step.as<uint32_t>() : nullptr;
     k_cache_reduce<<<(kParams + 255) / 256, 256, 0, st>>>(c->partial.as<float>(), blocks, c->loss_part.as<float>(),
-                                                          c->grad.as<float>(), c->loss.as<float>());
+                                                          c->grad.as<float>(), c->loss.as<float>(), adam_step);
     note_launch();
-    if (lr > 0.0f) {
-        ++c->step;
-        const float b1 = 0.9f, b2 = 0.99f;
-        const float bc1 = 1.0f - (float)std::pow((double)b1, (double)c->step);
-        const float bc2 = 1.0f - (float)std::pow((double)b2, (double)c->step);
+    if (adam_step) {
         k_cache_adam<<<(kParams + 255) / 256, 256, 0, st>>>(c->params.as<float>(), c->m.as<float>(), c->v.as<float>(),
-                                                            c->grad.as<float>(), lr, b1, b2, 1e-8f, bc1, bc2,
+                                                            c->grad.as<float>(), lr, 0.9f, 0.99f, 1e-8f, adam_step,
                                                             c->img.as<uint8_t>(), c->bias.as<float>());
         note_launch();
     }
     return cudaGetLastError();
 }
 
-cudaError_t cache_train_records(CacheState *c, const float4 *rec, uint32_t n_train, uint32_t depth, uint32_t stride,
-                                const float4 *L, uint32_t steps, uint32_t batch, float lr, cudaStream_t st,
-                                uint32_t *n_samples_out) {
+// Everything a render pass's training (cache_train_records) and inference
+// allocate or configure, for up to `cap` samples and batches of `batch`: done
+// before the passes, so that a pass allocates nothing and can be captured.
+cudaError_t cache_prepare(CacheState *c, size_t cap, uint32_t batch) {
     if (!c->has_params) return cudaErrorInvalidValue;
     cudaError_t e;
-    const size_t cap = (size_t)n_train * depth;
+    if (!g_infer_attr) {
+        if ((e = cudaFuncSetAttribute(k_cache_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem)) !=
+            cudaSuccess)
+            return e;
+        g_infer_attr = true;
+    }
+    if (!g_train_attr) {
+        if ((e = cudaFuncSetAttribute(k_cache_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem)) !=
+            cudaSuccess)
+            return e;
+        g_train_attr = true;
+    }
     if ((e = c->samples.ensure(cap * 64 + 64)) != cudaSuccess) return e;
+    if ((e = c->queries.ensure(cap * 64 + cap * 12)) != cudaSuccess) return e;
+    const uint32_t b = batch ? (uint32_t)std::min<size_t>(batch, std::max<size_t>(cap, 1)) : (uint32_t)std::max<size_t>(cap, 1);
+    if ((e = c->batch.ensure((size_t)b * 64)) != cudaSuccess) return e;
+    const uint32_t blocks = std::max(1u, std::min<uint32_t>((b + kTile - 1) / kTile, (uint32_t)sm_count()));
+    if ((e = c->partial.ensure((size_t)blocks * kParams * 4)) != cudaSuccess) return e;
+    if ((e = c->loss_part.ensure((size_t)blocks * 4)) != cudaSuccess) return e;
+    return c->judge.ensure(8 * sizeof(double));
+}
+
+// Device pointers of the cache's buffers (the identity of a captured pass).
+void cache_buffer_ptrs(const CacheState *c, const void *out[12]) {
+    const DBuf *b[12] = {&c->params, &c->m, &c->v, &c->img, &c->bias, &c->grad, &c->partial, &c->loss_part,
+                         &c->samples, &c->queries, &c->batch, &c->judge};
+    for (int k = 0; k < 12; ++k) out[k] = b[k]->p;
+}
+
+// One pass's training, with no host round trip: the sample count stays on the
+// device (the judge, the batch draws and the inference read it there), so the
+// pass can be replayed from a CUDA graph.  A batch of `batch` samples (0: the
+// capacity) is drawn per step; with fewer samples than that, samples repeat.
+cudaError_t cache_train_records(CacheState *c, const float4 *rec, uint32_t n_train, uint32_t depth, uint32_t stride,
+                                const float4 *L, uint32_t steps, uint32_t batch, float lr, cudaStream_t st) {
+    if (!c->has_params) return cudaErrorInvalidValue;
+    const size_t cap = (size_t)n_train * depth;
+    if (cap == 0) return cudaSuccess;
+    if (cap > 0xffffffffu) return cudaErrorInvalidValue;
+    cudaError_t e;
+    if ((e = cache_prepare(c, cap, batch)) != cudaSuccess) return e;    // no-op when prepared
     uint32_t *count = reinterpret_cast<uint32_t *>(c->samples.as<char>() + cap * 64);
     if ((e = cudaMemsetAsync(count, 0, 4, st)) != cudaSuccess) return e;
-    if (cap) {
-        k_cache_targets<<<(uint32_t)((cap + 255) / 256), 256, 0, st>>>(rec, n_train, depth, stride, L,
-                                                                      c->samples.as<float>(), count);
-        note_launch();
-    }
-    uint32_t n = 0;
-    if ((e = cudaMemcpyAsync(&n, count, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
-    if (n_samples_out) *n_samples_out = n;
-    if (n == 0) return cudaSuccess;
+    const uint32_t grid = (uint32_t)((cap + 255) / 256);
+    k_cache_targets<<<grid, 256, 0, st>>>(rec, n_train, depth, stride, L, c->samples.as<float>(), count);
+    note_launch();
     if (c->judge.p) {                              // judge the network on this pass's samples before training
-        if ((e = c->queries.ensure((size_t)n * 64 + (size_t)n * 12)) != cudaSuccess) return e;
         float4 *q = c->queries.as<float4>();
-        float *y = reinterpret_cast<float *>(c->queries.as<char>() + (size_t)n * 64);
-        k_cache_judge_queries<<<(n + 255) / 256, 256, 0, st>>>(c->samples.as<float4>(), n, q);
+        float *y = reinterpret_cast<float *>(c->queries.as<char>() + cap * 64);
+        k_cache_judge_queries<<<grid, 256, 0, st>>>(c->samples.as<float4>(), count, q);
         note_launch();
-        if ((e = cache_infer_device(c, q, nullptr, n, y, nullptr, nullptr, st)) != cudaSuccess) return e;
-        k_cache_judge<<<(n + 255) / 256, 256, 0, st>>>(c->samples.as<float4>(), y, n, c->judge.as<double>());
+        if ((e = cache_infer_device(c, q, count, (uint32_t)cap, y, nullptr, nullptr, st)) != cudaSuccess) return e;
+        k_cache_judge<<<grid, 256, 0, st>>>(c->samples.as<float4>(), y, count, c->judge.as<double>());
         note_launch();
     }
-    if (batch == 0 || batch > n) batch = n;
     if (steps == 0) return cudaSuccess;
-    if ((e = c->batch.ensure((size_t)batch * 64)) != cudaSuccess) return e;
+    const uint32_t b = batch ? (uint32_t)std::min<size_t>(batch, cap) : (uint32_t)cap;
     const uint32_t seed = pcg_hash(++c->passes);
     for (uint32_t s = 0; s < steps; ++s) {       // each step's batch spread over all samples of the pass
-        k_cache_gather<<<(batch + 255) / 256, 256, 0, st>>>(c->samples.as<float4>(), n, steps, s, batch, seed,
-                                                            c->batch.as<float4>());
+        k_cache_gather<<<(b + 255) / 256, 256, 0, st>>>(c->samples.as<float4>(), count, steps, s, b, seed,
+                                                        c->batch.as<float4>());
         note_launch();
-        if ((e = cache_step_device(c, c->batch.as<float>(), batch, batch, lr, st)) != cudaSuccess) return e;
+        if ((e = cache_step_device(c, c->batch.as<float>(), b, b, lr, st)) != cudaSuccess) return e;
     }
     return cudaSuccess;
 }

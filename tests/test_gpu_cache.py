@@ -187,3 +187,34 @@ def test_cache_bias_judge_and_fallback(ctx):
     trained = ctx.cache_stats()
     print("judged bias: constant cache", judged["bias"], "trained cache", trained["bias"])
     assert trained["stopped"] and max(abs(b) for b in trained["bias"]) < 0.25, trained
+
+
+def test_cached_passes_replay_as_a_graph(ctx):
+    """Cached passes have no host round trip, so MCRT_RENDER_GRAPH replays them
+    (training included).  With a learning rate of 0 the network stays fixed
+    while the training kernels run, and the graph replay equals the pass-by-pass
+    render bit for bit; with training on, the graph-replayed cache learns (the
+    judge finds it close to unbiased)."""
+    from mcrt_gb300 import scenes
+    sc = scenes.cornell_box(1234)
+    c = sc["camera"]
+    W = H = 64
+    cam = M.compute_camera(W, H, c["look_from"], c["look_at"], c["vfov"], 0.0)
+    ctx.upload_scene(vertices=sc["vertices"], triangles=sc["triangles"], materials=sc["materials"],
+                     env=M.gradient_env_map())
+    ctx.cache_config(query_vertex=1, train_stride=8, train_steps=2, lr=0.0)
+    ctx.cache_init(3)
+    sums = []
+    for graph in (False, True, True):
+        r = ctx.render(cam, W, H, 6, first_frame=40, max_depth=8, nee=True, spp_per_pass=2, cache=True,
+                       graph=graph, outputs=("sum",))
+        sums.append(r["sum"].view(np.uint64))
+    assert np.array_equal(sums[0], sums[1]) and np.array_equal(sums[0], sums[2])
+    ctx.cache_config(query_vertex=1, train_stride=16, train_steps=8, lr=1e-3)
+    ctx.cache_init(1)
+    for i in range(40):
+        ctx.render(cam, W, H, 16, first_frame=1000 + 16 * i, max_depth=8, nee=True, spp_per_pass=4, cache=True,
+                   graph=True, outputs=())
+    st = ctx.cache_stats()
+    print("graph-trained cache: judged bias", st["bias"])
+    assert st["samples"] > 0 and max(abs(b) for b in st["bias"]) < 0.25, st
