@@ -445,7 +445,7 @@ def views_cache_relmse(M, ctx, target=1e-3, ref_spp=1024, max_spp=1024):
         if cache:
             ctx.cache_config(**cache_cfg)
             ctx.cache_init(0)
-            for i in range(20):
+            for i in range(10):
                 ctx.render_views(views, 2, first_frame=(1 << 21) + 2 * i, max_depth=depth, nee=True, cache=True,
                                  graph=True, read_back=False)
                 ms += ctx.timings()["total_ms"]
@@ -462,7 +462,7 @@ def views_cache_relmse(M, ctx, target=1e-3, ref_spp=1024, max_spp=1024):
         out[name] = {"spp": total, "ms": round(ms, 2), "relmse": round(rel, 6), "reached": rel <= target}
         if cache:
             out[name]["judged_bias"] = [round(b, 4) for b in ctx.cache_stats()["bias"]]
-    out["nee_cache"]["config"] = dict(cache_cfg, warmup="20 passes x 2 spp over all views, in the time")
+    out["nee_cache"]["config"] = dict(cache_cfg, warmup="10 passes x 2 spp over all views, in the time")
     if out["nee"]["reached"] and out["nee_cache"]["reached"]:
         out["speedup_cache_vs_nee"] = round(out["nee"]["ms"] / out["nee_cache"]["ms"], 3)
     return out
