@@ -41,7 +41,8 @@ enum {
     MCRT_ERR_OOM = -2,
     MCRT_ERR_CUDA = -3,
     MCRT_ERR_TIMEOUT = -4,          /* a bounded device loop ran out */
-    MCRT_ERR_STACK_OVERFLOW = -5,   /* a traversal stack bound was reached */
+    MCRT_ERR_STACK_OVERFLOW = -5,   /* reserved: no call returns it (a ray whose traversal stack would
+                                       overflow is traced again without a stack) */
     MCRT_ERR_NO_SCENE = -6,
     MCRT_ERR_PARSE = -7,            /* SceneError::Parse, scene.rs:603 */
     MCRT_ERR_IO = -8,               /* SceneError::Io, scene.rs:601 */
@@ -209,9 +210,10 @@ typedef struct {
  * closest-hit kernel variant — BVH width (compact binary / quantised 4-wide),
  * block size, register budget (minimum resident blocks) and traversal stack
  * depth, see mcrt_variant_info — keeps the fastest for this context and
- * reports it.  A variant whose stack overflows on this scene is not a
- * candidate (its time is reported as -1).  out_ms (optional) receives the
- * extend time of every variant; its capacity is 8 floats. */
+ * reports it.  Every variant gives the same images: a ray whose stack would
+ * overflow is traced again without a stack, which costs its variant time on
+ * a deep tree but never a hit.  out_ms (optional) receives the extend time of
+ * every variant; its capacity is 8 floats. */
 /* out5: BVH width, block size, minimum resident blocks per SM, stack depth,
  * idle lanes at which a warp fetches new rays */
 mcrt_status mcrt_variant_info(uint32_t variant, uint32_t *out5);
@@ -259,7 +261,13 @@ mcrt_status mcrt_render_views(mcrt_ctx *ctx, const mcrt_view *views, uint32_t n_
  *     f32 running mean of frames first_frame .. first_frame+spp-1 (alpha 1), as
  *     out_rgba of mcrt_render.
  *   - w*h must not exceed 262144 pixels (MCRT_ERR_INVALID_ARG otherwise);
- *     KEEP_ACCUM is not supported; no G-buffer is produced.
+ *     KEEP_ACCUM, GBUFFER and CACHE are rejected (MCRT_ERR_INVALID_ARG);
+ *     GRAPH is ignored (the passes launch directly, with the same result).
+ *   - The closest-hit kernel is the context's autotuned variant (or
+ *     opts->variant); a 4-wide variant whose quantised tree has not been built
+ *     since the last BVH build (by an mcrt_render with a 4-wide variant) is
+ *     replaced by the binary variant 0, with the same image.
+ *   - The caller's current device is restored on return.
  *   - The scene is the one of an earlier mcrt_upload_scene on ctx.
  *   - All calls share the one array: calls that overlap on the GPU (other
  *     threads, streams or contexts on the same device) race; serialise them.
@@ -450,7 +458,9 @@ mcrt_status mcrt_read_image_rgba8(mcrt_ctx *ctx, uint32_t mode, uint8_t *out);
  * stream: [0] total, [1] trace (extend), [2] shade, [3] shadow rays, [4] resolve,
  * [5] BVH build (ms); counters: [0] rays traced, [1] shadow rays, [2] kernel
  * launches of the last render, [3] kernel launches of the last BVH build,
- * [4] extend launches of the last render.  out_ms: 6 floats, out_counts: 5 uint64. */
+ * [4] extend launches of the last render, [5] rays of the last render traced
+ * by the stackless walk because the traversal stack was too short for the
+ * tree (included in [0] and [1]).  out_ms: 6 floats, out_counts: 6 uint64. */
 mcrt_status mcrt_last_timings(mcrt_ctx *ctx, float *out_ms, uint64_t *out_counts);
 
 /* ------------------------------------------------------------------ denoiser */

@@ -75,7 +75,7 @@ struct mcrt_ctx {
     // timing
     std::vector<cudaEvent_t> ev_pool;
     float last_ms[6] = {0, 0, 0, 0, 0, 0};
-    unsigned long long last_counts[2] = {0, 0};
+    unsigned long long last_counts[3] = {0, 0, 0};   // rays, shadow rays, rays traced stackless
     unsigned long long last_render_launches = 0, last_build_launches = 0, last_extend_launches = 0;
     float last_build_ms = 0.0f;
     int extend_variant = 0;   // chosen by mcrt_autotune
@@ -302,9 +302,10 @@ mcrt_status finish_lights(mcrt_ctx *ctx) {
 // Path state for n_slots concurrent samples (structure of arrays in one allocation).
 mcrt_status ensure_path_buffers(mcrt_ctx *ctx, uint32_t n_slots) {
     if (ctx->pb.n_slots < n_slots) {
-        // thr L, q_o q_d x2, hits, sh o d c, pend sh_g (16 B each), pend_mat (4 B, last: keeps the
-        // others aligned); a path's random state travels in its ray's direction w
-        size_t per = 16 * 2 + 16 * 4 + 16 + 16 * 3 + 16 * 2 + 4;
+        // thr L, q_o q_d x2, hits, sh o d c, pend sh_g (16 B each), pend_mat and the overflow
+        // list (4 B each, last: keeps the others aligned); a path's random state travels in its
+        // ray's direction w
+        size_t per = 16 * 2 + 16 * 4 + 16 + 16 * 3 + 16 * 2 + 4 + 4;
         CK(ctx->pbmem.ensure((size_t)n_slots * per + 256), "allocate path state");
         char *p = ctx->pbmem.as<char>();
         auto take = [&](size_t bytes) { char *r = p; p += bytes; return r; };
@@ -321,6 +322,7 @@ mcrt_status ensure_path_buffers(mcrt_ctx *ctx, uint32_t n_slots) {
         ctx->pb.pend = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
         ctx->pb.sh_g = reinterpret_cast<float4 *>(take((size_t)n_slots * 16));
         ctx->pb.pend_mat = reinterpret_cast<uint32_t *>(take((size_t)n_slots * 4));
+        ctx->pb.ovf = reinterpret_cast<uint32_t *>(take((size_t)n_slots * 4));
         ctx->pb.n_slots = n_slots;
     }
     CK(ctx->counters.ensure(256), "allocate counters");
@@ -667,18 +669,13 @@ mcrt_status mcrt_trace_closest(mcrt_ctx *ctx, const mcrt_ray *rays, uint32_t n, 
     cudaStream_t st = ctx->stream;
     CK(ctx->io_a.ensure((size_t)n * 32), "allocate rays");
     CK(ctx->io_b.ensure((size_t)n * 16), "allocate hits");
-    CK(ctx->counters.ensure(64), "allocate counters");
     CK(cudaMemcpyAsync(ctx->io_a.p, rays, (size_t)n * 32, cudaMemcpyHostToDevice, st), "upload rays");
-    CK(cudaMemsetAsync(ctx->counters.p, 0, 64, st), "clear");
     mcrt::DeviceScene S = device_scene(ctx);
     mcrt::launch_trace_closest(S, ctx->io_a.as<mcrt_ray>(), n, ctx->io_b.as<mcrt_hit>(),
-                               (flags & MCRT_TRACE_REFERENCE_LAYOUT) != 0, ctx->counters.as<uint32_t>(), st);
+                               (flags & MCRT_TRACE_REFERENCE_LAYOUT) != 0, st);
     CK(cudaGetLastError(), "trace launch");
-    uint32_t overflow = 0;
     CK(cudaMemcpyAsync(hits, ctx->io_b.p, (size_t)n * 16, cudaMemcpyDeviceToHost, st), "read hits");
-    CK(cudaMemcpyAsync(&overflow, ctx->counters.p, 4, cudaMemcpyDeviceToHost, st), "read flag");
     CK(cudaStreamSynchronize(st), "trace");
-    if (overflow) return fail(ctx, MCRT_ERR_STACK_OVERFLOW, "traversal stack bound reached");
     return MCRT_OK;
 }
 
@@ -974,10 +971,8 @@ static mcrt_status render_core(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, ui
         ms[m.second] += t;
     }
     std::memcpy(ctx->last_ms, ms, sizeof(ms));
-    uint32_t ctr[4];
-    CK(cudaMemcpy(ctr, ctx->counters.p, 16, cudaMemcpyDeviceToHost), "read counters");
-    CK(cudaMemcpy(ctx->last_counts, ctx->pb.stats, 16, cudaMemcpyDeviceToHost), "read counters");
-    if (ctr[3]) return fail(ctx, MCRT_ERR_STACK_OVERFLOW, "traversal stack bound reached");
+    CK(cudaMemcpy(ctx->last_counts, ctx->pb.stats, sizeof(ctx->last_counts), cudaMemcpyDeviceToHost),
+       "read counters");
     return MCRT_OK;
 }
 
@@ -1134,10 +1129,8 @@ mcrt_status mcrt_adjoint(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t
     float ms[6] = {0, 0, 0, 0, 0, ctx->last_build_ms};
     cudaEventElapsedTime(&ms[0], e_begin, e_end);
     std::memcpy(ctx->last_ms, ms, sizeof(ms));
-    uint32_t ctr[4];
-    CK(cudaMemcpy(ctr, ctx->counters.p, 16, cudaMemcpyDeviceToHost), "read counters");
-    CK(cudaMemcpy(ctx->last_counts, ctx->pb.stats, 16, cudaMemcpyDeviceToHost), "read counters");
-    if (ctr[3]) return fail(ctx, MCRT_ERR_STACK_OVERFLOW, "traversal stack bound reached");
+    CK(cudaMemcpy(ctx->last_counts, ctx->pb.stats, sizeof(ctx->last_counts), cudaMemcpyDeviceToHost),
+       "read counters");
     CK(cudaMemcpy(grad, ctx->grad.p, 256 * sizeof(double), cudaMemcpyDeviceToHost), "read gradient");
     if (out_rgba)
         CK(cudaMemcpy(out_rgba, ctx->mean.p, (size_t)npix * 16, cudaMemcpyDeviceToHost), "read image");
@@ -1279,17 +1272,14 @@ mcrt_status mcrt_autotune(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_
     for (int v = 0; v < nv; ++v) {
         o.variant = (uint32_t)v + 1;
         float t = 0.0f;
-        bool ok = true;
-        for (int rep = 0; rep < 2 && ok; ++rep) {     // the first run warms caches and occupancy queries
+        for (int rep = 0; rep < 2; ++rep) {           // the first run warms caches and occupancy queries
             mcrt_status s = mcrt_render(ctx, cam, w, h, spp, 0, &o, nullptr, nullptr, nullptr);
-            if (s == MCRT_ERR_STACK_OVERFLOW) ok = false;   // stack too short for this scene: not a candidate
-            else if (s != MCRT_OK) return s;
-            t = ctx->last_ms[1];
+            if (s != MCRT_OK) return s;
+            t = ctx->last_ms[1];                      // extend time, stackless retries of a short stack included
         }
-        if (out_ms && v < 8) out_ms[v] = ok ? t : -1.0f;
-        if (ok && (best_v < 0 || t < best)) { best = t; best_v = v; }
+        if (out_ms && v < 8) out_ms[v] = t;
+        if (best_v < 0 || t < best) { best = t; best_v = v; }
     }
-    if (best_v < 0) return fail(ctx, MCRT_ERR_STACK_OVERFLOW, "every closest-hit variant overflowed its stack");
     ctx->extend_variant = best_v;
     if (out_variant) *out_variant = (uint32_t)best_v;
     return MCRT_OK;
@@ -1322,6 +1312,7 @@ mcrt_status mcrt_last_timings(mcrt_ctx *ctx, float *out_ms, uint64_t *out_counts
         out_counts[2] = ctx->last_render_launches;
         out_counts[3] = ctx->last_build_launches;
         out_counts[4] = ctx->last_extend_launches;
+        out_counts[5] = ctx->last_counts[2];
     }
     return MCRT_OK;
 }
@@ -1557,6 +1548,20 @@ mcrt_status mcrt_denoise_accum(mcrt_ctx *ctx, const mcrt_denoise_params *params,
 namespace mcrt {
 // The device scene and stream of a context, for entry points defined in other
 // translation units.  *err receives the context's error string.
+// The closest-hit variant of a render on ctx (opts variant k + 1, else the
+// context's autotuned one) when the layout it reads is ready without
+// allocating: a 4-wide variant whose quantised tree has not been built since
+// the last BVH build gives the binary variant 0 (the same images).  -1: the
+// requested variant is out of range.
+int context_variant(mcrt_ctx *ctx, const mcrt_render_opts &o) {
+    const int v = o.variant ? (int)o.variant - 1 : ctx->extend_variant;
+    if (v < 0 || v >= extend_variant_count()) return -1;
+    int info[5];
+    extend_variant_info(v, info);
+    if (info[0] == 4 && !(ctx->wide_valid && ctx->n_wnodes > 0)) return 0;
+    return v;
+}
+
 bool context_scene(mcrt_ctx *ctx, DeviceScene *out, cudaStream_t *stream, int *device, std::string **err) {
     *err = &ctx->err;
     if (!ctx->has_scene) {

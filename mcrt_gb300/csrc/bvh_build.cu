@@ -1419,7 +1419,17 @@ __global__ void k_compact(const mcrt_gpu_bvh_node *nodes, uint32_t n, const uint
     o[1] = make_float4(R.aabb_min[0], R.aabb_max[0], R.aabb_min[1], R.aabb_max[1]);
     o[2] = make_float4(L.aabb_min[2], L.aabb_max[2], R.aabb_min[2], R.aabb_max[2]);
     o[3] = make_float4(__uint_as_float(child_code(nodes, rank, l)), __uint_as_float(child_code(nodes, rank, r)),
-                       0.0f, 0.0f);
+                       __uint_as_float(kNoChild), 0.0f);
+}
+// Word 3.z of each compact record: its parent's index (the root keeps
+// kNoChild), the up-link of the stackless walk.  Runs after k_compact.
+__global__ void k_compact_parents(const mcrt_gpu_bvh_node *nodes, uint32_t n, const uint32_t *rank, float4 *out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || nodes[i].prim_count != 0) return;
+    const uint32_t kids[2] = {i + 1, nodes[i].right_or_offset};
+    for (int k = 0; k < 2; ++k)
+        if (nodes[kids[k]].prim_count == 0)
+            reinterpret_cast<uint32_t *>(out + 4ull * rank[kids[k]] + 3)[2] = rank[i];
 }
 // Shading records in original triangle order: the three vertex normals, the
 // first carrying the material word.
@@ -1485,6 +1495,8 @@ cudaError_t gpu_make_compact(const mcrt_gpu_bvh_node *d_nodes, uint32_t n_nodes,
     uint32_t n_int = last_rank + last_flag;
     if (*d_cnodes == nullptr) return cudaErrorInvalidValue;
     k_compact<<<(n_nodes + TB - 1) / TB, TB, 0, st>>>(d_nodes, n_nodes, rank, *d_cnodes); ::mcrt::note_launch();
+    k_compact_parents<<<(n_nodes + TB - 1) / TB, TB, 0, st>>>(d_nodes, n_nodes, rank, *d_cnodes);
+    ::mcrt::note_launch();
     *n_cnodes = n_int;
     return cudaGetLastError();
 }

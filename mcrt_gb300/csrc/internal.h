@@ -53,8 +53,12 @@ struct PathBuffers {
     float4 *sh_o = nullptr;      // shadow queue: origin | slot bits
     float4 *sh_d = nullptr;      // direction | t_max
     float4 *sh_c = nullptr;      // contribution rgb | unused
-    uint32_t *counters = nullptr;  // [0],[1] ray queue sizes, [2] shadow queue size, [3] overflow flag, [4..] stats
-    unsigned long long *stats = nullptr;  // [0] rays traced, [1] shadow rays
+    // [0],[1] ray queue sizes, [2] shadow queue size, [3] closest-hit overflow list size,
+    // [4],[5] work counters of the closest-hit and any-hit launches, [6] cache queries,
+    // [7] any-hit overflow list size
+    uint32_t *counters = nullptr;
+    unsigned long long *stats = nullptr;  // [0] rays traced, [1] shadow rays, [2] rays traced stackless
+    uint32_t *ovf = nullptr;     // overflow list: queue entries whose traversal stack would overflow
     // adjoint replay only
     float4 *pend = nullptr;      // per slot: d log(BSDF weight) / d(albedo rgb | roughness) of the last vertex
     uint32_t *pend_mat = nullptr;  // per slot: (material + 1) << 8 of that term, 0: none
@@ -105,7 +109,7 @@ void prepare_extend_variants();
 
 // Launchers (render.cu)
 void launch_trace_closest(const DeviceScene &S, const mcrt_ray *rays, uint32_t n, mcrt_hit *hits, bool ref_layout,
-                          uint32_t *overflow, cudaStream_t st);
+                          cudaStream_t st);
 // keep_radiance: replay of the same paths (the per-path radiance of the primal
 // pass stays in B.L as the radiance still to be accounted for).
 void launch_raygen(const DeviceScene &S, const RenderParams &P, PathBuffers &B, cudaStream_t st,

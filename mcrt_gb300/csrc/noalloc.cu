@@ -23,6 +23,11 @@
 //    first call before any stream capture is started on the device.
 //  * The scene comes from an earlier mcrt_upload_scene on the context (that
 //    set-up step allocates, as mcrt_upload_scene always does).
+//  * The closest-hit kernel is the context's autotuned variant (or the one the
+//    options name); a 4-wide variant whose quantised tree has not been built
+//    since the last BVH build (building it allocates) traces with the binary
+//    variant 0 instead, which gives the same image.
+//  * The caller's current device is restored before the call returns.
 #include <cstring>
 
 #include "common.cuh"
@@ -33,7 +38,8 @@ namespace {
 constexpr size_t kNoAllocScratchBytes = 64ull << 20;
 constexpr uint32_t kNoAllocMaxPixels = 262144;          // e.g. 512 x 512
 constexpr size_t kCounterBytes = 256;
-constexpr size_t kSlotBytes = 16 * 11;                  // thr, L, pend_mat, q_o x2, q_d x2, hits, sh_o, sh_d, sh_c
+// thr, L, q_o x2, q_d x2, hits, sh_o, sh_d, sh_c (16 B each) and the overflow list (4 B)
+constexpr size_t kSlotBytes = 16 * 10 + 4;
 constexpr size_t kSumBytesPerPixel = 24;                // f64 rgb
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
@@ -45,9 +51,19 @@ void *g_scratch_addr[kMaxDevices] = {};
 
 namespace mcrt {
 void set_global_error(const std::string &msg);
-// Scene of a context (api.cu).
+// Scene of a context, and the closest-hit variant a render on it uses (api.cu).
 bool context_scene(mcrt_ctx *ctx, DeviceScene *out, cudaStream_t *stream, int *device, std::string **err);
+int context_variant(mcrt_ctx *ctx, const mcrt_render_opts &o);
 }  // namespace mcrt
+
+namespace {
+// Puts the caller's current device back when the call returns.
+struct DeviceRestore {
+    int prev = -1;
+    DeviceRestore() { if (cudaGetDevice(&prev) != cudaSuccess) prev = -1; }
+    ~DeviceRestore() { if (prev >= 0) cudaSetDevice(prev); }
+};
+}  // namespace
 
 extern "C" mcrt_status mcrt_render_noalloc(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t w, uint32_t h,
                                            uint32_t spp, uint32_t first_frame, const mcrt_render_opts *opts,
@@ -67,8 +83,14 @@ extern "C" mcrt_status mcrt_render_noalloc(mcrt_ctx *ctx, const mcrt_camera_unif
     mcrt_render_opts o{};
     if (opts) o = *opts;
     if (o.flags & MCRT_RENDER_KEEP_ACCUM) return fail(MCRT_ERR_INVALID_ARG, "KEEP_ACCUM is not supported here");
+    if (o.flags & MCRT_RENDER_CACHE)
+        return fail(MCRT_ERR_INVALID_ARG, "the radiance cache is not supported here (its buffers are allocated)");
+    if (o.flags & MCRT_RENDER_GBUFFER) return fail(MCRT_ERR_INVALID_ARG, "no G-buffer is produced here");
     const uint32_t depth = o.max_depth ? o.max_depth : mcrt::kDefaultBounces;
     if (depth > 1024) return fail(MCRT_ERR_INVALID_ARG, "max_depth too large");
+    const int variant = mcrt::context_variant(ctx, o);
+    if (variant < 0) return fail(MCRT_ERR_INVALID_ARG, "variant out of range");
+    DeviceRestore restore;
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) return fail(MCRT_ERR_CUDA, "cudaSetDevice failed");
     // once per device: the device address of the static array
@@ -99,7 +121,6 @@ extern "C" mcrt_status mcrt_render_noalloc(mcrt_ctx *ctx, const mcrt_camera_unif
     B.n_slots = (uint32_t)n_slots;
     B.thr = take(n_slots * 16);
     B.L = take(n_slots * 16);
-    B.pend_mat = reinterpret_cast<uint32_t *>(take(n_slots * 16));   // 4 B used per slot
     for (int k = 0; k < 2; ++k) {
         B.q_o[k] = take(n_slots * 16);
         B.q_d[k] = take(n_slots * 16);
@@ -108,6 +129,7 @@ extern "C" mcrt_status mcrt_render_noalloc(mcrt_ctx *ctx, const mcrt_camera_unif
     B.sh_o = take(n_slots * 16);
     B.sh_d = take(n_slots * 16);
     B.sh_c = take(n_slots * 16);
+    B.ovf = reinterpret_cast<uint32_t *>(take(n_slots * 4));   // last: 4 B per slot
     // the array keeps the previous call's contents: clear the counters (the path
     // state and the sums are fully written by ray generation and the first resolve)
     e = cudaMemsetAsync(B.counters, 0, kCounterBytes, st);
@@ -120,9 +142,10 @@ extern "C" mcrt_status mcrt_render_noalloc(mcrt_ctx *ctx, const mcrt_camera_unif
         P.spp_pass = spp - done < spp_pass ? spp - done : spp_pass;
         P.frame0 = first_frame + done;
         P.max_depth = depth;
-        P.flags = o.flags;
+        P.flags = o.flags & ~(uint32_t)MCRT_RENDER_GRAPH;   // no capture here: the passes launch directly
         P.cam = *cam;
         P.gbuf_plane = -1;
+        P.extend_variant = variant;
         mcrt::launch_raygen(S, P, B, st);
         int qi = 0;
         for (uint32_t b = 0; b < depth; ++b) {
@@ -137,9 +160,5 @@ extern "C" mcrt_status mcrt_render_noalloc(mcrt_ctx *ctx, const mcrt_camera_unif
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return fail(MCRT_ERR_CUDA, cudaGetErrorString(e));
-    uint32_t overflow = 0;
-    e = cudaMemcpy(&overflow, B.counters + 3, 4, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return fail(MCRT_ERR_CUDA, cudaGetErrorString(e));
-    if (overflow) return fail(MCRT_ERR_STACK_OVERFLOW, "traversal stack bound reached");
     return MCRT_OK;
 }

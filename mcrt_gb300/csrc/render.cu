@@ -434,14 +434,13 @@ __device__ __forceinline__ float light_pdf_of_hit(const DeviceScene &S, float4 h
 
 // ------------------------------------------------------------------ kernels
 
-__global__ void k_trace_closest(DeviceScene S, const mcrt_ray *rays, uint32_t n, mcrt_hit *hits, int ref_layout,
-                                uint32_t *overflow) {
+__global__ void k_trace_closest(DeviceScene S, const mcrt_ray *rays, uint32_t n, mcrt_hit *hits, int ref_layout) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     mcrt_ray ry = rays[i];
     RayInv r = make_ray(mk3(ry.org[0], ry.org[1], ry.org[2]), mk3(ry.dir[0], ry.dir[1], ry.dir[2]));
     uint32_t nn = 0;
-    Closest c = world_hit(S, r, ry.tmin, ry.tmax, ref_layout != 0, &nn, overflow);
+    Closest c = world_hit(S, r, ry.tmin, ry.tmax, ref_layout != 0, &nn);
     mcrt_hit h;
     h.t = c.t;
     h.prim = c.prim;
@@ -454,8 +453,8 @@ __global__ void k_raygen(DeviceScene S, RenderParams P, PathBuffers B, int keep_
     uint32_t n = P.npix * P.spp_pass;
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) {
-        B.counters[0] = n; B.counters[1] = 0; B.counters[2] = 0; B.counters[4] = 0; B.counters[5] = 0;
-        B.counters[6] = 0;
+        B.counters[0] = n; B.counters[1] = 0; B.counters[2] = 0; B.counters[3] = 0; B.counters[4] = 0;
+        B.counters[5] = 0; B.counters[6] = 0; B.counters[7] = 0;
     }
     if (i >= n) return;
     if (P.cache_query_vertex && i % P.train_stride == 0u) {        // training path: no vertex recorded yet
@@ -510,10 +509,10 @@ __global__ void k_raygen(DeviceScene S, RenderParams P, PathBuffers B, int keep_
 // Closest-hit kernel variants, chosen per scene by mcrt_autotune: BVH width
 // (compact binary or quantised 4-wide), block size, minimum resident blocks per
 // SM (the register budget ptxas must meet), traversal stack depth (entries of 8
-// bytes in local memory; a ray that would overflow it raises the overflow flag
-// and the render reports MCRT_ERR_STACK_OVERFLOW, so the autotuner drops a
-// variant whose stack is too short for the scene) and the number of idle lanes
-// at which a warp fetches new rays.
+// bytes in local memory; a ray that would overflow it leaves the kernel's queue
+// for the overflow list, whose rays k_extend_retry traces without a stack, so
+// a short stack costs time on a deep tree but never a wrong or missing hit)
+// and the number of idle lanes at which a warp fetches new rays.
 struct ExtendVariant { int width, block, min_blocks, stack, refill; };
 constexpr int kExtendVariants = 8;
 constexpr ExtendVariant kVariantTable[kExtendVariants] = {
@@ -524,7 +523,7 @@ constexpr ExtendVariant kVariantTable[kExtendVariants] = {
 // continue with the nearer hit child, push the farther one.
 template <int STACK>
 __device__ __forceinline__ void visit_compact2(const DeviceScene &S, const RayInv &r, float tmax, uint32_t *cur,
-                                               float *cur_t, uint2 *stack, uint32_t *sp, uint32_t *overflow) {
+                                               float *cur_t, uint2 *stack, uint32_t *sp, bool *overflow) {
     const float4 *np = S.cnodes + 4ull * *cur;
     float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
     uint4 e = __ldg(reinterpret_cast<const uint4 *>(np + 3));
@@ -536,7 +535,7 @@ __device__ __forceinline__ void visit_compact2(const DeviceScene &S, const RayIn
         float tnear = tl, tfar = tr;
         if (tr < tl) { near = e.y; far = e.x; tnear = tr; tfar = tl; }
         if (*sp < (uint32_t)STACK) stack[(*sp)++] = make_uint2(far, __float_as_uint(tfar));
-        else *overflow = 1u;
+        else *overflow = true;
         *cur = near;
         *cur_t = tnear;
     } else if (hl) {
@@ -555,7 +554,7 @@ __device__ __forceinline__ void visit_compact2(const DeviceScene &S, const RayIn
 // the others farthest first.
 template <int STACK>
 __device__ __forceinline__ void visit_wide4(const DeviceScene &S, const RayInv &r, float tmax, uint32_t *cur,
-                                            float *cur_t, uint2 *stack, uint32_t *sp, uint32_t *overflow) {
+                                            float *cur_t, uint2 *stack, uint32_t *sp, bool *overflow) {
     const uint4 *np = S.wnodes + 4ull * *cur;
     const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3);
     const float ox = __uint_as_float(w0.x), oy = __uint_as_float(w0.y), oz = __uint_as_float(w0.z);
@@ -592,7 +591,7 @@ __device__ __forceinline__ void visit_wide4(const DeviceScene &S, const RayInv &
     for (int j = 3; j >= 1; --j) {
         if (key[j] == 0xffffffffu) continue;
         if (*sp < (uint32_t)STACK) stack[(*sp)++] = make_uint2(ref_of(key[j]), key[j] & ~3u);
-        else *overflow = 1u;
+        else *overflow = true;
     }
     if (key[0] == 0xffffffffu) {
         *cur = kNoChild;
@@ -602,17 +601,66 @@ __device__ __forceinline__ void visit_wide4(const DeviceScene &S, const RayInv &
     }
 }
 
+// The end of a traced queue entry.  Closest hit: the hit record, in queue
+// order.  Any hit (a shadow ray of path `slot`): an unoccluded ray adds its
+// contribution to the path's radiance; ADJ: the adjoint replay's shadow ray,
+// whose next-event term N leaves the radiance still ahead of its path
+// (B.L -= N) and contributes delta * N * dlog(f)/d(params) to its vertex's
+// material and delta * N / albedo to the emitter's radiance colour, collected
+// in the block's shared gacc.
+template <bool ANY, bool ADJ>
+__device__ __forceinline__ void finish_ray(const DeviceScene &S, const PathBuffers &B, const AdjointParams &A,
+                                           float *gacc, uint32_t ray, uint32_t slot, bool occl, Closest best) {
+    if (ANY) {
+        if (occl) return;
+        const float4 c = B.sh_c[ray];              // one shadow ray per path and bounce: no race on L
+        const float4 L = B.L[slot];
+        if (!ADJ) {
+            B.L[slot] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
+            return;
+        }
+        B.L[slot] = make_float4(L.x - c.x, L.y - c.y, L.z - c.z, 0.0f);
+        auto gadd = [&](uint32_t k, float v) {
+            if (v != 0.0f) atomicAdd(&gacc[k], v);
+        };
+        const uint32_t bits = __float_as_uint(c.w);
+        const uint32_t mi = bits & 0xffu, lm = (bits >> 8) & 0xffu;
+        const float4 di = A.dimg[slot / A.planes];
+        const f3 dn = (A.inv_spp * xyz(di)) * xyz(c);
+        const float4 g = B.sh_g[ray];
+        gadd(4u * mi + 0, dn.x * g.x);
+        gadd(4u * mi + 1, dn.y * g.y);
+        gadd(4u * mi + 2, dn.z * g.z);
+        gadd(4u * mi + 3, ((dn.x + dn.y) + dn.z) * g.w);
+        if (lm <= kMaxMatIdx) {                    // not the directional light
+            const float *la = S.materials->materials[lm].albedo_fuzz;
+            gadd(4u * lm + 0, safe_ratio(dn.x, la[0]));
+            gadd(4u * lm + 1, safe_ratio(dn.y, la[1]));
+            gadd(4u * lm + 2, safe_ratio(dn.z, la[2]));
+        }
+    } else {
+        if (best.prim == MCRT_HIT_MISS) best.t = -1.0f;
+        float u = (best.prim != MCRT_HIT_MISS && (best.prim & MCRT_HIT_SPHERE)) ? __uint_as_float(best.slot) : best.u;
+        __stcs(B.hits + ray, make_float4(best.t, __uint_as_float(best.prim), u, best.v));
+    }
+}
+
+// Overflow lists of the closest-hit and the any-hit launches: counters[3] and
+// counters[7] count the queue entries in B.ovf that k_extend_retry traces.
+// The closest-hit list is cleared by the shading kernel, the any-hit list by
+// the next closest-hit launch (neither runs while the list is in use).
+constexpr uint32_t kOvfClosest = 3u, kOvfAny = 7u;
+
 // ANY = true: the same persistent, refilled, speculative traversal for the
 // shadow-ray queue of next-event estimation, as an any-hit test: the cull
 // threshold stays the ray's t_max, so the set of boxes entered does not depend
 // on the visit order, and any accepted triangle hit in it (leaf_any) proves
 // the ray occluded, the answer of the closest-hit test; an unoccluded ray
 // adds its contribution to its path's radiance.
-// ADJ (with ANY): the adjoint replay's shadow rays.  An unoccluded ray's
-// next-event term N leaves the radiance still ahead of its path (B.L -= N) and
-// contributes delta * N * dlog(f)/d(params) to its vertex's material and
-// delta * N / albedo to the emitter's radiance colour, collected in shared
-// memory per block and added once per block at the end.
+// ADJ (with ANY): the adjoint replay's shadow rays (finish_ray), their
+// gradients collected in shared memory per block and added once per block.
+// A ray whose next push would overflow the stack stops here and joins the
+// overflow list (finished by k_extend_retry).
 template <int WIDTH, int BLOCK, int MINB, int STACK, int REFILL, bool ANY, bool ADJ>
 __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffers B, int qi, AdjointParams A) {
     __shared__ float gacc[ADJ ? 256 : 1];
@@ -621,7 +669,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
         __syncthreads();
     }
     const uint32_t n = ANY ? B.counters[2] : B.counters[qi];
-    if (!ANY && blockIdx.x == 0 && threadIdx.x == 0) { B.counters[qi ^ 1] = 0; B.counters[2] = 0; }
+    if (!ANY && blockIdx.x == 0 && threadIdx.x == 0) {
+        B.counters[qi ^ 1] = 0; B.counters[2] = 0; B.counters[kOvfAny] = 0;
+    }
     const float4 *qo = ANY ? B.sh_o : B.q_o[qi];
     const float4 *qd = ANY ? B.sh_d : B.q_d[qi];
     uint32_t *work = B.counters + (ANY ? 5 : 4);    // the queue's next unclaimed entry
@@ -640,6 +690,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
     uint32_t nn = 0;
     uint32_t slot = 0;                // ANY: the shadow ray's path
     bool occl = false;                // ANY: an accepted hit was found
+    // a ray whose stack would overflow keeps its queue index with bit 31 set
+    // (indices are below 2^31) until it joins the overflow list
+    constexpr uint32_t kOvfBit = 0x80000000u;
     for (;;) {
         // ---- refill idle lanes
         const bool idle = ray == 0xffffffffu;
@@ -703,8 +756,16 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
                     continue;
                 }
                 ++nn;
-                if (WIDTH == 4) visit_wide4<STACK>(S, r, best.t, &cur, &cur_t, stack, &sp, B.counters + 3);
-                else visit_compact2<STACK>(S, r, best.t, &cur, &cur_t, stack, &sp, B.counters + 3);
+                bool full = false;
+                if (WIDTH == 4) visit_wide4<STACK>(S, r, best.t, &cur, &cur_t, stack, &sp, &full);
+                else visit_compact2<STACK>(S, r, best.t, &cur, &cur_t, stack, &sp, &full);
+                if (full) {                                                   // to the overflow list
+                    ray |= kOvfBit;
+                    cur = kNoChild;
+                    sp = 0;
+                    leaf = kNoChild;
+                    break;
+                }
                 if (__all_sync(__activemask(), leaf != kNoChild)) break;
             }
             // ---- leaf phase
@@ -726,42 +787,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
             }
             // ---- finished ray
             if (cur == kNoChild && sp == 0) {
-                if (ANY) {
-                    if (!occl) {                       // one shadow ray per path and bounce: no race on L
-                        const float4 c = B.sh_c[ray];
-                        const float4 L = B.L[slot];
-                        if (!ADJ) {
-                            B.L[slot] = make_float4(L.x + c.x, L.y + c.y, L.z + c.z, 0.0f);
-                        } else {
-                            B.L[slot] = make_float4(L.x - c.x, L.y - c.y, L.z - c.z, 0.0f);
-                            auto gadd = [&](uint32_t k, float v) {
-                                if (v != 0.0f) atomicAdd(&gacc[k], v);
-                            };
-                            const uint32_t bits = __float_as_uint(c.w);
-                            const uint32_t mi = bits & 0xffu, lm = (bits >> 8) & 0xffu;
-                            const float4 di = A.dimg[slot / A.planes];
-                            const f3 dn = (A.inv_spp * xyz(di)) * xyz(c);
-                            const float4 g = B.sh_g[ray];
-                            gadd(4u * mi + 0, dn.x * g.x);
-                            gadd(4u * mi + 1, dn.y * g.y);
-                            gadd(4u * mi + 2, dn.z * g.z);
-                            gadd(4u * mi + 3, ((dn.x + dn.y) + dn.z) * g.w);
-                            if (lm <= kMaxMatIdx) {                       // not the directional light
-                                const float *la = S.materials->materials[lm].albedo_fuzz;
-                                gadd(4u * lm + 0, safe_ratio(dn.x, la[0]));
-                                gadd(4u * lm + 1, safe_ratio(dn.y, la[1]));
-                                gadd(4u * lm + 2, safe_ratio(dn.z, la[2]));
-                            }
-                        }
-                    }
+                if (ray & kOvfBit) {
+                    B.ovf[atomicAdd(B.counters + (ANY ? kOvfAny : kOvfClosest), 1u)] = ray & ~kOvfBit;
                 } else {
-                    if (best.prim == MCRT_HIT_MISS) best.t = -1.0f;
-                    float u = (best.prim != MCRT_HIT_MISS && (best.prim & MCRT_HIT_SPHERE))
-                                  ? __uint_as_float(best.slot) : best.u;
-                    __stcs(B.hits + ray, make_float4(best.t, __uint_as_float(best.prim), u, best.v));
+                    finish_ray<ANY, ADJ>(S, B, A, gacc, ray, slot, occl, best);
+                    ++traced;
                 }
                 ray = 0xffffffffu;
-                ++traced;
             }
         }
     }
@@ -769,6 +801,55 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
     if (ADJ) {
         __syncthreads();
         for (uint32_t k = threadIdx.x; k < 256u; k += BLOCK) {
+            const float v = gacc[k];
+            if (v != 0.0f) atomicAdd(A.grad + k, (double)v);
+        }
+    }
+}
+
+// The overflow list of the preceding closest-hit (ANY = false) or any-hit
+// launch: each ray traced again from the start, spheres first, with the
+// stackless walk, and finished as k_extend would (finish_ray).  Launched
+// after every extend launch; with an empty list its threads return at once.
+// stats[2] counts the rays it traced.
+constexpr int kRetryBlock = 128;
+template <bool ANY, bool ADJ>
+__global__ void __launch_bounds__(kRetryBlock) k_extend_retry(DeviceScene S, PathBuffers B, int qi, AdjointParams A) {
+    __shared__ float gacc[ADJ ? 256 : 1];
+    if (ADJ) {
+        for (uint32_t k = threadIdx.x; k < 256u; k += kRetryBlock) gacc[k] = 0.0f;
+        __syncthreads();
+    }
+    const uint32_t n = B.counters[ANY ? kOvfAny : kOvfClosest];
+    const float4 *qo = ANY ? B.sh_o : B.q_o[qi];
+    const float4 *qd = ANY ? B.sh_d : B.q_d[qi];
+    uint32_t traced = 0, nn = 0;
+    for (uint32_t i = blockIdx.x * kRetryBlock + threadIdx.x; i < n; i += gridDim.x * kRetryBlock) {
+        const uint32_t ray = B.ovf[i];
+        const float4 o4 = __ldcs(qo + ray), d4 = __ldcs(qd + ray);
+        const RayInv r = make_ray(xyz(o4), xyz(d4));
+        const float tmax = ANY ? d4.w : kTMax;
+        Closest best{tmax, MCRT_HIT_MISS, 0u, 0.0f, 0.0f};
+        spheres_hit(S, r, kTMin, tmax, best, &nn);
+        bool occl = false;
+        const uint32_t slot = __float_as_uint(o4.w);
+        if (ANY) {
+            occl = best.prim != MCRT_HIT_MISS;
+            best.t = tmax;
+            if (!occl) occl = mesh_walk_stackless<true>(S, r, kTMin, best, &nn);
+        } else {
+            mesh_walk_stackless<false>(S, r, kTMin, best, &nn);
+        }
+        finish_ray<ANY, ADJ>(S, B, A, gacc, ray, slot, occl, best);
+        ++traced;
+    }
+    if (traced) {
+        atomicAdd(B.stats + (ANY ? 1 : 0), (unsigned long long)traced);
+        atomicAdd(B.stats + 2, (unsigned long long)traced);
+    }
+    if (ADJ) {
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < 256u; k += kRetryBlock) {
             const float v = gacc[k];
             if (v != 0.0f) atomicAdd(A.grad + k, (double)v);
         }
@@ -788,11 +869,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
 //  * Stack: distributed over the lanes (entry k in lane k % 32, register
 //    k / 32), each entry the child code and the smallest entry distance of the
 //    lanes that entered it; popped entries no lane can still reach are dropped.
+//    A packet whose stack would overflow joins the overflow list (its rays
+//    are traced again by k_extend_retry).
 constexpr int kPacketBlock = 128;
 constexpr uint32_t kPacketStack = 64;
 __global__ void __launch_bounds__(kPacketBlock) k_extend_packet(DeviceScene S, PathBuffers B, int qi) {
     const uint32_t n = B.counters[qi];
-    if (blockIdx.x == 0 && threadIdx.x == 0) { B.counters[qi ^ 1] = 0; B.counters[2] = 0; }
+    if (blockIdx.x == 0 && threadIdx.x == 0) { B.counters[qi ^ 1] = 0; B.counters[2] = 0; B.counters[kOvfAny] = 0; }
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warp = (blockIdx.x * kPacketBlock + threadIdx.x) >> 5;
     const uint32_t n_warps = (gridDim.x * kPacketBlock) >> 5;
@@ -826,6 +909,7 @@ __global__ void __launch_bounds__(kPacketBlock) k_extend_packet(DeviceScene S, P
         }
         uint32_t sn0 = 0, sn1 = 0, st0 = 0, st1 = 0;   // this lane's stack entries k = lane, lane + 32
         uint32_t sp = 0;
+        bool ovf = false;                               // warp-uniform
         while (cur != kNoChild) {
             if (cur & kLeafBit) {
                 if (active) leaf_tris(S, r, (cur & ~kLeafBit) >> 4, leaf_count(S, cur), kTMin, best);
@@ -847,14 +931,14 @@ __global__ void __launch_bounds__(kPacketBlock) k_extend_packet(DeviceScene S, P
                     const uint32_t key = hit_far ? __float_as_uint(fmaxf(t_far, 0.0f)) : 0x7f800000u;
                     const uint32_t far_t = __reduce_min_sync(0xffffffffu, key);
                     const uint32_t far = right_first ? e.x : e.y;
-                    if (sp < kPacketStack) {
-                        if (lane == (sp & 31u)) {
-                            if (sp < 32u) { sn0 = far; st0 = far_t; } else { sn1 = far; st1 = far_t; }
-                        }
-                        ++sp;
-                    } else if (lane == 0) {
-                        B.counters[3] = 1u;
+                    if (sp == kPacketStack) {
+                        ovf = true;
+                        break;
                     }
+                    if (lane == (sp & 31u)) {
+                        if (sp < 32u) { sn0 = far; st0 = far_t; } else { sn1 = far; st1 = far_t; }
+                    }
+                    ++sp;
                     cur = right_first ? e.y : e.x;
                 } else if (ml) {
                     cur = e.x;
@@ -876,11 +960,15 @@ __global__ void __launch_bounds__(kPacketBlock) k_extend_packet(DeviceScene S, P
             }
         }
         if (active) {
-            if (best.prim == MCRT_HIT_MISS) best.t = -1.0f;
-            const float u = (best.prim != MCRT_HIT_MISS && (best.prim & MCRT_HIT_SPHERE))
-                                ? __uint_as_float(best.slot) : best.u;
-            __stcs(B.hits + ray, make_float4(best.t, __uint_as_float(best.prim), u, best.v));
-            ++traced;
+            if (ovf) {
+                B.ovf[atomicAdd(B.counters + kOvfClosest, 1u)] = ray;
+            } else {
+                if (best.prim == MCRT_HIT_MISS) best.t = -1.0f;
+                const float u = (best.prim != MCRT_HIT_MISS && (best.prim & MCRT_HIT_SPHERE))
+                                    ? __uint_as_float(best.slot) : best.u;
+                __stcs(B.hits + ray, make_float4(best.t, __uint_as_float(best.prim), u, best.v));
+                ++traced;
+            }
         }
     }
     if (traced) atomicAdd(B.stats, (unsigned long long)traced);
@@ -926,8 +1014,9 @@ __global__ void __launch_bounds__(256, ADJ ? 2 : 4) k_shade(DeviceScene S, Rende
     const uint32_t n = B.counters[qi];
     const bool nee = (P.flags & MCRT_RENDER_NEE) != 0 && (S.n_lights > 0 || S.has_sun);
     const uint32_t lane = threadIdx.x & 31u;
-    // work counters of the next extend and shadow launches (no kernel reads them now)
-    if (blockIdx.x == 0 && threadIdx.x == 0) { B.counters[4] = 0; B.counters[5] = 0; }
+    // work counters of the next extend and shadow launches, and the closest-hit
+    // overflow list (traced by now); no kernel reads them while this one runs
+    if (blockIdx.x == 0 && threadIdx.x == 0) { B.counters[4] = 0; B.counters[5] = 0; B.counters[kOvfClosest] = 0; }
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t i = base + threadIdx.x;
@@ -1310,9 +1399,9 @@ int sm_count() {
 }
 
 void launch_trace_closest(const DeviceScene &S, const mcrt_ray *rays, uint32_t n, mcrt_hit *hits, bool ref_layout,
-                          uint32_t *overflow, cudaStream_t st) {
+                          cudaStream_t st) {
     if (n == 0) return;
-    k_trace_closest<<<(n + 127) / 128, 128, 0, st>>>(S, rays, n, hits, ref_layout ? 1 : 0, overflow); ::mcrt::note_launch();
+    k_trace_closest<<<(n + 127) / 128, 128, 0, st>>>(S, rays, n, hits, ref_layout ? 1 : 0); ::mcrt::note_launch();
 }
 
 void launch_raygen(const DeviceScene &S, const RenderParams &P, PathBuffers &B, cudaStream_t st, bool keep_radiance) {
@@ -1376,21 +1465,31 @@ void prepare_extend_variants() {
     }
 }
 
+// The rays of the overflow list (a stack too short for the tree), after each extend launch.
+static void launch_retry(const DeviceScene &S, PathBuffers &B, int qi, bool any, const AdjointParams *adj,
+                         cudaStream_t st) {
+    const int blocks = sm_count();
+    if (adj) k_extend_retry<true, true><<<blocks, kRetryBlock, 0, st>>>(S, B, qi, *adj);
+    else if (any) k_extend_retry<true, false><<<blocks, kRetryBlock, 0, st>>>(S, B, qi, AdjointParams{});
+    else k_extend_retry<false, false><<<blocks, kRetryBlock, 0, st>>>(S, B, qi, AdjointParams{});
+    ::mcrt::note_launch();
+}
+
 void launch_extend(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, cudaStream_t st,
                    bool primary) {
     const int v = (P.extend_variant >= 0 && P.extend_variant < kExtendVariants) ? P.extend_variant : 0;
     prepare_extend_variants();
+    const uint32_t nmax = P.npix * P.spp_pass;
     if (primary) {                    // the camera rays: warp packets, every warp resident at once
-        const uint32_t nmax = P.npix * P.spp_pass;
         const int blocks = min(grid_blocks_for(nmax, kPacketBlock), sm_count() * g_packet_per_sm);
         k_extend_packet<<<blocks, kPacketBlock, 0, st>>>(S, B, qi); ::mcrt::note_launch();
-        return;
+    } else {
+        // persistent: as many resident blocks as fit, never more warps than rays
+        const int block = kVariantTable[v].block;
+        const int blocks = min(grid_blocks_for(nmax, block), sm_count() * g_extend_per_sm[v]);
+        kExtendKernels[v]<<<blocks, block, 0, st>>>(S, B, qi, AdjointParams{}); ::mcrt::note_launch();
     }
-    // persistent: as many resident blocks as fit, never more warps than rays
-    const int block = kVariantTable[v].block;
-    uint32_t nmax = P.npix * P.spp_pass;
-    int blocks = min(grid_blocks_for(nmax, block), sm_count() * g_extend_per_sm[v]);
-    kExtendKernels[v]<<<blocks, block, 0, st>>>(S, B, qi, AdjointParams{}); ::mcrt::note_launch();
+    launch_retry(S, B, qi, false, nullptr, st);
 }
 
 void launch_shade(const DeviceScene &S, const RenderParams &P, PathBuffers &B, int qi, uint32_t bounce,
@@ -1415,6 +1514,7 @@ void launch_shadow(const DeviceScene &S, const RenderParams &P, PathBuffers &B, 
     if (adj) kShadowAdjKernels[v]<<<blocks, block, 0, st>>>(S, B, 0, *adj);
     else kShadowKernels[v]<<<blocks, block, 0, st>>>(S, B, 0, AdjointParams{});
     ::mcrt::note_launch();
+    launch_retry(S, B, 0, true, adj, st);
 }
 
 void launch_resolve(const RenderParams &P, const PathBuffers &B, float4 *mean, double *sum, bool keep,

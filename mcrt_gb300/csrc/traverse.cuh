@@ -191,9 +191,124 @@ __device__ __forceinline__ void mesh_hit_ref(const DeviceScene &S, const RayInv 
     }
 }
 
-// Compact layout: node k = {Lx, Ly | Rx, Ry | Lz, Rz | codeL, codeR}.
+// Any hit in (tmin, tmax) with the same visibility rules (backface-culled
+// triangles are invisible from behind); used by shadow rays.
+// Any triangle of a leaf that mesh_hit_fast would accept as a hit before its
+// first one: tri_test passes, t < tmax, not culled by the backface flag.
+__device__ __forceinline__ bool leaf_any(const DeviceScene &S, const RayInv &r, uint32_t first, uint32_t count,
+                                         float tmin, float tmax) {
+    for (uint32_t j = 0; j < count; ++j) {
+        const TriRec *tr = S.tris + first + j;
+        float4 a = __ldg(&tr->v0), b = __ldg(&tr->e1), c = __ldg(&tr->e2);
+        float t, u, v;
+        if (!tri_test(r, xyz(a), xyz(b), xyz(c), tmin, &t, &u, &v)) continue;
+        if (!(t < tmax)) continue;
+        if (__float_as_uint(b.w) & MCRT_BACKFACE_CULL_FLAG) {       // path_trace.wgsl:438-452
+            f3 n = tri_shading_normal(S, __float_as_uint(a.w), u, v);
+            if (!(dot(r.d, n) < 0.0f)) continue;
+        }
+        return true;
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------- stackless walk
+// Closest hit and any hit over the compact layout without a stack, for rays
+// whose short stack overflowed (trees deeper than the stack: a degenerate
+// mesh can make the binned SAH tree as deep as it has triangles).  Each
+// compact record keeps its parent's index in word 3.z (kNoChild at the root),
+// so the walk goes down and back up (Hapala et al. 2011, "Efficient
+// stack-less BVH traversal for ray tracing"): a node's children are ordered
+// by entry distance with no far cull (ties: left first), so the order seen
+// on the way down is the order seen on the way back; the near child is
+// entered when its entry distance is <= the current closest t, the far one
+// when the walk comes back from the near one and the same test passes, and
+// after the far one the walk returns to the parent.  A child is skipped only
+// when its box starts beyond the current closest t, as in the stacked walk,
+// so every triangle that can be the closest hit is tested and the tie rule
+// gives the same answer.
+__device__ __forceinline__ uint32_t cnode_parent(const DeviceScene &S, uint32_t node) {
+    return __ldg(reinterpret_cast<const uint32_t *>(S.cnodes + 4ull * node + 3) + 2);
+}
+
+// Children of compact node `node` in visit order: c[0] nearer, c[1] farther
+// (kNoChild where a box is missed even with no far bound), entry distances t[].
+__device__ __forceinline__ void cnode_order(const DeviceScene &S, const RayInv &r, uint32_t node, float tmin,
+                                            uint32_t c[2], float t[2]) {
+    const float4 *np = S.cnodes + 4ull * node;
+    float4 a = __ldg(np), b = __ldg(np + 1), cc = __ldg(np + 2);
+    uint4 e = __ldg(reinterpret_cast<const uint4 *>(np + 3));
+    const float inf = __uint_as_float(0x7f800000u);
+    float tl = 0.0f, tr = 0.0f;
+    bool hl = e.x != kNoChild && slab(r, a.x, a.z, cc.x, a.y, a.w, cc.y, tmin, inf, &tl);
+    bool hr = e.y != kNoChild && slab(r, b.x, b.z, cc.z, b.y, b.w, cc.w, tmin, inf, &tr);
+    if (hl && hr && tr < tl) {
+        c[0] = e.y; t[0] = tr; c[1] = e.x; t[1] = tl;
+    } else {
+        c[0] = hl ? e.x : (hr ? e.y : kNoChild);
+        t[0] = hl ? tl : tr;
+        c[1] = (hl && hr) ? e.y : kNoChild;
+        t[1] = tr;
+    }
+}
+
+// ANY = false: closest hit into best; ANY = true: returns whether some
+// triangle is accepted before tmax (best.t must be tmax), stopping there.
+template <bool ANY>
+__device__ __noinline__ bool mesh_walk_stackless(const DeviceScene &S, const RayInv &r, float tmin, Closest &best,
+                                                 uint32_t *n_nodes) {
+    if (S.n_mesh_nodes == 0) return false;
+    {
+        const float4 *np = reinterpret_cast<const float4 *>(S.mesh_nodes);
+        float4 mn = __ldg(np), mx = __ldg(np + 1);
+        float te;
+        if (!slab(r, mn.x, mn.y, mn.z, mx.x, mx.y, mx.z, tmin, best.t, &te)) return false;
+        if (S.n_cnodes == 0) {                     // the whole tree is one leaf
+            uint4 meta = __ldg(reinterpret_cast<const uint4 *>(np + 2));
+            if (ANY) return leaf_any(S, r, meta.x, meta.y, tmin, best.t);
+            leaf_tris(S, r, meta.x, meta.y, tmin, best);
+            return false;
+        }
+    }
+    uint32_t node = 0, from = kNoChild;            // from: the child the walk returns from
+    for (;;) {
+        uint32_t c[2];
+        float t[2];
+        cnode_order(S, r, node, tmin, c, t);
+        if (from == kNoChild) ++*n_nodes;
+        uint32_t k = from == kNoChild ? 0u : (from == c[0] ? 1u : 2u);
+        uint32_t down = kNoChild;
+        for (; k < 2u; ++k) {
+            if (c[k] == kNoChild || !(t[k] <= best.t)) continue;
+            if (c[k] & kLeafBit) {
+                const uint32_t first = (c[k] & ~kLeafBit) >> 4, cnt = leaf_count(S, c[k]);
+                if (ANY) {
+                    if (leaf_any(S, r, first, cnt, tmin, best.t)) return true;
+                } else {
+                    leaf_tris(S, r, first, cnt, tmin, best);
+                }
+                continue;
+            }
+            down = c[k];
+            break;
+        }
+        if (down != kNoChild) {
+            node = down;
+            from = kNoChild;
+            continue;
+        }
+        const uint32_t up = cnode_parent(S, node);
+        if (up == kNoChild) return false;
+        from = node;
+        node = up;
+    }
+}
+
+// Compact layout: node k = {Lx, Ly | Rx, Ry | Lz, Rz | codeL, codeR, parent, 0}.
+// A ray that would overflow the stack is finished by the stackless walk from
+// its current closest hit (which only tightens the cull).
 __device__ __forceinline__ void mesh_hit_fast(const DeviceScene &S, const RayInv &r, float tmin, Closest &best,
-                                              uint32_t *n_nodes, uint32_t *overflow) {
+                                              uint32_t *n_nodes) {
     if (S.n_mesh_nodes == 0) return;
     if (S.n_cnodes == 0) {                       // the whole tree is one leaf
         const float4 *np = reinterpret_cast<const float4 *>(S.mesh_nodes);
@@ -226,8 +341,11 @@ __device__ __forceinline__ void mesh_hit_fast(const DeviceScene &S, const RayInv
             uint32_t near = e.x, far = e.y;
             float tfar = tr;
             if (tr < tl) { near = e.y; far = e.x; tfar = tl; }
-            if (sp < kStackSize) stack[sp++] = make_uint2(far, __float_as_uint(tfar));
-            else *overflow = 1u;
+            if (sp == kStackSize) {
+                mesh_walk_stackless<false>(S, r, tmin, best, n_nodes);
+                return;
+            }
+            stack[sp++] = make_uint2(far, __float_as_uint(tfar));
             next = near;
         } else if (hl) {
             next = e.x;
@@ -260,41 +378,19 @@ __device__ __forceinline__ void mesh_hit_fast(const DeviceScene &S, const RayInv
 // world_hit, path_trace.wgsl:471-479: spheres first, then the mesh with t_max =
 // the sphere distance; the mesh wins only when strictly closer.
 __device__ __forceinline__ Closest world_hit(const DeviceScene &S, const RayInv &r, float tmin, float tmax,
-                                             bool ref_layout, uint32_t *n_nodes, uint32_t *overflow) {
+                                             bool ref_layout, uint32_t *n_nodes) {
     Closest best{tmax, MCRT_HIT_MISS, 0u, 0.0f, 0.0f};
     spheres_hit(S, r, tmin, tmax, best, n_nodes);
     if (ref_layout) mesh_hit_ref(S, r, tmin, best, n_nodes);
-    else mesh_hit_fast(S, r, tmin, best, n_nodes, overflow);
+    else mesh_hit_fast(S, r, tmin, best, n_nodes);
     if (best.prim == MCRT_HIT_MISS) best.t = -1.0f;
     return best;
-}
-
-// Any hit in (tmin, tmax) with the same visibility rules (backface-culled
-// triangles are invisible from behind); used by shadow rays.
-// Any triangle of a leaf that mesh_hit_fast would accept as a hit before its
-// first one: tri_test passes, t < tmax, not culled by the backface flag.
-__device__ __forceinline__ bool leaf_any(const DeviceScene &S, const RayInv &r, uint32_t first, uint32_t count,
-                                         float tmin, float tmax) {
-    for (uint32_t j = 0; j < count; ++j) {
-        const TriRec *tr = S.tris + first + j;
-        float4 a = __ldg(&tr->v0), b = __ldg(&tr->e1), c = __ldg(&tr->e2);
-        float t, u, v;
-        if (!tri_test(r, xyz(a), xyz(b), xyz(c), tmin, &t, &u, &v)) continue;
-        if (!(t < tmax)) continue;
-        if (__float_as_uint(b.w) & MCRT_BACKFACE_CULL_FLAG) {       // path_trace.wgsl:438-452
-            f3 n = tri_shading_normal(S, __float_as_uint(a.w), u, v);
-            if (!(dot(r.d, n) < 0.0f)) continue;
-        }
-        return true;
-    }
-    return false;
 }
 
 // Is there a mesh hit in [tmin, tmax)?  mesh_hit_fast's traversal (same
 // order, same cull against tmax) up to its first accepted hit, which alone
 // decides whether it finds one, so the answer is the same; it stops there.
-__device__ __forceinline__ bool mesh_any_hit(const DeviceScene &S, const RayInv &r, float tmin, float tmax,
-                                             uint32_t *overflow) {
+__device__ __forceinline__ bool mesh_any_hit(const DeviceScene &S, const RayInv &r, float tmin, float tmax) {
     if (S.n_mesh_nodes == 0) return false;
     const float4 *root = reinterpret_cast<const float4 *>(S.mesh_nodes);
     {
@@ -321,8 +417,12 @@ __device__ __forceinline__ bool mesh_any_hit(const DeviceScene &S, const RayInv 
             uint32_t near = e.x, far = e.y;
             float tfar = tr;
             if (tr < tl) { near = e.y; far = e.x; tfar = tl; }
-            if (sp < kStackSize) stack[sp++] = make_uint2(far, __float_as_uint(tfar));
-            else *overflow = 1u;
+            if (sp == kStackSize) {                // too deep for the stack: walk without one
+                uint32_t nn = 0;
+                Closest b{tmax, MCRT_HIT_MISS, 0u, 0.0f, 0.0f};
+                return mesh_walk_stackless<true>(S, r, tmin, b, &nn);
+            }
+            stack[sp++] = make_uint2(far, __float_as_uint(tfar));
             next = near;
         } else if (hl) {
             next = e.x;
@@ -348,13 +448,12 @@ __device__ __forceinline__ bool mesh_any_hit(const DeviceScene &S, const RayInv 
     }
 }
 
-__device__ __forceinline__ bool occluded(const DeviceScene &S, const RayInv &r, float tmin, float tmax,
-                                         uint32_t *overflow) {
+__device__ __forceinline__ bool occluded(const DeviceScene &S, const RayInv &r, float tmin, float tmax) {
     uint32_t nn = 0;
     Closest best{tmax, MCRT_HIT_MISS, 0u, 0.0f, 0.0f};
     spheres_hit(S, r, tmin, tmax, best, &nn);
     if (best.prim != MCRT_HIT_MISS) return true;
-    return mesh_any_hit(S, r, tmin, tmax, overflow);
+    return mesh_any_hit(S, r, tmin, tmax);
 }
 
 }  // namespace mcrt

@@ -14,7 +14,8 @@ does not).
 * oracle_<name>.npz — the CPU oracle's 32x32, 4-spp renders (running mean,
   f64 sums, G-buffer) and closest hits of 4096 seeded rays for each scene.
 
-Usage: python tests/golden/make_golden.py [/path/to/reference]
+Usage: python tests/golden/make_golden.py /path/to/reference-checkout
+       (or MCRT_REFERENCE=/path/to/reference-checkout python tests/golden/make_golden.py)
 """
 import importlib.util
 import os
@@ -96,4 +97,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref_dir = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MCRT_REFERENCE")
+    if not ref_dir:
+        sys.exit("usage: make_golden.py /path/to/reference-checkout (or set MCRT_REFERENCE)")
+    main(ref_dir)
