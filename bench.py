@@ -28,9 +28,15 @@ batched_views : 16 uneven views of the voxel world traced together (CUDA graph)
            same views' time to relMSE 1e-3 with and without the radiance cache.
 radiance_cache_mlp : inference and one training step of the cache MLP on 2^20
            queries / samples against the measured bf16 tensor peak.
-cpu_baseline / --impl reference : the CPU oracle (a restatement of the reference's path:
-           its single-threaded SAH build and the path_trace.wgsl estimator on all host cores),
-           on a bounded row sample of the frame, extrapolated to one frame.
+cpu_baseline : the CPU oracle (a restatement of the reference's path: its single-threaded
+           SAH build and the path_trace.wgsl estimator on all host cores) on 128 rows of the
+           frame, scaled to one frame; cpu_baselines_other: the same oracle on the Cornell box,
+           the voxel world and the adjoint (see cpu_baselines).
+parity   : the GPU's images of the same frames equal the oracle's bit for bit (the 128 rows of
+           the benchmark frame, the whole Cornell and voxel-world frames).
+--impl reference : the oracle over whole frames, per step the single-threaded SAH build and
+           the full 1920 x 1080 x 16-spp frame on all host cores (no library of this
+           repository loaded).
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 Profiling cases (--leg bvh_build | cache_mlp | frame | adjoint | nee, and --small)
@@ -178,49 +184,72 @@ def camera(sc):
 
 
 # ------------------------------------------------------------------ CPU oracle (baseline / reference arm)
-def cpu_frame_estimate(sc, cam, rows_total=32, threads=0, stats=False):
-    """Reference SAH build (single thread, as the reference runs it) + the path_trace.wgsl
-    estimator on `rows_total` image rows spread over the frame (all host cores); returns
-    the extrapolated seconds per frame and the sample description."""
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as O
+    return O
+
+
+def oracle_camera(O, c, w, h):
+    return O.compute_camera(w, h, c["look_from"], c["look_at"], c["vfov"], c.get("aperture", 0.0))
+
+
+def oracle_strips(h, n_rects, rows):
+    return [int((k + 0.5) * h / n_rects) - rows // 2 for k in range(n_rects)]
+
+
+def cpu_frame_sample(sc, cam, rows_total=128, threads=0, stats=False):
+    """Reference SAH build (single thread, as the reference runs it) + the path_trace.wgsl
+    estimator on `rows_total` image rows in 8 strips spread over the frame (all host cores).
+    Returns (build s, render s, rows, strips [(y0, mean rgba)], traversal stats, oracle scene)."""
+    O = _oracle()
     t0 = time.perf_counter()
     osc = O.OracleScene(materials=sc["materials"], vertices=sc["vertices"], triangles=sc["triangles"], env=sc["env"])
     t_build = time.perf_counter() - t0
-    n_rects = 8
-    rows = max(1, rows_total // n_rects)
-    t_render, st = 0.0, dict(rays=0, nodes=0, prims=0)
-    for k in range(n_rects):
-        y0 = int((k + 0.5) * H / n_rects) - rows // 2
+    rows = max(1, rows_total // 8)
+    t_render, st, strips = 0.0, dict(rays=0, nodes=0, prims=0), []
+    for y0 in oracle_strips(H, 8, rows):
         t1 = time.perf_counter()
         r = osc.render(cam, W, H, SPP, 0, DEPTH, threads=threads, rect=(0, y0, W, rows), stats=stats)
         t_render += time.perf_counter() - t1
+        strips.append((y0, r["rgba"]))
         if stats:
             for key in st:
                 st[key] += r["stats"][key]
-    sampled_rows = rows * n_rects
-    t_frame = t_build + t_render * (H / sampled_rows)
-    sample = (f"reference SAH build of all {len(sc['triangles'])} triangles (1 thread, {t_build:.2f} s) + "
-              f"{sampled_rows} of {H} rows x {W} px x {SPP} spp (depth {DEPTH}, {t_render:.2f} s), "
-              f"render time scaled by {H / sampled_rows:.1f} to one frame")
-    return t_frame, sample, st, osc
+    return t_build, t_render, rows * 8, strips, st, osc
 
 
 def run_reference(args):
+    """The reference's path on the host cores: its single-threaded SAH build and the
+    path_trace.wgsl estimator (the oracle, a C++ restatement: the reference itself is Rust +
+    WGSL and has no CPU renderer) over the whole 1920 x 1080 x 16-spp frame on every core,
+    per step.  Camera and scene come from the oracle and numpy; no library of this
+    repository is loaded."""
     rank = int(os.environ.get("RANK", 0))
     if rank != 0:
         return
+    O = _oracle()
     sc = make_scene()
-    cam = camera(sc)
+    c = sc["camera"]
+    cam = oracle_camera(O, c, W, H)
     cores = os.cpu_count() or 1
-    times = []
-    sample = ""
+    times, builds = [], []
     for i in range(args.warmup + args.steps):
-        t_frame, sample, _, _ = cpu_frame_estimate(sc, cam, rows_total=64, threads=cores)
+        t0 = time.perf_counter()
+        osc = O.OracleScene(materials=sc["materials"], vertices=sc["vertices"], triangles=sc["triangles"],
+                            env=sc["env"])
+        t1 = time.perf_counter()
+        osc.render(cam, W, H, SPP, i * SPP, DEPTH, threads=cores)
+        t2 = time.perf_counter()
         if i >= args.warmup:
-            times.append(t_frame)
+            times.append(t2 - t0)
+            builds.append(t1 - t0)
+        del osc
     t = sum(times) / len(times)
     value = W * H * SPP / t / 1e6
+    sample = (f"whole frames: reference SAH build of all {len(sc['triangles'])} triangles (1 thread, "
+              f"{sum(builds) / len(builds):.2f} s) + all {H} rows x {W} px x {SPP} spp, depth {DEPTH} "
+              f"({t - sum(builds) / len(builds):.2f} s on {cores} threads), per step")
     print(json.dumps({
         "impl": "reference", "metric": "Msamples/s", "value": round(value, 4), "unit": "Msamples/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1000, 1),
@@ -231,6 +260,92 @@ def run_reference(args):
                          "sample": sample},
         "e2e": {"value": round(value, 4), "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
+
+
+def cpu_baselines(M, ctx, quality, cores):
+    """The oracle on the host cores for the other workloads, each image compared bit for
+    bit with the GPU's render of the same frames:
+      cornell : the seeded Cornell box 512 x 512, depth 8, reference estimator, 8 of its 64
+                frames of the whole image (Msamples/s and Mrays/s are rates of that sample);
+      cornell time to relMSE 1e-3 : the estimators are bit-identical on both sides, so the CPU
+                needs the spp the GPU leg needed; its time is that spp x the measured CPU
+                seconds per spp (8 frames of the whole image, each estimator), i.e. projected;
+      voxel_world : 1280 x 720, 8 spp, depth 6, sun + sky, NEE: the reference SAH build of the
+                4.94 M triangles (1 thread) and the whole frame (all cores);
+      adjoint : the oracle's brute-force (forward-mode) gradient of the GGX Cornell box,
+                256 x 256, 32 spp, NEE, 256 parameters: paths/s of the whole call."""
+    from mcrt_gb300 import scenes
+    O = _oracle()
+    env = M.gradient_env_map()
+    out = {"cores": cores}
+    parity = {}
+    # ---- Cornell box
+    sc = scenes.cornell_box(SEED)
+    c = sc["camera"]
+    cam = oracle_camera(O, c, 512, 512)
+    osc = O.OracleScene(materials=sc["materials"], vertices=sc["vertices"], triangles=sc["triangles"], env=env)
+    per_spp = {}
+    for name, nee in (("plain", False), ("nee", True)):
+        t0 = time.perf_counter()
+        r = osc.render(cam, 512, 512, 8, 0, 8, threads=cores, stats=True, nee=nee)
+        dt = time.perf_counter() - t0
+        per_spp[name] = dt / 8
+        if name == "plain":
+            out["cornell"] = {"msamples_per_s": round(512 * 512 * 8 / dt / 1e6, 3),
+                              "mrays_per_s": round(r["stats"]["rays"] / dt / 1e6, 3),
+                              "sample": f"512x512 x 8 of 64 spp, depth 8, reference estimator, {cores} threads"}
+        ctx.upload_scene(vertices=sc["vertices"], triangles=sc["triangles"], materials=sc["materials"], env=env)
+        g = ctx.render(cam, 512, 512, 8, max_depth=8, nee=nee, outputs=("rgba",))["rgba"]
+        parity[f"cornell_{name}"] = {"pixels": 512 * 512, "spp": 8,
+                                     "bit_exact": bool(np.array_equal(g.view(np.uint32), r["rgba"].view(np.uint32)))}
+    if quality:
+        proj = {}
+        for name in ("plain", "nee"):
+            spp_needed = quality[name]["spp"]
+            proj[name] = {"spp": spp_needed, "s": round(spp_needed * per_spp[name], 2),
+                          "cpu_s_per_spp": round(per_spp[name], 4)}
+        out["cornell_time_to_relmse"] = dict(proj, kind="projected: measured CPU s per spp x the spp the "
+                                                     "bit-identical estimator needed on the GPU")
+    # ---- voxel world
+    w = scenes.voxel_world(SEED)
+    p = w["params"]
+    cw = oracle_camera(O, w["camera"], w["width"], w["height"])
+    v, t = O.world_mesh(O.world_generate(p), w["block_material"], greedy=False, chunk_x0=p["chunk_x0"],
+                        chunk_z0=p["chunk_z0"])
+    t0 = time.perf_counter()
+    osc = O.OracleScene(materials=w["materials"], vertices=v, triangles=t, env=env, sun_dir=w["sun_dir"],
+                        sun_irradiance=w["sun_irradiance"])
+    t_build = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    r = osc.render(cw, w["width"], w["height"], w["spp"], 0, w["max_depth"], threads=cores, stats=True, nee=True)
+    t_render = time.perf_counter() - t0
+    del osc
+    n = w["width"] * w["height"] * w["spp"]
+    out["voxel_world"] = {"msamples_per_s": round(n / t_render / 1e6, 3),
+                          "mrays_per_s": round(r["stats"]["rays"] / t_render / 1e6, 3),
+                          "render_s": round(t_render, 2), "bvh_build_s": round(t_build, 2),
+                          "triangles": int(len(t)),
+                          "sample": f"whole frame 1280x720 x 8 spp, depth 6, NEE, {cores} threads; "
+                                    "reference SAH build on 1 thread"}
+    ctx.world_generate(p)
+    ctx.world_mesh(w["block_material"], greedy=False)
+    ctx.upload_scene(materials=w["materials"], env=env, sun_dir=w["sun_dir"], sun_irradiance=w["sun_irradiance"],
+                     world_mesh=True)
+    g = ctx.render(cw, w["width"], w["height"], w["spp"], max_depth=w["max_depth"], nee=True, outputs=("rgba",))["rgba"]
+    parity["voxel_world"] = {"pixels": w["width"] * w["height"], "spp": w["spp"],
+                             "bit_exact": bool(np.array_equal(g.view(np.uint32), r["rgba"].view(np.uint32)))}
+    # ---- adjoint
+    sc = scenes.cornell_box_ggx(SEED)
+    c = sc["camera"]
+    cam = oracle_camera(O, c, 256, 256)
+    osc = O.OracleScene(materials=sc["materials"], vertices=sc["vertices"], triangles=sc["triangles"], env=env)
+    d_img = np.random.default_rng(0).standard_normal((256, 256, 4)).astype(np.float32)
+    t0 = time.perf_counter()
+    osc.adjoint(cam, 256, 256, 32, d_img, max_depth=8, nee=True, threads=cores)
+    dt = time.perf_counter() - t0
+    out["adjoint"] = {"paths_per_s": round(256 * 256 * 32 / dt, 1), "s": round(dt, 3),
+                      "sample": f"whole call 256x256 x 32 spp, depth 8, NEE, 256 parameters, {cores} threads"}
+    return out, parity
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -597,10 +712,20 @@ def run_mcrt(args):
     peak, peak_kind = peaks()
     cpu = None
     st = None
+    parity = {}
+    cores = os.cpu_count() or 1
     if not args.no_cpu_baseline:
-        t_frame, sample, st, _ = cpu_frame_estimate(sc, cam, rows_total=128, threads=os.cpu_count() or 1, stats=True)
-        cpu = {"value": round(W * H * SPP / t_frame / 1e6, 4), "unit": "Msamples/s", "cores": os.cpu_count() or 1,
-               "kind": "port", "sample": sample}
+        t_build, t_render, n_rows, strips, st, _ = cpu_frame_sample(sc, cam, rows_total=128, threads=cores, stats=True)
+        t_frame = t_build + t_render * (H / n_rows)
+        cpu = {"value": round(W * H * SPP / t_frame / 1e6, 4), "unit": "Msamples/s", "cores": cores, "kind": "port",
+               "sample": (f"reference SAH build of all {len(sc['triangles'])} triangles (1 thread, {t_build:.2f} s) + "
+                          f"{n_rows} of {H} rows x {W} px x {SPP} spp (depth {DEPTH}, {t_render:.2f} s on {cores} "
+                          f"threads), render time scaled by {H / n_rows:.1f} to one frame")}
+        # the same frames on the GPU (outside the timed region): the oracle's rows, bit for bit
+        ctx.rebuild_bvh()
+        g = ctx.render(cam, W, H, SPP, first_frame=0, max_depth=DEPTH, outputs=("rgba",))["rgba"]
+        ok = all(np.array_equal(g[y0:y0 + m.shape[0]].view(np.uint32), m.view(np.uint32)) for y0, m in strips)
+        parity["displaced_icosphere"] = {"rows": n_rows, "pixels": n_rows * W, "spp": SPP, "bit_exact": bool(ok)}
     ext_ms = sum(e[0] for e in ext)
     ext_launches = sum(e[1] for e in ext)
     rays = sum(e[2] for e in ext)
@@ -624,7 +749,7 @@ def run_mcrt(args):
                 "n_tri": round(n_tri, 2), "n_source": n_source, "mrays_per_s": round(rays / (ext_ms / 1000.0) / 1e6, 1),
                 "avg_launch_ms": round(ext_ms / max(ext_launches, 1), 4)}
     clocks = clk.summary()
-    quality = adjoint = voxel = views = views_cache = mlp = None
+    quality = adjoint = voxel = views = views_cache = mlp = cpu_more = None
     if not args.small:
         mlp = mlp_rate(M, ctx)
         quality = time_to_relmse(M, ctx)
@@ -632,6 +757,9 @@ def run_mcrt(args):
         voxel = voxel_world_rate(M, ctx, stream)
         views = batched_views_rate(M, ctx, stream)
         views_cache = views_cache_relmse(M, ctx)
+        if not args.no_cpu_baseline:
+            cpu_more, more_parity = cpu_baselines(M, ctx, quality, cores)
+            parity.update(more_parity)
     out = {
         "metric": "Msamples/s", "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 3), "higher_is_better": True,
@@ -647,6 +775,8 @@ def run_mcrt(args):
         "gpu_launches": int(launches),
         "roofline": roof,
         "cpu_baseline": cpu,
+        "cpu_baselines_other": cpu_more,
+        "parity": parity or None,
         "clocks": clocks,
         "extend_ms_per_step": round(ext_ms / len(ext), 3),
         "breakdown_ms_per_step": device_breakdown,

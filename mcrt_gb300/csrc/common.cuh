@@ -25,6 +25,17 @@ constexpr float kTMin = 1e-4f;
 constexpr float kTMax = 1e9f;
 constexpr uint32_t kMaxFrameCount = 65535u;
 constexpr uint32_t kDefaultBounces = 8u;
+// Relative slack of every box test against the current closest t (entry) and
+// of the box exit: a box is entered when texit * kCullSlack > max(tenter, tmin)
+// and tenter <= t * kCullSlack.  A hit on a shared edge or vertex lies on the
+// boundary of its triangle's box, and the Moller-Trumbore t can lie outside it
+// by rounding (a few ulps, hundreds for a grazing ray); the exact test would
+// make the closest hit depend on which triangle the visit order found first.
+// With the slack (1 + 2^-12) every box that can hold a hit at or before t is
+// entered, so every traversal order gives the tie rule's answer over all
+// triangles the test accepts.
+constexpr float kCullSlack = 1.000244140625f;
+__host__ __device__ __forceinline__ float cull_t(float t) { return t * kCullSlack; }
 
 // ---------------------------------------------------------------- vectors
 struct f3 { float x, y, z; };

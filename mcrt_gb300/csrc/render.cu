@@ -500,9 +500,9 @@ __global__ void k_raygen(DeviceScene S, RenderParams P, PathBuffers B, int keep_
 //  * Traversal phase: a lane walks internal nodes; a leaf it reaches is
 //    postponed and the lane keeps traversing until every active lane of the
 //    warp holds a postponed leaf (warp vote); then the lanes test their leaves
-//    together.  The vote only shapes scheduling: the set of nodes and leaves
-//    visited per ray is decided by the same cull test (entry distance <=
-//    current closest t) as in the reference order, so the hit is the same.
+//    together.  The vote only shapes scheduling: every order enters every box
+//    that can hold a hit at or before the closest t (the cull's slack,
+//    kCullSlack), so the hit is the reference order's.
 // Sphere BVHs (the reference's binding 5) are traversed at ray fetch with the
 // reference-order walk (spheres_hit); their count is small.
 
@@ -741,11 +741,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
         if (ray != 0xffffffffu) {
             // ---- traversal phase
             for (;;) {
-                if (cur != kNoChild && cur_t > best.t) cur = kNoChild;      // culled since it was queued
+                if (cur != kNoChild && cur_t > cull_t(best.t)) cur = kNoChild;   // culled since it was queued
                 if (cur == kNoChild) {                                        // pop the next live entry
                     while (sp > 0) {
                         uint2 s = stack[--sp];
-                        if (__uint_as_float(s.y) <= best.t) { cur = s.x; cur_t = __uint_as_float(s.y); break; }
+                        if (__uint_as_float(s.y) <= cull_t(best.t)) { cur = s.x; cur_t = __uint_as_float(s.y); break; }
                     }
                     if (cur == kNoChild) break;
                 }
@@ -780,7 +780,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
                     leaf_tris(S, r, (leaf & ~kLeafBit) >> 4, leaf_count(S, leaf), kTMin, best);
                 }
                 leaf = kNoChild;
-                if (cur != kNoChild && (cur & kLeafBit) && cur_t <= best.t) {
+                if (cur != kNoChild && (cur & kLeafBit) && cur_t <= cull_t(best.t)) {
                     leaf = cur;
                     cur = kNoChild;
                 }
@@ -950,12 +950,13 @@ __global__ void __launch_bounds__(kPacketBlock) k_extend_packet(DeviceScene S, P
             }
             if (cur == kNoChild && sp > 0) {
                 // pop the next entry some lane can still reach
-                const uint32_t reach = __reduce_max_sync(0xffffffffu, active ? __float_as_uint(best.t) : 0u);
+                const float reach =
+                    cull_t(__uint_as_float(__reduce_max_sync(0xffffffffu, active ? __float_as_uint(best.t) : 0u)));
                 while (sp > 0) {
                     --sp;
                     const uint32_t node = __shfl_sync(0xffffffffu, sp < 32u ? sn0 : sn1, sp & 31u);
                     const uint32_t t = __shfl_sync(0xffffffffu, sp < 32u ? st0 : st1, sp & 31u);
-                    if (t <= reach) { cur = node; break; }
+                    if (__uint_as_float(t) <= reach) { cur = node; break; }
                 }
             }
         }

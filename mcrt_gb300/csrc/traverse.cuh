@@ -40,8 +40,9 @@ __device__ __forceinline__ RayInv make_ray(f3 o, f3 d) {
     return {o, d, mk3(inv_dir(d.x), inv_dir(d.y), inv_dir(d.z))};
 }
 
-// ray_aabb_hit, path_trace.wgsl:248-256, with `tenter <= t_max` so that exact
-// ties stay reachable in any visit order.
+// ray_aabb_hit, path_trace.wgsl:248-256, with the slack kCullSlack on the
+// entry cull and the exit, so that the closest hit does not depend on the
+// visit order.
 __device__ __forceinline__ bool slab(const RayInv &r, float lx, float ly, float lz, float hx, float hy, float hz,
                                      float tmin, float tmax, float *tenter_out) {
     float t0x = (lx - r.o.x) * r.inv.x, t1x = (hx - r.o.x) * r.inv.x;
@@ -50,7 +51,7 @@ __device__ __forceinline__ bool slab(const RayInv &r, float lx, float ly, float 
     float tenter = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
     float texit = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
     *tenter_out = tenter;
-    return texit > fmaxf(tenter, tmin) && tenter <= tmax;
+    return cull_t(texit) > fmaxf(tenter, tmin) && tenter <= cull_t(tmax);
 }
 
 // ray_sphere_hit root selection, path_trace.wgsl:262-281 (t_max applied by the caller).
@@ -279,7 +280,7 @@ __device__ __noinline__ bool mesh_walk_stackless(const DeviceScene &S, const Ray
         uint32_t k = from == kNoChild ? 0u : (from == c[0] ? 1u : 2u);
         uint32_t down = kNoChild;
         for (; k < 2u; ++k) {
-            if (c[k] == kNoChild || !(t[k] <= best.t)) continue;
+            if (c[k] == kNoChild || !(t[k] <= cull_t(best.t))) continue;
             if (c[k] & kLeafBit) {
                 const uint32_t first = (c[k] & ~kLeafBit) >> 4, cnt = leaf_count(S, c[k]);
                 if (ANY) {
@@ -359,7 +360,7 @@ __device__ __forceinline__ void mesh_hit_fast(const DeviceScene &S, const RayInv
                 next = kNoChild;
                 while (sp > 0) {
                     uint2 s = stack[--sp];
-                    if (__uint_as_float(s.y) <= best.t) { next = s.x; break; }
+                    if (__uint_as_float(s.y) <= cull_t(best.t)) { next = s.x; break; }
                 }
                 if (next == kNoChild) return;
             }
@@ -433,7 +434,7 @@ __device__ __forceinline__ bool mesh_any_hit(const DeviceScene &S, const RayInv 
             if (next == kNoChild) {
                 while (sp > 0) {
                     uint2 s = stack[--sp];
-                    if (__uint_as_float(s.y) <= tmax) { next = s.x; break; }
+                    if (__uint_as_float(s.y) <= cull_t(tmax)) { next = s.x; break; }
                 }
                 if (next == kNoChild) return false;
             }

@@ -113,14 +113,28 @@ struct Ray { V3 o, d; };
  * clamp such a ray counts as inside the slab and traversal equals brute force. */
 inline float inv_dir(float d) { return fabsf(d) < 1e-7f ? (d >= 0.0f ? 1e30f : -1e30f) : 1.0f / d; }
 
-/* path_trace.wgsl:248-256, with `tenter <= t_max` (tie reachability, see header) */
+/* The box test with a relative slack on both ends: a box is entered when
+ * texit * CULL_SLACK > max(tenter, t_min) and tenter <= t_max * CULL_SLACK.
+ * A hit on a shared edge or vertex lies on the boundary of its triangle's box,
+ * and the Moller-Trumbore t can lie outside the box by its rounding (a few
+ * ulps; hundreds for a grazing ray), so with the exact test such a box is
+ * culled or not depending on which triangle the visit order found first: the
+ * closest hit and the tie rule would depend on the order (about 1 in 200 rays
+ * aimed at mesh vertices and edges).  With the slack (1 + 2^-12, about 2000
+ * ulps) every box that can hold a hit at or before t is entered, so the
+ * answer is the tie rule's over every triangle the test accepts, in any visit
+ * order (no difference from brute force on 10^6 such rays). */
+constexpr float CULL_SLACK = 1.000244140625f;
+inline float cull_t(float t) { return t * CULL_SLACK; }
+
+/* path_trace.wgsl:248-256, with the slack of CULL_SLACK on entry and exit */
 inline bool ray_aabb_hit(const Ray &r, const orc_node &nd, float t_min, float t_max) {
     V3 inv = {inv_dir(r.d.x), inv_dir(r.d.y), inv_dir(r.d.z)};
     V3 t0 = (ld3(nd.aabb_min) - r.o) * inv;
     V3 t1 = (ld3(nd.aabb_max) - r.o) * inv;
     float tenter = fmaxf(fmaxf(fminf(t0.x, t1.x), fminf(t0.y, t1.y)), fminf(t0.z, t1.z));
     float texit = fminf(fminf(fmaxf(t0.x, t1.x), fmaxf(t0.y, t1.y)), fmaxf(t0.z, t1.z));
-    return texit > fmaxf(tenter, t_min) && tenter <= t_max;
+    return cull_t(texit) > fmaxf(tenter, t_min) && tenter <= cull_t(t_max);
 }
 
 /* path_trace.wgsl:262-281: candidate root with t > t_min (near first, then far),
@@ -726,9 +740,11 @@ struct Deriv {
  * its non-emissive vertex number `bounce` it keeps that vertex's light sample
  * (next-event estimation), then adds thr * max(c, 0) and ends. */
 struct CacheStop { uint32_t bounce; V3 c; };
+/* The closest-hit queries of one path: ray and hit of bounces 0 .. bmax-1. */
+struct PathLog { orc_ray *rays; orc_hit *hits; uint32_t bmax; };
 
 V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, float *gbuf, uint64_t *stats,
-              const Lights *lights, Deriv *D, const CacheStop *stop = nullptr) {
+              const Lights *lights, Deriv *D, const CacheStop *stop = nullptr, PathLog *log = nullptr) {
     const bool nee = lights && (lights->n > 0 || lights->has_sun);
     V3 thr = {1.0f, 1.0f, 1.0f};
     V3 Lacc = {0.0f, 0.0f, 0.0f};
@@ -746,6 +762,12 @@ V3 path_color(const orc_scene *sc, Ray ray, uint32_t &rng, uint32_t max_depth, f
         uint32_t nv = 0, pt = 0;
         Closest c = world_hit(sc, ray, T_MIN, T_MAX, &nv, &pt);
         if (stats) { stats[0] += 1; stats[1] += nv; stats[2] += pt; }
+        if (log && bounce < log->bmax) {
+            orc_ray &lr = log->rays[bounce];
+            lr.org[0] = ray.o.x; lr.org[1] = ray.o.y; lr.org[2] = ray.o.z; lr.tmin = T_MIN;
+            lr.dir[0] = ray.d.x; lr.dir[1] = ray.d.y; lr.dir[2] = ray.d.z; lr.tmax = T_MAX;
+            log->hits[bounce] = orc_hit{c.t, c.prim, c.u, c.v};
+        }
         if (c.t < 0.0f) {
             if (first && gbuf) { gbuf[0] = 0; gbuf[1] = 0; gbuf[2] = 0; gbuf[3] = T_MAX; }
             V3 e = thr * sample_env(sc, ray.d);
@@ -1071,6 +1093,37 @@ extern "C" {
 
 uint32_t orc_pcg_hash(uint32_t v) { return pcg_hash(v); }
 
+/* compute_camera, camera.rs:76-127 (glam Vec3 arithmetic; tan = sin / cos of
+ * the shared elementary functions).  out: the 112-byte CameraUniform. */
+void orc_compute_camera(uint32_t width, uint32_t height, const float look_from[3], const float look_at[3],
+                        float vfov_deg, float aperture, float focus_dist, orc_camera *out) {
+    const float aspect = (float)width / (float)height;
+    const V3 vup = {0.0f, 1.0f, 0.0f};
+    const float vfov_rad = vfov_deg * (PI_F / 180.0f);                      /* to_radians */
+    const float hh = of_tan(vfov_rad * 0.5f);
+    const float viewport_h = 2.0f * hh;
+    const float viewport_w = aspect * viewport_h;
+    const V3 from = ld3(look_from), at = ld3(look_at);
+    const V3 w = normalize(from - at);                                       /* backward */
+    const V3 c0 = cross(vup, w);
+    const V3 vup_safe = dot(c0, c0) > 1e-10f ? vup : V3{0.0f, 0.0f, 1.0f};   /* gimbal-lock guard */
+    const V3 u = normalize(cross(vup_safe, w));
+    const V3 v = cross(w, u);
+    const V3 horizontal = (focus_dist * viewport_w) * u;
+    const V3 vertical = (focus_dist * viewport_h) * v;
+    const V3 lower_left = ((from - 0.5f * horizontal) - 0.5f * vertical) - focus_dist * w;
+    const float lens_radius = aperture * 0.5f;
+    const V3 du = lens_radius * u, dv = lens_radius * v;
+    std::memset(out, 0, sizeof(*out));
+    auto put = [](float *dst, V3 x) { dst[0] = x.x; dst[1] = x.y; dst[2] = x.z; dst[3] = 0.0f; };
+    put(out->origin, from);
+    put(out->lower_left, lower_left);
+    put(out->horizontal, horizontal);
+    put(out->vertical, vertical);
+    put(out->defocus_u, du);
+    put(out->defocus_v, dv);
+}
+
 uint32_t orc_build_sphere_bvh(const orc_sphere *spheres, uint32_t n, orc_node *out_nodes,
                               orc_sphere *out_ordered, uint32_t *out_ids) {
     if (n == 0) return 0;                                                   /* bvh.rs:240-245 */
@@ -1187,6 +1240,34 @@ void orc_render_ex(const orc_scene *sc, const orc_camera *cam, uint32_t w, uint3
     }
     }
     if (out_stats) for (int k = 0; k < 3; ++k) out_stats[k] = tot[k];
+}
+
+void orc_dump_rays(const orc_scene *sc, const orc_camera *cam, uint32_t w, uint32_t h, uint32_t x0, uint32_t y0,
+                   uint32_t cw, uint32_t ch, uint32_t spp, uint32_t first_frame, uint32_t max_depth, uint32_t flags,
+                   uint32_t bmax, orc_ray *out_rays, orc_hit *out_hits, int threads) {
+    const int64_t npx = (int64_t)cw * ch;
+    Lights lights;
+    const Lights *lp = nullptr;
+    if (flags & ORC_RENDER_NEE) {
+        make_lights(sc, lights);
+        lp = &lights;
+    }
+#pragma omp parallel for schedule(dynamic, 16) num_threads(n_threads(threads))
+    for (int64_t i = 0; i < npx; ++i) {
+        const uint32_t x = x0 + (uint32_t)(i % cw), y = y0 + (uint32_t)(i / cw);
+        for (uint32_t k = 0; k < spp; ++k) {
+            const size_t base = ((size_t)i * spp + k) * bmax;
+            for (uint32_t b = 0; b < bmax; ++b) {                /* entries the path does not reach */
+                out_rays[base + b] = orc_ray{{0, 0, 0}, 0.0f, {0, 0, 0}, -1.0f};
+                out_hits[base + b] = orc_hit{-1.0f, ORC_HIT_MISS, 0.0f, 0.0f};
+            }
+            const uint32_t frame = first_frame + k;
+            uint32_t rng = pcg_hash(pcg_hash(x + y * w) ^ (frame * 2654435761u));   /* :636-637 */
+            Ray r = camera_ray(cam, x, y, w, h, rng);
+            PathLog log{out_rays + base, out_hits + base, bmax};
+            (void)path_color(sc, r, rng, max_depth, nullptr, nullptr, lp, nullptr, nullptr, &log);
+        }
+    }
 }
 
 void orc_render_cache_const(const orc_scene *sc, const orc_camera *cam, uint32_t w, uint32_t h, uint32_t spp,

@@ -60,6 +60,10 @@ uint32_t orc_build_mesh_bvh(const orc_vertex *verts, uint32_t nv,
                             const orc_triangle *tris, uint32_t nt,
                             orc_node *out_nodes, orc_triangle *out_ordered, uint32_t *out_ids);
 
+/* compute_camera, camera.rs:76-127: the CameraUniform of a thin-lens camera. */
+void orc_compute_camera(uint32_t width, uint32_t height, const float look_from[3], const float look_at[3],
+                        float vfov_deg, float aperture, float focus_dist, orc_camera *out);
+
 /* mode 0: reference traversal order with the tie rule; mode 1: brute force.
  * stats (optional, 2 entries per ray): nodes visited, primitives tested. */
 void orc_trace(const orc_scene *scene, const orc_ray *rays, uint32_t n, orc_hit *hits,
@@ -110,6 +114,15 @@ void orc_render_cache_const(const orc_scene *scene, const orc_camera *cam, uint3
                             uint32_t first_frame, uint32_t max_depth, uint32_t flags, uint32_t spp_pass,
                             uint32_t train_stride, uint32_t query_vertex, const float *c3, float *out_mean_rgba,
                             double *out_sum_rgb, int threads);
+
+/* The closest-hit queries of the sampled paths of a pixel rectangle (as
+ * orc_render_ex samples them): for each pixel (row-major), frame and bounce
+ * b < bmax, the ray (origin, direction, tmin = 1e-4, tmax = 1e9) and its hit by
+ * the reference traversal; entries past a path's end hold tmax = -1.
+ * out_rays / out_hits: cw*ch*spp*bmax entries. */
+void orc_dump_rays(const orc_scene *scene, const orc_camera *cam, uint32_t w, uint32_t h, uint32_t x0, uint32_t y0,
+                   uint32_t cw, uint32_t ch, uint32_t spp, uint32_t first_frame, uint32_t max_depth, uint32_t flags,
+                   uint32_t bmax, orc_ray *out_rays, orc_hit *out_hits, int threads);
 
 /* Brute-force gradient of an image loss with respect to the material
  * parameters, by forward-mode differentiation of every sampled path:

@@ -26,6 +26,9 @@ VERTEX = np.dtype([("position", "<f4", 4), ("normal", "<f4", 4), ("uv", "<f4", 4
 TRIANGLE = np.dtype([("v", "<u4", 3), ("mat_idx", "<u4")])
 RAY = np.dtype([("org", "<f4", 3), ("tmin", "<f4"), ("dir", "<f4", 3), ("tmax", "<f4")])
 HIT = np.dtype([("t", "<f4"), ("prim", "<u4"), ("u", "<f4"), ("v", "<f4")])
+CAMERA = np.dtype([("origin", "<f4", 4), ("lower_left", "<f4", 4), ("horizontal", "<f4", 4),
+                   ("vertical", "<f4", 4), ("defocus_u", "<f4", 4), ("defocus_v", "<f4", 4),
+                   ("frame_count", "<u4"), ("pad", "<u4", 3)])
 NEE = 1   # ORC_RENDER_NEE
 
 
@@ -189,6 +192,23 @@ class OracleScene:
             out["stats"] = dict(rays=int(st[0]), nodes=int(st[1]), prims=int(st[2]))
         return out
 
+    def dump_rays(self, camera, w, h, spp, rect=None, first_frame=0, max_depth=8, nee=False, bounces=4, threads=0):
+        """The closest-hit queries of the rect's sampled paths, bounces 0 .. bounces-1:
+        (rays, hits, bounce) of the queries the paths reach, in (pixel, frame, bounce) order."""
+        L = lib()
+        L.orc_dump_rays.restype = None
+        L.orc_dump_rays.argtypes = [POINTER(_Scene), c_void_p] + [c_uint32] * 11 + [c_void_p, c_void_p, c_int]
+        cam = np.ascontiguousarray(camera)
+        x0, y0, cw, ch = rect if rect else (0, 0, w, h)
+        n = cw * ch * spp * bounces
+        rays = np.zeros(n, RAY)
+        hits = np.zeros(n, HIT)
+        L.orc_dump_rays(ctypes.byref(self._s), _p(cam), w, h, x0, y0, cw, ch, spp, first_frame, max_depth,
+                        NEE if nee else 0, bounces, _p(rays), _p(hits), threads)
+        bounce = np.tile(np.arange(bounces, dtype=np.uint32), cw * ch * spp)
+        keep = rays["tmax"] > 0
+        return rays[keep], hits[keep], bounce[keep]
+
     def render_cache_const(self, camera, w, h, spp, c3, spp_pass, train_stride, query_vertex, first_frame=0,
                            max_depth=8, nee=False, threads=0):
         """Render with paths stopped into a constant radiance cache (see oracle.h)."""
@@ -216,6 +236,22 @@ class OracleScene:
         lib().orc_adjoint(ctypes.byref(self._s), _p(cam), w, h, spp, first_frame, max_depth, NEE if nee else 0,
                           _p(d), _p(grad), _p(acc), threads)
         return grad.reshape(64, 4), acc
+
+
+def compute_camera(width, height, look_from, look_at, vfov=60.0, aperture=0.0, focus_dist=None):
+    """CameraUniform (structured CAMERA record) of camera.rs:76-127; focus_dist defaults to
+    |look_from - look_at| in float32."""
+    L = lib()
+    L.orc_compute_camera.restype = None
+    L.orc_compute_camera.argtypes = [c_uint32, c_uint32, c_void_p, c_void_p, c_float, c_float, c_float, c_void_p]
+    lf = np.ascontiguousarray(look_from, np.float32)
+    la = np.ascontiguousarray(look_at, np.float32)
+    if focus_dist is None:
+        d = lf - la
+        focus_dist = float(np.sqrt(np.float32(d[0] * d[0] + d[1] * d[1]) + np.float32(d[2] * d[2])))
+    out = np.zeros((), CAMERA)
+    L.orc_compute_camera(width, height, _p(lf), _p(la), vfov, aperture, focus_dist, _p(out))
+    return out
 
 
 def denoise(rgba, gbuf, radius=3, sigma_s=2.0, sigma_d=0.5, normal_pow=8.0, sigma_color=0.0, sigma_normal=0.0):
