@@ -78,7 +78,10 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--small", action="store_true",
                    help="same scene at 480x270, 4 spp: the profiling case (not a bench line)")
-    p.add_argument("--leg", choices=["bvh_build", "cache_mlp", "frame", "adjoint", "nee"],
+    p.add_argument("--mid", action="store_true",
+                   help="same scene at 960x540, 16 spp (2 GB of path state): the profiling case for counter "
+                        "sets that need several passes (not a bench line)")
+    p.add_argument("--leg", choices=["bvh_build", "cache_mlp", "frame", "adjoint", "nee", "roofline_inputs"],
                    help="profiling case: only the GPU BVH builds of the workload's mesh, only the "
                         "radiance-cache MLP (2^18 queries), only frames of the workload (autotune: 8 "
                         "frames, then rebuild + render with the chosen closest-hit variant, 12 extend "
@@ -86,10 +89,14 @@ def parse():
                         "of the time-to-relMSE scene (Cornell 512x512, 128 spp, depth 8) without and with "
                         "NEE; prints its timings, not a bench line")
     a = p.parse_args()
+    global W, H, SPP, WORKLOAD
     if a.small:
-        global W, H, SPP, WORKLOAD
         W, H, SPP = 480, 270, 4
         WORKLOAD = WORKLOAD.replace("1920x1080_16spp", "480x270_4spp")
+    elif a.mid:
+        W, H = 960, 540
+        WORKLOAD = WORKLOAD.replace("1920x1080", "960x540")
+    a.small = a.small or a.mid
     return a
 
 
@@ -641,8 +648,22 @@ def run_mcrt(args):
         print(json.dumps({"leg": "bvh_build", "triangles": int(len(sc["triangles"])), "ms": ms,
                           "launches_per_build": builds[-1][1]}))
         return
+    if args.leg == "roofline_inputs":
+        variant, _ = ctx.autotune(cam, W, H, SPP, max_depth=DEPTH)
+        out = {"leg": "roofline_inputs", "workload": WORKLOAD, "variant": variant,
+               "copy_gbs": {f"{mb}MB": round(ctx.copy_bandwidth(mb << 20, 50), 1) for mb in (8, 16, 32, 48, 64, 96)}}
+        out["copy_gbs"]["2048MB"] = round(ctx.copy_bandwidth(2048 << 20, 10), 1)
+        ctx.rebuild_bvh()
+        ctx.render(cam, W, H, SPP, first_frame=0, max_depth=DEPTH, outputs=(), count=True)
+        t = ctx.timings()
+        out["counted"] = {k: int(t[k]) for k in ("rays", "node_fetches", "triangle_fetches", "extend_launches")}
+        ctx.rebuild_bvh()
+        ctx.render(cam, W, H, SPP, first_frame=0, max_depth=DEPTH, outputs=())
+        out["extend_ms"] = round(ctx.timings()["extend_ms"], 3)
+        print(json.dumps(out))
+        return
     if args.leg == "frame":
-        variant, _ = ctx.autotune(cam, W, H, SPP, max_depth=DEPTH)        # 8 frames, 12 extend launches each
+        variant, tune_ms = ctx.autotune(cam, W, H, SPP, max_depth=DEPTH)  # 8 frames, 12 extend launches each
         frames = []
         for i in range(args.warmup + args.steps):
             ctx.rebuild_bvh()
@@ -650,7 +671,8 @@ def run_mcrt(args):
             t = ctx.timings()
             frames.append({k: round(t[k], 3) for k in ("extend_ms", "shade_ms", "total_ms")} |
                           {"rays": t["rays"], "extend_launches": t["extend_launches"]})
-        print(json.dumps({"leg": "frame", "workload": WORKLOAD, "frames": frames[args.warmup:]}))
+        print(json.dumps({"leg": "frame", "workload": WORKLOAD, "variant": variant,
+                          "autotune_extend_ms": [round(x, 3) for x in tune_ms], "frames": frames[args.warmup:]}))
         return
     # set-up, outside the timed region: one frame of the workload per variant
     variant, tune_ms = ctx.autotune(cam, W, H, SPP, max_depth=DEPTH)

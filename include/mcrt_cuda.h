@@ -194,9 +194,13 @@ enum {
     MCRT_RENDER_KEEP_ACCUM = 1u << 2, /* continue the device running mean / f64 sum of the previous call */
     MCRT_RENDER_GRAPH = 1u << 3,      /* replay the passes as one captured CUDA graph (same results; no
                                          per-kernel timings for the replayed passes) */
-    MCRT_RENDER_CACHE = 1u << 4       /* terminate paths into the radiance cache and train it online
+    MCRT_RENDER_CACHE = 1u << 4,      /* terminate paths into the radiance cache and train it online
                                          (mcrt_cache_config); with MCRT_RENDER_GRAPH the cached passes,
                                          training included, are replayed as a graph too */
+    MCRT_RENDER_COUNT = 1u << 5       /* the closest-hit kernels count their record fetches (internal
+                                         nodes visited, triangles tested; counters [6], [7] of
+                                         mcrt_last_timings): the bytes-per-ray model of the traversal;
+                                         same image, slower kernels (not for timed runs) */
 };
 
 typedef struct {
@@ -460,8 +464,19 @@ mcrt_status mcrt_read_image_rgba8(mcrt_ctx *ctx, uint32_t mode, uint8_t *out);
  * launches of the last render, [3] kernel launches of the last BVH build,
  * [4] extend launches of the last render, [5] rays of the last render traced
  * by the stackless walk because the traversal stack was too short for the
- * tree (included in [0] and [1]).  out_ms: 6 floats, out_counts: 6 uint64. */
+ * tree (included in [0] and [1]), [6] / [7] with MCRT_RENDER_COUNT: compact
+ * BVH node records (64 B) and triangle records (48 B) the closest-hit kernels
+ * fetched (the bounce-0 warp packets fetch one record per warp).
+ * out_ms: 6 floats, out_counts: 8 uint64. */
 mcrt_status mcrt_last_timings(mcrt_ctx *ctx, float *out_ms, uint64_t *out_counts);
+
+/* Copy bandwidth of a plain float4 copy kernel over two `bytes`-sized device
+ * buffers (a warm-up launch, then one launch that copies back and forth `reps`
+ * times, timed on the context stream): out_gbs = 2 * bytes * reps / time
+ * (read + write).  Buffers that fit the L2 give its bandwidth, buffers far
+ * larger than it the HBM's: the measured denominators of the kernels'
+ * rooflines.  Allocates and frees its buffers.  (No reference counterpart.) */
+mcrt_status mcrt_copy_bandwidth(mcrt_ctx *ctx, uint64_t bytes, uint32_t reps, float *out_gbs);
 
 /* ------------------------------------------------------------------ denoiser */
 

@@ -314,15 +314,17 @@ class Context:
         return hits
 
     def render(self, camera, width, height, spp, first_frame=0, max_depth=0, nee=False, spp_per_pass=0,
-               keep=False, outputs=("rgba", "sum", "gbuf"), graph=False, cache=False, out_rgba=None, variant=None):
+               keep=False, outputs=("rgba", "sum", "gbuf"), graph=False, cache=False, out_rgba=None, variant=None,
+               count=False):
         """Render; outputs names the host arrays to return.  out_rgba: a caller-owned (height, width, 4)
         float32 C-contiguous array (pinned host memory for the fastest copy) that receives the image.
-        variant: a closest-hit kernel variant (0..7) instead of the context's autotuned one."""
+        variant: a closest-hit kernel variant (0..7) instead of the context's autotuned one.
+        count: the closest-hit kernels count their node and triangle record fetches (timings())."""
         cam = _arr(camera, CAMERA)
         o = N.RenderOpts(max_depth=max_depth, flags=(N.RENDER_NEE if nee else 0) |
                          (N.RENDER_KEEP_ACCUM if keep else 0) | (N.RENDER_GRAPH if graph else 0) |
-                         (N.RENDER_CACHE if cache else 0), spp_per_pass=spp_per_pass,
-                         variant=0 if variant is None else variant + 1)
+                         (N.RENDER_CACHE if cache else 0) | (N.RENDER_COUNT if count else 0),
+                         spp_per_pass=spp_per_pass, variant=0 if variant is None else variant + 1)
         if out_rgba is not None:
             if (out_rgba.dtype != np.float32 or out_rgba.shape != (height, width, 4)
                     or not out_rgba.flags["C_CONTIGUOUS"]):
@@ -467,7 +469,7 @@ class Context:
 
     def timings(self):
         ms = (c_float * 6)()
-        cnt = (c_uint64 * 6)()
+        cnt = (c_uint64 * 8)()
         self._check(lib().mcrt_last_timings(self._h, ms, cnt))
         keys = ["total", "extend", "shade", "shadow", "resolve", "bvh_build"]
         d = {f"{k}_ms": ms[i] for i, k in enumerate(keys)}
@@ -477,7 +479,15 @@ class Context:
         d["build_launches"] = cnt[3]
         d["extend_launches"] = cnt[4]
         d["stackless_rays"] = cnt[5]
+        d["node_fetches"] = cnt[6]
+        d["triangle_fetches"] = cnt[7]
         return d
+
+    def copy_bandwidth(self, nbytes, reps=20):
+        """GB/s (read + write) of the library's float4 copy kernel over two nbytes buffers."""
+        g = c_float()
+        self._check(lib().mcrt_copy_bandwidth(self._h, int(nbytes), int(reps), ctypes.byref(g)))
+        return g.value
 
     def denoise_accum(self, radius=3, sigma_s=2.0, sigma_d=0.5, normal_pow=8.0, sigma_color=0.0, sigma_normal=0.0,
                       read_back=True):

@@ -73,6 +73,7 @@ class CacheParams(ctypes.Structure):
 
 
 RENDER_CACHE = 16
+RENDER_COUNT = 32
 SCENE_WORLD_MESH = 1
 MESH_GREEDY, MESH_FACES = 0, 1
 
@@ -151,6 +152,7 @@ SIGNATURES = [
     ("mcrt_tonemap_aces_rgba8", c_int, [c_void_p, c_uint32, c_void_p]),
     ("mcrt_write_hdr", c_int, [c_char_p, c_void_p, c_uint32, c_uint32]),
     ("mcrt_last_timings", c_int, [c_void_p, POINTER(c_float), POINTER(c_uint64)]),
+    ("mcrt_copy_bandwidth", c_int, [c_void_p, c_uint64, c_uint32, POINTER(c_float)]),
     ("mcrt_denoise", c_int, [c_void_p, c_void_p, c_void_p, c_uint32, c_uint32, POINTER(DenoiseParams), c_void_p]),
     ("mcrt_scene_load_yaml", c_int, [c_char_p, POINTER(c_void_p)]),
     ("mcrt_scene_load_yaml_str", c_int, [c_char_p, c_char_p, POINTER(c_void_p)]),

@@ -75,7 +75,8 @@ struct mcrt_ctx {
     // timing
     std::vector<cudaEvent_t> ev_pool;
     float last_ms[6] = {0, 0, 0, 0, 0, 0};
-    unsigned long long last_counts[3] = {0, 0, 0};   // rays, shadow rays, rays traced stackless
+    // rays, shadow rays, rays traced stackless, node and triangle records fetched (MCRT_RENDER_COUNT)
+    unsigned long long last_counts[5] = {0, 0, 0, 0, 0};
     unsigned long long last_render_launches = 0, last_build_launches = 0, last_extend_launches = 0;
     float last_build_ms = 0.0f;
     int extend_variant = 0;   // chosen by mcrt_autotune
@@ -1300,6 +1301,56 @@ mcrt_status mcrt_read_image_rgba8(mcrt_ctx *ctx, uint32_t mode, uint8_t *out) {
     return MCRT_OK;
 }
 
+// A plain copy, float4 per thread and step, `reps` times in one launch (even
+// repetitions a -> b, odd ones b -> a; each thread copies its own elements, so
+// repetition r + 1 reads what the same thread wrote in r): the denominator of
+// a roofline, with no launch gaps between repetitions.
+__global__ void k_copy_float4(float4 *a, float4 *b, size_t n, uint32_t reps) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (uint32_t r = 0; r < reps; ++r) {
+        const float4 *src = (r & 1u) ? b : a;
+        float4 *dst = (r & 1u) ? a : b;
+        size_t i = i0;
+        for (; i + 3 * stride < n; i += 4 * stride) {
+            const float4 v0 = src[i], v1 = src[i + stride], v2 = src[i + 2 * stride], v3 = src[i + 3 * stride];
+            dst[i] = v0; dst[i + stride] = v1; dst[i + 2 * stride] = v2; dst[i + 3 * stride] = v3;
+        }
+        for (; i < n; i += stride) dst[i] = src[i];
+    }
+}
+
+mcrt_status mcrt_copy_bandwidth(mcrt_ctx *ctx, uint64_t bytes, uint32_t reps, float *out_gbs) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (!out_gbs || bytes < 16 || reps == 0 || bytes > (1ull << 36))
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "out_gbs required, 16 <= bytes <= 2^36, reps > 0");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const size_t n = (size_t)(bytes / 16);
+    void *src = nullptr, *dst = nullptr;
+    CK(cudaMalloc(&src, n * 16), "allocate copy source");
+    cudaError_t e = cudaMalloc(&dst, n * 16);
+    if (e != cudaSuccess) { cudaFree(src); return cuda_fail(ctx, e, "allocate copy destination"); }
+    cudaStream_t st = ctx->stream;
+    cudaMemsetAsync(src, 0, n * 16, st);
+    const int blocks = mcrt::sm_count() * 8;
+    cudaEvent_t a = ev(ctx, 0), b = ev(ctx, 1);
+    float4 *fa = static_cast<float4 *>(src), *fb = static_cast<float4 *>(dst);
+    k_copy_float4<<<blocks, 256, 0, st>>>(fa, fb, n, 4);   // warm-up: the buffers resident where they fit
+    ::mcrt::note_launch();
+    cudaEventRecord(a, st);
+    k_copy_float4<<<blocks, 256, 0, st>>>(fa, fb, n, reps);
+    ::mcrt::note_launch();
+    cudaEventRecord(b, st);
+    e = cudaEventSynchronize(b);
+    float ms = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    cudaFree(src);
+    cudaFree(dst);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "copy bandwidth");
+    *out_gbs = (float)(2.0 * (double)n * 16.0 * reps / (ms * 1e-3) / 1e9);
+    return MCRT_OK;
+}
+
 mcrt_status mcrt_last_timings(mcrt_ctx *ctx, float *out_ms, uint64_t *out_counts) {
     if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
     if (out_ms) {
@@ -1313,6 +1364,8 @@ mcrt_status mcrt_last_timings(mcrt_ctx *ctx, float *out_ms, uint64_t *out_counts
         out_counts[3] = ctx->last_build_launches;
         out_counts[4] = ctx->last_extend_launches;
         out_counts[5] = ctx->last_counts[2];
+        out_counts[6] = ctx->last_counts[3];
+        out_counts[7] = ctx->last_counts[4];
     }
     return MCRT_OK;
 }

@@ -661,7 +661,10 @@ constexpr uint32_t kOvfClosest = 3u, kOvfAny = 7u;
 // gradients collected in shared memory per block and added once per block.
 // A ray whose next push would overflow the stack stops here and joins the
 // overflow list (finished by k_extend_retry).
-template <int WIDTH, int BLOCK, int MINB, int STACK, int REFILL, bool ANY, bool ADJ>
+// COUNT: the traversal's own record fetches, for the bytes-per-ray model of
+// the kernel (outside timed runs): stats[3] += internal nodes visited (one
+// 64-byte record each), stats[4] += triangles tested (one 48-byte record each).
+template <int WIDTH, int BLOCK, int MINB, int STACK, int REFILL, bool ANY, bool ADJ, bool COUNT = false>
 __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffers B, int qi, AdjointParams A) {
     __shared__ float gacc[ADJ ? 256 : 1];
     if (ADJ) {
@@ -688,6 +691,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
     uint32_t leaf = kNoChild;         // postponed leaf code
     uint32_t traced = 0;
     uint32_t nn = 0;
+    uint32_t ntri = 0;                // COUNT: triangles tested
     uint32_t slot = 0;                // ANY: the shadow ray's path
     bool occl = false;                // ANY: an accepted hit was found
     // a ray whose stack would overflow keeps its queue index with bit 31 set
@@ -777,7 +781,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
                         sp = 0;
                     }
                 } else {
-                    leaf_tris(S, r, (leaf & ~kLeafBit) >> 4, leaf_count(S, leaf), kTMin, best);
+                    const uint32_t cnt = leaf_count(S, leaf);
+                    if (COUNT) ntri += cnt;
+                    leaf_tris(S, r, (leaf & ~kLeafBit) >> 4, cnt, kTMin, best);
                 }
                 leaf = kNoChild;
                 if (cur != kNoChild && (cur & kLeafBit) && cur_t <= cull_t(best.t)) {
@@ -798,6 +804,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
         }
     }
     if (traced) atomicAdd(B.stats + (ANY ? 1 : 0), (unsigned long long)traced);
+    if (COUNT) {
+        atomicAdd(B.stats + 3, (unsigned long long)nn);
+        atomicAdd(B.stats + 4, (unsigned long long)ntri);
+    }
     if (ADJ) {
         __syncthreads();
         for (uint32_t k = threadIdx.x; k < 256u; k += BLOCK) {
@@ -871,8 +881,11 @@ __global__ void __launch_bounds__(kRetryBlock) k_extend_retry(DeviceScene S, Pat
 //    lanes that entered it; popped entries no lane can still reach are dropped.
 //    A packet whose stack would overflow joins the overflow list (its rays
 //    are traced again by k_extend_retry).
+//  * COUNT: the warp's record fetches (one per node or triangle for the whole
+//    packet) into stats[3] / stats[4], as k_extend's COUNT.
 constexpr int kPacketBlock = 128;
 constexpr uint32_t kPacketStack = 64;
+template <bool COUNT = false>
 __global__ void __launch_bounds__(kPacketBlock) k_extend_packet(DeviceScene S, PathBuffers B, int qi) {
     const uint32_t n = B.counters[qi];
     if (blockIdx.x == 0 && threadIdx.x == 0) { B.counters[qi ^ 1] = 0; B.counters[2] = 0; B.counters[kOvfAny] = 0; }
@@ -880,7 +893,7 @@ __global__ void __launch_bounds__(kPacketBlock) k_extend_packet(DeviceScene S, P
     const uint32_t warp = (blockIdx.x * kPacketBlock + threadIdx.x) >> 5;
     const uint32_t n_warps = (gridDim.x * kPacketBlock) >> 5;
     const bool has_mesh = S.n_mesh_nodes > 0;
-    uint32_t traced = 0, nn = 0;
+    uint32_t traced = 0, nn = 0, nodes = 0, ntri = 0;
     for (uint32_t base = warp * 32u; base < n; base += n_warps * 32u) {
         const uint32_t ray = base + lane;
         const bool active = ray < n;
@@ -912,9 +925,11 @@ __global__ void __launch_bounds__(kPacketBlock) k_extend_packet(DeviceScene S, P
         bool ovf = false;                               // warp-uniform
         while (cur != kNoChild) {
             if (cur & kLeafBit) {
+                if (COUNT && lane == 0) ntri += leaf_count(S, cur);
                 if (active) leaf_tris(S, r, (cur & ~kLeafBit) >> 4, leaf_count(S, cur), kTMin, best);
                 cur = kNoChild;
             } else {
+                if (COUNT && lane == 0) ++nodes;
                 const float4 *np = S.cnodes + 4ull * cur;
                 const float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
                 const uint4 e = __ldg(reinterpret_cast<const uint4 *>(np + 3));
@@ -973,6 +988,10 @@ __global__ void __launch_bounds__(kPacketBlock) k_extend_packet(DeviceScene S, P
         }
     }
     if (traced) atomicAdd(B.stats, (unsigned long long)traced);
+    if (COUNT && lane == 0) {
+        atomicAdd(B.stats + 3, (unsigned long long)nodes);
+        atomicAdd(B.stats + 4, (unsigned long long)ntri);
+    }
 }
 
 // Shading of the queued hits.  ADJ = false: the forward estimator.  ADJ = true:
@@ -1426,12 +1445,21 @@ const ExtendKernel kExtendKernels[kExtendVariants] = MCRT_EXTEND_TABLE(false, fa
 const ExtendKernel kShadowKernels[kExtendVariants] = MCRT_EXTEND_TABLE(true, false);
 // the same for the adjoint replay, which adds gradients per unoccluded shadow ray
 const ExtendKernel kShadowAdjKernels[kExtendVariants] = MCRT_EXTEND_TABLE(true, true);
+// the closest-hit instantiations that count their record fetches (MCRT_RENDER_COUNT)
+#define MCRT_COUNT_KERNEL(i)                                                                            \
+    k_extend<kVariantTable[i].width, kVariantTable[i].block, kVariantTable[i].min_blocks, kVariantTable[i].stack, \
+             kVariantTable[i].refill, false, false, true>
+const ExtendKernel kCountKernels[kExtendVariants] = {
+    MCRT_COUNT_KERNEL(0), MCRT_COUNT_KERNEL(1), MCRT_COUNT_KERNEL(2), MCRT_COUNT_KERNEL(3),
+    MCRT_COUNT_KERNEL(4), MCRT_COUNT_KERNEL(5), MCRT_COUNT_KERNEL(6), MCRT_COUNT_KERNEL(7)};
+#undef MCRT_COUNT_KERNEL
 #undef MCRT_EXTEND_TABLE
 #undef MCRT_EXTEND_KERNEL
 int g_extend_per_sm[kExtendVariants] = {0, 0, 0, 0, 0, 0, 0, 0};
 int g_shadow_per_sm[kExtendVariants] = {0, 0, 0, 0, 0, 0, 0, 0};
 int g_shadow_adj_per_sm[kExtendVariants] = {0, 0, 0, 0, 0, 0, 0, 0};
 int g_packet_per_sm = 0;
+int g_count_per_sm[kExtendVariants] = {0, 0, 0, 0, 0, 0, 0, 0};
 }  // namespace
 
 void extend_variant_info(int v, int out[5]) {
@@ -1444,7 +1472,7 @@ void extend_variant_info(int v, int out[5]) {
 void prepare_extend_variants() {
     if (g_packet_per_sm == 0) {
         int n = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_extend_packet, kPacketBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_extend_packet<false>, kPacketBlock, 0);
         g_packet_per_sm = n > 0 ? n : 1;
     }
     for (int v = 0; v < kExtendVariants; ++v) {
@@ -1462,6 +1490,11 @@ void prepare_extend_variants() {
             int n = 0;
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kShadowAdjKernels[v], kVariantTable[v].block, 0);
             g_shadow_adj_per_sm[v] = n > 0 ? n : 1;
+        }
+        if (g_count_per_sm[v] == 0) {
+            int n = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kCountKernels[v], kVariantTable[v].block, 0);
+            g_count_per_sm[v] = n > 0 ? n : 1;
         }
     }
 }
@@ -1481,14 +1514,19 @@ void launch_extend(const DeviceScene &S, const RenderParams &P, PathBuffers &B, 
     const int v = (P.extend_variant >= 0 && P.extend_variant < kExtendVariants) ? P.extend_variant : 0;
     prepare_extend_variants();
     const uint32_t nmax = P.npix * P.spp_pass;
+    const bool count = (P.flags & MCRT_RENDER_COUNT) != 0;
     if (primary) {                    // the camera rays: warp packets, every warp resident at once
         const int blocks = min(grid_blocks_for(nmax, kPacketBlock), sm_count() * g_packet_per_sm);
-        k_extend_packet<<<blocks, kPacketBlock, 0, st>>>(S, B, qi); ::mcrt::note_launch();
+        if (count) k_extend_packet<true><<<blocks, kPacketBlock, 0, st>>>(S, B, qi);
+        else k_extend_packet<false><<<blocks, kPacketBlock, 0, st>>>(S, B, qi);
+        ::mcrt::note_launch();
     } else {
         // persistent: as many resident blocks as fit, never more warps than rays
         const int block = kVariantTable[v].block;
-        const int blocks = min(grid_blocks_for(nmax, block), sm_count() * g_extend_per_sm[v]);
-        kExtendKernels[v]<<<blocks, block, 0, st>>>(S, B, qi, AdjointParams{}); ::mcrt::note_launch();
+        const int per_sm = count ? g_count_per_sm[v] : g_extend_per_sm[v];
+        const int blocks = min(grid_blocks_for(nmax, block), sm_count() * per_sm);
+        (count ? kCountKernels[v] : kExtendKernels[v])<<<blocks, block, 0, st>>>(S, B, qi, AdjointParams{});
+        ::mcrt::note_launch();
     }
     launch_retry(S, B, qi, false, nullptr, st);
 }
