@@ -212,15 +212,17 @@ typedef struct {
 
 /* Autotuner (no reference counterpart): renders `spp` frames of w x h with each
  * closest-hit kernel variant — BVH width (compact binary / quantised 4-wide),
- * block size, register budget (minimum resident blocks) and traversal stack
- * depth, see mcrt_variant_info — keeps the fastest for this context and
+ * block size, register budget (minimum resident blocks), traversal stack
+ * depth and shared-memory staging of the tree's top levels, see
+ * mcrt_variant_info — keeps the fastest for this context and
  * reports it.  Every variant gives the same images: a ray whose stack would
  * overflow is traced again without a stack, which costs its variant time on
  * a deep tree but never a hit.  out_ms (optional) receives the extend time of
  * every variant; its capacity is 8 floats. */
-/* out5: BVH width, block size, minimum resident blocks per SM, stack depth,
- * idle lanes at which a warp fetches new rays */
-mcrt_status mcrt_variant_info(uint32_t variant, uint32_t *out5);
+/* out6: BVH width, block size, minimum resident blocks per SM, stack depth,
+ * idle lanes at which a warp fetches new rays, records of the compact tree's
+ * top levels staged in shared memory per block (0: none) */
+mcrt_status mcrt_variant_info(uint32_t variant, uint32_t *out6);
 mcrt_status mcrt_autotune(mcrt_ctx *ctx, const mcrt_camera_uniform *cam, uint32_t w, uint32_t h, uint32_t spp,
                           const mcrt_render_opts *opts, uint32_t *out_variant, float *out_ms);
 

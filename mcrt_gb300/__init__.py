@@ -172,10 +172,11 @@ def materials(entries) -> np.ndarray:
 
 
 def variant_info(variant: int) -> dict:
-    """Closest-hit kernel variant: BVH width, block size, minimum resident blocks, stack depth."""
-    out = (c_uint32 * 5)()
+    """Closest-hit kernel variant: BVH width, block size, minimum resident blocks, stack depth, refill
+    lanes, shared-memory top-tree records."""
+    out = (c_uint32 * 6)()
     check(lib().mcrt_variant_info(variant, out))
-    return dict(width=out[0], block=out[1], min_blocks=out[2], stack=out[3], refill=out[4])
+    return dict(width=out[0], block=out[1], min_blocks=out[2], stack=out[3], refill=out[4], top=out[5])
 
 
 def make_rays(org, dirs, tmin=1e-4, tmax=1e9) -> np.ndarray:

@@ -57,7 +57,7 @@ struct mcrt_ctx {
     uint32_t n_wnodes = 0;
     bool wide_valid = false;    // wnodes matches the current mesh BVH
     DBuf spheres, sphere_ids, sphere_nodes, vertices, triangles, mesh_nodes, tri_order, trirecs, cnodes, materials,
-        env, lights, light_cdf, tmp, staging, albedo, shade_recs;
+        env, lights, light_cdf, tmp, staging, albedo, shade_recs, top;
     uint32_t albedo_layers = 0, albedo_size = 0;
     size_t srgb_lut_offset = 0;
     uint32_t n_spheres = 0, n_sphere_nodes = 0, n_vertices = 0, n_triangles = 0, n_mesh_nodes = 0, n_cnodes = 0,
@@ -145,6 +145,7 @@ mcrt::DeviceScene device_scene(const mcrt_ctx *c) {
     S.shade_recs = c->shade_recs.as<float4>();
     S.cnodes = c->cnodes.as<float4>();
     S.n_cnodes = c->n_cnodes;
+    S.top = c->top.as<float4>();
     S.wnodes = c->wnodes.as<uint4>();
     S.n_wnodes = c->n_wnodes;
     S.materials = c->materials.as<mcrt_gpu_material_data>();
@@ -247,6 +248,9 @@ mcrt_status finish_mesh(mcrt_ctx *ctx) {
                               &ncn, ctx->trirecs.p, ctx->tmp.as<uint32_t>(), tmp_words, st),
        "compact BVH");
     ctx->n_cnodes = ncn;
+    if (ncn >= mcrt::kTopBit) return fail(ctx, MCRT_ERR_INVALID_ARG, "mesh too large for the compact BVH codes");
+    CK(ctx->top.ensure((size_t)mcrt::kTopNodes * 64), "allocate top tree");
+    CK(mcrt::gpu_make_top(cn, ncn, ctx->top.as<float4>(), st), "top tree");
     ctx->wide_valid = false;                  // the 4-wide layout is built when a render first needs it
     ctx->n_wnodes = 0;
     return MCRT_OK;
@@ -274,7 +278,7 @@ mcrt_status ensure_wide(mcrt_ctx *ctx) {
 mcrt_status render_variant(mcrt_ctx *ctx, const mcrt_render_opts &o, int *variant) {
     const int v = o.variant ? (int)o.variant - 1 : ctx->extend_variant;
     if (v < 0 || v >= mcrt::extend_variant_count()) return fail(ctx, MCRT_ERR_INVALID_ARG, "variant out of range");
-    int info[5];
+    int info[6];
     mcrt::extend_variant_info(v, info);
     if (info[0] == 4) {
         mcrt_status s = ensure_wide(ctx);
@@ -394,7 +398,7 @@ void mcrt_destroy(mcrt_ctx *ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     DBuf *bufs[] = {&ctx->spheres, &ctx->sphere_ids, &ctx->sphere_nodes, &ctx->vertices, &ctx->triangles,
-                    &ctx->mesh_nodes, &ctx->tri_order, &ctx->trirecs, &ctx->cnodes, &ctx->materials, &ctx->env,
+                    &ctx->mesh_nodes, &ctx->tri_order, &ctx->trirecs, &ctx->cnodes, &ctx->top, &ctx->materials, &ctx->env,
                     &ctx->lights, &ctx->light_cdf, &ctx->tmp, &ctx->staging, &ctx->albedo, &ctx->wnodes, &ctx->pbmem, &ctx->mean,
                     &ctx->sum, &ctx->gbuf, &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->counters, &ctx->dimg,
                     &ctx->grad, &ctx->world_vox, &ctx->world_matmap, &ctx->wmesh.counts, &ctx->wmesh.vertices,
@@ -1252,12 +1256,12 @@ mcrt_status mcrt_read_accum(mcrt_ctx *ctx, float *out_rgba, double *accum_rgb, f
     return MCRT_OK;
 }
 
-mcrt_status mcrt_variant_info(uint32_t variant, uint32_t *out5) {
-    if (!out5 || variant >= (uint32_t)mcrt::extend_variant_count())
-        return fail(nullptr, MCRT_ERR_INVALID_ARG, "variant out of range or out5 NULL");
-    int info[5];
+mcrt_status mcrt_variant_info(uint32_t variant, uint32_t *out6) {
+    if (!out6 || variant >= (uint32_t)mcrt::extend_variant_count())
+        return fail(nullptr, MCRT_ERR_INVALID_ARG, "variant out of range or out6 NULL");
+    int info[6];
     mcrt::extend_variant_info((int)variant, info);
-    for (int k = 0; k < 5; ++k) out5[k] = (uint32_t)info[k];
+    for (int k = 0; k < 6; ++k) out6[k] = (uint32_t)info[k];
     return MCRT_OK;
 }
 
@@ -1609,7 +1613,7 @@ namespace mcrt {
 int context_variant(mcrt_ctx *ctx, const mcrt_render_opts &o) {
     const int v = o.variant ? (int)o.variant - 1 : ctx->extend_variant;
     if (v < 0 || v >= extend_variant_count()) return -1;
-    int info[5];
+    int info[6];
     extend_variant_info(v, info);
     if (info[0] == 4 && !(ctx->wide_valid && ctx->n_wnodes > 0)) return 0;
     return v;

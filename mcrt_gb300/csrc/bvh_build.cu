@@ -1501,6 +1501,47 @@ cudaError_t gpu_make_compact(const mcrt_gpu_bvh_node *d_nodes, uint32_t n_nodes,
     return cudaGetLastError();
 }
 
+// The top levels of the compact tree in heap order, for the shared-memory
+// top-tree traversal: entry 0 is the root, entry j's children go to 2j+1 and
+// 2j+2 while those fit (kTopNodes entries, 7 levels); an internal child that
+// gets an entry is recoded kTopBit | entry, every other child keeps its code
+// (a deeper internal node's compact index, a leaf, or none).  One block, one
+// thread per entry, a level per step.
+__global__ void k_top_tree(const float4 *cnodes, uint32_t n_cnodes, float4 *top) {
+    __shared__ uint32_t src[kTopNodes];            // compact index held by an entry, or kNoChild
+    const uint32_t j = threadIdx.x;
+    if (j < kTopNodes) src[j] = (j == 0 && n_cnodes > 0) ? 0u : kNoChild;
+    __syncthreads();
+    for (uint32_t first = 0, width = 1; first < kTopNodes; first += width, width *= 2) {
+        if (j >= first && j < first + width && j < kTopNodes) {
+            float4 r[4] = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f),
+                           make_float4(0.f, 0.f, 0.f, 0.f),
+                           make_float4(__uint_as_float(kNoChild), __uint_as_float(kNoChild), 0.f, 0.f)};
+            if (src[j] != kNoChild) {
+                const float4 *np = cnodes + 4ull * src[j];
+                for (int k = 0; k < 4; ++k) r[k] = np[k];
+                uint32_t code[2] = {__float_as_uint(r[3].x), __float_as_uint(r[3].y)};
+                for (int side = 0; side < 2; ++side) {
+                    const uint32_t slot = 2 * j + 1 + side;
+                    if (code[side] != kNoChild && !(code[side] & kLeafBit) && slot < kTopNodes) {
+                        src[slot] = code[side];
+                        code[side] = kTopBit | slot;
+                    }
+                }
+                r[3].x = __uint_as_float(code[0]);
+                r[3].y = __uint_as_float(code[1]);
+            }
+            for (int k = 0; k < 4; ++k) top[4ull * j + k] = r[k];
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t gpu_make_top(const float4 *d_cnodes, uint32_t n_cnodes, float4 *d_top, cudaStream_t st) {
+    k_top_tree<<<1, 128, 0, st>>>(d_cnodes, n_cnodes, d_top); ::mcrt::note_launch();
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ quantised 4-wide layout
 // Collapse of the reference-layout binary BVH into 4-wide nodes (64 bytes):
 //   w0: origin.xyz (float, the node box minimum) | exponent bytes ex, ey, ez

@@ -35,6 +35,10 @@ constexpr uint32_t kDefaultBounces = 8u;
 // entered, so every traversal order gives the tie rule's answer over all
 // triangles the test accepts.
 constexpr float kCullSlack = 1.000244140625f;
+// Top levels of the compact BVH held in shared memory by the top-tree kernel
+// variants: 7 levels, 127 records of 64 bytes (8 KB per block).
+constexpr uint32_t kTopNodes = 127u;
+constexpr uint32_t kTopBit = 0x40000000u;   // node code of a top-tree entry (bit 31 clear: internal)
 __host__ __device__ __forceinline__ float cull_t(float t) { return t * kCullSlack; }
 
 // ---------------------------------------------------------------- vectors
@@ -106,6 +110,10 @@ struct DeviceScene {
     const TriRec *tris;
     // compact BVH2 (children boxes in the parent) for the fast traversal
     const float4 *cnodes; uint32_t n_cnodes;
+    // the compact tree's top levels in heap order (kTopNodes records: entry j's
+    // children at 2j+1, 2j+2), staged in shared memory by the top-tree variants;
+    // internal children inside it are coded kTopBit | entry
+    const float4 *top;
     // quantised 4-wide BVH collapsed from the same tree
     const uint4 *wnodes; uint32_t n_wnodes;
     const mcrt_gpu_material_data *materials;

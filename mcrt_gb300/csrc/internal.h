@@ -102,8 +102,9 @@ struct RenderParams {
 
 constexpr uint32_t kTrainRecordFloat4 = 6;
 int extend_variant_count();
-// (BVH width, block size, minimum resident blocks, stack depth, refill lanes) of a variant.
-void extend_variant_info(int v, int out[5]);
+// (BVH width, block size, minimum resident blocks, stack depth, refill lanes,
+// shared-memory top-tree records) of a variant.
+void extend_variant_info(int v, int out[6]);
 // Occupancy queries of every variant; call before capturing launches in a graph.
 void prepare_extend_variants();
 
@@ -143,6 +144,9 @@ cudaError_t gpu_make_compact(const mcrt_gpu_bvh_node *d_nodes, uint32_t n_nodes,
 // vertices and triangles in original order.
 void launch_shade_recs(const mcrt_gpu_vertex *d_verts, const mcrt_gpu_triangle *d_tris, uint32_t nt, float4 *out,
                        cudaStream_t st);
+
+// The compact tree's top levels in heap order (kTopNodes records of 64 B), see k_top_tree.
+cudaError_t gpu_make_top(const float4 *d_cnodes, uint32_t n_cnodes, float4 *d_top, cudaStream_t st);
 
 // Collapse into the quantised 4-wide layout (d_tmp: 2*n_nodes + 4 words).
 cudaError_t gpu_make_wide4(const mcrt_gpu_bvh_node *d_nodes, uint32_t n_nodes, uint4 *d_wide, uint32_t *n_wide,

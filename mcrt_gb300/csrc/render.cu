@@ -512,21 +512,34 @@ __global__ void k_raygen(DeviceScene S, RenderParams P, PathBuffers B, int keep_
 // bytes in local memory; a ray that would overflow it leaves the kernel's queue
 // for the overflow list, whose rays k_extend_retry traces without a stack, so
 // a short stack costs time on a deep tree but never a wrong or missing hit)
-// and the number of idle lanes at which a warp fetches new rays.
-struct ExtendVariant { int width, block, min_blocks, stack, refill; };
+// and the number of idle lanes at which a warp fetches new rays, and whether
+// the block stages the top 7 levels of the compact tree in shared memory
+// (top = kTopNodes records, 8 KB per block, loaded once per block; the nodes
+// below are read through L1 as in the other variants).
+struct ExtendVariant { int width, block, min_blocks, stack, refill, top; };
 constexpr int kExtendVariants = 8;
 constexpr ExtendVariant kVariantTable[kExtendVariants] = {
-    {2, 128, 8, 64, 8}, {2, 64, 20, 32, 8}, {2, 64, 20, 32, 4}, {2, 64, 20, 32, 16},
-    {2, 64, 22, 32, 8}, {4, 128, 8, 64, 8}, {2, 128, 10, 32, 8}, {2, 64, 18, 32, 8}};
+    {2, 128, 8, 64, 8, 0},  {2, 64, 20, 32, 8, 0},  {2, 64, 20, 32, 4, 0},   {2, 128, 10, 32, 8, (int)kTopNodes},
+    {2, 64, 18, 32, 8, (int)kTopNodes}, {4, 128, 8, 64, 8, 0}, {2, 128, 10, 32, 8, 0}, {2, 64, 18, 32, 8, 0}};
 
 // Visit an internal node of the compact binary layout: test both children,
-// continue with the nearer hit child, push the farther one.
-template <int STACK>
-__device__ __forceinline__ void visit_compact2(const DeviceScene &S, const RayInv &r, float tmax, uint32_t *cur,
-                                               float *cur_t, uint2 *stack, uint32_t *sp, bool *overflow) {
-    const float4 *np = S.cnodes + 4ull * *cur;
-    float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
-    uint4 e = __ldg(reinterpret_cast<const uint4 *>(np + 3));
+// continue with the nearer hit child, push the farther one.  TOP: a code with
+// kTopBit is an entry of the top tree staged in shared memory (s_top).
+template <int STACK, int TOP>
+__device__ __forceinline__ void visit_compact2(const DeviceScene &S, const float4 *s_top, const RayInv &r,
+                                               float tmax, uint32_t *cur, float *cur_t, uint2 *stack, uint32_t *sp,
+                                               bool *overflow) {
+    float4 a, b, c;
+    uint4 e;
+    if (TOP > 0 && (*cur & kTopBit)) {
+        const float4 *np = s_top + 4u * (*cur & ~kTopBit);
+        a = np[0]; b = np[1]; c = np[2];
+        e = *reinterpret_cast<const uint4 *>(np + 3);
+    } else {
+        const float4 *np = S.cnodes + 4ull * *cur;
+        a = __ldg(np); b = __ldg(np + 1); c = __ldg(np + 2);
+        e = __ldg(reinterpret_cast<const uint4 *>(np + 3));
+    }
     float tl, tr;
     bool hl = e.x != kNoChild && slab(r, a.x, a.z, c.x, a.y, a.w, c.y, kTMin, tmax, &tl);
     bool hr = e.y != kNoChild && slab(r, b.x, b.z, c.z, b.y, b.w, c.w, kTMin, tmax, &tr);
@@ -663,14 +676,21 @@ constexpr uint32_t kOvfClosest = 3u, kOvfAny = 7u;
 // overflow list (finished by k_extend_retry).
 // COUNT: the traversal's own record fetches, for the bytes-per-ray model of
 // the kernel (outside timed runs): stats[3] += internal nodes visited (one
-// 64-byte record each), stats[4] += triangles tested (one 48-byte record each).
-template <int WIDTH, int BLOCK, int MINB, int STACK, int REFILL, bool ANY, bool ADJ, bool COUNT = false>
+// 64-byte record each, those of the shared-memory top tree included),
+// stats[4] += triangles tested (one 48-byte record each).
+// TOP > 0 (binary layout): the block first copies the top tree (S.top, TOP
+// records) into shared memory and starts every ray at its entry 0.
+template <int WIDTH, int BLOCK, int MINB, int STACK, int REFILL, int TOP, bool ANY, bool ADJ, bool COUNT = false>
 __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffers B, int qi, AdjointParams A) {
     __shared__ float gacc[ADJ ? 256 : 1];
+    __shared__ float4 s_top[TOP > 0 ? 4 * TOP : 1];
     if (ADJ) {
         for (uint32_t k = threadIdx.x; k < 256u; k += BLOCK) gacc[k] = 0.0f;
-        __syncthreads();
     }
+    if constexpr (TOP > 0) {
+        for (uint32_t k = threadIdx.x; k < 4u * TOP; k += BLOCK) s_top[k] = __ldg(S.top + k);
+    }
+    if (ADJ || TOP > 0) __syncthreads();
     const uint32_t n = ANY ? B.counters[2] : B.counters[qi];
     if (!ANY && blockIdx.x == 0 && threadIdx.x == 0) {
         B.counters[qi ^ 1] = 0; B.counters[2] = 0; B.counters[kOvfAny] = 0;
@@ -733,7 +753,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
                                 uint4 meta = __ldg(reinterpret_cast<const uint4 *>(np + 2));
                                 cur = leaf_code(meta.x, meta.y);
                             } else {
-                                cur = 0;
+                                cur = TOP > 0 ? kTopBit : 0u;
                             }
                             cur_t = te;
                         }
@@ -762,7 +782,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_extend(DeviceScene S, PathBuffe
                 ++nn;
                 bool full = false;
                 if (WIDTH == 4) visit_wide4<STACK>(S, r, best.t, &cur, &cur_t, stack, &sp, &full);
-                else visit_compact2<STACK>(S, r, best.t, &cur, &cur_t, stack, &sp, &full);
+                else visit_compact2<STACK, TOP>(S, s_top, r, best.t, &cur, &cur_t, stack, &sp, &full);
                 if (full) {                                                   // to the overflow list
                     ray |= kOvfBit;
                     cur = kNoChild;
@@ -1435,7 +1455,7 @@ namespace {
 using ExtendKernel = void (*)(DeviceScene, PathBuffers, int, AdjointParams);
 #define MCRT_EXTEND_KERNEL(i, any, adj)                                                                  \
     k_extend<kVariantTable[i].width, kVariantTable[i].block, kVariantTable[i].min_blocks, kVariantTable[i].stack, \
-             kVariantTable[i].refill, any, adj>
+             kVariantTable[i].refill, kVariantTable[i].top, any, adj>
 #define MCRT_EXTEND_TABLE(any, adj)                                                                      \
     {MCRT_EXTEND_KERNEL(0, any, adj), MCRT_EXTEND_KERNEL(1, any, adj), MCRT_EXTEND_KERNEL(2, any, adj),    \
      MCRT_EXTEND_KERNEL(3, any, adj), MCRT_EXTEND_KERNEL(4, any, adj), MCRT_EXTEND_KERNEL(5, any, adj),    \
@@ -1448,7 +1468,7 @@ const ExtendKernel kShadowAdjKernels[kExtendVariants] = MCRT_EXTEND_TABLE(true, 
 // the closest-hit instantiations that count their record fetches (MCRT_RENDER_COUNT)
 #define MCRT_COUNT_KERNEL(i)                                                                            \
     k_extend<kVariantTable[i].width, kVariantTable[i].block, kVariantTable[i].min_blocks, kVariantTable[i].stack, \
-             kVariantTable[i].refill, false, false, true>
+             kVariantTable[i].refill, kVariantTable[i].top, false, false, true>
 const ExtendKernel kCountKernels[kExtendVariants] = {
     MCRT_COUNT_KERNEL(0), MCRT_COUNT_KERNEL(1), MCRT_COUNT_KERNEL(2), MCRT_COUNT_KERNEL(3),
     MCRT_COUNT_KERNEL(4), MCRT_COUNT_KERNEL(5), MCRT_COUNT_KERNEL(6), MCRT_COUNT_KERNEL(7)};
@@ -1462,9 +1482,9 @@ int g_packet_per_sm = 0;
 int g_count_per_sm[kExtendVariants] = {0, 0, 0, 0, 0, 0, 0, 0};
 }  // namespace
 
-void extend_variant_info(int v, int out[5]) {
+void extend_variant_info(int v, int out[6]) {
     const ExtendVariant &e = kVariantTable[(v >= 0 && v < kExtendVariants) ? v : 0];
-    out[0] = e.width; out[1] = e.block; out[2] = e.min_blocks; out[3] = e.stack; out[4] = e.refill;
+    out[0] = e.width; out[1] = e.block; out[2] = e.min_blocks; out[3] = e.stack; out[4] = e.refill; out[5] = e.top;
 }
 
 // Resident blocks per SM of every variant and of the packet kernel (occupancy
