@@ -10,10 +10,16 @@ Metric: Msamples/s = 1920*1080*16 / step time.
   e2e   : through the C ABI with host buffers: mcrt_update_vertices (vertex upload +
           rebuild) and mcrt_render returning the image to the host, copies inside the timer
 
-roofline : the closest-hit (extend) kernel against the bytes-per-ray memory roofline:
-           B_ray = 48 N_node + 64 N_tri + 48 bytes, N_node / N_tri = mean nodes visited and
-           triangles tested by the reference traversal of the reference BVH (oracle statistics
-           over a sample of the workload's own paths).
+roofline : the closest-hit kernels (12 launches per frame) against the measured HBM copy
+           bandwidth, with the bytes per ray of their own traversal:
+           B_ray = 64 N_node + 48 N_tri + 32 + 48 bytes (compact node record, triangle record,
+           root box, ray in and hit out), N_node / N_tri = record fetches per ray counted by the
+           counting kernels on one frame of this run (outside the timed region; the bounce-0
+           warp packets fetch a record once per warp); traffic = the DRAM bytes of a dated ncu
+           capture of the same launches; roofline.l2 = L2 traffic (ncu, 960x540 case) against
+           this run's L2-resident copy bandwidth; roofline.reference_traversal = the bytes the
+           reference traversal would fetch on the reference BVH (oracle statistics), a
+           reference figure, not a bound of these kernels.
 time_to_relmse : seeded Cornell box 512x512, depth 8: device time until the running
            estimate reaches relMSE 1e-3 against a 4096-spp NEE reference, reference
            estimator ("plain") and next-event estimation.
@@ -61,12 +67,15 @@ sys.path.insert(0, ROOT)
 W, H, SPP, DEPTH, LEVEL, SEED = 1920, 1080, 16, 12, 8, 1234
 WORKLOAD = "displaced_icosphere_l8_1.31Mtri_1920x1080_16spp_depth12_gpu_rebuild"
 # DRAM bytes (read + write) per traced ray of the closest-hit kernels on this
-# workload, from one ncu capture of a frame's 12 launches (9.97 GB / 71.5 M rays)
-EXTEND_DRAM_BYTES_PER_RAY = 139.4
-# the reference traversal's mean nodes visited / triangles tested per ray on the
-# reference BVH of this workload (oracle statistics over a sample of its paths),
-# used when a run skips the oracle sample (--no-cpu-baseline)
-REF_NODES_PER_RAY, REF_TRIS_PER_RAY = 46.3, 6.26
+# workload: one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# 12 launches of a frame, 10.42 GB / 71.54 M rays
+EXTEND_DRAM_CAPTURE = {"bytes_per_ray": 145.6, "captured": "2026-12-04",
+                       "profile": "profiles/k_extend_displaced_icosphere_1080p16.md"}
+# L2 traffic of the closest-hit launches of bounces 1 and 2 on the 960x540x16 case
+# (ncu lts__t_bytes.sum / gpu__time_duration.sum), with the L2 and L1 sector hit rates
+EXTEND_L2_CAPTURE = {"gbs": [2978.8, 4056.9], "l2_hit_pct": [71.6, 74.8], "l1_hit_pct": [68.2, 61.9],
+                     "captured": "2026-12-04", "case": "960x540, 16 spp, bounces 1 and 2",
+                     "profile": "profiles/k_extend_displaced_icosphere_1080p16.md"}
 
 
 def parse():
@@ -753,23 +762,45 @@ def run_mcrt(args):
     rays = sum(e[2] for e in ext)
     roof = None
     if not args.small:
-        if st and st["rays"]:
-            n_node, n_tri, n_source = st["nodes"] / st["rays"], st["prims"] / st["rays"], "oracle sample of this run"
-        else:
-            n_node, n_tri, n_source = REF_NODES_PER_RAY, REF_TRIS_PER_RAY, "recorded oracle statistics"
-        b_ray = 48 * n_node + 64 * n_tri + 32 + 16
-        achieved = rays * b_ray / (ext_ms / 1000.0) / 1e9
+        # outside the timed region: this run's copy bandwidths and the traversal's own record fetches
+        l2_copy = ctx.copy_bandwidth(16 << 20, 50)
+        hbm_copy = ctx.copy_bandwidth(2048 << 20, 10)
+        ctx.rebuild_bvh()
+        ctx.render(cam, W, H, SPP, first_frame=0, max_depth=DEPTH, outputs=(), count=True)
+        tc = ctx.timings()
+        n_node = tc["node_fetches"] / max(tc["rays"], 1)
+        n_tri = tc["triangle_fetches"] / max(tc["rays"], 1)
+        b_ray = 64 * n_node + 48 * n_tri + 32 + 48
+        sec = ext_ms / 1000.0
+        achieved = rays * b_ray / sec / 1e9
         rays_per_launch = rays / max(ext_launches, 1)
+        dram_b = EXTEND_DRAM_CAPTURE["bytes_per_ray"]
+        l2_gbs = sum(EXTEND_L2_CAPTURE["gbs"]) / len(EXTEND_L2_CAPTURE["gbs"])
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4),
-                # measured DRAM bytes per launch: ncu dram__bytes_read.sum + dram__bytes_write.sum over the
-                # 12 extend launches of one frame of this workload, per ray, times this run's rays per launch
-                "traffic": round(EXTEND_DRAM_BYTES_PER_RAY * rays_per_launch),
-                "traffic_unit": "B per launch", "traffic_per_ray": EXTEND_DRAM_BYTES_PER_RAY,
-                "peak_kind": peak_kind,
-                "kernel": "k_extend", "bytes_per_ray": round(b_ray, 1), "n_node": round(n_node, 2),
-                "n_tri": round(n_tri, 2), "n_source": n_source, "mrays_per_s": round(rays / (ext_ms / 1000.0) / 1e6, 1),
-                "avg_launch_ms": round(ext_ms / max(ext_launches, 1), 4)}
+                "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                "traffic": round(dram_b * rays_per_launch), "traffic_unit": "B per launch",
+                "traffic_source": dict(EXTEND_DRAM_CAPTURE, note="DRAM bytes per ray of the capture x this run's "
+                                                                 "rays per launch"),
+                "kernel": "k_extend_packet (bounce 0) + k_extend (bounces 1-11)",
+                "bytes_per_ray": round(b_ray, 1), "node_fetches_per_ray": round(n_node, 3),
+                "triangle_fetches_per_ray": round(n_tri, 3),
+                "fetch_source": "counting kernels, one frame of this run",
+                "mrays_per_s": round(rays / sec / 1e6, 1), "avg_launch_ms": round(ext_ms / max(ext_launches, 1), 4),
+                "hbm_copy_gbs_this_run": round(hbm_copy, 1),
+                "dram": {"achieved": round(dram_b * rays / sec / 1e9, 1), "frac": round(dram_b * rays / sec / 1e9 / peak, 4),
+                         "bytes_per_ray": dram_b},
+                "l2": {"achieved": round(l2_gbs, 1), "peak": round(l2_copy, 1), "frac": round(l2_gbs / l2_copy, 4),
+                       "unit": "GB/s", "peak_kind": "this run's float4 copy over 2 x 16 MB (L2-resident)",
+                       "source": EXTEND_L2_CAPTURE}}
+        if st and st["rays"]:
+            rn, rt = st["nodes"] / st["rays"], st["prims"] / st["rays"]
+            rb = 48 * rn + 64 * rt + 32 + 16
+            roof["reference_traversal"] = {
+                "bytes_per_ray": round(rb, 1), "node_visits_per_ray": round(rn, 2), "triangle_tests_per_ray": round(rt, 2),
+                "equivalent_gbs": round(rays * rb / sec / 1e9, 1),
+                "note": "the reference traversal's visits on the reference BVH (48 B node, 16 B triangle + 3 x 16 B "
+                        "positions), oracle statistics of this run's sample: more than HBM could deliver in the "
+                        "kernels' time, since these kernels fetch fewer records, most from L2 and L1"}
     clocks = clk.summary()
     quality = adjoint = voxel = views = views_cache = mlp = cpu_more = None
     if not args.small:
