@@ -90,7 +90,8 @@ def parse():
     p.add_argument("--mid", action="store_true",
                    help="same scene at 960x540, 16 spp (2 GB of path state): the profiling case for counter "
                         "sets that need several passes (not a bench line)")
-    p.add_argument("--leg", choices=["bvh_build", "cache_mlp", "frame", "adjoint", "nee", "roofline_inputs"],
+    p.add_argument("--leg", choices=["bvh_build", "cache_mlp", "frame", "adjoint", "nee", "roofline_inputs",
+                                     "cache_race"],
                    help="profiling case: only the GPU BVH builds of the workload's mesh, only the "
                         "radiance-cache MLP (2^18 queries), only frames of the workload (autotune: 8 "
                         "frames, then rebuild + render with the chosen closest-hit variant, 12 extend "
@@ -389,52 +390,167 @@ def nee_rate(M, ctx, n_warm=1, n_calls=2, w=512, h=512, spp=128, depth=8):
     return out
 
 
-def time_to_relmse(M, ctx, target=1e-3, w=512, h=512, depth=8, ref_spp=4096, max_spp=16384):
-    """Seeded Cornell box at 512 x 512, depth 8: device time for the running
-    estimate to reach relMSE <= target against a 4096-spp NEE reference (mean
-    over pixels and channels of (x - r)^2 / (r^2 + 1e-2)), for the reference
-    estimator and for NEE + MIS.  Estimates grow in chunks (KEEP_ACCUM); relMSE
-    is evaluated between chunks, outside the timed kernels."""
+def race(read_sum, render, ref, target, max_spp, warm=None, growth=1.1, min_chunk=1, denom_ref=None):
+    """Wall time for an estimator's running estimate to reach relMSE <= target
+    (mean over pixels and channels of (x - r)^2 / (r^2 + 1e-2)) against ref.
+    render(spp, first_frame, keep) adds spp frames to the device accumulation and
+    returns when they are done (the library's calls are synchronous); its wall
+    time is summed, with warm() (the cache's warm-up training) inside it.  The
+    estimate grows in chunks of about 10 % (growth); read_sum() reads the f64
+    sums between chunks, outside the time.  relMSE of an unbiased estimate falls
+    as 1/spp, so the crossing is interpolated linearly in 1/relMSE between the
+    last two checkpoints (spp_at_target, s_at_target), free of the chunk size.
+    denom_ref: the image whose squares normalise the error (default ref)."""
+    total, sec, hist = 0, 0.0, []
+    den = (ref if denom_ref is None else denom_ref) ** 2 + 1e-2
+    if warm:
+        t0 = time.perf_counter()
+        warm()
+        sec += time.perf_counter() - t0
+    rel = None
+    while total < max_spp:
+        chunk = min(max(min_chunk, int(total * (growth - 1.0))), max_spp - total)
+        t0 = time.perf_counter()
+        render(chunk, total, total > 0)
+        sec += time.perf_counter() - t0
+        total += chunk
+        x = read_sum() / total
+        rel = float(np.mean((x - ref) ** 2 / den))
+        hist.append((total, sec, rel))
+        if rel <= target:
+            break
+    out = {"spp": total, "s": round(sec, 4), "relmse": round(rel, 7), "reached": rel <= target,
+           "checkpoints": len(hist)}
+    if rel <= target:
+        n1, s1, r1 = hist[-1]
+        n0, s0, r0 = hist[-2] if len(hist) > 1 else (0, 0.0, float("inf"))
+        a0 = 0.0 if r0 == float("inf") else 1.0 / r0
+        f = (1.0 / target - a0) / max(1.0 / r1 - a0, 1e-30)
+        f = min(max(f, 0.0), 1.0)
+        out["spp_at_target"] = round(n0 + f * (n1 - n0), 1)
+        out["s_at_target"] = round(s0 + f * (s1 - s0), 4)
+    return out
+
+
+def _speedups(out, base, names):
+    for name in names:
+        if out[base]["reached"] and out[name]["reached"]:
+            out[f"speedup_{name}_vs_{base}"] = round(out[base]["s_at_target"] / out[name]["s_at_target"], 3)
+
+
+def ideal_cache_bound(render, read, full_ref, full, target, max_spp, vertices=(1, 2), ref_spp=4096, min_chunk=2):
+    """The speedup a perfect and free radiance cache could reach.  A path
+    stopped at vertex k (after its next-event sample) and given the exact
+    expected radiance of its remainder has at least the variance of the path
+    truncated there, and the cost of the truncated path.  render(spp, first,
+    keep, depth) renders with max_depth; for each k the tracer truncated to
+    depth k + 1 races (wall time) against its own ref_spp reference, its error
+    normalised by the full image (full_ref: the remainder a perfect cache adds
+    back is the difference of the two references), and full["s_at_target"] /
+    its time bounds the speedup of any cache that stops paths at vertex k.
+    The bound factors into the cost per sample and the samples needed."""
+    out = {}
+    for k in vertices:
+        render(ref_spp, 1 << 20, False, k + 1)
+        ref = read() / ref_spp
+        r = race(read, lambda spp, first, keep: render(spp, first, keep, k + 1), ref, target, max_spp,
+                 min_chunk=min_chunk, denom_ref=full_ref)
+        if r["reached"]:
+            r["ideal_speedup"] = round(full["s_at_target"] / r["s_at_target"], 3)
+            r["cost_per_spp_ratio"] = round((full["s"] / full["spp"]) / (r["s"] / r["spp"]), 3)
+            r["spp_ratio"] = round(full["spp_at_target"] / r["spp_at_target"], 3)
+        out[f"stop_at_vertex_{k}"] = r
+    return out
+
+
+def time_to_relmse(M, ctx, target=1e-3, w=512, h=512, depth=8, ref_spp=4096, max_spp=16384, bound=True,
+                   scene="cornell_box", cache_cfgs=None, plain=True):
+    """Seeded Cornell box at 512 x 512, depth 8: wall time for the running
+    estimate to reach relMSE <= target against a 4096-spp NEE reference (race),
+    for the reference estimator ("plain"), NEE + MIS ("nee") and NEE + the
+    online-trained radiance cache ("cache", warm-up and training in the time)."""
     from mcrt_gb300 import scenes
-    sc = scenes.cornell_box(SEED)
+    sc = getattr(scenes, scene)(SEED)
     c = sc["camera"]
     cam = M.compute_camera(w, h, c["look_from"], c["look_at"], c["vfov"], 0.0)
     ctx.upload_scene(vertices=sc["vertices"], triangles=sc["triangles"], materials=sc["materials"],
                      env=M.gradient_env_map())
     ref = ctx.render(cam, w, h, ref_spp, first_frame=1 << 20, max_depth=depth, nee=True, outputs=("sum",))["sum"]
     ref /= ref_spp
-    out = {"workload": f"cornell_box_seed{SEED}_{w}x{h}_depth{depth}", "target_relmse": target,
-           "reference": f"NEE {ref_spp} spp, independent frames"}
-    cache_cfg = dict(query_vertex=2, train_stride=64, train_steps=8, train_batch=1 << 14, lr=1e-3)
-    for name, nee, cache in (("plain", False, False), ("nee", True, False), ("cache", True, True)):
-        total, ms, rel = 0, 0.0, None
-        if cache:                                    # online training from scratch, timed
+    out = {"workload": f"{scene}_seed{SEED}_{w}x{h}_depth{depth}", "target_relmse": target,
+           "reference": f"NEE {ref_spp} spp, independent frames", "time": "wall clock of the render calls"}
+    cache_cfgs = cache_cfgs or [dict(query_vertex=2, train_stride=64, train_steps=8, train_batch=1 << 14, lr=1e-3)]
+    read = lambda: ctx.read_accum()[1]
+    runs = ([("plain", False, None)] if plain else []) + [("nee", True, None)] + \
+        [("cache" if k == 0 else f"cache_{k}", True, cfg) for k, cfg in enumerate(cache_cfgs)]
+    for name, nee, cache_cfg in runs:
+        warm = None
+        cache = cache_cfg is not None
+        if cache:
             ctx.cache_config(**cache_cfg)
             ctx.cache_init(0)
-            for i in range(5):
-                ctx.render(cam, w, h, 8, first_frame=(1 << 21) + 8 * i, max_depth=depth, nee=True, cache=True,
-                           outputs=())
-                ms += ctx.timings()["total_ms"]
-        while total < max_spp:
-            chunk = max(16, total // 8)
-            r = ctx.render(cam, w, h, chunk, first_frame=total, max_depth=depth, nee=nee, keep=total > 0,
-                           outputs=("sum",), cache=cache)
-            ms += ctx.timings()["total_ms"]
-            total += chunk
-            x = r["sum"] / total
-            rel = float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
-            if rel <= target:
-                break
-        out[name] = {"spp": total, "ms": round(ms, 2), "relmse": round(rel, 6), "reached": rel <= target,
-                     "msamples_per_s": round(w * h * total / (ms / 1000.0) / 1e6, 1)}
-        if cache:                                    # the bias judge's verdict on the last chunk
+
+            def warm():
+                for i in range(5):
+                    ctx.render(cam, w, h, 8, first_frame=(1 << 21) + 8 * i, max_depth=depth, nee=True, cache=True,
+                               outputs=())
+        out[name] = race(read, lambda spp, first, keep: ctx.render(
+            cam, w, h, spp, first_frame=first, max_depth=depth, nee=nee, keep=keep, outputs=(), cache=cache),
+            ref, target, max_spp, warm=warm, min_chunk=4)
+        if cache:
             out[name]["judged_bias"] = [round(b, 4) for b in ctx.cache_stats()["bias"]]
-    out["cache"]["config"] = dict(cache_cfg, warmup="5 passes x 8 spp, in the time")
-    for name in ("nee", "cache"):
-        if out["plain"]["reached"] and out[name]["reached"]:
-            out[f"speedup_{name}_vs_plain"] = round(out["plain"]["ms"] / out[name]["ms"], 2)
-    if out["nee"]["reached"] and out["cache"]["reached"]:
-        out["speedup_cache_vs_nee"] = round(out["nee"]["ms"] / out["cache"]["ms"], 2)
+            out[name]["config"] = dict(cache_cfg, warmup="5 passes x 8 spp, in the time")
+    caches = [r[0] for r in runs if r[2] is not None]
+    if plain:
+        _speedups(out, "plain", ["nee"] + caches)
+    _speedups(out, "nee", caches)
+    if bound and out["nee"]["reached"]:
+        out["ideal_cache_bound_vs_nee"] = ideal_cache_bound(
+            lambda spp, first, keep, d: ctx.render(cam, w, h, spp, first_frame=first, max_depth=d, nee=True,
+                                                   keep=keep, outputs=()),
+            read, ref, out["nee"], target, max_spp)
+    return out
+
+
+def icosphere_cache_relmse(M, ctx, target=1e-3, ref_spp=4096, max_spp=4096, configs=None, bound=True):
+    """The displaced icosphere (1.31 M triangles, 1920 x 1080, depth 12; lit by
+    its environment map alone, so next-event estimation has no light to sample
+    and the plain tracer is the tracer without the cache): wall time to relMSE
+    <= target against a 4096-spp reference for the tracer without and with the
+    online-trained radiance cache (race).  Long paths through dielectric and
+    GGX surfaces: what the cache stops is up to 10 more bounces per path."""
+    sc = make_scene()
+    c = sc["camera"]
+    cam = M.compute_camera(W, H, c["look_from"], c["look_at"], c["vfov"], c["aperture"])
+    ctx.upload_scene(vertices=sc["vertices"], triangles=sc["triangles"], materials=sc["materials"], env=sc["env"])
+    ref = ctx.render(cam, W, H, ref_spp, first_frame=1 << 20, max_depth=DEPTH, outputs=("sum",))["sum"] / ref_spp
+    out = {"workload": f"displaced_icosphere_l8_1.31Mtri_{W}x{H}_depth{DEPTH}", "target_relmse": target,
+           "reference": f"{ref_spp} spp, independent frames", "time": "wall clock of the render calls"}
+    read = lambda: ctx.read_accum()[1]
+    out["plain"] = race(read, lambda spp, first, keep: ctx.render(
+        cam, W, H, spp, first_frame=first, max_depth=DEPTH, keep=keep, outputs=(), graph=True),
+        ref, target, max_spp, min_chunk=2)
+    for k, cfg in enumerate(configs or [dict(query_vertex=1, train_stride=64, train_steps=16, train_batch=1 << 14,
+                                             lr=3e-3)]):
+        ctx.cache_config(**cfg)
+        ctx.cache_init(0)
+
+        def warm():
+            for i in range(4):
+                ctx.render(cam, W, H, 2, first_frame=(1 << 21) + 2 * i, max_depth=DEPTH, cache=True, graph=True,
+                           outputs=())
+        name = "cache" if k == 0 else f"cache_{k}"
+        out[name] = race(read, lambda spp, first, keep: ctx.render(
+            cam, W, H, spp, first_frame=first, max_depth=DEPTH, keep=keep, outputs=(), cache=True, graph=True),
+            ref, target, max_spp, warm=warm, min_chunk=2)
+        out[name]["judged_bias"] = [round(b, 4) for b in ctx.cache_stats()["bias"]]
+        out[name]["config"] = dict(cfg, warmup="4 passes x 2 spp, in the time")
+        _speedups(out, "plain", (name,))
+    if bound and out["plain"]["reached"]:
+        out["ideal_cache_bound_vs_plain"] = ideal_cache_bound(
+            lambda spp, first, keep, d: ctx.render(cam, W, H, spp, first_frame=first, max_depth=d, keep=keep,
+                                                   outputs=(), graph=True),
+            read, ref, out["plain"], target, max_spp)
     return out
 
 
@@ -547,18 +663,25 @@ def batched_views_rate(M, ctx, stream, spp=4, n_warm=1, n_steps=3):
             "speedup": round(t_seq / t_batch, 3)}
 
 
-def views_cache_relmse(M, ctx, target=1e-3, ref_spp=1024, max_spp=1024):
+def scenes_voxel_upload(M, ctx):
+    """Generate, mesh and upload the voxel world (the scene of voxel_world_rate)."""
+    from mcrt_gb300 import scenes
+    w = scenes.voxel_world(SEED)
+    ctx.world_generate(w["params"])
+    ctx.world_mesh(w["block_material"], greedy=False)
+    ctx.upload_scene(materials=w["materials"], env=M.gradient_env_map(), sun_dir=w["sun_dir"],
+                     sun_irradiance=w["sun_irradiance"], world_mesh=True)
+    return w
+
+
+def views_cache_relmse(M, ctx, target=1e-3, ref_spp=4096, max_spp=1024, bound=True):
     """The batched workload with the radiance cache: the 16 uneven views of the
     voxel world (left uploaded by voxel_world_rate), depth 6, sun NEE + sky.
-    Device time for the views' estimates (f64 sums / samples) to reach relMSE
-    <= target (over every pixel of every view) against a ref_spp NEE
-    reference, for the tracer without the cache and with the online-trained
-    cache (warm-up and training inside the time), both replaying their passes
-    as CUDA graphs (the cached passes with their training); each estimator
-    stops at max_spp.  The reference is 1024 spp rather
-    than 4096 to keep the leg within about a minute (12 Mpix); its own noise
-    then adds about 1/4 of the target to the relMSE the tracer without the
-    cache reaches, equally for both estimators."""
+    Wall time for the views' estimates to reach relMSE <= target (over every
+    pixel of every view) against a 4096-spp NEE reference (race), without the
+    cache and with the online-trained cache (warm-up and training inside the
+    time), both replaying their passes as CUDA graphs (the cached passes with
+    their training)."""
     from mcrt_gb300 import scenes
     w = scenes.voxel_world(SEED)
     vs = scenes.world_views(w, seed=SEED)
@@ -566,36 +689,35 @@ def views_cache_relmse(M, ctx, target=1e-3, ref_spp=1024, max_spp=1024):
               v["width"], v["height"]) for v in vs]
     depth = w["max_depth"]
     px = sum(v[1] * v[2] for v in views)
-    ctx.render_views(views, ref_spp, first_frame=1 << 20, max_depth=depth, nee=True, read_back=False)
+    ctx.render_views(views, ref_spp, first_frame=1 << 20, max_depth=depth, nee=True, graph=True, read_back=False)
     ref = ctx.read_accum()[1].reshape(-1, 3) / ref_spp
     out = {"workload": f"voxel_world_16_views_seed{SEED}_{px / 1e6:.2f}Mpix_depth{depth}_sun_nee",
-           "target_relmse": target, "reference": f"NEE {ref_spp} spp, independent frames"}
+           "target_relmse": target, "reference": f"NEE {ref_spp} spp, independent frames",
+           "time": "wall clock of the render calls"}
     cache_cfg = dict(query_vertex=2, train_stride=256, train_steps=16, train_batch=1 << 14, lr=3e-3)
+    read = lambda: ctx.read_accum()[1].reshape(-1, 3)
     for name, cache in (("nee", False), ("nee_cache", True)):
-        total, ms, rel = 0, 0.0, None
+        warm = None
         if cache:
             ctx.cache_config(**cache_cfg)
             ctx.cache_init(0)
-            for i in range(10):
-                ctx.render_views(views, 2, first_frame=(1 << 21) + 2 * i, max_depth=depth, nee=True, cache=True,
-                                 graph=True, read_back=False)
-                ms += ctx.timings()["total_ms"]
-        while total < max_spp:
-            chunk = max(8, total // 8)
-            ctx.render_views(views, chunk, first_frame=total, max_depth=depth, nee=True, keep=total > 0,
-                             cache=cache, graph=True, read_back=False)
-            ms += ctx.timings()["total_ms"]
-            total += chunk
-            x = ctx.read_accum()[1].reshape(-1, 3) / total
-            rel = float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
-            if rel <= target:
-                break
-        out[name] = {"spp": total, "ms": round(ms, 2), "relmse": round(rel, 6), "reached": rel <= target}
+
+            def warm():
+                for i in range(10):
+                    ctx.render_views(views, 2, first_frame=(1 << 21) + 2 * i, max_depth=depth, nee=True, cache=True,
+                                     graph=True, read_back=False)
+        out[name] = race(read, lambda spp, first, keep: ctx.render_views(
+            views, spp, first_frame=first, max_depth=depth, nee=True, keep=keep, cache=cache, graph=True,
+            read_back=False), ref, target, max_spp, warm=warm, min_chunk=2)
         if cache:
             out[name]["judged_bias"] = [round(b, 4) for b in ctx.cache_stats()["bias"]]
     out["nee_cache"]["config"] = dict(cache_cfg, warmup="10 passes x 2 spp over all views, in the time")
-    if out["nee"]["reached"] and out["nee_cache"]["reached"]:
-        out["speedup_cache_vs_nee"] = round(out["nee"]["ms"] / out["nee_cache"]["ms"], 3)
+    _speedups(out, "nee", ("nee_cache",))
+    if bound and out["nee"]["reached"]:
+        out["ideal_cache_bound_vs_nee"] = ideal_cache_bound(
+            lambda spp, first, keep, d: ctx.render_views(views, spp, first_frame=first, max_depth=d, nee=True,
+                                                         keep=keep, graph=True, read_back=False),
+            read, ref, out["nee"], target, max_spp)
     return out
 
 
@@ -656,6 +778,18 @@ def run_mcrt(args):
         ms = [b[0] for b in builds[args.warmup:]]
         print(json.dumps({"leg": "bvh_build", "triangles": int(len(sc["triangles"])), "ms": ms,
                           "launches_per_build": builds[-1][1]}))
+        return
+    if args.leg == "cache_race":          # the radiance cache against the tracer without it (wall time)
+        cfgs = json.loads(os.environ["MCRT_CACHE_CONFIGS"]) if os.environ.get("MCRT_CACHE_CONFIGS") else None
+        out = {"leg": "cache_race", "icosphere": icosphere_cache_relmse(M, ctx, configs=cfgs)}
+        if not os.environ.get("MCRT_CACHE_ICOSPHERE_ONLY"):
+            out["cornell"] = time_to_relmse(M, ctx)
+            ccfg = json.loads(os.environ["MCRT_CACHE_SHADED"]) if os.environ.get("MCRT_CACHE_SHADED") else None
+            out["cornell_shaded"] = time_to_relmse(M, ctx, scene="cornell_box_shaded", cache_cfgs=ccfg, plain=False)
+        if os.environ.get("MCRT_CACHE_VIEWS"):
+            w = scenes_voxel_upload(M, ctx)
+            out["views"] = views_cache_relmse(M, ctx)
+        print(json.dumps(out))
         return
     if args.leg == "roofline_inputs":
         variant, _ = ctx.autotune(cam, W, H, SPP, max_depth=DEPTH)
