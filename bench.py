@@ -20,10 +20,12 @@ roofline : the closest-hit kernels (12 launches per frame) against the measured 
            this run's L2-resident copy bandwidth; roofline.reference_traversal = the bytes the
            reference traversal would fetch on the reference BVH (oracle statistics), a
            reference figure, not a bound of these kernels.
-time_to_relmse : seeded Cornell box 512x512, depth 8: device time until the running
-           estimate reaches relMSE 1e-3 against a 4096-spp NEE reference, reference
-           estimator ("plain") and next-event estimation.
-           The same with the radiance cache (online training inside the time).
+time_to_relmse : seeded Cornell box 512x512, depth 8: wall time of the render calls until
+           the running estimate reaches relMSE 1e-3 against a 4096-spp NEE reference, for
+           the reference estimator ("plain"), next-event estimation and NEE + the radiance
+           cache (online training inside the time), with the bound of a perfect, free cache
+           (ideal_cache_bound); icosphere_cache_time_to_relmse: the same on the displaced
+           icosphere (long paths, environment light only).
 adjoint  : path-replay adjoint of the GGX Cornell box, 256x256, 32 spp: paths/s
            through mcrt_adjoint with host buffers.
 voxel_world : the 256x128x256 voxel world generated, meshed (4.94 M triangles),
@@ -464,20 +466,20 @@ def ideal_cache_bound(render, read, full_ref, full, target, max_spp, vertices=(1
 
 
 def time_to_relmse(M, ctx, target=1e-3, w=512, h=512, depth=8, ref_spp=4096, max_spp=16384, bound=True,
-                   scene="cornell_box", cache_cfgs=None, plain=True):
+                   cache_cfgs=None, plain=True):
     """Seeded Cornell box at 512 x 512, depth 8: wall time for the running
     estimate to reach relMSE <= target against a 4096-spp NEE reference (race),
     for the reference estimator ("plain"), NEE + MIS ("nee") and NEE + the
     online-trained radiance cache ("cache", warm-up and training in the time)."""
     from mcrt_gb300 import scenes
-    sc = getattr(scenes, scene)(SEED)
+    sc = scenes.cornell_box(SEED)
     c = sc["camera"]
     cam = M.compute_camera(w, h, c["look_from"], c["look_at"], c["vfov"], 0.0)
     ctx.upload_scene(vertices=sc["vertices"], triangles=sc["triangles"], materials=sc["materials"],
                      env=M.gradient_env_map())
     ref = ctx.render(cam, w, h, ref_spp, first_frame=1 << 20, max_depth=depth, nee=True, outputs=("sum",))["sum"]
     ref /= ref_spp
-    out = {"workload": f"{scene}_seed{SEED}_{w}x{h}_depth{depth}", "target_relmse": target,
+    out = {"workload": f"cornell_box_seed{SEED}_{w}x{h}_depth{depth}", "target_relmse": target,
            "reference": f"NEE {ref_spp} spp, independent frames", "time": "wall clock of the render calls"}
     cache_cfgs = cache_cfgs or [dict(query_vertex=2, train_stride=64, train_steps=8, train_batch=1 << 14, lr=1e-3)]
     read = lambda: ctx.read_accum()[1]
@@ -784,8 +786,10 @@ def run_mcrt(args):
         out = {"leg": "cache_race", "icosphere": icosphere_cache_relmse(M, ctx, configs=cfgs)}
         if not os.environ.get("MCRT_CACHE_ICOSPHERE_ONLY"):
             out["cornell"] = time_to_relmse(M, ctx)
-            ccfg = json.loads(os.environ["MCRT_CACHE_SHADED"]) if os.environ.get("MCRT_CACHE_SHADED") else None
-            out["cornell_shaded"] = time_to_relmse(M, ctx, scene="cornell_box_shaded", cache_cfgs=ccfg, plain=False)
+            cfgs_c = [dict(query_vertex=v, train_stride=64, train_steps=8, train_batch=1 << 14, lr=1e-3) for v in (1, 2)]
+            for tgt in (1e-2, 3e-3):
+                out[f"cornell_target_{tgt:g}"] = time_to_relmse(M, ctx, target=tgt, cache_cfgs=cfgs_c, plain=False,
+                                                                bound=False)
         if os.environ.get("MCRT_CACHE_VIEWS"):
             w = scenes_voxel_upload(M, ctx)
             out["views"] = views_cache_relmse(M, ctx)
@@ -936,14 +940,15 @@ def run_mcrt(args):
                         "positions), oracle statistics of this run's sample: more than HBM could deliver in the "
                         "kernels' time, since these kernels fetch fewer records, most from L2 and L1"}
     clocks = clk.summary()
-    quality = adjoint = voxel = views = views_cache = mlp = cpu_more = None
+    quality = adjoint = voxel = views = views_cache = icosphere_cache = mlp = cpu_more = None
     if not args.small:
         mlp = mlp_rate(M, ctx)
         quality = time_to_relmse(M, ctx)
         adjoint = adjoint_rate(M, ctx, stream)
         voxel = voxel_world_rate(M, ctx, stream)
         views = batched_views_rate(M, ctx, stream)
-        views_cache = views_cache_relmse(M, ctx)
+        views_cache = views_cache_relmse(M, ctx, bound=False)
+        icosphere_cache = icosphere_cache_relmse(M, ctx)
         if not args.no_cpu_baseline:
             cpu_more, more_parity = cpu_baselines(M, ctx, quality, cores)
             parity.update(more_parity)
@@ -972,6 +977,7 @@ def run_mcrt(args):
         "voxel_world": voxel,
         "batched_views": views,
         "batched_views_cache_time_to_relmse": views_cache,
+        "icosphere_cache_time_to_relmse": icosphere_cache,
         "radiance_cache_mlp": mlp,
     }
     print(json.dumps(out))

@@ -23,7 +23,7 @@ import numpy as np
 
 from ._native import MATERIAL_DATA, SPHERE, TRIANGLE, VERTEX, MAT_DIELECTRIC, MAT_EMISSIVE, MAT_GGX, MAT_LAMBERTIAN
 
-__all__ = ["cornell_box", "cornell_box_shaded", "cornell_box_ggx", "ggx_materials", "displaced_icosphere", "icosphere", "value_noise3", "smooth_noise_env"]
+__all__ = ["cornell_box", "cornell_box_ggx", "ggx_materials", "displaced_icosphere", "icosphere", "value_noise3", "smooth_noise_env"]
 
 
 def _mat(md, i, t, alb, w=0.0, x=1.0):
@@ -99,36 +99,6 @@ def cornell_box(seed: int = 1234, box_mats=(0, 0)):
     camera = dict(look_from=[0.5, 0.5, 2.4], look_at=[0.5, 0.5, 0.0], vfov=40.0, aperture=0.0)
     return dict(vertices=V, triangles=T, materials=md, spheres=np.zeros(0, SPHERE), camera=camera,
                 width=512, height=512, spp=64, max_depth=8)
-
-
-def cornell_box_shaded(seed: int = 1234, radiance=(68.0, 48.0, 16.0)):
-    """The seeded Cornell box with its lamp inside a shade: a 0.2 x 0.2 quad
-    light at y = 0.88 in a white box open at the top (bottom at y = 0.85, sides
-    up to y = 0.95, 0.3 x 0.3), so the light reaches only the ceiling and the
-    shade's inside directly and the room is lit by those bounces (indirect
-    light, where next-event estimation finds the light mostly hidden)."""
-    sc = cornell_box(seed)
-    md = sc["materials"].copy()
-    _mat(md, 3, MAT_EMISSIVE, radiance, 0.0, 1.0)
-    verts = list(sc["vertices"][:-4])                    # without the ceiling light quad
-    tris = [((int(t["v"][0]), int(t["v"][1]), int(t["v"][2])), int(t["mat_idx"])) for t in sc["triangles"][:-2]]
-    lo, hi, yb, yt = 0.35, 0.65, 0.85, 0.95
-    shade = [
-        ([(lo, yb, hi), (hi, yb, hi), (hi, yb, lo), (lo, yb, lo)], (0, -1, 0)),       # bottom, facing down
-        ([(lo, yb, lo), (hi, yb, lo), (hi, yt, lo), (lo, yt, lo)], (0, 0, -1)),
-        ([(hi, yb, hi), (lo, yb, hi), (lo, yt, hi), (hi, yt, hi)], (0, 0, 1)),
-        ([(lo, yb, hi), (lo, yb, lo), (lo, yt, lo), (lo, yt, hi)], (-1, 0, 0)),
-        ([(hi, yb, lo), (hi, yb, hi), (hi, yt, hi), (hi, yt, lo)], (1, 0, 0)),
-    ]
-    _quads_to_mesh([q[0] for q in shade], [q[1] for q in shade], [0] * 5, verts, tris)
-    L = 0.1
-    _quads_to_mesh([[(0.5 - L, 0.88, 0.5 + L), (0.5 + L, 0.88, 0.5 + L), (0.5 + L, 0.88, 0.5 - L),
-                     (0.5 - L, 0.88, 0.5 - L)]], [(0, 1, 0)], [3], verts, tris)
-    V = np.array(verts, VERTEX)
-    T = np.zeros(len(tris), TRIANGLE)
-    T["v"] = [t[0] for t in tris]
-    T["mat_idx"] = [t[1] for t in tris]
-    return dict(sc, vertices=V, triangles=T, materials=md)
 
 
 GGX_SLOTS = (0, 1, 2, 4, 5)      # white walls, red wall, green wall, short box, tall box

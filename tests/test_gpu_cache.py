@@ -122,11 +122,16 @@ def test_cache_stop_bit_exact(ctx, oracle):
         assert np.array_equal(r["sum"].view(np.uint64), o["sum"].view(np.uint64))
 
 
-def test_trained_cache_gains_over_untrained_and_plain(ctx):
-    """Cornell box 128 x 128: the tracer with the online-trained cache (paths
-    stopped at their third vertex) against the same tracer with an untrained
-    network and against the plain (reference) estimator at equal spp, all
-    measured as relMSE against a 4096-spp NEE reference."""
+def test_trained_cache_gains_over_untrained_and_nee(ctx):
+    """Cornell box 128 x 128, relMSE against a 4096-spp NEE reference.  The
+    tracer with the online-trained cache (next-event estimation, paths stopped
+    at their third vertex) against the same tracer with an untrained network
+    at equal spp, and against next-event estimation alone at an equal number of
+    traced rays (closest-hit and shadow rays, the training paths' included; the
+    warm-up training is not counted): the stopped paths are cheaper, and the
+    trained network's prediction is accurate enough that the extra samples pay.
+    (Counted with the warm-up, in wall time to relMSE 1e-3, the gain over NEE
+    alone is small: bench.py's time_to_relmse.)"""
     from mcrt_gb300 import scenes
     sc = scenes.cornell_box(1234)
     c = sc["camera"]
@@ -139,19 +144,31 @@ def test_trained_cache_gains_over_untrained_and_plain(ctx):
     def rel(x):
         return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
 
-    spp = 256
-    plain = rel(ctx.render(cam, W, H, spp, max_depth=8, outputs=("sum",))["sum"] / spp)
+    def rays():
+        t = ctx.timings()
+        return t["rays"] + t["shadow_rays"]
+
+    spp = 32
+    nee = rel(ctx.render(cam, W, H, spp, max_depth=8, nee=True, outputs=("sum",))["sum"] / spp)
+    nee_rays = rays()
     ctx.cache_config(query_vertex=2, train_stride=16, train_steps=0, lr=0.0)
     ctx.cache_init(1)
-    untrained = rel(ctx.render(cam, W, H, spp, max_depth=8, nee=True, cache=True, outputs=("sum",))["sum"] / spp)
+    untrained = rel(ctx.render(cam, W, H, 256, max_depth=8, nee=True, cache=True, outputs=("sum",))["sum"] / 256)
     ctx.cache_config(query_vertex=2, train_stride=16, train_steps=4, lr=1e-3)
     ctx.cache_init(1)
     for i in range(40):
         ctx.render(cam, W, H, 4, first_frame=100000 + 4 * i, max_depth=8, nee=True, cache=True, outputs=())
-    trained = rel(ctx.render(cam, W, H, spp, max_depth=8, nee=True, cache=True, outputs=("sum",))["sum"] / spp)
-    print("relMSE plain", plain, "untrained cache", untrained, "trained cache", trained)
+    trained = rel(ctx.render(cam, W, H, 256, max_depth=8, nee=True, cache=True, outputs=("sum",))["sum"] / 256)
+    per_spp = rays() / 256
+    spp_c = int(nee_rays / per_spp)                 # the cached tracer's spp for NEE's rays
+    cached = rel(ctx.render(cam, W, H, spp_c, first_frame=5000, max_depth=8, nee=True, cache=True,
+                            outputs=("sum",))["sum"] / spp_c)
+    assert rays() <= nee_rays
+    print("relMSE NEE", nee, "cache at equal rays", cached, f"({spp_c} spp)", "untrained", untrained,
+          "trained", trained)
     assert trained < untrained / 3
-    assert trained < plain / 3
+    assert spp_c > 1.3 * spp
+    assert cached < nee
 
 
 def test_cache_bias_judge_and_fallback(ctx):
