@@ -113,7 +113,7 @@ constexpr uint32_t kSmemAct = kSmemBias + kBiasFloats * 4;                 // 48
 constexpr uint32_t kTileIn = kTile * kIn * 2;                              // 24576
 constexpr uint32_t kTileHid = kTile * kHid * 2;                            // 16384
 // inference: image | bias | one activation tile | mbarrier | TMEM slot
-constexpr uint32_t kInferGroups = 5;                     // one CTA per SM (shared memory), 640 threads
+constexpr uint32_t kInferGroups = 7;                     // one CTA per SM (shared memory), 896 threads
 constexpr uint32_t kInferSmem = kSmemAct + kInferGroups * kTileIn + 64;
 constexpr uint32_t kInferTmemCols = 64 * kInferGroups <= 128 ? 128 : (64 * kInferGroups <= 256 ? 256 : 512);   // a power of 2
 static_assert(64 * kInferGroups <= 512, "TMEM columns of the inference pipelines");
@@ -146,17 +146,49 @@ __device__ void load_net(const NetDev &net, uint8_t *smem) {
     for (uint32_t i = threadIdx.x; i < kBiasFloats; i += blockDim.x) b[i] = net.bias[i];
 }
 
-// Encode the query of this thread's row into the input tile (bf16, 12 chunks of 8).
-__device__ void encode_row(const NetDev &net, const float q[12], bool valid, uint8_t *tile, uint32_t row) {
-    float f[kIn];
-    if (valid) encode(q, net.lo, net.inv_ext, f);
-    else for (int k = 0; k < kIn; ++k) f[k] = 0.0f;
+// Encode the query of this thread's row into the input tile (bf16, 12 chunks
+// of 8): the features of mlp::encode (the same arithmetic), written 8 at a
+// time as they are formed: one axis's 12 bands are three chunks
+// of 4 (sin, cos) pairs, so at most 8 features are live (the register budget
+// of the inference kernel's pipelines).
+__device__ __forceinline__ void store_chunk(uint8_t *tile, uint32_t row, int c, const float f[8]) {
+    *reinterpret_cast<uint4 *>(tile + tc::op_offset(row, 8 * c, kTile)) =
+        make_uint4(pack2(f[0], f[1]), pack2(f[2], f[3]), pack2(f[4], f[5]), pack2(f[6], f[7]));
+}
+__device__ void encode_row_streamed(const NetDev &net, const float q[12], bool valid, uint8_t *tile, uint32_t row) {
+    float u[3];
+    for (int a = 0; a < 3; ++a) {
+        float s = 0.0f, c = 0.0f;
+        if (valid) {
+            const float v = (q[a] - net.lo[a]) * net.inv_ext[a];
+            u[a] = v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v);
+            fm_sincos(u[a] * band_freq(0), &s, &c);
+        } else {
+            u[a] = 0.0f;
+        }
 #pragma unroll
-    for (int c = 0; c < kIn / 8; ++c) {
-        uint4 v = make_uint4(pack2(f[8 * c], f[8 * c + 1]), pack2(f[8 * c + 2], f[8 * c + 3]),
-                             pack2(f[8 * c + 4], f[8 * c + 5]), pack2(f[8 * c + 6], f[8 * c + 7]));
-        *reinterpret_cast<uint4 *>(tile + tc::op_offset(row, 8 * c, kTile)) = v;
+        for (int ch = 0; ch < 3; ++ch) {
+            float f[8];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                f[2 * k] = valid ? s : 0.0f;
+                f[2 * k + 1] = valid ? c : 0.0f;
+                const float s2 = (2.0f * s) * c, c2 = c * c - s * s;
+                s = s2;
+                c = c2;
+            }
+            store_chunk(tile, row, 3 * a + ch, f);
+        }
     }
+    const float z = 0.0f;
+    float f9[8] = {q[3], q[4], q[5], q[6], q[7], q[8], q[9], q[10]};
+    float f10[8] = {q[11], u[0], u[1], u[2], z, z, z, z};
+    if (!valid)
+        for (int k = 0; k < 8; ++k) { f9[k] = 0.0f; f10[k] = 0.0f; }
+    const float f11[8] = {z, z, z, z, z, z, z, z};
+    store_chunk(tile, row, 9, f9);
+    store_chunk(tile, row, 10, f10);
+    store_chunk(tile, row, 11, f11);
 }
 
 // Issue D = A * B for a K-major activation tile A (128 rows) and the K-major
@@ -246,7 +278,7 @@ __global__ void __launch_bounds__(128 * kInferGroups) k_cache_infer(NetDev net, 
             q[6] = c.x; q[7] = c.y; q[8] = c.z;
             q[9] = d.x; q[10] = d.y; q[11] = d.z;
         }
-        encode_row(net, q, valid, act, row);
+        encode_row_streamed(net, q, valid, act, row);
         group_operand_sync(bar_id);
         for (int l = 0; l < kLayers; ++l) {
             if (row == 0) issue_forward(taddr, act, smem + kSmemImg + img_off(l), l, mbar);
@@ -255,15 +287,19 @@ __global__ void __launch_bounds__(128 * kInferGroups) k_cache_infer(NetDev net, 
             tc::fence_after_sync();
             if (!ok) break;
             if (l < kLayers - 1) {
-                for (uint32_t c = 0; c < (uint32_t)kHid; c += 16) {
-                    float v[16];
-                    tc::tmem_ld16(taddr + lane_base + c, v);
-                    float h[16];
-                    for (int j = 0; j < 16; ++j) h[j] = relu(v[j] + bias[bias_idx(l) + c + j]);
-                    *reinterpret_cast<uint4 *>(act + tc::op_offset(row, c, kTile)) =
-                        make_uint4(pack2(h[0], h[1]), pack2(h[2], h[3]), pack2(h[4], h[5]), pack2(h[6], h[7]));
-                    *reinterpret_cast<uint4 *>(act + tc::op_offset(row, c + 8, kTile)) =
-                        make_uint4(pack2(h[8], h[9]), pack2(h[10], h[11]), pack2(h[12], h[13]), pack2(h[14], h[15]));
+#pragma unroll
+                for (uint32_t c = 0; c < (uint32_t)kHid; c += 32) {
+                    float v[32];
+                    tc::tmem_ld32(taddr + lane_base + c, v);
+#pragma unroll
+                    for (uint32_t k = 0; k < 32; k += 8) {
+                        const float *bb = bias + bias_idx(l) + c + k;
+                        *reinterpret_cast<uint4 *>(act + tc::op_offset(row, c + k, kTile)) = make_uint4(
+                            pack2(relu(v[k] + bb[0]), relu(v[k + 1] + bb[1])),
+                            pack2(relu(v[k + 2] + bb[2]), relu(v[k + 3] + bb[3])),
+                            pack2(relu(v[k + 4] + bb[4]), relu(v[k + 5] + bb[5])),
+                            pack2(relu(v[k + 6] + bb[6]), relu(v[k + 7] + bb[7])));
+                    }
                 }
                 group_operand_sync(bar_id);
             } else {
@@ -375,7 +411,7 @@ __global__ void __launch_bounds__(128, 1) k_cache_train(NetDev net, TrainIO io, 
         float q[12];
         for (int k = 0; k < 12; ++k) q[k] = s[k];
         const float tg0 = s[12], tg1 = s[13], tg2 = s[14];
-        encode_row(net, q, wgt > 0.0f, x0, row);
+        encode_row_streamed(net, q, wgt > 0.0f, x0, row);
         operand_sync();
         // ---- forward
         for (int l = 0; l < kLayers && ok; ++l) {
@@ -387,14 +423,19 @@ __global__ void __launch_bounds__(128, 1) k_cache_train(NetDev net, TrainIO io, 
             if (!ok) break;
             if (l < kLayers - 1) {
                 uint8_t *out = H(l + 1);
-                for (uint32_t c = 0; c < (uint32_t)kHid; c += 16) {
-                    float v[16], h[16];
-                    tc::tmem_ld16(taddr + lane_base + c, v);
-                    for (int j = 0; j < 16; ++j) h[j] = relu(v[j] + bias[bias_idx(l) + c + j]);
-                    *reinterpret_cast<uint4 *>(out + tc::op_offset(row, c, kTile)) =
-                        make_uint4(pack2(h[0], h[1]), pack2(h[2], h[3]), pack2(h[4], h[5]), pack2(h[6], h[7]));
-                    *reinterpret_cast<uint4 *>(out + tc::op_offset(row, c + 8, kTile)) =
-                        make_uint4(pack2(h[8], h[9]), pack2(h[10], h[11]), pack2(h[12], h[13]), pack2(h[14], h[15]));
+#pragma unroll
+                for (uint32_t c = 0; c < (uint32_t)kHid; c += 32) {
+                    float v[32];
+                    tc::tmem_ld32(taddr + lane_base + c, v);
+#pragma unroll
+                    for (uint32_t k = 0; k < 32; k += 8) {
+                        const float *bb = bias + bias_idx(l) + c + k;
+                        *reinterpret_cast<uint4 *>(out + tc::op_offset(row, c + k, kTile)) = make_uint4(
+                            pack2(relu(v[k] + bb[0]), relu(v[k + 1] + bb[1])),
+                            pack2(relu(v[k + 2] + bb[2]), relu(v[k + 3] + bb[3])),
+                            pack2(relu(v[k + 4] + bb[4]), relu(v[k + 5] + bb[5])),
+                            pack2(relu(v[k + 6] + bb[6]), relu(v[k + 7] + bb[7])));
+                    }
                 }
             } else {
                 float v[16];
