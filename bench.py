@@ -804,6 +804,14 @@ def run_mcrt(args):
         ctx.render(cam, W, H, SPP, first_frame=0, max_depth=DEPTH, outputs=(), count=True)
         t = ctx.timings()
         out["counted"] = {k: int(t[k]) for k in ("rays", "node_fetches", "triangle_fetches", "extend_launches")}
+        out["counted_per_variant"] = {}
+        for v in range(8):                      # each variant's own fetches and extend time on the same frame
+            ctx.render(cam, W, H, SPP, first_frame=0, max_depth=DEPTH, outputs=(), count=True, variant=v)
+            tv = ctx.timings()
+            ctx.render(cam, W, H, SPP, first_frame=0, max_depth=DEPTH, outputs=(), variant=v)
+            out["counted_per_variant"][v] = {"node_fetches_per_ray": round(tv["node_fetches"] / tv["rays"], 3),
+                                             "triangle_fetches_per_ray": round(tv["triangle_fetches"] / tv["rays"], 3),
+                                             "extend_ms": round(ctx.timings()["extend_ms"], 3)}
         ctx.rebuild_bvh()
         ctx.render(cam, W, H, SPP, first_frame=0, max_depth=DEPTH, outputs=())
         out["extend_ms"] = round(ctx.timings()["extend_ms"], 3)

@@ -173,7 +173,14 @@ struct BuildState {
     uint32_t *rkey[2], *rval[2];      // sort keys / primitive ids (ping-pong)
     uint32_t *rhist, *roffs;          // digit counts per tile and their exclusive scan
     float4 *qmin, *qmax, *qcen;       // second set of primitive bounds: the reordering target
+    // single-pass partition scan of a level (k_flag_scan): [0] tile ticket,
+    // [1] error word (a look-back wait gave up), [2 + t] status of tile t:
+    // flag << 32 | value (flag 1: the tile's own sum, 2: inclusive prefix)
+    unsigned long long *part;
 };
+constexpr uint32_t kFlagThreads = 256, kFlagItems = 8;   // k_flag_scan: positions per thread, per block
+constexpr uint32_t kFlagTile = kFlagThreads * kFlagItems;
+constexpr uint32_t kLookbackPolls = 1u << 20;              // polls of one predecessor before giving up
 constexpr uint32_t kSmallTask = 256;       // tasks up to this size are built by one warp each
 constexpr uint32_t kTinyTask = 8;          // and up to this size by one thread each
 constexpr uint32_t kMaxLevels = 4096;
@@ -1101,23 +1108,99 @@ __global__ void k_level_advance(BuildState S, uint32_t level) {
     }
 }
 
-__global__ void k_flags(BuildState S, int cur) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= S.nt) return;
-    int task = S.ptask[cur][i];
-    uint32_t f = 0;
-    if (task >= 0) {
-        int sp = S.t_split[task];
-        if (sp >= 0) {
-            int axis = sp >> 4, bin = sp & 15;
-            const float *cb = S.t_cb + 6 * task;
-            float4 c = S.pcen[S.perm[cur][i]];
-            float cc = axis == 0 ? c.x : (axis == 1 ? c.y : c.z);
-            float len = cb[3 + axis] - cb[axis];
-            f = bin_of(cc, cb[axis], len) <= (uint32_t)bin ? 1u : 0u;
-        }
+// Partition flag of position i: 1 when its primitive goes to the left child of
+// its large task's split, else 0.
+__device__ __forceinline__ uint32_t partition_flag(const BuildState &S, int cur, uint32_t i) {
+    const int task = S.ptask[cur][i];
+    if (task < 0) return 0u;
+    const int sp = S.t_split[task];
+    if (sp < 0) return 0u;
+    const int axis = sp >> 4, bin = sp & 15;
+    const float *cb = S.t_cb + 6 * task;
+    const float4 c = S.pcen[S.perm[cur][i]];
+    const float cc = axis == 0 ? c.x : (axis == 1 ? c.y : c.z);
+    const float len = cb[3 + axis] - cb[axis];
+    return bin_of(cc, cb[axis], len) <= (uint32_t)bin ? 1u : 0u;
+}
+
+// The partition flags of every position and their exclusive scan in one pass
+// (decoupled look-back, Merrill and Garland 2016): a block takes the next tile
+// from a ticket (tiles start in order, so every predecessor of a tile is
+// running or done), scans its kFlagTile flags, publishes its sum, adds its
+// predecessors' published sums walking back to the first inclusive prefix,
+// and publishes its own.  Every wait is bounded: after kLookbackPolls polls the
+// tile records the error word and goes on (the host fails the build).
+__global__ void __launch_bounds__(kFlagThreads) k_flag_scan(BuildState S, int cur) {
+    __shared__ uint32_t s_tile, s_excl, s_warp[kFlagThreads / 32];
+    const uint32_t t = threadIdx.x, lane = t & 31u, w = t >> 5;
+    unsigned long long *status = S.part + 2;
+    if (t == 0) s_tile = atomicAdd(reinterpret_cast<unsigned int *>(S.part), 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t i0 = tile * kFlagTile + t * kFlagItems;
+    uint32_t f[kFlagItems], sum = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < kFlagItems; ++k) {
+        f[k] = i0 + k < S.nt ? partition_flag(S, cur, i0 + k) : 0u;
+        sum += f[k];
     }
-    S.flags[i] = f;
+    uint32_t x = sum;                                          // inclusive scan over the warp
+#pragma unroll
+    for (uint32_t d = 1; d < 32; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, x, d);
+        if (lane >= d) x += y;
+    }
+    if (lane == 31) s_warp[w] = x;
+    __syncthreads();
+    if (w == 0) {                                              // inclusive scan of the warp totals
+        uint32_t v = lane < kFlagThreads / 32 ? s_warp[lane] : 0u;
+#pragma unroll
+        for (uint32_t d = 1; d < kFlagThreads / 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFull, v, d);
+            if (lane >= d) v += y;
+        }
+        if (lane < kFlagThreads / 32) s_warp[lane] = v;
+    }
+    __syncthreads();
+    const uint32_t block_total = s_warp[kFlagThreads / 32 - 1];
+    const uint32_t thread_excl = (w ? s_warp[w - 1] : 0u) + x - sum;
+    if (t == 0) {
+        uint32_t excl = 0;
+        if (tile == 0) {
+            __threadfence();
+            atomicExch(status, (2ull << 32) | block_total);
+        } else {
+            atomicExch(status + tile, (1ull << 32) | block_total);
+            uint32_t j = tile - 1, polls = 0;
+            for (;;) {
+                const unsigned long long v = *reinterpret_cast<volatile unsigned long long *>(status + j);
+                const uint32_t flag = (uint32_t)(v >> 32);
+                if (flag == 0u) {
+                    if (++polls > kLookbackPolls) {
+                        atomicExch(reinterpret_cast<unsigned int *>(S.part + 1), 1u);
+                        break;
+                    }
+                    continue;
+                }
+                excl += (uint32_t)v;
+                if (flag == 2u || j == 0) break;
+                --j;
+            }
+            __threadfence();
+            atomicExch(status + tile, (2ull << 32) | (excl + block_total));
+        }
+        s_excl = excl;
+    }
+    __syncthreads();
+    uint32_t run = s_excl + thread_excl;
+#pragma unroll
+    for (uint32_t k = 0; k < kFlagItems; ++k) {
+        if (i0 + k < S.nt) {
+            S.flags[i0 + k] = f[k];
+            S.scan[i0 + k] = run;
+        }
+        run += f[k];
+    }
 }
 
 __global__ void k_scatter(BuildState S, int cur) {
@@ -1208,6 +1291,7 @@ static cudaError_t gpu_build(const mcrt_gpu_vertex *d_verts, const mcrt_gpu_tria
         acc(256 * tiles * 4); acc(256 * tiles * 4);          // digit counts, offsets
         acc(n * 16); acc(n * 16); acc(n * 16);               // reordered bounds
         for (int k = 0; k < 2; ++k) { acc(tc * 4); acc(tc * 4); acc(tc * 4); acc(tc * 24); }   // tiny tasks
+        acc((2 + (n + kFlagTile - 1) / kFlagTile) * 8);     // partition scan state
         cudaError_t e = cudaMalloc(&sc->mem, bytes);
         if (e != cudaSuccess) { if (err) *err = "BVH scratch allocation failed"; return e; }
         sc->cap = nt;
@@ -1237,6 +1321,7 @@ static cudaError_t gpu_build(const mcrt_gpu_vertex *d_verts, const mcrt_gpu_tria
             S.y_start[k] = carve<uint32_t>(p, tc); S.y_count[k] = carve<uint32_t>(p, tc);
             S.y_node[k] = carve<uint32_t>(p, tc); S.y_bounds[k] = carve<float>(p, 6 * tc);
         }
+        S.part = carve<unsigned long long>(p, 2 + (n + kFlagTile - 1) / kFlagTile);
     }
     BuildState S = sc->s;
     S.nt = nt;
@@ -1297,6 +1382,8 @@ static cudaError_t gpu_build(const mcrt_gpu_vertex *d_verts, const mcrt_gpu_tria
     uint32_t level = 0;
     int cur = 0;
     uint32_t host_counters[8] = {};
+    uint32_t scan_error = 0;
+    const uint32_t n_flag_tiles = (nt + kFlagTile - 1) / kFlagTile;
     auto advance = [&]() -> bool {
         if (level + 1 >= kMaxLevels) {
             if (err) *err = "BVH build exceeded 4096 levels";
@@ -1322,14 +1409,16 @@ static cudaError_t gpu_build(const mcrt_gpu_vertex *d_verts, const mcrt_gpu_tria
         k_centroid_bounds<<<nbp, 256, 0, st>>>(S, cur); ::mcrt::note_launch();
         k_bins<<<nbp, 256, 0, st>>>(S, cur); ::mcrt::note_launch();
         k_split<<<(n_large + 127) / 128, 128, 0, st>>>(S, cur, n_large); ::mcrt::note_launch();
-        k_flags<<<nb, TB, 0, st>>>(S, cur); ::mcrt::note_launch();
-        exclusive_scan_u32(S.flags, S.scan, nt, sc->scan_tmp, st);
+        cudaMemsetAsync(S.part, 0, (2 + (size_t)n_flag_tiles) * 8, st);
+        k_flag_scan<<<n_flag_tiles, kFlagThreads, 0, st>>>(S, cur); ::mcrt::note_launch();
         k_scatter<<<nb, TB, 0, st>>>(S, cur); ::mcrt::note_launch();
         small_round(n_small, n_tiny);
         cur ^= 1;
         cudaMemcpyAsync(host_counters, S.counters, sizeof(host_counters), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(&scan_error, S.part + 1, 4, cudaMemcpyDeviceToHost, st);
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) { if (err) *err = "BVH build level failed"; return e; }
+        if (scan_error) { if (err) *err = "BVH build: partition scan look-back gave up"; return cudaErrorUnknown; }
         n_large = host_counters[0];
         n_small = host_counters[4];
         n_tiny = host_counters[6];
