@@ -147,7 +147,11 @@ typedef struct {
 enum {
     /* take the triangle mesh from the context's last mcrt_world_mesh
      * (vertices / triangles must be NULL); the mesh BVH is built on the GPU */
-    MCRT_SCENE_WORLD_MESH = 1u << 0
+    MCRT_SCENE_WORLD_MESH = 1u << 0,
+    /* take the triangle mesh from the context's device mesh (mcrt_mesh_append,
+     * mcrt_mesh_append_obj, mcrt_mesh_append_scene; vertices / triangles must
+     * be NULL); the mesh BVH is built on the GPU */
+    MCRT_SCENE_DEVICE_MESH = 1u << 1
 };
 
 /* Upload (or replace) the scene.  Replaces gpu_layout::build_scene_buffers
@@ -335,6 +339,52 @@ mcrt_status mcrt_world_mesh(mcrt_ctx *ctx, uint32_t mode, const uint32_t *block_
 mcrt_status mcrt_world_read_mesh(mcrt_ctx *ctx, mcrt_gpu_vertex *vertices, uint32_t vertex_capacity,
                                  mcrt_gpu_triangle *triangles, uint32_t triangle_capacity);
 
+/* ------------------------------------------------------------------ scene ingestion on the device
+ * The context's device mesh collects vertex and triangle records in call order,
+ * as load_scene_from_str concatenates a scene's objects (scene.rs:687-899,
+ * :865-878); mcrt_upload_scene takes it with MCRT_SCENE_DEVICE_MESH.  OBJ text
+ * is parsed on the device (no host parse). */
+
+/* Empty the device mesh (its memory is kept). */
+mcrt_status mcrt_mesh_reset(mcrt_ctx *ctx);
+
+/* Append host records; triangle vertex indices are relative to this call's
+ * first vertex (the library adds the mesh's current vertex count). */
+mcrt_status mcrt_mesh_append(mcrt_ctx *ctx, const mcrt_gpu_vertex *vertices, uint32_t n_vertices,
+                             const mcrt_gpu_triangle *triangles, uint32_t n_triangles);
+
+/* A mesh object's transform, TransformDesc (scene.rs:438-495): uniform scale,
+ * then Euler rotation in degrees (euler_to_mat3, scene.rs:396-405), then the
+ * translation; an absent part is skipped exactly as the reference skips it. */
+typedef struct {
+    uint32_t has_translate, has_rotate, has_scale;
+    float translate[3];
+    float rotate_deg[3];
+    float scale;
+} mcrt_mesh_transform;
+
+/* Parse Wavefront OBJ text on the device and append it: load_obj
+ * (mesh.rs:474-642) with every triangle's mat_idx, then the object's transform
+ * (scene.rs:838-861; NULL = none).  Bit-identical to the reference's records:
+ * UTF-8 check, str::lines / trim / split_ascii_whitespace, correctly rounded
+ * f32 parsing, 1-based and negative indices, (position, uv, normal) vertex
+ * sharing by first occurrence, fan triangulation and the geometric-normal
+ * patch.  Errors (the device mesh is unchanged):
+ *   MCRT_ERR_MESH_LOAD   not UTF-8, or no face (the reference's messages, with
+ *                        source as the path);
+ *   MCRT_ERR_INVALID_ARG scale not positive (checked after parsing, as the
+ *                        reference asserts it), or text of 4 GiB or more.
+ * out_n_vertices / out_n_triangles (optional): this call's counts. */
+mcrt_status mcrt_mesh_append_obj(mcrt_ctx *ctx, const char *text, uint64_t len, uint32_t mat_idx,
+                                 const mcrt_mesh_transform *xf, const char *source, uint32_t *out_n_vertices,
+                                 uint32_t *out_n_triangles);
+
+/* Copy the device mesh to the host (capacities in records; NULL arrays are
+ * skipped); out_n_* receive the mesh's counts. */
+mcrt_status mcrt_mesh_read(mcrt_ctx *ctx, mcrt_gpu_vertex *vertices, uint32_t vertex_capacity,
+                           mcrt_gpu_triangle *triangles, uint32_t triangle_capacity, uint32_t *out_n_vertices,
+                           uint32_t *out_n_triangles);
+
 /* ------------------------------------------------------------------ radiance-cache MLP */
 
 /* Probe of one tensor-core product (no reference counterpart; it pins the
@@ -518,6 +568,21 @@ typedef struct mcrt_loaded_scene mcrt_loaded_scene;
 mcrt_status mcrt_scene_load_yaml(const char *path, mcrt_loaded_scene **out);
 mcrt_status mcrt_scene_load_yaml_str(const char *text, const char *source, mcrt_loaded_scene **out);
 void mcrt_scene_free(mcrt_loaded_scene *scene);
+
+enum {
+    /* Read each mesh object's OBJ file but leave it unparsed: the scene's host
+     * vertices / triangles then hold only the tessellated primitives, and
+     * mcrt_mesh_append_scene parses the meshes on the device. */
+    MCRT_LOAD_DEFER_MESHES = 1u << 0
+};
+mcrt_status mcrt_scene_load_yaml_ex(const char *path, uint32_t flags, mcrt_loaded_scene **out);
+mcrt_status mcrt_scene_load_yaml_str_ex(const char *text, const char *source, uint32_t flags,
+                                        mcrt_loaded_scene **out);
+/* Append a loaded scene's triangle geometry to the context's device mesh in the
+ * reference's object order: tessellated primitives from the host, mesh objects
+ * (of a MCRT_LOAD_DEFER_MESHES load) through mcrt_mesh_append_obj, and the
+ * reference's one-triangle stub when the scene has no geometry (scene.rs:887-899). */
+mcrt_status mcrt_mesh_append_scene(mcrt_ctx *ctx, const mcrt_loaded_scene *scene);
 
 typedef struct {
     const mcrt_gpu_sphere *spheres; uint32_t n_spheres;

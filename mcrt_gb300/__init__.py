@@ -221,8 +221,9 @@ class Context:
 
     def upload_scene(self, *, materials, spheres=None, vertices=None, triangles=None, env=None, sphere_bvh=None,
                      sphere_order=None, mesh_bvh=None, triangle_order=None, albedo=None, sun_dir=None,
-                     sun_irradiance=None, world_mesh=False):
+                     sun_irradiance=None, world_mesh=False, device_mesh=False):
         """world_mesh: take the triangles from the last world_mesh() call (no host geometry).
+        device_mesh: take them from the device mesh (mesh_append*, no host geometry).
         sun_dir / sun_irradiance: a directional light sampled by next-event estimation."""
         sph = _arr(spheres, SPHERE)
         ver = _arr(vertices, VERTEX)
@@ -256,8 +257,72 @@ class Context:
                 d.sun_irradiance[k] = float(sun_irradiance[k])
         if world_mesh:
             d.flags |= N.SCENE_WORLD_MESH
+        if device_mesh:
+            d.flags |= N.SCENE_DEVICE_MESH
         self._check(lib().mcrt_upload_scene(self._h, ctypes.byref(d)))
-        self.n_triangles = self._world_tris if world_mesh else d.n_triangles
+        self.n_triangles = (self._world_tris if world_mesh else self.mesh_counts()[1] if device_mesh
+                            else d.n_triangles)
+
+    # ---------------------------------------------------------------- scene ingestion on the device
+    def mesh_reset(self):
+        """Empty the device mesh."""
+        self._check(lib().mcrt_mesh_reset(self._h))
+
+    def mesh_append(self, vertices, triangles):
+        """Append host records (triangle indices relative to these vertices)."""
+        ver = _arr(vertices, VERTEX)
+        tri = _arr(triangles, TRIANGLE)
+        self._check(lib().mcrt_mesh_append(self._h, ptr(ver), 0 if ver is None else len(ver), ptr(tri),
+                                           0 if tri is None else len(tri)))
+
+    def mesh_append_obj(self, text, mat_idx=0, translate=None, rotate=None, scale=None, source=None):
+        """Parse OBJ text (bytes or str) on the device (load_obj, mesh.rs:474-642) and append
+        it with the mesh object's transform (scene.rs:838-861); returns this call's
+        (n_vertices, n_triangles)."""
+        data = text.encode() if isinstance(text, str) else bytes(text)
+        xf = None
+        if translate is not None or rotate is not None or scale is not None:
+            xf = N.MeshTransform()
+            if translate is not None:
+                xf.has_translate = 1
+                xf.translate[:] = [float(x) for x in translate]
+            if rotate is not None:
+                xf.has_rotate = 1
+                xf.rotate_deg[:] = [float(x) for x in rotate]
+            if scale is not None:
+                xf.has_scale = 1
+                xf.scale = float(scale)
+        nv, nt = c_uint32(), c_uint32()
+        self._check(lib().mcrt_mesh_append_obj(self._h, data, len(data), mat_idx,
+                                               None if xf is None else ctypes.byref(xf),
+                                               None if source is None else source.encode(), ctypes.byref(nv),
+                                               ctypes.byref(nt)))
+        return nv.value, nt.value
+
+    def mesh_counts(self):
+        nv, nt = c_uint32(), c_uint32()
+        self._check(lib().mcrt_mesh_read(self._h, None, 0, None, 0, ctypes.byref(nv), ctypes.byref(nt)))
+        return nv.value, nt.value
+
+    def mesh_read(self):
+        """The device mesh as (vertices, triangles) host records."""
+        nv, nt = self.mesh_counts()
+        v = np.zeros(nv, VERTEX)
+        t = np.zeros(nt, TRIANGLE)
+        self._check(lib().mcrt_mesh_read(self._h, ptr(v), nv, ptr(t), nt, None, None))
+        return v, t
+
+    def mesh_append_scene_yaml(self, path):
+        """Load a scene YAML with its mesh objects left unparsed and append its geometry
+        to the device mesh in object order (OBJ text parsed on the device); returns the
+        host Scene (spheres, materials, camera; its vertices hold the primitives only)."""
+        h = c_void_p()
+        check(lib().mcrt_scene_load_yaml_ex(path.encode(), N.LOAD_DEFER_MESHES, ctypes.byref(h)))
+        try:
+            self._check(lib().mcrt_mesh_append_scene(self._h, h))
+            return _scene_from_handle(h)
+        finally:
+            lib().mcrt_scene_free(h)
 
     # ---------------------------------------------------------------- voxel world
     def world_generate(self, params, read_back=False):

@@ -75,6 +75,8 @@ class CacheParams(ctypes.Structure):
 RENDER_CACHE = 16
 RENDER_COUNT = 32
 SCENE_WORLD_MESH = 1
+SCENE_DEVICE_MESH = 2
+LOAD_DEFER_MESHES = 1
 MESH_GREEDY, MESH_FACES = 0, 1
 
 
@@ -85,6 +87,11 @@ class WorldParams(ctypes.Structure):
                 ("height_octaves", c_uint32), ("lacunarity", c_float), ("gain", c_float),
                 ("cave_freq", c_float), ("cave_octaves", c_uint32), ("cave_threshold", c_float),
                 ("cave_contrast", c_float), ("cave_min_y", c_uint32), ("sea_level", c_float), ("sand_line", c_float)]
+
+
+class MeshTransform(ctypes.Structure):
+    _fields_ = [("has_translate", c_uint32), ("has_rotate", c_uint32), ("has_scale", c_uint32),
+                ("translate", c_float * 3), ("rotate_deg", c_float * 3), ("scale", c_float)]
 
 
 class RenderOpts(ctypes.Structure):
@@ -144,6 +151,13 @@ SIGNATURES = [
     ("mcrt_world_upload", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_int32, c_int32]),
     ("mcrt_world_mesh", c_int, [c_void_p, c_uint32, c_void_p, c_float, POINTER(c_uint32), POINTER(c_uint32)]),
     ("mcrt_world_read_mesh", c_int, [c_void_p, c_void_p, c_uint32, c_void_p, c_uint32]),
+    ("mcrt_mesh_reset", c_int, [c_void_p]),
+    ("mcrt_mesh_append", c_int, [c_void_p, c_void_p, c_uint32, c_void_p, c_uint32]),
+    ("mcrt_mesh_append_obj", c_int, [c_void_p, c_char_p, c_uint64, c_uint32, POINTER(MeshTransform), c_char_p,
+                                     POINTER(c_uint32), POINTER(c_uint32)]),
+    ("mcrt_mesh_read", c_int, [c_void_p, c_void_p, c_uint32, c_void_p, c_uint32, POINTER(c_uint32),
+                               POINTER(c_uint32)]),
+    ("mcrt_mesh_append_scene", c_int, [c_void_p, c_void_p]),
     ("mcrt_adjoint", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_uint32, POINTER(RenderOpts),
                              c_void_p, c_void_p, c_void_p]),
     ("mcrt_autotune", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, POINTER(RenderOpts),
@@ -156,6 +170,8 @@ SIGNATURES = [
     ("mcrt_denoise", c_int, [c_void_p, c_void_p, c_void_p, c_uint32, c_uint32, POINTER(DenoiseParams), c_void_p]),
     ("mcrt_scene_load_yaml", c_int, [c_char_p, POINTER(c_void_p)]),
     ("mcrt_scene_load_yaml_str", c_int, [c_char_p, c_char_p, POINTER(c_void_p)]),
+    ("mcrt_scene_load_yaml_ex", c_int, [c_char_p, c_uint32, POINTER(c_void_p)]),
+    ("mcrt_scene_load_yaml_str_ex", c_int, [c_char_p, c_char_p, c_uint32, POINTER(c_void_p)]),
     ("mcrt_scene_free", None, [c_void_p]),
     ("mcrt_scene_view_get", c_int, [c_void_p, POINTER(SceneView)]),
     ("mcrt_scene_material_name", c_char_p, [c_void_p, c_uint32]),

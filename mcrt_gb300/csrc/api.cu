@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "host/scene_internal.h"
 #include "internal.h"
 #include "mlp_net.cuh"
 
@@ -92,6 +93,10 @@ struct mcrt_ctx {
     int32_t world_cx0 = 0, world_cz0 = 0;
     mcrt::WorldMeshBuffers wmesh;
     bool wmesh_valid = false;
+    // device mesh assembled by mcrt_mesh_append / mcrt_mesh_append_obj
+    mcrt::DeviceMesh dmesh;
+    mcrt::ObjScratch obj;
+    unsigned long long last_obj_lines = 0, last_obj_tokens = 0;
     // batched views and graph replay
     DBuf views, pass_state;
     std::vector<char> view_blob, graph_key;
@@ -403,7 +408,8 @@ void mcrt_destroy(mcrt_ctx *ctx) {
                     &ctx->sum, &ctx->gbuf, &ctx->io_a, &ctx->io_b, &ctx->io_c, &ctx->counters, &ctx->dimg,
                     &ctx->grad, &ctx->world_vox, &ctx->world_matmap, &ctx->wmesh.counts, &ctx->wmesh.vertices,
                     &ctx->wmesh.triangles, &ctx->views, &ctx->pass_state, &ctx->cache_q, &ctx->cache_rec,
-                    &ctx->shade_recs};
+                    &ctx->shade_recs, &ctx->dmesh.vertices, &ctx->dmesh.triangles, &ctx->obj.text,
+                    &ctx->obj.lines, &ctx->obj.tokens, &ctx->obj.staging};
     for (DBuf *b : bufs) b->release();
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     mcrt::cache_destroy(ctx->cache);
@@ -419,10 +425,14 @@ mcrt_status mcrt_upload_scene(mcrt_ctx *ctx, const mcrt_scene_desc *d) {
     if (!d->materials) return fail(ctx, MCRT_ERR_INVALID_ARG, "materials is NULL");
     if (d->n_spheres && !d->spheres) return fail(ctx, MCRT_ERR_INVALID_ARG, "spheres is NULL");
     const bool world_mesh = (d->flags & MCRT_SCENE_WORLD_MESH) != 0;
-    if (world_mesh) {
+    const bool device_mesh = (d->flags & MCRT_SCENE_DEVICE_MESH) != 0;
+    if (world_mesh && device_mesh)
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "MCRT_SCENE_WORLD_MESH and MCRT_SCENE_DEVICE_MESH are exclusive");
+    if (world_mesh || device_mesh) {
         if (d->vertices || d->triangles || d->n_vertices || d->n_triangles || d->mesh_bvh)
-            return fail(ctx, MCRT_ERR_INVALID_ARG, "MCRT_SCENE_WORLD_MESH takes no host vertices, triangles or BVH");
-        if (!ctx->wmesh_valid) return fail(ctx, MCRT_ERR_INVALID_ARG, "no world mesh (call mcrt_world_mesh first)");
+            return fail(ctx, MCRT_ERR_INVALID_ARG, "a device-resident mesh takes no host vertices, triangles or BVH");
+        if (world_mesh && !ctx->wmesh_valid)
+            return fail(ctx, MCRT_ERR_INVALID_ARG, "no world mesh (call mcrt_world_mesh first)");
     }
     for (int k = 0; k < 3; ++k)
         if (!std::isfinite(d->sun_dir[k]) || !std::isfinite(d->sun_irradiance[k]) || d->sun_irradiance[k] < 0.0f)
@@ -459,8 +469,10 @@ mcrt_status mcrt_upload_scene(mcrt_ctx *ctx, const mcrt_scene_desc *d) {
     ctx->has_scene = false;
     ctx->acc_valid = false;
     const uint32_t ns = d->n_spheres;
-    const uint32_t nv = world_mesh ? 4 * ctx->wmesh.n_quads : d->n_vertices;
-    const uint32_t nt = world_mesh ? 2 * ctx->wmesh.n_quads : d->n_triangles;
+    const uint32_t nv = world_mesh ? 4 * ctx->wmesh.n_quads : device_mesh ? ctx->dmesh.nv : d->n_vertices;
+    const uint32_t nt = world_mesh ? 2 * ctx->wmesh.n_quads : device_mesh ? ctx->dmesh.nt : d->n_triangles;
+    const void *dev_vertices = world_mesh ? ctx->wmesh.vertices.p : device_mesh ? ctx->dmesh.vertices.p : nullptr;
+    const void *dev_triangles = world_mesh ? ctx->wmesh.triangles.p : device_mesh ? ctx->dmesh.triangles.p : nullptr;
 
     // ---- spheres, stored in BVH order, with their original ids
     CK(ctx->spheres.ensure((size_t)ns * 32), "allocate spheres");
@@ -498,8 +510,8 @@ mcrt_status mcrt_upload_scene(mcrt_ctx *ctx, const mcrt_scene_desc *d) {
     // ---- vertices
     CK(ctx->vertices.ensure((size_t)nv * 48), "allocate vertices");
     if (nv)
-        CK(cudaMemcpyAsync(ctx->vertices.p, world_mesh ? ctx->wmesh.vertices.p : (const void *)d->vertices,
-                           (size_t)nv * 48, world_mesh ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st),
+        CK(cudaMemcpyAsync(ctx->vertices.p, dev_vertices ? dev_vertices : (const void *)d->vertices,
+                           (size_t)nv * 48, dev_vertices ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st),
            "upload");
     ctx->n_vertices = nv;
     // ---- triangles (kept in original order on the device) and the mesh BVH
@@ -526,8 +538,8 @@ mcrt_status mcrt_upload_scene(mcrt_ctx *ctx, const mcrt_scene_desc *d) {
             mcrt_status s = finish_mesh(ctx);
             if (s != MCRT_OK) return s;
         } else {
-            CK(cudaMemcpyAsync(ctx->triangles.p, world_mesh ? ctx->wmesh.triangles.p : (const void *)d->triangles,
-                               (size_t)nt * 16, world_mesh ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st),
+            CK(cudaMemcpyAsync(ctx->triangles.p, dev_triangles ? dev_triangles : (const void *)d->triangles,
+                               (size_t)nt * 16, dev_triangles ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st),
                "upload");
             mcrt_status s = build_mesh_bvh_gpu(ctx);
             if (s != MCRT_OK) return s;
@@ -1235,6 +1247,115 @@ mcrt_status mcrt_world_read_mesh(mcrt_ctx *ctx, mcrt_gpu_vertex *vertices, uint3
         CK(cudaMemcpy(triangles, ctx->wmesh.triangles.p, (size_t)nt * sizeof(mcrt_gpu_triangle),
                       cudaMemcpyDeviceToHost),
            "read triangles");
+    return MCRT_OK;
+}
+
+// ---------------------------------------------------------------- scene ingestion on the device
+
+mcrt_status mcrt_mesh_reset(mcrt_ctx *ctx) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    ctx->dmesh.nv = ctx->dmesh.nt = 0;
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_mesh_append(mcrt_ctx *ctx, const mcrt_gpu_vertex *vertices, uint32_t n_vertices,
+                             const mcrt_gpu_triangle *triangles, uint32_t n_triangles) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if ((n_vertices && !vertices) || (n_triangles && !triangles))
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "vertices or triangles is NULL");
+    for (uint32_t i = 0; i < n_triangles; ++i)
+        for (int k = 0; k < 3; ++k)
+            if (triangles[i].v[k] >= n_vertices)
+                return fail(ctx, MCRT_ERR_INVALID_ARG,
+                            "triangle " + std::to_string(i) + " references a vertex beyond n_vertices");
+    if ((uint64_t)ctx->dmesh.nv + n_vertices >= (1ull << 31) || (uint64_t)ctx->dmesh.nt + n_triangles >= (1ull << 27))
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "device mesh too large");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    CK(mcrt::mesh_append_host(ctx->dmesh, vertices, n_vertices, triangles, n_triangles, ctx->obj.staging, ctx->stream),
+       "append to the device mesh");
+    return MCRT_OK;
+}
+
+namespace {
+// Utf8Error::error_len of the invalid sequence at text[i] (core::str::run_utf8_validation):
+// 1-3 bytes, or 0 when the text ends inside the sequence.
+int utf8_error_len(const unsigned char *t, unsigned long long len, unsigned long long i) {
+    const unsigned char b = t[i];
+    auto cont = [](unsigned char x) { return (x & 0xC0) == 0x80; };
+    const int w = (b >= 0xC2 && b <= 0xDF) ? 2 : (b >= 0xE0 && b <= 0xEF) ? 3 : (b >= 0xF0 && b <= 0xF4) ? 4 : 0;
+    if (w == 0) return 1;
+    if (i + 1 >= len) return 0;
+    const unsigned char b1 = t[i + 1];
+    bool ok = w == 2   ? cont(b1)
+              : w == 3 ? (b == 0xE0 && b1 >= 0xA0 && b1 <= 0xBF) || (b >= 0xE1 && b <= 0xEC && cont(b1)) ||
+                             (b == 0xED && b1 >= 0x80 && b1 <= 0x9F) || (b >= 0xEE && cont(b1))
+                       : (b == 0xF0 && b1 >= 0x90 && b1 <= 0xBF) || (b >= 0xF1 && b <= 0xF3 && cont(b1)) ||
+                             (b == 0xF4 && b1 >= 0x80 && b1 <= 0x8F);
+    if (!ok) return 1;
+    for (int k = 2; k < w; ++k) {
+        if (i + k >= len) return 0;
+        if (!cont(t[i + k])) return k;
+    }
+    return 1;   // not reached for a sequence the device check rejected
+}
+}  // namespace
+
+mcrt_status mcrt_mesh_append_obj(mcrt_ctx *ctx, const char *text, uint64_t len, uint32_t mat_idx,
+                                 const mcrt_mesh_transform *xf, const char *source, uint32_t *out_n_vertices,
+                                 uint32_t *out_n_triangles) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (len && !text) return fail(ctx, MCRT_ERR_INVALID_ARG, "text is NULL");
+    const std::string src = source ? source : "<obj>";
+    mcrt::ObjTransform X{};
+    X.identity = !xf || (!xf->has_translate && !xf->has_rotate && !xf->has_scale);
+    X.s = xf && xf->has_scale ? xf->scale : 1.0f;
+    X.has_r = xf && xf->has_rotate;
+    for (int k = 0; k < 3; ++k) X.t[k] = xf && xf->has_translate ? xf->translate[k] : 0.0f;
+    if (X.has_r) mcrt_host::rotation_matrix(xf->rotate_deg, X.m);
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const uint32_t nv0 = ctx->dmesh.nv, nt0 = ctx->dmesh.nt;
+    mcrt::ObjOutcome r;
+    cudaError_t e = mcrt::obj_append(text, len, mat_idx, X, ctx->dmesh, ctx->obj, ctx->stream, &r);
+    if (e == cudaErrorInvalidValue)
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "OBJ text '" + src + "' is beyond the device parser's limits");
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "OBJ parse");
+    const std::string head = "mesh load error: failed to load mesh '" + src + "': '" + src + "'";   // scene.rs:835-837
+    if (r.code == mcrt::ObjOutcome::kNotUtf8) {                                                        // mesh.rs:477-478
+        const int el = utf8_error_len(reinterpret_cast<const unsigned char *>(text), len, r.valid_up_to);
+        return fail(ctx, MCRT_ERR_MESH_LOAD,
+                    head + " is not valid UTF-8: " +
+                        (el ? "invalid utf-8 sequence of " + std::to_string(el) + " bytes from index "
+                            : std::string("incomplete utf-8 byte sequence from index ")) +
+                        std::to_string(r.valid_up_to));
+    }
+    if (r.code == mcrt::ObjOutcome::kNoGeometry)                                                       // mesh.rs:636-638
+        return fail(ctx, MCRT_ERR_MESH_LOAD, head + ": no geometry found after parsing");
+    if (!(X.s > 0.0f)) {                                           // scene.rs:842-847, checked after the load
+        ctx->dmesh.nv = nv0;
+        ctx->dmesh.nt = nt0;
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "mesh '" + src + "' transform.scale must be positive");
+    }
+    ctx->last_obj_lines = r.n_lines;
+    ctx->last_obj_tokens = r.n_tokens;
+    if (out_n_vertices) *out_n_vertices = r.n_vertices;
+    if (out_n_triangles) *out_n_triangles = r.n_triangles;
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_mesh_read(mcrt_ctx *ctx, mcrt_gpu_vertex *vertices, uint32_t vertex_capacity,
+                           mcrt_gpu_triangle *triangles, uint32_t triangle_capacity, uint32_t *out_n_vertices,
+                           uint32_t *out_n_triangles) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    const uint32_t nv = ctx->dmesh.nv, nt = ctx->dmesh.nt;
+    if (out_n_vertices) *out_n_vertices = nv;
+    if (out_n_triangles) *out_n_triangles = nt;
+    if ((vertices && vertex_capacity < nv) || (triangles && triangle_capacity < nt))
+        return fail(ctx, MCRT_ERR_INVALID_ARG, "capacity too small");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if (vertices && nv)
+        CK(cudaMemcpy(vertices, ctx->dmesh.vertices.p, (size_t)nv * 48, cudaMemcpyDeviceToHost), "read vertices");
+    if (triangles && nt)
+        CK(cudaMemcpy(triangles, ctx->dmesh.triangles.p, (size_t)nt * 16, cudaMemcpyDeviceToHost), "read triangles");
     return MCRT_OK;
 }
 

@@ -74,7 +74,7 @@ extern "C" mcrt_status mcrt_headless_run(const char *scene_path, const char *out
     uint32_t N = spp ? spp : (sc.spp ? sc.spp : 64);
     W = W ? W : 1; H = H ? H : 1; N = N ? N : 1;
     mcrt_loaded_scene *ls = nullptr;
-    mcrt_status st = mcrt_scene_load_yaml(scene_path, &ls);
+    mcrt_status st = mcrt_scene_load_yaml_ex(scene_path, MCRT_LOAD_DEFER_MESHES, &ls);   // OBJ meshes parse on the device
     if (st != MCRT_OK) return st;
     mcrt_scene_view v;
     mcrt_scene_view_get(ls, &v);
@@ -85,11 +85,11 @@ extern "C" mcrt_status mcrt_headless_run(const char *scene_path, const char *out
     if (st != MCRT_OK) { mcrt_scene_free(ls); return st; }
     mcrt_scene_desc d{};
     d.spheres = v.spheres; d.n_spheres = v.n_spheres;
-    d.vertices = v.vertices; d.n_vertices = v.n_vertices;
-    d.triangles = v.triangles; d.n_triangles = v.n_triangles;
     d.materials = v.materials;
     d.env_rgba = env.data(); d.env_w = MCRT_ENV_MAP_WIDTH; d.env_h = MCRT_ENV_MAP_HEIGHT;
-    st = mcrt_upload_scene(ctx, &d);
+    d.flags = MCRT_SCENE_DEVICE_MESH;
+    st = mcrt_mesh_append_scene(ctx, ls);
+    if (st == MCRT_OK) st = mcrt_upload_scene(ctx, &d);
     std::vector<float> img((size_t)W * H * 4);
     if (st == MCRT_OK) {
         float lf[3] = {0.0f, 1.0f, 3.5f}, la[3] = {0.0f, 0.0f, 0.0f};

@@ -244,36 +244,121 @@ void push_quad_face(const float c[3], const float n[3], float hw, float hh, uint
 
 }  // namespace
 
-// ---- OBJ loader (mesh.rs:474-642)
+// ---- OBJ loader (mesh.rs:474-642), with the Rust string rules it relies on
 namespace {
 inline void normalize3_obj(const float v[3], float o[3]) {     // mesh.rs:663-670
     float len = sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
     if (len < 1e-8f) { o[0] = 0.0f; o[1] = 1.0f; o[2] = 0.0f; return; }
     o[0] = v[0] / len; o[1] = v[1] / len; o[2] = v[2] / len;
 }
-bool parse_f32_strict(const std::string &s, float *out) {      // Rust str::parse::<f32>
-    if (s.empty()) return false;
-    for (char c : s) if (c == 'x' || c == 'X') return false;
-    char *end = nullptr;
-    float v = strtof(s.c_str(), &end);
-    if (end == s.c_str() || *end != '\0') return false;
-    *out = v;
+// String::from_utf8: the first invalid sequence and its length (0: the text
+// ends inside it), as core::str::run_utf8_validation reports them.
+bool utf8_valid(const std::string &t, size_t *at, int *error_len) {
+    const size_t n = t.size();
+    auto byte = [&](size_t i) { return (unsigned char)t[i]; };
+    auto cont = [](unsigned char b) { return (b & 0xC0) == 0x80; };
+    for (size_t i = 0; i < n;) {
+        const unsigned char b = byte(i);
+        if (b < 0x80) { ++i; continue; }
+        *at = i;
+        const int w = (b >= 0xC2 && b <= 0xDF) ? 2 : (b >= 0xE0 && b <= 0xEF) ? 3 : (b >= 0xF0 && b <= 0xF4) ? 4 : 0;
+        if (w == 0) { *error_len = 1; return false; }
+        if (i + 1 >= n) { *error_len = 0; return false; }
+        const unsigned char b1 = byte(i + 1);
+        const bool ok = w == 2   ? cont(b1)
+                        : w == 3 ? (b == 0xE0 && b1 >= 0xA0 && b1 <= 0xBF) || (b >= 0xE1 && b <= 0xEC && cont(b1)) ||
+                                       (b == 0xED && b1 >= 0x80 && b1 <= 0x9F) || (b >= 0xEE && cont(b1))
+                                 : (b == 0xF0 && b1 >= 0x90 && b1 <= 0xBF) || (b >= 0xF1 && b <= 0xF3 && cont(b1)) ||
+                                       (b == 0xF4 && b1 >= 0x80 && b1 <= 0x8F);
+        if (!ok) { *error_len = 1; return false; }
+        for (int k = 2; k < w; ++k) {
+            if (i + k >= n) { *error_len = 0; return false; }
+            if (!cont(byte(i + k))) { *error_len = k; return false; }
+        }
+        i += w;
+    }
     return true;
 }
-bool parse_i64_strict(const std::string &s, long long *out) {
-    if (s.empty()) return false;
-    char *end = nullptr;
-    long long v = strtoll(s.c_str(), &end, 10);
-    if (end == s.c_str() || *end != '\0') return false;
-    *out = v;
-    return true;
+// char::is_whitespace of the character that starts at s[i] (bytes), or 0.
+int ws_len_at(const std::string &s, size_t i, size_t end) {
+    const unsigned char c = s[i];
+    auto at = [&](size_t k) { return i + k < end ? (unsigned char)s[i + k] : 0u; };
+    if (c == ' ' || (c >= 0x09 && c <= 0x0D)) return 1;
+    if (c == 0xC2 && (at(1) == 0x85 || at(1) == 0xA0)) return 2;
+    if (c == 0xE1 && at(1) == 0x9A && at(2) == 0x80) return 3;
+    if (c == 0xE2 && at(1) == 0x80 && i + 2 < end && (at(2) <= 0x8A || at(2) == 0xA8 || at(2) == 0xA9 || at(2) == 0xAF))
+        return 3;
+    if (c == 0xE2 && at(1) == 0x81 && at(2) == 0x9F) return 3;
+    if (c == 0xE3 && at(1) == 0x80 && at(2) == 0x80) return 3;
+    return 0;
 }
-std::vector<std::string> split_ws(const std::string &s) {
+// str::trim of s[b, e) (valid UTF-8).
+void trim_range(const std::string &s, size_t *b, size_t *e) {
+    int n;
+    while (*b < *e && (n = ws_len_at(s, *b, *e)) > 0) *b += n;
+    for (;;) {
+        if (*e > *b && ws_len_at(s, *e - 1, *e) == 1) { *e -= 1; continue; }
+        if (*e >= *b + 2 && ws_len_at(s, *e - 2, *e) == 2) { *e -= 2; continue; }
+        if (*e >= *b + 3 && ws_len_at(s, *e - 3, *e) == 3) { *e -= 3; continue; }
+        break;
+    }
+}
+inline bool ascii_ws(char c) { return c == ' ' || c == '\t' || c == '\n' || c == '\x0C' || c == '\r'; }
+std::vector<std::string> split_ascii_ws(const std::string &s, size_t b, size_t e) {   // str::split_ascii_whitespace
     std::vector<std::string> out;
-    std::istringstream ss(s);
-    std::string t;
-    while (ss >> t) out.push_back(t);
+    while (b < e) {
+        while (b < e && ascii_ws(s[b])) ++b;
+        size_t t = b;
+        while (b < e && !ascii_ws(s[b])) ++b;
+        if (b > t) out.push_back(s.substr(t, b - t));
+    }
     return out;
+}
+// str::parse::<f32> (core::num::dec2flt grammar; strtof rounds correctly).
+bool parse_f32_strict(const std::string &s, float *out) {
+    size_t i = 0;
+    bool neg = false;
+    if (i < s.size() && (s[i] == '+' || s[i] == '-')) { neg = s[i] == '-'; ++i; }
+    std::string body = s.substr(i);
+    for (char &c : body) c = (char)((c >= 'A' && c <= 'Z') ? c - 'A' + 'a' : c);
+    if (body == "inf" || body == "infinity") { *out = neg ? -INFINITY : INFINITY; return true; }
+    if (body == "nan") {
+        const uint32_t bits = neg ? 0xFFC00000u : 0x7FC00000u;
+        std::memcpy(out, &bits, 4);
+        return true;
+    }
+    size_t digits = 0;
+    while (i < s.size() && s[i] >= '0' && s[i] <= '9') { ++i; ++digits; }
+    if (i < s.size() && s[i] == '.')
+        for (++i; i < s.size() && s[i] >= '0' && s[i] <= '9'; ++i) ++digits;
+    if (digits == 0) return false;
+    if (i < s.size() && (s[i] == 'e' || s[i] == 'E')) {
+        ++i;
+        if (i < s.size() && (s[i] == '+' || s[i] == '-')) ++i;
+        size_t ed = 0;
+        for (; i < s.size() && s[i] >= '0' && s[i] <= '9'; ++i) ++ed;
+        if (ed == 0) return false;
+    }
+    if (i != s.size()) return false;
+    *out = strtof(s.c_str(), nullptr);
+    return true;
+}
+// str::parse::<i64>: optional sign, digits, no overflow.
+bool parse_i64_strict(const std::string &s, long long *out) {
+    size_t i = 0;
+    bool neg = false;
+    if (i < s.size() && (s[i] == '+' || s[i] == '-')) { neg = s[i] == '-'; ++i; }
+    if (i == s.size()) return false;
+    const unsigned long long lim = neg ? 9223372036854775808ull : 9223372036854775807ull;
+    unsigned long long v = 0;
+    for (; i < s.size(); ++i) {
+        if (s[i] < '0' || s[i] > '9') return false;
+        const unsigned d = (unsigned)(s[i] - '0');
+        if (v > (lim - d) / 10) return false;
+        v = v * 10 + d;
+    }
+    *out = neg ? (long long)(0ull - v) : (long long)v;
+    return true;
 }
 std::vector<std::string> split_char(const std::string &s, char c) {
     std::vector<std::string> out;
@@ -290,10 +375,20 @@ std::vector<std::string> split_char(const std::string &s, char c) {
 
 bool load_obj_text(const std::string &content, uint32_t mat_idx, std::vector<mcrt_gpu_vertex> *verts_out,
                    std::vector<mcrt_gpu_triangle> *tris_out, std::string *err) {
+    size_t bad_at = 0;
+    int bad_len = 0;
+    if (!utf8_valid(content, &bad_at, &bad_len)) {                              // mesh.rs:477-478
+        *err = std::string(" is not valid UTF-8: ") +
+               (bad_len ? "invalid utf-8 sequence of " + std::to_string(bad_len) + " bytes from index "
+                        : std::string("incomplete utf-8 byte sequence from index ")) +
+               std::to_string(bad_at);
+        return false;
+    }
     std::vector<float> pos, nrm, uvs;   // flattened 3 / 3 / 2
     std::vector<mcrt_gpu_vertex> vertices;
     std::vector<mcrt_gpu_triangle> triangles;
-    std::map<std::tuple<uint32_t, uint32_t, uint32_t>, uint32_t> cache;
+    std::unordered_map<uint64_t, uint32_t> cache_pt;               // (pos, uv) -> dense id
+    std::unordered_map<uint64_t, uint32_t> cache;                  // (dense id, normal) -> vertex
     auto resolve = [](const std::string &raw, size_t len, uint32_t *out) {
         long long i;
         if (!parse_i64_strict(raw, &i)) return false;
@@ -301,12 +396,13 @@ bool load_obj_text(const std::string &content, uint32_t mat_idx, std::vector<mcr
         if (idx >= 0 && (size_t)idx < len) { *out = (uint32_t)idx; return true; }
         return false;
     };
-    std::istringstream in(content);
-    std::string line;
-    while (std::getline(in, line)) {
-        if (!line.empty() && line.back() == '\r') line.pop_back();
-        std::vector<std::string> parts = split_ws(line);
-        if (parts.empty() || parts[0][0] == '#') continue;
+    for (size_t lb = 0; lb < content.size();) {                                // str::lines + str::trim
+        size_t nl = content.find('\n', lb);
+        size_t b = lb, e = nl == std::string::npos ? content.size() : nl;
+        lb = nl == std::string::npos ? content.size() : nl + 1;
+        trim_range(content, &b, &e);
+        if (b == e || content[b] == '#') continue;
+        std::vector<std::string> parts = split_ascii_ws(content, b, e);
         const std::string &tag = parts[0];
         std::vector<std::string> rest(parts.begin() + 1, parts.end());
         auto f = [&](size_t k) { float v = 0.0f; if (!parse_f32_strict(rest[k], &v)) v = 0.0f; return v; };
@@ -339,13 +435,14 @@ bool load_obj_text(const std::string &content, uint32_t mat_idx, std::vector<mcr
                     return v;
                 };
                 uint32_t vi;
-                if (ni != 0xffffffffu) {
-                    auto key = std::make_tuple(pi, ti, ni);
+                if (ni != 0xffffffffu) {                                       // vert_cache, mesh.rs:556-575
+                    auto ins = cache_pt.emplace((uint64_t)pi | ((uint64_t)ti << 32), (uint32_t)cache_pt.size());
+                    const uint64_t key = (uint64_t)ins.first->second | ((uint64_t)ni << 32);
                     auto it = cache.find(key);
                     if (it == cache.end()) {
                         vi = (uint32_t)vertices.size();
                         vertices.push_back(make_vertex(true));
-                        cache[key] = vi;
+                        cache.emplace(key, vi);
                     } else {
                         vi = it->second;
                     }
@@ -355,7 +452,7 @@ bool load_obj_text(const std::string &content, uint32_t mat_idx, std::vector<mcr
                 }
                 face.push_back(vi);
             }
-            for (size_t i = 1; i + 1 < face.size(); ++i) {              // fan, mesh.rs:580-613
+            for (size_t i = 1; i + 1 < face.size(); ++i) {              // fan, mesh.rs:593-630
                 uint32_t v0 = face[0], v1 = face[i], v2 = face[i + 1];
                 const std::string keys[3] = {rest[0], rest[i], i + 1 < rest.size() ? rest[i + 1] : std::string()};
                 const uint32_t vis[3] = {v0, v1, v2};
@@ -378,14 +475,21 @@ bool load_obj_text(const std::string &content, uint32_t mat_idx, std::vector<mcr
             }
         }
     }
-    if (vertices.empty() || triangles.empty()) { *err = "no geometry found after parsing"; return false; }
+    if (vertices.empty() || triangles.empty()) { *err = ": no geometry found after parsing"; return false; }
     *verts_out = std::move(vertices);
     *tris_out = std::move(triangles);
     return true;
 }
 
+void rotation_matrix(const float deg[3], float m[9]) {
+    M3 r = euler_to_mat3(deg[0], deg[1], deg[2]);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) m[3 * i + j] = r.m[i][j];
+}
+
 // ---- load_scene_from_str (scene.rs:640-978)
-mcrt_status load_scene(const std::string &text, const std::string &src, LoadedScene *out, std::string *errmsg) {
+mcrt_status load_scene(const std::string &text, const std::string &src, LoadedScene *out, std::string *errmsg,
+                       bool defer_meshes) {
     YNode root;
     std::string yerr;
     if (!yaml_parse(text, &root, &yerr)) {
@@ -505,11 +609,24 @@ mcrt_status load_scene(const std::string &text, const std::string &src, LoadedSc
                     *errmsg = "mesh load error: failed to load mesh '" + path + "': cannot read '" + path + "'";
                     return MCRT_ERR_MESH_LOAD;
                 }
+                if (defer_meshes) {                       // parsed on the device by mcrt_mesh_append_scene
+                    LoadedScene::MeshRef m;
+                    m.path = path;
+                    m.text = std::move(content);
+                    m.mat_idx = mi;
+                    m.xf.has_translate = t.has_t; m.xf.has_rotate = t.has_r; m.xf.has_scale = t.has_s;
+                    for (int k = 0; k < 3; ++k) { m.xf.translate[k] = t.t[k]; m.xf.rotate_deg[k] = t.r[k]; }
+                    m.xf.scale = t.s;
+                    m.at_vertex = S.vertices.size();
+                    m.at_triangle = S.triangles.size();
+                    S.meshes.push_back(std::move(m));
+                    continue;
+                }
                 std::vector<mcrt_gpu_vertex> mv;
                 std::vector<mcrt_gpu_triangle> mt;
                 std::string oerr;
                 if (!load_obj_text(content, mi, &mv, &mt, &oerr)) {
-                    *errmsg = "mesh load error: failed to load mesh '" + path + "': '" + path + "': " + oerr;
+                    *errmsg = "mesh load error: failed to load mesh '" + path + "': '" + path + "'" + oerr;
                     return MCRT_ERR_MESH_LOAD;
                 }
                 if (!(t.s > 0.0f)) {
@@ -538,7 +655,8 @@ mcrt_status load_scene(const std::string &text, const std::string &src, LoadedSc
             }
         }
     }
-    if (S.vertices.empty()) {                                                     // scene.rs:887-899
+    S.deferred = defer_meshes;
+    if (S.vertices.empty() && S.meshes.empty()) {                                 // scene.rs:887-899
         mcrt_gpu_vertex v{};
         v.position[0] = 1.0e9f; v.position[1] = 1.0e9f; v.position[2] = 1.0e9f; v.position[3] = 1.0f;
         v.normal[1] = 1.0f;
@@ -751,12 +869,15 @@ void load_env_map_data(const char *scene_path, float *out) {
 // ====================================================================== ABI
 extern "C" {
 
-mcrt_status mcrt_scene_load_yaml_str(const char *text, const char *source, mcrt_loaded_scene **out) {
+mcrt_status mcrt_scene_load_yaml_str_ex(const char *text, const char *source, uint32_t flags,
+                                        mcrt_loaded_scene **out) {
     if (!text || !out) { mcrt::set_global_error("NULL argument"); return MCRT_ERR_INVALID_ARG; }
+    if (flags & ~(uint32_t)MCRT_LOAD_DEFER_MESHES) { mcrt::set_global_error("unknown flags"); return MCRT_ERR_INVALID_ARG; }
     *out = nullptr;
     auto *ls = new mcrt_loaded_scene();
     std::string err;
-    mcrt_status s = mcrt_host::load_scene(text, source ? source : "<inline>", &ls->s, &err);
+    mcrt_status s = mcrt_host::load_scene(text, source ? source : "<inline>", &ls->s, &err,
+                                          (flags & MCRT_LOAD_DEFER_MESHES) != 0);
     if (s != MCRT_OK) {
         delete ls;
         mcrt::set_global_error(err);
@@ -766,14 +887,48 @@ mcrt_status mcrt_scene_load_yaml_str(const char *text, const char *source, mcrt_
     return MCRT_OK;
 }
 
-mcrt_status mcrt_scene_load_yaml(const char *path, mcrt_loaded_scene **out) {
+mcrt_status mcrt_scene_load_yaml_str(const char *text, const char *source, mcrt_loaded_scene **out) {
+    return mcrt_scene_load_yaml_str_ex(text, source, 0, out);
+}
+
+mcrt_status mcrt_scene_load_yaml_ex(const char *path, uint32_t flags, mcrt_loaded_scene **out) {
     if (!path || !out) { mcrt::set_global_error("NULL argument"); return MCRT_ERR_INVALID_ARG; }
     std::string text;
     if (!mcrt_host::read_file(path, &text)) {
         mcrt::set_global_error(std::string("I/O error: cannot read '") + path + "'");
         return MCRT_ERR_IO;
     }
-    return mcrt_scene_load_yaml_str(text.c_str(), path, out);
+    return mcrt_scene_load_yaml_str_ex(text.c_str(), path, flags, out);
+}
+
+mcrt_status mcrt_scene_load_yaml(const char *path, mcrt_loaded_scene **out) {
+    return mcrt_scene_load_yaml_ex(path, 0, out);
+}
+
+// The scene's objects in order (scene.rs:687-899): runs of host records
+// between the deferred mesh objects, each mesh parsed on the device.
+mcrt_status mcrt_mesh_append_scene(mcrt_ctx *ctx, const mcrt_loaded_scene *scene) {
+    if (!ctx || !scene) { mcrt::set_global_error("NULL argument"); return MCRT_ERR_INVALID_ARG; }
+    const mcrt_host::LoadedScene &S = scene->s;
+    size_t v_done = 0, t_done = 0;
+    auto host_run = [&](size_t v_end, size_t t_end) -> mcrt_status {
+        std::vector<mcrt_gpu_triangle> tris(S.triangles.begin() + t_done, S.triangles.begin() + t_end);
+        for (auto &t : tris)
+            for (int k = 0; k < 3; ++k) t.v[k] -= (uint32_t)v_done;
+        mcrt_status st = mcrt_mesh_append(ctx, S.vertices.data() + v_done, (uint32_t)(v_end - v_done), tris.data(),
+                                          (uint32_t)tris.size());
+        v_done = v_end;
+        t_done = t_end;
+        return st;
+    };
+    for (const auto &m : S.meshes) {
+        mcrt_status st = host_run(m.at_vertex, m.at_triangle);
+        if (st != MCRT_OK) return st;
+        st = mcrt_mesh_append_obj(ctx, m.text.data(), m.text.size(), m.mat_idx, &m.xf, m.path.c_str(), nullptr,
+                                  nullptr);
+        if (st != MCRT_OK) return st;
+    }
+    return host_run(S.vertices.size(), S.triangles.size());
 }
 
 void mcrt_scene_free(mcrt_loaded_scene *scene) { delete scene; }

@@ -26,9 +26,24 @@ struct LoadedScene {
     bool has_env_map = false;
     std::string env_map_path;
     std::vector<std::string> material_names;
+    // Mesh objects of a deferred load (MCRT_LOAD_DEFER_MESHES), in object
+    // order: the OBJ text, and where its records go between the host records.
+    struct MeshRef {
+        std::string path, text;
+        uint32_t mat_idx = 0;
+        mcrt_mesh_transform xf{};
+        size_t at_vertex = 0, at_triangle = 0;
+    };
+    std::vector<MeshRef> meshes;
+    bool deferred = false;
 };
 
-mcrt_status load_scene(const std::string &text, const std::string &src, LoadedScene *out, std::string *errmsg);
+mcrt_status load_scene(const std::string &text, const std::string &src, LoadedScene *out, std::string *errmsg,
+                       bool defer_meshes = false);
+// euler_to_mat3 (scene.rs:396-405) of angles in degrees, row-major.
+void rotation_matrix(const float deg[3], float m[9]);
+// load_obj (mesh.rs:474-642) of OBJ text; on failure err is the reference's
+// message after "'<path>'" (" is not valid UTF-8: ..." or ": no geometry ...").
 bool load_obj_text(const std::string &content, uint32_t mat_idx, std::vector<mcrt_gpu_vertex> *verts,
                    std::vector<mcrt_gpu_triangle> *tris, std::string *err);
 void compute_camera(uint32_t width, uint32_t height, const float lf[3], const float la[3], float vfov_deg,

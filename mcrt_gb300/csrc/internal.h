@@ -163,6 +163,40 @@ void launch_world_generate(const mcrt_world_params &P, uint8_t *vox, cudaStream_
 cudaError_t world_mesh(const uint8_t *d_vox, uint32_t nx, uint32_t ny, uint32_t nz, int32_t chunk_x0, int32_t chunk_z0,
                        bool greedy, const uint32_t *d_mat_of, float voxel, WorldMeshBuffers &M, cudaStream_t st);
 
+// Scene ingestion on the device (obj.cu)
+// The context's device mesh: vertex and triangle records in append order.
+struct DeviceMesh {
+    DBuf vertices, triangles;
+    uint32_t nv = 0, nt = 0;
+};
+struct ObjScratch {
+    DBuf text, lines, tokens, staging;
+};
+// A mesh object's transform (scene.rs:438-495) as the kernel applies it:
+// q = p * s, then m (row-major, has_r) applied to q, then + t.
+struct ObjTransform {
+    int identity;
+    int has_r;
+    float s;
+    float m[9];
+    float t[3];
+};
+struct ObjOutcome {
+    enum { kOk = 0, kNotUtf8 = 1, kNoGeometry = 2 };
+    int code = kNoGeometry;
+    unsigned long long valid_up_to = 0;   // first invalid byte (kNotUtf8)
+    uint32_t n_vertices = 0, n_triangles = 0, n_lines = 0, n_tokens = 0;
+};
+// Grow the mesh's buffers (keeping their records) for add_v / add_t more.
+cudaError_t mesh_reserve(DeviceMesh &M, uint32_t add_v, uint32_t add_t, cudaStream_t st);
+// Append host records; triangle indices are relative to this piece's first vertex.
+cudaError_t mesh_append_host(DeviceMesh &M, const mcrt_gpu_vertex *v, uint32_t nv, const mcrt_gpu_triangle *t,
+                             uint32_t nt, DBuf &staging, cudaStream_t st);
+// load_obj (mesh.rs:474-642) of host OBJ text on the device, transformed and
+// appended to M.  cudaErrorInvalidValue: text or mesh beyond the parser's limits.
+cudaError_t obj_append(const char *host_text, unsigned long long len, uint32_t mat_idx, const ObjTransform &X,
+                       DeviceMesh &M, ObjScratch &S, cudaStream_t st, ObjOutcome *out);
+
 // Radiance-cache MLP (mlp.cu)
 struct CacheState;
 CacheState *cache_create();

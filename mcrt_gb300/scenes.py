@@ -335,3 +335,110 @@ def displaced_icosphere(seed: int = 1234, level: int = 8, width: int = 1920, hei
     camera = dict(look_from=[0.0, 2.2, 4.2], look_at=[0.0, 1.1, 0.0], vfov=40.0, aperture=0.0)
     return dict(vertices=V, triangles=T, materials=md, spheres=np.zeros(0, SPHERE), env=env, camera=camera,
                 width=width, height=height, spp=16, max_depth=12)
+
+
+# ---------------------------------------------------------------------------- OBJ text
+
+def _fixed_field(x: np.ndarray, width: int, decimals: int) -> np.ndarray:
+    """Fixed-point decimal text of float values, right-aligned in `width` bytes
+    (leading spaces): uint8 (n, width)."""
+    x = np.asarray(x, np.float64)
+    q = np.rint(np.abs(x) * 10.0 ** decimals).astype(np.int64)
+    neg = (x < 0) & (q > 0)
+    ip = q // 10 ** decimals
+    n_int = np.maximum(1, np.floor(np.log10(np.maximum(ip, 1))).astype(np.int64) + 1)
+    if (n_int + decimals + 1 + neg > width).any():
+        raise ValueError("value too wide for the field")
+    out = np.full((len(x), width), ord(" "), np.uint8)
+    for c in range(width):                     # c: column from the right
+        col = width - 1 - c
+        if c < decimals:
+            out[:, col] = ord("0") + (q // 10 ** c) % 10
+        elif c == decimals:
+            out[:, col] = ord(".")
+        else:
+            j = c - decimals - 1               # integer digit j
+            dig = ord("0") + (ip // 10 ** min(j, 18)) % 10
+            out[:, col] = np.where(j < n_int, dig, np.where((j == n_int) & neg, ord("-"), ord(" ")))
+    return out
+
+
+def _index_pair_field(a: np.ndarray, b: np.ndarray | None, width: int) -> np.ndarray:
+    """Face tokens "a" or "a//b" (1-based indices) right-aligned in `width` bytes."""
+    a = np.asarray(a, np.int64)
+    nd = lambda v: np.floor(np.log10(np.maximum(v, 1))).astype(np.int64) + 1
+    na = nd(a)
+    nb = np.zeros_like(na) if b is None else nd(np.asarray(b, np.int64))
+    tail = np.zeros_like(na) if b is None else nb + 2
+    if (na + tail > width).any():
+        raise ValueError("index too wide for the field")
+    out = np.full((len(a), width), ord(" "), np.uint8)
+    for c in range(width):
+        col = width - 1 - c
+        ja = c - tail
+        da = ord("0") + (a // 10 ** np.clip(ja, 0, 18)) % 10
+        ch = np.where((ja >= 0) & (ja < na), da, ord(" "))
+        if b is not None:
+            db = ord("0") + (np.asarray(b, np.int64) // 10 ** min(c, 18)) % 10
+            ch = np.where(c < nb, db, np.where((c >= nb) & (c < nb + 2), ord("/"), ch))
+        out[:, col] = ch
+    return out
+
+
+def obj_text(positions: np.ndarray, faces: np.ndarray, normals: np.ndarray | None = None,
+             face_normals: np.ndarray | None = None, decimals: int = 6) -> bytes:
+    """Wavefront OBJ text: ``v`` lines of positions (n, 3), ``vn`` lines of
+    normals (m, 3) if given, then one ``f`` line per row of faces (k, c)
+    (0-based vertex indices, c >= 3) with tokens ``a`` or ``a//n`` (normal
+    indices from face_normals (k, c), or the vertex index when normals has one
+    row per position).  Coordinates are fixed-point with `decimals` places;
+    fields are space-padded to a fixed width (valid OBJ: tokens are split at
+    whitespace)."""
+    P = np.asarray(positions)
+    F = np.asarray(faces, np.int64)
+    w = 6 + decimals
+    def lines(tag, cols):
+        n = len(cols[0])
+        parts = [np.frombuffer(tag, np.uint8)[None, :].repeat(n, 0)]
+        for c in cols:
+            parts.append(np.full((n, 1), ord(" "), np.uint8))
+            parts.append(c)
+        parts.append(np.full((n, 1), ord("\n"), np.uint8))
+        return np.concatenate(parts, 1).tobytes()
+    out = [lines(b"v", [_fixed_field(P[:, k], w, decimals) for k in range(3)])]
+    if normals is not None:
+        Nn = np.asarray(normals)
+        out.append(lines(b"vn", [_fixed_field(Nn[:, k], w, decimals) for k in range(3)]))
+        FN = F if face_normals is None else np.asarray(face_normals, np.int64)
+        iw = 2 * len(str(max(len(P), len(Nn)))) + 2
+        out.append(lines(b"f", [_index_pair_field(F[:, k] + 1, FN[:, k] + 1, iw) for k in range(F.shape[1])]))
+    else:
+        iw = len(str(len(P)))
+        out.append(lines(b"f", [_index_pair_field(F[:, k] + 1, None, iw) for k in range(F.shape[1])]))
+    return b"".join(out)
+
+
+def displaced_icosphere_obj(seed: int = 1234, level: int = 8) -> bytes:
+    """The displaced icosphere's sphere mesh (without the ground) as OBJ text:
+    positions and smooth normals to 6 decimals, faces ``a//a b//b c//c``
+    (20 * 4**level triangles sharing vertices through the OBJ loader's
+    (position, uv, normal) cache)."""
+    sc = displaced_icosphere(seed, level)
+    nv = len(sc["vertices"]) - 4
+    m = len(sc["triangles"]) - 2
+    P = sc["vertices"]["position"][:nv, :3]
+    Nn = sc["vertices"]["normal"][:nv, :3]
+    return obj_text(P, sc["triangles"]["v"][:m], normals=Nn)
+
+
+def world_mesh_obj(vertices: np.ndarray, triangles: np.ndarray) -> bytes:
+    """The voxel world's face mesh (4 vertices per quad) as OBJ text: one ``v``
+    per vertex, the six axis normals as ``vn``, and the mesh's own triangles as
+    ``f a//n b//n c//n`` (the mesher flips the winding of some quads, so the
+    triangles are written as they are rather than as quads)."""
+    V = np.asarray(vertices)
+    T = np.asarray(triangles)["v"].astype(np.int64)
+    axes = np.array([(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)], np.float32)
+    n = V["normal"][:, :3]
+    nidx = np.argmax((n[:, None, :] * axes[None, :, :]).sum(-1), axis=1)
+    return obj_text(V["position"][:, :3], T, normals=axes, face_normals=nidx[T])

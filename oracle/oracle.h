@@ -6,6 +6,7 @@
  *   - path_color / cs_main    src/shaders/path_trace.wgsl:194-242, :485-662
  *   - joint-bilateral denoise src/shaders/denoise.wgsl:52-120
  *   - image metrics           src/regression.rs:120-181
+ *   - OBJ loader              src/mesh.rs:474-642
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it.
  */
 #ifndef MCRT_ORACLE_H
@@ -190,6 +191,16 @@ void orc_ggx_dg(double alpha, double mz, double cos_o, double cos_i, double *out
 void orc_math_eval(int fn, const float *x, const float *y, float *out, uint32_t n);
 
 uint32_t orc_pcg_hash(uint32_t v);
+
+/* load_obj (mesh.rs:474-642) on the text of one OBJ file (obj.cpp).  Returns a
+ * handle holding the vertices and triangles (NULL on error, with the text that
+ * follows "'<path>' " / "'<path>': " in the reference's message in err). */
+void *orc_obj_load(const char *text, uint64_t len, uint32_t mat_idx, uint32_t *n_vertices, uint32_t *n_triangles,
+                   char *err, uint32_t err_cap);
+void orc_obj_copy(void *handle, orc_vertex *vertices, orc_triangle *triangles);
+void orc_obj_free(void *handle);
+/* str::parse::<f32> of one token: 1 and the value, or 0 on a syntax error. */
+int orc_parse_f32(const char *s, uint32_t len, float *out);
 
 #ifdef __cplusplus
 }

@@ -402,3 +402,45 @@ def tonemap_aces_rgba8(rgba):
     out = np.zeros(rgba.shape[:-1] + (4,), np.uint8)
     L.orc_tonemap_aces_rgba8(_p(rgba), rgba.size // 4, _p(out))
     return out
+
+
+VERTEX = np.dtype([("position", np.float32, 4), ("normal", np.float32, 4), ("uv", np.float32, 4)])
+TRIANGLE = np.dtype([("v", np.uint32, 3), ("mat_idx", np.uint32)])
+
+
+class ObjError(ValueError):
+    """load_obj's error text after "'<path>' " or "'<path>': "."""
+
+
+def obj_load(text, mat_idx=0):
+    """load_obj (mesh.rs:474-642) on OBJ text (bytes): (vertices, triangles) as
+    the reference's GpuVertex / GpuTriangle records, or ObjError."""
+    L = lib()
+    L.orc_obj_load.restype = c_void_p
+    L.orc_obj_load.argtypes = [ctypes.c_char_p, ctypes.c_uint64, c_uint32, POINTER(c_uint32), POINTER(c_uint32),
+                               ctypes.c_char_p, c_uint32]
+    L.orc_obj_copy.restype = None
+    L.orc_obj_copy.argtypes = [c_void_p, c_void_p, c_void_p]
+    L.orc_obj_free.restype = None
+    L.orc_obj_free.argtypes = [c_void_p]
+    data = bytes(text)
+    nv, nt = c_uint32(0), c_uint32(0)
+    err = ctypes.create_string_buffer(512)
+    h = L.orc_obj_load(data, len(data), mat_idx, ctypes.byref(nv), ctypes.byref(nt), err, 512)
+    if not h:
+        raise ObjError(err.value.decode())
+    v = np.zeros(nv.value, VERTEX)
+    t = np.zeros(nt.value, TRIANGLE)
+    L.orc_obj_copy(h, _p(v), _p(t))
+    L.orc_obj_free(h)
+    return v, t
+
+
+def parse_f32(token):
+    """str::parse::<f32> of one token (bytes): the float, or None on a syntax error."""
+    L = lib()
+    L.orc_parse_f32.restype = ctypes.c_int
+    L.orc_parse_f32.argtypes = [ctypes.c_char_p, c_uint32, c_void_p]
+    out = np.zeros(1, np.float32)
+    tok = bytes(token)
+    return out[0] if L.orc_parse_f32(tok, len(tok), _p(out)) else None
