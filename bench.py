@@ -93,7 +93,7 @@ def parse():
                    help="same scene at 960x540, 16 spp (2 GB of path state): the profiling case for counter "
                         "sets that need several passes (not a bench line)")
     p.add_argument("--leg", choices=["bvh_build", "cache_mlp", "frame", "adjoint", "nee", "roofline_inputs",
-                                     "cache_race"],
+                                     "cache_race", "ingest"],
                    help="profiling case: only the GPU BVH builds of the workload's mesh, only the "
                         "radiance-cache MLP (2^18 queries), only frames of the workload (autotune: 8 "
                         "frames, then rebuild + render with the chosen closest-hit variant, 12 extend "
@@ -727,6 +727,74 @@ MLP_FLOP_INFER = 2 * (96 * 64 + 4 * 64 * 64 + 64 * 16)                    # per 
 MLP_FLOP_TRAIN = MLP_FLOP_INFER + 2 * (16 * 64 + 4 * 64 * 64) + MLP_FLOP_INFER   # + backward data + weight grads
 
 
+def ingest_rate(M, ctx, n_warm=1, n_steps=3, cpu=True):
+    """Scene ingestion on the device: the benchmark meshes as Wavefront OBJ text
+    (host bytes) parsed into the device mesh by mcrt_mesh_append_obj (load_obj,
+    mesh.rs:474-642; the call's wall time, text copy included), then the GPU
+    BVH build of the parsed mesh (mcrt_upload_scene with the device mesh).
+    Parity: the icosphere's records equal the oracle's load_obj bit for bit;
+    the voxel world's parsed triangles equal the device mesher's own.  CPU
+    baselines: the oracle's load_obj (a restatement of the reference's
+    single-threaded loader) and the library's host loader, 1 thread each."""
+    from mcrt_gb300 import scenes
+    out = {}
+    sc = scenes.displaced_icosphere(SEED, LEVEL)
+    texts = {"displaced_icosphere_l8": scenes.displaced_icosphere_obj(SEED, LEVEL)}
+    wd = scenes.voxel_world(SEED)
+    ctx.world_generate(wd["params"])
+    ctx.world_mesh(wd["block_material"], greedy=False)
+    wv, wt = ctx.world_read_mesh()
+    texts["voxel_world_faces"] = scenes.world_mesh_obj(wv, wt)
+    for name, text in texts.items():
+        rows = []
+        for i in range(n_warm + n_steps):
+            ctx.mesh_reset()
+            t0 = time.perf_counter()
+            nv, nt = ctx.mesh_append_obj(text)
+            wall = (time.perf_counter() - t0) * 1e3
+            st = ctx.mesh_obj_stats()
+            ctx.upload_scene(materials=sc["materials"], device_mesh=True)
+            if i >= n_warm:
+                rows.append((wall, st["h2d_ms"], st["kernel_ms"], ctx.timings()["bvh_build_ms"]))
+        m = [statistics.median(r[k] for r in rows) for k in range(4)]
+        mb = len(text) / 1e6
+        r = {"text_mb": round(mb, 1), "lines": int(st["lines"]), "face_tokens": int(st["tokens"]),
+             "vertices": int(nv), "triangles": int(nt), "kernel_launches": int(st["launches"]),
+             "wall_ms": round(m[0], 3), "h2d_ms": round(m[1], 3), "kernel_ms": round(m[2], 3),
+             "text_gbs_wall": round(mb / m[0], 2), "text_gbs_kernels": round(mb / m[2], 2),
+             "h2d_gbs": round(mb / m[1], 2), "mtriangles_per_s_wall": round(nt / m[0] / 1e3, 1),
+             "bvh_build_ms": round(m[3], 3), "ingest_and_build_ms": round(m[0] + m[3], 3)}
+        v_d, t_d = ctx.mesh_read()
+        if name == "displaced_icosphere_l8":
+            O = _oracle()
+            t0 = time.perf_counter()
+            v_o, t_o = O.obj_load(text, 0)
+            t_oracle = time.perf_counter() - t0
+            canon = lambda v: np.where(np.isnan(v.view(np.float32)), np.float32(np.nan), v.view(np.float32)).view(np.uint32)
+            r["parity"] = {"against": "oracle load_obj", "bit_exact": bool(
+                np.array_equal(canon(v_d), canon(v_o)) and np.array_equal(t_d.view(np.uint32), t_o.view(np.uint32)))}
+            if cpu:
+                import tempfile
+                with tempfile.NamedTemporaryFile(suffix=".obj", delete=False) as f:
+                    f.write(text)
+                    path = f.name
+                t0 = time.perf_counter()
+                M.load_scene_yaml_str(f"objects:\n  - type: mesh\n    path: {path}\n    material: {{ type: lambertian }}\n")
+                t_host = time.perf_counter() - t0
+                os.remove(path)
+                r["cpu_baseline"] = {"oracle_load_obj_s": round(t_oracle, 3), "host_loader_s": round(t_host, 3),
+                                     "cores": 1, "kind": "port",
+                                     "sample": "the whole OBJ text (file read included for the host loader)"}
+                r["speedup_wall_vs_oracle"] = round(t_oracle * 1e3 / m[0], 1)
+        else:
+            ok = (np.array_equal(v_d["position"][t_d["v"]], wv["position"][wt["v"]]) and
+                  np.array_equal(v_d["normal"][t_d["v"]][..., :3], wv["normal"][wt["v"]][..., :3]))
+            r["parity"] = {"against": "the device mesher's triangles (corner positions and normals)",
+                           "bit_exact": bool(ok)}
+        out[name] = r
+    return out
+
+
 def mlp_rate(M, ctx, n=1 << 20, reps=10):
     """Radiance-cache MLP on the tensor cores: inference over 2^20 synthetic
     queries and one training step on 2^20 samples (device time), against the
@@ -769,6 +837,10 @@ def run_mcrt(args):
         return
     if args.leg == "nee":
         print(json.dumps(nee_rate(M, ctx, n_warm=args.warmup, n_calls=args.steps)))
+        return
+    if args.leg == "ingest":
+        print(json.dumps({"leg": "ingest"} | ingest_rate(M, ctx, n_warm=args.warmup, n_steps=args.steps,
+                                                         cpu=not args.no_cpu_baseline)))
         return
     ctx.upload_scene(vertices=sc["vertices"], triangles=sc["triangles"], materials=sc["materials"], env=sc["env"])
     if args.leg == "bvh_build":
@@ -948,7 +1020,7 @@ def run_mcrt(args):
                         "positions), oracle statistics of this run's sample: more than HBM could deliver in the "
                         "kernels' time, since these kernels fetch fewer records, most from L2 and L1"}
     clocks = clk.summary()
-    quality = adjoint = voxel = views = views_cache = icosphere_cache = mlp = cpu_more = None
+    quality = adjoint = voxel = views = views_cache = icosphere_cache = mlp = cpu_more = ingest = None
     if not args.small:
         mlp = mlp_rate(M, ctx)
         quality = time_to_relmse(M, ctx)
@@ -960,6 +1032,8 @@ def run_mcrt(args):
         if not args.no_cpu_baseline:
             cpu_more, more_parity = cpu_baselines(M, ctx, quality, cores)
             parity.update(more_parity)
+        ingest = ingest_rate(M, ctx, cpu=not args.no_cpu_baseline)
+        parity.update({f"obj_{k}": v["parity"] for k, v in ingest.items()})
     out = {
         "metric": "Msamples/s", "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 3), "higher_is_better": True,
@@ -987,6 +1061,7 @@ def run_mcrt(args):
         "batched_views_cache_time_to_relmse": views_cache,
         "icosphere_cache_time_to_relmse": icosphere_cache,
         "radiance_cache_mlp": mlp,
+        "scene_ingestion": ingest,
     }
     print(json.dumps(out))
     barrier(world)

@@ -379,6 +379,12 @@ mcrt_status mcrt_mesh_append_obj(mcrt_ctx *ctx, const char *text, uint64_t len, 
                                  const mcrt_mesh_transform *xf, const char *source, uint32_t *out_n_vertices,
                                  uint32_t *out_n_triangles);
 
+/* The last successful mcrt_mesh_append_obj: out_ms2 = [text copy to the device,
+ * parse kernels] (ms, CUDA events on the context stream; the kernel figure
+ * excludes the parser's host waits for sizes); out_counts4 = [text bytes,
+ * lines, face tokens, kernel launches]. */
+mcrt_status mcrt_mesh_obj_stats(mcrt_ctx *ctx, float *out_ms2, uint64_t *out_counts4);
+
 /* Copy the device mesh to the host (capacities in records; NULL arrays are
  * skipped); out_n_* receive the mesh's counts. */
 mcrt_status mcrt_mesh_read(mcrt_ctx *ctx, mcrt_gpu_vertex *vertices, uint32_t vertex_capacity,

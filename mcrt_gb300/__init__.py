@@ -299,6 +299,14 @@ class Context:
                                                ctypes.byref(nt)))
         return nv.value, nt.value
 
+    def mesh_obj_stats(self):
+        """The last mesh_append_obj: dict of the text copy and kernel times (ms) and the
+        text bytes, lines, face tokens and kernel launches."""
+        ms = (c_float * 2)()
+        cnt = (c_uint64 * 4)()
+        self._check(lib().mcrt_mesh_obj_stats(self._h, ms, cnt))
+        return dict(h2d_ms=ms[0], kernel_ms=ms[1], bytes=cnt[0], lines=cnt[1], tokens=cnt[2], launches=cnt[3])
+
     def mesh_counts(self):
         nv, nt = c_uint32(), c_uint32()
         self._check(lib().mcrt_mesh_read(self._h, None, 0, None, 0, ctypes.byref(nv), ctypes.byref(nt)))

@@ -158,6 +158,7 @@ SIGNATURES = [
     ("mcrt_mesh_read", c_int, [c_void_p, c_void_p, c_uint32, c_void_p, c_uint32, POINTER(c_uint32),
                                POINTER(c_uint32)]),
     ("mcrt_mesh_append_scene", c_int, [c_void_p, c_void_p]),
+    ("mcrt_mesh_obj_stats", c_int, [c_void_p, POINTER(c_float), POINTER(c_uint64)]),
     ("mcrt_adjoint", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_uint32, POINTER(RenderOpts),
                              c_void_p, c_void_p, c_void_p]),
     ("mcrt_autotune", c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, POINTER(RenderOpts),

@@ -96,7 +96,8 @@ struct mcrt_ctx {
     // device mesh assembled by mcrt_mesh_append / mcrt_mesh_append_obj
     mcrt::DeviceMesh dmesh;
     mcrt::ObjScratch obj;
-    unsigned long long last_obj_lines = 0, last_obj_tokens = 0;
+    unsigned long long last_obj_counts[4] = {0, 0, 0, 0};   // bytes, lines, face tokens, kernel launches
+    float last_obj_ms[2] = {0.0f, 0.0f};                    // text copy, kernels
     // batched views and graph replay
     DBuf views, pass_state;
     std::vector<char> view_blob, graph_key;
@@ -411,6 +412,8 @@ void mcrt_destroy(mcrt_ctx *ctx) {
                     &ctx->shade_recs, &ctx->dmesh.vertices, &ctx->dmesh.triangles, &ctx->obj.text,
                     &ctx->obj.lines, &ctx->obj.tokens, &ctx->obj.staging};
     for (DBuf *b : bufs) b->release();
+    for (cudaEvent_t e : ctx->obj.ev)
+        if (e) cudaEventDestroy(e);
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     mcrt::cache_destroy(ctx->cache);
     mcrt::free_bvh_scratch(ctx->bvh_scratch);
@@ -1335,10 +1338,22 @@ mcrt_status mcrt_mesh_append_obj(mcrt_ctx *ctx, const char *text, uint64_t len, 
         ctx->dmesh.nt = nt0;
         return fail(ctx, MCRT_ERR_INVALID_ARG, "mesh '" + src + "' transform.scale must be positive");
     }
-    ctx->last_obj_lines = r.n_lines;
-    ctx->last_obj_tokens = r.n_tokens;
+    ctx->last_obj_counts[0] = len;
+    ctx->last_obj_counts[1] = r.n_lines;
+    ctx->last_obj_counts[2] = r.n_tokens;
+    ctx->last_obj_counts[3] = r.launches;
+    ctx->last_obj_ms[0] = r.h2d_ms;
+    ctx->last_obj_ms[1] = r.kernel_ms;
     if (out_n_vertices) *out_n_vertices = r.n_vertices;
     if (out_n_triangles) *out_n_triangles = r.n_triangles;
+    return MCRT_OK;
+}
+
+mcrt_status mcrt_mesh_obj_stats(mcrt_ctx *ctx, float *out_ms2, uint64_t *out_counts4) {
+    if (!ctx) return fail(nullptr, MCRT_ERR_INVALID_ARG, "ctx is NULL");
+    if (out_ms2) std::memcpy(out_ms2, ctx->last_obj_ms, sizeof(ctx->last_obj_ms));
+    if (out_counts4)
+        for (int k = 0; k < 4; ++k) out_counts4[k] = ctx->last_obj_counts[k];
     return MCRT_OK;
 }
 

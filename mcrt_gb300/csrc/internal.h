@@ -171,6 +171,7 @@ struct DeviceMesh {
 };
 struct ObjScratch {
     DBuf text, lines, tokens, staging;
+    cudaEvent_t ev[9] = {};   // copy and kernel stages of the last parse
 };
 // A mesh object's transform (scene.rs:438-495) as the kernel applies it:
 // q = p * s, then m (row-major, has_r) applied to q, then + t.
@@ -186,6 +187,8 @@ struct ObjOutcome {
     int code = kNoGeometry;
     unsigned long long valid_up_to = 0;   // first invalid byte (kNotUtf8)
     uint32_t n_vertices = 0, n_triangles = 0, n_lines = 0, n_tokens = 0;
+    float h2d_ms = 0.0f, kernel_ms = 0.0f;    // text copy; kernel stages (CUDA events, host waits excluded)
+    unsigned long long launches = 0;
 };
 // Grow the mesh's buffers (keeping their records) for add_v / add_t more.
 cudaError_t mesh_reserve(DeviceMesh &M, uint32_t add_v, uint32_t add_t, cudaStream_t st);

@@ -727,6 +727,9 @@ cudaError_t obj_append(const char *host_text, unsigned long long len, uint32_t m
     *out = ObjOutcome{};
     out->code = ObjOutcome::kNoGeometry;
     if (len == 0) return cudaSuccess;
+    if (!S.ev[0])
+        for (cudaEvent_t &e : S.ev) OBJ_CK(cudaEventCreate(&e));
+    const unsigned long long launches0 = launch_count();
     if (len > 0xFFFFFF00ull) return cudaErrorInvalidValue;      // byte offsets are 32-bit
     // ---- stage 1: text, newline counts per block, UTF-8 check
     const uint32_t n16 = (uint32_t)((len + 15) / 16);
@@ -744,11 +747,14 @@ cudaError_t obj_append(const char *host_text, unsigned long long len, uint32_t m
     uint32_t *scan_tmp = carve<uint32_t>(p, scan_words);
     unsigned long long *small = carve<unsigned long long>(p, 16);   // [0] first bad byte, [1..] counters
     OBJ_CK(cudaMemsetAsync(text + (size_t)n16 * 16 - 16, 0, 32, st));
+    OBJ_CK(cudaEventRecord(S.ev[0], st));
     OBJ_CK(cudaMemcpyAsync(text, host_text, len, cudaMemcpyHostToDevice, st));
+    OBJ_CK(cudaEventRecord(S.ev[1], st));
     OBJ_CK(cudaMemsetAsync(small, 0xFF, 8, st));
     k_obj_scan_text<<<nb, kObjThreads, 0, st>>>(reinterpret_cast<const uint4 *>(text), len, n16, block_nl, small);
     note_launch();
     exclusive_scan_u32(block_nl, block_off, nb, scan_tmp, st);
+    OBJ_CK(cudaEventRecord(S.ev[2], st));
     unsigned long long first_bad = 0;
     uint32_t last_pair[2] = {0, 0};
     OBJ_CK(cudaMemcpyAsync(&first_bad, small, 8, cudaMemcpyDeviceToHost, st));
@@ -780,6 +786,7 @@ cudaError_t obj_append(const char *host_text, unsigned long long len, uint32_t m
     uint32_t *scan_tmp_l = carve<uint32_t>(p, scan_words_l);
     uint32_t *last5 = carve<uint32_t>(p, 16);
     uint32_t *tot5 = last5 + 8;
+    OBJ_CK(cudaEventRecord(S.ev[3], st));
     k_obj_lines<<<nb, kObjThreads, 0, st>>>(reinterpret_cast<const uint4 *>(text), n16, block_off, nl_pos);
     note_launch();
     k_obj_classify<<<blocks_for(L), kObjThreads, 0, st>>>(text, len, n_nl, nl_pos, L, A, last5);
@@ -787,6 +794,7 @@ cudaError_t obj_append(const char *host_text, unsigned long long len, uint32_t m
     for (int j = 0; j < 5; ++j) exclusive_scan_u32(A.cnt[j], A.cnt[j], L, scan_tmp_l, st);
     k_obj_totals<<<1, 32, 0, st>>>(A, L, last5, tot5);
     note_launch();
+    OBJ_CK(cudaEventRecord(S.ev[4], st));
     uint32_t tot[5];
     OBJ_CK(cudaMemcpyAsync(tot, tot5, sizeof(tot), cudaMemcpyDeviceToHost, st));
     OBJ_CK(cudaStreamSynchronize(st));
@@ -818,6 +826,7 @@ cudaError_t obj_append(const char *host_text, unsigned long long len, uint32_t m
     uint32_t *flags = carve<uint32_t>(p, 16);         // [0] table error, [1] last first-flag
     OBJ_CK(cudaMemsetAsync(keys_a, 0xFF, 2 * carve_bytes(cap, 8) + carve_bytes(cap, 4), st));   // keys_a, keys_b, min_tok
     OBJ_CK(cudaMemsetAsync(flags, 0, 64, st));
+    OBJ_CK(cudaEventRecord(S.ev[5], st));
     k_obj_parse<<<blocks_for(L), kObjThreads, 0, st>>>(text, L, A, pos, nrm, uv, T);
     note_launch();
     k_obj_dedup<<<blocks_for(n_tok), kObjThreads, 0, st>>>(n_tok, T, keys_a, keys_b, cap - 1, min_tok, flags);
@@ -825,6 +834,7 @@ cudaError_t obj_append(const char *host_text, unsigned long long len, uint32_t m
     k_obj_first<<<blocks_for(n_tok), kObjThreads, 0, st>>>(n_tok, T, min_tok, flags + 1);
     note_launch();
     exclusive_scan_u32(T.first, T.first, n_tok, scan_tmp_t, st);
+    OBJ_CK(cudaEventRecord(S.ev[6], st));
     uint32_t fl[2], last_first_scan = 0;
     OBJ_CK(cudaMemcpyAsync(fl, flags, 8, cudaMemcpyDeviceToHost, st));
     OBJ_CK(cudaMemcpyAsync(&last_first_scan, T.first + n_tok - 1, 4, cudaMemcpyDeviceToHost, st));
@@ -836,6 +846,7 @@ cudaError_t obj_append(const char *host_text, unsigned long long len, uint32_t m
     // ---- stage 4: records, appended at the end of the device mesh
     OBJ_CK(mesh_reserve(M, NV, n_tri, st));
     float4 *verts = M.vertices.as<float4>() + 3ull * M.nv;
+    OBJ_CK(cudaEventRecord(S.ev[7], st));
     k_obj_vertices<<<blocks_for(n_tok), kObjThreads, 0, st>>>(n_tok, T, min_tok, pos, nrm, uv, verts);
     note_launch();
     k_obj_faces<<<blocks_for(L), kObjThreads, 0, st>>>(L, n_tok, A, T, verts, M.nv, M.triangles.as<uint4>() + M.nt,
@@ -846,7 +857,17 @@ cudaError_t obj_append(const char *host_text, unsigned long long len, uint32_t m
         note_launch();
     }
     OBJ_CK(cudaGetLastError());
+    OBJ_CK(cudaEventRecord(S.ev[8], st));
     OBJ_CK(cudaStreamSynchronize(st));
+    float ms[5];
+    OBJ_CK(cudaEventElapsedTime(&ms[0], S.ev[0], S.ev[1]));
+    OBJ_CK(cudaEventElapsedTime(&ms[1], S.ev[1], S.ev[2]));
+    OBJ_CK(cudaEventElapsedTime(&ms[2], S.ev[3], S.ev[4]));
+    OBJ_CK(cudaEventElapsedTime(&ms[3], S.ev[5], S.ev[6]));
+    OBJ_CK(cudaEventElapsedTime(&ms[4], S.ev[7], S.ev[8]));
+    out->h2d_ms = ms[0];
+    out->kernel_ms = ms[1] + ms[2] + ms[3] + ms[4];
+    out->launches = launch_count() - launches0;
     M.nv += NV;
     M.nt += n_tri;
     out->code = ObjOutcome::kOk;
