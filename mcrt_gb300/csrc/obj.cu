@@ -12,8 +12,8 @@
 //                    the face tokens' resolved (position, uv, normal) indices
 //   k_obj_dedup      (position, uv, normal) key -> its first face token, in two
 //                    open-addressing tables (the reference's HashMap cache)
-//   k_obj_first      first occurrences -> (scan) -> vertex numbers
-//   k_obj_vertices   the vertex records
+//   k_obj_first      first occurrences (and their block sums)
+//   k_obj_vertices   vertex numbers (scan) and the vertex records
 //   k_obj_faces      fan triangles and the geometric-normal patch
 //   k_obj_transform  scale -> rotate -> translate
 //
@@ -73,12 +73,14 @@ __device__ bool parse_i64(const uint8_t *p, const uint8_t *e, long long *out) {
     bool neg = false;
     if (p < e && (*p == '+' || *p == '-')) { neg = *p == '-'; ++p; }
     if (p == e) return false;
-    const unsigned long long lim = neg ? 9223372036854775808ull : 9223372036854775807ull;
     unsigned long long v = 0;
-    for (; p < e; ++p) {
-        if (!is_digit(*p)) return false;
-        const unsigned d = *p - '0';
-        if (v > (lim - d) / 10) return false;
+    #pragma unroll 1
+    for (int n = 0; p < e; ++p, ++n) {
+        const uint32_t d = (uint32_t)*p - '0';
+        if (d > 9) return false;
+        // only a 19th digit (or later) can leave the range: 2^63 - 1 = 922337203685477580 * 10 + 7
+        if (n >= 18 && (v > 922337203685477580ull || (v == 922337203685477580ull && d > (neg ? 8u : 7u))))
+            return false;
         v = v * 10 + d;
     }
     *out = neg ? (long long)(0ull - v) : (long long)v;
@@ -86,7 +88,13 @@ __device__ bool parse_i64(const uint8_t *p, const uint8_t *e, long long *out) {
 }
 
 // resolve (mesh.rs:491-500): 1-based or negative (from the end) index into a
-// list of n entries.
+// list of n entries, of an already parsed integer.
+__device__ __forceinline__ bool resolve_value(long long i, uint32_t n, uint32_t *out) {
+    const long long idx = i < 0 ? (long long)n + i : i - 1;
+    if (idx < 0 || idx >= (long long)n) return false;
+    *out = (uint32_t)idx;
+    return true;
+}
 __device__ bool resolve(const uint8_t *p, const uint8_t *e, uint32_t n, uint32_t *out) {
     long long i;
     if (!parse_i64(p, e, &i)) return false;
@@ -95,6 +103,9 @@ __device__ bool resolve(const uint8_t *p, const uint8_t *e, uint32_t n, uint32_t
     *out = (uint32_t)idx;
     return true;
 }
+
+// Powers of ten exact in binary32 (5^10 < 2^24): Clinger's fast path.
+__device__ const float kPow10f[11] = {1e0f, 1e1f, 1e2f, 1e3f, 1e4f, 1e5f, 1e6f, 1e7f, 1e8f, 1e9f, 1e10f};
 
 // Correctly rounded powers of ten 1e-65 .. 1e39 (the compiler rounds each literal).
 __device__ const double kPow10[105] = {
@@ -114,12 +125,14 @@ constexpr int kBigWords = 26;
 struct Big {
     uint32_t w[kBigWords];
     __device__ void set(unsigned long long v) {
+        #pragma unroll 1
         for (int i = 0; i < kBigWords; ++i) w[i] = 0;
         w[0] = (uint32_t)v;
         w[1] = (uint32_t)(v >> 32);
     }
     __device__ void mul_add(uint32_t m, uint32_t a) {
         unsigned long long carry = a;
+        #pragma unroll 1
         for (int i = 0; i < kBigWords; ++i) {
             unsigned long long t = (unsigned long long)w[i] * m + carry;
             w[i] = (uint32_t)t;
@@ -127,13 +140,16 @@ struct Big {
         }
     }
     __device__ void mul_pow5(int k) {
+        #pragma unroll 1
         while (k >= 13) { mul_add(1220703125u, 0); k -= 13; }     // 5^13
         uint32_t p = 1;
+        #pragma unroll 1
         while (k-- > 0) p *= 5;
         mul_add(p, 0);
     }
     __device__ void shl(int bits) {
         const int ws = bits >> 5, bs = bits & 31;
+        #pragma unroll 1
         for (int i = kBigWords - 1; i >= 0; --i) {
             uint32_t hi = i - ws >= 0 ? w[i - ws] : 0u;
             uint32_t lo = i - ws - 1 >= 0 ? w[i - ws - 1] : 0u;
@@ -142,6 +158,7 @@ struct Big {
     }
 };
 __device__ int big_cmp(const Big &a, const Big &b) {
+    #pragma unroll 1
     for (int i = kBigWords - 1; i >= 0; --i)
         if (a.w[i] != b.w[i]) return a.w[i] < b.w[i] ? -1 : 1;
     return 0;
@@ -158,6 +175,7 @@ __device__ __noinline__ int cmp_decimal_midpoint(const uint8_t *p, const uint8_t
     int nd = 0;
     long long e10 = 0;
     bool sticky = false, nonzero = false;
+    #pragma unroll 1
     for (; p < e && is_digit(*p); ++p) {
         const uint32_t d = *p - '0';
         if (nd < 120) {
@@ -168,6 +186,7 @@ __device__ __noinline__ int cmp_decimal_midpoint(const uint8_t *p, const uint8_t
         }
     }
     if (p < e && *p == '.') {
+        #pragma unroll 1
         for (++p; p < e && is_digit(*p); ++p) {
             const uint32_t d = *p - '0';
             if (nd < 120) {
@@ -183,6 +202,7 @@ __device__ __noinline__ int cmp_decimal_midpoint(const uint8_t *p, const uint8_t
         ++p;
         bool eneg = false;
         if (p < e && (*p == '+' || *p == '-')) { eneg = *p == '-'; ++p; }
+        #pragma unroll 1
         for (; p < e && is_digit(*p); ++p)
             if (ex < 0x10000) ex = ex * 10 + (*p - '0');
         if (eneg) ex = -ex;
@@ -191,6 +211,7 @@ __device__ __noinline__ int cmp_decimal_midpoint(const uint8_t *p, const uint8_t
     const unsigned long long bits = (unsigned long long)__double_as_longlong(mid);
     unsigned long long c = (bits & ((1ull << 52) - 1)) | (1ull << 52);
     int q = (int)((bits >> 52) & 0x7FF) - 1075;
+    #pragma unroll 1
     while (!(c & 1)) { c >>= 1; ++q; }
     Big B;
     B.set(c);
@@ -210,7 +231,7 @@ __device__ __forceinline__ double f32_value(uint32_t b) {   // 0x7F800000 stands
 
 // The binary32 nearest to m * 10^E (m < 10^19 the first significant digits,
 // E in [-65, 39]); ties and near-ties are settled exactly against the token.
-__device__ float round_decimal(unsigned long long m, int E, const uint8_t *tok, const uint8_t *tok_end) {
+__device__ __noinline__ float round_decimal(unsigned long long m, int E, const uint8_t *tok, const uint8_t *tok_end) {
     const double d = __dmul_rn(__ull2double_rn(m), kPow10[E + 65]);   // relative error < 3.4e-16 (+1e-18 dropped digits)
     const float f = __double2float_rn(d);
     const uint32_t fb = __float_as_uint(f);
@@ -253,6 +274,7 @@ __device__ bool parse_f32(const uint8_t *p, const uint8_t *e, float *out) {
     int nd = 0;
     long long e10 = 0;
     bool any = false;
+    #pragma unroll 1
     for (; p < e && is_digit(*p); ++p) {
         any = true;
         const uint32_t d = *p - '0';
@@ -263,6 +285,7 @@ __device__ bool parse_f32(const uint8_t *p, const uint8_t *e, float *out) {
         }
     }
     if (p < e && *p == '.') {
+        #pragma unroll 1
         for (++p; p < e && is_digit(*p); ++p) {
             any = true;
             const uint32_t d = *p - '0';
@@ -279,6 +302,7 @@ __device__ bool parse_f32(const uint8_t *p, const uint8_t *e, float *out) {
         bool eneg = false;
         if (p < e && (*p == '+' || *p == '-')) { eneg = *p == '-'; ++p; }
         if (p == e || !is_digit(*p)) return false;
+        #pragma unroll 1
         for (; p < e && is_digit(*p); ++p)
             if (ex < 0x10000) ex = ex * 10 + (*p - '0');
         if (eneg) ex = -ex;
@@ -287,9 +311,16 @@ __device__ bool parse_f32(const uint8_t *p, const uint8_t *e, float *out) {
     float r = 0.0f;
     if (m != 0) {
         const long long E = e10 + ex;
-        if (nd - 1 + E >= 39) r = INFINITY;            // >= 1e39: above the overflow threshold
-        else if (nd + E <= -46) r = 0.0f;              // < 1e-46: below half the least subnormal
-        else r = round_decimal(m, (int)E, tok, e);
+        if (m <= (1u << 24) && E >= -10 && E <= 10) {  // both operands exact: one rounding (Clinger)
+            const float fm = (float)(uint32_t)m;
+            r = E < 0 ? __fdiv_rn(fm, kPow10f[-E]) : __fmul_rn(fm, kPow10f[E]);
+        } else if (nd - 1 + E >= 39) {
+            r = INFINITY;                              // >= 1e39: above the overflow threshold
+        } else if (nd + E <= -46) {
+            r = 0.0f;                                  // < 1e-46: below half the least subnormal
+        } else {
+            r = round_decimal(m, (int)E, tok, e);
+        }
     }
     *out = neg ? -r : r;
     return true;
@@ -303,9 +334,11 @@ __device__ __forceinline__ float f32_or_zero(const uint8_t *p, const uint8_t *e)
 // Next ASCII-whitespace-separated token in [*p, e).
 __device__ __forceinline__ bool next_token(const uint8_t *&p, const uint8_t *e, const uint8_t *&tb,
                                            const uint8_t *&te) {
+    #pragma unroll 1
     while (p < e && ascii_ws(*p)) ++p;
     if (p == e) return false;
     tb = p;
+    #pragma unroll 1
     while (p < e && !ascii_ws(*p)) ++p;
     te = p;
     return true;
@@ -381,7 +414,85 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *t
     __syncthreads();
     const uint32_t before = warp ? warp_sums[warp - 1] : 0u;
     if (total) *total = warp_sums[kObjThreads / 32 - 1];
+    __syncthreads();                      // warp_sums is reused by the next call
     return before + x - v;
+}
+
+// Block-wide exclusive scans of N values per thread at once (one set of barriers).
+template <int N>
+__device__ __forceinline__ void block_exclusive_scan_n(const uint32_t (&v)[N], uint32_t (&ex)[N]) {
+    __shared__ uint32_t wsum[kObjThreads / 32][N];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x[N];
+    for (int j = 0; j < N; ++j) x[j] = v[j];
+    for (int o = 1; o < 32; o <<= 1)
+        for (int j = 0; j < N; ++j) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x[j], o);
+            if (lane >= o) x[j] += y;
+        }
+    if (lane == 31)
+        for (int j = 0; j < N; ++j) wsum[warp][j] = x[j];
+    __syncthreads();
+    for (int j = 0; j < N; ++j) {
+        uint32_t before = 0;
+        for (int w = 0; w < warp; ++w) before += wsum[w][j];
+        ex[j] = before + x[j] - v[j];
+    }
+    __syncthreads();
+}
+
+// Multi-field exclusive scans without waits between blocks: each block of
+// kObjThreads elements writes its sums (sums[f * nb + block]); k_scan_top
+// scans every field's block sums in place (one block; totals[f] = the field's
+// total); the consumer kernels, launched over the same blocks, add a block
+// scan of the elements to their block's prefix.
+
+__global__ void __launch_bounds__(1024) k_scan_top(uint32_t *sums, uint32_t nb, int nf, uint32_t *totals) {
+    constexpr uint32_t kItems = 8, kChunk = 1024 * kItems;
+    __shared__ uint32_t stage[kChunk];
+    __shared__ uint32_t ws[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int f = 0; f < nf; ++f) {
+        uint32_t *a = sums + (size_t)f * nb;
+        uint32_t carry = 0;
+        for (uint32_t base = 0; base < nb; base += kChunk) {
+            for (uint32_t j = threadIdx.x; j < kChunk; j += 1024)          // coalesced loads
+                stage[j] = base + j < nb ? a[base + j] : 0u;
+            __syncthreads();
+            uint32_t v[kItems], sum = 0;
+            for (uint32_t j = 0; j < kItems; ++j) {
+                v[j] = stage[threadIdx.x * kItems + j];
+                sum += v[j];
+            }
+            uint32_t x = sum;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane == 31) ws[warp] = x;
+            __syncthreads();
+            if (warp == 0) {
+                uint32_t w = ws[lane];
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+                    if (lane >= o) w += y;
+                }
+                ws[lane] = w;
+            }
+            __syncthreads();
+            uint32_t run = carry + (warp ? ws[warp - 1] : 0u) + x - sum;
+            for (uint32_t j = 0; j < kItems; ++j) {
+                stage[threadIdx.x * kItems + j] = run;
+                run += v[j];
+            }
+            carry += ws[31];
+            __syncthreads();
+            for (uint32_t j = threadIdx.x; j < kChunk; j += 1024)          // coalesced stores
+                if (base + j < nb) a[base + j] = stage[j];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) totals[f] = carry;
+    }
 }
 
 __global__ void __launch_bounds__(kObjThreads) k_obj_scan_text(const uint4 *t16, unsigned long long len, uint32_t n16,
@@ -429,16 +540,15 @@ __device__ __forceinline__ void line_bounds(uint32_t k, uint32_t n_nl, const uin
     *e = k < n_nl ? nl_pos[k] : (uint32_t)len;
 }
 
-// str::lines + str::trim + '#' + split_ascii_whitespace + the tag match (mesh.rs:502-521).
-__global__ void __launch_bounds__(kObjThreads) k_obj_classify(const uint8_t *t, unsigned long long len, uint32_t n_nl,
-                                                              const uint32_t *nl_pos, uint32_t L, LineArrays A,
-                                                              uint32_t *last5) {
-    const uint32_t k = blockIdx.x * kObjThreads + threadIdx.x;
-    if (k >= L) return;
+// str::lines + str::trim + '#' + split_ascii_whitespace + the tag match of line k.
+__device__ __forceinline__ void classify_line(const uint8_t *t, unsigned long long len, uint32_t n_nl,
+                                                   const uint32_t *nl_pos, uint32_t k, LineArrays A, uint32_t c[5]) {
     uint32_t b, e;
     line_bounds(k, n_nl, nl_pos, len, &b, &e);
     int n;
+    #pragma unroll 1
     while (b < e && (n = ws_forward(t + b, t + e)) > 0) b += n;
+    #pragma unroll 1
     while (e > b && (n = ws_backward(t + b, t + e)) > 0) e -= n;
     uint8_t kind = kLineNone;
     uint32_t ntok = 0, rest = e;
@@ -448,6 +558,7 @@ __global__ void __launch_bounds__(kObjThreads) k_obj_classify(const uint8_t *t, 
         const long long tl = te - tb;
         const uint8_t *rb, *re;
         const uint8_t *q = p;
+        #pragma unroll 1
         while (next_token(q, pe, rb, re)) {
             if (ntok == 0) rest = (uint32_t)(rb - t);
             ++ntok;
@@ -460,26 +571,52 @@ __global__ void __launch_bounds__(kObjThreads) k_obj_classify(const uint8_t *t, 
     A.kind[k] = kind;
     A.rest_b[k] = rest;
     A.rest_e[k] = e;
-    const uint32_t c[5] = {kind == kLineV, kind == kLineVN, kind == kLineVT, kind == kLineF ? ntok : 0u,
-                           kind == kLineF ? ntok - 2 : 0u};
+    c[0] = kind == kLineV;
+    c[1] = kind == kLineVN;
+    c[2] = kind == kLineVT;
+    c[3] = kind == kLineF ? ntok : 0u;
+    c[4] = kind == kLineF ? ntok - 2 : 0u;
     for (int j = 0; j < 5; ++j) A.cnt[j][k] = c[j];
-    if (k == L - 1)
-        for (int j = 0; j < 5; ++j) last5[j] = c[j];
 }
 
-__global__ void k_obj_totals(const LineArrays A, uint32_t L, const uint32_t *last5, uint32_t *tot5) {
-    if (threadIdx.x < 5) tot5[threadIdx.x] = A.cnt[threadIdx.x][L - 1] + last5[threadIdx.x];
+// Per-line kind and counts (mesh.rs:502-521), and each block's sums of the counts.
+__global__ void __launch_bounds__(kObjThreads) k_obj_classify(const uint8_t *t, unsigned long long len, uint32_t n_nl,
+                                                              const uint32_t *nl_pos, uint32_t L, LineArrays A,
+                                                              uint32_t *block_sums) {
+    const uint32_t k = blockIdx.x * kObjThreads + threadIdx.x;
+    uint32_t c[5] = {0, 0, 0, 0, 0}, ex[5];
+    if (k < L) classify_line(t, len, n_nl, nl_pos, k, A, c);
+    block_exclusive_scan_n<5>(c, ex);
+    if (threadIdx.x == kObjThreads - 1)
+        for (int j = 0; j < 5; ++j) block_sums[(size_t)j * gridDim.x + blockIdx.x] = ex[j] + c[j];
 }
 
 struct TokenArrays {
-    uint32_t *pi, *ti, *ni, *slot, *first, *v;
+    uint32_t *pi, *ti, *ni, *slot, *first;   // first: first-occurrence flag, then the vertex number
 };
 
 // Coordinates of v / vn / vt lines (mesh.rs:514-531) and the resolved indices
 // of every face token (mesh.rs:532-550).
-__global__ void __launch_bounds__(kObjThreads) k_obj_parse(const uint8_t *t, uint32_t L, LineArrays A, float *pos,
-                                                           float *nrm, float *uv, TokenArrays T) {
+// Exclusive prefixes of line k's counts of fields J0..J0+N-1: the block's
+// prefix (scanned block sums) plus the block scan of the raw counts.  Every
+// thread of the block must call it.
+template <int J0, int N>
+__device__ __forceinline__ void line_offsets(const LineArrays &A, const uint32_t *line_sums, uint32_t L, uint32_t k,
+                                             uint32_t (&off)[N]) {
+    uint32_t c[N];
+    for (int j = 0; j < N; ++j) c[j] = k < L ? A.cnt[J0 + j][k] : 0u;
+    block_exclusive_scan_n<N>(c, off);
+    for (int j = 0; j < N; ++j) off[j] += line_sums[(size_t)(J0 + j) * gridDim.x + blockIdx.x];
+}
+
+__global__ void __launch_bounds__(kObjThreads) k_obj_parse(const uint8_t *t, uint32_t L, LineArrays A,
+                                                           const uint32_t *line_sums, float *pos, float *nrm,
+                                                           float *uv, TokenArrays T) {
     const uint32_t k = blockIdx.x * kObjThreads + threadIdx.x;
+    uint32_t off[4];
+    line_offsets<0, 4>(A, line_sums, L, k, off);
+    const uint32_t nV = off[0], nVN = off[1], nVT = off[2];
+    uint32_t s = off[3];
     if (k >= L) return;
     const uint8_t kind = A.kind[k];
     if (kind == kLineNone) return;
@@ -487,28 +624,29 @@ __global__ void __launch_bounds__(kObjThreads) k_obj_parse(const uint8_t *t, uin
     if (kind != kLineF) {
         float c[3];
         const int nc = kind == kLineVT ? 2 : 3;
+        #pragma unroll 1
         for (int j = 0; j < nc; ++j) {
             next_token(p, e, tb, te);
             c[j] = f32_or_zero(tb, te);
         }
         if (kind == kLineV) {
-            float *o = pos + 3ull * A.cnt[0][k];
+            float *o = pos + 3ull * nV;
             o[0] = c[0]; o[1] = c[1]; o[2] = c[2];
         } else if (kind == kLineVN) {
             const float3 nn = normalize3(c[0], c[1], c[2]);
-            float *o = nrm + 3ull * A.cnt[1][k];
+            float *o = nrm + 3ull * nVN;
             o[0] = nn.x; o[1] = nn.y; o[2] = nn.z;
         } else {
-            float *o = uv + 2ull * A.cnt[2][k];
+            float *o = uv + 2ull * nVT;
             o[0] = c[0]; o[1] = c[1];
         }
         return;
     }
-    const uint32_t nV = A.cnt[0][k], nVN = A.cnt[1][k], nVT = A.cnt[2][k];
-    uint32_t s = A.cnt[3][k];
+    #pragma unroll 1
     while (next_token(p, e, tb, te)) {
         // token.split('/'): parts 0, 1, 2 (later parts are not read)
         const uint8_t *s1 = tb;
+        #pragma unroll 1
         while (s1 < te && *s1 != '/') ++s1;
         uint32_t pi = 0, ti = kNone, ni = kNone, r;
         bool pres = resolve(tb, s1, nV, &r);
@@ -516,14 +654,16 @@ __global__ void __launch_bounds__(kObjThreads) k_obj_parse(const uint8_t *t, uin
         bool has_norm = false;
         if (s1 < te) {
             const uint8_t *b1 = s1 + 1, *s2 = b1;
+            #pragma unroll 1
             while (s2 < te && *s2 != '/') ++s2;
             if (s2 > b1 && resolve(b1, s2, nVT, &r)) ti = r;
             if (s2 < te) {
                 const uint8_t *b2 = s2 + 1, *s3 = b2;
+                #pragma unroll 1
                 while (s3 < te && *s3 != '/') ++s3;
-                if (resolve(b2, s3, nVN, &r)) ni = r;
-                long long dummy;
-                has_norm = s3 > b2 && parse_i64(b2, s3, &dummy);
+                long long iv;
+                has_norm = parse_i64(b2, s3, &iv);        // an empty part does not parse
+                if (has_norm && resolve_value(iv, nVN, &r)) ni = r;
             }
         }
         T.pi[s] = pi | ((pres || nV > 0) ? kPosOk : 0u) | (has_norm ? kHasNorm : 0u);
@@ -538,15 +678,31 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long x) {   //
     x ^= x >> 27; x *= 0x94D049BB133111EBull;
     return x ^ (x >> 31);
 }
-// Slot of key in an open-addressing table (inserted if absent); kNone if the
-// table is full, which the capacity (twice the tokens) rules out.
-__device__ uint32_t table_slot(unsigned long long *keys, uint32_t mask, unsigned long long key) {
+// Open-addressing hash table entry: a 64-bit key and the least face token
+// that carries it, in one 16-byte record (one sector per probe).
+struct alignas(16) Slot {
+    unsigned long long key;
+    uint32_t min_tok;
+    uint32_t pad;
+};
+// How (position, uv, normal) becomes a table key: one mixed-radix 64-bit key
+// when the three index ranges fit (rp * rt * rn < 2^63), else two tables:
+// (position, uv) -> slot of table A, then (slot A, normal).
+struct KeyPack {
+    int packed;
+    unsigned long long rp, rt;
+    uint32_t no_uv;            // uv index written as kNone -> rt - 1
+};
+
+// Slot of key (inserted if absent); kNone if the table is full, which the
+// capacity (twice the face tokens) rules out.
+__device__ uint32_t table_slot(Slot *tab, uint32_t mask, unsigned long long key) {
     uint32_t h = (uint32_t)mix64(key) & mask;
     for (uint32_t probe = 0; probe <= mask; ++probe, h = (h + 1) & mask) {
-        const unsigned long long cur = keys[h];
+        const unsigned long long cur = tab[h].key;
         if (cur == key) return h;
         if (cur == kEmptyKey) {
-            const unsigned long long old = atomicCAS(&keys[h], kEmptyKey, key);
+            const unsigned long long old = atomicCAS(&tab[h].key, kEmptyKey, key);
             if (old == kEmptyKey || old == key) return h;
         }
     }
@@ -555,45 +711,53 @@ __device__ uint32_t table_slot(unsigned long long *keys, uint32_t mask, unsigned
 
 // vert_cache (mesh.rs:486-489, :556-575): tokens with a resolved normal share
 // a vertex per (position, uv, normal); the vertex belongs to the key's first
-// token.  (position, uv) -> slot of table A, then (slot A, normal) -> slot of
-// table B, each a 64-bit key.
-__global__ void __launch_bounds__(kObjThreads) k_obj_dedup(uint32_t n_tok, TokenArrays T, unsigned long long *keys_a,
-                                                           unsigned long long *keys_b, uint32_t mask,
-                                                           uint32_t *min_tok, uint32_t *err) {
+// token (the least token number).
+__global__ void __launch_bounds__(kObjThreads) k_obj_dedup(uint32_t n_tok, TokenArrays T, Slot *tab_a, Slot *tab_b,
+                                                           uint32_t mask, KeyPack kp, uint32_t *err) {
     const uint32_t s = blockIdx.x * kObjThreads + threadIdx.x;
     if (s >= n_tok) return;
     const uint32_t ni = T.ni[s];
     if (ni == kNone) { T.slot[s] = kNone; return; }
-    const unsigned long long ka = (unsigned long long)(T.pi[s] & kPosMask) | ((unsigned long long)T.ti[s] << 32);
-    const uint32_t a = table_slot(keys_a, mask, ka);
-    const uint32_t b = a == kNone ? kNone : table_slot(keys_b, mask, (unsigned long long)a | ((unsigned long long)ni << 32));
+    const uint32_t pi = T.pi[s] & kPosMask, ti = T.ti[s];
+    uint32_t b;
+    if (kp.packed) {
+        const unsigned long long tt = ti == kNone ? kp.no_uv : ti;
+        b = table_slot(tab_b, mask, pi + kp.rp * (tt + kp.rt * ni));
+    } else {
+        const uint32_t a = table_slot(tab_a, mask, (unsigned long long)pi | ((unsigned long long)ti << 32));
+        b = a == kNone ? kNone : table_slot(tab_b, mask, (unsigned long long)a | ((unsigned long long)ni << 32));
+    }
     if (b == kNone) { atomicExch(err, 1u); T.slot[s] = kNone; return; }
-    atomicMin(&min_tok[b], s);
+    atomicMin(&tab_b[b].min_tok, s);
     T.slot[s] = b;
 }
 
 // 1 for the token that creates a vertex: no resolved normal (always a fresh
-// vertex, mesh.rs:576-591) or the first token of its key.
-__global__ void __launch_bounds__(kObjThreads) k_obj_first(uint32_t n_tok, TokenArrays T, const uint32_t *min_tok,
-                                                           uint32_t *last) {
+// vertex, mesh.rs:576-591) or the first token of its key; block sums for the scan.
+__global__ void __launch_bounds__(kObjThreads) k_obj_first(uint32_t n_tok, TokenArrays T, const Slot *tab,
+                                                           uint32_t *block_sums) {
     const uint32_t s = blockIdx.x * kObjThreads + threadIdx.x;
-    if (s >= n_tok) return;
-    const uint32_t slot = T.slot[s];
-    const uint32_t f = (slot == kNone || min_tok[slot] == s) ? 1u : 0u;
-    T.first[s] = f;
-    if (s == n_tok - 1) *last = f;
+    uint32_t f = 0;
+    if (s < n_tok) {
+        const uint32_t slot = T.slot[s];
+        f = (slot == kNone || tab[slot].min_tok == s) ? 1u : 0u;
+        T.first[s] = f;
+    }
+    uint32_t total;
+    block_exclusive_scan(f, &total);
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
 }
 
-__global__ void __launch_bounds__(kObjThreads) k_obj_vertices(uint32_t n_tok, TokenArrays T, const uint32_t *min_tok,
+// The records of the tokens that create vertices; their vertex numbers (the
+// exclusive scan of the first-occurrence flags) replace the flags in T.first.
+__global__ void __launch_bounds__(kObjThreads) k_obj_vertices(uint32_t n_tok, TokenArrays T, const uint32_t *tok_sums,
                                                               const float *pos, const float *nrm, const float *uv,
                                                               float4 *verts) {
     const uint32_t s = blockIdx.x * kObjThreads + threadIdx.x;
-    if (s >= n_tok) return;
-    const uint32_t slot = T.slot[s];
-    const uint32_t owner = slot == kNone ? s : min_tok[slot];
-    const uint32_t vid = T.first[owner];            // exclusive scan of the first-occurrence flags
-    T.v[s] = vid;
-    if (owner != s) return;
+    const uint32_t f = s < n_tok ? T.first[s] : 0u;
+    const uint32_t vid = tok_sums[blockIdx.x] + block_exclusive_scan(f, nullptr);
+    if (!f) return;
+    T.first[s] = vid;
     const uint32_t pw = T.pi[s], ti = T.ti[s], ni = T.ni[s];
     float4 P = make_float4(0.0f, 0.0f, 0.0f, 1.0f), N = make_float4(0.0f, 1.0f, 0.0f, 0.0f),
            U = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -618,25 +782,36 @@ __global__ void __launch_bounds__(kObjThreads) k_obj_vertices(uint32_t n_tok, To
 // that contains it; the last one wins: triangle min(j, n-2) for token j >= 1,
 // triangle n-2 for token 0.  Such tokens own fresh vertices, so no two threads
 // write one vertex.
-__global__ void __launch_bounds__(kObjThreads) k_obj_faces(uint32_t L, uint32_t n_tok, LineArrays A, TokenArrays T,
-                                                           float4 *verts, uint32_t base_v, uint4 *tris,
-                                                           uint32_t mat_idx) {
+__device__ __forceinline__ uint32_t token_vertex(const TokenArrays &T, const Slot *tab, uint32_t x) {
+    const uint32_t slot = T.slot[x];
+    return T.first[slot == kNone ? x : tab[slot].min_tok];
+}
+
+__global__ void __launch_bounds__(kObjThreads) k_obj_faces(uint32_t L, LineArrays A, const uint32_t *line_sums,
+                                                           TokenArrays T, const Slot *tab, float4 *verts,
+                                                           uint32_t base_v, uint4 *tris, uint32_t mat_idx) {
     const uint32_t k = blockIdx.x * kObjThreads + threadIdx.x;
+    uint32_t off[2];
+    line_offsets<3, 2>(A, line_sums, L, k, off);
+    const uint32_t s0 = off[0], t0 = off[1];
     if (k >= L || A.kind[k] != kLineF) return;
-    const uint32_t s0 = A.cnt[3][k];
-    const uint32_t n = (k + 1 < L ? A.cnt[3][k + 1] : n_tok) - s0;
-    const uint32_t t0 = A.cnt[4][k];
-    const uint32_t v0 = T.v[s0];
-    for (uint32_t i = 1; i + 1 < n; ++i)
-        tris[t0 + i - 1] = make_uint4(base_v + v0, base_v + T.v[s0 + i], base_v + T.v[s0 + i + 1], mat_idx);
+    const uint32_t n = A.cnt[3][k];
+    const uint32_t v0 = token_vertex(T, tab, s0);
+    uint32_t vb = token_vertex(T, tab, s0 + 1);
+    for (uint32_t i = 1; i + 1 < n; ++i) {
+        const uint32_t vc = token_vertex(T, tab, s0 + i + 1);
+        tris[t0 + i - 1] = make_uint4(base_v + v0, base_v + vb, base_v + vc, mat_idx);
+        vb = vc;
+    }
     for (uint32_t j = 0; j < n; ++j) {
         if (T.pi[s0 + j] & kHasNorm) continue;
         const uint32_t i = j == 0 ? n - 2 : min(j, n - 2);
-        const float4 p0 = verts[3ull * v0], p1 = verts[3ull * T.v[s0 + i]], p2 = verts[3ull * T.v[s0 + i + 1]];
+        const float4 p0 = verts[3ull * v0], p1 = verts[3ull * token_vertex(T, tab, s0 + i)],
+                     p2 = verts[3ull * token_vertex(T, tab, s0 + i + 1)];
         const float e1x = p1.x - p0.x, e1y = p1.y - p0.y, e1z = p1.z - p0.z;
         const float e2x = p2.x - p0.x, e2y = p2.y - p0.y, e2z = p2.z - p0.z;
         const float3 g = normalize3(e1y * e2z - e1z * e2y, e1z * e2x - e1x * e2z, e1x * e2y - e1y * e2x);
-        verts[3ull * T.v[s0 + j] + 1] = make_float4(g.x, g.y, g.z, 0.0f);
+        verts[3ull * token_vertex(T, tab, s0 + j) + 1] = make_float4(g.x, g.y, g.z, 0.0f);
     }
 }
 
@@ -734,18 +909,15 @@ cudaError_t obj_append(const char *host_text, unsigned long long len, uint32_t m
     // ---- stage 1: text, newline counts per block, UTF-8 check
     const uint32_t n16 = (uint32_t)((len + 15) / 16);
     const uint32_t nb = blocks_for(n16);
-    const size_t scan_words = scan_tmp_words(std::max<uint32_t>(nb, 1));
     {
-        const size_t bytes = carve_bytes((size_t)n16 * 16 + 16, 1) + 2 * carve_bytes(nb, 4) +
-                             carve_bytes(scan_words, 4) + carve_bytes(16, 8);
+        const size_t bytes = carve_bytes((size_t)n16 * 16 + 16, 1) + carve_bytes(nb, 4) + carve_bytes(16, 8);
         OBJ_CK(S.text.ensure(bytes));
     }
     char *p = S.text.as<char>();
     uint8_t *text = carve<uint8_t>(p, (size_t)n16 * 16 + 16);
-    uint32_t *block_nl = carve<uint32_t>(p, nb);
-    uint32_t *block_off = carve<uint32_t>(p, nb);
-    uint32_t *scan_tmp = carve<uint32_t>(p, scan_words);
-    unsigned long long *small = carve<unsigned long long>(p, 16);   // [0] first bad byte, [1..] counters
+    uint32_t *block_nl = carve<uint32_t>(p, nb);                      // newlines per block -> block offsets
+    unsigned long long *small = carve<unsigned long long>(p, 16);     // [0] first bad byte, [1..] totals
+    uint32_t *totals = reinterpret_cast<uint32_t *>(small + 2);       // [0] newlines, [1..5] line fields, [6] vertices
     OBJ_CK(cudaMemsetAsync(text + (size_t)n16 * 16 - 16, 0, 32, st));
     OBJ_CK(cudaEventRecord(S.ev[0], st));
     OBJ_CK(cudaMemcpyAsync(text, host_text, len, cudaMemcpyHostToDevice, st));
@@ -753,27 +925,26 @@ cudaError_t obj_append(const char *host_text, unsigned long long len, uint32_t m
     OBJ_CK(cudaMemsetAsync(small, 0xFF, 8, st));
     k_obj_scan_text<<<nb, kObjThreads, 0, st>>>(reinterpret_cast<const uint4 *>(text), len, n16, block_nl, small);
     note_launch();
-    exclusive_scan_u32(block_nl, block_off, nb, scan_tmp, st);
+    k_scan_top<<<1, 1024, 0, st>>>(block_nl, nb, 1, totals);
+    note_launch();
     OBJ_CK(cudaEventRecord(S.ev[2], st));
     unsigned long long first_bad = 0;
-    uint32_t last_pair[2] = {0, 0};
+    uint32_t n_nl = 0;
     OBJ_CK(cudaMemcpyAsync(&first_bad, small, 8, cudaMemcpyDeviceToHost, st));
-    OBJ_CK(cudaMemcpyAsync(&last_pair[0], block_off + nb - 1, 4, cudaMemcpyDeviceToHost, st));
-    OBJ_CK(cudaMemcpyAsync(&last_pair[1], block_nl + nb - 1, 4, cudaMemcpyDeviceToHost, st));
+    OBJ_CK(cudaMemcpyAsync(&n_nl, totals, 4, cudaMemcpyDeviceToHost, st));
     OBJ_CK(cudaStreamSynchronize(st));
     if (first_bad < len) {
         out->code = ObjOutcome::kNotUtf8;
         out->valid_up_to = first_bad;
         return cudaSuccess;
     }
-    const uint32_t n_nl = last_pair[0] + last_pair[1];
     const uint32_t L = n_nl + (host_text[len - 1] != '\n' ? 1u : 0u);
     if (L == 0) return cudaSuccess;
-    // ---- stage 2: lines, classification, scans
-    const size_t scan_words_l = scan_tmp_words(L);
+    // ---- stage 2: lines, classification, the five line scans
+    const uint32_t nbl = blocks_for(L);
     {
         const size_t bytes = carve_bytes(std::max<uint32_t>(n_nl, 1), 4) + carve_bytes(L, 1) +
-                             7 * carve_bytes(L, 4) + carve_bytes(scan_words_l, 4) + carve_bytes(16, 4);
+                             7 * carve_bytes(L, 4) + carve_bytes(5ull * nbl, 4);
         OBJ_CK(S.lines.ensure(bytes));
     }
     p = S.lines.as<char>();
@@ -783,20 +954,17 @@ cudaError_t obj_append(const char *host_text, unsigned long long len, uint32_t m
     A.rest_b = carve<uint32_t>(p, L);
     A.rest_e = carve<uint32_t>(p, L);
     for (int j = 0; j < 5; ++j) A.cnt[j] = carve<uint32_t>(p, L);
-    uint32_t *scan_tmp_l = carve<uint32_t>(p, scan_words_l);
-    uint32_t *last5 = carve<uint32_t>(p, 16);
-    uint32_t *tot5 = last5 + 8;
+    uint32_t *line_sums = carve<uint32_t>(p, 5ull * nbl);
     OBJ_CK(cudaEventRecord(S.ev[3], st));
-    k_obj_lines<<<nb, kObjThreads, 0, st>>>(reinterpret_cast<const uint4 *>(text), n16, block_off, nl_pos);
+    k_obj_lines<<<nb, kObjThreads, 0, st>>>(reinterpret_cast<const uint4 *>(text), n16, block_nl, nl_pos);
     note_launch();
-    k_obj_classify<<<blocks_for(L), kObjThreads, 0, st>>>(text, len, n_nl, nl_pos, L, A, last5);
+    k_obj_classify<<<nbl, kObjThreads, 0, st>>>(text, len, n_nl, nl_pos, L, A, line_sums);
     note_launch();
-    for (int j = 0; j < 5; ++j) exclusive_scan_u32(A.cnt[j], A.cnt[j], L, scan_tmp_l, st);
-    k_obj_totals<<<1, 32, 0, st>>>(A, L, last5, tot5);
+    k_scan_top<<<1, 1024, 0, st>>>(line_sums, nbl, 5, totals + 1);
     note_launch();
     OBJ_CK(cudaEventRecord(S.ev[4], st));
     uint32_t tot[5];
-    OBJ_CK(cudaMemcpyAsync(tot, tot5, sizeof(tot), cudaMemcpyDeviceToHost, st));
+    OBJ_CK(cudaMemcpyAsync(tot, totals + 1, sizeof(tot), cudaMemcpyDeviceToHost, st));
     OBJ_CK(cudaStreamSynchronize(st));
     const uint32_t nV = tot[0], nVN = tot[1], nVT = tot[2], n_tok = tot[3], n_tri = tot[4];
     if (n_tri == 0) return cudaSuccess;           // no face line: no vertices and no triangles
@@ -804,11 +972,17 @@ cudaError_t obj_append(const char *host_text, unsigned long long len, uint32_t m
     // ---- stage 3: coordinates, face tokens, first occurrences
     uint32_t cap = 1024;
     while (cap < 2u * n_tok) cap <<= 1;
-    const size_t scan_words_t = scan_tmp_words(n_tok);
+    KeyPack kp;
+    kp.rp = std::max(nV, 1u);
+    kp.rt = (unsigned long long)nVT + 1;
+    kp.no_uv = nVT;
+    const unsigned long long rn = std::max(nVN, 1u);
+    kp.packed = kp.rp * kp.rt <= (1ull << 62) / rn;      // rp * rt * rn < 2^63: one table
+    const uint32_t ntok_blocks = blocks_for(n_tok);
     {
         const size_t bytes = carve_bytes(3ull * std::max(nV, 1u), 4) + carve_bytes(3ull * std::max(nVN, 1u), 4) +
-                             carve_bytes(2ull * std::max(nVT, 1u), 4) + 6 * carve_bytes(n_tok, 4) +
-                             2 * carve_bytes(cap, 8) + carve_bytes(cap, 4) + carve_bytes(scan_words_t, 4) +
+                             carve_bytes(2ull * std::max(nVT, 1u), 4) + 5 * carve_bytes(n_tok, 4) +
+                             (kp.packed ? 1 : 2) * carve_bytes(cap, sizeof(Slot)) + carve_bytes(ntok_blocks, 4) +
                              carve_bytes(16, 4);
         OBJ_CK(S.tokens.ensure(bytes));
     }
@@ -818,39 +992,38 @@ cudaError_t obj_append(const char *host_text, unsigned long long len, uint32_t m
     float *uv = carve<float>(p, 2ull * std::max(nVT, 1u));
     TokenArrays T;
     T.pi = carve<uint32_t>(p, n_tok); T.ti = carve<uint32_t>(p, n_tok); T.ni = carve<uint32_t>(p, n_tok);
-    T.slot = carve<uint32_t>(p, n_tok); T.first = carve<uint32_t>(p, n_tok); T.v = carve<uint32_t>(p, n_tok);
-    unsigned long long *keys_a = carve<unsigned long long>(p, cap);
-    unsigned long long *keys_b = carve<unsigned long long>(p, cap);
-    uint32_t *min_tok = carve<uint32_t>(p, cap);
-    uint32_t *scan_tmp_t = carve<uint32_t>(p, scan_words_t);
-    uint32_t *flags = carve<uint32_t>(p, 16);         // [0] table error, [1] last first-flag
-    OBJ_CK(cudaMemsetAsync(keys_a, 0xFF, 2 * carve_bytes(cap, 8) + carve_bytes(cap, 4), st));   // keys_a, keys_b, min_tok
+    T.slot = carve<uint32_t>(p, n_tok); T.first = carve<uint32_t>(p, n_tok);
+    Slot *tab_b = carve<Slot>(p, cap);
+    Slot *tab_a = kp.packed ? nullptr : carve<Slot>(p, cap);
+    uint32_t *tok_sums = carve<uint32_t>(p, ntok_blocks);
+    uint32_t *flags = carve<uint32_t>(p, 16);         // [0] table error
+    OBJ_CK(cudaMemsetAsync(tab_b, 0xFF, (kp.packed ? 1 : 2) * carve_bytes(cap, sizeof(Slot)), st));   // empty keys
     OBJ_CK(cudaMemsetAsync(flags, 0, 64, st));
     OBJ_CK(cudaEventRecord(S.ev[5], st));
-    k_obj_parse<<<blocks_for(L), kObjThreads, 0, st>>>(text, L, A, pos, nrm, uv, T);
+    k_obj_parse<<<nbl, kObjThreads, 0, st>>>(text, L, A, line_sums, pos, nrm, uv, T);
     note_launch();
-    k_obj_dedup<<<blocks_for(n_tok), kObjThreads, 0, st>>>(n_tok, T, keys_a, keys_b, cap - 1, min_tok, flags);
+    k_obj_dedup<<<ntok_blocks, kObjThreads, 0, st>>>(n_tok, T, tab_a, tab_b, cap - 1, kp, flags);
     note_launch();
-    k_obj_first<<<blocks_for(n_tok), kObjThreads, 0, st>>>(n_tok, T, min_tok, flags + 1);
+    k_obj_first<<<ntok_blocks, kObjThreads, 0, st>>>(n_tok, T, tab_b, tok_sums);
     note_launch();
-    exclusive_scan_u32(T.first, T.first, n_tok, scan_tmp_t, st);
+    k_scan_top<<<1, 1024, 0, st>>>(tok_sums, ntok_blocks, 1, totals + 6);
+    note_launch();
     OBJ_CK(cudaEventRecord(S.ev[6], st));
-    uint32_t fl[2], last_first_scan = 0;
-    OBJ_CK(cudaMemcpyAsync(fl, flags, 8, cudaMemcpyDeviceToHost, st));
-    OBJ_CK(cudaMemcpyAsync(&last_first_scan, T.first + n_tok - 1, 4, cudaMemcpyDeviceToHost, st));
+    uint32_t table_err = 0, NV = 0;
+    OBJ_CK(cudaMemcpyAsync(&table_err, flags, 4, cudaMemcpyDeviceToHost, st));
+    OBJ_CK(cudaMemcpyAsync(&NV, totals + 6, 4, cudaMemcpyDeviceToHost, st));
     OBJ_CK(cudaStreamSynchronize(st));
-    if (fl[0]) return cudaErrorUnknown;               // a full table: excluded by its capacity
-    const uint32_t NV = last_first_scan + fl[1];
+    if (table_err) return cudaErrorUnknown;           // a full table: excluded by its capacity
     if ((unsigned long long)M.nv + NV >= (1ull << 31) || (unsigned long long)M.nt + n_tri >= (1ull << 27))
         return cudaErrorInvalidValue;
     // ---- stage 4: records, appended at the end of the device mesh
     OBJ_CK(mesh_reserve(M, NV, n_tri, st));
     float4 *verts = M.vertices.as<float4>() + 3ull * M.nv;
     OBJ_CK(cudaEventRecord(S.ev[7], st));
-    k_obj_vertices<<<blocks_for(n_tok), kObjThreads, 0, st>>>(n_tok, T, min_tok, pos, nrm, uv, verts);
+    k_obj_vertices<<<ntok_blocks, kObjThreads, 0, st>>>(n_tok, T, tok_sums, pos, nrm, uv, verts);
     note_launch();
-    k_obj_faces<<<blocks_for(L), kObjThreads, 0, st>>>(L, n_tok, A, T, verts, M.nv, M.triangles.as<uint4>() + M.nt,
-                                                       mat_idx);
+    k_obj_faces<<<nbl, kObjThreads, 0, st>>>(L, A, line_sums, T, tab_b, verts, M.nv,
+                                             M.triangles.as<uint4>() + M.nt, mat_idx);
     note_launch();
     if (!X.identity) {
         k_obj_transform<<<blocks_for(NV), kObjThreads, 0, st>>>(verts, NV, X);
