@@ -134,8 +134,14 @@ __device__ __forceinline__ uint32_t bf16_bits(float x) {
 }
 __device__ __forceinline__ float bf16_float(uint32_t b) { return __uint_as_float(b << 16); }
 __device__ __forceinline__ uint32_t pack2(float a, float b) { return bf16_bits(a) | (bf16_bits(b) << 16); }
-// ReLU with a canonical +0 for every non-positive (and NaN) input.
-__device__ __forceinline__ float relu(float x) { return x > 0.0f ? x : 0.0f; }
+// bf16 pair of max(a, 0), max(b, 0) in one conversion: cvt.rn.relu.bf16x2.f32
+// rounds both to bf16 and clamps negative results to +0 (rounding keeps the
+// sign, so the order of the clamp and the rounding does not matter).
+__device__ __forceinline__ uint32_t pack2_relu(float a, float b) {
+    uint32_t d;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(b), "f"(a));
+    return d;
+}
 
 // Stage the weight image and biases in shared memory (16-byte vector copies).
 __device__ void load_net(const NetDev &net, uint8_t *smem) {
@@ -295,10 +301,10 @@ __global__ void __launch_bounds__(128 * kInferGroups) k_cache_infer(NetDev net, 
                     for (uint32_t k = 0; k < 32; k += 8) {
                         const float *bb = bias + bias_idx(l) + c + k;
                         *reinterpret_cast<uint4 *>(act + tc::op_offset(row, c + k, kTile)) = make_uint4(
-                            pack2(relu(v[k] + bb[0]), relu(v[k + 1] + bb[1])),
-                            pack2(relu(v[k + 2] + bb[2]), relu(v[k + 3] + bb[3])),
-                            pack2(relu(v[k + 4] + bb[4]), relu(v[k + 5] + bb[5])),
-                            pack2(relu(v[k + 6] + bb[6]), relu(v[k + 7] + bb[7])));
+                            pack2_relu(v[k] + bb[0], v[k + 1] + bb[1]),
+                            pack2_relu(v[k + 2] + bb[2], v[k + 3] + bb[3]),
+                            pack2_relu(v[k + 4] + bb[4], v[k + 5] + bb[5]),
+                            pack2_relu(v[k + 6] + bb[6], v[k + 7] + bb[7]));
                     }
                 }
                 group_operand_sync(bar_id);
@@ -431,10 +437,10 @@ __global__ void __launch_bounds__(128, 1) k_cache_train(NetDev net, TrainIO io, 
                     for (uint32_t k = 0; k < 32; k += 8) {
                         const float *bb = bias + bias_idx(l) + c + k;
                         *reinterpret_cast<uint4 *>(out + tc::op_offset(row, c + k, kTile)) = make_uint4(
-                            pack2(relu(v[k] + bb[0]), relu(v[k + 1] + bb[1])),
-                            pack2(relu(v[k + 2] + bb[2]), relu(v[k + 3] + bb[3])),
-                            pack2(relu(v[k + 4] + bb[4]), relu(v[k + 5] + bb[5])),
-                            pack2(relu(v[k + 6] + bb[6]), relu(v[k + 7] + bb[7])));
+                            pack2_relu(v[k] + bb[0], v[k + 1] + bb[1]),
+                            pack2_relu(v[k + 2] + bb[2], v[k + 3] + bb[3]),
+                            pack2_relu(v[k + 4] + bb[4], v[k + 5] + bb[5]),
+                            pack2_relu(v[k + 6] + bb[6], v[k + 7] + bb[7]));
                     }
                 }
             } else {
