@@ -379,10 +379,13 @@ mcrt_status mcrt_mesh_append_obj(mcrt_ctx *ctx, const char *text, uint64_t len, 
                                  const mcrt_mesh_transform *xf, const char *source, uint32_t *out_n_vertices,
                                  uint32_t *out_n_triangles);
 
-/* The last successful mcrt_mesh_append_obj: out_ms2 = [text copy to the device,
- * parse kernels] (ms, CUDA events on the context stream; the kernel figure
- * excludes the parser's host waits for sizes); out_counts4 = [text bytes,
- * lines, face tokens, kernel launches]. */
+/* The last successful mcrt_mesh_append_obj: out_ms2 = [text to the device,
+ * the other parse stages] (ms, CUDA events on the context stream, the parser's
+ * host waits for sizes excluded); out_counts4 = [text bytes, lines, face
+ * tokens, kernel launches].  On a device that reaches pageable host memory
+ * (cudaDevAttrPageableMemoryAccess) the parser's first pass reads the text in
+ * place and copies it as it counts the lines: out_ms2[0] is that pass; else it
+ * is the copy (MCRT_OBJ_COPY_TEXT=1 in the environment forces the copy). */
 mcrt_status mcrt_mesh_obj_stats(mcrt_ctx *ctx, float *out_ms2, uint64_t *out_counts4);
 
 /* Copy the device mesh to the host (capacities in records; NULL arrays are

@@ -97,6 +97,7 @@ struct mcrt_ctx {
     mcrt::DeviceMesh dmesh;
     mcrt::ObjScratch obj;
     unsigned long long last_obj_counts[4] = {0, 0, 0, 0};   // bytes, lines, face tokens, kernel launches
+    int pageable_access = -1;                                 // cudaDevAttrPageableMemoryAccess (-1: not read)
     float last_obj_ms[2] = {0.0f, 0.0f};                    // text copy, kernels
     // batched views and graph replay
     DBuf views, pass_state;
@@ -1316,9 +1317,15 @@ mcrt_status mcrt_mesh_append_obj(mcrt_ctx *ctx, const char *text, uint64_t len, 
     for (int k = 0; k < 3; ++k) X.t[k] = xf && xf->has_translate ? xf->translate[k] : 0.0f;
     if (X.has_r) mcrt_host::rotation_matrix(xf->rotate_deg, X.m);
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if (ctx->pageable_access < 0)
+        CK(cudaDeviceGetAttribute(&ctx->pageable_access, cudaDevAttrPageableMemoryAccess, ctx->device), "attribute");
+    // the device reads the host text in place where it can reach pageable
+    // memory (coherent systems); MCRT_OBJ_COPY_TEXT=1 copies it first instead
+    const char *copy_env = getenv("MCRT_OBJ_COPY_TEXT");
+    const bool direct = ctx->pageable_access == 1 && !(copy_env && copy_env[0] == '1');
     const uint32_t nv0 = ctx->dmesh.nv, nt0 = ctx->dmesh.nt;
     mcrt::ObjOutcome r;
-    cudaError_t e = mcrt::obj_append(text, len, mat_idx, X, ctx->dmesh, ctx->obj, ctx->stream, &r);
+    cudaError_t e = mcrt::obj_append(text, len, mat_idx, X, ctx->dmesh, ctx->obj, ctx->stream, direct, &r);
     if (e == cudaErrorInvalidValue)
         return fail(ctx, MCRT_ERR_INVALID_ARG, "OBJ text '" + src + "' is beyond the device parser's limits");
     if (e != cudaSuccess) return cuda_fail(ctx, e, "OBJ parse");

@@ -187,7 +187,7 @@ struct ObjOutcome {
     int code = kNoGeometry;
     unsigned long long valid_up_to = 0;   // first invalid byte (kNotUtf8)
     uint32_t n_vertices = 0, n_triangles = 0, n_lines = 0, n_tokens = 0;
-    float h2d_ms = 0.0f, kernel_ms = 0.0f;    // text copy; kernel stages (CUDA events, host waits excluded)
+    float h2d_ms = 0.0f, kernel_ms = 0.0f;    // text to the device; the other stages (CUDA events, host waits excluded)
     unsigned long long launches = 0;
 };
 // Grow the mesh's buffers (keeping their records) for add_v / add_t more.
@@ -196,9 +196,11 @@ cudaError_t mesh_reserve(DeviceMesh &M, uint32_t add_v, uint32_t add_t, cudaStre
 cudaError_t mesh_append_host(DeviceMesh &M, const mcrt_gpu_vertex *v, uint32_t nv, const mcrt_gpu_triangle *t,
                              uint32_t nt, DBuf &staging, cudaStream_t st);
 // load_obj (mesh.rs:474-642) of host OBJ text on the device, transformed and
-// appended to M.  cudaErrorInvalidValue: text or mesh beyond the parser's limits.
+// appended to M.  direct: the device reads the (pageable) host text in place
+// in its first pass instead of a copy beforehand.  cudaErrorInvalidValue: text
+// or mesh beyond the parser's limits.
 cudaError_t obj_append(const char *host_text, unsigned long long len, uint32_t mat_idx, const ObjTransform &X,
-                       DeviceMesh &M, ObjScratch &S, cudaStream_t st, ObjOutcome *out);
+                       DeviceMesh &M, ObjScratch &S, cudaStream_t st, bool direct, ObjOutcome *out);
 
 // Radiance-cache MLP (mlp.cu)
 struct CacheState;

@@ -495,18 +495,43 @@ __global__ void __launch_bounds__(1024) k_scan_top(uint32_t *sums, uint32_t nb, 
     }
 }
 
-__global__ void __launch_bounds__(kObjThreads) k_obj_scan_text(const uint4 *t16, unsigned long long len, uint32_t n16,
+// Bytes of 32-bit word j of 16-byte group i16 that lie in the text [off, end).
+__device__ __forceinline__ uint32_t word_in_text(uint32_t i16, int j, uint32_t off, uint32_t end) {
+    const uint32_t p0 = 16u * i16 + 4u * (uint32_t)j;
+    if (p0 >= off && p0 + 4u <= end) return 0xFFFFFFFFu;
+    uint32_t m = 0;
+    for (uint32_t b = 0; b < 4; ++b)
+        if (p0 + b >= off && p0 + b < end) m |= 0xFFu << (8 * b);
+    return m;
+}
+
+// First pass over the text, 16 bytes per thread: src holds the text at byte
+// offset off of 16-byte groups (the caller's host buffer read in place, its
+// groups aligned down, or the device copy); dst (optional) receives the
+// groups.  Newlines per block and the UTF-8 check, both over [off, off + len)
+// only (an aligned group never crosses a page, so reading the groups that
+// overlap the text reads mapped memory only).
+__global__ void __launch_bounds__(kObjThreads) k_obj_scan_text(const uint4 *src16, uint4 *dst16, uint32_t off,
+                                                               unsigned long long len, uint32_t n16,
                                                                uint32_t *block_nl, unsigned long long *first_bad) {
     const uint32_t i16 = blockIdx.x * kObjThreads + threadIdx.x;
+    const uint32_t end = off + (uint32_t)len;
     uint32_t cnt = 0;
     if (i16 < n16) {
-        const uint4 w = t16[i16];
-        cnt = (__popc(nl_mask(w.x)) + __popc(nl_mask(w.y)) + __popc(nl_mask(w.z)) + __popc(nl_mask(w.w)));
-        if ((w.x | w.y | w.z | w.w) & 0x80808080u) {
-            const uint8_t *t = reinterpret_cast<const uint8_t *>(t16);
+        const uint4 w = src16[i16];
+        if (dst16) dst16[i16] = w;
+        const uint32_t r[4] = {word_in_text(i16, 0, off, end), word_in_text(i16, 1, off, end),
+                               word_in_text(i16, 2, off, end), word_in_text(i16, 3, off, end)};
+        cnt = __popc(nl_mask(w.x) & r[0]) + __popc(nl_mask(w.y) & r[1]) + __popc(nl_mask(w.z) & r[2]) +
+              __popc(nl_mask(w.w) & r[3]);
+        if (((w.x & r[0]) | (w.y & r[1]) | (w.z & r[2]) | (w.w & r[3])) & 0x80808080u) {
+            const uint8_t *t = reinterpret_cast<const uint8_t *>(src16) + off;     // the text itself
             for (int k = 0; k < 16; ++k) {
-                const unsigned long long i = 16ull * i16 + k;
-                if (i < len && !utf8_byte_ok(t, len, i)) { atomicMin(first_bad, i); break; }
+                const long long i = 16ll * i16 + k - off;
+                if (i >= 0 && (unsigned long long)i < len && !utf8_byte_ok(t, len, (unsigned long long)i)) {
+                    atomicMin(first_bad, (unsigned long long)i);
+                    break;
+                }
             }
         }
     }
@@ -515,36 +540,38 @@ __global__ void __launch_bounds__(kObjThreads) k_obj_scan_text(const uint4 *t16,
     if (threadIdx.x == 0) block_nl[blockIdx.x] = total;
 }
 
-__global__ void __launch_bounds__(kObjThreads) k_obj_lines(const uint4 *t16, uint32_t n16, const uint32_t *block_off,
-                                                           uint32_t *nl_pos) {
+// Newline positions (in buffer coordinates) of the text [off, end).
+__global__ void __launch_bounds__(kObjThreads) k_obj_lines(const uint4 *t16, uint32_t n16, uint32_t off, uint32_t end,
+                                                           const uint32_t *block_off, uint32_t *nl_pos) {
     const uint32_t i16 = blockIdx.x * kObjThreads + threadIdx.x;
     uint4 w = make_uint4(0, 0, 0, 0);
     if (i16 < n16) w = t16[i16];
-    const uint32_t m[4] = {nl_mask(w.x), nl_mask(w.y), nl_mask(w.z), nl_mask(w.w)};
+    const uint32_t m[4] = {nl_mask(w.x) & word_in_text(i16, 0, off, end), nl_mask(w.y) & word_in_text(i16, 1, off, end),
+                           nl_mask(w.z) & word_in_text(i16, 2, off, end), nl_mask(w.w) & word_in_text(i16, 3, off, end)};
     const uint32_t cnt = __popc(m[0]) + __popc(m[1]) + __popc(m[2]) + __popc(m[3]);
     uint32_t at = block_off[blockIdx.x] + block_exclusive_scan(cnt, nullptr);
     for (int k = 0; k < 4; ++k)
         for (int b = 0; b < 4; ++b)
             if (m[k] & (0x80u << (8 * b))) nl_pos[at++] = 16u * i16 + 4u * k + b;
 }
-
 struct LineArrays {
     uint8_t *kind;
     uint32_t *rest_b, *rest_e;
-    uint32_t *cnt[5];   // v, vn, vt, face tokens, triangles (exclusive-scanned in place)
+    uint32_t *cnt[5];   // per line: v, vn, vt, face tokens, triangles (prefixes: line_offsets)
 };
 
-__device__ __forceinline__ void line_bounds(uint32_t k, uint32_t n_nl, const uint32_t *nl_pos,
-                                            unsigned long long len, uint32_t *b, uint32_t *e) {
-    *b = k == 0 ? 0u : nl_pos[k - 1] + 1u;
-    *e = k < n_nl ? nl_pos[k] : (uint32_t)len;
+// Line k of the text [off, end) of the buffer.
+__device__ __forceinline__ void line_bounds(uint32_t k, uint32_t n_nl, const uint32_t *nl_pos, uint32_t off,
+                                            uint32_t end, uint32_t *b, uint32_t *e) {
+    *b = k == 0 ? off : nl_pos[k - 1] + 1u;
+    *e = k < n_nl ? nl_pos[k] : end;
 }
 
 // str::lines + str::trim + '#' + split_ascii_whitespace + the tag match of line k.
-__device__ __forceinline__ void classify_line(const uint8_t *t, unsigned long long len, uint32_t n_nl,
-                                                   const uint32_t *nl_pos, uint32_t k, LineArrays A, uint32_t c[5]) {
+__device__ __forceinline__ void classify_line(const uint8_t *t, uint32_t off, uint32_t end, uint32_t n_nl,
+                                              const uint32_t *nl_pos, uint32_t k, LineArrays A, uint32_t c[5]) {
     uint32_t b, e;
-    line_bounds(k, n_nl, nl_pos, len, &b, &e);
+    line_bounds(k, n_nl, nl_pos, off, end, &b, &e);
     int n;
     #pragma unroll 1
     while (b < e && (n = ws_forward(t + b, t + e)) > 0) b += n;
@@ -580,12 +607,12 @@ __device__ __forceinline__ void classify_line(const uint8_t *t, unsigned long lo
 }
 
 // Per-line kind and counts (mesh.rs:502-521), and each block's sums of the counts.
-__global__ void __launch_bounds__(kObjThreads) k_obj_classify(const uint8_t *t, unsigned long long len, uint32_t n_nl,
-                                                              const uint32_t *nl_pos, uint32_t L, LineArrays A,
-                                                              uint32_t *block_sums) {
+__global__ void __launch_bounds__(kObjThreads) k_obj_classify(const uint8_t *t, uint32_t off, uint32_t end,
+                                                              uint32_t n_nl, const uint32_t *nl_pos, uint32_t L,
+                                                              LineArrays A, uint32_t *block_sums) {
     const uint32_t k = blockIdx.x * kObjThreads + threadIdx.x;
     uint32_t c[5] = {0, 0, 0, 0, 0}, ex[5];
-    if (k < L) classify_line(t, len, n_nl, nl_pos, k, A, c);
+    if (k < L) classify_line(t, off, end, n_nl, nl_pos, k, A, c);
     block_exclusive_scan_n<5>(c, ex);
     if (threadIdx.x == kObjThreads - 1)
         for (int j = 0; j < 5; ++j) block_sums[(size_t)j * gridDim.x + blockIdx.x] = ex[j] + c[j];
@@ -898,16 +925,22 @@ cudaError_t mesh_append_host(DeviceMesh &M, const mcrt_gpu_vertex *v, uint32_t n
 }
 
 cudaError_t obj_append(const char *host_text, unsigned long long len, uint32_t mat_idx, const ObjTransform &X,
-                       DeviceMesh &M, ObjScratch &S, cudaStream_t st, ObjOutcome *out) {
+                       DeviceMesh &M, ObjScratch &S, cudaStream_t st, bool direct, ObjOutcome *out) {
     *out = ObjOutcome{};
     out->code = ObjOutcome::kNoGeometry;
     if (len == 0) return cudaSuccess;
     if (!S.ev[0])
         for (cudaEvent_t &e : S.ev) OBJ_CK(cudaEventCreate(&e));
     const unsigned long long launches0 = launch_count();
-    if (len > 0xFFFFFF00ull) return cudaErrorInvalidValue;      // byte offsets are 32-bit
-    // ---- stage 1: text, newline counts per block, UTF-8 check
-    const uint32_t n16 = (uint32_t)((len + 15) / 16);
+    if (len > 0xFFFFFF00ull - 16) return cudaErrorInvalidValue;  // byte offsets are 32-bit
+    // ---- stage 1: text, newline counts per block, UTF-8 check.  direct: the
+    // first pass reads the caller's buffer in place (pageable memory the GPU
+    // reaches through the host page tables) and copies it as it scans; the
+    // text then starts at byte `off` of its first 16-byte group.
+    const uintptr_t hp = reinterpret_cast<uintptr_t>(host_text);
+    const uint32_t off = direct ? (uint32_t)(hp & 15u) : 0u;
+    const uint32_t end = off + (uint32_t)len;
+    const uint32_t n16 = (uint32_t)((off + len + 15) / 16);
     const uint32_t nb = blocks_for(n16);
     {
         const size_t bytes = carve_bytes((size_t)n16 * 16 + 16, 1) + carve_bytes(nb, 4) + carve_bytes(16, 8);
@@ -919,12 +952,20 @@ cudaError_t obj_append(const char *host_text, unsigned long long len, uint32_t m
     unsigned long long *small = carve<unsigned long long>(p, 16);     // [0] first bad byte, [1..] totals
     uint32_t *totals = reinterpret_cast<uint32_t *>(small + 2);       // [0] newlines, [1..5] line fields, [6] vertices
     OBJ_CK(cudaMemsetAsync(text + (size_t)n16 * 16 - 16, 0, 32, st));
-    OBJ_CK(cudaEventRecord(S.ev[0], st));
-    OBJ_CK(cudaMemcpyAsync(text, host_text, len, cudaMemcpyHostToDevice, st));
-    OBJ_CK(cudaEventRecord(S.ev[1], st));
     OBJ_CK(cudaMemsetAsync(small, 0xFF, 8, st));
-    k_obj_scan_text<<<nb, kObjThreads, 0, st>>>(reinterpret_cast<const uint4 *>(text), len, n16, block_nl, small);
-    note_launch();
+    OBJ_CK(cudaEventRecord(S.ev[0], st));
+    if (direct) {
+        k_obj_scan_text<<<nb, kObjThreads, 0, st>>>(reinterpret_cast<const uint4 *>(hp - off),
+                                                    reinterpret_cast<uint4 *>(text), off, len, n16, block_nl, small);
+        note_launch();
+        OBJ_CK(cudaEventRecord(S.ev[1], st));
+    } else {
+        OBJ_CK(cudaMemcpyAsync(text, host_text, len, cudaMemcpyHostToDevice, st));
+        OBJ_CK(cudaEventRecord(S.ev[1], st));
+        k_obj_scan_text<<<nb, kObjThreads, 0, st>>>(reinterpret_cast<const uint4 *>(text), nullptr, 0u, len, n16,
+                                                    block_nl, small);
+        note_launch();
+    }
     k_scan_top<<<1, 1024, 0, st>>>(block_nl, nb, 1, totals);
     note_launch();
     OBJ_CK(cudaEventRecord(S.ev[2], st));
@@ -956,9 +997,9 @@ cudaError_t obj_append(const char *host_text, unsigned long long len, uint32_t m
     for (int j = 0; j < 5; ++j) A.cnt[j] = carve<uint32_t>(p, L);
     uint32_t *line_sums = carve<uint32_t>(p, 5ull * nbl);
     OBJ_CK(cudaEventRecord(S.ev[3], st));
-    k_obj_lines<<<nb, kObjThreads, 0, st>>>(reinterpret_cast<const uint4 *>(text), n16, block_nl, nl_pos);
+    k_obj_lines<<<nb, kObjThreads, 0, st>>>(reinterpret_cast<const uint4 *>(text), n16, off, end, block_nl, nl_pos);
     note_launch();
-    k_obj_classify<<<nbl, kObjThreads, 0, st>>>(text, len, n_nl, nl_pos, L, A, line_sums);
+    k_obj_classify<<<nbl, kObjThreads, 0, st>>>(text, off, end, n_nl, nl_pos, L, A, line_sums);
     note_launch();
     k_scan_top<<<1, 1024, 0, st>>>(line_sums, nbl, 5, totals + 1);
     note_launch();

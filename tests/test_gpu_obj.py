@@ -16,6 +16,17 @@ import obj_cases as C  # noqa: E402
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(params=["direct", "copy"], autouse=True)
+def text_path(request, monkeypatch):
+    """Every test twice: the parser's first pass reading the host text in place
+    (where the device reaches pageable memory) and a copy of it first."""
+    if request.param == "copy":
+        monkeypatch.setenv("MCRT_OBJ_COPY_TEXT", "1")
+    else:
+        monkeypatch.delenv("MCRT_OBJ_COPY_TEXT", raising=False)
+    return request.param
+
+
 def dev_load(ctx, text, mat=0, **xf):
     ctx.mesh_reset()
     nv, nt = ctx.mesh_append_obj(text, mat, **xf)
@@ -241,11 +252,36 @@ def test_icosphere_level8_matches_oracle(ctx, oracle):
     assert same(v_d, t_d, v_o, t_o)
 
 
-def test_voxel_world_faces_round_trip(ctx):
+def test_text_at_every_alignment(ctx, oracle, mcrt):
+    """The text starting at every offset within a 16-byte group of the caller's
+    buffer (the in-place first pass reads whole aligned groups and keeps only
+    the text's bytes), and ending at every offset too."""
+    import ctypes
+    from mcrt_gb300 import _native as N
+    text = C.EDGE_CASES["mixed_has_norm_fan"] + C.EDGE_CASES["uv_keys"] + b"\n# \xc3\xa9\n"
+    v_o, t_o = oracle.obj_load(text, 4)
+    for shift in range(16):
+        for tail in (0, 5):
+            data = text[:len(text) - tail] if tail else text
+            v_want, t_want = (v_o, t_o) if not tail else oracle.obj_load(data, 4)
+            buf = ctypes.create_string_buffer(b"\n" * 16 + data + b"f 1 2 3\n" * 4, len(data) + 64)
+            addr = ctypes.addressof(buf) + 16 + shift - (ctypes.addressof(buf) + 16) % 16
+            ctypes.memmove(addr, data, len(data))
+            ctx.mesh_reset()
+            nv, nt = ctypes.c_uint32(), ctypes.c_uint32()
+            N.check(N.lib().mcrt_mesh_append_obj(ctx._h, ctypes.cast(addr, ctypes.c_char_p), len(data), 4, None,
+                                                 None, ctypes.byref(nv), ctypes.byref(nt)), ctx._h)
+            v_d, t_d = ctx.mesh_read()
+            assert same(v_d, t_d, v_want, t_want), (shift, tail)
+
+
+def test_voxel_world_faces_round_trip(ctx, text_path):
     """The voxel world's face mesh (256 x 128 x 256, ~4.9 M triangles) written as
     OBJ and parsed on the device gives the mesher's own triangles: the same
     corner positions and normals in the same order (positions are multiples of
     1/8: exact in 6 decimals)."""
+    if text_path == "copy":
+        pytest.skip("the 667 MB text runs once, with the in-place first pass")
     from mcrt_gb300 import scenes
     w = scenes.voxel_world(1234)
     ctx.world_generate(w["params"])
