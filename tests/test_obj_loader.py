@@ -107,3 +107,25 @@ def test_deferred_load_keeps_primitives_only(tmp_path):
         assert len(M._scene_from_handle(h).triangles) == 1
     finally:
         N.lib().mcrt_scene_free(h)
+
+
+def test_obj_writer_round_trips_through_the_loader(oracle):
+    """scenes.obj_text (the benchmark meshes' OBJ text): fixed-point
+    coordinates to 6 decimals in space-padded fields, 1-based a//n face tokens;
+    loaded back, the positions are the 6-decimal values and the triangles the
+    mesh's own, vertices shared by (position, normal)."""
+    from mcrt_gb300 import scenes
+    rng = np.random.default_rng(3)
+    P = rng.uniform(-50, 50, (200, 3)).astype(np.float32)
+    Nn = rng.normal(size=(200, 3)).astype(np.float32)
+    F = rng.integers(0, 200, (300, 3))
+    text = scenes.obj_text(P, F, normals=Nn)
+    v, t = oracle.obj_load(text, 0)
+    assert len(t) == 300
+    got = v["position"][t["v"]][..., :3]
+    want = np.round(P[F].astype(np.float64), 6)
+    assert np.allclose(got, want, atol=1e-5, rtol=0)
+    text2 = scenes.obj_text(P, F[:, [0, 1, 2]])            # no normals: a fresh vertex per face token
+    v2, t2 = oracle.obj_load(text2, 0)
+    assert len(v2) == 900 and len(t2) == 300
+    assert np.allclose(v2["position"][:, :3], want.reshape(-1, 3), atol=1e-5, rtol=0)
