@@ -70,12 +70,12 @@ W, H, SPP, DEPTH, LEVEL, SEED = 1920, 1080, 16, 12, 8, 1234
 WORKLOAD = "displaced_icosphere_l8_1.31Mtri_1920x1080_16spp_depth12_gpu_rebuild"
 # DRAM bytes (read + write) per traced ray of the closest-hit kernels on this
 # workload: one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the
-# 12 launches of a frame, 9.42 GB / 71.54 M rays
-EXTEND_DRAM_CAPTURE = {"bytes_per_ray": 131.7, "captured": "2026-12-04",
+# 12 launches of a frame, 10.47 GB / 71.54 M rays
+EXTEND_DRAM_CAPTURE = {"bytes_per_ray": 146.3, "captured": "2026-12-04",
                        "profile": "profiles/k_extend_displaced_icosphere_1080p16.md"}
 # L2 traffic of the closest-hit launches of bounces 1 and 2 on the 960x540x16 case
 # (ncu lts__t_bytes.sum / gpu__time_duration.sum), with the L2 and L1 sector hit rates
-EXTEND_L2_CAPTURE = {"gbs": [2999.3, 4154.9], "l2_hit_pct": [71.5, 74.8], "l1_hit_pct": [68.2, 61.9],
+EXTEND_L2_CAPTURE = {"gbs": [3389.2, 4355.2], "l2_hit_pct": [72.0, 73.9], "l1_hit_pct": [66.0, 60.8],
                      "captured": "2026-12-04", "case": "960x540, 16 spp, bounces 1 and 2",
                      "profile": "profiles/k_extend_displaced_icosphere_1080p16.md"}
 

@@ -32,31 +32,29 @@ __host__ __device__ __forceinline__ uint32_t leaf_code(uint32_t first, uint32_t 
 // 1/d with the clamp of the reference's traversal test (bvh.rs:808-812,
 // mesh.rs:950-954): |d| < 1e-7 -> +-1e30, so a ray lying in a slab plane counts
 // as inside the slab instead of producing 0 * inf = NaN.
-// The clamp value is +-2^100 here (the reference's 1e30 elsewhere): a power of
-// two keeps o * inv exact, so the slab below gives the clamped axis the
-// reference's sign, and exactly 0 for an origin on the plane, while every
-// magnitude it produces stays beyond any hit distance, as 1e30 does.
 __device__ __forceinline__ float inv_dir(float d) {
-    return fabsf(d) < 1e-7f ? (d >= 0.0f ? 0x1p100f : -0x1p100f) : 1.0f / d;
+    return fabsf(d) < 1e-7f ? (d >= 0.0f ? 1e30f : -1e30f) : 1.0f / d;
 }
-struct RayInv { f3 o, d, inv, oinv; };          // oinv = o * inv
+struct RayInv { f3 o, d, inv; };
 __device__ __forceinline__ RayInv make_ray(f3 o, f3 d) {
-    const f3 inv = mk3(inv_dir(d.x), inv_dir(d.y), inv_dir(d.z));
-    return {o, d, inv, mk3(o.x * inv.x, o.y * inv.y, o.z * inv.z)};
+    return {o, d, mk3(inv_dir(d.x), inv_dir(d.y), inv_dir(d.z))};
 }
 
 // ray_aabb_hit, path_trace.wgsl:248-256, with the slack kCullSlack on the
 // entry cull and the exit, so that the closest hit does not depend on the
-// visit order.  The plane distances are fma(plane, inv, -o * inv) (one
-// rounding instead of two): they differ from (plane - o) * inv by a few ulps,
-// far inside the slack, so a box is still entered whenever the exact interval
+// visit order.  Each plane distance (plane - o) * inv carries relative errors
+// only (the difference, the product and 1/d rounded once each), a few ulps,
+// inside the slack, so a box is still entered whenever the exact interval
 // reaches the closest hit, and the hit found is the same (the box test only
-// decides which boxes are visited).
+// decides which boxes are visited).  The fused form fma(plane, inv, -o * inv)
+// is not used: rounding o * inv adds an ABSOLUTE error of up to |o * inv|
+// 2^-25, beyond any relative slack for a ray that barely moves along an axis
+// and starts near a box plane of that axis far from the world origin.
 __device__ __forceinline__ bool slab(const RayInv &r, float lx, float ly, float lz, float hx, float hy, float hz,
                                      float tmin, float tmax, float *tenter_out) {
-    float t0x = fmaf(lx, r.inv.x, -r.oinv.x), t1x = fmaf(hx, r.inv.x, -r.oinv.x);
-    float t0y = fmaf(ly, r.inv.y, -r.oinv.y), t1y = fmaf(hy, r.inv.y, -r.oinv.y);
-    float t0z = fmaf(lz, r.inv.z, -r.oinv.z), t1z = fmaf(hz, r.inv.z, -r.oinv.z);
+    float t0x = (lx - r.o.x) * r.inv.x, t1x = (hx - r.o.x) * r.inv.x;
+    float t0y = (ly - r.o.y) * r.inv.y, t1y = (hy - r.o.y) * r.inv.y;
+    float t0z = (lz - r.o.z) * r.inv.z, t1z = (hz - r.o.z) * r.inv.z;
     float tenter = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
     float texit = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
     *tenter_out = tenter;

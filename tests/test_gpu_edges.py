@@ -61,3 +61,68 @@ def test_empty_ray_batch_and_zero_area_triangle(ctx, oracle):
     assert np.array_equal(got["prim"], want["prim"])
     assert np.array_equal(bits(got["t"]), bits(want["t"]))
     assert not np.any(got["prim"] == len(T) - 1)       # the zero-area triangle is never hit
+
+
+def _grazing_walls(k=4096, seed=9):
+    """k rays far from the origin in x (200..3000) with tiny direction x
+    components (2e-6..3e-5), each towards its own triangle in the plane a few
+    ulps of the origin away in x: a plane distance (plane - o) / d of the order
+    of the rounding of o / d itself.  Each triangle ends 0.05..3 past its hit in
+    z, so the box's exit there lies within that rounding of the entry."""
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(200, 3000, k).astype(np.float32)
+    dx = (rng.uniform(2e-6, 3e-5, k) * rng.choice([-1, 1], k)).astype(np.float32)
+    xk = (x + np.sign(dx) * rng.integers(1, 40, k) * np.spacing(x)).astype(np.float32)
+    y = (2.0 * np.arange(k)).astype(np.float32)
+    th = (xk.astype(np.float64) - x) / dx
+    z0, z1 = th - rng.uniform(0.5, 5, k), th + rng.uniform(0.05, 3, k)
+    V = np.zeros(3 * k, M._native.VERTEX)
+    V["position"][0::3] = np.column_stack([xk, y - 0.5, z0, np.ones(k)])
+    V["position"][1::3] = np.column_stack([xk, y + 0.5, z0, np.ones(k)])
+    V["position"][2::3] = np.column_stack([xk, y, z1, np.ones(k)])
+    T = np.zeros(k, M._native.TRIANGLE)
+    T["v"] = np.arange(3 * k).reshape(k, 3)
+    rays = M.make_rays(np.column_stack([x, y, np.zeros(k)]), np.column_stack([dx, np.zeros(k), np.ones(k)]))
+    return V, T, rays
+
+
+def test_grazing_rays_far_from_the_origin_find_their_hits(ctx, oracle):
+    """The box test's plane distances carry the rounding of o / d, absolute
+    and up to tens of units here; the interval is widened by its bound, so
+    every ray still enters its triangle's box and returns the oracle's hit."""
+    V, T, rays = _grazing_walls()
+    md = M.materials([(0, (0.5, 0.5, 0.5), 0, 1)])
+    ctx.upload_scene(vertices=V, triangles=T, materials=md)
+    want = oracle.OracleScene(materials=md, vertices=V, triangles=T).trace(rays, brute_force=True)
+    assert np.array_equal(want["prim"], np.arange(len(T), dtype=np.uint32))
+    for ref_layout in (False, True):
+        got = ctx.trace_closest(rays, reference_layout=ref_layout)
+        assert np.array_equal(got["prim"], want["prim"])
+        assert np.array_equal(bits(got["t"]), bits(want["t"]))
+
+
+def test_grazing_camera_every_variant_renders_the_oracle_image(ctx, oracle):
+    """Camera rays from x = 1234.5677 with direction x components of 1..21
+    ulps of that origin per 100 units, onto a wall 2 ulps away in x that ends
+    at z = 30: the wall's far edge is where the rounding of o / d decides the
+    box test.  Every closest-hit variant renders the oracle's image."""
+    X = np.float32(1234.5677)
+    u = np.spacing(X)
+    xw = np.float32(X + 2 * u)
+    V = np.zeros(4, M._native.VERTEX)
+    V["position"] = [[xw, -60, 0, 1], [xw, 60, 0, 1], [xw, 60, 30, 1], [xw, -60, 30, 1]]
+    T = np.zeros(2, M._native.TRIANGLE)
+    T["v"] = [(0, 1, 2), (0, 2, 3)]
+    md = M.materials([(0, (0.7, 0.6, 0.5), 0, 1)])
+    env = M.gradient_env_map()
+    cam = np.zeros((), M._native.CAMERA)
+    cam["origin"] = [X, 0, 0, 0]
+    cam["lower_left"] = [np.float32(X + u), -50, 100, 0]
+    cam["horizontal"] = [20 * u, 0, 0, 0]
+    cam["vertical"] = [0, 100, 0, 0]
+    w, h, spp = 48, 32, 2
+    ctx.upload_scene(vertices=V, triangles=T, materials=md, env=env)
+    want = oracle.OracleScene(materials=md, vertices=V, triangles=T, env=env).render(cam, w, h, spp, max_depth=3)
+    for v in range(8):
+        got = ctx.render(cam, w, h, spp, max_depth=3, variant=v)
+        assert np.array_equal(bits(got["rgba"]), bits(want["rgba"])), f"variant {v}"
