@@ -1641,10 +1641,10 @@ cudaError_t gpu_make_top(const float4 *d_cnodes, uint32_t n_cnodes, float4 *d_to
 // A node takes the two children of a binary node and repeatedly replaces the
 // internal child of largest surface area by its two children until it has
 // four.  Leaves are the reference's leaves.  Child boxes are rounded outward:
-// the builder checks, in the float arithmetic the traversal uses
-// (origin + q * step), that every dequantised plane lies outside the exact
-// child box, so a ray that reaches a leaf of the reference tree also reaches it
-// here.
+// the builder checks that every grid plane origin + q * step, as an exact real
+// number, lies outside the exact child box (the traversal bounds its plane
+// distances from that exact value), so a ray that reaches a leaf of the
+// reference tree also reaches it here.
 namespace {
 
 __device__ __forceinline__ float step_of(uint32_t e) { return __uint_as_float(e << 23); }
@@ -1660,17 +1660,28 @@ __device__ __forceinline__ uint32_t grid_exponent(float extent) {
     return e;
 }
 
+// Sign of the exact real origin + qs - v (qs = q * step, exact: step is a
+// power of two).  The rounded sum s lies within half an ulp of the exact one,
+// so s != v decides; at s == v the error-free residual of the sum (Knuth's
+// TwoSum: s + err is exactly origin + qs) does.
+__device__ __forceinline__ int grid_plane_vs(float origin, float qs, float v) {
+    const float s = origin + qs;
+    if (s != v) return s < v ? -1 : 1;
+    const float bb = s - origin;
+    const float err = (origin - (s - bb)) + (qs - bb);
+    return err < 0.0f ? -1 : (err > 0.0f ? 1 : 0);
+}
 __device__ __forceinline__ uint32_t quant_lo(float origin, float step, float v) {
     float q = floorf((v - origin) / step);
     int qi = q < 0.0f ? 0 : (q > 255.0f ? 255 : (int)q);
-    while (qi > 0 && origin + (float)qi * step > v) --qi;
+    while (qi > 0 && grid_plane_vs(origin, (float)qi * step, v) > 0) --qi;
     return (uint32_t)qi;
 }
 __device__ __forceinline__ uint32_t quant_hi(float origin, float step, float v, bool *ok) {
     float q = ceilf((v - origin) / step);
     int qi = q < 0.0f ? 0 : (q > 255.0f ? 255 : (int)q);
-    while (qi < 255 && origin + (float)qi * step < v) ++qi;
-    if (origin + (float)qi * step < v) *ok = false;
+    while (qi < 255 && grid_plane_vs(origin, (float)qi * step, v) < 0) ++qi;
+    if (grid_plane_vs(origin, (float)qi * step, v) < 0) *ok = false;
     return (uint32_t)qi;
 }
 

@@ -560,20 +560,38 @@ __device__ __forceinline__ void visit_compact2(const DeviceScene &S, const float
     }
 }
 
-// Visit a quantised 4-wide node: dequantise each child box on the node's grid
-// (origin + q * step, the float sequence the builder verified to enclose the
-// exact box), slab-test, order the hits by entry distance with a sorting
-// network on (distance bits, child) keys, continue with the nearest and push
-// the others farthest first.
+// Visit a quantised 4-wide node: slab-test each child box on the node's grid,
+// order the hits by entry distance with a sorting network on (distance bits,
+// child) keys, continue with the nearest and push the others farthest first.
+// A plane origin + q * step (the builder guarantees that the exact real value
+// lies outside the child box) is at distance q * a + b along the ray, with
+// a = step * inv exact (step is a power of two) and b = (origin - o) * inv
+// computed once per node and axis.  b carries two roundings, at most
+// 2^-23 |b|; scaled by 1 -+ 2^-22 it becomes a bound from below for the plane
+// that gives the entry on that axis and from above for the exit, so each
+// child's fma(q, a, b) interval contains the exact one up to the fma's own
+// relative rounding, which the cull's slack covers (as for slab()).
 template <int STACK>
 __device__ __forceinline__ void visit_wide4(const DeviceScene &S, const RayInv &r, float tmax, uint32_t *cur,
                                             float *cur_t, uint2 *stack, uint32_t *sp, bool *overflow) {
     const uint4 *np = S.wnodes + 4ull * *cur;
     const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3);
-    const float ox = __uint_as_float(w0.x), oy = __uint_as_float(w0.y), oz = __uint_as_float(w0.z);
-    const float sx = __uint_as_float((w0.w & 0xffu) << 23), sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23),
-                sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
+    const float org[3] = {__uint_as_float(w0.x), __uint_as_float(w0.y), __uint_as_float(w0.z)};
+    const float inv[3] = {r.inv.x, r.inv.y, r.inv.z}, o[3] = {r.o.x, r.o.y, r.o.z};
+    float a[3], blo[3], bhi[3];                     // b bounds for the low and the high planes
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        a[k] = __uint_as_float(((w0.w >> (8 * k)) & 0xffu) << 23) * inv[k];
+        const float b = (org[k] - o[k]) * inv[k];
+        const float p = b * 0.99999976158142089844f, q = b * 1.0000002384185791016f;   // b (1 -+ 2^-22)
+        const float dn = fminf(p, q), up = fmaxf(p, q);
+        blo[k] = inv[k] >= 0.0f ? dn : up;          // inv >= 0: the low plane is the entry
+        bhi[k] = inv[k] >= 0.0f ? up : dn;
+    }
     const uint32_t refs[4] = {w3.x, w3.y, w3.z, w3.w};
+    // the byte j of a word as a float: 0x4B0000bb is 2^23 + byte, exactly
+    auto qf = [](uint32_t w, uint32_t sel) { return __uint_as_float(__byte_perm(w, 0x4B000000u, sel)) - 8388608.0f; };
+    const float reach = cull_t(tmax);
     // key = entry distance bits (non-negative floats order as integers) with the
     // child index in the two low bits: the distance loses at most 3 ulp
     // downward, which only makes the later cull (distance <= closest t) looser.
@@ -582,13 +600,13 @@ __device__ __forceinline__ void visit_wide4(const DeviceScene &S, const RayInv &
     for (int j = 0; j < 4; ++j) {
         key[j] = 0xffffffffu;
         if (refs[j] == kNoChild) continue;
-        const int sh = 8 * j;
-        float lx = ox + (float)((w1.x >> sh) & 0xffu) * sx, ly = oy + (float)((w1.y >> sh) & 0xffu) * sy,
-              lz = oz + (float)((w1.z >> sh) & 0xffu) * sz;
-        float hx = ox + (float)((w1.w >> sh) & 0xffu) * sx, hy = oy + (float)((w2.x >> sh) & 0xffu) * sy,
-              hz = oz + (float)((w2.y >> sh) & 0xffu) * sz;
-        float te;
-        if (slab(r, lx, ly, lz, hx, hy, hz, kTMin, tmax, &te))
+        const uint32_t sel = 0x7440u + (uint32_t)j;
+        const float t0x = fmaf(qf(w1.x, sel), a[0], blo[0]), t1x = fmaf(qf(w1.w, sel), a[0], bhi[0]);
+        const float t0y = fmaf(qf(w1.y, sel), a[1], blo[1]), t1y = fmaf(qf(w2.x, sel), a[1], bhi[1]);
+        const float t0z = fmaf(qf(w1.z, sel), a[2], blo[2]), t1z = fmaf(qf(w2.y, sel), a[2], bhi[2]);
+        const float te = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
+        const float tx = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+        if (cull_t(tx) > fmaxf(te, kTMin) && te <= reach)
             key[j] = (__float_as_uint(fmaxf(te, 0.0f)) & ~3u) | (uint32_t)j;
     }
     auto cx = [](uint32_t &a, uint32_t &b) {
