@@ -1128,8 +1128,11 @@ __device__ __forceinline__ uint32_t partition_flag(const BuildState &S, int cur,
 // from a ticket (tiles start in order, so every predecessor of a tile is
 // running or done), scans its kFlagTile flags, publishes its sum, adds its
 // predecessors' published sums walking back to the first inclusive prefix,
-// and publishes its own.  Every wait is bounded: after kLookbackPolls polls the
-// tile records the error word and goes on (the host fails the build).
+// and publishes its own.  The walk reads 32 predecessors per step, one per lane
+// of the first warp: the nearest inclusive prefix among them (ballot) ends it,
+// else their sums are added and the window moves back.  Every wait is bounded:
+// after kLookbackPolls polls of a predecessor the tile records the error word
+// and goes on (the host fails the build).
 __global__ void __launch_bounds__(kFlagThreads) k_flag_scan(BuildState S, int cur) {
     __shared__ uint32_t s_tile, s_excl, s_warp[kFlagThreads / 32];
     const uint32_t t = threadIdx.x, lane = t & 31u, w = t >> 5;
@@ -1164,32 +1167,41 @@ __global__ void __launch_bounds__(kFlagThreads) k_flag_scan(BuildState S, int cu
     __syncthreads();
     const uint32_t block_total = s_warp[kFlagThreads / 32 - 1];
     const uint32_t thread_excl = (w ? s_warp[w - 1] : 0u) + x - sum;
-    if (t == 0) {
+    if (w == 0) {
         uint32_t excl = 0;
         if (tile == 0) {
-            __threadfence();
-            atomicExch(status, (2ull << 32) | block_total);
-        } else {
-            atomicExch(status + tile, (1ull << 32) | block_total);
-            uint32_t j = tile - 1, polls = 0;
-            for (;;) {
-                const unsigned long long v = *reinterpret_cast<volatile unsigned long long *>(status + j);
-                const uint32_t flag = (uint32_t)(v >> 32);
-                if (flag == 0u) {
-                    if (++polls > kLookbackPolls) {
-                        atomicExch(reinterpret_cast<unsigned int *>(S.part + 1), 1u);
-                        break;
-                    }
-                    continue;
-                }
-                excl += (uint32_t)v;
-                if (flag == 2u || j == 0) break;
-                --j;
+            if (lane == 0) {
+                __threadfence();
+                atomicExch(status, (2ull << 32) | block_total);
             }
-            __threadfence();
-            atomicExch(status + tile, (2ull << 32) | (excl + block_total));
+        } else {
+            if (lane == 0) atomicExch(status + tile, (1ull << 32) | block_total);
+            bool gave_up = false;
+            for (int j = (int)tile - 1; !gave_up;) {            // window: predecessors j, j - 1, ..., j - 31
+                const int idx = j - (int)lane;
+                unsigned long long v = 2ull << 32;              // before tile 0: an inclusive prefix of 0
+                if (idx >= 0) {
+                    uint32_t polls = 0;
+                    for (;;) {
+                        v = *reinterpret_cast<volatile unsigned long long *>(status + idx);
+                        if ((uint32_t)(v >> 32) != 0u) break;
+                        if (++polls > kLookbackPolls) { v = 2ull << 32; gave_up = true; break; }
+                    }
+                }
+                gave_up = __any_sync(kFull, gave_up);
+                const unsigned incl = __ballot_sync(kFull, (uint32_t)(v >> 32) == 2u);
+                const uint32_t last = incl ? (uint32_t)__ffs(incl) - 1u : 31u;   // nearest inclusive lane
+                excl += __reduce_add_sync(kFull, lane <= last ? (uint32_t)v : 0u);
+                if (incl) break;
+                j -= 32;
+            }
+            if (lane == 0) {
+                if (gave_up) atomicExch(reinterpret_cast<unsigned int *>(S.part + 1), 1u);
+                __threadfence();
+                atomicExch(status + tile, (2ull << 32) | (excl + block_total));
+            }
         }
-        s_excl = excl;
+        if (lane == 0) s_excl = excl;
     }
     __syncthreads();
     uint32_t run = s_excl + thread_excl;
