@@ -388,8 +388,25 @@ __global__ void k_final_order(const uint32_t *perm, const uint32_t *sorted_ids, 
     if (i < n) out[i] = sorted_ids[perm[i]];
 }
 
-__global__ void k_task_reset(BuildState S, uint32_t ntasks) {
+// The start of a level: the current level's small and tiny task counts (those
+// of the level before), the node count at its start, and fresh child-task
+// counters.  One thread.
+__device__ __forceinline__ void level_advance(BuildState &S, uint32_t level) {
+    S.counters[0] = 0;
+    S.counters[5] = S.counters[4];
+    S.counters[4] = 0;
+    S.counters[7] = S.counters[6];
+    S.counters[6] = 0;
+    S.level_end[level] = S.counters[1];
+}
+
+// The start of a level with large tasks, in one launch: level_advance, the
+// status words of the level's partition scan zeroed (n_part), and the large
+// tasks' centroid bounds and bins set to empty.
+__global__ void k_task_reset(BuildState S, uint32_t level, uint32_t ntasks, uint32_t n_part) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) level_advance(S, level);
+    if (i < n_part) S.part[i] = 0ull;
     if (i >= ntasks * (6 + kTaskBinWords)) return;
     uint32_t t = i / (6 + kTaskBinWords), k = i % (6 + kTaskBinWords);
     if (k < 6) {
@@ -1095,17 +1112,9 @@ __global__ void __launch_bounds__(kTinyThreads) k_tiny_level(BuildState S, int c
         for (uint32_t p = start + lcount; p < start + n; ++p) out1[p] = out0[p];
 }
 
-// Between small-task levels: the next level's task count, the node count of
-// the level just built, and a fresh child-task counter.
+// The start of a level without large tasks (level_advance alone).
 __global__ void k_level_advance(BuildState S, uint32_t level) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        S.counters[0] = 0;
-        S.counters[5] = S.counters[4];
-        S.counters[4] = 0;
-        S.counters[7] = S.counters[6];
-        S.counters[6] = 0;
-        S.level_end[level] = S.counters[1];
-    }
+    if (threadIdx.x == 0 && blockIdx.x == 0) level_advance(S, level);
 }
 
 // Partition flag of position i: 1 when its primitive goes to the left child of
@@ -1396,11 +1405,15 @@ static cudaError_t gpu_build(const mcrt_gpu_vertex *d_verts, const mcrt_gpu_tria
     uint32_t host_counters[8] = {};
     uint32_t scan_error = 0;
     const uint32_t n_flag_tiles = (nt + kFlagTile - 1) / kFlagTile;
-    auto advance = [&]() -> bool {
+    auto level_ok = [&]() -> bool {
         if (level + 1 >= kMaxLevels) {
             if (err) *err = "BVH build exceeded 4096 levels";
             return false;
         }
+        return true;
+    };
+    auto advance = [&]() -> bool {
+        if (!level_ok()) return false;
         k_level_advance<<<1, 1, 0, st>>>(S, level++); ::mcrt::note_launch();
         return true;
     };
@@ -1414,14 +1427,14 @@ static cudaError_t gpu_build(const mcrt_gpu_vertex *d_verts, const mcrt_gpu_tria
             ::mcrt::note_launch();
         }
     };
+    const uint32_t n_part = 2 + n_flag_tiles;
     while (n_large > 0) {
-        if (!advance()) return cudaErrorUnknown;
-        const uint32_t nw = n_large * (6 + kTaskBinWords);
-        k_task_reset<<<(nw + TB - 1) / TB, TB, 0, st>>>(S, n_large); ::mcrt::note_launch();
+        if (!level_ok()) return cudaErrorUnknown;
+        const uint32_t nw = std::max(n_large * (6 + kTaskBinWords), n_part);
+        k_task_reset<<<(nw + TB - 1) / TB, TB, 0, st>>>(S, level++, n_large, n_part); ::mcrt::note_launch();
         k_centroid_bounds<<<nbp, 256, 0, st>>>(S, cur); ::mcrt::note_launch();
         k_bins<<<nbp, 256, 0, st>>>(S, cur); ::mcrt::note_launch();
         k_split<<<(n_large + 127) / 128, 128, 0, st>>>(S, cur, n_large); ::mcrt::note_launch();
-        cudaMemsetAsync(S.part, 0, (2 + (size_t)n_flag_tiles) * 8, st);
         k_flag_scan<<<n_flag_tiles, kFlagThreads, 0, st>>>(S, cur); ::mcrt::note_launch();
         k_scatter<<<nb, TB, 0, st>>>(S, cur); ::mcrt::note_launch();
         small_round(n_small, n_tiny);
