@@ -1,13 +1,20 @@
 """GPU edge cases against the oracle, bit for bit: a scene with no geometry,
 ragged image sizes with sample counts that do not divide into their passes, a
-one-pixel image, single-bounce paths, an empty ray batch and a zero-area
+one-pixel image, single-bounce paths, an empty ray batch, a zero-area
 triangle (the reference's Moller-Trumbore test rejects it by its determinant,
-path_trace.wgsl:300-317)."""
+path_trace.wgsl:300-317), and rays that graze box planes far from the world
+origin (traced, and rendered by every closest-hit variant)."""
+import os
+import sys
+
 import numpy as np
 import pytest
 
 import mcrt_gb300 as M
 from mcrt_gb300 import scenes
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+import grazing_cases as G  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
@@ -63,34 +70,11 @@ def test_empty_ray_batch_and_zero_area_triangle(ctx, oracle):
     assert not np.any(got["prim"] == len(T) - 1)       # the zero-area triangle is never hit
 
 
-def _grazing_walls(k=4096, seed=9):
-    """k rays far from the origin in x (200..3000) with tiny direction x
-    components (2e-6..3e-5), each towards its own triangle in the plane a few
-    ulps of the origin away in x: a plane distance (plane - o) / d of the order
-    of the rounding of o / d itself.  Each triangle ends 0.05..3 past its hit in
-    z, so the box's exit there lies within that rounding of the entry."""
-    rng = np.random.default_rng(seed)
-    x = rng.uniform(200, 3000, k).astype(np.float32)
-    dx = (rng.uniform(2e-6, 3e-5, k) * rng.choice([-1, 1], k)).astype(np.float32)
-    xk = (x + np.sign(dx) * rng.integers(1, 40, k) * np.spacing(x)).astype(np.float32)
-    y = (2.0 * np.arange(k)).astype(np.float32)
-    th = (xk.astype(np.float64) - x) / dx
-    z0, z1 = th - rng.uniform(0.5, 5, k), th + rng.uniform(0.05, 3, k)
-    V = np.zeros(3 * k, M._native.VERTEX)
-    V["position"][0::3] = np.column_stack([xk, y - 0.5, z0, np.ones(k)])
-    V["position"][1::3] = np.column_stack([xk, y + 0.5, z0, np.ones(k)])
-    V["position"][2::3] = np.column_stack([xk, y, z1, np.ones(k)])
-    T = np.zeros(k, M._native.TRIANGLE)
-    T["v"] = np.arange(3 * k).reshape(k, 3)
-    rays = M.make_rays(np.column_stack([x, y, np.zeros(k)]), np.column_stack([dx, np.zeros(k), np.ones(k)]))
-    return V, T, rays
-
-
 def test_grazing_rays_far_from_the_origin_find_their_hits(ctx, oracle):
-    """The box test's plane distances carry the rounding of o / d, absolute
-    and up to tens of units here; the interval is widened by its bound, so
-    every ray still enters its triangle's box and returns the oracle's hit."""
-    V, T, rays = _grazing_walls()
+    """Rays that graze box planes far from the world origin (grazing_cases):
+    every ray still enters its triangle's box and returns the oracle's
+    brute-force hit, through both node layouts."""
+    V, T, rays = G.grazing_walls()
     md = M.materials([(0, (0.5, 0.5, 0.5), 0, 1)])
     ctx.upload_scene(vertices=V, triangles=T, materials=md)
     want = oracle.OracleScene(materials=md, vertices=V, triangles=T).trace(rays, brute_force=True)

@@ -4,11 +4,16 @@ Each test names the reference test it restates.  These pin the oracle's BVH
 builder, traversal and metrics before it is trusted as the checker.
 """
 import math
+import os
+import sys
 
 import numpy as np
 import pytest
 
 import pyoracle as O
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+import grazing_cases as G  # noqa: E402
 
 
 def sph(cx, cz, r, mat=0):
@@ -257,6 +262,19 @@ def test_random_rays_bvh_equals_brute_force():
 
 
 # ---------------------------------------------------------------- regression.rs metric KATs
+def test_grazing_rays_far_from_the_origin_bvh_equals_brute_force():
+    """The oracle's traversal (the reference's (plane - o) * inv box test with
+    the cull slack) on rays that graze box planes far from the world origin:
+    every ray finds its own triangle, as brute force does."""
+    V, T, rays = G.grazing_walls()
+    sc = O.OracleScene(materials=np.zeros(3088, np.uint8), vertices=V, triangles=T)
+    a = sc.trace(rays)
+    b = sc.trace(rays, brute_force=True)
+    assert np.array_equal(b["prim"], np.arange(len(T), dtype=np.uint32))
+    assert np.array_equal(a["prim"], b["prim"])
+    assert np.array_equal(a["t"].view(np.uint32), b["t"].view(np.uint32))
+
+
 def solid(w, h, r, g, b, a=255):
     x = np.zeros((h, w, 4), np.uint8)
     x[...] = (r, g, b, a)
