@@ -3,6 +3,7 @@ edge cases, a seeded generator of irregular files, decimals that sit on or near
 binary32 rounding boundaries, and an exact decimal -> binary32 rounding in
 rational arithmetic (the value str::parse::<f32> must return)."""
 from fractions import Fraction
+import random
 import re
 
 import numpy as np
@@ -167,6 +168,29 @@ def random_obj(seed, n_lines=400):
             out.append(ws + "f" + ws + " ".join(idx(nv) for _ in range(3)) + ws)
     eol = "\r\n" if rng.random() < 0.3 else "\n"
     return (eol.join(out) + (eol if rng.random() < 0.7 else "")).encode()
+
+
+def mutated_obj(seed):
+    """An edge-case or seeded random file with 1..6 byte-level edits drawn from
+    the characters OBJ text is made of (inserted, replaced, deleted, or a
+    run duplicated): near-valid text that exercises the loader's error paths
+    and its tokenising next to them."""
+    rng = random.Random(seed)
+    seeds = [EDGE_CASES[k] for k in sorted(EDGE_CASES)]
+    text = bytearray(rng.choice(seeds) if rng.random() < 0.5 else random_obj(rng.randrange(6)))
+    alphabet = b" /\n\r\t0123456789-+.eEfvtn#"
+    for _ in range(rng.randint(1, 6)):
+        op = rng.random()
+        if op < 0.25 and text:
+            text[rng.randrange(len(text))] = rng.choice(alphabet)
+        elif op < 0.45 and text:
+            del text[rng.randrange(len(text))]
+        elif op < 0.75:
+            text.insert(rng.randrange(len(text) + 1), rng.choice(alphabet))
+        elif text:
+            i = rng.randrange(len(text))
+            text[i:i] = text[i:min(len(text), i + rng.randint(1, 40))]
+    return bytes(text)
 
 
 def canon(v):

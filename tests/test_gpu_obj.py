@@ -61,6 +61,23 @@ def test_random_files_match_oracle(ctx, oracle, mcrt, seed):
     assert same(v_d, t_d, v_o, t_o)
 
 
+@pytest.mark.parametrize("chunk", range(4))
+def test_mutated_files_match_oracle(ctx, oracle, mcrt, chunk):
+    """Seeded near-valid files (obj_cases.mutated_obj, 50 per chunk): the
+    device parse gives the oracle's records, or fails with its message."""
+    for seed in range(50 * chunk, 50 * chunk + 50):
+        text = C.mutated_obj(seed)
+        try:
+            v_o, t_o = oracle.obj_load(text, 2)
+        except oracle.ObjError as e:
+            with pytest.raises(mcrt.MCRTError) as ed:
+                dev_load(ctx, text, 2)
+            assert str(ed.value).endswith(str(e)), seed
+            continue
+        v_d, t_d = dev_load(ctx, text, 2)
+        assert same(v_d, t_d, v_o, t_o), seed
+
+
 @pytest.mark.parametrize("case", C.ERROR_CASES, ids=[c[0] for c in C.ERROR_CASES])
 def test_errors_leave_the_mesh_unchanged(ctx, mcrt, case):
     name, text, msg = case

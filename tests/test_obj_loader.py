@@ -72,6 +72,24 @@ def test_host_loader_matches_oracle_random_files(oracle, tmp_path, seed):
     assert np.array_equal(t_h.view(np.uint32), t_o.view(np.uint32))
 
 
+@pytest.mark.parametrize("chunk", range(4))
+def test_host_loader_matches_oracle_mutated_files(oracle, tmp_path, chunk):
+    """Seeded near-valid files (obj_cases.mutated_obj, 50 per chunk): the
+    host loader gives the oracle's records, or fails with its message."""
+    for seed in range(50 * chunk, 50 * chunk + 50):
+        text = C.mutated_obj(seed)
+        try:
+            v_o, t_o = oracle.obj_load(text, 0)
+        except oracle.ObjError as e:
+            with pytest.raises(N.MCRTError) as eh:
+                host_load(tmp_path, text)
+            assert str(eh.value).endswith(str(e)), seed
+            continue
+        v_h, t_h = host_load(tmp_path, text)
+        assert np.array_equal(C.canon(v_h), C.canon(v_o)), seed
+        assert np.array_equal(t_h.view(np.uint32), t_o.view(np.uint32)), seed
+
+
 @pytest.mark.parametrize("case", C.ERROR_CASES, ids=[c[0] for c in C.ERROR_CASES])
 def test_host_loader_error_messages(oracle, tmp_path, case):
     name, text, msg = case
