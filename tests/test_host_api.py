@@ -1,6 +1,8 @@
-"""Host side of libmcrt_cuda.so (no GPU needed): exported symbols, the scene
-YAML API against the reference's scene/camera/texture unit-test known answers,
-tone mapping and the PNG writer."""
+"""Host side of libmcrt_cuda.so (no GPU needed): exported symbols, every
+entry point's refusal of NULL arguments, the scene YAML API against the
+reference's scene/camera/texture unit-test known answers, tone mapping and the
+PNG writer."""
+import ctypes
 import math
 import os
 import re
@@ -25,6 +27,42 @@ def test_library_exports_every_declared_symbol():
     assert not missing, missing
     assert {n for n, _, _ in N.SIGNATURES} == names
     assert b"sm_103a" in L.mcrt_version()
+
+
+_NULL_CALLS = r"""
+import ctypes, sys
+sys.path.insert(0, sys.argv[1])
+from mcrt_gb300 import _native as N
+L = N.lib()
+for name, res, args in N.SIGNATURES:
+    vals = []
+    for t in args:
+        if t in (ctypes.c_float, ctypes.c_double):
+            vals.append(0.0)
+        elif t in (ctypes.c_int, ctypes.c_uint32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_size_t, ctypes.c_uint8):
+            vals.append(0)
+        else:
+            vals.append(None)
+    r = getattr(L, name)(*vals)
+    print(name, r, flush=True)
+"""
+
+
+def test_every_entry_point_returns_a_status_on_null_arguments():
+    """Every declared function called with NULL for each pointer (the context
+    included) and 0 for each number, in one child process: each returns (a
+    status, or nothing for the void ones) and none crashes.  Every status
+    function refuses the call, except the tone maps of zero pixels."""
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, "-c", _NULL_CALLS, ROOT], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got = dict(line.split(" ", 1) for line in r.stdout.strip().splitlines())
+    assert set(got) == {n for n, _, _ in N.SIGNATURES}
+    ok_with_nothing = {"mcrt_tonemap_rgba8", "mcrt_tonemap_aces_rgba8"}
+    for name, res, _ in N.SIGNATURES:
+        if res is ctypes.c_int and name not in ok_with_nothing:
+            assert int(got[name]) < 0, (name, got[name])
 
 
 def test_record_sizes_match_reference_layouts():                    # bvh.rs:649, mesh.rs:683-690, scene.rs:1194
