@@ -48,7 +48,7 @@ __device__ __forceinline__ RayInv make_ray(f3 o, f3 d) {
 // reaches the closest hit, and the hit found is the same (the box test only
 // decides which boxes are visited).  The fused form fma(plane, inv, -o * inv)
 // is not used: rounding o * inv adds an ABSOLUTE error of up to |o * inv|
-// 2^-25, beyond any relative slack for a ray that barely moves along an axis
+// 2^-24, beyond any relative slack for a ray that barely moves along an axis
 // and starts near a box plane of that axis far from the world origin.
 __device__ __forceinline__ bool slab(const RayInv &r, float lx, float ly, float lz, float hx, float hy, float hz,
                                      float tmin, float tmax, float *tenter_out) {
